@@ -1,0 +1,175 @@
+"""Python host mirror of the renderer boundary, over the C ABI (include/agb.h).
+
+`Renderer` uploads a SceneDesc (aurora_gb300.scenes) through the same calls Aurora's C++ backend
+classes make -- geometry, images, materials, instances, environment, frame data -- then renders and
+reads back, mirroring IRenderer::render(sampleStart, sampleCount) and IRenderBuffer::data()
+(Aurora.h:714-751, 1196).  Errors from the library raise AgbError; there is no CPU path.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _abi
+from ._abi import check, library, ptr
+
+
+class Renderer:
+    def __init__(self, device=0, stream=None):
+        self._lib = library()
+        h = ctypes.c_void_p()
+        check(self._lib.agb_context_create(device, stream, ctypes.byref(h)))
+        self.ctx = h
+        self.scene = None
+        self._keep = []
+
+    def close(self):
+        if self.ctx:
+            self._lib.agb_context_destroy(self.ctx)
+            self.ctx = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------------------- scene upload
+    def upload(self, s):
+        """Uploads a scenes.SceneDesc: the equivalent of IScene construction + the first update."""
+        lib = self._lib
+        geo = []
+        for m in s.meshes:
+            g = ctypes.c_int32()
+            check(lib.agb_geometry_create(self.ctx, ptr(m["positions"]), ptr(m["normals"]),
+                                          ptr(m["texcoords"]), ptr(m["indices"]),
+                                          len(m["positions"]), len(m["indices"]), ctypes.byref(g)))
+            geo.append(g.value)
+        imgs = []
+        for im in s.images:
+            g = ctypes.c_int32()
+            check(lib.agb_image_create(self.ctx, ptr(im["pixels"]), im["width"], im["height"],
+                                       im["format"], im["linear"], ctypes.byref(g)))
+            imgs.append(g.value)
+        mats = np.ascontiguousarray(s.materials)
+        tex = None if s.textures is None else np.ascontiguousarray(s.textures)
+        check(lib.agb_materials_set(self.ctx, ptr(mats), ptr(tex), len(mats)))
+        insts = (_abi.Instance * len(s.instances))()
+        layer_arrays = []
+        for k, inst in enumerate(s.instances):
+            insts[k].geometry = geo[inst["mesh"]]
+            insts[k].material = inst["material"]
+            insts[k].object_to_world[:] = [float(x) for x in inst["xform"]]
+            layers = inst.get("layers") or []
+            insts[k].layer_count = len(layers)
+            if layers:
+                arr = (_abi.Layer * len(layers))()
+                for j, (mat, uv) in enumerate(layers):
+                    arr[j].material = mat
+                    arr[j].texcoords = uv.ctypes.data
+                layer_arrays.append(arr)
+                insts[k].layers = ctypes.cast(arr, ctypes.c_void_p)
+        check(lib.agb_instances_set(self.ctx, insts, len(s.instances)))
+        env = np.ascontiguousarray(s.env).copy()
+        check(lib.agb_environment_set(self.ctx, ptr(env.reshape(1)),
+                                      imgs[s.env_light] if s.env_light >= 0 else -1,
+                                      imgs[s.env_background] if s.env_background >= 0 else -1))
+        self.set_frame(s.frame)
+        self.scene = s
+
+    def set_frame(self, frame):
+        f = np.ascontiguousarray(np.asarray(frame, dtype=_abi.FRAME_DTYPE).reshape(1))
+        check(self._lib.agb_frame_set(self.ctx, ptr(f)))
+
+    # --------------------------------------------------------------------------- rendering
+    def render(self, sample_start, sample_count, width=None, height=None,
+               accumulation=_abi.ACCUM_RUNNING_MEAN | _abi.ACCUM_KAHAN, max_paths=0, stats=False):
+        opt = _abi.RenderOptions()
+        opt.width = width or self.scene.width
+        opt.height = height or self.scene.height
+        opt.accumulation = accumulation
+        opt.max_paths_in_flight = max_paths
+        st = _abi.RenderStats() if stats else None
+        check(self._lib.agb_render(self.ctx, ctypes.byref(opt), sample_start, sample_count,
+                                   ctypes.byref(st) if st is not None else None))
+        if stats:
+            out = {f: getattr(st, f) for f, _ in _abi.RenderStats._fields_}
+            out["kernel_ms"] = dict(zip(_abi.KERNEL_FAMILIES, list(st.kernel_ms)))
+            out["kernel_count"] = dict(zip(_abi.KERNEL_FAMILIES, list(st.kernel_count)))
+            return out
+        return None
+
+    def wait(self):
+        check(self._lib.agb_wait(self.ctx))
+
+    def set_counting(self, enabled):
+        check(self._lib.agb_set_counting(self.ctx, 1 if enabled else 0))
+
+    def set_profiling(self, enabled):
+        check(self._lib.agb_set_profiling(self.ctx, 1 if enabled else 0))
+
+    def read(self, mode=_abi.ACCUM_RUNNING_MEAN, width=None, height=None, out=None):
+        w = width or self.scene.width
+        h = height or self.scene.height
+        if out is None:
+            out = np.empty((h, w, 4), np.float32)
+        check(self._lib.agb_accum_read(self.ctx, mode, ptr(out), out.size))
+        return out
+
+    def accum_device_ptr(self, mode=_abi.ACCUM_RUNNING_MEAN):
+        p = ctypes.c_void_p()
+        check(self._lib.agb_accum_device(self.ctx, mode, ctypes.byref(p)))
+        return p.value
+
+    def post_process(self, mode=_abi.ACCUM_RUNNING_MEAN, brightness=(1.0, 1.0, 1.0),
+                     tone_map=False, gamma=True):
+        w, h = self.scene.width, self.scene.height
+        o32 = np.empty((h, w, 4), np.float32)
+        o8 = np.empty((h, w, 4), np.uint8)
+        b = np.asarray(brightness, np.float32)
+        check(self._lib.agb_post_process(self.ctx, mode, ptr(b), 1 if tone_map else 0,
+                                         1 if gamma else 0, ptr(o32), ptr(o8)))
+        return o32, o8
+
+    def memory_bytes(self):
+        b = ctypes.c_uint64()
+        check(self._lib.agb_context_memory(self.ctx, ctypes.byref(b)))
+        return b.value
+
+    def environment_alias(self):
+        s = self.scene
+        im = s.images[s.env_light]
+        n = im["width"] * im["height"]
+        out = np.zeros(n, dtype=_abi.ALIAS_DTYPE)
+        integral = ctypes.c_double()
+        check(self._lib.agb_environment_alias(self.ctx, ptr(out), n, ctypes.byref(integral)))
+        return out, integral.value
+
+    # ------------------------------------------------------------- unit entry points (device)
+    def intersect(self, rays_dev_ptr, n, any_hit, out_tuv_ptr, out_ip_ptr):
+        check(self._lib.agb_intersect_batch(self.ctx, ctypes.c_void_p(rays_dev_ptr), n,
+                                            1 if any_hit else 0, ctypes.c_void_p(out_tuv_ptr),
+                                            ctypes.c_void_p(out_ip_ptr)))
+
+    def env_sample(self, rnd_ptr, n, out_r, out_d, out_pdf):
+        check(self._lib.agb_env_sample_batch(self.ctx, ctypes.c_void_p(rnd_ptr), n,
+                                             ctypes.c_void_p(out_r), ctypes.c_void_p(out_d),
+                                             ctypes.c_void_p(out_pdf)))
+
+
+def bsdf_batch(op, mats_ptr, idx_ptr, frames_ptr, v_ptr, l_ptr, rnd_ptr, n, out_value, out_dir,
+               out_pdf, out_lobe, stream=None):
+    """Device-array BSDF batch (agb_bsdf_batch); all arguments are device pointers (ints)."""
+    vp = lambda x: None if x is None else ctypes.c_void_p(x)  # noqa: E731
+    check(library().agb_bsdf_batch(op, vp(mats_ptr), vp(idx_ptr), vp(frames_ptr), vp(v_ptr),
+                                   vp(l_ptr), vp(rnd_ptr), n, vp(out_value), vp(out_dir),
+                                   vp(out_pdf), vp(out_lobe), stream))
+
+
+def random_stream(sample_index, width, px, py, n, out_ptr):
+    check(library().agb_random_stream(sample_index, width, px, py, n, ctypes.c_void_p(out_ptr), None))

@@ -1,0 +1,987 @@
+// C ABI of the GB300 path-tracing backend (include/agb.h): context, scene upload, environment,
+// rendering, readback.  All inputs are validated on the host before any kernel sees them, so no
+// kernel indexes memory with an unchecked value.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "agb_kernels.h"
+
+using namespace agb;
+
+namespace
+{
+
+thread_local std::string g_lastError;
+
+float bitsToFloat(int32_t v)
+{
+    float f;
+    memcpy(&f, &v, sizeof f);
+    return f;
+}
+
+agb_status fail(agb_status code, const std::string& msg)
+{
+    g_lastError = msg;
+    return code;
+}
+
+agb_status cudaFail(cudaError_t e, const char* what)
+{
+    agb_status code = (e == cudaErrorMemoryAllocation) ? AGB_ERR_OOM : AGB_ERR_CUDA;
+    return fail(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define AGB_CUDA(call, what)                                                                       \
+    do                                                                                             \
+    {                                                                                              \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return cudaFail(e_, what);                                                             \
+    } while (0)
+
+// A device allocation owned by the context.
+struct DevBuf
+{
+    void* ptr    = nullptr;
+    size_t bytes = 0;
+    DevBuf()     = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (ptr)
+            cudaFree(ptr);
+        ptr   = nullptr;
+        bytes = 0;
+    }
+    cudaError_t ensure(size_t n)
+    {
+        if (bytes >= n && ptr)
+            return cudaSuccess;
+        release();
+        if (n == 0)
+            return cudaSuccess;
+        cudaError_t e = cudaMalloc(&ptr, n);
+        if (e == cudaSuccess)
+            bytes = n;
+        else
+            ptr = nullptr;
+        return e;
+    }
+    template <class T>
+    T* as() const
+    {
+        return static_cast<T*>(ptr);
+    }
+};
+
+struct Geometry
+{
+    DevBuf positions, normals, texcoords, indices, tris, nodes;
+    DevMesh mesh{};
+    float bounds[6]; // lo, hi in object space
+};
+
+struct Image
+{
+    DevBuf data;
+    DevImage view{};
+};
+
+} // namespace
+
+struct agb_context
+{
+    int device          = 0;
+    cudaStream_t stream = nullptr;
+    bool ownsStream     = false;
+    int smCount         = 0;
+    bool counting       = false;
+    bool profiling      = false;
+    KernelMarks marks;
+
+    std::vector<std::unique_ptr<Geometry>> geometries;
+    DevBuf meshTable;
+    std::vector<std::unique_ptr<Image>> images;
+    DevBuf imageTable;
+
+    DevBuf materials, matTex;
+    uint32_t materialCount = 0;
+    bool hasMatTex         = false;
+
+    DevBuf instances, tlasNodes, tlasOrder, layers;
+    std::vector<std::unique_ptr<DevBuf>> layerUVs;
+    uint32_t instanceCount = 0;
+    int32_t tlasRoot       = 0;
+    int32_t tlasDepth      = 0;
+
+    agb_environment_data env{};
+    int32_t envLight = -1, envBackground = -1;
+    DevBuf alias;
+    EnvBuildScratch envScratch;
+    double envIntegral = 0.0;
+
+    agb_frame_data frame{};
+    bool frameSet = false;
+
+    // Wave buffers.
+    size_t pathCapacity = 0;
+    DevBuf pathState, queues, counters, stats;
+    WaveBuffers wb{};
+    // Accumulation.
+    uint32_t accW = 0, accH = 0;
+    DevBuf accMean, accSum, accComp, lastSample;
+    uint32_t accumulatedSamples = 0;
+    uint32_t lastAccumMode      = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    ~agb_context()
+    {
+        freeEnvScratch(envScratch);
+        if (ev0)
+            cudaEventDestroy(ev0);
+        if (ev1)
+            cudaEventDestroy(ev1);
+        if (ownsStream && stream)
+            cudaStreamDestroy(stream);
+    }
+
+    DevScene scene() const
+    {
+        DevScene s{};
+        s.meshes        = meshTable.as<DevMesh>();
+        s.instances     = instances.as<DevInstance>();
+        s.tlas          = tlasNodes.as<BNode>();
+        s.tlasRoot      = tlasRoot;
+        s.instanceCount = int32_t(instanceCount);
+        s.tlasOrder     = tlasOrder.as<int32_t>();
+        s.materials     = materials.as<agb_material>();
+        s.matTex        = hasMatTex ? matTex.as<agb_material_textures>() : nullptr;
+        s.materialCount = int32_t(materialCount);
+        s.imageCount    = int32_t(images.size());
+        s.images        = imageTable.as<DevImage>();
+        s.layers        = layers.as<DevLayer>();
+        s.env           = env;
+        s.envLight      = DevImage{};
+        s.envBackground = DevImage{};
+        if (envLight >= 0 && size_t(envLight) < images.size())
+            s.envLight = images[envLight]->view;
+        if (envBackground >= 0 && size_t(envBackground) < images.size())
+            s.envBackground = images[envBackground]->view;
+        s.alias = alias.as<agb_alias_entry>();
+        return s;
+    }
+};
+
+namespace
+{
+
+agb_status setDevice(agb_context* ctx)
+{
+    AGB_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    return AGB_OK;
+}
+
+// Carves the wave buffers for `paths` paths and `depth` bounces out of a few allocations.
+agb_status ensureWave(agb_context* ctx, size_t paths, int depth, size_t waves)
+{
+    if (paths > ctx->pathCapacity)
+    {
+        size_t P = paths;
+        size_t stateBytes = P * (sizeof(uint2) + sizeof(float4) * 7 + sizeof(uint32_t) * 3 +
+                                    sizeof(float4) * kMaxShadowSlots * 2 + sizeof(float4));
+        size_t queueBytes = P * (2 * (2 * sizeof(float4) + sizeof(uint32_t)) + sizeof(float4) +
+                                    sizeof(int32_t) + sizeof(uint32_t) * kMaxShadowSlots +
+                                    sizeof(uint32_t)) + 1024;
+        AGB_CUDA(ctx->pathState.ensure(stateBytes + 4096), "allocate path state");
+        AGB_CUDA(ctx->queues.ensure(queueBytes + 4096), "allocate ray queues");
+        char* s = ctx->pathState.as<char>();
+        auto take = [&](size_t bytes) {
+            char* r = s;
+            s += (bytes + 255) & ~size_t(255);
+            return r;
+        };
+        WaveBuffers& w   = ctx->wb;
+        w.rng            = reinterpret_cast<uint2*>(take(P * sizeof(uint2)));
+        w.contrib        = reinterpret_cast<float4*>(take(P * sizeof(float4)));
+        w.flags          = reinterpret_cast<uint32_t*>(take(P * sizeof(uint32_t)));
+        w.outDirect      = reinterpret_cast<float4*>(take(P * sizeof(float4)));
+        w.outDiffuse     = reinterpret_cast<float4*>(take(P * sizeof(float4)));
+        w.outGlossy      = reinterpret_cast<float4*>(take(P * sizeof(float4)));
+        w.lastIndirect   = reinterpret_cast<float4*>(take(P * sizeof(float4)));
+        w.pendEmission   = reinterpret_cast<float4*>(take(P * sizeof(float4)));
+        w.pendSegContrib = reinterpret_cast<float4*>(take(P * sizeof(float4)));
+        w.pendSlot       = reinterpret_cast<float4*>(take(P * kMaxShadowSlots * sizeof(float4)));
+        w.pendBits       = reinterpret_cast<uint32_t*>(take(P * sizeof(uint32_t)));
+        w.occluded       = reinterpret_cast<uint32_t*>(take(P * sizeof(uint32_t)));
+        w.shOrg          = reinterpret_cast<float4*>(take(P * sizeof(float4)));
+        w.shDir          = reinterpret_cast<float4*>(take(P * kMaxShadowSlots * sizeof(float4)));
+        if (size_t(s - ctx->pathState.as<char>()) > ctx->pathState.bytes)
+            return fail(AGB_ERR_LIMIT, "internal: path state carve overflow");
+        s = ctx->queues.as<char>();
+        for (int b = 0; b < 2; b++)
+        {
+            w.rayOrg[b]  = reinterpret_cast<float4*>(take(P * sizeof(float4)));
+            w.rayDir[b]  = reinterpret_cast<float4*>(take(P * sizeof(float4)));
+            w.rayPath[b] = reinterpret_cast<uint32_t*>(take(P * sizeof(uint32_t)));
+        }
+        w.hitTUV      = reinterpret_cast<float4*>(take(P * sizeof(float4)));
+        w.hitInst     = reinterpret_cast<int32_t*>(take(P * sizeof(int32_t)));
+        w.shTag       = reinterpret_cast<uint32_t*>(take(P * kMaxShadowSlots * sizeof(uint32_t)));
+        w.resolveList = reinterpret_cast<uint32_t*>(take(P * sizeof(uint32_t)));
+        if (size_t(s - ctx->queues.as<char>()) > ctx->queues.bytes)
+            return fail(AGB_ERR_LIMIT, "internal: queue carve overflow");
+        ctx->pathCapacity = P;
+    }
+    size_t counterWords = size_t(depth + 2) * 4 * waves;
+    AGB_CUDA(ctx->counters.ensure(counterWords * sizeof(uint32_t)), "allocate counters");
+    AGB_CUDA(ctx->stats.ensure(8 * sizeof(unsigned long long)), "allocate stats");
+    ctx->wb.stats = ctx->stats.as<unsigned long long>();
+    return AGB_OK;
+}
+
+agb_status ensureAccum(agb_context* ctx, uint32_t W, uint32_t H)
+{
+    if (ctx->accW == W && ctx->accH == H && ctx->accMean.ptr)
+        return AGB_OK;
+    size_t n = size_t(W) * H;
+    AGB_CUDA(ctx->accMean.ensure(n * sizeof(float4)), "allocate accumulation");
+    AGB_CUDA(ctx->accSum.ensure(n * sizeof(float4)), "allocate accumulation");
+    AGB_CUDA(ctx->accComp.ensure(n * sizeof(float4)), "allocate accumulation");
+    AGB_CUDA(ctx->lastSample.ensure(n * sizeof(float4)), "allocate accumulation");
+    AGB_CUDA(cudaMemsetAsync(ctx->accMean.ptr, 0, n * sizeof(float4), ctx->stream), "clear");
+    AGB_CUDA(cudaMemsetAsync(ctx->accSum.ptr, 0, n * sizeof(float4), ctx->stream), "clear");
+    AGB_CUDA(cudaMemsetAsync(ctx->accComp.ptr, 0, n * sizeof(float4), ctx->stream), "clear");
+    ctx->accW = W;
+    ctx->accH = H;
+    ctx->accumulatedSamples = 0;
+    return AGB_OK;
+}
+
+agb_status rebuildMeshTable(agb_context* ctx)
+{
+    std::vector<DevMesh> t(ctx->geometries.size());
+    for (size_t i = 0; i < t.size(); i++)
+        t[i] = ctx->geometries[i]->mesh;
+    if (t.empty())
+        return AGB_OK;
+    AGB_CUDA(ctx->meshTable.ensure(t.size() * sizeof(DevMesh)), "allocate mesh table");
+    AGB_CUDA(cudaMemcpyAsync(ctx->meshTable.ptr, t.data(), t.size() * sizeof(DevMesh),
+                 cudaMemcpyHostToDevice, ctx->stream),
+        "upload mesh table");
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "upload mesh table");
+    return AGB_OK;
+}
+
+agb_status upload(agb_context* ctx, DevBuf& dst, const void* src, size_t bytes, const char* what)
+{
+    AGB_CUDA(dst.ensure(bytes), what);
+    if (bytes)
+        AGB_CUDA(cudaMemcpyAsync(dst.ptr, src, bytes, cudaMemcpyHostToDevice, ctx->stream), what);
+    return AGB_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+AGB_API const char* agb_version(void) { return "aurora-gb300 0.1 (sm_103a)"; }
+
+AGB_API const char* agb_last_error(void) { return g_lastError.c_str(); }
+
+AGB_API agb_status agb_context_create(int32_t device, void* cuda_stream, agb_context** out)
+{
+    if (!out)
+        return fail(AGB_ERR_INVALID_ARG, "agb_context_create: out is null");
+    *out = nullptr;
+    int count = 0;
+    AGB_CUDA(cudaGetDeviceCount(&count), "cudaGetDeviceCount");
+    if (device < 0 || device >= count)
+        return fail(AGB_ERR_INVALID_ARG, "agb_context_create: no CUDA device " + std::to_string(device));
+    std::unique_ptr<agb_context> ctx(new agb_context());
+    ctx->device = device;
+    AGB_CUDA(cudaSetDevice(device), "cudaSetDevice");
+    AGB_CUDA(cudaDeviceGetAttribute(&ctx->smCount, cudaDevAttrMultiProcessorCount, device),
+        "query SM count");
+    if (cuda_stream)
+        ctx->stream = static_cast<cudaStream_t>(cuda_stream);
+    else
+    {
+        AGB_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "create stream");
+        ctx->ownsStream = true;
+    }
+    AGB_CUDA(cudaEventCreate(&ctx->ev0), "create event");
+    AGB_CUDA(cudaEventCreate(&ctx->ev1), "create event");
+    setTraceAttributes();
+    // Default environment: the reference's gradient defaults (EnvironmentBase.cpp:33-45),
+    // identity transforms.
+    agb_environment_data& e = ctx->env;
+    const float lt[3] = { 1.f, 1.f, 1.f }, lb[3] = { 0.f, 0.f, 0.f };
+    const float bt[3] = { 0.02f, 0.25f, 0.60f }, bb[3] = { 0.32f, 0.79f, 1.0f };
+    memcpy(e.light_top, lt, sizeof lt);
+    memcpy(e.light_bottom, lb, sizeof lb);
+    memcpy(e.background_top, bt, sizeof bt);
+    memcpy(e.background_bottom, bb, sizeof bb);
+    for (int k = 0; k < 4; k++)
+    {
+        e.light_transform[5 * k] = e.light_transform_inv[5 * k] = e.background_transform[5 * k] = 1.f;
+    }
+    *out = ctx.release();
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_context_destroy(agb_context* ctx)
+{
+    if (!ctx)
+        return AGB_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    delete ctx;
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_context_memory(agb_context* ctx, uint64_t* bytes)
+{
+    if (!ctx || !bytes)
+        return fail(AGB_ERR_INVALID_ARG, "agb_context_memory: null argument");
+    uint64_t b = ctx->meshTable.bytes + ctx->imageTable.bytes + ctx->materials.bytes +
+        ctx->matTex.bytes + ctx->instances.bytes + ctx->tlasNodes.bytes + ctx->tlasOrder.bytes +
+        ctx->layers.bytes + ctx->alias.bytes + ctx->pathState.bytes + ctx->queues.bytes +
+        ctx->counters.bytes + ctx->accMean.bytes + ctx->accSum.bytes + ctx->accComp.bytes +
+        ctx->lastSample.bytes;
+    for (auto& g : ctx->geometries)
+        b += g->positions.bytes + g->normals.bytes + g->texcoords.bytes + g->indices.bytes +
+            g->tris.bytes + g->nodes.bytes;
+    for (auto& i : ctx->images)
+        b += i->data.bytes;
+    for (auto& l : ctx->layerUVs)
+        b += l->bytes;
+    *bytes = b;
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_set_counting(agb_context* ctx, int32_t enabled)
+{
+    if (!ctx)
+        return fail(AGB_ERR_INVALID_ARG, "agb_set_counting: null context");
+    ctx->counting = enabled != 0;
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_set_profiling(agb_context* ctx, int32_t enabled)
+{
+    if (!ctx)
+        return fail(AGB_ERR_INVALID_ARG, "agb_set_profiling: null context");
+    ctx->profiling = enabled != 0;
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_geometry_create(agb_context* ctx, const float* positions,
+    const float* normals, const float* texcoords, const uint32_t* indices, uint32_t vertex_count,
+    uint32_t index_count, int32_t* out_geometry)
+{
+    if (!ctx || !positions || !out_geometry)
+        return fail(AGB_ERR_INVALID_ARG, "agb_geometry_create: null argument");
+    if (vertex_count == 0 || index_count == 0 || index_count % 3 != 0)
+        return fail(AGB_ERR_INVALID_ARG, "agb_geometry_create: index count must be a positive multiple of 3");
+    if (!indices && index_count != vertex_count)
+        return fail(AGB_ERR_INVALID_ARG, "agb_geometry_create: non-indexed geometry needs index_count == vertex_count");
+    if (uint64_t(index_count / 3) >= (1ull << 28))
+        return fail(AGB_ERR_LIMIT, "agb_geometry_create: more than 2^28 triangles");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    std::vector<uint32_t> idx;
+    if (indices)
+    {
+        idx.assign(indices, indices + index_count);
+        for (uint32_t i = 0; i < index_count; i++)
+            if (idx[i] >= vertex_count)
+                return fail(AGB_ERR_INVALID_ARG, "agb_geometry_create: index " + std::to_string(i) +
+                        " = " + std::to_string(idx[i]) + " out of range");
+    }
+    else
+    {
+        // Sequential indices for non-indexed geometry (HGIGeometry.cpp:37-47).
+        idx.resize(index_count);
+        for (uint32_t i = 0; i < index_count; i++)
+            idx[i] = i;
+    }
+    uint32_t ntri = index_count / 3;
+    std::unique_ptr<Geometry> g(new Geometry());
+    for (int k = 0; k < 3; k++)
+    {
+        g->bounds[k]     = INFINITY;
+        g->bounds[3 + k] = -INFINITY;
+    }
+    std::vector<float> boxes(size_t(ntri) * 6);
+    for (uint32_t t = 0; t < ntri; t++)
+    {
+        float* b = &boxes[6 * size_t(t)];
+        for (int k = 0; k < 3; k++)
+        {
+            b[k]     = INFINITY;
+            b[3 + k] = -INFINITY;
+        }
+        for (int v = 0; v < 3; v++)
+        {
+            const float* p = positions + 3 * size_t(idx[3 * size_t(t) + v]);
+            for (int k = 0; k < 3; k++)
+            {
+                if (!std::isfinite(p[k]))
+                    return fail(AGB_ERR_INVALID_ARG, "agb_geometry_create: non-finite position");
+                b[k]     = std::min(b[k], p[k]);
+                b[3 + k] = std::max(b[3 + k], p[k]);
+            }
+        }
+        for (int k = 0; k < 3; k++)
+        {
+            g->bounds[k]     = std::min(g->bounds[k], b[k]);
+            g->bounds[3 + k] = std::max(g->bounds[3 + k], b[3 + k]);
+        }
+    }
+    BuiltBVH bvh;
+    buildBVH2(boxes.data(), ntri, 4, 34, bvh);
+    if (bvh.depth > 34)
+        return fail(AGB_ERR_LIMIT, "agb_geometry_create: BLAS deeper than the traversal stack allows");
+    std::vector<float4> tris(size_t(ntri) * 3);
+    for (uint32_t s = 0; s < ntri; s++)
+    {
+        uint32_t t = bvh.order[s];
+        for (int v = 0; v < 3; v++)
+        {
+            const float* p = positions + 3 * size_t(idx[3 * size_t(t) + v]);
+            tris[3 * size_t(s) + v] =
+                make_float4(p[0], p[1], p[2], v == 0 ? bitsToFloat(int32_t(t)) : 0.f);
+        }
+    }
+    st = upload(ctx, g->positions, positions, size_t(vertex_count) * 3 * sizeof(float), "upload positions");
+    if (!st && normals)
+        st = upload(ctx, g->normals, normals, size_t(vertex_count) * 3 * sizeof(float), "upload normals");
+    if (!st && texcoords)
+        st = upload(ctx, g->texcoords, texcoords, size_t(vertex_count) * 2 * sizeof(float), "upload texcoords");
+    if (!st)
+        st = upload(ctx, g->indices, idx.data(), idx.size() * sizeof(uint32_t), "upload indices");
+    if (!st)
+        st = upload(ctx, g->tris, tris.data(), tris.size() * sizeof(float4), "upload triangles");
+    if (!st && !bvh.nodes.empty())
+        st = upload(ctx, g->nodes, bvh.nodes.data(), bvh.nodes.size() * sizeof(BNode), "upload BVH");
+    if (st)
+        return st;
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "upload geometry");
+    DevMesh& m      = g->mesh;
+    m.positions     = g->positions.as<float>();
+    m.normals       = normals ? g->normals.as<float>() : nullptr;
+    m.texcoords     = texcoords ? g->texcoords.as<float>() : nullptr;
+    m.indices       = g->indices.as<uint32_t>();
+    m.tris          = g->tris.as<float4>();
+    m.nodes         = g->nodes.as<BNode>();
+    m.vertexCount   = vertex_count;
+    m.triangleCount = ntri;
+    m.root          = bvh.root;
+    m.depth         = bvh.depth;
+    ctx->geometries.push_back(std::move(g));
+    *out_geometry = int32_t(ctx->geometries.size() - 1);
+    return rebuildMeshTable(ctx);
+}
+
+AGB_API agb_status agb_image_create(agb_context* ctx, const void* pixels, uint32_t width,
+    uint32_t height, int32_t format, int32_t linear, int32_t* out_image)
+{
+    if (!ctx || !pixels || !out_image || width == 0 || height == 0)
+        return fail(AGB_ERR_INVALID_ARG, "agb_image_create: invalid argument");
+    if (format != AGB_FORMAT_RGBA8_UNORM && format != AGB_FORMAT_RGBA32F && format != AGB_FORMAT_RGB32F)
+        return fail(AGB_ERR_INVALID_ARG, "agb_image_create: unsupported format");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    std::unique_ptr<Image> im(new Image());
+    size_t n = size_t(width) * height;
+    if (format == AGB_FORMAT_RGB32F)
+    {
+        std::vector<float4> rgba(n);
+        const float* p = static_cast<const float*>(pixels);
+        for (size_t i = 0; i < n; i++)
+            rgba[i] = make_float4(p[3 * i], p[3 * i + 1], p[3 * i + 2], 1.f);
+        st = upload(ctx, im->data, rgba.data(), n * sizeof(float4), "upload image");
+        format = AGB_FORMAT_RGBA32F;
+        if (!st)
+            AGB_CUDA(cudaStreamSynchronize(ctx->stream), "upload image");
+    }
+    else
+    {
+        size_t texel = format == AGB_FORMAT_RGBA8_UNORM ? 4 : 16;
+        st = upload(ctx, im->data, pixels, n * texel, "upload image");
+        if (!st)
+            AGB_CUDA(cudaStreamSynchronize(ctx->stream), "upload image");
+    }
+    if (st)
+        return st;
+    im->view = DevImage{ im->data.ptr, width, height, format, linear ? 1 : 0 };
+    ctx->images.push_back(std::move(im));
+    std::vector<DevImage> table(ctx->images.size());
+    for (size_t i = 0; i < table.size(); i++)
+        table[i] = ctx->images[i]->view;
+    st = upload(ctx, ctx->imageTable, table.data(), table.size() * sizeof(DevImage), "upload image table");
+    if (st)
+        return st;
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "upload image table");
+    *out_image = int32_t(ctx->images.size() - 1);
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_materials_set(agb_context* ctx, const agb_material* materials,
+    const agb_material_textures* textures, uint32_t count)
+{
+    if (!ctx || (!materials && count))
+        return fail(AGB_ERR_INVALID_ARG, "agb_materials_set: null argument");
+    if (textures)
+        for (uint32_t i = 0; i < count; i++)
+            for (int k = 0; k < AGB_TEX_SLOTS; k++)
+                if (textures[i].image[k] >= int32_t(ctx->images.size()))
+                    return fail(AGB_ERR_INVALID_ARG, "agb_materials_set: texture image index out of range");
+    agb_status st = setDevice(ctx);
+    if (!st)
+        st = upload(ctx, ctx->materials, materials, size_t(count) * sizeof(agb_material), "upload materials");
+    if (!st && textures)
+        st = upload(ctx, ctx->matTex, textures, size_t(count) * sizeof(agb_material_textures), "upload material textures");
+    if (st)
+        return st;
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "upload materials");
+    ctx->materialCount = count;
+    ctx->hasMatTex     = textures != nullptr;
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_instances_set(agb_context* ctx, const agb_instance* inst, uint32_t count)
+{
+    if (!ctx || (!inst && count))
+        return fail(AGB_ERR_INVALID_ARG, "agb_instances_set: null argument");
+    if (count >= (1u << 27))
+        return fail(AGB_ERR_LIMIT, "agb_instances_set: too many instances");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    std::vector<DevInstance> di(count);
+    std::vector<DevLayer> dl;
+    std::vector<std::unique_ptr<DevBuf>> uvs;
+    std::vector<float> boxes(size_t(count) * 6);
+    for (uint32_t i = 0; i < count; i++)
+    {
+        const agb_instance& s = inst[i];
+        if (s.geometry < 0 || size_t(s.geometry) >= ctx->geometries.size())
+            return fail(AGB_ERR_INVALID_ARG, "agb_instances_set: instance " + std::to_string(i) + " geometry out of range");
+        if (s.material < 0 || uint32_t(s.material) >= ctx->materialCount)
+            return fail(AGB_ERR_INVALID_ARG, "agb_instances_set: instance " + std::to_string(i) + " material out of range");
+        if (s.layer_count < 0 || s.layer_count > 64 || (s.layer_count > 0 && !s.layers))
+            return fail(AGB_ERR_INVALID_ARG, "agb_instances_set: bad layer list");
+        for (int k = 0; k < 12; k++)
+            if (!std::isfinite(s.object_to_world[k]))
+                return fail(AGB_ERR_INVALID_ARG, "agb_instances_set: non-finite transform");
+        DevInstance& d = di[i];
+        memcpy(d.o2w, s.object_to_world, sizeof d.o2w);
+        invertAffine(d.o2w, d.w2o);
+        for (int k = 0; k < 12; k++)
+            if (!std::isfinite(d.w2o[k]))
+                return fail(AGB_ERR_INVALID_ARG, "agb_instances_set: singular transform");
+        d.mesh        = s.geometry;
+        d.material    = s.material;
+        d.layerCount  = s.layer_count;
+        d.layerOffset = int32_t(dl.size());
+        const Geometry& g = *ctx->geometries[s.geometry];
+        for (int l = 0; l < s.layer_count; l++)
+        {
+            const agb_layer& L = s.layers[l];
+            if (L.material < 0 || uint32_t(L.material) >= ctx->materialCount || !L.texcoords)
+                return fail(AGB_ERR_INVALID_ARG, "agb_instances_set: bad layer material or UVs");
+            std::unique_ptr<DevBuf> b(new DevBuf());
+            st = upload(ctx, *b, L.texcoords, size_t(g.mesh.vertexCount) * 2 * sizeof(float), "upload layer UVs");
+            if (st)
+                return st;
+            // Layers are applied outermost first: the reference loops li = count .. 1 over
+            // layer index li - 1, so store them in the given order.
+            dl.push_back(DevLayer{ L.material, 0, b->as<float>() });
+            uvs.push_back(std::move(b));
+        }
+        float* box = &boxes[6 * size_t(i)];
+        for (int k = 0; k < 3; k++)
+        {
+            box[k]     = INFINITY;
+            box[3 + k] = -INFINITY;
+        }
+        for (int c = 0; c < 8; c++)
+        {
+            float p[3] = { (c & 1) ? g.bounds[3] : g.bounds[0], (c & 2) ? g.bounds[4] : g.bounds[1],
+                (c & 4) ? g.bounds[5] : g.bounds[2] };
+            for (int r = 0; r < 3; r++)
+            {
+                float w = d.o2w[4 * r] * p[0] + d.o2w[4 * r + 1] * p[1] + d.o2w[4 * r + 2] * p[2] +
+                    d.o2w[4 * r + 3];
+                box[r]     = std::min(box[r], w);
+                box[3 + r] = std::max(box[3 + r], w);
+            }
+        }
+        for (int k = 0; k < 3; k++)
+        {
+            float pad = 1e-5f * (std::fabs(box[k]) + std::fabs(box[3 + k])) + 1e-6f;
+            box[k] -= pad;
+            box[3 + k] += pad;
+        }
+    }
+    BuiltBVH tl;
+    buildBVH2(boxes.data(), count, 1, 12, tl);
+    int maxBlas = 0;
+    for (auto& g : ctx->geometries)
+        maxBlas = std::max(maxBlas, g->mesh.depth);
+    if (tl.depth + maxBlas + 2 > kStackSize)
+        return fail(AGB_ERR_LIMIT, "agb_instances_set: TLAS + BLAS depth exceeds the traversal stack");
+    std::vector<int32_t> order(tl.order.begin(), tl.order.end());
+    st = upload(ctx, ctx->instances, di.data(), di.size() * sizeof(DevInstance), "upload instances");
+    if (!st && !tl.nodes.empty())
+        st = upload(ctx, ctx->tlasNodes, tl.nodes.data(), tl.nodes.size() * sizeof(BNode), "upload TLAS");
+    if (!st)
+        st = upload(ctx, ctx->tlasOrder, order.data(), order.size() * sizeof(int32_t), "upload TLAS order");
+    if (!st && !dl.empty())
+        st = upload(ctx, ctx->layers, dl.data(), dl.size() * sizeof(DevLayer), "upload layers");
+    if (st)
+        return st;
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "upload instances");
+    ctx->layerUVs      = std::move(uvs);
+    ctx->instanceCount = count;
+    ctx->tlasRoot      = tl.root;
+    ctx->tlasDepth     = tl.depth;
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_environment_set(agb_context* ctx, const agb_environment_data* env,
+    int32_t light_image, int32_t background_image)
+{
+    if (!ctx || !env)
+        return fail(AGB_ERR_INVALID_ARG, "agb_environment_set: null argument");
+    if (light_image >= int32_t(ctx->images.size()) || background_image >= int32_t(ctx->images.size()))
+        return fail(AGB_ERR_INVALID_ARG, "agb_environment_set: image index out of range");
+    if (light_image >= 0 && ctx->images[light_image]->view.format != AGB_FORMAT_RGBA32F)
+        return fail(AGB_ERR_INVALID_ARG, "agb_environment_set: light image must be float RGB(A)");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    ctx->env           = *env;
+    ctx->envLight      = light_image;
+    ctx->envBackground = background_image;
+    ctx->env.has_light_tex      = light_image >= 0 ? 1 : 0;
+    ctx->env.has_background_tex = background_image >= 0 ? 1 : 0;
+    if (light_image >= 0)
+    {
+        const DevImage& v = ctx->images[light_image]->view;
+        uint64_t n = uint64_t(v.width) * v.height;
+        if (n >= (1ull << 31))
+            return fail(AGB_ERR_LIMIT, "agb_environment_set: light image too large");
+        AGB_CUDA(ctx->alias.ensure(n * sizeof(agb_alias_entry)), "allocate alias table");
+        double integral = 0.0;
+        AGB_CUDA(buildEnvAlias(static_cast<const float4*>(v.data), v.width, v.height,
+                     ctx->alias.as<agb_alias_entry>(), &integral, ctx->envScratch, ctx->stream),
+            "build environment alias table");
+        ctx->envIntegral = integral;
+        ctx->env.light_tex_luminance_integral = float(integral);
+    }
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_environment_alias(agb_context* ctx, agb_alias_entry* host_out,
+    uint64_t capacity, double* integral)
+{
+    if (!ctx || ctx->envLight < 0)
+        return fail(AGB_ERR_NOT_READY, "agb_environment_alias: no light image");
+    const DevImage& v = ctx->images[ctx->envLight]->view;
+    uint64_t n = uint64_t(v.width) * v.height;
+    if (!host_out || capacity < n)
+        return fail(AGB_ERR_INVALID_ARG, "agb_environment_alias: output too small");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    AGB_CUDA(cudaMemcpyAsync(host_out, ctx->alias.ptr, n * sizeof(agb_alias_entry),
+                 cudaMemcpyDeviceToHost, ctx->stream),
+        "read alias table");
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "read alias table");
+    if (integral)
+        *integral = ctx->envIntegral;
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_frame_set(agb_context* ctx, const agb_frame_data* frame)
+{
+    if (!ctx || !frame)
+        return fail(AGB_ERR_INVALID_ARG, "agb_frame_set: null argument");
+    ctx->frame = *frame;
+    // RendererBase.cpp:280-282 clamps the trace depth to [1, kMaxTraceDepth = 10].
+    ctx->frame.trace_depth = std::max(1, std::min(10, ctx->frame.trace_depth));
+    if (ctx->frame.distant_light_count < 0 || ctx->frame.distant_light_count > 4)
+        return fail(AGB_ERR_INVALID_ARG, "agb_frame_set: distant_light_count must be 0..4");
+    ctx->frameSet = true;
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
+    uint32_t sample_start, uint32_t sample_count, agb_render_stats* stats)
+{
+    if (!ctx || !opt)
+        return fail(AGB_ERR_INVALID_ARG, "agb_render: null argument");
+    if (!ctx->frameSet)
+        return fail(AGB_ERR_NOT_READY, "agb_render: frame data not set");
+    if (opt->width == 0 || opt->height == 0 || uint64_t(opt->width) * opt->height > (1ull << 26))
+        return fail(AGB_ERR_INVALID_ARG, "agb_render: bad image size");
+    if (ctx->instanceCount > 0 && ctx->materialCount == 0)
+        return fail(AGB_ERR_NOT_READY, "agb_render: no materials");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    if (!ctx->frame.is_force_opaque_shadows_enabled)
+        return fail(AGB_ERR_INVALID_ARG,
+            "agb_render: transparent (any-hit) shadows are not supported; set "
+            "is_force_opaque_shadows_enabled as the HGI backend does");
+    uint32_t accumMode = opt->accumulation ? opt->accumulation : AGB_ACCUM_RUNNING_MEAN;
+    uint32_t pixels    = opt->width * opt->height;
+    uint64_t maxPaths  = opt->max_paths_in_flight ? opt->max_paths_in_flight : (1u << 22);
+    uint32_t spw       = uint32_t(std::max<uint64_t>(1, maxPaths / pixels));
+    spw                = std::min(spw, std::max(1u, sample_count));
+    if (uint64_t(spw) * pixels >= (1ull << 29))
+        return fail(AGB_ERR_LIMIT, "agb_render: wave too large");
+    uint32_t waves = sample_count ? (sample_count + spw - 1) / spw : 0;
+    int depth      = ctx->frame.trace_depth;
+    st = ensureAccum(ctx, opt->width, opt->height);
+    if (!st)
+        st = ensureWave(ctx, size_t(spw) * pixels, depth, std::max(1u, waves));
+    if (st)
+        return st;
+    if (sample_start == 0)
+        ctx->accumulatedSamples = 0;
+    else if (ctx->accumulatedSamples != sample_start || (ctx->lastAccumMode & accumMode) != accumMode)
+        return fail(AGB_ERR_INVALID_ARG, "agb_render: sample_start must continue the accumulated "
+                                         "sequence in the same accumulation mode");
+    size_t counterWords = size_t(depth + 2) * 4;
+    AGB_CUDA(cudaMemsetAsync(ctx->counters.ptr, 0, counterWords * waves * sizeof(uint32_t), ctx->stream),
+        "clear counters");
+    AGB_CUDA(cudaMemsetAsync(ctx->stats.ptr, 0, 8 * sizeof(unsigned long long), ctx->stream), "clear stats");
+    DevScene scene = ctx->scene();
+    WaveBuffers wb = ctx->wb;
+    wb.accumMean  = ctx->accMean.as<float4>();
+    wb.accumSum   = ctx->accSum.as<float4>();
+    wb.accumComp  = ctx->accComp.as<float4>();
+    wb.lastSample = ctx->lastSample.as<float4>();
+    uint64_t launches = 0;
+    ctx->marks.reset();
+    KernelMarks* marks = ctx->profiling ? &ctx->marks : nullptr;
+    AGB_CUDA(cudaEventRecord(ctx->ev0, ctx->stream), "record event");
+    for (uint32_t w = 0; w < waves; w++)
+    {
+        WaveParams wp{};
+        wp.width          = opt->width;
+        wp.height         = opt->height;
+        wp.pixels         = pixels;
+        wp.sampleBase     = sample_start + w * spw;
+        wp.samples        = std::min(spw, sample_start + sample_count - wp.sampleBase);
+        wp.paths          = wp.samples * pixels;
+        wp.accumMode      = accumMode;
+        wp.countTraversal = ctx->counting ? 1 : 0;
+        wb.counters       = ctx->counters.as<uint32_t>() + counterWords * w;
+        launchWave(scene, ctx->frame, wp, wb, ctx->stream, ctx->smCount, launches, marks);
+        AGB_CUDA(cudaGetLastError(), "launch wave");
+    }
+    AGB_CUDA(cudaEventRecord(ctx->ev1, ctx->stream), "record event");
+    ctx->accumulatedSamples = sample_start + sample_count;
+    ctx->lastAccumMode      = sample_start == 0 ? accumMode : ctx->lastAccumMode;
+    if (stats)
+    {
+        AGB_CUDA(cudaEventSynchronize(ctx->ev1), "render");
+        std::vector<uint32_t> c(counterWords * waves);
+        AGB_CUDA(cudaMemcpy(c.data(), ctx->counters.ptr, c.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost),
+            "read counters");
+        unsigned long long s[8];
+        AGB_CUDA(cudaMemcpy(s, ctx->stats.ptr, sizeof s, cudaMemcpyDeviceToHost), "read stats");
+        if (s[4])
+            return fail(AGB_ERR_LIMIT, "agb_render: traversal stack overflow");
+        agb_render_stats r{};
+        r.paths = uint64_t(sample_count) * pixels;
+        for (uint32_t w = 0; w < waves; w++)
+            for (int b = 0; b < depth; b++)
+            {
+                r.closest_rays += c[counterWords * w + 4 * b + 0];
+                r.shadow_rays += c[counterWords * w + 4 * b + 1];
+            }
+        r.node_visits        = s[2];
+        r.tri_tests          = s[3];
+        r.shadow_node_visits = s[5];
+        r.shadow_tri_tests   = s[6];
+        r.kernel_launches    = launches;
+        if (marks)
+        {
+            double ms[KC_COUNT];
+            marks->sum(ms);
+            for (int k = 0; k < 6; k++)
+                r.kernel_ms[k] = ms[k];
+            for (size_t i = 0; i < marks->category.size(); i++)
+                if (marks->category[i] < 6)
+                    r.kernel_count[marks->category[i]]++;
+        }
+        float ms = 0.f;
+        AGB_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "event time");
+        r.gpu_ms = ms;
+        *stats   = r;
+    }
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_wait(agb_context* ctx)
+{
+    if (!ctx)
+        return fail(AGB_ERR_INVALID_ARG, "agb_wait: null context");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "agb_wait");
+    unsigned long long s[8] = { 0 };
+    if (ctx->stats.ptr)
+    {
+        AGB_CUDA(cudaMemcpy(s, ctx->stats.ptr, sizeof s, cudaMemcpyDeviceToHost), "read stats");
+        if (s[4])
+            return fail(AGB_ERR_LIMIT, "traversal stack overflow during render");
+    }
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_accum_device(agb_context* ctx, int32_t mode, float** device_rgba)
+{
+    if (!ctx || !device_rgba || !ctx->accMean.ptr)
+        return fail(AGB_ERR_NOT_READY, "agb_accum_device: nothing rendered");
+    *device_rgba = mode == AGB_ACCUM_KAHAN ? ctx->accSum.as<float>() : ctx->accMean.as<float>();
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_last_sample_device(agb_context* ctx, float** device_rgba)
+{
+    if (!ctx || !device_rgba || !ctx->lastSample.ptr)
+        return fail(AGB_ERR_NOT_READY, "agb_last_sample_device: nothing rendered");
+    *device_rgba = ctx->lastSample.as<float>();
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_accum_read(agb_context* ctx, int32_t mode, float* host_rgba,
+    uint64_t capacity_floats)
+{
+    if (!ctx || !host_rgba || !ctx->accMean.ptr)
+        return fail(AGB_ERR_NOT_READY, "agb_accum_read: nothing rendered");
+    size_t n = size_t(ctx->accW) * ctx->accH * 4;
+    if (capacity_floats < n)
+        return fail(AGB_ERR_INVALID_ARG, "agb_accum_read: buffer too small");
+    if (mode != AGB_ACCUM_RUNNING_MEAN && mode != AGB_ACCUM_KAHAN)
+        return fail(AGB_ERR_INVALID_ARG, "agb_accum_read: bad mode");
+    if (!(ctx->lastAccumMode & uint32_t(mode)))
+        return fail(AGB_ERR_NOT_READY, "agb_accum_read: mode was not accumulated");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    const void* src = mode == AGB_ACCUM_KAHAN ? ctx->accSum.ptr : ctx->accMean.ptr;
+    AGB_CUDA(cudaMemcpyAsync(host_rgba, src, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream),
+        "read accumulation");
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "read accumulation");
+    if (mode == AGB_ACCUM_KAHAN && ctx->accumulatedSamples)
+    {
+        float inv = 1.f / float(ctx->accumulatedSamples);
+        for (size_t i = 0; i < n; i++)
+            host_rgba[i] *= inv;
+    }
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_post_process(agb_context* ctx, int32_t mode, const float brightness[3],
+    int32_t tone_map, int32_t gamma, float* out_rgba32f, uint8_t* out_rgba8)
+{
+    if (!ctx || !ctx->accMean.ptr || !brightness)
+        return fail(AGB_ERR_NOT_READY, "agb_post_process: nothing rendered");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    size_t pixels = size_t(ctx->accW) * ctx->accH;
+    DevBuf o32, o8;
+    AGB_CUDA(o32.ensure(pixels * sizeof(float4)), "allocate post output");
+    AGB_CUDA(o8.ensure(pixels * sizeof(uchar4)), "allocate post output");
+    const float4* src = mode == AGB_ACCUM_KAHAN ? ctx->accSum.as<float4>() : ctx->accMean.as<float4>();
+    float inv = ctx->accumulatedSamples ? 1.f / float(ctx->accumulatedSamples) : 1.f;
+    AGB_CUDA(launchPostProcess(src, nullptr, mode, inv, uint32_t(pixels),
+                 make_float3(brightness[0], brightness[1], brightness[2]), tone_map, gamma,
+                 o32.as<float4>(), o8.as<uchar4>(), ctx->stream),
+        "post-process");
+    if (out_rgba32f)
+        AGB_CUDA(cudaMemcpyAsync(out_rgba32f, o32.ptr, pixels * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream),
+            "read post output");
+    if (out_rgba8)
+        AGB_CUDA(cudaMemcpyAsync(out_rgba8, o8.ptr, pixels * sizeof(uchar4), cudaMemcpyDeviceToHost, ctx->stream),
+            "read post output");
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "post-process");
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_bsdf_batch(int32_t op, const agb_material* materials,
+    const int32_t* material_index, const float* frames, const float* V, const float* L,
+    const float* rnd, int64_t n, float* out_value, float* out_dir, float* out_pdf,
+    int32_t* out_lobe, void* cuda_stream)
+{
+    if (op < 0 || op > 2 || n < 0 || (n > 0 && (!materials || !material_index || !frames || !V || !out_value)))
+        return fail(AGB_ERR_INVALID_ARG, "agb_bsdf_batch: invalid argument");
+    if ((op == 0 || op == 2) && n > 0 && !L)
+        return fail(AGB_ERR_INVALID_ARG, "agb_bsdf_batch: L required");
+    if (op >= 1 && n > 0 && (!rnd || !out_pdf || !out_lobe || (op == 1 && !out_dir)))
+        return fail(AGB_ERR_INVALID_ARG, "agb_bsdf_batch: sampling outputs required");
+    AGB_CUDA(launchBsdfBatch(op, materials, material_index, frames, V, L, rnd, n, out_value, out_dir,
+                 out_pdf, out_lobe, static_cast<cudaStream_t>(cuda_stream)),
+        "agb_bsdf_batch");
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_intersect_batch(agb_context* ctx, const float* rays, int64_t n,
+    int32_t any_hit, float* out_tuv, int32_t* out_inst_prim)
+{
+    if (!ctx || n < 0 || (n > 0 && (!rays || !out_tuv || !out_inst_prim)))
+        return fail(AGB_ERR_INVALID_ARG, "agb_intersect_batch: invalid argument");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    AGB_CUDA(launchIntersectBatch(ctx->scene(), rays, n, any_hit, out_tuv, out_inst_prim,
+                 ctx->stream, ctx->smCount),
+        "agb_intersect_batch");
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "agb_intersect_batch");
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_env_sample_batch(agb_context* ctx, const float* rnd, int64_t n,
+    float* out_radiance, float* out_dir, float* out_pdf)
+{
+    if (!ctx || n < 0 || (n > 0 && (!rnd || !out_radiance || !out_dir || !out_pdf)))
+        return fail(AGB_ERR_INVALID_ARG, "agb_env_sample_batch: invalid argument");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    AGB_CUDA(launchEnvSampleBatch(ctx->scene(), rnd, n, out_radiance, out_dir, out_pdf, ctx->stream),
+        "agb_env_sample_batch");
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "agb_env_sample_batch");
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_random_stream(uint32_t sample_index, uint32_t screen_width, uint32_t px,
+    uint32_t py, int32_t n, float* out, void* cuda_stream)
+{
+    if (!out || n < 0)
+        return fail(AGB_ERR_INVALID_ARG, "agb_random_stream: invalid argument");
+    AGB_CUDA(launchRandomStream(sample_index, screen_width, px, py, n, out,
+                 static_cast<cudaStream_t>(cuda_stream)),
+        "agb_random_stream");
+    return AGB_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,120 @@
+// Internal declarations shared by the CUDA translation units of libagb_cuda.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "agb_wavefront.cuh"
+
+namespace agb
+{
+
+constexpr int kTraceBlock       = 128; // threads per traversal block
+constexpr int kTraceBlocksPerSM = 8;   // 8 x 128 threads x 48 stack entries x 4 B = 192 KB / SM
+constexpr int kShadeBlock       = 128;
+
+// Kernel categories for per-kernel device timing.
+enum KernelCategory
+{
+    KC_CAMERA = 0,
+    KC_CLOSEST,
+    KC_SHADE,
+    KC_SHADOW,
+    KC_RESOLVE,
+    KC_FINALIZE,
+    KC_END,
+    KC_COUNT
+};
+
+// CUDA events recorded before each launch; interval i is charged to the launch after mark i.
+struct KernelMarks
+{
+    std::vector<cudaEvent_t> pool;
+    std::vector<int> category;
+    size_t used = 0;
+    void reset() { used = 0, category.clear(); }
+    void record(int cat, cudaStream_t st)
+    {
+        if (used == pool.size())
+        {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            pool.push_back(e);
+        }
+        cudaEventRecord(pool[used], st);
+        category.push_back(cat);
+        used++;
+    }
+    // Milliseconds per category (call after the stream has completed).
+    void sum(double ms[KC_COUNT]) const
+    {
+        for (int k = 0; k < KC_COUNT; k++)
+            ms[k] = 0.0;
+        for (size_t i = 0; i + 1 < used; i++)
+        {
+            if (category[i] == KC_END)
+                continue;
+            float t = 0.f;
+            cudaEventElapsedTime(&t, pool[i], pool[i + 1]);
+            ms[category[i]] += t;
+        }
+    }
+    ~KernelMarks()
+    {
+        for (auto e : pool)
+            cudaEventDestroy(e);
+    }
+};
+
+// agb_pt.cu
+void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp,
+    const WaveBuffers& wb, cudaStream_t st, int smCount, uint64_t& launches, KernelMarks* marks);
+void setTraceAttributes();
+
+// agb_env_build.cu: FP64-prefix-sum alias table on the device.  rgba: device RGBA32F texels.
+// Returns the luminance integral.  scratch is reused across calls.
+struct EnvBuildScratch
+{
+    double* weights   = nullptr; // per texel (luminance x solid angle), then normalised p
+    double* scanA     = nullptr;
+    double* scanB     = nullptr;
+    uint32_t* ranks   = nullptr;
+    uint32_t* heavyIdx = nullptr;
+    double* heavyIncl = nullptr;
+    double* lightIncl = nullptr;
+    double* blockSums = nullptr;
+    uint32_t* blockCounts = nullptr;
+    size_t capacity   = 0;
+};
+cudaError_t buildEnvAlias(const float4* rgba, uint32_t width, uint32_t height,
+    agb_alias_entry* out, double* integralOut, EnvBuildScratch& scratch, cudaStream_t st);
+void freeEnvScratch(EnvBuildScratch& s);
+
+// agb_bvh_build.cpp: host binned-SAH builder producing the device layout.
+struct BuiltBVH
+{
+    std::vector<BNode> nodes;
+    std::vector<uint32_t> order; // primitive index per leaf slot
+    int32_t root  = 0;
+    int32_t depth = 0;
+};
+// boxes: 6 floats per primitive (lo xyz, hi xyz).
+void buildBVH2(const float* boxes, uint32_t count, int maxLeaf, int maxDepth, BuiltBVH& out);
+// Double-precision inverse of a 3x4 affine transform rounded to float.
+void invertAffine(const float* m, float* out);
+
+// agb_unit.cu
+cudaError_t launchBsdfBatch(int op, const agb_material* mats, const int32_t* matIndex,
+    const float* frames, const float* V, const float* L, const float* rnd, int64_t n,
+    float* outValue, float* outDir, float* outPdf, int32_t* outLobe, cudaStream_t st);
+cudaError_t launchIntersectBatch(const DevScene& s, const float* rays, int64_t n, int anyHit,
+    float* outTUV, int32_t* outInstPrim, cudaStream_t st, int smCount);
+cudaError_t launchEnvSampleBatch(const DevScene& s, const float* rnd, int64_t n,
+    float* outRadiance, float* outDir, float* outPdf, cudaStream_t st);
+cudaError_t launchRandomStream(uint32_t sampleIndex, uint32_t width, uint32_t px, uint32_t py,
+    int n, float* out, cudaStream_t st);
+cudaError_t launchPostProcess(const float4* accum, const float* accumComp, int mode,
+    float invCount, uint32_t pixels, float3 brightness, int toneMap, int gamma, float4* out32,
+    uchar4* out8, cudaStream_t st);
+
+} // namespace agb

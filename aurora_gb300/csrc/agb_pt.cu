@@ -1,0 +1,718 @@
+// Wavefront path-tracing kernels.  One wave traces `samples` sample indices for every pixel; the
+// host (agb_render.cu) launches, per wave:
+//   k_camera                                   RayGenShader prologue (MainEntryPoints.slang:70-121)
+//   per bounce b < traceDepth:
+//     k_trace_closest   closest-hit rays        TraceRay (RayTrace.slang:185-210)
+//     k_shade           hit / miss shading      InstanceClosestHitShader + InstanceMissShader
+//                                               (HitShaderEntryPoints.slang:35-486,
+//                                                MainEntryPoints.slang:355-426)
+//     k_trace_shadow    shadow rays             traceShadowRay (RayTrace.slang:221-270)
+//     k_resolve         visibility x pending contributions, RayGen accumulation
+//                                               (HitShaderEntryPoints.slang:394-467,
+//                                                MainEntryPoints.slang:160-243)
+//   k_shade (depth limit) environment at rayDepth == traceDepth (MainEntryPoints.slang:127-138)
+//   k_finalize          adjustRadiance + accumulation (PathTracingCommon.slang:59-82,
+//                                               HGI/Shaders/Accumulation.glsl:14-34)
+// Shading arithmetic is compiled without multiply-add contraction (see the build flags) so that
+// FP32 results follow the reference's operation order.
+#include "agb_kernels.h"
+
+namespace agb
+{
+
+__device__ __forceinline__ unsigned long long* statPtr(const WaveBuffers& wb, int k)
+{
+    return wb.stats + k;
+}
+
+// ------------------------------------------------------------------------------ camera rays
+// RayTrace.slang:130-182
+__device__ void cameraRay(const agb_frame_data& f, uint32_t px, uint32_t py, uint32_t W,
+    uint32_t H, Rng& rng, v3& o, v3& d)
+{
+    v2 sc = v2{ float(px), float(py) };
+    if (f.is_temporal_jitter_enabled)
+        sc = sc + v2{ 0.5f + f.camera_jitter[0], 0.5f + f.camera_jitter[1] };
+    else
+        sc = sc + random2D(rng);
+    v2 ndc = v2{ sc.x / float(W), sc.y / float(H) };
+    ndc    = v2{ ndc.x * 2.f - 1.f, ndc.y * 2.f - 1.f };
+    ndc.y  = -ndc.y;
+    const float* m = f.camera_inv_view;
+    v3 right = v3{ m[0], m[4], m[8] };
+    v3 up    = v3{ m[1], m[5], m[9] };
+    v3 front = -v3{ m[2], m[6], m[10] };
+    v3 eye   = v3{ m[3], m[7], m[11] };
+    float sx = f.view_size[0] * 0.5f, sy = f.view_size[1] * 0.5f;
+    v3 off   = right * (sx * ndc.x) + up * (sy * ndc.y);
+    if (f.is_ortho_projection)
+    {
+        d = front;
+        o = eye + off;
+    }
+    else
+    {
+        d = normalize(front + off);
+        o = eye;
+    }
+    if (f.lens_radius > 0.f)
+    {
+        v3 focal = o + d * f.focal_distance;
+        v2 lo    = sampleDisk(random2D(rng), f.lens_radius);
+        o        = o + right * lo.x + up * lo.y;
+        d        = normalize(focal - o);
+    }
+}
+
+__global__ void k_camera(agb_frame_data f, WaveParams wp, WaveBuffers wb)
+{
+    uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < wp.paths; p += stride)
+    {
+        uint32_t pixel = p % wp.pixels;
+        uint32_t k     = p / wp.pixels;
+        uint32_t px = pixel % wp.width, py = pixel / wp.width;
+        Rng rng     = rngInit(wp.sampleBase + k, wp.width, px, py);
+        v3 o, d;
+        cameraRay(f, px, py, wp.width, wp.height, rng, o, d);
+        wb.rayOrg[0][p]  = make_float4(o.x, o.y, o.z, 0.f);
+        wb.rayDir[0][p]  = make_float4(d.x, d.y, d.z, __int_as_float(0x7f800000));
+        wb.rayPath[0][p] = p;
+        wb.rng[p]        = make_uint2(rng.x, rng.y);
+        wb.contrib[p]    = make_float4(1.f, 1.f, 1.f, 0.f);
+        wb.flags[p] = PF_PRIMARY | (uint32_t(CAMERA_RAY) << PF_RAYTYPE_SHIFT) |
+            (uint32_t(NO_SECONDARY_RAY) << PF_MISLOBE_SHIFT);
+        float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        wb.outDirect[p]    = z;
+        wb.outDiffuse[p]   = z;
+        wb.outGlossy[p]    = z;
+        wb.lastIndirect[p] = z;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        wb.counters[0] = wp.paths;
+}
+
+// --------------------------------------------------------------------------------- tracing
+extern __shared__ int32_t g_stack[];
+
+template <bool kCount>
+__global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_closest(DevScene s, WaveBuffers wb, int bounce, int cur)
+{
+    uint32_t n      = wb.counters[bounce * 4 + 0];
+    int32_t* stack  = g_stack + threadIdx.x;
+    TraceCounters c = { 0, 0 };
+    bool overflow   = false;
+    uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        float4 o4 = wb.rayOrg[cur][i], d4 = wb.rayDir[cur][i];
+        RayHit h;
+        bool hit = castRay<false, kCount>(s, v3{ o4.x, o4.y, o4.z }, v3{ d4.x, d4.y, d4.z }, o4.w,
+            d4.w, h, stack, kTraceBlock, c, overflow);
+        wb.hitTUV[i]  = make_float4(hit ? h.t : -1.f, h.u, h.v, __int_as_float(h.prim));
+        wb.hitInst[i] = hit ? h.inst : -1;
+    }
+    if (kCount)
+    {
+        atomicAdd(statPtr(wb, 2), c.nodes);
+        atomicAdd(statPtr(wb, 3), c.tris);
+    }
+    if (overflow)
+        atomicAdd(statPtr(wb, 4), 1ull);
+}
+
+template <bool kCount>
+__global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_shadow(DevScene s, WaveBuffers wb, int bounce)
+{
+    uint32_t n      = wb.counters[bounce * 4 + 1];
+    int32_t* stack  = g_stack + threadIdx.x;
+    TraceCounters c = { 0, 0 };
+    bool overflow   = false;
+    uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        uint32_t tag = wb.shTag[i];
+        uint32_t p = tag >> 3, k = tag & 7u;
+        float4 o4 = wb.shOrg[p];
+        float4 d4 = wb.shDir[size_t(p) * kMaxShadowSlots + k];
+        RayHit h;
+        bool hit = castRay<true, kCount>(s, v3{ o4.x, o4.y, o4.z }, v3{ d4.x, d4.y, d4.z }, kRayTMin,
+            __int_as_float(0x7f800000), h, stack, kTraceBlock, c, overflow);
+        if (hit)
+            atomicOr(wb.occluded + p, 1u << k);
+    }
+    if (kCount)
+    {
+        atomicAdd(statPtr(wb, 5), c.nodes);
+        atomicAdd(statPtr(wb, 6), c.tris);
+    }
+    if (overflow)
+        atomicAdd(statPtr(wb, 4), 1ull);
+}
+
+// -------------------------------------------------------------------------------- shading
+// ShadeFunctions.slang:51-89
+__device__ __forceinline__ v3 shadeDistantLight(const agb_distant_light& l, const Mat& m,
+    const Frame& fr, v3 V, Rng& rng, v3& dirOut)
+{
+    v2 r    = random2D(rng);
+    v3 L    = sampleCone(r, ld3(l.direction), l.cos_radius);
+    v3 bsdf = evaluateMaterial(m, fr, V, L);
+    if (isBlack(bsdf))
+    {
+        dirOut = splat(0.f);
+        return splat(0.f);
+    }
+    dirOut = L;
+    return ld3(l.color_and_intensity) * l.color_and_intensity[3] * bsdf;
+}
+
+__device__ __forceinline__ void accumulateSegment(WaveBuffers& wb, uint32_t p, int bounce,
+    uint32_t flags, uint32_t rayType, v3 direct, v3 indirect, float clampLum)
+{
+    if (bounce == 0)
+    {
+        wb.outDirect[p] = make_float4(direct.x, direct.y, direct.z, 0.f);
+        float4 ind      = make_float4(indirect.x, indirect.y, indirect.z, 0.f);
+        if (pfMisLobe(flags) == DIFFUSE_LOBE)
+            wb.outDiffuse[p] = ind;
+        else
+            wb.outGlossy[p] = ind;
+        return;
+    }
+    v3 radiance = direct + indirect;
+    if (clampLum > 0.f)
+    {
+        float lum = luminance(radiance);
+        if (lum > clampLum)
+            radiance *= clampLum / lum;
+        if (isnan(radiance.x) || isnan(radiance.y) || isnan(radiance.z) || isinf(radiance.x) ||
+            isinf(radiance.y) || isinf(radiance.z))
+            radiance = splat(0.f);
+    }
+    float4* dst = rayType == DIFFUSE_LOBE ? wb.outDiffuse + p : wb.outGlossy + p;
+    float4 a    = *dst;
+    *dst        = make_float4(a.x + radiance.x, a.y + radiance.y, a.z + radiance.z, 0.f);
+}
+
+__global__ void __launch_bounds__(kShadeBlock) k_shade(DevScene s, agb_frame_data f,
+    WaveParams wp, WaveBuffers wb, int bounce, int cur, int depthLimit)
+{
+    uint32_t n      = wb.counters[bounce * 4 + 0];
+    uint32_t stride = gridDim.x * blockDim.x;
+    const float clampLum = f.indirect_bounce_clamp_scale > 0.f
+        ? f.max_luminance * f.indirect_bounce_clamp_scale
+        : 0.f;
+    v2 screen = v2{ float(wp.width), float(wp.height) };
+    // Warp-uniform loop: every lane of a warp runs the same number of iterations so the queue
+    // appends at the end of the body are executed by the whole warp.
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride)
+    {
+        uint32_t i     = base + threadIdx.x;
+        bool valid     = i < n;
+        bool pushNext  = false;
+        bool resolve   = false;
+        uint32_t slots = 0;
+        uint32_t p     = 0;
+        v3 nextO = splat(0.f), nextD = splat(0.f);
+        if (valid)
+        {
+            p          = wb.rayPath[cur][i];
+            float4 d4  = wb.rayDir[cur][i];
+            v3 dir     = v3{ d4.x, d4.y, d4.z };
+            uint32_t flags = wb.flags[p];
+            float4 c4  = wb.contrib[p];
+            v3 contrib = v3{ c4.x, c4.y, c4.z };
+            uint32_t rayType = pfRayType(flags);
+            bool primary = (flags & PF_PRIMARY) != 0;
+            uint32_t pixel = p % wp.pixels;
+            v2 pixel2 = v2{ float(pixel % wp.width), float(pixel / wp.width) };
+            bool bg = primary || rayType == TRANSMISSION_LOBE || rayType == GROUND_PLANE_REFLECTION_RAY;
+            if (depthLimit)
+            {
+                v3 direct = evaluateEnvironment(s, dir, bg, pixel2, screen) * contrib;
+                float4 li = wb.lastIndirect[p];
+                accumulateSegment(wb, p, bounce, flags, rayType, direct, v3{ li.x, li.y, li.z },
+                    clampLum);
+            }
+            else
+            {
+                float4 h  = wb.hitTUV[i];
+                int32_t inst = wb.hitInst[i];
+                if (inst < 0)
+                {
+                    v3 direct = bg ? evaluateEnvironment(s, dir, true, pixel2, screen) * contrib
+                                   : splat(0.f);
+                    accumulateSegment(wb, p, bounce, flags, rayType, direct, splat(0.f), clampLum);
+                }
+                else
+                {
+                    Rng rng;
+                    {
+                        uint2 r = wb.rng[p];
+                        rng     = Rng{ r.x, r.y };
+                    }
+                    const DevInstance& in = s.instances[inst];
+                    v3 V       = -dir;
+                    Shading sh = computeShading(s, in, uint32_t(__float_as_int(h.w)), h.y, h.z);
+                    v2 baseUV  = sh.uv;
+                    bool hitLayer = false;
+                    Mat m;
+                    v3 matNormal = sh.N;
+                    bool genNormal = false;
+                    float P = 0.f;
+                    for (int li = in.layerCount; li >= 0; li--)
+                    {
+                        int32_t mi;
+                        if (li == 0)
+                        {
+                            mi    = in.material;
+                            sh.uv = baseUV;
+                        }
+                        else
+                        {
+                            const DevLayer& L = s.layers[in.layerOffset + li - 1];
+                            mi = L.material;
+                            v2 uv = v2{ 0.f, 0.f };
+                            float b3[3] = { sh.bary.x, sh.bary.y, sh.bary.z };
+                            for (int q = 0; q < 3; q++)
+                            {
+                                v2 t = v2{ __ldg(L.texcoords + 2 * size_t(sh.idx[q])),
+                                    __ldg(L.texcoords + 2 * size_t(sh.idx[q]) + 1) };
+                                uv = uv + t * b3[q];
+                            }
+                            sh.uv = uv;
+                        }
+                        matNormal = sh.N;
+                        m = loadMaterial(s, mi, sh, matNormal, genNormal);
+                        if (!primary && f.is_path_regularization_enabled)
+                        {
+                            float fl = lerpf(0.05f, lerpf(0.05f, 0.35f, f.path_regularization_strength),
+                                saturatef(float(bounce) / 3.f));
+                            m.specularRoughness = m.specularRoughness > fl ? m.specularRoughness : fl;
+                            m.coatRoughness     = m.coatRoughness > fl ? m.coatRoughness : fl;
+                        }
+                        v3 transparency = splat(1.f) - m.opacity;
+                        P        = luminance(transparency);
+                        hitLayer = random2D(rng).x >= P;
+                        if (hitLayer)
+                            break;
+                        contrib *= transparency / P;
+                    }
+                    if (!hitLayer)
+                    {
+                        // No layer absorbed the ray: continue straight on (skipContribution).
+                        nextO    = sh.geomPosition;
+                        nextD    = dir;
+                        pushNext = true;
+                        wb.lastIndirect[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+                    else
+                    {
+                        Frame fr = Frame{ sh.N, sh.X, sh.Y };
+                        if (genNormal)
+                        {
+                            fr.N = matNormal;
+                            buildBasis(fr.N, fr.X, fr.Y);
+                        }
+                        v3 emission = m.emissionColor * m.emission * lerp3(splat(1.f), m.coatColor, m.coat);
+                        v3 so = dot(V, fr.N) < 0.f ? sh.geomPosition : sh.position;
+                        float4* pslot = wb.pendSlot + size_t(p) * kMaxShadowSlots;
+                        float4* pdir  = wb.shDir + size_t(p) * kMaxShadowSlots;
+                        int nl = f.distant_light_count;
+                        if (!f.is_denoising_aovs_enabled && nl > 1)
+                        {
+                            for (int l = 0; l < nl && l < 4; l++)
+                            {
+                                if (f.distant_lights[l].color_and_intensity[3] <= 0.f)
+                                    continue;
+                                v3 sd;
+                                v3 r = shadeDistantLight(f.distant_lights[l], m, fr, V, rng, sd);
+                                if (isBlack(r))
+                                    continue;
+                                pslot[l] = make_float4(r.x, r.y, r.z, 0.f);
+                                pdir[l]  = make_float4(sd.x, sd.y, sd.z, 0.f);
+                                slots |= 1u << l;
+                            }
+                        }
+                        else if (nl > 0)
+                        {
+                            float w[4];
+                            float total = 0.f;
+                            for (int l = 0; l < nl && l < 4; l++)
+                            {
+                                const float* ci = f.distant_lights[l].color_and_intensity;
+                                w[l] = luminance(v3{ ci[0], ci[1], ci[2] }) * ci[3];
+                                total += w[l];
+                            }
+                            int idx = 0;
+                            float selPdf = 1.f / float(nl);
+                            if (total > 0.f)
+                            {
+                                float r = random2D(rng).x * total;
+                                float cum = 0.f;
+                                for (int l = 0; l < nl && l < 4; l++)
+                                {
+                                    cum += w[l];
+                                    if (r <= cum || l == nl - 1)
+                                    {
+                                        idx    = l;
+                                        selPdf = w[l] / total;
+                                        break;
+                                    }
+                                }
+                            }
+                            else
+                                idx = int(random2D(rng).x * float(nl));
+                            if (f.distant_lights[idx].color_and_intensity[3] > 0.f)
+                            {
+                                v3 sd;
+                                v3 r = shadeDistantLight(f.distant_lights[idx], m, fr, V, rng, sd);
+                                r    = r / fmaxf_(selPdf, 1e-4f);
+                                if (!isBlack(r))
+                                {
+                                    pslot[0] = make_float4(r.x, r.y, r.z, 0.f);
+                                    pdir[0]  = make_float4(sd.x, sd.y, sd.z, 0.f);
+                                    slots |= 1u;
+                                }
+                            }
+                        }
+                        // Environment MIS (ShadeFunctions.slang:135-259): one random pair for both halves.
+                        int misLobe;
+                        bool mis = false;
+                        {
+                            v2 rnd = random2D(rng);
+                            v3 L;
+                            float mpdf;
+                            v3 bsdf = sampleMaterial(m, fr, V, rnd, L, mpdf, misLobe);
+                            if (misLobe != TRANSMISSION_LOBE)
+                            {
+                                v3 lr = evaluateEnvironment(s, L, false, pixel2, screen);
+                                if (!isBlack(lr) && !isBlack(bsdf))
+                                {
+                                    float lpdf = s.env.has_light_tex && s.envLight.data
+                                        ? luminance(lr) / s.env.light_tex_luminance_integral
+                                        : divPi(0.25f);
+                                    v3 res = lr * misWeight(mpdf, lpdf) * bsdf / mpdf;
+                                    pslot[4] = make_float4(res.x, res.y, res.z, 0.f);
+                                    pdir[4]  = make_float4(L.x, L.y, L.z, 0.f);
+                                    slots |= 1u << 4;
+                                }
+                                float lpdf;
+                                lr = sampleEnvironment(s, rnd, L, lpdf);
+                                int el;
+                                bsdf = evaluateMaterialAndPDF(m, fr, V, L, rnd, mpdf, el);
+                                if (!isBlack(lr) && !isBlack(bsdf))
+                                {
+                                    v3 res = lr * misWeight(lpdf, mpdf) * bsdf / lpdf;
+                                    pslot[5] = make_float4(res.x, res.y, res.z, 0.f);
+                                    pdir[5]  = make_float4(L.x, L.y, L.z, 0.f);
+                                    slots |= 1u << 5;
+                                }
+                                mis = (slots & 0x30u) != 0;
+                            }
+                        }
+                        contrib *= m.opacity / (1.f - P);
+                        bool alpha = (flags & PF_ALPHA) != 0;
+                        alpha = !(!alpha && rayType == TRANSMISSION_LOBE);
+                        flags = alpha ? (flags | PF_ALPHA) : (flags & ~PF_ALPHA);
+                        // setupIndirectLightRay (ShadeFunctions.slang:263-310)
+                        int nextType;
+                        v3 nextContrib = splat(1.f);
+                        {
+                            v3 L;
+                            float pdf;
+                            int lobe;
+                            v3 bsdf = sampleMaterial(m, fr, V, random2D(rng), L, pdf, lobe);
+                            if (isBlack(bsdf))
+                                nextType = NO_SECONDARY_RAY;
+                            else
+                            {
+                                bool tr = lobe == TRANSMISSION_LOBE;
+                                nextO = (dot(V, fr.N) < 0.f || tr) ? sh.geomPosition : sh.position;
+                                nextD = L;
+                                nextContrib = bsdf / pdf;
+                                nextType = lobe;
+                            }
+                        }
+                        bool ended = nextType == NO_SECONDARY_RAY;
+                        uint32_t bits = slots;
+                        if (mis)
+                        {
+                            bits |= RS_MIS;
+                            flags = pfSetMisLobe(flags, uint32_t(misLobe));
+                        }
+                        if (bounce == 0)
+                        {
+                            bits |= RS_DEPTH0;
+                            if (pfMisLobe(flags) == DIFFUSE_LOBE)
+                                bits |= RS_DIFFUSE_ROUTE;
+                        }
+                        else if (rayType == DIFFUSE_LOBE)
+                            bits |= RS_DIFFUSE_ROUTE;
+                        wb.pendEmission[p]   = make_float4(emission.x, emission.y, emission.z, 0.f);
+                        wb.pendSegContrib[p] = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
+                        wb.pendBits[p]       = bits;
+                        wb.occluded[p]       = 0u;
+                        if (slots)
+                            wb.shOrg[p] = make_float4(so.x, so.y, so.z, 0.f);
+                        flags &= ~PF_PRIMARY;
+                        if (nextType == TRANSMISSION_LOBE)
+                            flags ^= PF_INSIDE;
+                        contrib *= nextContrib;
+                        if (f.is_russian_roulette_enabled && bounce + 1 >= f.russian_roulette_start_depth)
+                        {
+                            float mx   = fmaxf_(contrib.x, fmaxf_(contrib.y, contrib.z));
+                            float surv = clampf(mx, 0.05f, 1.f);
+                            if (random2D(rng).x > surv)
+                                ended = true;
+                            else
+                                contrib = contrib / surv;
+                        }
+                        flags    = pfSetRayType(flags, uint32_t(nextType));
+                        pushNext = !ended;
+                        resolve  = true;
+                    }
+                    wb.rng[p]     = make_uint2(rng.x, rng.y);
+                    wb.contrib[p] = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
+                    wb.flags[p]   = flags;
+                }
+            }
+        }
+        // Warp-aggregated queue appends (all lanes of the warp reach this point together).
+        __syncwarp();
+        uint32_t slotNext = warpAppend(wb.counters + (bounce + 1) * 4 + 0, pushNext);
+        if (pushNext)
+        {
+            wb.rayOrg[cur ^ 1][slotNext]  = make_float4(nextO.x, nextO.y, nextO.z, kRayTMin);
+            wb.rayDir[cur ^ 1][slotNext]  = make_float4(nextD.x, nextD.y, nextD.z, __int_as_float(0x7f800000));
+            wb.rayPath[cur ^ 1][slotNext] = p;
+        }
+        uint32_t slotRes = warpAppend(wb.counters + bounce * 4 + 2, resolve);
+        if (resolve)
+            wb.resolveList[slotRes] = p;
+        // Shadow rays: variable count per lane, warp prefix sum then one atomic.
+        uint32_t cnt = __popc(slots);
+        uint32_t incl = cnt;
+        int lane = threadIdx.x & 31;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1)
+        {
+            uint32_t v = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= off)
+                incl += v;
+        }
+        uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        uint32_t sbase = 0;
+        if (lane == 31 && total)
+            sbase = atomicAdd(wb.counters + bounce * 4 + 1, total);
+        sbase = __shfl_sync(0xffffffffu, sbase, 31);
+        uint32_t w = sbase + incl - cnt;
+        for (uint32_t k = 0; k < uint32_t(kMaxShadowSlots); k++)
+            if (slots & (1u << k))
+                wb.shTag[w++] = (p << 3) | k;
+    }
+}
+
+// Applies shadow visibility to the pending contributions and accumulates the segment.
+__global__ void k_resolve(agb_frame_data f, WaveBuffers wb, int bounce)
+{
+    uint32_t n      = wb.counters[bounce * 4 + 2];
+    uint32_t stride = gridDim.x * blockDim.x;
+    const float clampLum = f.indirect_bounce_clamp_scale > 0.f
+        ? f.max_luminance * f.indirect_bounce_clamp_scale
+        : 0.f;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        uint32_t p    = wb.resolveList[i];
+        uint32_t bits = wb.pendBits[p];
+        uint32_t occ  = wb.occluded[p];
+        float4 e      = wb.pendEmission[p];
+        v3 direct     = v3{ e.x, e.y, e.z };
+        const float4* ps = wb.pendSlot + size_t(p) * kMaxShadowSlots;
+        for (int k = 0; k < 4; k++)
+            if (bits & (1u << k))
+            {
+                float vis = (occ >> k) & 1u ? 0.f : 1.f;
+                float4 c  = ps[k];
+                direct += splat(vis) * v3{ c.x, c.y, c.z };
+            }
+        v3 indirect = splat(0.f);
+        if (bits & RS_MIS)
+        {
+            v3 misr = splat(0.f);
+            for (int k = 4; k < 6; k++)
+                if (bits & (1u << k))
+                {
+                    float vis = (occ >> k) & 1u ? 0.f : 1.f;
+                    float4 c  = ps[k];
+                    misr += splat(vis) * v3{ c.x, c.y, c.z };
+                }
+            indirect = misr;
+        }
+        float4 sc4 = wb.pendSegContrib[p];
+        v3 sc      = v3{ sc4.x, sc4.y, sc4.z };
+        direct *= sc;
+        indirect *= sc;
+        wb.lastIndirect[p] = make_float4(indirect.x, indirect.y, indirect.z, 0.f);
+        if (bits & RS_DEPTH0)
+        {
+            wb.outDirect[p] = make_float4(direct.x, direct.y, direct.z, 0.f);
+            float4 ind      = make_float4(indirect.x, indirect.y, indirect.z, 0.f);
+            if (bits & RS_DIFFUSE_ROUTE)
+                wb.outDiffuse[p] = ind;
+            else
+                wb.outGlossy[p] = ind;
+            continue;
+        }
+        v3 radiance = direct + indirect;
+        if (clampLum > 0.f)
+        {
+            float lum = luminance(radiance);
+            if (lum > clampLum)
+                radiance *= clampLum / lum;
+            if (isnan(radiance.x) || isnan(radiance.y) || isnan(radiance.z) || isinf(radiance.x) ||
+                isinf(radiance.y) || isinf(radiance.z))
+                radiance = splat(0.f);
+        }
+        float4* dst = (bits & RS_DIFFUSE_ROUTE) ? wb.outDiffuse + p : wb.outGlossy + p;
+        float4 a    = *dst;
+        *dst        = make_float4(a.x + radiance.x, a.y + radiance.y, a.z + radiance.z, 0.f);
+    }
+}
+
+// PathTracingCommon.slang:59-82
+__device__ __forceinline__ void adjustRadiance(float maxLum, bool displayErrors, v3& r)
+{
+    float lum = luminance(r);
+    if (lum > maxLum)
+        r *= maxLum / lum;
+    if (isnan(r.x) || isnan(r.y) || isnan(r.z))
+        r = displayErrors ? v3{ __int_as_float(0x7f800000), 0.f, 0.f } : splat(0.f);
+    else if (isinf(r.x) || isinf(r.y) || isinf(r.z))
+        r = displayErrors ? v3{ 0.f, __int_as_float(0x7f800000), 0.f } : splat(0.f);
+}
+
+// Per pixel: final radiance of each sample of the wave in sample order, then accumulation.
+__global__ void k_finalize(agb_frame_data f, WaveParams wp, WaveBuffers wb)
+{
+    uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < wp.pixels; pixel += stride)
+    {
+        float4 mean = make_float4(0.f, 0.f, 0.f, 0.f), sum = mean, comp = mean;
+        if ((wp.accumMode & AGB_ACCUM_RUNNING_MEAN) && wp.sampleBase > 0)
+            mean = wb.accumMean[pixel];
+        if ((wp.accumMode & AGB_ACCUM_KAHAN) && wp.sampleBase > 0)
+        {
+            sum  = wb.accumSum[pixel];
+            comp = wb.accumComp[pixel];
+        }
+        float4 res = mean;
+        for (uint32_t k = 0; k < wp.samples; k++)
+        {
+            uint32_t p = k * wp.pixels + pixel;
+            float4 a = wb.outDirect[p], b = wb.outDiffuse[p], c = wb.outGlossy[p];
+            v3 fin = (v3{ a.x, a.y, a.z } + v3{ b.x, b.y, b.z }) + v3{ c.x, c.y, c.z };
+            adjustRadiance(f.max_luminance, f.is_display_errors_enabled != 0, fin);
+            res = make_float4(fin.x, fin.y, fin.z, (wb.flags[p] & PF_ALPHA) ? 1.f : 0.f);
+            uint32_t s = wp.sampleBase + k;
+            if (wp.accumMode & AGB_ACCUM_RUNNING_MEAN)
+            {
+                if (s == 0)
+                    mean = res;
+                else
+                {
+                    float t  = __fdiv_rn(1.f, float(s + 1));
+                    float om = __fsub_rn(1.f, t);
+                    mean = make_float4(__fadd_rn(__fmul_rn(mean.x, om), __fmul_rn(res.x, t)),
+                        __fadd_rn(__fmul_rn(mean.y, om), __fmul_rn(res.y, t)),
+                        __fadd_rn(__fmul_rn(mean.z, om), __fmul_rn(res.z, t)),
+                        __fadd_rn(__fmul_rn(mean.w, om), __fmul_rn(res.w, t)));
+                }
+            }
+            if (wp.accumMode & AGB_ACCUM_KAHAN)
+            {
+                // Kahan-compensated sum: y = x - c; t = sum + y; c = (t - sum) - y; sum = t.
+                float* sp = &sum.x;
+                float* cp = &comp.x;
+                const float* xp = &res.x;
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                {
+                    float y  = __fsub_rn(xp[q], cp[q]);
+                    float tt = __fadd_rn(sp[q], y);
+                    cp[q]    = __fsub_rn(__fsub_rn(tt, sp[q]), y);
+                    sp[q]    = tt;
+                }
+            }
+        }
+        if (wp.accumMode & AGB_ACCUM_RUNNING_MEAN)
+            wb.accumMean[pixel] = mean;
+        if (wp.accumMode & AGB_ACCUM_KAHAN)
+        {
+            wb.accumSum[pixel]  = sum;
+            wb.accumComp[pixel] = comp;
+        }
+        if (wb.lastSample)
+            wb.lastSample[pixel] = res;
+    }
+}
+
+// ------------------------------------------------------------------------------ launchers
+void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp,
+    const WaveBuffers& wb, cudaStream_t st, int smCount, uint64_t& launches, KernelMarks* marks)
+{
+    auto mark = [&](int category) {
+        if (marks)
+            marks->record(category, st);
+    };
+    int grid = smCount * 8;
+    int traceGrid = smCount * kTraceBlocksPerSM;
+    mark(KC_CAMERA);
+    k_camera<<<grid, 256, 0, st>>>(f, wp, wb);
+    launches++;
+    int cur = 0;
+    int depth = f.trace_depth;
+    size_t stackBytes = size_t(kStackSize) * kTraceBlock * sizeof(int32_t);
+    for (int b = 0; b <= depth; b++)
+    {
+        if (b == depth)
+        {
+            mark(KC_SHADE);
+            k_shade<<<grid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 1);
+            launches++;
+            break;
+        }
+        mark(KC_CLOSEST);
+        if (wp.countTraversal)
+            k_trace_closest<true><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, cur);
+        else
+            k_trace_closest<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, cur);
+        mark(KC_SHADE);
+        k_shade<<<grid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 0);
+        mark(KC_SHADOW);
+        if (wp.countTraversal)
+            k_trace_shadow<true><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b);
+        else
+            k_trace_shadow<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b);
+        mark(KC_RESOLVE);
+        k_resolve<<<grid, 256, 0, st>>>(f, wb, b);
+        launches += 4;
+        cur ^= 1;
+    }
+    mark(KC_FINALIZE);
+    k_finalize<<<grid, 256, 0, st>>>(f, wp, wb);
+    launches++;
+    mark(KC_END);
+}
+
+void setTraceAttributes()
+{
+    size_t stackBytes = size_t(kStackSize) * kTraceBlock * sizeof(int32_t);
+    cudaFuncSetAttribute(k_trace_closest<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(stackBytes));
+    cudaFuncSetAttribute(k_trace_closest<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(stackBytes));
+    cudaFuncSetAttribute(k_trace_shadow<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(stackBytes));
+    cudaFuncSetAttribute(k_trace_shadow<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(stackBytes));
+}
+
+} // namespace agb

@@ -1,0 +1,365 @@
+// Device-resident scene layout and the per-hit shading code that reads it:
+//   images / texture sampling  (Texture2D.SampleLevel with repeat addressing),
+//   environment evaluation and alias-table sampling (Shaders/Environment.slang:35-186),
+//   computeShadingData (Shaders/Geometry.slang:131-265),
+//   evaluateDefaultMaterial (Shaders/DefaultMaterial.slang:88-239).
+#pragma once
+
+#include "../../include/agb.h"
+#include "agb_bsdf.cuh"
+
+namespace agb
+{
+
+// ------------------------------------------------------------------------------ HBM layout
+// BVH2 node, 64 bytes = four 128-bit loads.  Child refs: >= 0 interior node index; < 0 leaf with
+// ~ref = (first << 3) | (count - 1), count <= 8 primitives.
+struct __align__(16) BNode
+{
+    float4 c0xy; // child 0: lo.x hi.x lo.y hi.y
+    float4 c1xy; // child 1: lo.x hi.x lo.y hi.y
+    float4 cz;   // child 0 lo.z hi.z, child 1 lo.z hi.z
+    int4 ref;    // child 0 ref, child 1 ref, unused, unused
+};
+static_assert(sizeof(BNode) == 64, "BNode is 64 bytes");
+
+AGB_HD int32_t leafRef(uint32_t first, uint32_t count) { return ~int32_t((first << 3) | (count - 1)); }
+
+struct DevImage
+{
+    const void* data; // RGBA8 or RGBA32F texels, rows top to bottom
+    uint32_t width, height;
+    int32_t format;   // AGB_FORMAT_RGBA8_UNORM or AGB_FORMAT_RGBA32F
+    int32_t linear;
+};
+
+struct DevMesh
+{
+    const float* positions; // 3 per vertex
+    const float* normals;   // 3 per vertex or null
+    const float* texcoords; // 2 per vertex or null
+    const uint32_t* indices; // 3 per triangle
+    const float4* tris;     // 3 per triangle in BVH leaf order: v0 (w = triangle id as int), v1, v2
+    const BNode* nodes;
+    uint32_t vertexCount, triangleCount;
+    int32_t root;           // root ref
+    int32_t depth;
+};
+
+struct DevLayer
+{
+    int32_t material;
+    int32_t _pad;
+    const float* texcoords; // 2 per base-mesh vertex
+};
+
+struct DevInstance
+{
+    float o2w[12];
+    float w2o[12];
+    int32_t mesh;
+    int32_t material;
+    int32_t layerCount;
+    int32_t layerOffset; // into DevScene::layers
+};
+
+struct DevScene
+{
+    const DevMesh* meshes;
+    const DevInstance* instances;
+    const BNode* tlas;
+    int32_t tlasRoot;
+    int32_t instanceCount;
+    const int32_t* tlasOrder; // instance index per TLAS leaf slot
+    const agb_material* materials;
+    const agb_material_textures* matTex; // may be null
+    int32_t materialCount;
+    int32_t imageCount;
+    const DevImage* images;
+    const DevLayer* layers;
+    // Environment.
+    agb_environment_data env;
+    DevImage envLight;        // data null when absent
+    DevImage envBackground;   // data null when absent
+    const agb_alias_entry* alias;
+};
+
+// -------------------------------------------------------------------------- texture sampling
+AGB_D float4 texel(const DevImage& im, int x, int y)
+{
+    int w = int(im.width), h = int(im.height);
+    x     = x % w;
+    x     = x < 0 ? x + w : x;
+    y     = y % h;
+    y     = y < 0 ? y + h : y;
+    size_t i = size_t(y) * size_t(w) + size_t(x);
+    if (im.format == AGB_FORMAT_RGBA8_UNORM)
+    {
+        uchar4 c = __ldg(static_cast<const uchar4*>(im.data) + i);
+        return make_float4(float(c.x) / 255.f, float(c.y) / 255.f, float(c.z) / 255.f,
+            float(c.w) / 255.f);
+    }
+    return __ldg(static_cast<const float4*>(im.data) + i);
+}
+AGB_D float4 lerp4(float4 a, float4 b, float t)
+{
+    return make_float4(a.x + t * (b.x - a.x), a.y + t * (b.y - a.y), a.z + t * (b.z - a.z),
+        a.w + t * (b.w - a.w));
+}
+// SampleLevel(uv, 0) with repeat addressing; texel centres at (i + 0.5) / size.
+AGB_D float4 sampleImage(const DevImage& im, v2 uv)
+{
+    float fw = float(im.width), fh = float(im.height);
+    if (!im.linear)
+        return texel(im, int(floorf(uv.x * fw)), int(floorf(uv.y * fh)));
+    float x  = uv.x * fw - 0.5f;
+    float y  = uv.y * fh - 0.5f;
+    float x0 = floorf(x), y0 = floorf(y);
+    float fx = x - x0, fy = y - y0;
+    int ix = int(x0), iy = int(y0);
+    float4 a = lerp4(texel(im, ix, iy), texel(im, ix + 1, iy), fx);
+    float4 b = lerp4(texel(im, ix, iy + 1), texel(im, ix + 1, iy + 1), fx);
+    return lerp4(a, b, fy);
+}
+
+// --------------------------------------------------------------------------- environment
+AGB_D v2 dirToLatLong(v3 d)
+{
+    return v2{ ((atan2f(d.x, -d.z) * 1.0f) / kPi) * 0.5f + 0.5f,
+        ((-asinf(d.y)) * 1.0f) / kPi + 0.5f };
+}
+AGB_D v3 latLongToDir(v2 uv)
+{
+    float phi   = (uv.x + 0.25f) * 2.f * kPi;
+    float theta = uv.y * kPi;
+    float sp, cp, st, ct;
+    sincosf(phi, &sp, &cp);
+    sincosf(theta, &st, &ct);
+    return v3{ cp * st, ct, sp * st };
+}
+AGB_D v3 mulDir(const float* m, v3 d)
+{
+    return v3{ m[0] * d.x + m[1] * d.y + m[2] * d.z + m[3] * 0.f,
+        m[4] * d.x + m[5] * d.y + m[6] * d.z + m[7] * 0.f,
+        m[8] * d.x + m[9] * d.y + m[10] * d.z + m[11] * 0.f };
+}
+// Environment.slang:98-133.  pixel / screen are used only with background_use_screen.
+AGB_D v3 evaluateEnvironment(const DevScene& s, v3 dir, bool asBackground, v2 pixel, v2 screen)
+{
+    const agb_environment_data& c = s.env;
+    if (asBackground)
+    {
+        v2 uv = c.background_use_screen ? v2{ pixel.x / screen.x, pixel.y / screen.y }
+                                        : dirToLatLong(normalize(mulDir(c.background_transform, dir)));
+        if (c.has_background_tex && s.envBackground.data)
+        {
+            float4 t = sampleImage(s.envBackground, uv);
+            return v3{ t.x, t.y, t.z };
+        }
+        return lerp3(ld3(c.background_top), ld3(c.background_bottom), uv.y);
+    }
+    v2 uv = dirToLatLong(normalize(mulDir(c.light_transform, dir)));
+    if (c.has_light_tex && s.envLight.data)
+    {
+        float4 t = sampleImage(s.envLight, uv);
+        return v3{ t.x, t.y, t.z };
+    }
+    return lerp3(ld3(c.light_top), ld3(c.light_bottom), uv.y);
+}
+// Environment.slang:137-186
+AGB_D v3 sampleEnvironment(const DevScene& s, v2 r, v3& L, float& pdf)
+{
+    const agb_environment_data& c = s.env;
+    if (c.has_light_tex && s.envLight.data)
+    {
+        uint32_t w = s.envLight.width, h = s.envLight.height, count = w * h;
+        uint32_t index = uint32_t(float(count) * r.x);
+        index          = index < count - 1 ? index : count - 1;
+        float4 e       = __ldg(reinterpret_cast<const float4*>(s.alias) + index);
+        if (e.y < r.y)
+        {
+            index = __float_as_uint(e.x);
+            e     = __ldg(reinterpret_cast<const float4*>(s.alias) + index);
+        }
+        pdf        = e.z;
+        uint32_t x = index % w, y = index / w;
+        L = latLongToDir(v2{ (float(x) + 0.5f) / float(w), (float(y) + 0.5f) / float(h) });
+        L = normalize(mulDir(c.light_transform_inv, L));
+        float4 t = texel(s.envLight, int(x), int(y));
+        return v3{ t.x, t.y, t.z };
+    }
+    L     = sampleUniformDirection(r, pdf);
+    L     = normalize(mulDir(c.light_transform_inv, L));
+    v2 uv = dirToLatLong(L);
+    return lerp3(ld3(c.light_top), ld3(c.light_bottom), uv.y);
+}
+
+// ------------------------------------------------------------------------------ shading data
+struct Shading
+{
+    v3 N, X, Y;         // world normal, tangent, bitangent
+    v3 position;        // shadow-terminator shading position (world)
+    v3 geomPosition;    // geometric hit position (world)
+    v2 uv;
+    uint32_t idx[3];
+    v3 bary;
+};
+
+AGB_D v3 xfPoint(const float* m, v3 p)
+{
+    return v3{ m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3],
+        m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7],
+        m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11] };
+}
+AGB_D v3 xfVector(const float* m, v3 v)
+{
+    return v3{ m[0] * v.x + m[1] * v.y + m[2] * v.z, m[4] * v.x + m[5] * v.y + m[6] * v.z,
+        m[8] * v.x + m[9] * v.y + m[10] * v.z };
+}
+AGB_D v3 ldg3(const float* p) { return v3{ __ldg(p), __ldg(p + 1), __ldg(p + 2) }; }
+AGB_D v3 projectOnPlane(v3 p, v3 o, v3 n) { return p - n * dot(p - o, n); }
+
+// Geometry.slang:152-265, tangent from the up vector (HGI reports no tangents).
+AGB_D Shading computeShading(const DevScene& s, const DevInstance& in, uint32_t tri, float u, float v)
+{
+    const DevMesh& m = s.meshes[in.mesh];
+    Shading sh;
+    sh.bary = v3{ 1.f - u - v, u, v };
+    uint3 id = make_uint3(__ldg(m.indices + 3 * size_t(tri)), __ldg(m.indices + 3 * size_t(tri) + 1),
+        __ldg(m.indices + 3 * size_t(tri) + 2));
+    sh.idx[0] = id.x;
+    sh.idx[1] = id.y;
+    sh.idx[2] = id.z;
+    v3 p[3], nn[3];
+    v3 gp = splat(0.f), n = splat(0.f);
+    v2 uv = v2{ 0.f, 0.f };
+    float b[3] = { sh.bary.x, sh.bary.y, sh.bary.z };
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+    {
+        p[i] = ldg3(m.positions + 3 * size_t(sh.idx[i]));
+        gp += p[i] * b[i];
+        if (m.normals)
+        {
+            nn[i] = ldg3(m.normals + 3 * size_t(sh.idx[i]));
+            n += nn[i] * b[i];
+        }
+        if (m.texcoords)
+        {
+            v2 t = v2{ __ldg(m.texcoords + 2 * size_t(sh.idx[i])),
+                __ldg(m.texcoords + 2 * size_t(sh.idx[i]) + 1) };
+            uv = uv + t * b[i];
+        }
+    }
+    v3 on = normalize(m.normals ? n : cross(p[1] - p[0], p[2] - p[0]));
+    v3 op = gp;
+    if (m.normals)
+    {
+        v3 sp = projectOnPlane(gp, p[0], nn[0]) * b[0] + projectOnPlane(gp, p[1], nn[1]) * b[1] +
+            projectOnPlane(gp, p[2], nn[2]) * b[2];
+        op = dot(sp - gp, n) > 0.f ? sp : gp;
+    }
+    sh.position     = xfPoint(in.o2w, op);
+    sh.geomPosition = xfPoint(in.o2w, gp);
+    sh.N            = normalize(xfVector(in.o2w, on));
+    v3 up           = fabsf(sh.N.y) < 0.999f ? v3{ 0.f, 1.f, 0.f } : v3{ 1.f, 0.f, 0.f };
+    sh.X            = normalize(cross(sh.N, up));
+    sh.Y            = cross(sh.N, sh.X);
+    sh.uv           = uv;
+    return sh;
+}
+
+// DefaultMaterial.slang:88-105
+AGB_D v2 uvTransform(v2 uv, const float* pivot, const float* scale, float rotate, const float* offset)
+{
+    v2 sub = v2{ uv.x - pivot[0], uv.y - pivot[1] };
+    v2 sc  = v2{ sub.x / scale[0], sub.y / scale[1] };
+    float r = rotate * (kPi / 180.f);
+    float sa, ca;
+    sincosf(r, &sa, &ca);
+    v2 rot = v2{ ca * sc.x + sa * sc.y, -sa * sc.x + ca * sc.y };
+    return v2{ (rot.x - offset[0]) + pivot[0], (rot.y - offset[1]) + pivot[1] };
+}
+
+AGB_D bool materialTexture(const DevScene& s, int32_t mat, int slot, v2 uv, const float* pivot,
+    const float* scale, float rotation, const float* offset, v3& rgb)
+{
+    if (!s.matTex)
+        return false;
+    int32_t img = s.matTex[mat].image[slot];
+    if (img < 0 || img >= s.imageCount)
+        return false;
+    float4 t = sampleImage(s.images[img], uvTransform(uv, pivot, scale, rotation, offset));
+    rgb      = v3{ t.x, t.y, t.z };
+    return true;
+}
+
+// DefaultMaterial.slang:130-239
+AGB_D Mat loadMaterial(const DevScene& s, int32_t mi, const Shading& sh, v3& materialNormal,
+    bool& generatedNormal)
+{
+    const agb_material& b = s.materials[mi];
+    Mat m;
+    m.base               = b.base;
+    m.baseColor          = ld3(b.base_color);
+    m.diffuseRoughness   = b.diffuse_roughness;
+    m.metalness          = b.metalness;
+    m.specular           = b.specular;
+    m.specularColor      = ld3(b.specular_color);
+    m.specularRoughness  = b.specular_roughness;
+    m.specularIOR        = b.specular_IOR;
+    m.specularAnisotropy = b.specular_anisotropy;
+    m.specularRotation   = b.specular_rotation;
+    m.transmission       = b.transmission;
+    m.transmissionColor  = ld3(b.transmission_color);
+    m.subsurface         = b.subsurface;
+    m.subsurfaceColor    = ld3(b.subsurface_color);
+    m.sheen              = b.sheen;
+    m.sheenColor         = ld3(b.sheen_color);
+    m.sheenRoughness     = b.sheen_roughness;
+    m.coat               = b.coat;
+    m.coatColor          = ld3(b.coat_color);
+    m.coatRoughness      = b.coat_roughness;
+    m.coatAnisotropy     = b.coat_anisotropy;
+    m.coatRotation       = b.coat_rotation;
+    m.coatIOR            = b.coat_IOR;
+    m.coatAffectColor    = b.coat_affect_color;
+    m.coatAffectRoughness = b.coat_affect_roughness;
+    m.emission           = b.emission;
+    m.emissionColor      = ld3(b.emission_color);
+    m.opacity            = ld3(b.opacity);
+    m.thinWalled         = b.thin_walled != 0;
+    v3 rgb;
+    if (b.has_base_color_image &&
+        materialTexture(s, mi, AGB_TEX_BASE_COLOR, sh.uv, b.base_color_image_pivot,
+            b.base_color_image_scale, b.base_color_image_rotation, b.base_color_image_offset, rgb))
+        m.baseColor = rgb;
+    if (b.has_specular_roughness_image &&
+        materialTexture(s, mi, AGB_TEX_SPECULAR_ROUGHNESS, sh.uv, b.specular_roughness_image_pivot,
+            b.specular_roughness_image_scale, b.specular_roughness_image_rotation,
+            b.specular_roughness_image_offset, rgb))
+        m.specularRoughness = rgb.x;
+    if (b.has_emission_color_image &&
+        materialTexture(s, mi, AGB_TEX_EMISSION, sh.uv, b.emission_color_image_pivot,
+            b.emission_color_image_scale, b.emission_color_image_rotation,
+            b.emission_color_image_offset, rgb))
+        m.emissionColor = rgb;
+    if (b.has_opacity_image &&
+        materialTexture(s, mi, AGB_TEX_OPACITY, sh.uv, b.opacity_image_pivot, b.opacity_image_scale,
+            b.opacity_image_rotation, b.opacity_image_offset, rgb))
+        m.opacity = rgb;
+    generatedNormal = false;
+    if (b.has_normal_image &&
+        materialTexture(s, mi, AGB_TEX_NORMAL, sh.uv, b.normal_image_pivot, b.normal_image_scale,
+            b.normal_image_rotation, b.normal_image_offset, rgb))
+    {
+        v3 vv  = rgb * 2.f - splat(1.f);
+        v3 Bn  = normalize(cross(sh.N, sh.X));
+        materialNormal  = normalize(sh.X * vv.x * 1.f + Bn * vv.y * 1.f + sh.N * vv.z);
+        generatedNormal = true;
+    }
+    m.metalColor = m.baseColor;
+    return m;
+}
+
+} // namespace agb

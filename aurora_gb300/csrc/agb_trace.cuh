@@ -1,0 +1,312 @@
+// Ray casting on the device: two-level BVH2 traversal (TLAS over instances, BLAS per mesh) with
+// the traversal stack in shared memory, 128-bit node and triangle fetches, and the watertight
+// ray/triangle test of Woop, Benthin and Wald (JCGT 2(1), 2013).
+//
+// This replaces the driver's hardware traversal behind TraceRay (Shaders/RayTrace.slang:185-270):
+//   closest hit:  RAY_FLAG_FORCE_OPAQUE, tmin <= t < tmax, barycentrics (u, v) = weights of
+//                 vertices 1 and 2 (Shaders/Geometry.slang:108-118);
+//   shadow rays:  RAY_FLAG_ACCEPT_FIRST_HIT_AND_END_SEARCH | FORCE_OPAQUE, any hit ends the search.
+//
+// The triangle test uses explicit round-to-nearest intrinsics so that no multiply-add is
+// contracted: the edge functions of two triangles sharing an edge are then computed from the same
+// operands in the same order, which is what makes the test watertight.  Box tests are widened by
+// a few ulp so they never reject a hit the triangle test accepts.
+#pragma once
+
+#include "agb_scene.cuh"
+
+namespace agb
+{
+
+constexpr int kStackSize = 48; // entries per thread; the BVH builder keeps TLAS + BLAS depth below
+
+struct TraceCounters
+{
+    unsigned long long nodes;
+    unsigned long long tris;
+};
+
+struct RayHit
+{
+    float t, u, v;
+    int32_t inst, prim;
+};
+
+AGB_D float sel3(v3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+// Per-ray constants of the watertight test.
+struct WtRay
+{
+    v3 o;
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+};
+AGB_D WtRay wtSetup(v3 o, v3 d)
+{
+    WtRay r;
+    r.o      = o;
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    r.kz     = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    r.kx     = r.kz + 1 == 3 ? 0 : r.kz + 1;
+    r.ky     = r.kx + 1 == 3 ? 0 : r.kx + 1;
+    float dz = sel3(d, r.kz);
+    if (dz < 0.f)
+    {
+        int t = r.kx;
+        r.kx  = r.ky;
+        r.ky  = t;
+    }
+    r.Sx = __fdiv_rn(sel3(d, r.kx), dz);
+    r.Sy = __fdiv_rn(sel3(d, r.ky), dz);
+    r.Sz = __fdiv_rn(1.f, dz);
+    return r;
+}
+
+// Watertight test; accepts tmin <= t < tmax.
+AGB_D bool wtIntersect(const WtRay& r, float4 a4, float4 b4, float4 c4, float tmin, float tmax,
+    float& t, float& u, float& v)
+{
+    v3 A = v3{ __fsub_rn(a4.x, r.o.x), __fsub_rn(a4.y, r.o.y), __fsub_rn(a4.z, r.o.z) };
+    v3 B = v3{ __fsub_rn(b4.x, r.o.x), __fsub_rn(b4.y, r.o.y), __fsub_rn(b4.z, r.o.z) };
+    v3 C = v3{ __fsub_rn(c4.x, r.o.x), __fsub_rn(c4.y, r.o.y), __fsub_rn(c4.z, r.o.z) };
+    float Akz = sel3(A, r.kz), Bkz = sel3(B, r.kz), Ckz = sel3(C, r.kz);
+    float Ax = __fsub_rn(sel3(A, r.kx), __fmul_rn(r.Sx, Akz));
+    float Ay = __fsub_rn(sel3(A, r.ky), __fmul_rn(r.Sy, Akz));
+    float Bx = __fsub_rn(sel3(B, r.kx), __fmul_rn(r.Sx, Bkz));
+    float By = __fsub_rn(sel3(B, r.ky), __fmul_rn(r.Sy, Bkz));
+    float Cx = __fsub_rn(sel3(C, r.kx), __fmul_rn(r.Sx, Ckz));
+    float Cy = __fsub_rn(sel3(C, r.ky), __fmul_rn(r.Sy, Ckz));
+    float U  = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V  = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W  = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (U == 0.f || V == 0.f || W == 0.f)
+    {
+        // Edge functions that round to zero are re-evaluated in double (paper, section 3.4).
+        U = float(__dsub_rn(__dmul_rn(double(Cx), double(By)), __dmul_rn(double(Cy), double(Bx))));
+        V = float(__dsub_rn(__dmul_rn(double(Ax), double(Cy)), __dmul_rn(double(Ay), double(Cx))));
+        W = float(__dsub_rn(__dmul_rn(double(Bx), double(Ay)), __dmul_rn(double(By), double(Ax))));
+    }
+    if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f))
+        return false;
+    float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.f)
+        return false;
+    float Az = __fmul_rn(r.Sz, Akz), Bz = __fmul_rn(r.Sz, Bkz), Cz = __fmul_rn(r.Sz, Ckz);
+    float Tn  = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
+    float rcp = __fdiv_rn(1.f, det);
+    float tt  = __fmul_rn(Tn, rcp);
+    if (!(tt >= tmin && tt < tmax))
+        return false;
+    t = tt;
+    u = __fmul_rn(V, rcp);
+    v = __fmul_rn(W, rcp);
+    return true;
+}
+
+// Affine transform of a ray into object space, unrounded-contraction-free so that host and device
+// agree: ((m0 x + m1 y) + m2 z) + m3.
+AGB_D v3 xfPointRn(const float* m, v3 p)
+{
+    return v3{ __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[0], p.x), __fmul_rn(m[1], p.y)),
+                             __fmul_rn(m[2], p.z)), m[3]),
+        __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[4], p.x), __fmul_rn(m[5], p.y)),
+                      __fmul_rn(m[6], p.z)), m[7]),
+        __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[8], p.x), __fmul_rn(m[9], p.y)),
+                      __fmul_rn(m[10], p.z)), m[11]) };
+}
+AGB_D v3 xfVectorRn(const float* m, v3 v)
+{
+    return v3{ __fadd_rn(__fadd_rn(__fmul_rn(m[0], v.x), __fmul_rn(m[1], v.y)), __fmul_rn(m[2], v.z)),
+        __fadd_rn(__fadd_rn(__fmul_rn(m[4], v.x), __fmul_rn(m[5], v.y)), __fmul_rn(m[6], v.z)),
+        __fadd_rn(__fadd_rn(__fmul_rn(m[8], v.x), __fmul_rn(m[9], v.y)), __fmul_rn(m[10], v.z)) };
+}
+
+struct SlabRay
+{
+    v3 inv;  // 1 / direction (tiny components clamped)
+    v3 oinv; // origin * inv
+};
+AGB_D SlabRay slabSetup(v3 o, v3 d)
+{
+    const float eps = 1e-20f;
+    float dx = fabsf(d.x) > eps ? d.x : copysignf(eps, d.x);
+    float dy = fabsf(d.y) > eps ? d.y : copysignf(eps, d.y);
+    float dz = fabsf(d.z) > eps ? d.z : copysignf(eps, d.z);
+    SlabRay s;
+    s.inv  = v3{ 1.f / dx, 1.f / dy, 1.f / dz };
+    s.oinv = v3{ o.x * s.inv.x, o.y * s.inv.y, o.z * s.inv.z };
+    return s;
+}
+// Two child boxes of a node against [tmin, tmax]; returns entry distances.
+AGB_D void slab2(const SlabRay& s, float4 c0xy, float4 c1xy, float4 cz, float tmin, float tmax,
+    bool& h0, bool& h1, float& t0, float& t1)
+{
+    // Box planes at lo/hi per axis, entry/exit distances with one FMA each.
+    float a0 = fmaf(c0xy.x, s.inv.x, -s.oinv.x), b0 = fmaf(c0xy.y, s.inv.x, -s.oinv.x);
+    float a1 = fmaf(c0xy.z, s.inv.y, -s.oinv.y), b1 = fmaf(c0xy.w, s.inv.y, -s.oinv.y);
+    float a2 = fmaf(cz.x, s.inv.z, -s.oinv.z), b2 = fmaf(cz.y, s.inv.z, -s.oinv.z);
+    float n0 = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), tmin));
+    float f0 = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tmax));
+    float c0 = fmaf(c1xy.x, s.inv.x, -s.oinv.x), d0 = fmaf(c1xy.y, s.inv.x, -s.oinv.x);
+    float c1 = fmaf(c1xy.z, s.inv.y, -s.oinv.y), d1 = fmaf(c1xy.w, s.inv.y, -s.oinv.y);
+    float c2 = fmaf(cz.z, s.inv.z, -s.oinv.z), d2 = fmaf(cz.w, s.inv.z, -s.oinv.z);
+    float n1 = fmaxf(fmaxf(fminf(c0, d0), fminf(c1, d1)), fmaxf(fminf(c2, d2), tmin));
+    float f1 = fminf(fminf(fmaxf(c0, d0), fmaxf(c1, d1)), fminf(fmaxf(c2, d2), tmax));
+    // Conservative widening (about 8 ulp relative plus an absolute floor).
+    const float kWiden = 1.0000010f;
+    h0 = n0 * (n0 > 0.f ? 1.f / kWiden : kWiden) <= f0 * (f0 > 0.f ? kWiden : 1.f / kWiden) + 1e-30f;
+    h1 = n1 * (n1 > 0.f ? 1.f / kWiden : kWiden) <= f1 * (f1 > 0.f ? kWiden : 1.f / kWiden) + 1e-30f;
+    t0 = n0;
+    t1 = n1;
+}
+
+// Traverses one instance's BLAS with the object-space ray; the stack region above `base` is used.
+// closest: updates hit/tmax; anyHit: returns true at the first hit.
+template <bool kAnyHit, bool kCount>
+AGB_D bool traverseBLAS(const DevMesh& m, int32_t inst, v3 oo, v3 od, float tmin, float& tmax,
+    RayHit& hit, int32_t* stack, int base, int stride, TraceCounters& cnt, bool& overflow)
+{
+    WtRay wr   = wtSetup(oo, od);
+    SlabRay sr = slabSetup(oo, od);
+    int sp     = base;
+    int32_t ref = m.root;
+    bool found = false;
+    for (;;)
+    {
+        if (ref >= 0)
+        {
+            const float4* np = reinterpret_cast<const float4*>(m.nodes + ref);
+            float4 c0xy = __ldg(np), c1xy = __ldg(np + 1), cz = __ldg(np + 2);
+            int4 refs   = __ldg(reinterpret_cast<const int4*>(np + 3));
+            if (kCount)
+                cnt.nodes++;
+            bool h0, h1;
+            float t0, t1;
+            slab2(sr, c0xy, c1xy, cz, tmin, tmax, h0, h1, t0, t1);
+            if (h0 && h1)
+            {
+                int32_t nearRef = t0 <= t1 ? refs.x : refs.y;
+                int32_t farRef  = t0 <= t1 ? refs.y : refs.x;
+                if (sp >= kStackSize - 1)
+                {
+                    overflow = true;
+                    return found;
+                }
+                stack[sp * stride] = farRef;
+                sp++;
+                ref = nearRef;
+                continue;
+            }
+            if (h0 || h1)
+            {
+                ref = h0 ? refs.x : refs.y;
+                continue;
+            }
+        }
+        else
+        {
+            uint32_t code  = uint32_t(~ref);
+            uint32_t first = code >> 3, count = (code & 7u) + 1u;
+            for (uint32_t k = 0; k < count; k++)
+            {
+                const float4* tp = m.tris + 3 * size_t(first + k);
+                float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                if (kCount)
+                    cnt.tris++;
+                float t, u, v;
+                if (wtIntersect(wr, a, b, c, tmin, tmax, t, u, v))
+                {
+                    found    = true;
+                    tmax     = t;
+                    hit.t    = t;
+                    hit.u    = u;
+                    hit.v    = v;
+                    hit.inst = inst;
+                    hit.prim = __float_as_int(a.w);
+                    if (kAnyHit)
+                        return true;
+                }
+            }
+        }
+        if (sp == base)
+            break;
+        sp--;
+        ref = stack[sp * stride];
+    }
+    return found;
+}
+
+// Full two-level cast of a world-space ray.  stack: this thread's column of the block's
+// shared-memory stack (entry i at stack[i * stride]).
+template <bool kAnyHit, bool kCount>
+AGB_D bool castRay(const DevScene& s, v3 o, v3 d, float tmin, float tmax, RayHit& hit,
+    int32_t* stack, int stride, TraceCounters& cnt, bool& overflow)
+{
+    hit.t = -1.f;
+    hit.inst = hit.prim = -1;
+    if (s.instanceCount <= 0)
+        return false;
+    SlabRay sr = slabSetup(o, d);
+    int sp     = 0;
+    int32_t ref = s.tlasRoot;
+    bool found = false;
+    for (;;)
+    {
+        if (ref >= 0)
+        {
+            const float4* np = reinterpret_cast<const float4*>(s.tlas + ref);
+            float4 c0xy = __ldg(np), c1xy = __ldg(np + 1), cz = __ldg(np + 2);
+            int4 refs   = __ldg(reinterpret_cast<const int4*>(np + 3));
+            if (kCount)
+                cnt.nodes++;
+            bool h0, h1;
+            float t0, t1;
+            slab2(sr, c0xy, c1xy, cz, tmin, tmax, h0, h1, t0, t1);
+            if (h0 && h1)
+            {
+                if (sp >= kStackSize - 1)
+                {
+                    overflow = true;
+                    return found;
+                }
+                stack[sp * stride] = t0 <= t1 ? refs.y : refs.x;
+                sp++;
+                ref = t0 <= t1 ? refs.x : refs.y;
+                continue;
+            }
+            if (h0 || h1)
+            {
+                ref = h0 ? refs.x : refs.y;
+                continue;
+            }
+        }
+        else
+        {
+            uint32_t code  = uint32_t(~ref);
+            uint32_t first = code >> 3, count = (code & 7u) + 1u;
+            for (uint32_t k = 0; k < count; k++)
+            {
+                int32_t ii = __ldg(s.tlasOrder + first + k);
+                const DevInstance& in = s.instances[ii];
+                v3 oo = xfPointRn(in.w2o, o);
+                v3 od = xfVectorRn(in.w2o, d);
+                if (traverseBLAS<kAnyHit, kCount>(s.meshes[in.mesh], ii, oo, od, tmin, tmax, hit,
+                        stack, sp, stride, cnt, overflow))
+                {
+                    found = true;
+                    if (kAnyHit)
+                        return true;
+                }
+                if (overflow)
+                    return found;
+            }
+        }
+        if (sp == 0)
+            break;
+        sp--;
+        ref = stack[sp * stride];
+    }
+    return found;
+}
+
+} // namespace agb

@@ -1,0 +1,87 @@
+// Wavefront path-tracer state: the per-path and per-queue arrays that live in HBM between the
+// kernels of one wave.  A wave holds `samples` consecutive sample indices for every pixel; path
+// p covers pixel p % pixels and sample sampleBase + p / pixels.
+#pragma once
+
+#include "agb_trace.cuh"
+
+namespace agb
+{
+
+constexpr int kMaxShadowSlots = 6; // up to 4 distant lights + 2 environment-MIS rays per hit
+
+// Path flag bits (mirrors the reference payload bit fields, RayTrace.slang:52-126).
+enum : uint32_t
+{
+    PF_PRIMARY      = 1u << 0,
+    PF_ALPHA        = 1u << 1,  // outputAlpha == 1
+    PF_INSIDE       = 1u << 2,
+    PF_RAYTYPE_SHIFT = 3,       // 5 bits: ray type of the segment being traced
+    PF_MISLOBE_SHIFT = 8,       // 5 bits: misLobeID
+};
+AGB_HD uint32_t pfRayType(uint32_t f) { return (f >> PF_RAYTYPE_SHIFT) & 31u; }
+AGB_HD uint32_t pfMisLobe(uint32_t f) { return (f >> PF_MISLOBE_SHIFT) & 31u; }
+AGB_HD uint32_t pfSetRayType(uint32_t f, uint32_t t)
+{
+    return (f & ~(31u << PF_RAYTYPE_SHIFT)) | (t << PF_RAYTYPE_SHIFT);
+}
+AGB_HD uint32_t pfSetMisLobe(uint32_t f, uint32_t t)
+{
+    return (f & ~(31u << PF_MISLOBE_SHIFT)) | (t << PF_MISLOBE_SHIFT);
+}
+
+// Pending-resolve record bits: which shadow slots carry a contribution and how the segment's
+// radiance is routed (RayGen accumulation, MainEntryPoints.slang:160-243).
+enum : uint32_t
+{
+    RS_SLOT_MASK      = 0x3Fu,   // bit k: slot k holds a contribution
+    RS_MIS            = 1u << 6, // MIS emitted shadow rays (indirect = mis result)
+    RS_DEPTH0         = 1u << 7, // accumulated as the rayDepth == 0 segment
+    RS_DIFFUSE_ROUTE  = 1u << 8, // depth 0: misLobeID == DIFFUSE; depth > 0: rayType == DIFFUSE
+};
+
+struct WaveBuffers
+{
+    // Per path.
+    uint2* rng;
+    float4* contrib;     // rayContribution (xyz)
+    uint32_t* flags;
+    float4* outDirect;   // xyz direct radiance
+    float4* outDiffuse;  // xyz indirect diffuse
+    float4* outGlossy;   // xyz indirect glossy
+    float4* lastIndirect; // payload.indirect left by the last traced segment (xyz)
+    // Pending shadow-ray contributions of the segment shaded at the current bounce.
+    float4* pendEmission;   // xyz emission
+    float4* pendSegContrib; // xyz rayContribution the segment is scaled by
+    float4* pendSlot;       // kMaxShadowSlots per path: xyz contribution
+    uint32_t* pendBits;     // RS_* bits
+    uint32_t* occluded;     // bit k: shadow slot k occluded
+    // Queues.
+    float4* rayOrg[2];      // xyz origin, w tmin
+    float4* rayDir[2];      // xyz direction, w tmax
+    uint32_t* rayPath[2];
+    float4* hitTUV;         // t (or -1), u, v, prim (int bits)
+    int32_t* hitInst;
+    float4* shOrg;
+    float4* shDir;
+    uint32_t* shTag;        // path << 3 | slot
+    uint32_t* resolveList;  // paths with a pending record this bounce
+    uint32_t* counters;     // per bounce: [rays, shadow, resolve, spare]
+    // Accumulation targets (per pixel).
+    float4* accumMean;
+    float4* accumSum;
+    float4* accumComp;
+    float4* lastSample;
+    unsigned long long* stats; // [closest rays, shadow rays, nodes, tris, overflow]
+};
+
+struct WaveParams
+{
+    uint32_t width, height, pixels;
+    uint32_t sampleBase, samples; // this wave
+    uint32_t paths;               // pixels * samples
+    uint32_t accumMode;           // AGB_ACCUM_* bits
+    int32_t countTraversal;
+};
+
+} // namespace agb

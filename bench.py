@@ -1,0 +1,330 @@
+#!/usr/bin/env python3
+"""Benchmark: path-samples/s of the GB300 path tracer on the large plain-method configuration
+(1920x1080, 64 spp, up to 8 bounces, one 1,310,720-triangle icosphere BLAS instanced 64 times,
+2048x1024 HDR environment), the configuration the headline metric is quoted on.
+
+One step = one render of the frame at 64 samples per pixel from sample 0 (132,710,400 path
+samples) through agb_render, scene resident in HBM.  L2 is flushed (a 256 MB write) between timed
+steps, outside the timed region.  Device time comes from CUDA events on the renderer's stream.
+
+  e2e          the same metric through the C ABI with host buffers: per step agb_frame_set from
+               pinned host memory (512 bytes), agb_render, agb_accum_read of the RGBA32F image into
+               pinned host memory; wall time per step.
+  roofline     dominant kernel (closest-hit traversal): algorithmic bytes (node visits x 64 B +
+               triangle tests x 48 B, counted by the kernels on the same samples) / its device time.
+  cpu_baseline the FP32 oracle (the project's CPU restatement of the reference shaders, kind
+               "port") on the host cores, on a bounded band of rows at 1 spp.
+
+--impl reference times that CPU implementation alone (the reference itself has no CPU path).
+--gpus N runs N independent replicas (one per rank); the path tracer needs no collective.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "path-samples/s"
+UNIT = "path-samples/s"
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--config", default="large", choices=["large", "small"])
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_scene(name):
+    from aurora_gb300 import scenes
+    if name == "small":
+        return scenes.config_small(seed=0)
+    return scenes.config_large(seed=0)
+
+
+def workload(s, name):
+    return {"workload": ("plain method, large: icosphere level 8 (1,310,720 tris) x64 instances, "
+                         "1920x1080, 64 spp, 8 bounces, 2048x1024 HDR env")
+            if name == "large" else
+            "plain method, small: 8x8 UV spheres + quad, 512x512, 16 spp, 5 bounces",
+            "width": s.width, "height": s.height, "spp": s.spp,
+            "trace_depth": int(s.frame["trace_depth"]), "unique_triangles": s.unique_triangles,
+            "instances": len(s.instances), "instanced_triangles": s.triangle_count,
+            "seed": 0, "accumulation": "FP32 running mean + Kahan-compensated sum",
+            "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas"}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-i", str(self.index), "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        rows = []
+        for line in open(self.file.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = np.array([float(r[1]) for r in rows])
+        mx = float(rows[0][2])
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "samples": len(rows),
+                "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_render_rate(s, seconds, start_row=None):
+    """Oracle FP32 on all host cores over a band of rows at 1 spp; returns (paths/s, threads,
+    description)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    o = pyoracle.OracleScene(s)
+    threads = os.cpu_count() or 1
+    o.tracer(32)  # build the BVHs outside the timed part
+    mid = s.height // 2
+    probe_rows = max(4, s.height // 64)
+    rect = (0, mid - probe_rows // 2, s.width, mid - probe_rows // 2 + probe_rows)
+    r = o.render(0, 1, threads=threads, rect=rect, want_mean=False)
+    rate = s.width * probe_rows / max(r["seconds"], 1e-6)
+    rows = int(min(s.height, max(probe_rows, rate * seconds / s.width)))
+    y0 = max(0, mid - rows // 2)
+    rect = (0, y0, s.width, y0 + rows)
+    r = o.render(1, 1, threads=threads, rect=rect, want_mean=False)
+    paths = s.width * rows
+    o.close()
+    return paths / r["seconds"], threads, (
+        f"rows {y0}-{y0 + rows} of the {s.width}x{s.height} frame at 1 spp (sample index 1), "
+        f"{paths} path samples, {r['seconds']:.1f} s, FP32 oracle, BVH build excluded")
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    s = make_scene(args.config)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    o = pyoracle.OracleScene(s)
+    threads = os.cpu_count() or 1
+    o.tracer(32)
+    # Each step: a band of rows at 1 spp sized to ~10 s on this host.
+    mid = s.height // 2
+    probe_rows = max(4, s.height // 64)
+    rect = (0, mid - probe_rows // 2, s.width, mid - probe_rows // 2 + probe_rows)
+    r = o.render(0, 1, threads=threads, rect=rect, want_mean=False)
+    rate = s.width * probe_rows / max(r["seconds"], 1e-6)
+    rows = int(min(s.height, max(probe_rows, rate * 10.0 / s.width)))
+    y0 = max(0, mid - rows // 2)
+    rect = (0, y0, s.width, y0 + rows)
+    for w in range(args.warmup):
+        o.render(w, 1, threads=threads, rect=rect, want_mean=False)
+    secs = 0.0
+    for k in range(args.steps):
+        secs += o.render(args.warmup + k, 1, threads=threads, rect=rect, want_mean=False)["seconds"]
+    paths = s.width * rows * args.steps
+    value = paths / secs
+    sample = (f"rows {y0}-{y0 + rows} of the {s.width}x{s.height} frame, 1 spp per step, FP32 "
+              f"oracle port of the reference shaders on {threads} host threads")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)", "config": workload(s, args.config),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's own backend needs a Vulkan ray-tracing device (no CPU path); "
+                "its lavapipe run is unavailable on this box, so its CPU restatement is timed"}))
+    o.close()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    rank, world, local = dist_env()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from aurora_gb300 import _abi, api, build
+    build.build()
+    s = make_scene(args.config)
+    stream = torch.cuda.Stream()
+    r = api.Renderer(local, stream=stream.cuda_stream)
+    r.upload(s)
+    paths_per_step = s.width * s.height * s.spp
+
+    # Counting pass (untimed): node visits and triangle tests of exactly the timed work.
+    r.set_counting(True)
+    counted = r.render(0, s.spp, stats=True)
+    r.set_counting(False)
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        r.render(0, s.spp)
+    r.set_profiling(True)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    step_ms = []
+    kernel_ms = {k: 0.0 for k in _abi.KERNEL_FAMILIES}
+    kernel_count = {k: 0 for k in _abi.KERNEL_FAMILIES}
+    launches = 0
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = r.render(0, s.spp, stats=True)
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        launches += st["kernel_launches"]
+        for k in _abi.KERNEL_FAMILIES:
+            kernel_ms[k] += st["kernel_ms"][k]
+            kernel_count[k] += st["kernel_count"][k]
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    total_ms = float(sum(step_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = paths_per_step * args.steps * world / (total_ms / 1000.0)
+    r.set_profiling(False)
+
+    # End to end through the C ABI with host buffers.
+    frame_host = torch.from_numpy(np.frombuffer(np.ascontiguousarray(s.frame).tobytes(),
+                                                np.uint8).copy()).pin_memory()
+    img_host = torch.empty((s.height, s.width, 4), dtype=torch.float32).pin_memory()
+    img_np = img_host.numpy()
+    frame_np = frame_host.numpy().view(_abi.FRAME_DTYPE)
+    e2e_s = []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        r.set_frame(frame_np)
+        r.render(0, s.spp)
+        r.read(_abi.ACCUM_KAHAN, out=img_np)
+        if k >= args.warmup:
+            e2e_s.append(time.perf_counter() - t0)
+    e2e_time = float(np.sum(e2e_s))
+    if world > 1:
+        t = torch.tensor([e2e_time], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_time = float(t.item())
+    e2e_value = paths_per_step * args.steps * world / e2e_time
+
+    # Roofline of the dominant kernel family.
+    steps = args.steps
+    closest_ms = kernel_ms["trace_closest"] / steps
+    closest_bytes = counted["node_visits"] * 64 + counted["tri_tests"] * 48
+    shadow_ms = kernel_ms["trace_shadow"] / steps
+    shadow_bytes = counted["shadow_node_visits"] * 64 + counted["shadow_tri_tests"] * 48
+    dominant = max(kernel_ms, key=lambda k: kernel_ms[k])
+    peaks = measured_peaks()
+    peak = peaks["hbm_gbs"] if peaks else 6800.0
+    achieved = closest_bytes / (closest_ms / 1000.0) / 1e9
+    roofline = {
+        "bound": "hbm", "kernel": "k_trace_closest (closest-hit BVH2 traversal)",
+        "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+        "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
+        "traffic": None,
+        "algorithmic_bytes_per_step": int(closest_bytes),
+        "launches_per_step": kernel_count["trace_closest"] / steps,
+        "ms_per_step": closest_ms,
+        "bytes_model": "node visits x 64 B (BVH2 node, both child boxes) + triangle tests x 48 B "
+                       "(3 x float4 vertices), counted on the timed samples",
+        "shadow_kernel": {"achieved_gbs": shadow_bytes / max(shadow_ms, 1e-9) / 1e6,
+                          "ms_per_step": shadow_ms, "algorithmic_bytes_per_step": int(shadow_bytes)},
+        "dominant_family_by_time": dominant,
+        "kernel_ms_per_step": {k: v / steps for k, v in kernel_ms.items()},
+    }
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": workload(s, args.config),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(_abi.FRAME_DTYPE.itemsize),
+                "d2h_bytes_per_step": int(s.width * s.height * 16),
+                "ms_per_step": 1000.0 * e2e_time / args.steps},
+        "gpu_launches": int(launches),
+        "rays_per_step": {"closest": counted["closest_rays"], "shadow": counted["shadow_rays"]},
+        "roofline": roofline,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu, threads, sample = cpu_render_rate(s, args.cpu_seconds)
+        out["cpu_baseline"] = {"value": cpu, "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": sample}
+    r.close()
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

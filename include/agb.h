@@ -1,0 +1,409 @@
+/*
+ * agb.h - C ABI of the GB300 path-tracing backend for Aurora.
+ *
+ * This is the boundary between Aurora's C++ renderer interfaces (IRenderer / IScene / IMaterial /
+ * IRenderBuffer, Libraries/Aurora/API/Aurora/Aurora.h:714-1226) and the sm_103a CUDA kernels.  The
+ * reference has no such boundary: its HGI backend calls Vulkan ray tracing through USD Hgi.  Each
+ * entry point below names the reference call it replaces.  Only plain C types cross it: no C++,
+ * no CUDA or torch types.  Every function returns an agb_status (0 = success, negative = error);
+ * agb_last_error() gives the message of the last failure on the calling thread.
+ *
+ * Pointers documented as "host" are read or written by the call itself (the call copies them);
+ * "device" pointers must be CUDA device (or managed) memory on the context's GPU.
+ */
+#ifndef AGB_H
+#define AGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define AGB_API __declspec(dllexport)
+#else
+#define AGB_API __attribute__((visibility("default")))
+#endif
+
+typedef int32_t agb_status;
+enum
+{
+    AGB_OK              = 0,
+    AGB_ERR_INVALID_ARG = -1,
+    AGB_ERR_CUDA        = -2,
+    AGB_ERR_OOM         = -3,
+    AGB_ERR_TIMEOUT     = -4,
+    AGB_ERR_NOT_READY   = -5,
+    AGB_ERR_LIMIT       = -6
+};
+
+/* ------------------------------------------------------------------------------------------ */
+/* Data layouts shared with the reference (byte-identical).                                   */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Standard Surface material block, 400 bytes, std140 (Shaders/DefaultMaterialUniformBuffer.slang;
+ * property order and defaults MaterialBase.cpp:28-167).  Uploaded per material by HGIMaterial
+ * (HGI/HGIMaterial.cpp:23-60). */
+typedef struct agb_material
+{
+    float base;
+    float base_color[3];
+    float diffuse_roughness;
+    float metalness;
+    float specular;
+    int32_t _pad0;
+    float specular_color[3];
+    float specular_roughness;
+    float specular_IOR;
+    float specular_anisotropy;
+    float specular_rotation;
+    float transmission;
+    float transmission_color[3];
+    float subsurface;
+    float subsurface_color[3];
+    int32_t _pad1;
+    float subsurface_radius[3];
+    float subsurface_scale;
+    float subsurface_anisotropy;
+    float sheen;
+    int32_t _pad2;
+    int32_t _pad3;
+    float sheen_color[3];
+    float sheen_roughness;
+    float coat;
+    float coat_color[3];
+    float coat_roughness;
+    float coat_anisotropy;
+    float coat_rotation;
+    float coat_IOR;
+    float coat_affect_color;
+    float coat_affect_roughness;
+    float emission;
+    int32_t _pad4;
+    float emission_color[3];
+    int32_t _pad5;
+    float opacity[3];
+    int32_t thin_walled;
+    int32_t has_base_color_image;
+    float base_color_image_offset[2];
+    int32_t _pad6;
+    float base_color_image_scale[2];
+    float base_color_image_pivot[2];
+    float base_color_image_rotation;
+    int32_t has_specular_roughness_image;
+    float specular_roughness_image_offset[2];
+    float specular_roughness_image_scale[2];
+    float specular_roughness_image_pivot[2];
+    float specular_roughness_image_rotation;
+    int32_t has_emission_color_image;
+    float emission_color_image_offset[2];
+    float emission_color_image_scale[2];
+    float emission_color_image_pivot[2];
+    float emission_color_image_rotation;
+    int32_t has_opacity_image;
+    float opacity_image_offset[2];
+    float opacity_image_scale[2];
+    float opacity_image_pivot[2];
+    float opacity_image_rotation;
+    int32_t has_normal_image;
+    float normal_image_offset[2];
+    float normal_image_scale[2];
+    float normal_image_pivot[2];
+    float normal_image_rotation;
+    int32_t _pad7;
+    int32_t _pad8;
+    int32_t _pad9;
+} agb_material;
+
+/* Texture slots of the built-in material, reference order (MaterialBase.cpp:97-103). */
+enum
+{
+    AGB_TEX_BASE_COLOR         = 0,
+    AGB_TEX_SPECULAR_ROUGHNESS = 1,
+    AGB_TEX_OPACITY            = 2,
+    AGB_TEX_NORMAL             = 3,
+    AGB_TEX_EMISSION           = 4,
+    AGB_TEX_SLOTS              = 5
+};
+/* Image index bound to each texture slot of one material; -1 = none. */
+typedef struct agb_material_textures
+{
+    int32_t image[AGB_TEX_SLOTS];
+} agb_material_textures;
+
+/* One distant light (SceneBase.h:34-45; packed by HGIScene.cpp:118-132): direction already
+ * negated (points toward the light), cos_radius = cos(0.5 * angular diameter). */
+typedef struct agb_distant_light
+{
+    float color_and_intensity[4];
+    float direction[3];
+    float cos_radius;
+} agb_distant_light;
+
+/* Per-frame data, the reference's RendererBase::FrameData (RendererBase.h:136-241) byte for byte.
+ * camera_inv_view holds the camera-to-world matrix stored row-major (the bytes of the reference's
+ * transpose(inverse(view))): right = (m0,m4,m8), up = (m1,m5,m9), back = (m2,m6,m10),
+ * eye = (m3,m7,m11).  view_size = (2 / P[0][0], 2 / P[1][1]). */
+typedef struct agb_frame_data
+{
+    float camera_view_proj[16];
+    float camera_view_proj_prev[16];
+    float camera_inv_view[16];
+    float camera_inv_view_prev[16];
+    float view_size[2];
+    float camera_jitter[2];
+    float camera_jitter_prev[2];
+    int32_t is_ortho_projection;
+    float focal_distance;
+    float lens_radius;
+    float time_delta_ms;
+    int32_t is_temporal_jitter_enabled;
+    float scene_size;
+    int32_t is_force_opaque_shadows_enabled;
+    int32_t is_depth_ndc_enabled;
+    int32_t is_diffuse_only_enabled;
+    int32_t is_display_errors_enabled;
+    int32_t is_denoising_enabled;
+    int32_t is_denoising_aovs_enabled;
+    int32_t trace_depth;
+    float max_luminance;
+    int32_t is_russian_roulette_enabled;
+    int32_t russian_roulette_start_depth;
+    int32_t is_path_regularization_enabled;
+    float path_regularization_strength;
+    float indirect_bounce_clamp_scale;
+    float sky_view_z;
+    float _padding1[2];
+    agb_distant_light distant_lights[4];
+    int32_t distant_light_count;
+    int32_t _light_pad[3];
+} agb_frame_data;
+
+/* Environment constants, the reference's EnvironmentBase::EnvironmentData (EnvironmentBase.h:33-55)
+ * byte for byte.  Matrices are stored row-major and applied to column vectors.  The luminance
+ * integral is filled in by agb_environment_set when a light image is given. */
+typedef struct agb_environment_data
+{
+    float light_top[3];
+    float _padding1;
+    float light_bottom[3];
+    float light_tex_luminance_integral;
+    float light_transform[16];
+    float light_transform_inv[16];
+    float background_top[3];
+    float _padding3;
+    float background_bottom[3];
+    float _padding4;
+    float background_transform[16];
+    int32_t background_use_screen;
+    int32_t has_light_tex;
+    int32_t has_background_tex;
+} agb_environment_data;
+
+/* Alias-table entry (AliasMap.h:23-29). */
+typedef struct agb_alias_entry
+{
+    uint32_t alias;
+    float prob;
+    float pdf;
+    float _padding1;
+} agb_alias_entry;
+
+/* ------------------------------------------------------------------------------------------ */
+/* Scene description.                                                                          */
+/* ------------------------------------------------------------------------------------------ */
+
+/* One material layer of an instance (layer material + per-vertex UV set of the base mesh), the
+ * DirectX layer data of PTScene.cpp:1051-1166 / GlobalBufferAccessors.slang:60-83.
+ * texcoords: host, 2 floats per base-mesh vertex. */
+typedef struct agb_layer
+{
+    int32_t material;
+    int32_t _pad;
+    const float* texcoords;
+} agb_layer;
+
+/* One instance (IScene::addInstancePointer, Aurora.h:1027-1029; HGIScene.cpp:383-397).
+ * object_to_world: 3x4 row-major (rows of the reference's column-major mat4).  layers: host,
+ * layer_count entries, outermost first as LayerDefinitions lists them. */
+typedef struct agb_instance
+{
+    int32_t geometry;
+    int32_t material;
+    float object_to_world[12];
+    int32_t layer_count;
+    int32_t _pad;
+    const agb_layer* layers;
+} agb_instance;
+
+/* Pixel formats of agb_image_create (Aurora.h:413-446 ImageFormat subset). */
+enum
+{
+    AGB_FORMAT_RGBA8_UNORM = 0,
+    AGB_FORMAT_RGBA32F     = 1,
+    AGB_FORMAT_RGB32F      = 2
+};
+
+/* Accumulation modes of agb_render. */
+enum
+{
+    /* FP32 running mean mix(prev, cur, 1/(n+1)) (HGI/Shaders/Accumulation.glsl:22-30). */
+    AGB_ACCUM_RUNNING_MEAN = 1,
+    /* FP32 Kahan-compensated sum and sample count; resolve divides. */
+    AGB_ACCUM_KAHAN = 2
+};
+
+/* Render options beyond FrameData. */
+typedef struct agb_render_options
+{
+    uint32_t width;
+    uint32_t height;
+    uint32_t accumulation;      /* AGB_ACCUM_* bitmask */
+    uint32_t max_paths_in_flight; /* wave size in paths; 0 = default */
+    int32_t env_filter_linear;  /* environment sampler: 0 nearest (Hgi default), 1 bilinear */
+    int32_t _pad[3];
+} agb_render_options;
+
+typedef struct agb_context agb_context;
+
+/* Per-render statistics, filled by agb_render when stats is non-null (the call then waits for the
+ * render to finish). */
+typedef struct agb_render_stats
+{
+    uint64_t paths;               /* camera paths traced */
+    uint64_t closest_rays;        /* closest-hit rays traced (all segments) */
+    uint64_t shadow_rays;         /* shadow rays traced */
+    uint64_t node_visits;         /* closest-hit BVH node visits (when counting is enabled) */
+    uint64_t tri_tests;           /* closest-hit triangle tests (when counting is enabled) */
+    uint64_t shadow_node_visits;  /* shadow-ray BVH node visits (when counting is enabled) */
+    uint64_t shadow_tri_tests;    /* shadow-ray triangle tests (when counting is enabled) */
+    uint64_t kernel_launches;     /* CUDA kernels launched by this call */
+    double gpu_ms;                /* device time of the call (CUDA events) */
+    /* Device time per kernel family (when profiling is enabled): camera, closest-hit traversal,
+     * shading, shadow traversal, resolve, finalize. */
+    double kernel_ms[6];
+    uint64_t kernel_count[6];     /* launches per kernel family */
+} agb_render_stats;
+
+/* ------------------------------------------------------------------------------------------ */
+/* Context.                                                                                    */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Creates a renderer context on a CUDA device (replaces HGIRenderer construction,
+ * HGI/HGIRenderer.cpp:36-62, and its Hgi device).  stream may be null (a stream is created). */
+AGB_API agb_status agb_context_create(int32_t device, void* cuda_stream, agb_context** out);
+AGB_API agb_status agb_context_destroy(agb_context* ctx);
+/* Message of the last failing call on this thread (empty when none). */
+AGB_API const char* agb_last_error(void);
+/* Bytes of device memory the context holds. */
+AGB_API agb_status agb_context_memory(agb_context* ctx, uint64_t* bytes);
+/* Enables device-side counting of node visits / triangle tests (for the roofline). */
+AGB_API agb_status agb_set_counting(agb_context* ctx, int32_t enabled);
+/* Enables per-kernel-family device timing with CUDA events (agb_render_stats::kernel_ms). */
+AGB_API agb_status agb_set_profiling(agb_context* ctx, int32_t enabled);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Scene.                                                                                      */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Copies one triangle mesh to the device and builds its BLAS (replaces HGIGeometry::update,
+ * HGI/HGIGeometry.cpp:35-161).  Host pointers; normals/texcoords may be null; indices may be null
+ * for non-indexed geometry (sequential indices, HGIGeometry.cpp:37-47).  index_count is 3 x
+ * triangles (vertex_count when indices is null). */
+AGB_API agb_status agb_geometry_create(agb_context* ctx, const float* positions,
+    const float* normals, const float* texcoords, const uint32_t* indices, uint32_t vertex_count,
+    uint32_t index_count, int32_t* out_geometry);
+
+/* Uploads an image (material texture or environment).  Host pixels, rows top to bottom.
+ * linear: 1 bilinear, 0 nearest filtering (repeat addressing). */
+AGB_API agb_status agb_image_create(agb_context* ctx, const void* pixels, uint32_t width,
+    uint32_t height, int32_t format, int32_t linear, int32_t* out_image);
+
+/* Replaces the material table (HGIMaterial::update uploads, HGI/HGIMaterial.cpp:23-60).
+ * textures may be null. Host arrays of count entries. */
+AGB_API agb_status agb_materials_set(agb_context* ctx, const agb_material* materials,
+    const agb_material_textures* textures, uint32_t count);
+
+/* Replaces the instance list and rebuilds the TLAS (HGIScene::rebuildInstanceList and
+ * rebuildAccelerationStructure, HGI/HGIScene.cpp:192-449). Host array. */
+AGB_API agb_status agb_instances_set(agb_context* ctx, const agb_instance* instances,
+    uint32_t count);
+
+/* Sets the environment (HGIEnvironment / HGIImage alias-map build, HGI/HGIImage.cpp:45-90;
+ * EnvironmentBase.cpp:52-71).  light_image / background_image: image handles or -1.  With a light
+ * image, builds the alias table on the GPU from FP64 prefix sums and fills
+ * light_tex_luminance_integral. */
+AGB_API agb_status agb_environment_set(agb_context* ctx, const agb_environment_data* env,
+    int32_t light_image, int32_t background_image);
+/* Reads back the environment alias table (width*height entries) and luminance integral. */
+AGB_API agb_status agb_environment_alias(agb_context* ctx, agb_alias_entry* host_out,
+    uint64_t capacity, double* integral);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Rendering.                                                                                  */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Sets the per-frame data (replaces the FrameData UBO blit, HGI/HGIRenderer.cpp:502-513). */
+AGB_API agb_status agb_frame_set(agb_context* ctx, const agb_frame_data* frame);
+
+/* Renders sample_count samples starting at sample_start into the context's accumulation buffers
+ * (replaces the HGIRenderer::render sample loop, HGI/HGIRenderer.cpp:494-587: ray dispatch +
+ * accumulation).  sample_start == 0 restarts accumulation.  Asynchronous on the context stream. */
+AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* options,
+    uint32_t sample_start, uint32_t sample_count, agb_render_stats* stats);
+
+/* Waits for the context stream (IRenderer::waitForTask, Aurora.h:1199). */
+AGB_API agb_status agb_wait(agb_context* ctx);
+
+/* Copies the accumulated image to the host as RGBA32F (IRenderBuffer::data, HGIRenderBuffer.cpp).
+ * mode: AGB_ACCUM_RUNNING_MEAN reads the running mean; AGB_ACCUM_KAHAN reads sum / count. */
+AGB_API agb_status agb_accum_read(agb_context* ctx, int32_t mode, float* host_rgba,
+    uint64_t capacity_floats);
+/* Device pointer to the accumulation buffer of a mode (RGBA32F, width*height*4 floats). */
+AGB_API agb_status agb_accum_device(agb_context* ctx, int32_t mode, float** device_rgba);
+/* Per-sample output of the last rendered sample (RGBA32F device buffer), like gResult. */
+AGB_API agb_status agb_last_sample_device(agb_context* ctx, float** device_rgba);
+
+/* Post-processing (HGI/Shaders/PostProcessing.glsl:37-64): brightness, optional ACES, optional
+ * sRGB approximation, alpha 1.  Writes RGBA32F (out_rgba32f) and/or RGBA8 (out_rgba8) host
+ * buffers. */
+AGB_API agb_status agb_post_process(agb_context* ctx, int32_t mode, const float brightness[3],
+    int32_t tone_map, int32_t gamma, float* out_rgba32f, uint8_t* out_rgba8);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Unit kernels over device arrays (used by the parity tests; stream may be null = default).   */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Standard Surface BSDF over n shading points (StandardSurfaceBSDF.slang:598-1372).
+ * op 0 evaluateMaterial(V, L); 1 sampleMaterial(V, rnd) -> L, pdf, lobe;
+ * 2 evaluateMaterialAndPDF(V, L, rnd) -> pdf, lobe.  frames: 12 floats per point (normal, tangent,
+ * bitangent, unused).  Vectors 3 floats, rnd 2 floats.  All device pointers. */
+AGB_API agb_status agb_bsdf_batch(int32_t op, const agb_material* materials,
+    const int32_t* material_index, const float* frames, const float* V, const float* L,
+    const float* rnd, int64_t n, float* out_value, float* out_dir, float* out_pdf,
+    int32_t* out_lobe, void* cuda_stream);
+
+/* Ray casts against the context's scene: rays 8 floats (origin, tmin, direction, tmax);
+ * out_tuv 3 floats (t or -1, u, v); out_inst_prim 2 ints.  any_hit: occlusion query.  Device. */
+AGB_API agb_status agb_intersect_batch(agb_context* ctx, const float* rays, int64_t n,
+    int32_t any_hit, float* out_tuv, int32_t* out_inst_prim);
+
+/* Environment sampling through the context's alias table (Environment.slang:137-186):
+ * rnd 2 floats -> radiance 3, direction 3, pdf 1.  Device pointers. */
+AGB_API agb_status agb_env_sample_batch(agb_context* ctx, const float* rnd, int64_t n,
+    float* out_radiance, float* out_dir, float* out_pdf);
+
+/* PCG2D stream (Random.slang:96-137) for one pixel sample, n pairs.  Device pointer. */
+AGB_API agb_status agb_random_stream(uint32_t sample_index, uint32_t screen_width, uint32_t px,
+    uint32_t py, int32_t n, float* out, void* cuda_stream);
+
+/* Library version string. */
+AGB_API const char* agb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AGB_H */

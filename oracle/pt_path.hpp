@@ -1,0 +1,745 @@
+// Oracle (test infrastructure, never linked into the product): the path-level restatement.
+//   Shaders/Random.slang:96-137          PCG2D random numbers
+//   Shaders/RayTrace.slang:130-182       computeCameraRay
+//   Shaders/RayTrace.slang:221-270       traceShadowRay (forced-opaque and transparent shadows)
+//   Shaders/Geometry.slang:131-265       computeShadingData
+//   Shaders/DefaultMaterial.slang:130-239 evaluateDefaultMaterial (textures, UV transforms)
+//   Shaders/ShadeFunctions.slang:31-310  emission, distant light, environment MIS, next ray
+//   Shaders/HitShaderEntryPoints.slang:35-486 closest hit incl. the material-layer loop
+//       (DirectX branch of GlobalBufferAccessors.slang:60-127 for layer data)
+//   Shaders/MainEntryPoints.slang:70-334, 355-426 ray-gen path loop and miss shader
+//   Shaders/PathTracingCommon.slang:59-82 adjustRadiance
+//   HGI/Shaders/Accumulation.glsl:14-34  running-mean accumulation
+//   HGI/Shaders/PostProcessing.glsl:37-64 brightness, ACES, sRGB, alpha = 1
+// The random numbers are always computed in FP32 (uint -> float), so the FP32 and FP64
+// instantiations draw identical sample streams.
+#pragma once
+
+#include "pt_bsdf.hpp"
+#include "pt_bvh.hpp"
+#include "pt_env.hpp"
+
+namespace orc
+{
+
+struct Rng
+{
+    uint32_t x = 0, y = 0;
+};
+
+// Random.slang:96-108
+inline Rng pcg2DInit(uint32_t sampleIndex, uint32_t screenWidth, uint32_t px, uint32_t py)
+{
+    Rng r;
+    r.x = py * screenWidth + px;
+    r.y = sampleIndex;
+    return r;
+}
+// Random.slang:113-137
+inline V2<float> random2Df(Rng& rng)
+{
+    uint32_t vx = rng.x, vy = rng.y;
+    vx += vy * 1664525u;
+    vy += vx * 1664525u;
+    vx ^= vx >> 16u;
+    vy ^= vy >> 16u;
+    vx += vy * 1664525u;
+    vy += vx * 1664525u;
+    vx ^= vx >> 16u;
+    vy ^= vy >> 16u;
+    rng.x = vx;
+    rng.y = vy;
+    const float denom = float(0xFFFFFFFFu);
+    return V2<float>(float(vx) / denom, float(vy) / denom);
+}
+// Note on the advance: pcg2D() returns the hashed pair and pcg2DNext2D() stores that pair back as
+// the state (Random.slang:133), so the LCG step inside pcg2D is overwritten and the next draw hashes
+// the previous output.
+
+template <class T>
+inline V2<T> random2D(Rng& rng)
+{
+    V2<float> r = random2Df(rng);
+    return V2<T>(T(r.x), T(r.y));
+}
+
+struct Scene
+{
+    const Mesh* meshes               = nullptr;
+    int32_t meshCount                = 0;
+    const Instance* instances        = nullptr;
+    int32_t instanceCount            = 0;
+    const MaterialBlock* materials   = nullptr;
+    int32_t materialCount            = 0;
+    const MaterialTextures* materialTextures = nullptr; // may be null (no textures)
+    const Image* images              = nullptr;
+    int32_t imageCount               = 0;
+    const EnvData* env               = nullptr;
+    const Image* envLight            = nullptr;
+    const Image* envBackground       = nullptr;
+    const AliasEntry* envAlias       = nullptr;
+};
+
+template <class T>
+struct PathTracer
+{
+    using v2 = V2<T>;
+    using v3 = V3<T>;
+    using B  = BSDF<T>;
+    using E  = Env<T>;
+
+    const Scene* scene    = nullptr;
+    const FrameData* frame = nullptr;
+    Caster<T> caster;
+    typename E::Scene env;
+    uint32_t screenW = 0, screenH = 0;
+
+    // Per-thread statistics (camera-path segments and shadow rays traced).
+    struct Stats
+    {
+        uint64_t raysTraced = 0, shadowRaysTraced = 0;
+    };
+    static Stats& stats()
+    {
+        static thread_local Stats s;
+        return s;
+    }
+
+    void init(const Scene* s, const FrameData* f, uint32_t w, uint32_t h, bool bruteForce = false)
+    {
+        scene   = s;
+        frame   = f;
+        screenW = w;
+        screenH = h;
+        caster.bruteForce = bruteForce;
+        caster.build(s->meshes, s->meshCount, s->instances, s->instanceCount);
+        env.data       = s->env;
+        env.lightImage = s->envLight;
+        env.background = s->envBackground;
+        env.alias      = s->envAlias;
+    }
+
+    // RayTrace.slang:130-182
+    void computeCameraRay(uint32_t px, uint32_t py, Rng& rng, v3& origin, v3& direction) const
+    {
+        const FrameData& f = *frame;
+        v2 sc{T(float(px)), T(float(py))};
+        if (f.isTemporalJitterEnabled)
+            sc = sc + v2(T(0.5f) + T(f.cameraJitter[0]), T(0.5f) + T(f.cameraJitter[1]));
+        else
+            sc = sc + random2D<T>(rng);
+        v2 ndc(sc.x / T(float(screenW)), sc.y / T(float(screenH)));
+        ndc         = v2(ndc.x * T(2) - T(1), ndc.y * T(2) - T(1));
+        ndc.y       = -ndc.y;
+        const float* m = f.cameraInvView;
+        v3 right{T(m[0]), T(m[4]), T(m[8])};
+        v3 up{T(m[1]), T(m[5]), T(m[9])};
+        v3 front = -v3(T(m[2]), T(m[6]), T(m[10]));
+        v3 eye{T(m[3]), T(m[7]), T(m[11])};
+        v2 size{T(f.viewSize[0]) * T(0.5f), T(f.viewSize[1]) * T(0.5f)};
+        v3 offset = right * (size.x * ndc.x) + up * (size.y * ndc.y);
+        if (f.isOrthoProjection)
+        {
+            direction = front;
+            origin    = eye + offset;
+        }
+        else
+        {
+            direction = normalize(front + offset);
+            origin    = eye;
+        }
+        if (f.lensRadius > 0.f)
+        {
+            v3 focalPoint = origin + direction * T(f.focalDistance);
+            v2 off        = B::sampleDisk(random2D<T>(rng), T(f.lensRadius));
+            origin        = origin + right * off.x + up * off.y;
+            direction     = normalize(focalPoint - origin);
+        }
+    }
+
+    // Geometry.slang:131-148
+    static v3 projectOnPlane(const v3& p, const v3& o, const v3& n) { return p - n * dot(p - o, n); }
+
+    // Geometry.slang:152-265 (tangent from the up vector: HGI never reports tangents).
+    ShadingData<T> computeShadingData(int32_t inst, uint32_t tri, T u, T v) const
+    {
+        const Instance& in = scene->instances[inst];
+        const Mesh& m      = scene->meshes[in.mesh];
+        ShadingData<T> sh;
+        v3 bary{T(1) - u - v, u, v};
+        sh.barycentrics = bary;
+        uint32_t idx[3] = { m.indices[3 * size_t(tri)], m.indices[3 * size_t(tri) + 1],
+            m.indices[3 * size_t(tri) + 2] };
+        v3 pos[3], nrm[3];
+        v3 gp(0), n(0);
+        v2 uv{T(0), T(0)};
+        for (int i = 0; i < 3; i++)
+        {
+            pos[i] = v3::from(m.positions + 3 * size_t(idx[i]));
+            gp += pos[i] * bary[i];
+            if (m.normals)
+            {
+                nrm[i] = v3::from(m.normals + 3 * size_t(idx[i]));
+                n += nrm[i] * bary[i];
+            }
+            if (m.texcoords)
+            {
+                v2 t{T(m.texcoords[2 * size_t(idx[i])]), T(m.texcoords[2 * size_t(idx[i]) + 1])};
+                uv = uv + t * bary[i];
+            }
+            sh.indices[i] = idx[i];
+        }
+        v3 objectNormal = normalize(m.normals ? n : cross(pos[1] - pos[0], pos[2] - pos[0]));
+        v3 objectPosition = gp;
+        if (m.normals)
+        {
+            v3 p0 = projectOnPlane(gp, pos[0], nrm[0]);
+            v3 p1 = projectOnPlane(gp, pos[1], nrm[1]);
+            v3 p2 = projectOnPlane(gp, pos[2], nrm[2]);
+            v3 sp = p0 * bary.x + p1 * bary.y + p2 * bary.z;
+            objectPosition = dot(sp - gp, n) > T(0) ? sp : gp;
+        }
+        Xform<T> x;
+        for (int k = 0; k < 12; k++)
+            x.m[k] = T(in.objectToWorld[k]);
+        sh.position     = x.point(objectPosition);
+        sh.geomPosition = x.point(gp);
+        sh.normal       = normalize(x.vector(objectNormal));
+        v3 up = std::fabs(sh.normal.y) < T(0.999f) ? v3(0, 1, 0) : v3(1, 0, 0);
+        sh.tangent   = normalize(cross(sh.normal, up));
+        sh.bitangent = cross(sh.normal, sh.tangent);
+        sh.texCoord  = uv;
+        return sh;
+    }
+
+    // DefaultMaterial.slang:88-105
+    static v2 applyUVTransform(v2 uv, const float* pivot, const float* scale, float rotate,
+        const float* offset)
+    {
+        v2 p{T(pivot[0]), T(pivot[1])};
+        v2 sub = uv - p;
+        v2 scaled(sub.x / T(scale[0]), sub.y / T(scale[1]));
+        T r  = T(rotate) * (Consts<T>::PI / T(180));
+        T sa = std::sin(r), ca = std::cos(r);
+        v2 rot(ca * scaled.x + sa * scaled.y, -sa * scaled.x + ca * scaled.y);
+        v2 tr(rot.x - T(offset[0]), rot.y - T(offset[1]));
+        return tr + p;
+    }
+
+    bool sampleMaterialTexture(int32_t material, int slot, v2 uv, const float* pivot,
+        const float* scale, float rotation, const float* offset, v3& rgb) const
+    {
+        if (!scene->materialTextures)
+            return false;
+        int32_t img = scene->materialTextures[material].image[slot];
+        if (img < 0 || img >= scene->imageCount)
+            return false;
+        T a;
+        E::sample(scene->images[img], applyUVTransform(uv, pivot, scale, rotation, offset), rgb, a);
+        return true;
+    }
+
+    // DefaultMaterial.slang:130-239
+    Material<T> evaluateDefaultMaterial(int32_t matIndex, const ShadingData<T>& sh,
+        v3& materialNormal, bool& isGeneratedNormal) const
+    {
+        const MaterialBlock& b = scene->materials[matIndex];
+        Material<T> m;
+        m.base               = T(b.base);
+        m.baseColor          = v3::from(b.baseColor);
+        m.diffuseRoughness   = T(b.diffuseRoughness);
+        m.metalness          = T(b.metalness);
+        m.specular           = T(b.specular);
+        m.specularColor      = v3::from(b.specularColor);
+        m.specularRoughness  = T(b.specularRoughness);
+        m.specularIOR        = T(b.specularIOR);
+        m.specularAnisotropy = T(b.specularAnisotropy);
+        m.specularRotation   = T(b.specularRotation);
+        m.transmission       = T(b.transmission);
+        m.transmissionColor  = v3::from(b.transmissionColor);
+        m.subsurface         = T(b.subsurface);
+        m.subsurfaceColor    = v3::from(b.subsurfaceColor);
+        m.subsurfaceRadius   = v3::from(b.subsurfaceRadius);
+        m.subsurfaceScale    = T(b.subsurfaceScale);
+        m.subsurfaceAnisotropy = T(b.subsurfaceAnisotropy);
+        m.sheen              = T(b.sheen);
+        m.sheenColor         = v3::from(b.sheenColor);
+        m.sheenRoughness     = T(b.sheenRoughness);
+        m.coat               = T(b.coat);
+        m.coatColor          = v3::from(b.coatColor);
+        m.coatRoughness      = T(b.coatRoughness);
+        m.coatAnisotropy     = T(b.coatAnisotropy);
+        m.coatRotation       = T(b.coatRotation);
+        m.coatIOR            = T(b.coatIOR);
+        m.coatAffectColor    = T(b.coatAffectColor);
+        m.coatAffectRoughness = T(b.coatAffectRoughness);
+        m.emission           = T(b.emission);
+        m.emissionColor      = v3::from(b.emissionColor);
+        m.opacity            = v3::from(b.opacity);
+        m.thinWalled         = b.thinWalled != 0;
+        v3 rgb;
+        if (b.hasBaseColorTex &&
+            sampleMaterialTexture(matIndex, kTexBaseColor, sh.texCoord, b.baseColorTexPivot,
+                b.baseColorTexScale, b.baseColorTexRotation, b.baseColorTexOffset, rgb))
+            m.baseColor = rgb;
+        if (b.hasSpecularRoughnessTex &&
+            sampleMaterialTexture(matIndex, kTexSpecularRoughness, sh.texCoord,
+                b.specularRoughnessTexPivot, b.specularRoughnessTexScale,
+                b.specularRoughnessTexRotation, b.specularRoughnessTexOffset, rgb))
+            m.specularRoughness = rgb.x;
+        if (b.hasEmissionColorTex &&
+            sampleMaterialTexture(matIndex, kTexEmission, sh.texCoord, b.emissionColorTexPivot,
+                b.emissionColorTexScale, b.emissionColorTexRotation, b.emissionColorTexOffset, rgb))
+            m.emissionColor = rgb;
+        if (b.hasOpacityTex &&
+            sampleMaterialTexture(matIndex, kTexOpacity, sh.texCoord, b.opacityTexPivot,
+                b.opacityTexScale, b.opacityTexRotation, b.opacityTexOffset, rgb))
+            m.opacity = rgb;
+        isGeneratedNormal = false;
+        if (b.hasNormalTex &&
+            sampleMaterialTexture(matIndex, kTexNormal, sh.texCoord, b.normalTexPivot,
+                b.normalTexScale, b.normalTexRotation, b.normalTexOffset, rgb))
+        {
+            v3 vv = rgb * T(2) - v3(1);
+            v3 Bn = normalize(cross(sh.normal, sh.tangent));
+            materialNormal    = normalize(sh.tangent * vv.x * T(1) + Bn * vv.y * T(1) + sh.normal * vv.z);
+            isGeneratedNormal = true;
+        }
+        m.metalColor = m.baseColor;
+        return m;
+    }
+
+    // ShadeFunctions.slang:31-48
+    static v3 shadeEmission(const Material<T>& m)
+    {
+        v3 blend = lerp(v3(1), m.coatColor, m.coat);
+        return m.emissionColor * m.emission * blend;
+    }
+
+    // ShadeFunctions.slang:51-89
+    static v3 shadeDirectionalLight(const DistantLight& l, const Material<T>& m,
+        const ShadingData<T>& sh, const v3& V, Rng& rng, v3& shadowDir)
+    {
+        v2 random = random2D<T>(rng);
+        v3 L      = B::sampleCone(random, v3::from(l.direction), T(l.cosRadius));
+        v3 bsdf   = B::evaluateMaterial(m, sh, V, L);
+        if (isBlack(bsdf))
+        {
+            shadowDir = v3(0);
+            return v3(0);
+        }
+        v3 radiance = v3::from(l.colorAndIntensity) * T(l.colorAndIntensity[3]);
+        shadowDir   = L;
+        return radiance * bsdf;
+    }
+
+    struct MISOut
+    {
+        int lobeID              = NO_SECONDARY_RAY;
+        bool emitsMaterial      = false;
+        v3 materialResult       = v3(0);
+        v3 materialDir          = v3(0);
+        bool emitsLight         = false;
+        v3 lightResult          = v3(0);
+        v3 lightDir             = v3(0);
+    };
+
+    // ShadeFunctions.slang:135-259
+    void shadeEnvironmentLightMIS(const Material<T>& m, const ShadingData<T>& sh, const v3& V,
+        Rng& rng, MISOut& o, v2 pixel) const
+    {
+        v2 random = random2D<T>(rng);
+        v3 L;
+        T materialPDF;
+        v3 bsdf = B::sampleMaterial(m, sh, V, random, L, materialPDF, o.lobeID);
+        if (o.lobeID == TRANSMISSION_LOBE)
+            return;
+        v2 ss{T(float(screenW)), T(float(screenH))};
+        v3 lightRadiance = E::evaluate(env, L, o.lobeID == TRANSMISSION_LOBE, pixel, ss);
+        if (!isBlack(lightRadiance) && !isBlack(bsdf))
+        {
+            T lightPDF = scene->env->hasLightTex
+                ? luminance(lightRadiance) / T(scene->env->lightTexLuminanceIntegral)
+                : B::divPi(T(0.25f));
+            T w = B::computeMISWeight(materialPDF, lightPDF);
+            o.materialResult = lightRadiance * w * bsdf / materialPDF;
+            o.materialDir    = L;
+            o.emitsMaterial  = true;
+        }
+        T lightPDF;
+        lightRadiance = E::sampleEnvironment(env, random, L, lightPDF);
+        int evaluatedLobe;
+        bsdf = B::evaluateMaterialAndPDF(m, sh, V, L, random, materialPDF, evaluatedLobe);
+        if (!isBlack(lightRadiance) && !isBlack(bsdf))
+        {
+            T w           = B::computeMISWeight(lightPDF, materialPDF);
+            o.lightResult = lightRadiance * w * bsdf / lightPDF;
+            o.lightDir    = L;
+            o.emitsLight  = true;
+        }
+    }
+
+    // ShadeFunctions.slang:263-310
+    static int setupIndirectLightRay(const Material<T>& m, const ShadingData<T>& sh, const v3& V,
+        Rng& rng, v3& dir, v3& origin, v3& color)
+    {
+        v3 L;
+        T pdf;
+        int lobeID;
+        v3 bsdf = B::sampleMaterial(m, sh, V, random2D<T>(rng), L, pdf, lobeID);
+        if (isBlack(bsdf))
+            return NO_SECONDARY_RAY;
+        bool isTransmission = lobeID == TRANSMISSION_LOBE;
+        origin = (dot(V, sh.normal) < T(0) || isTransmission) ? sh.geomPosition : sh.position;
+        dir    = L;
+        color  = bsdf / pdf;
+        return lobeID;
+    }
+
+    // Opacity the transparent-shadow any-hit shader subtracts (HitShaderEntryPoints.slang:490-552).
+    v3 shadowOpacity(const Hit& h) const
+    {
+        const Instance& in = scene->instances[h.inst];
+        const MaterialBlock& b = scene->materials[in.material];
+        bool hasOpacityImage = scene->materialTextures && b.hasOpacityTex &&
+            scene->materialTextures[in.material].image[kTexOpacity] >= 0;
+        bool opaque = b.opacity[0] == 1.f && b.opacity[1] == 1.f && b.opacity[2] == 1.f &&
+            !hasOpacityImage && b.transmission == 0.f;
+        if (opaque)
+            return v3(1);
+        ShadingData<T> sh = computeShadingData(h.inst, uint32_t(h.prim), T(h.u), T(h.v));
+        v3 mn = sh.normal;
+        bool gen;
+        Material<T> m = evaluateDefaultMaterial(in.material, sh, mn, gen);
+        return m.opacity * (v3(1) - m.transmissionColor * m.transmission);
+    }
+
+    // RayTrace.slang:221-270
+    v3 traceShadowRay(const v3& origin, const v3& L, int depth, int maxDepth) const
+    {
+        if (depth == maxDepth + 1)
+            return v3(1);
+        stats().shadowRaysTraced++;
+        if (frame->isForceOpaqueShadowsEnabled)
+            return caster.occluded(origin, L, Consts<T>::RAY_TMIN, T(INFINITY)) ? v3(0) : v3(1);
+        // Transparent shadows: multiply (1 - opacity) over every intersection along the ray.
+        v3 vis(1);
+        T tmin = Consts<T>::RAY_TMIN;
+        for (int guard = 0; guard < 4096; guard++)
+        {
+            Hit h;
+            if (!caster.closest(origin, L, tmin, T(INFINITY), h))
+                break;
+            vis *= v3(1) - shadowOpacity(h);
+            if (isBlack(vis))
+                break;
+            tmin = std::nextafter(T(h.t), T(INFINITY));
+        }
+        return vis;
+    }
+
+    struct Payload
+    {
+        Rng rng;
+        v3 rayContribution = v3(1);
+        v3 nextRayOrigin, nextRayDirection;
+        v3 direct = v3(0), indirect = v3(0);
+        bool isPrimaryRay = true, pathEnded = false, skipContribution = false, isInside = false;
+        int rayType = CAMERA_RAY, nextRayType = 0, misLobeID = NO_SECONDARY_RAY, rayDepth = 0;
+        T outputAlpha = T(0);
+    };
+
+    // Closest-hit shader (HitShaderEntryPoints.slang:35-486).
+    void closestHit(Payload& p, const v3& rayDirection, const Hit& hit, v2 pixel) const
+    {
+        const FrameData& f = *frame;
+        int maxTraceDepth  = f.traceDepth;
+        v3 nextRayContribution(1);
+        v3 V              = -rayDirection;
+        ShadingData<T> sh = computeShadingData(hit.inst, uint32_t(hit.prim), T(hit.u), T(hit.v));
+        const Instance& in = scene->instances[hit.inst];
+        bool hitLayer      = false;
+        v2 baseLayerUV     = sh.texCoord;
+        int layerCount     = in.layerCount;
+        for (int li = layerCount; li >= 0; li--)
+        {
+            int32_t matIndex;
+            if (li == 0)
+            {
+                matIndex    = in.material;
+                sh.texCoord = baseLayerUV;
+            }
+            else
+            {
+                const Layer& L = in.layers[li - 1];
+                matIndex       = L.material;
+                v2 uv{T(0), T(0)};
+                for (int i = 0; i < 3; i++)
+                {
+                    v2 t(T(L.texcoords[2 * size_t(sh.indices[i])]),
+                        T(L.texcoords[2 * size_t(sh.indices[i]) + 1]));
+                    uv = uv + t * sh.barycentrics[i];
+                }
+                sh.texCoord = uv;
+            }
+            bool isGeneratedNormal = false;
+            v3 materialNormal      = sh.normal;
+            Material<T> m = evaluateDefaultMaterial(matIndex, sh, materialNormal, isGeneratedNormal);
+            if (!p.isPrimaryRay && f.isPathRegularizationEnabled)
+            {
+                T fl = lerp(T(0.05f), lerp(T(0.05f), T(0.35f), T(f.pathRegularizationStrength)),
+                    saturate(T(float(p.rayDepth)) / T(3)));
+                m.specularRoughness = m.specularRoughness > fl ? m.specularRoughness : fl;
+                m.coatRoughness     = m.coatRoughness > fl ? m.coatRoughness : fl;
+            }
+            v3 transparency = v3(1) - m.opacity;
+            T P             = luminance(transparency);
+            hitLayer        = random2D<T>(p.rng).x >= P;
+            v3 dirShadowDir(0), dirColor(0);
+            bool hasDirectionalLight = false;
+            if (hitLayer)
+            {
+                if (isGeneratedNormal)
+                {
+                    sh.normal = materialNormal;
+                    B::buildBasis(sh.normal, sh.tangent, sh.bitangent);
+                }
+                p.direct += shadeEmission(m);
+                const LightData& lights = f.lights;
+                bool evaluateAll = !f.isDenoisingAOVsEnabled && lights.distantLightCount > 1;
+                if (evaluateAll)
+                {
+                    v3 o = dot(V, sh.normal) < T(0) ? sh.geomPosition : sh.position;
+                    for (int li2 = 0; li2 < lights.distantLightCount; li2++)
+                    {
+                        if (lights.distantLights[li2].colorAndIntensity[3] <= 0.f)
+                            continue;
+                        v3 sd;
+                        v3 r = shadeDirectionalLight(lights.distantLights[li2], m, sh, V, p.rng, sd);
+                        if (isBlack(r))
+                            continue;
+                        v3 vis = traceShadowRay(o, sd, p.rayDepth, maxTraceDepth);
+                        p.direct += vis * r;
+                    }
+                }
+                else if (lights.distantLightCount > 0)
+                {
+                    float weights[4];
+                    float total = 0.f;
+                    for (int i = 0; i < lights.distantLightCount; i++)
+                    {
+                        const float* ci = lights.distantLights[i].colorAndIntensity;
+                        float w = (ci[0] * 0.2125f + ci[1] * 0.7154f + ci[2] * 0.0721f) * ci[3];
+                        weights[i] = w;
+                        total += w;
+                    }
+                    int idx        = 0;
+                    float selPdf   = 1.f / float(lights.distantLightCount);
+                    if (total > 0.f)
+                    {
+                        float r   = random2Df(p.rng).x * total;
+                        float cum = 0.f;
+                        for (int i = 0; i < lights.distantLightCount; i++)
+                        {
+                            cum += weights[i];
+                            if (r <= cum || i == lights.distantLightCount - 1)
+                            {
+                                idx    = i;
+                                selPdf = weights[i] / total;
+                                break;
+                            }
+                        }
+                    }
+                    else
+                        idx = int(random2Df(p.rng).x * float(lights.distantLightCount));
+                    if (lights.distantLights[idx].colorAndIntensity[3] > 0.f)
+                    {
+                        dirColor = shadeDirectionalLight(
+                            lights.distantLights[idx], m, sh, V, p.rng, dirShadowDir);
+                        dirColor /= T(selPdf > 1e-4f ? selPdf : 1e-4f);
+                        hasDirectionalLight = true;
+                    }
+                }
+                MISOut mis;
+                shadeEnvironmentLightMIS(m, sh, V, p.rng, mis, pixel);
+                p.rayContribution *= m.opacity / (T(1) - P);
+                p.outputAlpha = (p.outputAlpha == T(0) && p.rayType == TRANSMISSION_LOBE) ? T(0) : T(1);
+                p.nextRayType = setupIndirectLightRay(
+                    m, sh, V, p.rng, p.nextRayDirection, p.nextRayOrigin, nextRayContribution);
+                v3 so = dot(V, sh.normal) < T(0) ? sh.geomPosition : sh.position;
+                if (hasDirectionalLight)
+                {
+                    v3 vis = traceShadowRay(so, dirShadowDir, p.rayDepth, maxTraceDepth);
+                    p.direct += vis * dirColor;
+                }
+                if (mis.emitsLight || mis.emitsMaterial)
+                {
+                    v3 misResult(0);
+                    if (mis.emitsMaterial)
+                        misResult += traceShadowRay(so, mis.materialDir, p.rayDepth, maxTraceDepth) *
+                            mis.materialResult;
+                    if (mis.emitsLight)
+                        misResult += traceShadowRay(so, mis.lightDir, p.rayDepth, maxTraceDepth) *
+                            mis.lightResult;
+                    p.misLobeID = mis.lobeID;
+                    p.indirect  = misResult;
+                }
+                if (p.nextRayType == NO_SECONDARY_RAY)
+                    p.pathEnded = true;
+                p.isPrimaryRay = false;
+                break;
+            }
+            else
+                p.rayContribution *= transparency / P;
+        }
+        if (!hitLayer)
+        {
+            p.nextRayDirection = -V;
+            p.nextRayOrigin    = sh.geomPosition;
+            p.skipContribution = true;
+            return;
+        }
+        if (p.nextRayType == TRANSMISSION_LOBE)
+            p.isInside = !p.isInside;
+        p.direct *= p.rayContribution;
+        p.indirect *= p.rayContribution;
+        p.rayContribution *= nextRayContribution;
+        if (f.isRussianRouletteEnabled && p.rayDepth + 1 >= f.russianRouletteStartDepth)
+        {
+            v3 tp  = p.rayContribution;
+            T mx   = tp.x > (tp.y > tp.z ? tp.y : tp.z) ? tp.x : (tp.y > tp.z ? tp.y : tp.z);
+            T surv = clampT(mx, T(0.05f), T(1));
+            if (random2D<T>(p.rng).x > surv)
+                p.pathEnded = true;
+            else
+                p.rayContribution = p.rayContribution / surv;
+        }
+    }
+
+    // PathTracingCommon.slang:59-82
+    static void adjustRadiance(T maxLuminance, bool displayErrors, v3& radiance)
+    {
+        T lum = luminance(radiance);
+        if (lum > maxLuminance)
+            radiance *= maxLuminance / lum;
+        bool isnan_ = std::isnan(radiance.x) || std::isnan(radiance.y) || std::isnan(radiance.z);
+        bool isinf_ = std::isinf(radiance.x) || std::isinf(radiance.y) || std::isinf(radiance.z);
+        if (isnan_)
+            radiance = displayErrors ? v3(T(INFINITY), 0, 0) : v3(0);
+        else if (isinf_)
+            radiance = displayErrors ? v3(0, T(INFINITY), 0) : v3(0);
+    }
+
+    // Ray-generation shader (MainEntryPoints.slang:70-270) for one pixel sample.  Returns RGBA.
+    void tracePath(uint32_t px, uint32_t py, uint32_t sampleIndex, T out[4]) const
+    {
+        const FrameData& f = *frame;
+        int maxTraceDepth  = f.traceDepth;
+        Payload p;
+        p.rng = pcg2DInit(sampleIndex, screenW, px, py);
+        v3 rayOrigin, rayDirection;
+        computeCameraRay(px, py, p.rng, rayOrigin, rayDirection);
+        v3 outDirect(0), outDiffuse(0), outGlossy(0);
+        T outAlpha = T(0);
+        v2 pixel{T(float(px)), T(float(py))};
+        v2 ss{T(float(screenW)), T(float(screenH))};
+        for (int rayDepth = 0; rayDepth <= maxTraceDepth && !p.pathEnded; rayDepth++)
+        {
+            if (rayDepth == maxTraceDepth)
+            {
+                bool bg = p.isPrimaryRay || p.rayType == TRANSMISSION_LOBE ||
+                    p.rayType == GROUND_PLANE_REFLECTION_RAY;
+                p.direct = E::evaluate(env, rayDirection, bg, pixel, ss);
+                p.direct *= p.rayContribution;
+                p.pathEnded = true;
+            }
+            else
+            {
+                T minT     = rayDepth == 0 ? T(0) : Consts<T>::RAY_TMIN;
+                p.rayDepth = rayDepth;
+                p.direct   = v3(0);
+                p.indirect = v3(0);
+                Hit hit;
+                stats().raysTraced++;
+                if (caster.closest(rayOrigin, rayDirection, minT, T(INFINITY), hit))
+                    closestHit(p, rayDirection, hit, pixel);
+                else
+                {
+                    bool bg = p.isPrimaryRay || p.rayType == TRANSMISSION_LOBE ||
+                        p.rayType == GROUND_PLANE_REFLECTION_RAY;
+                    if (bg)
+                    {
+                        p.direct = E::evaluate(env, rayDirection, true, pixel, ss);
+                        p.direct *= p.rayContribution;
+                    }
+                    p.pathEnded = true;
+                }
+                rayOrigin    = p.nextRayOrigin;
+                rayDirection = p.nextRayDirection;
+                outAlpha     = p.outputAlpha;
+                if (p.skipContribution)
+                {
+                    p.skipContribution = false;
+                    continue;
+                }
+            }
+            if (rayDepth == 0)
+            {
+                p.isPrimaryRay = false;
+                outDirect      = p.direct;
+                if (p.misLobeID == DIFFUSE_LOBE)
+                    outDiffuse = p.indirect;
+                else
+                    outGlossy = p.indirect;
+            }
+            else
+            {
+                v3 radiance = p.direct + p.indirect;
+                if (f.indirectBounceClampScale > 0.f)
+                    adjustRadiance(T(f.maxLuminance) * T(f.indirectBounceClampScale), false, radiance);
+                if (p.rayType == DIFFUSE_LOBE)
+                    outDiffuse += radiance;
+                else
+                    outGlossy += radiance;
+            }
+            p.rayType = p.nextRayType;
+        }
+        v3 fin = outDirect + outDiffuse + outGlossy;
+        adjustRadiance(T(f.maxLuminance), f.isDisplayErrorsEnabled != 0, fin);
+        out[0] = fin.x;
+        out[1] = fin.y;
+        out[2] = fin.z;
+        out[3] = outAlpha;
+    }
+};
+
+// Accumulation.glsl:14-34: mix(prev, cur, 1 / (n + 1)) for n > 0, else cur.
+inline void accumulateRunningMean(float* acc, const float* cur, uint32_t sampleIndex)
+{
+    if (sampleIndex == 0)
+    {
+        for (int k = 0; k < 4; k++)
+            acc[k] = cur[k];
+        return;
+    }
+    float t = 1.0f / float(sampleIndex + 1);
+    for (int k = 0; k < 4; k++)
+        acc[k] = acc[k] * (1.0f - t) + cur[k] * t;
+}
+
+// PostProcessing.glsl:37-64
+inline void postProcess(const float* acc, const float brightness[3], bool toneMap, bool gamma,
+    float out[4])
+{
+    V3<float> c(acc[0] * brightness[0], acc[1] * brightness[1], acc[2] * brightness[2]);
+    if (toneMap)
+        c = toneMapACES(c);
+    if (gamma)
+        c = linearTosRGB(clamp3(c, 0.f, 1.f));
+    out[0] = c.x;
+    out[1] = c.y;
+    out[2] = c.z;
+    out[3] = 1.f;
+}
+
+} // namespace orc

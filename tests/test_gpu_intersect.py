@@ -1,0 +1,112 @@
+"""Ray casting on the GPU (two-level BVH2, watertight test) against the oracle's brute-force
+caster: same hit/miss, instance and primitive, same t/u/v bits; no leaks through shared edges."""
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import dev, empty, host
+
+pytestmark = pytest.mark.gpu
+
+
+def random_rays(n, lo, hi, seed):
+    rng = np.random.default_rng(seed)
+    o = rng.uniform(lo, hi, (n, 3))
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r = np.zeros((n, 8), np.float32)
+    r[:, 0:3], r[:, 4:7] = o, d
+    r[:, 3] = np.where(rng.uniform(size=n) < 0.5, 0.0, 0.01)
+    r[:, 7] = np.where(rng.uniform(size=n) < 0.9, np.inf, rng.uniform(1, 30, n))
+    return r
+
+
+def cast_gpu(renderer, rays, any_hit):
+    n = len(rays)
+    dr = dev(rays)
+    tuv = empty((n, 3), torch.float32)
+    ip = empty((n, 2), torch.int32)
+    renderer.intersect(dr.data_ptr(), n, any_hit, tuv.data_ptr(), ip.data_ptr())
+    return host(tuv), host(ip)
+
+
+@pytest.fixture(scope="module")
+def small_scene(agb, oracle):
+    from aurora_gb300 import api, scenes
+    s = scenes.config_small(width=64, height=64, spp=1)
+    r = api.Renderer()
+    r.upload(s)
+    o = oracle.OracleScene(s)
+    yield s, r, o
+    r.close()
+
+
+def test_closest_hits_match_oracle(small_scene):
+    s, r, o = small_scene
+    rays = random_rays(60_000, -14, 14, 3)
+    rays[:, 1] = np.abs(rays[:, 1]) + 0.001  # above the ground
+    g_tuv, g_ip = cast_gpu(r, rays, False)
+    o_tuv, o_ip = o.intersect(rays, any_hit=False, brute=True)
+    assert (g_ip[:, 0] != -2).all(), "traversal stack overflow"
+    hit_g, hit_o = g_ip[:, 0] >= 0, o_ip[:, 0] >= 0
+    assert hit_o.mean() > 0.2
+    np.testing.assert_array_equal(hit_g, hit_o)
+    same = (g_ip == o_ip).all(axis=1)
+    # Exact ties (a ray through a shared edge hits both triangles at the same t) may pick either.
+    tie = ~same & (g_tuv[:, 0] == o_tuv[:, 0])
+    assert (same | tie).all()
+    np.testing.assert_array_equal(g_tuv[hit_o, 0], o_tuv[hit_o, 0])
+    sel = hit_o & same
+    np.testing.assert_array_equal(g_tuv[sel], o_tuv[sel])
+
+
+def test_any_hit_matches_oracle(small_scene):
+    s, r, o = small_scene
+    rays = random_rays(60_000, -14, 14, 4)
+    g_tuv, g_ip = cast_gpu(r, rays, True)
+    o_tuv, o_ip = o.intersect(rays, any_hit=True, brute=True)
+    np.testing.assert_array_equal(g_ip[:, 0] >= 0, o_ip[:, 0] >= 0)
+
+
+def test_empty_and_degenerate_rays(small_scene):
+    s, r, o = small_scene
+    rays = np.zeros((4, 8), np.float32)
+    rays[:, 4:7] = [[0, -1, 0], [0, 0, 1e-30], [1, 0, 0], [0, 1, 0]]
+    rays[:, 0:3] = [[0, 50, 0], [0, 1, 0], [-100, 1, 0], [0, 5, 0]]
+    rays[:, 7] = np.inf
+    rays[3, 3], rays[3, 7] = 2.0, 1.0  # tmin > tmax: no hit
+    g_tuv, g_ip = cast_gpu(r, rays, False)
+    o_tuv, o_ip = o.intersect(rays, any_hit=False, brute=True)
+    np.testing.assert_array_equal(g_ip[:, 0] >= 0, o_ip[:, 0] >= 0)
+    assert g_ip[3, 0] == -1
+    g_tuv0, g_ip0 = cast_gpu(r, np.zeros((0, 8), np.float32), False)
+    assert g_ip0.shape == (0, 2)
+
+
+def test_watertight_no_leaks_through_shared_edges_and_vertices(agb, oracle):
+    from aurora_gb300 import api, scenes
+    s = scenes.SceneDesc("ico")
+    p, n, uv, idx = scenes.icosphere(5, radius=3.0, displacement=0.0)
+    s.add_mesh(p, n, uv, idx)
+    s.materials = scenes.materials(1)
+    s.instances.append(dict(mesh=0, material=0, xform=scenes.translation(0.3, -0.2, 0.1), layers=[]))
+    s.width = s.height = 8
+    s.frame = scenes.frame_data(np.eye(4), scenes.perspective(45, 1))
+    with api.Renderer() as r:
+        r.upload(s)
+        tri = idx.reshape(-1, 3)
+        # Rays from the centre of the sphere through every vertex and every edge midpoint: each
+        # must hit the closed surface.
+        targets = np.concatenate([p, 0.5 * (p[tri[:, 0]] + p[tri[:, 1]])])
+        org = np.array([0.3, -0.2, 0.1], np.float32)
+        d = targets / np.linalg.norm(targets, axis=1, keepdims=True)
+        rays = np.zeros((len(d), 8), np.float32)
+        rays[:, 0:3] = org
+        rays[:, 4:7] = d
+        rays[:, 7] = np.inf
+        g_tuv, g_ip = cast_gpu(r, rays, False)
+        assert (g_ip[:, 0] >= 0).all(), f"{(g_ip[:, 0] < 0).sum()} rays leaked"
+        o = oracle.OracleScene(s)
+        o_tuv, o_ip = o.intersect(rays, any_hit=False, brute=True)
+        assert (o_ip[:, 0] >= 0).all()
+        np.testing.assert_array_equal(g_tuv[:, 0], o_tuv[:, 0])

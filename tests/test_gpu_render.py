@@ -1,0 +1,95 @@
+"""Whole-path parity: the wavefront renderer against the oracle's restatement of the ray-gen /
+closest-hit / miss shaders at equal samples (the same PCG2D streams), plus progressive
+accumulation, Kahan accumulation and host-side error handling."""
+import numpy as np
+import pytest
+
+from aurora_gb300 import _abi
+
+pytestmark = pytest.mark.gpu
+
+
+def render_both(oracle, s, spp, precision=32, max_paths=0):
+    from aurora_gb300 import api
+    with api.Renderer() as r:
+        r.upload(s)
+        r.render(0, spp, max_paths=max_paths)
+        g = r.read(_abi.ACCUM_RUNNING_MEAN)
+        gk = r.read(_abi.ACCUM_KAHAN)
+    o = oracle.OracleScene(s).render(0, spp, precision=precision, want_sum=True)
+    return g, gk, o
+
+
+def test_tiny_scene_all_features_matches_oracle(agb, oracle):
+    from aurora_gb300 import scenes
+    s = scenes.config_tiny(width=48, height=32, spp=8)
+    g, gk, o = render_both(oracle, s, 8)
+    err = oracle.rel_mse(g, o["mean"])
+    print("tiny relMSE vs FP32 oracle", err)
+    assert err < 1e-6
+    assert np.abs(g[..., 3] - o["mean"][..., 3]).max() == 0.0
+    # Kahan sum / n agrees with the running mean.
+    assert oracle.rel_mse(gk, o["sum"] / 8) < 1e-9
+
+
+def test_small_config_matches_oracle(agb, oracle):
+    from aurora_gb300 import scenes
+    s = scenes.config_small(width=96, height=96, spp=4)
+    g, gk, o = render_both(oracle, s, 4)
+    err = oracle.rel_mse(g, o["mean"])
+    print("small relMSE vs FP32 oracle", err)
+    assert err < 1e-6
+    o64 = __import__("pyoracle").OracleScene(s).render(0, 4, precision=64)
+    err64 = oracle.rel_mse(g, o64["mean"])
+    print("small relMSE vs FP64 oracle", err64)
+    assert err64 < 1e-3
+
+
+def test_layered_decals_match_oracle(agb, oracle):
+    from aurora_gb300 import scenes
+    s = scenes.config_layered(width=64, height=48, spp=2, blas=2, instances=6,
+                              tri_range=(200, 1000), decal_size=64)
+    g, gk, o = render_both(oracle, s, 2)
+    err = oracle.rel_mse(g, o["mean"])
+    print("layered relMSE vs FP32 oracle", err)
+    assert err < 1e-6
+
+
+def test_wave_split_and_progressive_resume_are_exact(agb):
+    from aurora_gb300 import api, scenes
+    s = scenes.config_tiny(width=40, height=30, spp=6)
+    with api.Renderer() as r:
+        r.upload(s)
+        r.render(0, 6)
+        a = r.read(_abi.ACCUM_RUNNING_MEAN)
+        r.render(0, 6, max_paths=40 * 30)  # one sample per wave
+        b = r.read(_abi.ACCUM_RUNNING_MEAN)
+        r.render(0, 2)
+        r.render(2, 4)
+        c = r.read(_abi.ACCUM_RUNNING_MEAN)
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(a, c)
+
+
+def test_invalid_inputs_are_rejected(agb):
+    from aurora_gb300 import api, scenes
+    s = scenes.config_tiny()
+    with api.Renderer() as r:
+        m = s.meshes[0]
+        bad = m["indices"].copy()
+        bad[5] = len(m["positions"])
+        with pytest.raises(_abi.AgbError):
+            import ctypes
+            g = ctypes.c_int32()
+            _abi.check(r._lib.agb_geometry_create(r.ctx, _abi.ptr(m["positions"]), None, None,
+                                                  _abi.ptr(bad), len(m["positions"]), len(bad),
+                                                  ctypes.byref(g)))
+        r.upload(s)
+        f = np.asarray(s.frame).copy()
+        f["is_force_opaque_shadows_enabled"] = 0
+        r.set_frame(f)
+        with pytest.raises(_abi.AgbError):
+            r.render(0, 1)
+        r.set_frame(s.frame)
+        with pytest.raises(_abi.AgbError):
+            r.render(5, 1)  # does not continue the accumulated sequence
