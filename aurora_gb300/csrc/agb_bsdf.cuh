@@ -60,7 +60,7 @@ AGB_D v3 sampleUniformDirection(v2 r, float& pdf)
     float sinTheta = sqrtf(1.f - cosTheta * cosTheta);
     float phi      = 2.f * kPi * r.x;
     float s, c;
-    sincosf(phi, &s, &c);
+    agb_fm::sincos(phi, &s, &c);
     pdf = divPi(0.25f);
     return v3{ sinTheta * c, sinTheta * s, cosTheta };
 }
@@ -85,7 +85,7 @@ AGB_D v3 sampleCone(v2 r, v3 dir, float cosThetaMax)
     float sinTheta = sqrtf(1.f - cosTheta * cosTheta);
     float phi      = r.y * 2.f * kPi;
     float s, c;
-    sincosf(phi, &s, &c);
+    agb_fm::sincos(phi, &s, &c);
     return xb * c * sinTheta + yb * s * sinTheta + dir * cosTheta;
 }
 AGB_D v2 sampleDisk(v2 r, float radius)
@@ -93,7 +93,7 @@ AGB_D v2 sampleDisk(v2 r, float radius)
     float rr  = radius * sqrtf(r.x);
     float phi = 2.f * kPi * r.y;
     float s, c;
-    sincosf(phi, &s, &c);
+    agb_fm::sincos(phi, &s, &c);
     return v2{ c * rr, s * rr };
 }
 AGB_D float misWeight(float f, float g) { return (f * f) / (f * f + g * g); }
@@ -130,7 +130,7 @@ AGB_D v3 sampleGGXVNDF(v3 V, v2 a, v2 r)
     float rr  = sqrtf(r.x);
     float phi = 2.f * kPi * r.y;
     float s, c;
-    sincosf(phi, &s, &c);
+    agb_fm::sincos(phi, &s, &c);
     float t1 = rr * c;
     float t2 = rr * s;
     float sv = 0.5f * (1.f + Vh.z);
@@ -202,7 +202,7 @@ AGB_D v2 dirAlbedoAB(float NdotV, float roughness)
     float r1 = roughness * -0.0275f + 0.0425f;
     float r2 = roughness * -0.572f + 1.04f;
     float r3 = roughness * 0.022f + -0.04f;
-    float a004 = fminf_(r0 * r0, exp2f(-9.28f * NdotV)) * r0 + r1;
+    float a004 = fminf_(r0 * r0, agb_fm::exp2(-9.28f * NdotV)) * r0 + r1;
     return v2{ -1.04f * a004 + r2, 1.04f * a004 + r3 };
 }
 AGB_D float dirAlbedo(float NdotV, float roughness, float F0, float F90)
@@ -287,7 +287,7 @@ AGB_D float sheenNDF(float cosTheta, float roughness)
 {
     float inv  = 1.f / roughness;
     float sin2 = 1.f - cosTheta * cosTheta;
-    return (2.f + inv) * powf(sin2, inv * 0.5f) / (2.f * kPi);
+    return (2.f + inv) * agb_fm::pow(sin2, inv * 0.5f) / (2.f * kPi);
 }
 AGB_D float sheenAlbedo(float cosTheta, float roughness)
 {
@@ -349,7 +349,7 @@ AGB_D v3 rotateVector(v3 v, float degrees, v3 axis)
     float ang = degrees * (kPi / 180.f);
     axis      = normalize(axis);
     float s, c;
-    sincosf(ang, &s, &c);
+    agb_fm::sincos(ang, &s, &c);
     float oc = 1.f - c;
     v3 r0    = v3{ oc * axis.x * axis.x + c, oc * axis.x * axis.y - axis.z * s,
         oc * axis.z * axis.x + axis.y * s };

@@ -6,6 +6,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "agb_fmath.h"
+
 #define AGB_HD __host__ __device__ __forceinline__
 #define AGB_D __device__ __forceinline__
 
@@ -80,7 +82,7 @@ AGB_HD v3 max3(v3 v, float lo)
     return v3{ v.x > lo ? v.x : lo, v.y > lo ? v.y : lo, v.z > lo ? v.z : lo };
 }
 AGB_HD v3 sqrt3(v3 v) { return v3{ sqrtf(v.x), sqrtf(v.y), sqrtf(v.z) }; }
-AGB_HD v3 pow3(v3 v, float e) { return v3{ powf(v.x, e), powf(v.y, e), powf(v.z, e) }; }
+AGB_HD v3 pow3(v3 v, float e) { return v3{ agb_fm::pow(v.x, e), agb_fm::pow(v.y, e), agb_fm::pow(v.z, e) }; }
 AGB_HD v3 abs3(v3 v) { return v3{ fabsf(v.x), fabsf(v.y), fabsf(v.z) }; }
 AGB_HD bool isBlack(v3 c) { return c.x == 0.f && c.y == 0.f && c.z == 0.f; }
 AGB_HD v3 reflect(v3 i, v3 n) { return i - n * (2.f * dot(n, i)); }

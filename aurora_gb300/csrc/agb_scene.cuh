@@ -125,16 +125,16 @@ AGB_D float4 sampleImage(const DevImage& im, v2 uv)
 // --------------------------------------------------------------------------- environment
 AGB_D v2 dirToLatLong(v3 d)
 {
-    return v2{ ((atan2f(d.x, -d.z) * 1.0f) / kPi) * 0.5f + 0.5f,
-        ((-asinf(d.y)) * 1.0f) / kPi + 0.5f };
+    return v2{ ((agb_fm::atan2(d.x, -d.z) * 1.0f) / kPi) * 0.5f + 0.5f,
+        ((-agb_fm::asin(d.y)) * 1.0f) / kPi + 0.5f };
 }
 AGB_D v3 latLongToDir(v2 uv)
 {
     float phi   = (uv.x + 0.25f) * 2.f * kPi;
     float theta = uv.y * kPi;
     float sp, cp, st, ct;
-    sincosf(phi, &sp, &cp);
-    sincosf(theta, &st, &ct);
+    agb_fm::sincos(phi, &sp, &cp);
+    agb_fm::sincos(theta, &st, &ct);
     return v3{ cp * st, ct, sp * st };
 }
 AGB_D v3 mulDir(const float* m, v3 d)
@@ -276,7 +276,7 @@ AGB_D v2 uvTransform(v2 uv, const float* pivot, const float* scale, float rotate
     v2 sc  = v2{ sub.x / scale[0], sub.y / scale[1] };
     float r = rotate * (kPi / 180.f);
     float sa, ca;
-    sincosf(r, &sa, &ca);
+    agb_fm::sincos(r, &sa, &ca);
     v2 rot = v2{ ca * sc.x + sa * sc.y, -sa * sc.x + ca * sc.y };
     return v2{ (rot.x - offset[0]) + pivot[0], (rot.y - offset[1]) + pivot[1] };
 }

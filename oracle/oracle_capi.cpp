@@ -366,3 +366,37 @@ ORC_API void orc_post_process(const float* accum, int64_t pixels, const float* b
     for (int64_t i = 0; i < pixels; i++)
         postProcess(accum + 4 * i, brightness, toneMap != 0, gamma != 0, out + 4 * i);
 }
+
+// The single-precision transcendentals the FP32 instantiation uses (agb_fmath.h), for the
+// accuracy test against double-precision libm.  which: 0 sin, 1 cos, 2 exp2, 3 log2, 4 pow(x, y),
+// 5 atan2(x, y), 6 asin.
+ORC_API void orc_fmath(int which, const float* x, const float* y, int64_t n, float* out)
+{
+    for (int64_t i = 0; i < n; i++)
+    {
+        switch (which)
+        {
+        case 0:
+            out[i] = agb_fm::sin(x[i]);
+            break;
+        case 1:
+            out[i] = agb_fm::cos(x[i]);
+            break;
+        case 2:
+            out[i] = agb_fm::exp2(x[i]);
+            break;
+        case 3:
+            out[i] = agb_fm::log2(x[i]);
+            break;
+        case 4:
+            out[i] = agb_fm::pow(x[i], y[i]);
+            break;
+        case 5:
+            out[i] = agb_fm::atan2(x[i], y[i]);
+            break;
+        default:
+            out[i] = agb_fm::asin(x[i]);
+            break;
+        }
+    }
+}

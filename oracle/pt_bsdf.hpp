@@ -109,7 +109,7 @@ struct BSDF
         T cosTheta = T(1) - T(2) * random[1];
         T sinTheta = std::sqrt(T(1) - cosTheta * cosTheta);
         T phi      = T(2) * PI * random[0];
-        v3 dir(sinTheta * std::cos(phi), sinTheta * std::sin(phi), cosTheta);
+        v3 dir(sinTheta * tcos(phi), sinTheta * tsin(phi), cosTheta);
         pdf = divPi(T(0.25f));
         return dir;
     }
@@ -136,14 +136,14 @@ struct BSDF
         T cosTheta = (T(1) - random[0]) + random[0] * cosThetaMax;
         T sinTheta = std::sqrt(T(1) - cosTheta * cosTheta);
         T phi      = random[1] * T(2) * PI;
-        return xb * std::cos(phi) * sinTheta + yb * std::sin(phi) * sinTheta + direction * cosTheta;
+        return xb * tcos(phi) * sinTheta + yb * tsin(phi) * sinTheta + direction * cosTheta;
     }
     // Sampling.slang:87-93
     static v2 sampleDisk(v2 random, T radius)
     {
         T r   = radius * std::sqrt(random[0]);
         T phi = T(2) * PI * random[1];
-        return v2(std::cos(phi), std::sin(phi)) * r;
+        return v2(tcos(phi), tsin(phi)) * r;
     }
     // Sampling.slang:98-104 (power heuristic with n = 1)
     static T computeMISWeight(T fPDF, T gPDF)
@@ -214,8 +214,8 @@ struct BSDF
         v3 T2    = cross(Vh, T1);
         T r      = std::sqrt(random.x);
         T phi    = T(2) * PI * random.y;
-        T t1     = r * std::cos(phi);
-        T t2     = r * std::sin(phi);
+        T t1     = r * tcos(phi);
+        T t2     = r * tsin(phi);
         T s      = T(0.5f) * (T(1) + Vh.z);
         t2       = (T(1) - s) * std::sqrt(T(1) - t1 * t1) + s * t2;
         v3 Nh    = T1 * t1 + T2 * t2 + Vh * std::sqrt(fmax_(T(0), T(1) - t1 * t1 - t2 * t2));
@@ -297,7 +297,7 @@ struct BSDF
         T r[4];
         for (int i = 0; i < 4; i++)
             r[i] = roughness * c0[i] + c1[i];
-        T a004 = fmin_(r[0] * r[0], std::exp2(T(-9.28f) * NdotV)) * r[0] + r[1];
+        T a004 = fmin_(r[0] * r[0], texp2(T(-9.28f) * NdotV)) * r[0] + r[1];
         T ABx  = T(-1.04f) * a004 + r[2];
         T ABy  = T(1.04f) * a004 + r[3];
         return F0 * ABx + F90 * ABy;
@@ -387,7 +387,7 @@ struct BSDF
         T invR = T(1) / roughness;
         T cos2 = cosTheta * cosTheta;
         T sin2 = T(1) - cos2;
-        return (T(2) + invR) * std::pow(sin2, invR * T(0.5f)) / (T(2) * PI);
+        return (T(2) + invR) * tpow(sin2, invR * T(0.5f)) / (T(2) * PI);
     }
     static T mx_imageworks_sheen_directional_albedo(T cosTheta, T roughness)
     {
@@ -449,8 +449,8 @@ struct BSDF
     {
         T angle = amountDegrees * (PI / T(180));
         axis    = normalize(axis);
-        T s     = std::sin(angle);
-        T c     = std::cos(angle);
+        T s     = tsin(angle);
+        T c     = tcos(angle);
         T oc    = T(1) - c;
         T r0[3] = { oc * axis.x * axis.x + c, oc * axis.x * axis.y - axis.z * s,
             oc * axis.z * axis.x + axis.y * s };

@@ -68,8 +68,8 @@ struct Env
     static v2 directionToLatLongUV(const v3& d)
     {
         v2 uv;
-        uv.x = ((std::atan2(d.x, -d.z) * T(1)) / PI) * T(0.5f) + T(0.5f);
-        uv.y = ((-std::asin(d.y)) * T(1)) / PI + T(0.5f);
+        uv.x = ((tatan2(d.x, -d.z) * T(1)) / PI) * T(0.5f) + T(0.5f);
+        uv.y = ((-tasin(d.y)) * T(1)) / PI + T(0.5f);
         return uv;
     }
     // Environment.slang:46-59
@@ -77,7 +77,7 @@ struct Env
     {
         T phi   = (uv.x + T(0.25f)) * T(2) * PI;
         T theta = uv.y * PI;
-        return v3(std::cos(phi) * std::sin(theta), std::cos(theta), std::sin(phi) * std::sin(theta));
+        return v3(tcos(phi) * tsin(theta), tcos(theta), tsin(phi) * tsin(theta));
     }
     static v3 mulDir(const float* m, const v3& d)
     {

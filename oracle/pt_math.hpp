@@ -11,8 +11,27 @@
 #include <cstdint>
 #include <cstring>
 
+// The FP32 instantiation uses the product's own transcendental functions (plain IEEE arithmetic,
+// identical bits on host and device) so that FP32 parity checks compare the shading algebra and
+// not two libm implementations; the FP64 instantiation uses the C++ standard library and is the
+// accuracy reference.  agb_fmath.h's accuracy is checked against FP64 libm by the tests.
+#include "../aurora_gb300/csrc/agb_fmath.h"
+
 namespace orc
 {
+
+inline float tsin(float x) { return agb_fm::sin(x); }
+inline float tcos(float x) { return agb_fm::cos(x); }
+inline float tpow(float x, float y) { return agb_fm::pow(x, y); }
+inline float texp2(float x) { return agb_fm::exp2(x); }
+inline float tatan2(float y, float x) { return agb_fm::atan2(y, x); }
+inline float tasin(float x) { return agb_fm::asin(x); }
+inline double tsin(double x) { return std::sin(x); }
+inline double tcos(double x) { return std::cos(x); }
+inline double tpow(double x, double y) { return std::pow(x, y); }
+inline double texp2(double x) { return std::exp2(x); }
+inline double tatan2(double y, double x) { return std::atan2(y, x); }
+inline double tasin(double x) { return std::asin(x); }
 
 template <class T>
 struct V2
@@ -159,7 +178,7 @@ inline V3<T> sqrt3(const V3<T>& v)
 template <class T>
 inline V3<T> pow3(const V3<T>& v, T e)
 {
-    return V3<T>(std::pow(v.x, e), std::pow(v.y, e), std::pow(v.z, e));
+    return V3<T>(tpow(v.x, e), tpow(v.y, e), tpow(v.z, e));
 }
 template <class T>
 inline V3<T> abs3(const V3<T>& v)

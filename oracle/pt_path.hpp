@@ -220,7 +220,7 @@ struct PathTracer
         v2 sub = uv - p;
         v2 scaled(sub.x / T(scale[0]), sub.y / T(scale[1]));
         T r  = T(rotate) * (Consts<T>::PI / T(180));
-        T sa = std::sin(r), ca = std::cos(r);
+        T sa = tsin(r), ca = tcos(r);
         v2 rot(ca * scaled.x + sa * scaled.y, -sa * scaled.x + ca * scaled.y);
         v2 tr(rot.x - T(offset[0]), rot.y - T(offset[1]));
         return tr + p;

@@ -46,6 +46,7 @@ def lib():
         L.orc_tracer_create.argtypes = [ctypes.c_int, P, P, ctypes.c_uint32, ctypes.c_uint32,
                                         ctypes.c_int]
         L.orc_tracer_destroy.argtypes = [P]
+        L.orc_fmath.argtypes = [ctypes.c_int, P, P, ctypes.c_int64, P]
         L.orc_tracer_render.restype = ctypes.c_double
         L.orc_tracer_render.argtypes = [P, P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, P, P,
                                         P, P, P]
@@ -273,6 +274,16 @@ def post_process(accum, brightness=(1.0, 1.0, 1.0), tone_map=False, gamma=True):
     b = np.asarray(brightness, np.float32)
     lib().orc_post_process(_p(a), a.size // 4, _p(b), 1 if tone_map else 0, 1 if gamma else 0,
                            _p(out))
+    return out
+
+
+def fmath(which, x, y=None):
+    """Evaluates one of agb_fmath.h's functions (0 sin, 1 cos, 2 exp2, 3 log2, 4 pow, 5 atan2,
+    6 asin) on float32 inputs."""
+    x = np.ascontiguousarray(x, np.float32)
+    y = None if y is None else np.ascontiguousarray(y, np.float32)
+    out = np.zeros_like(x)
+    lib().orc_fmath(which, _p(x), _p(y), len(x), _p(out))
     return out
 
 
