@@ -114,7 +114,9 @@ def alias_build(rgb, precision=32):
 class OracleScene:
     """Holds the oracle-side copy of a SceneDesc (and keeps its buffers alive)."""
 
-    def __init__(self, s):
+    def __init__(self, s, alias=None, integral=None):
+        """alias / integral: an environment table to sample with instead of the reference's
+        (the device's table makes the two renders sample-identical)."""
         self.desc = s
         self._keep = []
         meshes = (Mesh * len(s.meshes))()
@@ -153,7 +155,10 @@ class OracleScene:
         if s.env_light >= 0:
             light = s.images[s.env_light]
             src = light["pixels"][..., :3] if light["format"] != 0 else rgba[s.env_light][..., :3]
-            self.alias, integral = alias_build(np.ascontiguousarray(src, np.float32))
+            if alias is None:
+                self.alias, integral = alias_build(np.ascontiguousarray(src, np.float32))
+            else:
+                self.alias = np.ascontiguousarray(alias).copy()
             self.env["light_tex_luminance_integral"] = integral
             self.env["has_light_tex"] = 1
         self.env["has_background_tex"] = 1 if s.env_background >= 0 else 0
