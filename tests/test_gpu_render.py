@@ -49,19 +49,24 @@ def test_small_config_matches_oracle(agb, oracle):
     assert err64 < 1e-4
 
 
-def test_converged_image_matches_fp64_oracle_with_reference_table(agb, oracle):
-    """Same estimator, independent environment samples: the device table (FP64 prefix sums)
-    against the reference's FP32 sequential table, both converged at 1024 spp."""
+def test_device_table_is_unbiased_against_reference_table(agb, oracle):
+    """Same estimator, independent environment samples: the device table (FP64 prefix sums) and
+    the reference's FP32 sequential table, 4096 spp each.  Their difference must sit inside the
+    Monte Carlo noise floor measured between two independent reference-table renders."""
     from aurora_gb300 import api, scenes
-    s = scenes.config_tiny(width=16, height=12, spp=1024, lights=False)
+    spp = 4096
+    s = scenes.config_tiny(width=16, height=12, spp=spp, lights=False)
     with api.Renderer() as r:
         r.upload(s)
-        r.render(0, 1024)
+        r.render(0, spp)
         g = r.read(_abi.ACCUM_KAHAN)
-    o = oracle.OracleScene(s).render(0, 1024, precision=64, want_sum=True)
-    err = oracle.rel_mse(g, o["sum"] / 1024)
-    print("converged relMSE (device table vs reference table, FP64 oracle)", err)
-    assert err < 1e-3
+    o = oracle.OracleScene(s)
+    a = o.render(0, spp, precision=64, want_sum=True)["sum"] / spp
+    b = o.render(spp, spp, precision=64, want_sum=True)["sum"] / spp
+    err = oracle.rel_mse(g, a)
+    floor = oracle.rel_mse(a, b)
+    print(f"device vs reference table relMSE {err:.3g}; noise floor {floor:.3g}")
+    assert err < 1.5 * floor
 
 
 def test_layered_decals_match_oracle(agb, oracle):
