@@ -22,6 +22,8 @@ ACCUM_KAHAN = 2
 FORMAT_RGBA8 = 0
 FORMAT_RGBA32F = 1
 FORMAT_RGB32F = 2
+ENV_TABLE_REFERENCE = 0
+ENV_TABLE_FP64 = 1
 TEX_BASE_COLOR, TEX_SPECULAR_ROUGHNESS, TEX_OPACITY, TEX_NORMAL, TEX_EMISSION = range(5)
 
 
@@ -136,7 +138,9 @@ SIGNATURES = {
     "agb_materials_set": (_I32, [_P, _P, _P, _U32]),
     "agb_instances_set": (_I32, [_P, _P, _U32]),
     "agb_environment_set": (_I32, [_P, _P, _I32, _I32]),
-    "agb_environment_alias": (_I32, [_P, _P, _U64, ctypes.POINTER(ctypes.c_double)]),
+    "agb_environment_alias": (_I32, [_P, _P, _U64, ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(ctypes.c_double)]),
+    "agb_set_environment_table": (_I32, [_P, _I32]),
     "agb_frame_set": (_I32, [_P, _P]),
     "agb_render": (_I32, [_P, ctypes.POINTER(RenderOptions), _U32, _U32, ctypes.POINTER(RenderStats)]),
     "agb_wait": (_I32, [_P]),

@@ -141,13 +141,22 @@ class Renderer:
         check(self._lib.agb_context_memory(self.ctx, ctypes.byref(b)))
         return b.value
 
-    def environment_alias(self):
+    def set_environment_table(self, layout):
+        """_abi.ENV_TABLE_REFERENCE (default) or _abi.ENV_TABLE_FP64; applies to the next upload."""
+        check(self._lib.agb_set_environment_table(self.ctx, layout))
+
+    def environment_alias(self, fp64_integral=False):
+        """(table, integral the shading divides by[, FP64 integral])."""
         s = self.scene
         im = s.images[s.env_light]
         n = im["width"] * im["height"]
         out = np.zeros(n, dtype=_abi.ALIAS_DTYPE)
         integral = ctypes.c_double()
-        check(self._lib.agb_environment_alias(self.ctx, ptr(out), n, ctypes.byref(integral)))
+        i64 = ctypes.c_double()
+        check(self._lib.agb_environment_alias(self.ctx, ptr(out), n, ctypes.byref(integral),
+                                              ctypes.byref(i64)))
+        if fp64_integral:
+            return out, integral.value, i64.value
         return out, integral.value
 
     # ------------------------------------------------------------- unit entry points (device)

@@ -125,7 +125,9 @@ struct agb_context
     int32_t envLight = -1, envBackground = -1;
     DevBuf alias;
     EnvBuildScratch envScratch;
-    double envIntegral = 0.0;
+    double envIntegral     = 0.0; // FP64 luminance integral
+    double envShadingIntegral = 0.0;
+    int32_t envLayout      = AGB_ENV_TABLE_REFERENCE;
 
     agb_frame_data frame{};
     bool frameSet = false;
@@ -683,18 +685,43 @@ AGB_API agb_status agb_environment_set(agb_context* ctx, const agb_environment_d
         if (n >= (1ull << 31))
             return fail(AGB_ERR_LIMIT, "agb_environment_set: light image too large");
         AGB_CUDA(ctx->alias.ensure(n * sizeof(agb_alias_entry)), "allocate alias table");
+        // Per-row solid angles exactly as the reference computes them on the host
+        // (AliasMap.cpp:101-110): FP32 increments, FP32 running latitude, float sin.
+        std::vector<float> rowSA(v.height);
+        {
+            const double kPi   = 3.14159265358979323846;
+            float lonIncrement = static_cast<float>(2.0f * kPi / v.width);
+            float latIncrement = static_cast<float>(kPi / v.height);
+            float latAngle     = static_cast<float>(kPi / 2.0);
+            for (uint32_t y = 0; y < v.height; y++)
+            {
+                rowSA[y] = (std::sin(latAngle) - std::sin(latAngle - latIncrement)) * lonIncrement;
+                latAngle -= latIncrement;
+            }
+        }
         double integral = 0.0;
-        AGB_CUDA(buildEnvAlias(static_cast<const float4*>(v.data), v.width, v.height,
-                     ctx->alias.as<agb_alias_entry>(), &integral, ctx->envScratch, ctx->stream),
+        float shadingIntegral = 0.f;
+        AGB_CUDA(buildEnvAlias(static_cast<const float4*>(v.data), v.width, v.height, ctx->envLayout,
+                     rowSA.data(), ctx->alias.as<agb_alias_entry>(), &integral, &shadingIntegral,
+                     ctx->envScratch, ctx->stream),
             "build environment alias table");
-        ctx->envIntegral = integral;
-        ctx->env.light_tex_luminance_integral = float(integral);
+        ctx->envIntegral        = integral;
+        ctx->envShadingIntegral = shadingIntegral;
+        ctx->env.light_tex_luminance_integral = shadingIntegral;
     }
     return AGB_OK;
 }
 
+AGB_API agb_status agb_set_environment_table(agb_context* ctx, int32_t layout)
+{
+    if (!ctx || (layout != AGB_ENV_TABLE_REFERENCE && layout != AGB_ENV_TABLE_FP64))
+        return fail(AGB_ERR_INVALID_ARG, "agb_set_environment_table: bad layout");
+    ctx->envLayout = layout;
+    return AGB_OK;
+}
+
 AGB_API agb_status agb_environment_alias(agb_context* ctx, agb_alias_entry* host_out,
-    uint64_t capacity, double* integral)
+    uint64_t capacity, double* shading_integral, double* fp64_integral)
 {
     if (!ctx || ctx->envLight < 0)
         return fail(AGB_ERR_NOT_READY, "agb_environment_alias: no light image");
@@ -709,8 +736,10 @@ AGB_API agb_status agb_environment_alias(agb_context* ctx, agb_alias_entry* host
                  cudaMemcpyDeviceToHost, ctx->stream),
         "read alias table");
     AGB_CUDA(cudaStreamSynchronize(ctx->stream), "read alias table");
-    if (integral)
-        *integral = ctx->envIntegral;
+    if (shading_integral)
+        *shading_integral = ctx->envShadingIntegral;
+    if (fp64_integral)
+        *fp64_integral = ctx->envIntegral;
     return AGB_OK;
 }
 

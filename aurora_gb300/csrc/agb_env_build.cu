@@ -294,46 +294,244 @@ __global__ void k_env_alias(const double* p, const float* lum, uint32_t n, const
     out[i] = e;
 }
 
+// ---------------------------------------------------------------- reference table layout
+// The reference's table (AliasMap.cpp:71-166) rebuilt bit for bit: FP32 luminance x row solid
+// angle (row angles from the host, as the reference computes them), FP32 sequential integral, the
+// same index map (below-average texels first in index order, the others from the end), and the
+// same sequential sweep.  The sweep is inherently sequential; one warp runs it, lanes prefetching
+// the next windows of the small and large queues into shared memory while lane 0 consumes them.
+
+__global__ void k_ref_lum(const float4* rgba, uint32_t width, uint32_t n, const float* rowSA,
+    float* lum, float* lumArea)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    float4 c = rgba[i];
+    float l  = __fadd_rn(__fadd_rn(__fmul_rn(c.x, 0.2125f), __fmul_rn(c.y, 0.7154f)),
+        __fmul_rn(c.z, 0.0721f));
+    lum[i]     = l;
+    lumArea[i] = __fmul_rn(rowSA[i / width], l);
+}
+
+// One warp: FP32 sum of v[0, n) in index order, as a sequential loop would compute it.
+__global__ void k_ref_seq_sum(const float* v, uint32_t n, float* out)
+{
+    constexpr uint32_t kChunk = 4096;
+    __shared__ float buf[kChunk];
+    int lane  = threadIdx.x;
+    float acc = 0.f;
+    for (uint32_t base = 0; base < n; base += kChunk)
+    {
+        uint32_t cnt = n - base < kChunk ? n - base : kChunk;
+        for (uint32_t k = lane; k < cnt; k += 32)
+            buf[k] = v[base + k];
+        __syncwarp();
+        if (lane == 0)
+            for (uint32_t k = 0; k < cnt; k++)
+                acc = __fadd_rn(acc, buf[k]);
+        __syncwarp();
+    }
+    if (lane == 0)
+        *out = acc;
+}
+
+__global__ void k_ref_probs(const float* lum, const float* lumArea, uint32_t n,
+    const float* integral, float* prob, float* pdf, uint32_t* alias, uint32_t* tileSmall)
+{
+    uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    float I       = *integral;
+    float average = __fdiv_rn(I, float(n));
+    uint32_t smalls = 0;
+    for (int q = 0; q < kScanItems; q++)
+    {
+        uint32_t i = base + q;
+        if (i >= n)
+            break;
+        float pr = __fdiv_rn(lumArea[i], average);
+        prob[i]  = pr;
+        pdf[i]   = __fdiv_rn(lum[i], I);
+        alias[i] = i;
+        smalls += pr < 1.f ? 1u : 0u;
+    }
+    double t;
+    blockExclusiveScan(double(smalls), t);
+    if (threadIdx.x == 0)
+        tileSmall[blockIdx.x] = uint32_t(t);
+}
+
+__global__ void k_ref_index(const float* prob, uint32_t n, const uint32_t* tileSmallExcl,
+    uint32_t* indexMap)
+{
+    uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    uint32_t smalls = 0;
+    bool isSmall[kScanItems];
+    for (int q = 0; q < kScanItems; q++)
+    {
+        uint32_t i = base + q;
+        isSmall[q] = i < n && prob[i] < 1.f;
+        smalls += isSmall[q] ? 1u : 0u;
+    }
+    double t;
+    uint32_t before = uint32_t(blockExclusiveScan(double(smalls), t)) + tileSmallExcl[blockIdx.x];
+    for (int q = 0; q < kScanItems; q++)
+    {
+        uint32_t i = base + q;
+        if (i >= n)
+            break;
+        if (isSmall[q])
+            indexMap[before++] = i;
+        else
+            indexMap[n - 1 - (i - before)] = i; // k-th large (index order) at position n-1-k
+    }
+}
+
+// The sweep: for (sml = 0; sml < lrg && lrg < n; sml++) pair indexMap[sml] with indexMap[lrg].
+__global__ void k_ref_sweep(const uint32_t* indexMap, float* prob, uint32_t* alias, uint32_t n,
+    const uint32_t* smallCount)
+{
+    constexpr int kWin = 256; // queue window per batch (8 entries per lane)
+    __shared__ uint32_t sIdx[kWin], lIdx[kWin];
+    __shared__ float sProb[kWin], lProb[kWin];
+    __shared__ uint8_t sFinal[kWin];
+    __shared__ uint32_t st[3]; // sml, lrg, done
+    int lane = threadIdx.x;
+    uint32_t S = *smallCount;
+    uint32_t curLarge = 0;
+    float w = 0.f;
+    if (lane == 0)
+    {
+        st[0] = 0;
+        st[1] = S;
+        st[2] = (S == 0 || S >= n) ? 1u : 0u;
+        if (!st[2])
+        {
+            curLarge = indexMap[S];
+            w        = prob[curLarge];
+        }
+    }
+    __syncwarp();
+    while (!st[2])
+    {
+        uint32_t sml = st[0], lrg = st[1];
+        // Prefetch the small-queue window [sml, sml + kWin) and the large-queue window
+        // (lrg, lrg + kWin].  Small entries below S never change; entries at positions in
+        // [S, lrg) are larges already exhausted, whose probability is final.
+        for (int k = lane; k < kWin; k += 32)
+        {
+            uint32_t ps = sml + uint32_t(k);
+            if (ps < n)
+            {
+                uint32_t idx = indexMap[ps];
+                sIdx[k]      = idx;
+                bool fin     = ps < S || ps < lrg;
+                sFinal[k]    = fin ? 1 : 0;
+                sProb[k]     = fin ? prob[idx] : 0.f;
+            }
+            uint32_t pl = lrg + 1u + uint32_t(k);
+            if (pl < n)
+            {
+                uint32_t idx = indexMap[pl];
+                lIdx[k]      = idx;
+                lProb[k]     = prob[idx]; // untouched until it becomes the current large
+            }
+        }
+        __syncwarp();
+        if (lane == 0)
+        {
+            int si = 0, li = 0;
+            while (si < kWin && li < kWin)
+            {
+                if (!(sml < lrg && lrg < n))
+                {
+                    st[2] = 1;
+                    break;
+                }
+                uint32_t small = sIdx[si];
+                float ps       = sFinal[si] ? sProb[si] : prob[small];
+                alias[small]   = curLarge;
+                w              = __fsub_rn(w, __fsub_rn(1.f, ps));
+                if (w < 1.f)
+                {
+                    prob[curLarge] = w;
+                    lrg++;
+                    if (lrg < n)
+                    {
+                        curLarge = lIdx[li];
+                        w        = lProb[li];
+                        li++;
+                    }
+                }
+                sml++;
+                si++;
+            }
+            st[0] = sml;
+            st[1] = lrg;
+            if (lrg >= n || sml >= lrg)
+                st[2] = 1;
+            if (st[2] && lrg < n)
+                prob[curLarge] = w;
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void k_ref_pack(const uint32_t* alias, const float* prob, const float* pdf, uint32_t n,
+    agb_alias_entry* out)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    agb_alias_entry e;
+    e.alias     = alias[i];
+    e.prob      = prob[i];
+    e.pdf       = pdf[i];
+    e._padding1 = 0.f;
+    out[i]      = e;
+}
+
 } // namespace
 
 void freeEnvScratch(EnvBuildScratch& s)
 {
     cudaFree(s.weights);
     cudaFree(s.scanA);
-    cudaFree(s.scanB);
     cudaFree(s.ranks);
     cudaFree(s.heavyIdx);
     cudaFree(s.heavyIncl);
     cudaFree(s.lightIncl);
     cudaFree(s.blockSums);
     cudaFree(s.blockCounts);
+    cudaFree(s.rowSA);
     s = EnvBuildScratch();
 }
 
-cudaError_t buildEnvAlias(const float4* rgba, uint32_t width, uint32_t height,
-    agb_alias_entry* out, double* integralOut, EnvBuildScratch& s, cudaStream_t st)
+cudaError_t buildEnvAlias(const float4* rgba, uint32_t width, uint32_t height, int layout,
+    const float* rowSolidAngle, agb_alias_entry* out, double* integralFP64Out,
+    float* integralShadingOut, EnvBuildScratch& s, cudaStream_t st)
 {
     uint32_t n     = width * height;
     uint32_t tiles = (n + kScanTile - 1) / kScanTile;
-    if (s.capacity < n)
+    if (s.capacity < n || s.rows < height)
     {
         freeEnvScratch(s);
         size_t tileCap = size_t(tiles) * 3 + 8;
         cudaError_t e  = cudaSuccess;
         if ((e = cudaMalloc(&s.weights, sizeof(double) * n)) != cudaSuccess ||
             (e = cudaMalloc(&s.scanA, sizeof(double) * n)) != cudaSuccess ||
-            (e = cudaMalloc(&s.scanB, sizeof(double) * n)) != cudaSuccess ||
             (e = cudaMalloc(&s.ranks, sizeof(uint32_t) * n * 2)) != cudaSuccess ||
             (e = cudaMalloc(&s.heavyIdx, sizeof(uint32_t) * n)) != cudaSuccess ||
             (e = cudaMalloc(&s.heavyIncl, sizeof(double) * n)) != cudaSuccess ||
             (e = cudaMalloc(&s.lightIncl, sizeof(double) * n)) != cudaSuccess ||
             (e = cudaMalloc(&s.blockSums, sizeof(double) * tileCap)) != cudaSuccess ||
-            (e = cudaMalloc(&s.blockCounts, sizeof(uint32_t) * (tiles + 8))) != cudaSuccess)
+            (e = cudaMalloc(&s.blockCounts, sizeof(uint32_t) * (tiles + 8))) != cudaSuccess ||
+            (e = cudaMalloc(&s.rowSA, sizeof(float) * height + 16)) != cudaSuccess)
         {
             freeEnvScratch(s);
             return e;
         }
         s.capacity = n;
+        s.rows     = height;
     }
     float* lum       = reinterpret_cast<float*>(s.ranks + n); // second half of ranks
     double* tileW    = s.blockSums;
@@ -341,23 +539,59 @@ cudaError_t buildEnvAlias(const float4* rgba, uint32_t width, uint32_t height,
     double* tileSur  = s.blockSums + 2 * tiles;
     double* integral = s.blockSums + 3 * tiles;
     uint32_t* lightCount = s.blockCounts + tiles;
+    // FP64 luminance integral (always): prefix sums over luminance x solid angle.
     k_env_weights<<<tiles, kScanThreads, 0, st>>>(rgba, width, height, lum, s.weights, tileW);
     k_scan_tiles<<<1, kScanThreads, 0, st>>>(tileW, tiles, integral);
-    k_env_classify<<<tiles, kScanThreads, 0, st>>>(s.weights, n, integral, s.scanA, tileDef,
-        tileSur, s.blockCounts);
-    k_scan_tiles<<<1, kScanThreads, 0, st>>>(tileDef, tiles, nullptr);
-    k_scan_tiles<<<1, kScanThreads, 0, st>>>(tileSur, tiles, nullptr);
-    k_scan_tiles_u32<<<1, kScanThreads, 0, st>>>(s.blockCounts, tiles, lightCount);
-    k_env_scatter<<<tiles, kScanThreads, 0, st>>>(s.scanA, n, tileDef, tileSur, s.blockCounts,
-        s.ranks, s.lightIncl, s.heavyIncl, s.heavyIdx);
-    k_env_alias<<<(n + 255) / 256, 256, 0, st>>>(s.scanA, lum, n, integral, s.ranks,
-        s.lightIncl, s.heavyIncl, s.heavyIdx, lightCount, out);
-    cudaError_t e = cudaMemcpyAsync(integralOut, integral, sizeof(double), cudaMemcpyDeviceToHost, st);
+    float* shadingIntegral = reinterpret_cast<float*>(s.blockSums + 3 * tiles + 1);
+    if (layout == 1)
+    {
+        k_env_classify<<<tiles, kScanThreads, 0, st>>>(s.weights, n, integral, s.scanA, tileDef,
+            tileSur, s.blockCounts);
+        k_scan_tiles<<<1, kScanThreads, 0, st>>>(tileDef, tiles, nullptr);
+        k_scan_tiles<<<1, kScanThreads, 0, st>>>(tileSur, tiles, nullptr);
+        k_scan_tiles_u32<<<1, kScanThreads, 0, st>>>(s.blockCounts, tiles, lightCount);
+        k_env_scatter<<<tiles, kScanThreads, 0, st>>>(s.scanA, n, tileDef, tileSur, s.blockCounts,
+            s.ranks, s.lightIncl, s.heavyIncl, s.heavyIdx);
+        k_env_alias<<<(n + 255) / 256, 256, 0, st>>>(s.scanA, lum, n, integral, s.ranks,
+            s.lightIncl, s.heavyIncl, s.heavyIdx, lightCount, out);
+    }
+    else
+    {
+        // Reference layout.  Scratch reuse: lumArea / prob / pdf in the FP64 weight arrays,
+        // alias / index map in the FP64 prefix arrays.
+        float* lumArea    = reinterpret_cast<float*>(s.scanA);
+        float* prob       = reinterpret_cast<float*>(s.scanA) + n;
+        float* pdf        = reinterpret_cast<float*>(s.heavyIncl);
+        uint32_t* alias   = reinterpret_cast<uint32_t*>(s.heavyIncl) + n;
+        uint32_t* indexMap = reinterpret_cast<uint32_t*>(s.lightIncl);
+        uint32_t* smallCount = lightCount;
+        cudaError_t e = cudaMemcpyAsync(s.rowSA, rowSolidAngle, sizeof(float) * height,
+            cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess)
+            return e;
+        k_ref_lum<<<(n + 255) / 256, 256, 0, st>>>(rgba, width, n, s.rowSA, lum, lumArea);
+        k_ref_seq_sum<<<1, 32, 0, st>>>(lumArea, n, shadingIntegral);
+        k_ref_probs<<<tiles, kScanThreads, 0, st>>>(lum, lumArea, n, shadingIntegral, prob, pdf,
+            alias, s.blockCounts);
+        k_scan_tiles_u32<<<1, kScanThreads, 0, st>>>(s.blockCounts, tiles, smallCount);
+        k_ref_index<<<tiles, kScanThreads, 0, st>>>(prob, n, s.blockCounts, indexMap);
+        k_ref_sweep<<<1, 32, 0, st>>>(indexMap, prob, alias, n, smallCount);
+        k_ref_pack<<<(n + 255) / 256, 256, 0, st>>>(alias, prob, pdf, n, out);
+    }
+    cudaError_t e = cudaMemcpyAsync(integralFP64Out, integral, sizeof(double), cudaMemcpyDeviceToHost, st);
     if (e != cudaSuccess)
         return e;
+    if (layout != 1)
+    {
+        e = cudaMemcpyAsync(integralShadingOut, shadingIntegral, sizeof(float), cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess)
+            return e;
+    }
     e = cudaStreamSynchronize(st);
     if (e != cudaSuccess)
         return e;
+    if (layout == 1)
+        *integralShadingOut = float(*integralFP64Out);
     return cudaGetLastError();
 }
 

@@ -71,23 +71,28 @@ void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp
     const WaveBuffers& wb, cudaStream_t st, int smCount, uint64_t& launches, KernelMarks* marks);
 void setTraceAttributes();
 
-// agb_env_build.cu: FP64-prefix-sum alias table on the device.  rgba: device RGBA32F texels.
-// Returns the luminance integral.  scratch is reused across calls.
+// agb_env_build.cu: environment sampling table on the device.  rgba: device RGBA32F texels.
+// layout 0: the reference's table bit for bit (rowSolidAngle: host, one FP32 solid angle per row
+// computed as the reference does); layout 1: FP64 prefix-sum sweep.  integralFP64Out receives the
+// FP64 luminance integral, integralShadingOut the integral the shading divides by (the
+// reference's FP32 sum for layout 0).  scratch is reused across calls.
 struct EnvBuildScratch
 {
     double* weights   = nullptr; // per texel (luminance x solid angle), then normalised p
     double* scanA     = nullptr;
-    double* scanB     = nullptr;
     uint32_t* ranks   = nullptr;
     uint32_t* heavyIdx = nullptr;
     double* heavyIncl = nullptr;
     double* lightIncl = nullptr;
     double* blockSums = nullptr;
     uint32_t* blockCounts = nullptr;
+    float* rowSA      = nullptr;
     size_t capacity   = 0;
+    uint32_t rows     = 0;
 };
-cudaError_t buildEnvAlias(const float4* rgba, uint32_t width, uint32_t height,
-    agb_alias_entry* out, double* integralOut, EnvBuildScratch& scratch, cudaStream_t st);
+cudaError_t buildEnvAlias(const float4* rgba, uint32_t width, uint32_t height, int layout,
+    const float* rowSolidAngle, agb_alias_entry* out, double* integralFP64Out,
+    float* integralShadingOut, EnvBuildScratch& scratch, cudaStream_t st);
 void freeEnvScratch(EnvBuildScratch& s);
 
 // agb_bvh_build.cpp: host binned-SAH builder producing the device layout.

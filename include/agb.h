@@ -337,9 +337,23 @@ AGB_API agb_status agb_instances_set(agb_context* ctx, const agb_instance* insta
  * light_tex_luminance_integral. */
 AGB_API agb_status agb_environment_set(agb_context* ctx, const agb_environment_data* env,
     int32_t light_image, int32_t background_image);
-/* Reads back the environment alias table (width*height entries) and luminance integral. */
+/* Reads back the environment alias table (width*height entries), the luminance integral the
+ * shading divides by, and the FP64 luminance integral (either pointer may be null). */
 AGB_API agb_status agb_environment_alias(agb_context* ctx, agb_alias_entry* host_out,
-    uint64_t capacity, double* integral);
+    uint64_t capacity, double* shading_integral, double* fp64_integral);
+
+/* Layout of the table agb_environment_set builds.  AGB_ENV_TABLE_REFERENCE (default) reproduces
+ * the reference's AliasMap::build bit for bit (FP32 sequential integral and sweep; the sweep runs
+ * on one warp).  The reference's environment MIS reuses one random pair for the table bucket and
+ * for the BSDF lobe choice (ShadeFunctions.slang:146,220,237), so its converged image depends on
+ * the bucket layout, and matching its images needs its layout.  AGB_ENV_TABLE_FP64 builds the
+ * table from FP64 prefix sums (exact texel distribution, FP64 integral). */
+enum
+{
+    AGB_ENV_TABLE_REFERENCE = 0,
+    AGB_ENV_TABLE_FP64      = 1
+};
+AGB_API agb_status agb_set_environment_table(agb_context* ctx, int32_t layout);
 
 /* ------------------------------------------------------------------------------------------ */
 /* Rendering.                                                                                  */

@@ -41,31 +41,58 @@ def env_scene(img):
     return s
 
 
-@pytest.mark.parametrize("shape,seed", [((1024, 2048), 5), ((32, 64), 6), ((7, 13), 7), ((1, 1), 8)])
-def test_alias_table_distribution_and_pdf(agb, oracle, shape, seed):
-    from aurora_gb300 import api, scenes
-    h, w = shape
-    img = scenes.hdr_env(w, h, seed) if h >= 32 else \
+def env_image(h, w, seed):
+    from aurora_gb300 import scenes
+    return scenes.hdr_env(w, h, seed) if h >= 32 else \
         np.random.default_rng(seed).uniform(0, 4, (h, w, 3)).astype(np.float32)
+
+
+SHAPES = [((1024, 2048), 5), ((32, 64), 6), ((7, 13), 7), ((1, 1), 8)]
+
+
+@pytest.mark.parametrize("shape,seed", SHAPES)
+def test_reference_layout_table_is_bit_identical_to_reference(agb, oracle, shape, seed):
+    """Default table: the reference's AliasMap::build reproduced bit for bit on the device."""
+    from aurora_gb300 import api
+    h, w = shape
+    img = env_image(h, w, seed)
     with api.Renderer() as r:
         r.upload(env_scene(img))
-        table, integral = r.environment_alias()
+        table, integral, i64 = r.environment_alias(fp64_integral=True)
+    ref, ref_integral = oracle.alias_build(img)
+    np.testing.assert_array_equal(table["alias"], ref["alias"])
+    np.testing.assert_array_equal(table["prob"], ref["prob"])
+    np.testing.assert_array_equal(table["pdf"], ref["pdf"])
+    assert np.float32(integral) == np.float32(ref_integral)
     expect, lum, total = exact_distribution(img)
-    assert abs(integral - total) <= 1e-9 * total
+    assert abs(i64 - total) <= 1e-9 * total
+    print(f"{w}x{h}: reference FP32 integral off by {ref_integral / total - 1:.2e}")
+
+
+@pytest.mark.parametrize("shape,seed", SHAPES)
+def test_fp64_layout_table_distribution_and_pdf(agb, oracle, shape, seed):
+    """FP64 prefix-sum table: exact texel distribution, pdf = luminance / FP64 integral."""
+    from aurora_gb300 import _abi, api
+    h, w = shape
+    img = env_image(h, w, seed)
+    with api.Renderer() as r:
+        r.set_environment_table(_abi.ENV_TABLE_FP64)
+        r.upload(env_scene(img))
+        table, integral, i64 = r.environment_alias(fp64_integral=True)
+    expect, lum, total = exact_distribution(img)
+    assert abs(i64 - total) <= 1e-9 * total
+    assert np.float32(integral) == np.float32(i64)
     got = implied(table["alias"], table["prob"])
     np.testing.assert_allclose(got, expect, rtol=1e-5, atol=1e-12)
     assert (table["alias"] < w * h).all()
-    # Per-texel pdf = luminance / integral, the reference's formula (AliasMap.cpp:113-114).  The
-    # reference sums the integral sequentially in FP32, which drifts with the texel count (0.5% at
-    # 2048x1024); the FP64 prefix sum does not, so the two pdfs differ by that constant factor.
+    np.testing.assert_allclose(table["pdf"], (lum / np.float32(i64)).astype(np.float32), rtol=1e-6)
+    # Same per-texel formula as the reference, up to its FP32 integral drift.
     ref, ref_integral = oracle.alias_build(img)
-    print(f"{w}x{h}: reference FP32 integral off by {ref_integral / total - 1:.2e}")
-    np.testing.assert_allclose(table["pdf"], (lum / np.float32(integral)).astype(np.float32), rtol=1e-6)
-    scaled = table["pdf"].astype(np.float64) * integral / ref_integral
+    scaled = table["pdf"].astype(np.float64) * i64 / ref_integral
     np.testing.assert_allclose(scaled, ref["pdf"], rtol=2e-6, atol=0)
 
 
-def test_environment_sampling_matches_oracle_with_same_table(agb, oracle):
+def test_environment_sampling_matches_oracle(agb, oracle):
     from aurora_gb300 import api, scenes
     img = scenes.hdr_env(256, 128, 3)
     s = env_scene(img)
@@ -79,21 +106,29 @@ def test_environment_sampling_matches_oracle_with_same_table(agb, oracle):
             empty((n,), torch.float32)
         r.env_sample(d_rnd.data_ptr(), n, out_r.data_ptr(), out_d.data_ptr(), out_p.data_ptr())
         gr, gd, gp = host(out_r), host(out_d), host(out_p)
+    ref, ref_integral = oracle.alias_build(img)
     env = np.ascontiguousarray(s.env).reshape(1).copy()
     env["has_light_tex"] = 1
-    env["light_tex_luminance_integral"] = integral
+    env["light_tex_luminance_integral"] = ref_integral
     rgba = np.ones((128, 256, 4), np.float32)
     rgba[..., :3] = img
-    orr, od, op = oracle.env_sample(env, rgba, table, rnd)
+    orr, od, op = oracle.env_sample(env, rgba, ref, rnd)
     np.testing.assert_array_equal(gr, orr)
     np.testing.assert_array_equal(gp, op)
-    assert np.abs(gd - od).max() < 2e-6
+    np.testing.assert_array_equal(gd, od)
 
 
-def test_all_black_environment_is_safe(agb):
-    from aurora_gb300 import api
+def test_all_black_environment(agb, oracle):
+    from aurora_gb300 import _abi, api
     img = np.zeros((8, 16, 3), np.float32)
     with api.Renderer() as r:
+        r.upload(env_scene(img))
+        table, integral = r.environment_alias()
+    ref, ref_integral = oracle.alias_build(img)  # the reference divides 0 by 0 here
+    np.testing.assert_array_equal(table["alias"], ref["alias"])
+    np.testing.assert_array_equal(table["prob"], ref["prob"])
+    with api.Renderer() as r:
+        r.set_environment_table(_abi.ENV_TABLE_FP64)
         r.upload(env_scene(img))
         table, integral = r.environment_alias()
     assert integral == 0.0

@@ -10,17 +10,15 @@ pytestmark = pytest.mark.gpu
 
 
 def render_both(oracle, s, spp, precision=32, max_paths=0):
-    """GPU render and oracle render with the same environment table (the device's FP64-built
-    one), so both trace identical sample streams."""
+    """GPU render and oracle render at equal samples: both use the reference's environment table
+    layout, so they trace identical sample streams."""
     from aurora_gb300 import api
     with api.Renderer() as r:
         r.upload(s)
         r.render(0, spp, max_paths=max_paths)
         g = r.read(_abi.ACCUM_RUNNING_MEAN)
         gk = r.read(_abi.ACCUM_KAHAN)
-        alias, integral = r.environment_alias()
-    o = oracle.OracleScene(s, alias=alias, integral=np.float32(integral)).render(
-        0, spp, precision=precision, want_sum=True)
+    o = oracle.OracleScene(s).render(0, spp, precision=precision, want_sum=True)
     return g, gk, o
 
 
@@ -49,24 +47,38 @@ def test_small_config_matches_oracle(agb, oracle):
     assert err64 < 1e-4
 
 
-def test_device_table_is_unbiased_against_reference_table(agb, oracle):
-    """Same estimator, independent environment samples: the device table (FP64 prefix sums) and
-    the reference's FP32 sequential table, 4096 spp each.  Their difference must sit inside the
-    Monte Carlo noise floor measured between two independent reference-table renders."""
+def test_environment_table_layout_only_matters_through_lobe_selection(agb, oracle):
+    """The reference's environment MIS reuses one random pair for the table bucket and for the
+    lobe choice in evaluateMaterialAndPDF, so its converged image depends on the table layout.
+    With deterministic lobe selection (diffuse-only materials) the FP64 layout and the reference
+    layout must converge to the same image; the noise floor is measured between two independent
+    reference-layout renders."""
     from aurora_gb300 import api, scenes
     spp = 4096
     s = scenes.config_tiny(width=16, height=12, spp=spp, lights=False)
+    for k in ("specular", "coat", "metalness", "sheen", "transmission", "subsurface"):
+        s.materials[k] = 0.0
     with api.Renderer() as r:
+        r.set_environment_table(_abi.ENV_TABLE_FP64)
         r.upload(s)
         r.render(0, spp)
         g = r.read(_abi.ACCUM_KAHAN)
     o = oracle.OracleScene(s)
     a = o.render(0, spp, precision=64, want_sum=True)["sum"] / spp
     b = o.render(spp, spp, precision=64, want_sum=True)["sum"] / spp
-    err = oracle.rel_mse(g, a)
-    floor = oracle.rel_mse(a, b)
-    print(f"device vs reference table relMSE {err:.3g}; noise floor {floor:.3g}")
+    err, floor = oracle.rel_mse(g, a), oracle.rel_mse(a, b)
+    print(f"FP64 layout vs reference layout relMSE {err:.3g}; noise floor {floor:.3g}")
     assert err < 1.5 * floor
+
+
+def test_converged_image_matches_fp64_oracle(agb, oracle):
+    """1024 spp: the device image against the FP64 oracle at equal samples."""
+    from aurora_gb300 import scenes
+    s = scenes.config_tiny(width=16, height=12, spp=1024)
+    g, gk, o = render_both(oracle, s, 1024, precision=64)
+    err = oracle.rel_mse(gk, o["sum"] / 1024)
+    print("converged relMSE vs FP64 oracle", err)
+    assert err < 1e-3
 
 
 def test_layered_decals_match_oracle(agb, oracle):
