@@ -44,6 +44,9 @@ def parse_args():
     p.add_argument("--config", default="large", choices=["large", "small"])
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--res", default=None, help="WxH override (profiling runs)")
+    p.add_argument("--spp", type=int, default=None, help="samples per pixel override (profiling runs)")
     return p.parse_args()
 
 
@@ -54,11 +57,17 @@ def dist_env():
     return rank, world, local
 
 
-def make_scene(name):
+def make_scene(name, res=None, spp=None):
     from aurora_gb300 import scenes
+    kw = {}
+    if res:
+        w, h = (int(x) for x in res.lower().split("x"))
+        kw.update(width=w, height=h)
+    if spp:
+        kw.update(spp=spp)
     if name == "small":
-        return scenes.config_small(seed=0)
-    return scenes.config_large(seed=0)
+        return scenes.config_small(seed=0, **kw)
+    return scenes.config_large(seed=0, **kw)
 
 
 def workload(s, name):
@@ -207,7 +216,7 @@ def main():
     torch.cuda.set_device(local)
     from aurora_gb300 import _abi, api, build
     build.build()
-    s = make_scene(args.config)
+    s = make_scene(args.config, args.res, args.spp)
     stream = torch.cuda.Stream()
     r = api.Renderer(local, stream=stream.cuda_stream)
     r.upload(s)
@@ -262,14 +271,14 @@ def main():
     img_np = img_host.numpy()
     frame_np = frame_host.numpy().view(_abi.FRAME_DTYPE)
     e2e_s = []
-    for k in range(args.warmup + args.steps):
+    for k in range(0 if args.no_e2e else args.warmup + args.steps):
         t0 = time.perf_counter()
         r.set_frame(frame_np)
         r.render(0, s.spp)
         r.read(_abi.ACCUM_KAHAN, out=img_np)
         if k >= args.warmup:
             e2e_s.append(time.perf_counter() - t0)
-    e2e_time = float(np.sum(e2e_s))
+    e2e_time = float(np.sum(e2e_s)) if e2e_s else float("nan")
     if world > 1:
         t = torch.tensor([e2e_time], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
