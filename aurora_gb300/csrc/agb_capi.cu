@@ -241,7 +241,7 @@ agb_status ensureWave(agb_context* ctx, size_t paths, int depth, size_t waves)
             return fail(AGB_ERR_LIMIT, "internal: queue carve overflow");
         ctx->pathCapacity = P;
     }
-    size_t counterWords = size_t(depth + 2) * 4 * waves;
+    size_t counterWords = size_t(depth + 2) * kCounterStride * waves;
     AGB_CUDA(ctx->counters.ensure(counterWords * sizeof(uint32_t)), "allocate counters");
     AGB_CUDA(ctx->stats.ensure(8 * sizeof(unsigned long long)), "allocate stats");
     ctx->wb.stats = ctx->stats.as<unsigned long long>();
@@ -638,6 +638,13 @@ AGB_API agb_status agb_instances_set(agb_context* ctx, const agb_instance* inst,
     }
     BuiltBVH tl;
     buildBVH2(boxes.data(), count, 1, 12, tl);
+    // The traversal enters exactly one instance per TLAS leaf.
+    auto singleLeaf = [](int32_t r) { return r >= 0 || ((uint32_t(~r) & 7u) == 0u); };
+    if (!singleLeaf(tl.root))
+        return fail(AGB_ERR_LIMIT, "agb_instances_set: TLAS leaf with more than one instance");
+    for (const BNode& nd : tl.nodes)
+        if (!singleLeaf(nd.ref.x) || !singleLeaf(nd.ref.y))
+            return fail(AGB_ERR_LIMIT, "agb_instances_set: TLAS leaf with more than one instance");
     int maxBlas = 0;
     for (auto& g : ctx->geometries)
         maxBlas = std::max(maxBlas, g->mesh.depth);
@@ -793,7 +800,7 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
     else if (ctx->accumulatedSamples != sample_start || (ctx->lastAccumMode & accumMode) != accumMode)
         return fail(AGB_ERR_INVALID_ARG, "agb_render: sample_start must continue the accumulated "
                                          "sequence in the same accumulation mode");
-    size_t counterWords = size_t(depth + 2) * 4;
+    size_t counterWords = size_t(depth + 2) * kCounterStride;
     AGB_CUDA(cudaMemsetAsync(ctx->counters.ptr, 0, counterWords * waves * sizeof(uint32_t), ctx->stream),
         "clear counters");
     AGB_CUDA(cudaMemsetAsync(ctx->stats.ptr, 0, 8 * sizeof(unsigned long long), ctx->stream), "clear stats");
@@ -840,8 +847,8 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
         for (uint32_t w = 0; w < waves; w++)
             for (int b = 0; b < depth; b++)
             {
-                r.closest_rays += c[counterWords * w + 4 * b + 0];
-                r.shadow_rays += c[counterWords * w + 4 * b + 1];
+                r.closest_rays += c[counterWords * w + kCounterStride * b + CNT_RAYS];
+                r.shadow_rays += c[counterWords * w + kCounterStride * b + CNT_SHADOW];
             }
         r.node_visits        = s[2];
         r.tri_tests          = s[3];
@@ -981,10 +988,19 @@ AGB_API agb_status agb_intersect_batch(agb_context* ctx, const float* rays, int6
     agb_status st = setDevice(ctx);
     if (st)
         return st;
+    if (n >= (1ll << 31))
+        return fail(AGB_ERR_LIMIT, "agb_intersect_batch: at most 2^31 - 1 rays per call");
+    AGB_CUDA(ctx->stats.ensure(8 * sizeof(unsigned long long)), "allocate stats");
+    AGB_CUDA(cudaMemsetAsync(ctx->stats.ptr, 0, 8 * sizeof(unsigned long long), ctx->stream), "clear stats");
+    unsigned long long* st64 = ctx->stats.as<unsigned long long>();
     AGB_CUDA(launchIntersectBatch(ctx->scene(), rays, n, any_hit, out_tuv, out_inst_prim,
-                 ctx->stream, ctx->smCount),
+                 reinterpret_cast<uint32_t*>(st64 + 7), st64 + 4, ctx->stream, ctx->smCount),
         "agb_intersect_batch");
+    unsigned long long ov = 0;
+    AGB_CUDA(cudaMemcpyAsync(&ov, st64 + 4, sizeof ov, cudaMemcpyDeviceToHost, ctx->stream), "read overflow");
     AGB_CUDA(cudaStreamSynchronize(ctx->stream), "agb_intersect_batch");
+    if (ov)
+        return fail(AGB_ERR_LIMIT, "agb_intersect_batch: traversal stack overflow");
     return AGB_OK;
 }
 

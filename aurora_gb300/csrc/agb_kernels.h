@@ -113,7 +113,8 @@ cudaError_t launchBsdfBatch(int op, const agb_material* mats, const int32_t* mat
     const float* frames, const float* V, const float* L, const float* rnd, int64_t n,
     float* outValue, float* outDir, float* outPdf, int32_t* outLobe, cudaStream_t st);
 cudaError_t launchIntersectBatch(const DevScene& s, const float* rays, int64_t n, int anyHit,
-    float* outTUV, int32_t* outInstPrim, cudaStream_t st, int smCount);
+    float* outTUV, int32_t* outInstPrim, uint32_t* work, unsigned long long* overflowCount,
+    cudaStream_t st, int smCount);
 cudaError_t launchEnvSampleBatch(const DevScene& s, const float* rnd, int64_t n,
     float* outRadiance, float* outDir, float* outPdf, cudaStream_t st);
 cudaError_t launchRandomStream(uint32_t sampleIndex, uint32_t width, uint32_t px, uint32_t py,

@@ -95,23 +95,69 @@ __global__ void k_camera(agb_frame_data f, WaveParams wp, WaveBuffers wb)
 // --------------------------------------------------------------------------------- tracing
 extern __shared__ int32_t g_stack[];
 
+struct QueueRayLoader
+{
+    const float4* org;
+    const float4* dir;
+    AGB_D void operator()(uint32_t i, v3& o, v3& d, float& tmin, float& tmax) const
+    {
+        float4 o4 = org[i], d4 = dir[i];
+        o    = v3{ o4.x, o4.y, o4.z };
+        d    = v3{ d4.x, d4.y, d4.z };
+        tmin = o4.w;
+        tmax = d4.w;
+    }
+};
+struct HitWriter
+{
+    float4* tuv;
+    int32_t* inst;
+    AGB_D void operator()(uint32_t i, bool hit, const RayHit& h) const
+    {
+        tuv[i]  = make_float4(hit ? h.t : -1.f, h.u, h.v, __int_as_float(h.prim));
+        inst[i] = hit ? h.inst : -1;
+    }
+};
+struct ShadowLoader
+{
+    const uint32_t* tag;
+    const float4* org;
+    const float4* dir;
+    AGB_D void operator()(uint32_t i, v3& o, v3& d, float& tmin, float& tmax) const
+    {
+        uint32_t t = tag[i];
+        uint32_t p = t >> 3, k = t & 7u;
+        float4 o4 = org[p];
+        float4 d4 = dir[size_t(p) * kMaxShadowSlots + k];
+        o    = v3{ o4.x, o4.y, o4.z };
+        d    = v3{ d4.x, d4.y, d4.z };
+        tmin = kRayTMin;
+        tmax = __int_as_float(0x7f800000);
+    }
+};
+struct OcclusionWriter
+{
+    const uint32_t* tag;
+    uint32_t* occluded;
+    AGB_D void operator()(uint32_t i, bool hit, const RayHit&) const
+    {
+        if (hit)
+        {
+            uint32_t t = tag[i];
+            atomicOr(occluded + (t >> 3), 1u << (t & 7u));
+        }
+    }
+};
+
 template <bool kCount>
 __global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_closest(DevScene s, WaveBuffers wb, int bounce, int cur)
 {
-    uint32_t n      = wb.counters[bounce * 4 + 0];
-    int32_t* stack  = g_stack + threadIdx.x;
+    uint32_t n      = wb.counters[bounce * kCounterStride + CNT_RAYS];
     TraceCounters c = { 0, 0 };
     bool overflow   = false;
-    uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-    {
-        float4 o4 = wb.rayOrg[cur][i], d4 = wb.rayDir[cur][i];
-        RayHit h;
-        bool hit = castRay<false, kCount>(s, v3{ o4.x, o4.y, o4.z }, v3{ d4.x, d4.y, d4.z }, o4.w,
-            d4.w, h, stack, kTraceBlock, c, overflow);
-        wb.hitTUV[i]  = make_float4(hit ? h.t : -1.f, h.u, h.v, __int_as_float(h.prim));
-        wb.hitInst[i] = hit ? h.inst : -1;
-    }
+    persistentTrace<false, kCount>(s, n, wb.counters + bounce * kCounterStride + CNT_CLOSEST_WORK,
+        QueueRayLoader{ wb.rayOrg[cur], wb.rayDir[cur] }, HitWriter{ wb.hitTUV, wb.hitInst },
+        g_stack + threadIdx.x, kTraceBlock, c, overflow);
     if (kCount)
     {
         atomicAdd(statPtr(wb, 2), c.nodes);
@@ -124,23 +170,12 @@ __global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_closes
 template <bool kCount>
 __global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_shadow(DevScene s, WaveBuffers wb, int bounce)
 {
-    uint32_t n      = wb.counters[bounce * 4 + 1];
-    int32_t* stack  = g_stack + threadIdx.x;
+    uint32_t n      = wb.counters[bounce * kCounterStride + CNT_SHADOW];
     TraceCounters c = { 0, 0 };
     bool overflow   = false;
-    uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-    {
-        uint32_t tag = wb.shTag[i];
-        uint32_t p = tag >> 3, k = tag & 7u;
-        float4 o4 = wb.shOrg[p];
-        float4 d4 = wb.shDir[size_t(p) * kMaxShadowSlots + k];
-        RayHit h;
-        bool hit = castRay<true, kCount>(s, v3{ o4.x, o4.y, o4.z }, v3{ d4.x, d4.y, d4.z }, kRayTMin,
-            __int_as_float(0x7f800000), h, stack, kTraceBlock, c, overflow);
-        if (hit)
-            atomicOr(wb.occluded + p, 1u << k);
-    }
+    persistentTrace<true, kCount>(s, n, wb.counters + bounce * kCounterStride + CNT_SHADOW_WORK,
+        ShadowLoader{ wb.shTag, wb.shOrg, wb.shDir }, OcclusionWriter{ wb.shTag, wb.occluded },
+        g_stack + threadIdx.x, kTraceBlock, c, overflow);
     if (kCount)
     {
         atomicAdd(statPtr(wb, 5), c.nodes);
@@ -198,7 +233,7 @@ __device__ __forceinline__ void accumulateSegment(WaveBuffers& wb, uint32_t p, i
 __global__ void __launch_bounds__(kShadeBlock) k_shade(DevScene s, agb_frame_data f,
     WaveParams wp, WaveBuffers wb, int bounce, int cur, int depthLimit)
 {
-    uint32_t n      = wb.counters[bounce * 4 + 0];
+    uint32_t n      = wb.counters[bounce * kCounterStride + CNT_RAYS];
     uint32_t stride = gridDim.x * blockDim.x;
     const float clampLum = f.indirect_bounce_clamp_scale > 0.f
         ? f.max_luminance * f.indirect_bounce_clamp_scale
@@ -481,14 +516,14 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(DevScene s, agb_frame_dat
         }
         // Warp-aggregated queue appends (all lanes of the warp reach this point together).
         __syncwarp();
-        uint32_t slotNext = warpAppend(wb.counters + (bounce + 1) * 4 + 0, pushNext);
+        uint32_t slotNext = warpAppend(wb.counters + (bounce + 1) * kCounterStride + CNT_RAYS, pushNext);
         if (pushNext)
         {
             wb.rayOrg[cur ^ 1][slotNext]  = make_float4(nextO.x, nextO.y, nextO.z, kRayTMin);
             wb.rayDir[cur ^ 1][slotNext]  = make_float4(nextD.x, nextD.y, nextD.z, __int_as_float(0x7f800000));
             wb.rayPath[cur ^ 1][slotNext] = p;
         }
-        uint32_t slotRes = warpAppend(wb.counters + bounce * 4 + 2, resolve);
+        uint32_t slotRes = warpAppend(wb.counters + bounce * kCounterStride + CNT_RESOLVE, resolve);
         if (resolve)
             wb.resolveList[slotRes] = p;
         // Shadow rays: variable count per lane, warp prefix sum then one atomic.
@@ -505,7 +540,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(DevScene s, agb_frame_dat
         uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
         uint32_t sbase = 0;
         if (lane == 31 && total)
-            sbase = atomicAdd(wb.counters + bounce * 4 + 1, total);
+            sbase = atomicAdd(wb.counters + bounce * kCounterStride + CNT_SHADOW, total);
         sbase = __shfl_sync(0xffffffffu, sbase, 31);
         uint32_t w = sbase + incl - cnt;
         for (uint32_t k = 0; k < uint32_t(kMaxShadowSlots); k++)
@@ -517,7 +552,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(DevScene s, agb_frame_dat
 // Applies shadow visibility to the pending contributions and accumulates the segment.
 __global__ void k_resolve(agb_frame_data f, WaveBuffers wb, int bounce)
 {
-    uint32_t n      = wb.counters[bounce * 4 + 2];
+    uint32_t n      = wb.counters[bounce * kCounterStride + CNT_RESOLVE];
     uint32_t stride = gridDim.x * blockDim.x;
     const float clampLum = f.indirect_bounce_clamp_scale > 0.f
         ? f.max_luminance * f.indirect_bounce_clamp_scale

@@ -309,4 +309,184 @@ AGB_D bool castRay(const DevScene& s, v3 o, v3 d, float tmin, float tmax, RayHit
     return found;
 }
 
+// ------------------------------------------------------------------ persistent traversal
+// Each warp loops over a shared work counter.  A lane whose ray has finished takes the next ray
+// index at once (one atomic per warp per refill), so no lane idles while a slower ray in its warp
+// is still traversing (Aila & Laine, "Understanding the Efficiency of Ray Traversal on GPUs",
+// HPG 2009, persistent threads with per-lane fetch).  The two-level traversal is a resumable
+// per-lane state machine: entering an instance pushes kExitInstance on the shared-memory stack;
+// popping it restores the world ray and the TLAS.
+
+constexpr int32_t kExitInstance   = int32_t(0x80000000); // never a node or leaf ref
+constexpr int kStepsPerRefill     = 24;                  // node / leaf steps between refill checks
+
+template <bool kAnyHit, bool kCount, class Loader, class Writer>
+AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const Loader& load,
+    const Writer& write, int32_t* stack, int stride, TraceCounters& cnt, bool& overflow)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane      = threadIdx.x & 31;
+    bool active = false, exhausted = false;
+    uint32_t rayIdx = 0;
+    v3 o = splat(0.f), d = splat(0.f);
+    float tmin = 0.f, tmax = 0.f;
+    SlabRay sr;
+    WtRay wr;
+    int32_t ref = 0;
+    int sp      = 0;
+    int32_t inst = -1;
+    const float4* nodes = nullptr;
+    const float4* tris  = nullptr;
+    RayHit hit;
+    bool found = false;
+    for (;;)
+    {
+        // Refill lanes whose ray is done.
+        bool need       = !active && !exhausted;
+        unsigned needMask = __ballot_sync(FULL, need);
+        if (needMask)
+        {
+            int leader    = __ffs(needMask) - 1;
+            uint32_t base = 0;
+            if (lane == leader)
+                base = atomicAdd(work, uint32_t(__popc(needMask)));
+            base = __shfl_sync(FULL, base, leader);
+            if (need)
+            {
+                rayIdx = base + uint32_t(__popc(needMask & ((1u << lane) - 1u)));
+                if (rayIdx < n)
+                {
+                    load(rayIdx, o, d, tmin, tmax);
+                    sr       = slabSetup(o, d);
+                    ref      = s.instanceCount > 0 ? s.tlasRoot : kExitInstance;
+                    sp       = 0;
+                    inst     = -1;
+                    nodes    = reinterpret_cast<const float4*>(s.tlas);
+                    found    = false;
+                    hit.inst = hit.prim = -1;
+                    hit.t = hit.u = hit.v = 0.f;
+                    active   = s.instanceCount > 0;
+                    if (!active)
+                        write(rayIdx, false, hit);
+                }
+                else
+                    exhausted = true;
+            }
+        }
+        if (__all_sync(FULL, exhausted))
+            break;
+        if (!__any_sync(FULL, active))
+            continue;
+        if (active)
+        {
+            bool done = false;
+            for (int step = 0; step < kStepsPerRefill && !done; step++)
+            {
+                if (ref >= 0)
+                {
+                    const float4* np = nodes + 4 * size_t(ref);
+                    float4 c0xy = __ldg(np), c1xy = __ldg(np + 1), cz = __ldg(np + 2);
+                    int4 refs   = __ldg(reinterpret_cast<const int4*>(np + 3));
+                    if (kCount)
+                        cnt.nodes++;
+                    bool h0, h1;
+                    float t0, t1;
+                    slab2(sr, c0xy, c1xy, cz, tmin, tmax, h0, h1, t0, t1);
+                    if (h0 && h1)
+                    {
+                        if (sp >= kStackSize - 1)
+                        {
+                            overflow = true;
+                            done     = true;
+                            break;
+                        }
+                        stack[sp * stride] = t0 <= t1 ? refs.y : refs.x;
+                        sp++;
+                        ref = t0 <= t1 ? refs.x : refs.y;
+                        continue;
+                    }
+                    if (h0 || h1)
+                    {
+                        ref = h0 ? refs.x : refs.y;
+                        continue;
+                    }
+                }
+                else if (ref == kExitInstance)
+                {
+                    inst  = -1;
+                    nodes = reinterpret_cast<const float4*>(s.tlas);
+                    sr    = slabSetup(o, d);
+                }
+                else
+                {
+                    uint32_t code  = uint32_t(~ref);
+                    uint32_t first = code >> 3, count = (code & 7u) + 1u;
+                    if (inst < 0)
+                    {
+                        // TLAS leaf: one instance (the TLAS is built with single-instance leaves).
+                        int32_t ii = __ldg(s.tlasOrder + first);
+                        const DevInstance& in = s.instances[ii];
+                        const DevMesh& m      = s.meshes[in.mesh];
+                        if (sp >= kStackSize - 1)
+                        {
+                            overflow = true;
+                            done     = true;
+                            break;
+                        }
+                        stack[sp * stride] = kExitInstance;
+                        sp++;
+                        v3 oo = xfPointRn(in.w2o, o);
+                        v3 od = xfVectorRn(in.w2o, d);
+                        wr    = wtSetup(oo, od);
+                        sr    = slabSetup(oo, od);
+                        inst  = ii;
+                        nodes = reinterpret_cast<const float4*>(m.nodes);
+                        tris  = m.tris;
+                        ref   = m.root;
+                        continue;
+                    }
+                    for (uint32_t k = 0; k < count; k++)
+                    {
+                        const float4* tp = tris + 3 * size_t(first + k);
+                        float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                        if (kCount)
+                            cnt.tris++;
+                        float t, u, v;
+                        if (wtIntersect(wr, a, b, c, tmin, tmax, t, u, v))
+                        {
+                            found    = true;
+                            tmax     = t;
+                            hit.t    = t;
+                            hit.u    = u;
+                            hit.v    = v;
+                            hit.inst = inst;
+                            hit.prim = __float_as_int(a.w);
+                            if (kAnyHit)
+                                break;
+                        }
+                    }
+                    if (kAnyHit && found)
+                    {
+                        done = true;
+                        break;
+                    }
+                }
+                // Pop the next entry; an empty stack ends the ray.
+                if (sp == 0)
+                {
+                    done = true;
+                    break;
+                }
+                sp--;
+                ref = stack[sp * stride];
+            }
+            if (done)
+            {
+                write(rayIdx, found, hit);
+                active = false;
+            }
+        }
+    }
+}
+
 } // namespace agb

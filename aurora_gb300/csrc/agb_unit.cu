@@ -86,26 +86,43 @@ __global__ void k_bsdf_batch(int op, const agb_material* mats, const int32_t* mi
 
 extern __shared__ int32_t u_stack[];
 
-__global__ void __launch_bounds__(kTraceBlock) k_intersect_batch(DevScene s, const float* rays,
-    int64_t n, int anyHit, float* outTUV, int32_t* outIP)
+struct BatchRayLoader
 {
-    int32_t* stack = u_stack + threadIdx.x;
-    TraceCounters c = { 0, 0 };
-    bool overflow = false;
-    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
-         i += int64_t(gridDim.x) * blockDim.x)
+    const float* rays;
+    AGB_D void operator()(uint32_t i, v3& o, v3& d, float& tmin, float& tmax) const
     {
-        const float* r = rays + 8 * i;
-        v3 o = v3{ r[0], r[1], r[2] }, d = v3{ r[4], r[5], r[6] };
-        RayHit h;
-        bool hit = anyHit ? castRay<true, false>(s, o, d, r[3], r[7], h, stack, kTraceBlock, c, overflow)
-                          : castRay<false, false>(s, o, d, r[3], r[7], h, stack, kTraceBlock, c, overflow);
-        outTUV[3 * i]     = hit ? h.t : -1.f;
-        outTUV[3 * i + 1] = hit ? h.u : 0.f;
-        outTUV[3 * i + 2] = hit ? h.v : 0.f;
-        outIP[2 * i]      = hit ? h.inst : (overflow ? -2 : -1);
-        outIP[2 * i + 1]  = hit ? h.prim : -1;
+        const float* r = rays + 8 * size_t(i);
+        o    = v3{ r[0], r[1], r[2] };
+        d    = v3{ r[4], r[5], r[6] };
+        tmin = r[3];
+        tmax = r[7];
     }
+};
+struct BatchHitWriter
+{
+    float* tuv;
+    int32_t* ip;
+    AGB_D void operator()(uint32_t i, bool hit, const RayHit& h) const
+    {
+        tuv[3 * size_t(i)]     = hit ? h.t : -1.f;
+        tuv[3 * size_t(i) + 1] = hit ? h.u : 0.f;
+        tuv[3 * size_t(i) + 2] = hit ? h.v : 0.f;
+        ip[2 * size_t(i)]      = hit ? h.inst : -1;
+        ip[2 * size_t(i) + 1]  = hit ? h.prim : -1;
+    }
+};
+
+// Same persistent traversal as the renderer's trace kernels.
+template <bool kAnyHit>
+__global__ void __launch_bounds__(kTraceBlock) k_intersect_batch(DevScene s, const float* rays,
+    uint32_t n, uint32_t* work, float* outTUV, int32_t* outIP, unsigned long long* overflowCount)
+{
+    TraceCounters c = { 0, 0 };
+    bool overflow   = false;
+    persistentTrace<kAnyHit, false>(s, n, work, BatchRayLoader{ rays }, BatchHitWriter{ outTUV, outIP },
+        u_stack + threadIdx.x, kTraceBlock, c, overflow);
+    if (overflow)
+        atomicAdd(overflowCount, 1ull);
 }
 
 __global__ void k_env_sample_batch(DevScene s, const float* rnd, int64_t n, float* outR,
@@ -189,15 +206,23 @@ cudaError_t launchBsdfBatch(int op, const agb_material* mats, const int32_t* mat
 }
 
 cudaError_t launchIntersectBatch(const DevScene& s, const float* rays, int64_t n, int anyHit,
-    float* outTUV, int32_t* outInstPrim, cudaStream_t st, int smCount)
+    float* outTUV, int32_t* outInstPrim, uint32_t* work, unsigned long long* overflowCount,
+    cudaStream_t st, int smCount)
 {
     if (n <= 0)
         return cudaSuccess;
     size_t smem = size_t(kStackSize) * kTraceBlock * sizeof(int32_t);
-    cudaFuncSetAttribute(k_intersect_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     int64_t blocks = (n + kTraceBlock - 1) / kTraceBlock;
     int grid       = int(blocks < int64_t(smCount) * 8 ? blocks : int64_t(smCount) * 8);
-    k_intersect_batch<<<grid, kTraceBlock, smem, st>>>(s, rays, n, anyHit, outTUV, outInstPrim);
+    cudaError_t e = cudaMemsetAsync(work, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess)
+        return e;
+    if (anyHit)
+        k_intersect_batch<true><<<grid, kTraceBlock, smem, st>>>(s, rays, uint32_t(n), work, outTUV,
+            outInstPrim, overflowCount);
+    else
+        k_intersect_batch<false><<<grid, kTraceBlock, smem, st>>>(s, rays, uint32_t(n), work, outTUV,
+            outInstPrim, overflowCount);
     return cudaGetLastError();
 }
 

@@ -10,6 +10,17 @@ namespace agb
 
 constexpr int kMaxShadowSlots = 6; // up to 4 distant lights + 2 environment-MIS rays per hit
 
+// Per-bounce device counters (kCounterStride words per bounce).
+enum : int
+{
+    CNT_RAYS          = 0, // rays in the bounce's queue
+    CNT_SHADOW        = 1, // shadow rays appended by shading
+    CNT_RESOLVE       = 2, // paths with a pending record
+    CNT_CLOSEST_WORK  = 3, // persistent traversal work counter (closest-hit rays)
+    CNT_SHADOW_WORK   = 4, // persistent traversal work counter (shadow rays)
+    kCounterStride    = 8
+};
+
 // Path flag bits (mirrors the reference payload bit fields, RayTrace.slang:52-126).
 enum : uint32_t
 {
@@ -66,7 +77,7 @@ struct WaveBuffers
     float4* shDir;
     uint32_t* shTag;        // path << 3 | slot
     uint32_t* resolveList;  // paths with a pending record this bounce
-    uint32_t* counters;     // per bounce: [rays, shadow, resolve, spare]
+    uint32_t* counters;     // per bounce: kCounterStride words (CNT_*)
     // Accumulation targets (per pixel).
     float4* accumMean;
     float4* accumSum;
