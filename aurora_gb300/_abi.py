@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libagb_cuda.so")
 AGB_OK = 0
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "timeout",
           -5: "not ready", -6: "limit exceeded"}
+ERR_LIMIT = -6
 
 ACCUM_RUNNING_MEAN = 1
 ACCUM_KAHAN = 2
@@ -24,6 +25,7 @@ FORMAT_RGBA32F = 1
 FORMAT_RGB32F = 2
 ENV_TABLE_REFERENCE = 0
 ENV_TABLE_FP64 = 1
+ENV_NOALLOC_MAX_TEXELS = 262144  # AGB_ENV_NOALLOC_MAX_TEXELS
 TEX_BASE_COLOR, TEX_SPECULAR_ROUGHNESS, TEX_OPACITY, TEX_NORMAL, TEX_EMISSION = range(5)
 
 
@@ -141,6 +143,9 @@ SIGNATURES = {
     "agb_environment_alias": (_I32, [_P, _P, _U64, ctypes.POINTER(ctypes.c_double),
                                       ctypes.POINTER(ctypes.c_double)]),
     "agb_set_environment_table": (_I32, [_P, _I32]),
+    "agb_environment_alias_build_noalloc": (_I32, [_P, _U32, _U32, _I32, _P,
+                                                   ctypes.POINTER(ctypes.c_double),
+                                                   ctypes.POINTER(ctypes.c_double), _P]),
     "agb_frame_set": (_I32, [_P, _P]),
     "agb_render": (_I32, [_P, ctypes.POINTER(RenderOptions), _U32, _U32, ctypes.POINTER(RenderStats)]),
     "agb_wait": (_I32, [_P]),

@@ -750,6 +750,38 @@ AGB_API agb_status agb_environment_alias(agb_context* ctx, agb_alias_entry* host
     return AGB_OK;
 }
 
+AGB_API agb_status agb_environment_alias_build_noalloc(const float* rgba_device, uint32_t width,
+    uint32_t height, int32_t layout, agb_alias_entry* table_device, double* shading_integral,
+    double* fp64_integral, void* stream)
+{
+    if (!rgba_device || !table_device)
+        return fail(AGB_ERR_INVALID_ARG, "agb_environment_alias_build_noalloc: null device pointer");
+    if (width == 0 || height == 0)
+        return fail(AGB_ERR_INVALID_ARG, "agb_environment_alias_build_noalloc: empty image");
+    if (layout != AGB_ENV_TABLE_REFERENCE && layout != AGB_ENV_TABLE_FP64)
+        return fail(AGB_ERR_INVALID_ARG, "agb_environment_alias_build_noalloc: bad layout");
+    if (uint64_t(width) * height > AGB_ENV_NOALLOC_MAX_TEXELS)
+        return fail(AGB_ERR_LIMIT, "agb_environment_alias_build_noalloc: " + std::to_string(width) +
+                                       "x" + std::to_string(height) + " = " +
+                                       std::to_string(uint64_t(width) * height) +
+                                       " texels exceeds the limit of " +
+                                       std::to_string(AGB_ENV_NOALLOC_MAX_TEXELS) +
+                                       " texels (AGB_ENV_NOALLOC_MAX_TEXELS)");
+    if ((reinterpret_cast<uintptr_t>(rgba_device) & 15u) || (reinterpret_cast<uintptr_t>(table_device) & 15u))
+        return fail(AGB_ERR_INVALID_ARG, "agb_environment_alias_build_noalloc: device pointers must be "
+                                         "16-byte aligned");
+    double integral       = 0.0;
+    float shadingIntegral = 0.f;
+    AGB_CUDA(buildEnvAliasNoAlloc(reinterpret_cast<const float4*>(rgba_device), width, height, layout,
+                 table_device, &integral, &shadingIntegral, static_cast<cudaStream_t>(stream)),
+        "agb_environment_alias_build_noalloc");
+    if (shading_integral)
+        *shading_integral = shadingIntegral;
+    if (fp64_integral)
+        *fp64_integral = integral;
+    return AGB_OK;
+}
+
 AGB_API agb_status agb_frame_set(agb_context* ctx, const agb_frame_data* frame)
 {
     if (!ctx || !frame)

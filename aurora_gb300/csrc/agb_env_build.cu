@@ -506,6 +506,9 @@ void freeEnvScratch(EnvBuildScratch& s)
     s = EnvBuildScratch();
 }
 
+size_t envScratchTileDoubles(uint32_t texels) { return size_t((texels + kScanTile - 1) / kScanTile) * 3 + 8; }
+size_t envScratchTileCounts(uint32_t texels) { return size_t((texels + kScanTile - 1) / kScanTile) + 8; }
+
 cudaError_t buildEnvAlias(const float4* rgba, uint32_t width, uint32_t height, int layout,
     const float* rowSolidAngle, agb_alias_entry* out, double* integralFP64Out,
     float* integralShadingOut, EnvBuildScratch& s, cudaStream_t st)
@@ -515,7 +518,7 @@ cudaError_t buildEnvAlias(const float4* rgba, uint32_t width, uint32_t height, i
     if (s.capacity < n || s.rows < height)
     {
         freeEnvScratch(s);
-        size_t tileCap = size_t(tiles) * 3 + 8;
+        size_t tileCap = envScratchTileDoubles(n);
         cudaError_t e  = cudaSuccess;
         if ((e = cudaMalloc(&s.weights, sizeof(double) * n)) != cudaSuccess ||
             (e = cudaMalloc(&s.scanA, sizeof(double) * n)) != cudaSuccess ||
@@ -524,7 +527,7 @@ cudaError_t buildEnvAlias(const float4* rgba, uint32_t width, uint32_t height, i
             (e = cudaMalloc(&s.heavyIncl, sizeof(double) * n)) != cudaSuccess ||
             (e = cudaMalloc(&s.lightIncl, sizeof(double) * n)) != cudaSuccess ||
             (e = cudaMalloc(&s.blockSums, sizeof(double) * tileCap)) != cudaSuccess ||
-            (e = cudaMalloc(&s.blockCounts, sizeof(uint32_t) * (tiles + 8))) != cudaSuccess ||
+            (e = cudaMalloc(&s.blockCounts, sizeof(uint32_t) * envScratchTileCounts(n))) != cudaSuccess ||
             (e = cudaMalloc(&s.rowSA, sizeof(float) * height + 16)) != cudaSuccess)
         {
             freeEnvScratch(s);
@@ -533,6 +536,16 @@ cudaError_t buildEnvAlias(const float4* rgba, uint32_t width, uint32_t height, i
         s.capacity = n;
         s.rows     = height;
     }
+    return launchEnvAliasBuild(rgba, width, height, layout, rowSolidAngle, out, integralFP64Out,
+        integralShadingOut, s, st);
+}
+
+cudaError_t launchEnvAliasBuild(const float4* rgba, uint32_t width, uint32_t height, int layout,
+    const float* rowSolidAngle, agb_alias_entry* out, double* integralFP64Out,
+    float* integralShadingOut, const EnvBuildScratch& s, cudaStream_t st)
+{
+    uint32_t n       = width * height;
+    uint32_t tiles   = (n + kScanTile - 1) / kScanTile;
     float* lum       = reinterpret_cast<float*>(s.ranks + n); // second half of ranks
     double* tileW    = s.blockSums;
     double* tileDef  = s.blockSums + tiles;
@@ -565,10 +578,13 @@ cudaError_t buildEnvAlias(const float4* rgba, uint32_t width, uint32_t height, i
         uint32_t* alias   = reinterpret_cast<uint32_t*>(s.heavyIncl) + n;
         uint32_t* indexMap = reinterpret_cast<uint32_t*>(s.lightIncl);
         uint32_t* smallCount = lightCount;
-        cudaError_t e = cudaMemcpyAsync(s.rowSA, rowSolidAngle, sizeof(float) * height,
-            cudaMemcpyHostToDevice, st);
-        if (e != cudaSuccess)
-            return e;
+        if (rowSolidAngle)
+        {
+            cudaError_t e = cudaMemcpyAsync(s.rowSA, rowSolidAngle, sizeof(float) * height,
+                cudaMemcpyHostToDevice, st);
+            if (e != cudaSuccess)
+                return e;
+        }
         k_ref_lum<<<(n + 255) / 256, 256, 0, st>>>(rgba, width, n, s.rowSA, lum, lumArea);
         k_ref_seq_sum<<<1, 32, 0, st>>>(lumArea, n, shadingIntegral);
         k_ref_probs<<<tiles, kScanThreads, 0, st>>>(lum, lumArea, n, shadingIntegral, prob, pdf,

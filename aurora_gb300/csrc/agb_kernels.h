@@ -94,6 +94,20 @@ cudaError_t buildEnvAlias(const float4* rgba, uint32_t width, uint32_t height, i
     const float* rowSolidAngle, agb_alias_entry* out, double* integralFP64Out,
     float* integralShadingOut, EnvBuildScratch& scratch, cudaStream_t st);
 void freeEnvScratch(EnvBuildScratch& s);
+// The kernel sequence of buildEnvAlias on scratch that is already large enough (capacity >= texels,
+// rows >= height; the tile arrays sized by the two helpers below).  rowSolidAngle: host array of
+// per-row solid angles copied into scratch.rowSA, or null when scratch.rowSA already holds them.
+// Synchronises the stream before returning.
+cudaError_t launchEnvAliasBuild(const float4* rgba, uint32_t width, uint32_t height, int layout,
+    const float* rowSolidAngle, agb_alias_entry* out, double* integralFP64Out,
+    float* integralShadingOut, const EnvBuildScratch& scratch, cudaStream_t st);
+size_t envScratchTileDoubles(uint32_t texels); // blockSums entries
+size_t envScratchTileCounts(uint32_t texels);  // blockCounts entries
+
+// agb_env_noalloc.cu: the same build on a fixed scratch array in the library's device image.
+// Returns cudaErrorInvalidValue when width * height exceeds AGB_ENV_NOALLOC_MAX_TEXELS.
+cudaError_t buildEnvAliasNoAlloc(const float4* rgba, uint32_t width, uint32_t height, int layout,
+    agb_alias_entry* out, double* integralFP64Out, float* integralShadingOut, cudaStream_t st);
 
 // agb_bvh_build.cpp: host binned-SAH builder producing the device layout.
 struct BuiltBVH

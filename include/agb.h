@@ -355,6 +355,29 @@ enum
 };
 AGB_API agb_status agb_set_environment_table(agb_context* ctx, int32_t layout);
 
+/* Builds the environment alias table like agb_environment_set (same kernels, same table and
+ * integrals) without allocating any memory.  No counterpart in the reference: it is for hosts
+ * that cannot allocate when the light image changes (a host whose device memory is all handed
+ * out by its own allocator or budget, or one that must not stall other streams on cudaMalloc /
+ * cudaFree).
+ *   rgba_device  width*height RGBA32F texels in device memory, rows from the top, 16-byte aligned
+ *   table_device width*height entries of device memory, 16-byte aligned
+ *   layout       AGB_ENV_TABLE_REFERENCE or AGB_ENV_TABLE_FP64
+ *   shading_integral, fp64_integral: host outputs, either may be null
+ *   stream       a cudaStream_t of the current device (null: legacy default stream)
+ * Scratch is one fixed array in the library's device image (about 12.6 MB, reserved by the CUDA
+ * driver when it loads this part of the library), so width*height is at most
+ * AGB_ENV_NOALLOC_MAX_TEXELS; larger images are rejected with AGB_ERR_LIMIT.  Works on the
+ * current device.  The first call on each device does one-time setup (it looks up the scratch
+ * address, which can make the driver load the module): make it before any stream capture.
+ * Returns after the stream has finished the build.  All calls on a device share the one scratch
+ * array: calls that overlap in time (two host threads, or two streams) race and corrupt each
+ * other's tables, so callers serialise them. */
+#define AGB_ENV_NOALLOC_MAX_TEXELS 262144u /* e.g. 512 x 512, 724 x 362 or 1024 x 256 */
+AGB_API agb_status agb_environment_alias_build_noalloc(const float* rgba_device, uint32_t width,
+    uint32_t height, int32_t layout, agb_alias_entry* table_device, double* shading_integral,
+    double* fp64_integral, void* stream);
+
 /* ------------------------------------------------------------------------------------------ */
 /* Rendering.                                                                                  */
 /* ------------------------------------------------------------------------------------------ */
