@@ -64,7 +64,7 @@ AGB_D WtRay wtSetup(v3 o, v3 d)
 
 // Watertight test; accepts tmin <= t < tmax.
 AGB_D bool wtIntersect(const WtRay& r, float4 a4, float4 b4, float4 c4, float tmin, float tmax,
-    float& t, float& u, float& v)
+    bool inclusive, float& t, float& u, float& v)
 {
     v3 A = v3{ __fsub_rn(a4.x, r.o.x), __fsub_rn(a4.y, r.o.y), __fsub_rn(a4.z, r.o.z) };
     v3 B = v3{ __fsub_rn(b4.x, r.o.x), __fsub_rn(b4.y, r.o.y), __fsub_rn(b4.z, r.o.z) };
@@ -95,7 +95,7 @@ AGB_D bool wtIntersect(const WtRay& r, float4 a4, float4 b4, float4 c4, float tm
     float Tn  = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
     float rcp = __fdiv_rn(1.f, det);
     float tt  = __fmul_rn(Tn, rcp);
-    if (!(tt >= tmin && tt < tmax))
+    if (!(tt >= tmin && (tt < tmax || (inclusive && tt == tmax))))
         return false;
     t = tt;
     u = __fmul_rn(V, rcp);
@@ -126,6 +126,14 @@ struct SlabRay
     v3 inv;  // 1 / direction (tiny components clamped)
     v3 oinv; // origin * inv
 };
+// Reciprocal with about 1 ulp error (PTX rcp.approx); the slab test only culls, and its boxes are
+// widened by about 8 ulp, so it does not need a correctly rounded reciprocal.
+AGB_D float rcpApprox(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 AGB_D SlabRay slabSetup(v3 o, v3 d)
 {
     const float eps = 1e-20f;
@@ -133,7 +141,7 @@ AGB_D SlabRay slabSetup(v3 o, v3 d)
     float dy = fabsf(d.y) > eps ? d.y : copysignf(eps, d.y);
     float dz = fabsf(d.z) > eps ? d.z : copysignf(eps, d.z);
     SlabRay s;
-    s.inv  = v3{ 1.f / dx, 1.f / dy, 1.f / dz };
+    s.inv  = v3{ rcpApprox(dx), rcpApprox(dy), rcpApprox(dz) };
     s.oinv = v3{ o.x * s.inv.x, o.y * s.inv.y, o.z * s.inv.z };
     return s;
 }
@@ -160,165 +168,35 @@ AGB_D void slab2(const SlabRay& s, float4 c0xy, float4 c1xy, float4 cz, float tm
     t1 = n1;
 }
 
-// Traverses one instance's BLAS with the object-space ray; the stack region above `base` is used.
-// closest: updates hit/tmax; anyHit: returns true at the first hit.
-template <bool kAnyHit, bool kCount>
-AGB_D bool traverseBLAS(const DevMesh& m, int32_t inst, v3 oo, v3 od, float tmin, float& tmax,
-    RayHit& hit, int32_t* stack, int base, int stride, TraceCounters& cnt, bool& overflow)
-{
-    WtRay wr   = wtSetup(oo, od);
-    SlabRay sr = slabSetup(oo, od);
-    int sp     = base;
-    int32_t ref = m.root;
-    bool found = false;
-    for (;;)
-    {
-        if (ref >= 0)
-        {
-            const float4* np = reinterpret_cast<const float4*>(m.nodes + ref);
-            float4 c0xy = __ldg(np), c1xy = __ldg(np + 1), cz = __ldg(np + 2);
-            int4 refs   = __ldg(reinterpret_cast<const int4*>(np + 3));
-            if (kCount)
-                cnt.nodes++;
-            bool h0, h1;
-            float t0, t1;
-            slab2(sr, c0xy, c1xy, cz, tmin, tmax, h0, h1, t0, t1);
-            if (h0 && h1)
-            {
-                int32_t nearRef = t0 <= t1 ? refs.x : refs.y;
-                int32_t farRef  = t0 <= t1 ? refs.y : refs.x;
-                if (sp >= kStackSize - 1)
-                {
-                    overflow = true;
-                    return found;
-                }
-                stack[sp * stride] = farRef;
-                sp++;
-                ref = nearRef;
-                continue;
-            }
-            if (h0 || h1)
-            {
-                ref = h0 ? refs.x : refs.y;
-                continue;
-            }
-        }
-        else
-        {
-            uint32_t code  = uint32_t(~ref);
-            uint32_t first = code >> 3, count = (code & 7u) + 1u;
-            for (uint32_t k = 0; k < count; k++)
-            {
-                const float4* tp = m.tris + 3 * size_t(first + k);
-                float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-                if (kCount)
-                    cnt.tris++;
-                float t, u, v;
-                if (wtIntersect(wr, a, b, c, tmin, tmax, t, u, v))
-                {
-                    found    = true;
-                    tmax     = t;
-                    hit.t    = t;
-                    hit.u    = u;
-                    hit.v    = v;
-                    hit.inst = inst;
-                    hit.prim = __float_as_int(a.w);
-                    if (kAnyHit)
-                        return true;
-                }
-            }
-        }
-        if (sp == base)
-            break;
-        sp--;
-        ref = stack[sp * stride];
-    }
-    return found;
-}
-
-// Full two-level cast of a world-space ray.  stack: this thread's column of the block's
-// shared-memory stack (entry i at stack[i * stride]).
-template <bool kAnyHit, bool kCount>
-AGB_D bool castRay(const DevScene& s, v3 o, v3 d, float tmin, float tmax, RayHit& hit,
-    int32_t* stack, int stride, TraceCounters& cnt, bool& overflow)
-{
-    hit.t = -1.f;
-    hit.inst = hit.prim = -1;
-    if (s.instanceCount <= 0)
-        return false;
-    SlabRay sr = slabSetup(o, d);
-    int sp     = 0;
-    int32_t ref = s.tlasRoot;
-    bool found = false;
-    for (;;)
-    {
-        if (ref >= 0)
-        {
-            const float4* np = reinterpret_cast<const float4*>(s.tlas + ref);
-            float4 c0xy = __ldg(np), c1xy = __ldg(np + 1), cz = __ldg(np + 2);
-            int4 refs   = __ldg(reinterpret_cast<const int4*>(np + 3));
-            if (kCount)
-                cnt.nodes++;
-            bool h0, h1;
-            float t0, t1;
-            slab2(sr, c0xy, c1xy, cz, tmin, tmax, h0, h1, t0, t1);
-            if (h0 && h1)
-            {
-                if (sp >= kStackSize - 1)
-                {
-                    overflow = true;
-                    return found;
-                }
-                stack[sp * stride] = t0 <= t1 ? refs.y : refs.x;
-                sp++;
-                ref = t0 <= t1 ? refs.x : refs.y;
-                continue;
-            }
-            if (h0 || h1)
-            {
-                ref = h0 ? refs.x : refs.y;
-                continue;
-            }
-        }
-        else
-        {
-            uint32_t code  = uint32_t(~ref);
-            uint32_t first = code >> 3, count = (code & 7u) + 1u;
-            for (uint32_t k = 0; k < count; k++)
-            {
-                int32_t ii = __ldg(s.tlasOrder + first + k);
-                const DevInstance& in = s.instances[ii];
-                v3 oo = xfPointRn(in.w2o, o);
-                v3 od = xfVectorRn(in.w2o, d);
-                if (traverseBLAS<kAnyHit, kCount>(s.meshes[in.mesh], ii, oo, od, tmin, tmax, hit,
-                        stack, sp, stride, cnt, overflow))
-                {
-                    found = true;
-                    if (kAnyHit)
-                        return true;
-                }
-                if (overflow)
-                    return found;
-            }
-        }
-        if (sp == 0)
-            break;
-        sp--;
-        ref = stack[sp * stride];
-    }
-    return found;
-}
-
 // ------------------------------------------------------------------ persistent traversal
-// Each warp loops over a shared work counter.  A lane whose ray has finished takes the next ray
-// index at once (one atomic per warp per refill), so no lane idles while a slower ray in its warp
-// is still traversing (Aila & Laine, "Understanding the Efficiency of Ray Traversal on GPUs",
-// HPG 2009, persistent threads with per-lane fetch).  The two-level traversal is a resumable
-// per-lane state machine: entering an instance pushes kExitInstance on the shared-memory stack;
-// popping it restores the world ray and the TLAS.
+// Each warp loops over a shared work counter: lanes whose ray has finished take the next ray
+// indices (one atomic per warp per refill), so no lane idles while a slower ray in its warp is
+// still traversing (Aila & Laine, "Understanding the Efficiency of Ray Traversal on GPUs",
+// HPG 2009: persistent threads, while-while traversal with postponed leaves).
+//
+// Every outer iteration has three phases with uniform work inside each, so the lanes of a warp run
+// the same instructions together:
+//   node phase      lanes step through internal nodes (TLAS or BLAS).  A lane that reaches a BLAS
+//                   leaf parks it in `leaf` and keeps traversing speculatively; a lane that reaches
+//                   an instance boundary waits.  The phase ends once every lane holds a parked leaf,
+//                   waits at a boundary or has finished.
+//   leaf phase      lanes with a parked leaf test its triangles.
+//   boundary phase  lanes at a TLAS leaf enter its instance (object-space ray, watertight and slab
+//                   setup); lanes at kExitInstance return to the world-space ray and the TLAS.
+// Entering an instance pushes kExitInstance on the shared-memory stack; popping it restores the
+// world-space ray and the TLAS.  A parked leaf belongs to the instance the lane is in, so a lane
+// with a parked leaf stops at an instance boundary until the leaf has been tested.
+//
+// Closest hit keeps the smallest (t, instance, triangle): a triangle at exactly the current t
+// replaces the hit only with a smaller (instance, triangle) key, so the result does not depend on
+// traversal order (edges shared by two triangles give equal t).
 
-constexpr int32_t kExitInstance   = int32_t(0x80000000); // never a node or leaf ref
-constexpr int kStepsPerRefill     = 24;                  // node / leaf steps between refill checks
+constexpr int32_t kExitInstance = int32_t(0x80000000);
+// No leaf ref equals kExitInstance or kDone: leaves hold at most 4 triangles (low 3 bits <= 3) and
+// meshes at most 2^28 triangles.
+constexpr int32_t kDone = int32_t(0x80000001);
+
+AGB_D bool isLeafRef(int32_t ref) { return ref < 0 && ref != kExitInstance && ref != kDone; }
 
 template <bool kAnyHit, bool kCount, class Loader, class Writer>
 AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const Loader& load,
@@ -332,17 +210,23 @@ AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const 
     float tmin = 0.f, tmax = 0.f;
     SlabRay sr;
     WtRay wr;
-    int32_t ref = 0;
-    int sp      = 0;
+    int32_t ref = kDone, leaf = 0;
+    int sp       = 0;
     int32_t inst = -1;
     const float4* nodes = nullptr;
     const float4* tris  = nullptr;
     RayHit hit;
     bool found = false;
+    auto pop = [&]() -> int32_t {
+        if (sp == 0)
+            return kDone;
+        sp--;
+        return stack[sp * stride];
+    };
     for (;;)
     {
         // Refill lanes whose ray is done.
-        bool need       = !active && !exhausted;
+        bool need         = !active && !exhausted;
         unsigned needMask = __ballot_sync(FULL, need);
         if (needMask)
         {
@@ -358,16 +242,15 @@ AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const 
                 {
                     load(rayIdx, o, d, tmin, tmax);
                     sr       = slabSetup(o, d);
-                    ref      = s.instanceCount > 0 ? s.tlasRoot : kExitInstance;
+                    ref      = s.instanceCount > 0 ? s.tlasRoot : kDone;
+                    leaf     = 0;
                     sp       = 0;
                     inst     = -1;
                     nodes    = reinterpret_cast<const float4*>(s.tlas);
                     found    = false;
                     hit.inst = hit.prim = -1;
                     hit.t = hit.u = hit.v = 0.f;
-                    active   = s.instanceCount > 0;
-                    if (!active)
-                        write(rayIdx, false, hit);
+                    active   = true;
                 }
                 else
                     exhausted = true;
@@ -375,116 +258,121 @@ AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const 
         }
         if (__all_sync(FULL, exhausted))
             break;
-        if (!__any_sync(FULL, active))
-            continue;
-        if (active)
+
+        // Node phase: internal nodes only.  A lane stops at a BLAS leaf (parked in `leaf`; it goes
+        // on speculatively through internal nodes), at an instance boundary (TLAS leaf or
+        // kExitInstance) or at the end of its ray.
+        for (;;)
         {
-            bool done = false;
-            for (int step = 0; step < kStepsPerRefill && !done; step++)
+            if (active && leaf == 0 && inst >= 0 && isLeafRef(ref))
             {
-                if (ref >= 0)
+                leaf = ref;
+                ref  = pop();
+            }
+            bool nodeWork = active && ref >= 0;
+            if (!__any_sync(FULL, nodeWork && leaf == 0))
+                break;
+            if (!nodeWork)
+                continue;
+            const float4* np = nodes + 4 * size_t(ref);
+            float4 c0xy = __ldg(np), c1xy = __ldg(np + 1), cz = __ldg(np + 2);
+            int4 refs   = __ldg(reinterpret_cast<const int4*>(np + 3));
+            if (kCount)
+                cnt.nodes++;
+            bool h0, h1;
+            float t0, t1;
+            slab2(sr, c0xy, c1xy, cz, tmin, tmax, h0, h1, t0, t1);
+            if (h0 && h1)
+            {
+                if (sp >= kStackSize - 1)
                 {
-                    const float4* np = nodes + 4 * size_t(ref);
-                    float4 c0xy = __ldg(np), c1xy = __ldg(np + 1), cz = __ldg(np + 2);
-                    int4 refs   = __ldg(reinterpret_cast<const int4*>(np + 3));
-                    if (kCount)
-                        cnt.nodes++;
-                    bool h0, h1;
-                    float t0, t1;
-                    slab2(sr, c0xy, c1xy, cz, tmin, tmax, h0, h1, t0, t1);
-                    if (h0 && h1)
-                    {
-                        if (sp >= kStackSize - 1)
-                        {
-                            overflow = true;
-                            done     = true;
-                            break;
-                        }
-                        stack[sp * stride] = t0 <= t1 ? refs.y : refs.x;
-                        sp++;
-                        ref = t0 <= t1 ? refs.x : refs.y;
-                        continue;
-                    }
-                    if (h0 || h1)
-                    {
-                        ref = h0 ? refs.x : refs.y;
-                        continue;
-                    }
+                    overflow = true;
+                    ref = kDone, leaf = 0, sp = 0;
+                    continue;
                 }
-                else if (ref == kExitInstance)
+                stack[sp * stride] = t0 <= t1 ? refs.y : refs.x;
+                sp++;
+                ref = t0 <= t1 ? refs.x : refs.y;
+            }
+            else if (h0 || h1)
+                ref = h0 ? refs.x : refs.y;
+            else
+                ref = pop();
+        }
+
+        // Leaf phase.
+        if (leaf != 0)
+        {
+            uint32_t code  = uint32_t(~leaf);
+            uint32_t first = code >> 3, count = (code & 7u) + 1u;
+            leaf           = 0;
+            for (uint32_t k = 0; k < count; k++)
+            {
+                const float4* tp = tris + 3 * size_t(first + k);
+                float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                if (kCount)
+                    cnt.tris++;
+                float t, u, v;
+                if (wtIntersect(wr, a, b, c, tmin, tmax, !kAnyHit && found, t, u, v))
                 {
-                    inst  = -1;
-                    nodes = reinterpret_cast<const float4*>(s.tlas);
-                    sr    = slabSetup(o, d);
-                }
-                else
-                {
-                    uint32_t code  = uint32_t(~ref);
-                    uint32_t first = code >> 3, count = (code & 7u) + 1u;
-                    if (inst < 0)
+                    int32_t prim = __float_as_int(a.w);
+                    if (!found || t < tmax || inst < hit.inst || (inst == hit.inst && prim < hit.prim))
                     {
-                        // TLAS leaf: one instance (the TLAS is built with single-instance leaves).
-                        int32_t ii = __ldg(s.tlasOrder + first);
-                        const DevInstance& in = s.instances[ii];
-                        const DevMesh& m      = s.meshes[in.mesh];
-                        if (sp >= kStackSize - 1)
-                        {
-                            overflow = true;
-                            done     = true;
-                            break;
-                        }
-                        stack[sp * stride] = kExitInstance;
-                        sp++;
-                        v3 oo = xfPointRn(in.w2o, o);
-                        v3 od = xfVectorRn(in.w2o, d);
-                        wr    = wtSetup(oo, od);
-                        sr    = slabSetup(oo, od);
-                        inst  = ii;
-                        nodes = reinterpret_cast<const float4*>(m.nodes);
-                        tris  = m.tris;
-                        ref   = m.root;
-                        continue;
+                        found    = true;
+                        tmax     = t;
+                        hit.t    = t;
+                        hit.u    = u;
+                        hit.v    = v;
+                        hit.inst = inst;
+                        hit.prim = prim;
                     }
-                    for (uint32_t k = 0; k < count; k++)
+                    if (kAnyHit)
                     {
-                        const float4* tp = tris + 3 * size_t(first + k);
-                        float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-                        if (kCount)
-                            cnt.tris++;
-                        float t, u, v;
-                        if (wtIntersect(wr, a, b, c, tmin, tmax, t, u, v))
-                        {
-                            found    = true;
-                            tmax     = t;
-                            hit.t    = t;
-                            hit.u    = u;
-                            hit.v    = v;
-                            hit.inst = inst;
-                            hit.prim = __float_as_int(a.w);
-                            if (kAnyHit)
-                                break;
-                        }
-                    }
-                    if (kAnyHit && found)
-                    {
-                        done = true;
+                        ref = kDone, sp = 0;
                         break;
                     }
                 }
-                // Pop the next entry; an empty stack ends the ray.
-                if (sp == 0)
-                {
-                    done = true;
-                    break;
-                }
-                sp--;
-                ref = stack[sp * stride];
             }
-            if (done)
+        }
+
+        // Instance boundaries, taken together by the lanes that reached one.
+        if (active && leaf == 0 && ref == kExitInstance)
+        {
+            inst  = -1;
+            nodes = reinterpret_cast<const float4*>(s.tlas);
+            sr    = slabSetup(o, d);
+            ref   = pop();
+        }
+        else if (active && leaf == 0 && inst < 0 && isLeafRef(ref))
+        {
+            // TLAS leaf: one instance (the TLAS is built with single-instance leaves).
+            if (sp >= kStackSize - 1)
             {
-                write(rayIdx, found, hit);
-                active = false;
+                overflow = true;
+                ref = kDone, sp = 0;
             }
+            else
+            {
+                uint32_t first = uint32_t(~ref) >> 3;
+                int32_t ii     = __ldg(s.tlasOrder + first);
+                const DevInstance& in = s.instances[ii];
+                const DevMesh& m      = s.meshes[in.mesh];
+                stack[sp * stride] = kExitInstance;
+                sp++;
+                v3 oo = xfPointRn(in.w2o, o);
+                v3 od = xfVectorRn(in.w2o, d);
+                wr    = wtSetup(oo, od);
+                sr    = slabSetup(oo, od);
+                inst  = ii;
+                nodes = reinterpret_cast<const float4*>(m.nodes);
+                tris  = m.tris;
+                ref   = m.root;
+            }
+        }
+        if (active && ref == kDone && leaf == 0)
+        {
+            write(rayIdx, found, hit);
+            active = false;
         }
     }
 }

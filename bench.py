@@ -138,28 +138,36 @@ def measured_peaks():
         return None
 
 
-def cpu_render_rate(s, seconds, start_row=None):
-    """Oracle FP32 on all host cores over a band of rows at 1 spp; returns (paths/s, threads,
+def cpu_sample_plan(o, s, seconds, threads):
+    """Sizes a bounded CPU sample of the frame: a band of rows around the middle, and more than
+    one sample index once the whole frame takes less than `seconds`.  Returns (rect, spp)."""
+    mid = s.height // 2
+    probe_rows = max(4, s.height // 64)
+    rect = (0, mid - probe_rows // 2, s.width, mid - probe_rows // 2 + probe_rows)
+    r = o.render(0, 1, threads=threads, rect=rect, want_mean=False)
+    rate = s.width * probe_rows / max(r["seconds"], 1e-6)
+    want = rate * seconds
+    rows = int(min(s.height, max(probe_rows, want / s.width)))
+    spp = int(max(1, min(s.spp, round(want / (s.width * rows)))))
+    y0 = max(0, mid - rows // 2)
+    return (0, y0, s.width, y0 + rows), spp
+
+
+def cpu_render_rate(s, seconds):
+    """Oracle FP32 on all host cores over a bounded part of the frame; returns (paths/s, threads,
     description)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     o = pyoracle.OracleScene(s)
     threads = os.cpu_count() or 1
     o.tracer(32)  # build the BVHs outside the timed part
-    mid = s.height // 2
-    probe_rows = max(4, s.height // 64)
-    rect = (0, mid - probe_rows // 2, s.width, mid - probe_rows // 2 + probe_rows)
-    r = o.render(0, 1, threads=threads, rect=rect, want_mean=False)
-    rate = s.width * probe_rows / max(r["seconds"], 1e-6)
-    rows = int(min(s.height, max(probe_rows, rate * seconds / s.width)))
-    y0 = max(0, mid - rows // 2)
-    rect = (0, y0, s.width, y0 + rows)
-    r = o.render(1, 1, threads=threads, rect=rect, want_mean=False)
-    paths = s.width * rows
+    rect, spp = cpu_sample_plan(o, s, seconds, threads)
+    r = o.render(1, spp, threads=threads, rect=rect, want_mean=False)
+    paths = (rect[2] - rect[0]) * (rect[3] - rect[1]) * spp
     o.close()
     return paths / r["seconds"], threads, (
-        f"rows {y0}-{y0 + rows} of the {s.width}x{s.height} frame at 1 spp (sample index 1), "
-        f"{paths} path samples, {r['seconds']:.1f} s, FP32 oracle, BVH build excluded")
+        f"rows {rect[1]}-{rect[3]} of the {s.width}x{s.height} frame at {spp} spp (sample indices "
+        f"1-{spp}), {paths} path samples, {r['seconds']:.1f} s, FP32 oracle, BVH build excluded")
 
 
 def run_reference(args):
@@ -172,24 +180,18 @@ def run_reference(args):
     o = pyoracle.OracleScene(s)
     threads = os.cpu_count() or 1
     o.tracer(32)
-    # Each step: a band of rows at 1 spp sized to ~10 s on this host.
-    mid = s.height // 2
-    probe_rows = max(4, s.height // 64)
-    rect = (0, mid - probe_rows // 2, s.width, mid - probe_rows // 2 + probe_rows)
-    r = o.render(0, 1, threads=threads, rect=rect, want_mean=False)
-    rate = s.width * probe_rows / max(r["seconds"], 1e-6)
-    rows = int(min(s.height, max(probe_rows, rate * 10.0 / s.width)))
-    y0 = max(0, mid - rows // 2)
-    rect = (0, y0, s.width, y0 + rows)
+    # Each step: a bounded part of the frame sized to ~10 s on this host.
+    rect, spp = cpu_sample_plan(o, s, 10.0, threads)
     for w in range(args.warmup):
-        o.render(w, 1, threads=threads, rect=rect, want_mean=False)
+        o.render(w * spp, spp, threads=threads, rect=rect, want_mean=False)
     secs = 0.0
     for k in range(args.steps):
-        secs += o.render(args.warmup + k, 1, threads=threads, rect=rect, want_mean=False)["seconds"]
-    paths = s.width * rows * args.steps
+        secs += o.render((args.warmup + k) * spp, spp, threads=threads, rect=rect,
+                         want_mean=False)["seconds"]
+    paths = (rect[2] - rect[0]) * (rect[3] - rect[1]) * spp * args.steps
     value = paths / secs
-    sample = (f"rows {y0}-{y0 + rows} of the {s.width}x{s.height} frame, 1 spp per step, FP32 "
-              f"oracle port of the reference shaders on {threads} host threads")
+    sample = (f"rows {rect[1]}-{rect[3]} of the {s.width}x{s.height} frame, {spp} spp per step, "
+              f"FP32 oracle port of the reference shaders on {threads} host threads")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / args.steps,
@@ -321,6 +323,11 @@ def main():
                 "ms_per_step": 1000.0 * e2e_time / args.steps},
         "gpu_launches": int(launches),
         "rays_per_step": {"closest": counted["closest_rays"], "shadow": counted["shadow_rays"]},
+        "per_ray": {
+            "closest_node_visits": counted["node_visits"] / max(1, counted["closest_rays"]),
+            "closest_tri_tests": counted["tri_tests"] / max(1, counted["closest_rays"]),
+            "shadow_node_visits": counted["shadow_node_visits"] / max(1, counted["shadow_rays"]),
+            "shadow_tri_tests": counted["shadow_tri_tests"] / max(1, counted["shadow_rays"])},
         "roofline": roofline,
         "clocks": clk,
     }

@@ -6,7 +6,8 @@
 //     double-precision re-evaluation of edge functions that come out exactly zero, barycentrics
 //     reported as (u, v) = weights of vertices 1 and 2 (Shaders/Geometry.slang:108-118);
 //   * a binned-SAH BVH2 per mesh and one over the instances, or brute force (checker of checkers);
-//   * closest hit accepts tmin <= t < tmax; shadow rays accept any hit (RAY_FLAG_ACCEPT_FIRST_HIT).
+//   * closest hit accepts tmin <= t < tmax and keeps the smallest (t, instance, triangle); shadow
+//     rays accept any hit (RAY_FLAG_ACCEPT_FIRST_HIT).
 // Rays are intersected in object space: origin and direction go through the instance's
 // world-to-object transform without renormalisation, so t is shared by all instances.
 #pragma once
@@ -70,9 +71,9 @@ struct WatertightRay
         Sy = d[ky] / d[kz];
         Sz = T(1) / d[kz];
     }
-    // Returns true and writes t/u/v when tmin <= t < tmax.
-    bool intersect(const V3<T>& p0, const V3<T>& p1, const V3<T>& p2, T tmin, T tmax, T& tOut,
-        T& uOut, T& vOut) const
+    // Returns true and writes t/u/v when tmin <= t < tmax (t <= tmax when inclusive).
+    bool intersect(const V3<T>& p0, const V3<T>& p1, const V3<T>& p2, T tmin, T tmax, bool inclusive,
+        T& tOut, T& uOut, T& vOut) const
     {
         V3<T> A = p0 - org, B = p1 - org, C = p2 - org;
         T Ax = A[kx] - Sx * A[kz], Ay = A[ky] - Sy * A[kz];
@@ -96,7 +97,7 @@ struct WatertightRay
         T Tn  = U * Az + V * Bz + W * Cz;
         T rcp = T(1) / det;
         T t   = Tn * rcp;
-        if (!(t >= tmin && t < tmax))
+        if (!(t >= tmin && (t < tmax || (inclusive && t == tmax))))
             return false;
         tOut = t;
         uOut = V * rcp;
@@ -361,11 +362,17 @@ struct Caster
         WatertightRay<T> wr;
         wr.setup(o, d);
         bool found = false;
+        // Closest hit keeps the smallest (t, instance, triangle), so the result does not depend on
+        // the order triangles are tested in (a hit on an edge shared by two triangles has equal t).
         auto testTri = [&](uint32_t tri) -> bool {
             T t, u, v;
-            if (wr.intersect(vertex(m, tri, 0), vertex(m, tri, 1), vertex(m, tri, 2), tmin, tmax, t,
-                    u, v))
+            bool have = best.inst >= 0;
+            if (wr.intersect(vertex(m, tri, 0), vertex(m, tri, 1), vertex(m, tri, 2), tmin, tmax,
+                    !anyHit && have, t, u, v))
             {
+                if (have && !anyHit && !(t < tmax) &&
+                    !(inst < best.inst || (inst == best.inst && int32_t(tri) < best.prim)))
+                    return false;
                 tmax      = t;
                 best.t    = float(t);
                 best.u    = float(u);
@@ -420,6 +427,7 @@ struct Caster
     bool cast(const V3<T>& o, const V3<T>& d, T tmin, T tmax, Hit& hit, bool anyHit) const
     {
         bool found = false;
+        hit        = Hit();
         auto visit = [&](int32_t i) -> bool {
             V3<T> oo, od;
             objectRay(i, o, d, oo, od);
