@@ -416,7 +416,7 @@ AGB_D MatCommon prepare(const Mat& m, const Frame& f)
 }
 
 // evaluateMaterial (StandardSurfaceBSDF.slang:598-718): BSDF x cosine for world V, L.
-AGB_D v3 evaluateMaterial(const Mat& m, const Frame& f, v3 Vw, v3 Lw)
+AGB_DN v3 evaluateMaterial(const Mat& m, const Frame& f, v3 Vw, v3 Lw)
 {
     MatCommon c = prepare(m, f);
     v3 dif      = diffuseReflection(Lw, Vw, m.base, c.diffuseColor, m.diffuseRoughness, f.N);
@@ -486,7 +486,7 @@ AGB_D v3 computeRefraction(v3 V, float ior, bool& reflected)
 }
 
 // evaluateMaterialAndPDF (StandardSurfaceBSDF.slang:862-1088).
-AGB_D v3 evaluateMaterialAndPDF(const Mat& m, const Frame& f, v3 Vw, v3 Lw, v2 rnd, float& pdf,
+AGB_DN v3 evaluateMaterialAndPDF(const Mat& m, const Frame& f, v3 Vw, v3 Lw, v2 rnd, float& pdf,
     int& lobe)
 {
     v3 V        = toTangent(Vw, f);
@@ -557,7 +557,7 @@ AGB_D v3 evaluateMaterialAndPDF(const Mat& m, const Frame& f, v3 Vw, v3 Lw, v2 r
 }
 
 // sampleMaterial (StandardSurfaceBSDF.slang:1093-1372).
-AGB_D v3 sampleMaterial(const Mat& m, const Frame& f, v3 Vw, v2 rnd, v3& Lw, float& pdf,
+AGB_DN v3 sampleMaterial(const Mat& m, const Frame& f, v3 Vw, v2 rnd, v3& Lw, float& pdf,
     int& lobe)
 {
     v3 L;

@@ -10,6 +10,14 @@
 
 #define AGB_HD __host__ __device__ __forceinline__
 #define AGB_D __device__ __forceinline__
+// The large shading functions (BSDF evaluate / sample, environment lookups) are called from
+// several places in the shading kernel; keeping one out-of-line copy of each keeps that kernel's
+// code within the instruction cache.
+#ifdef AGB_BSDF_INLINE
+#define AGB_DN __device__ __forceinline__
+#else
+#define AGB_DN static __device__ __noinline__
+#endif
 
 namespace agb
 {

@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_shadow
 
 // -------------------------------------------------------------------------------- shading
 // ShadeFunctions.slang:51-89
-__device__ __forceinline__ v3 shadeDistantLight(const agb_distant_light& l, const Mat& m,
+AGB_DN v3 shadeDistantLight(const agb_distant_light& l, const Mat& m,
     const Frame& fr, v3 V, Rng& rng, v3& dirOut)
 {
     v2 r    = random2D(rng);
@@ -230,7 +230,7 @@ __device__ __forceinline__ void accumulateSegment(WaveBuffers& wb, uint32_t p, i
     *dst        = make_float4(a.x + radiance.x, a.y + radiance.y, a.z + radiance.z, 0.f);
 }
 
-__global__ void __launch_bounds__(kShadeBlock) k_shade(DevScene s, agb_frame_data f,
+__global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene s, agb_frame_data f,
     WaveParams wp, WaveBuffers wb, int bounce, int cur, int depthLimit)
 {
     uint32_t n      = wb.counters[bounce * kCounterStride + CNT_RAYS];
@@ -702,6 +702,7 @@ void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp
             marks->record(category, st);
     };
     int grid = smCount * 8;
+    int shadeGrid = smCount * (kShadeMinBlocks > 8 ? kShadeMinBlocks : 8);
     int traceGrid = smCount * kTraceBlocksPerSM;
     mark(KC_CAMERA);
     k_camera<<<grid, 256, 0, st>>>(f, wp, wb);
@@ -714,7 +715,7 @@ void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp
         if (b == depth)
         {
             mark(KC_SHADE);
-            k_shade<<<grid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 1);
+            k_shade<<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 1);
             launches++;
             break;
         }
@@ -724,7 +725,7 @@ void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp
         else
             k_trace_closest<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, cur);
         mark(KC_SHADE);
-        k_shade<<<grid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 0);
+        k_shade<<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 0);
         mark(KC_SHADOW);
         if (wp.countTraversal)
             k_trace_shadow<true><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b);

@@ -144,7 +144,7 @@ AGB_D v3 mulDir(const float* m, v3 d)
         m[8] * d.x + m[9] * d.y + m[10] * d.z + m[11] * 0.f };
 }
 // Environment.slang:98-133.  pixel / screen are used only with background_use_screen.
-AGB_D v3 evaluateEnvironment(const DevScene& s, v3 dir, bool asBackground, v2 pixel, v2 screen)
+AGB_DN v3 evaluateEnvironment(const DevScene& s, v3 dir, bool asBackground, v2 pixel, v2 screen)
 {
     const agb_environment_data& c = s.env;
     if (asBackground)
@@ -167,7 +167,7 @@ AGB_D v3 evaluateEnvironment(const DevScene& s, v3 dir, bool asBackground, v2 pi
     return lerp3(ld3(c.light_top), ld3(c.light_bottom), uv.y);
 }
 // Environment.slang:137-186
-AGB_D v3 sampleEnvironment(const DevScene& s, v2 r, v3& L, float& pdf)
+AGB_DN v3 sampleEnvironment(const DevScene& s, v2 r, v3& L, float& pdf)
 {
     const agb_environment_data& c = s.env;
     if (c.has_light_tex && s.envLight.data)
