@@ -108,7 +108,8 @@ class Instance(ctypes.Structure):
 class RenderOptions(ctypes.Structure):
     _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
                 ("accumulation", ctypes.c_uint32), ("max_paths_in_flight", ctypes.c_uint32),
-                ("env_filter_linear", ctypes.c_int32), ("_pad", ctypes.c_int32 * 3)]
+                ("env_filter_linear", ctypes.c_int32), ("seed_offset", ctypes.c_uint32),
+                ("_pad", ctypes.c_int32 * 2)]
 
 
 class RenderStats(ctypes.Structure):
@@ -121,6 +122,19 @@ class RenderStats(ctypes.Structure):
 
 KERNEL_FAMILIES = ("camera", "trace_closest", "shade", "trace_shadow", "resolve", "finalize")
 
+
+class AovBuffers(ctypes.Structure):
+    _fields_ = [("depth_view", ctypes.c_void_p), ("normal_roughness", ctypes.c_void_p),
+                ("base_color_metalness", ctypes.c_void_p), ("motion", ctypes.c_void_p)]
+
+
+class TemporalSettings(ctypes.Structure):
+    """agb_temporal_settings; defaults of PTRenderer.cpp:2043-2046."""
+    _fields_ = [("is_reset", ctypes.c_uint32), ("blend_alpha_min", ctypes.c_float),
+                ("blend_alpha_max", ctypes.c_float), ("speed_reference", ctypes.c_float)]
+
+
+POST_SOURCE_TEMPORAL = 4
 
 # Every symbol include/agb.h declares, with its ctypes signature.
 _P = ctypes.c_void_p
@@ -153,6 +167,13 @@ SIGNATURES = {
     "agb_accum_device": (_I32, [_P, _I32, ctypes.POINTER(_P)]),
     "agb_last_sample_device": (_I32, [_P, ctypes.POINTER(_P)]),
     "agb_post_process": (_I32, [_P, _I32, _P, _I32, _I32, _P, _P]),
+    "agb_aov_read": (_I32, [_P, _P, _P, _P, _P]),
+    "agb_aov_device": (_I32, [_P, ctypes.POINTER(AovBuffers)]),
+    "agb_temporal_resolve": (_I32, [_P, ctypes.POINTER(TemporalSettings)]),
+    "agb_temporal_read": (_I32, [_P, _P, _U64]),
+    "agb_temporal_resolve_batch": (_I32, [_P, _P, _P, _P, _U32, _U32,
+                                          ctypes.POINTER(TemporalSettings), _P, _P]),
+    "agb_temporal_jitter": (None, [_U32, _U32, ctypes.POINTER(ctypes.c_float)]),
     "agb_bsdf_batch": (_I32, [_I32, _P, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _P]),
     "agb_intersect_batch": (_I32, [_P, _P, _I64, _I32, _P, _P]),
     "agb_env_sample_batch": (_I32, [_P, _P, _I64, _P, _P, _P]),

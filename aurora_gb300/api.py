@@ -88,8 +88,10 @@ class Renderer:
 
     # --------------------------------------------------------------------------- rendering
     def render(self, sample_start, sample_count, width=None, height=None,
-               accumulation=_abi.ACCUM_RUNNING_MEAN | _abi.ACCUM_KAHAN, max_paths=0, stats=False):
+               accumulation=_abi.ACCUM_RUNNING_MEAN | _abi.ACCUM_KAHAN, max_paths=0, stats=False,
+               seed_offset=0):
         opt = _abi.RenderOptions()
+        opt.seed_offset = seed_offset
         opt.width = width or self.scene.width
         opt.height = height or self.scene.height
         opt.accumulation = accumulation
@@ -136,6 +138,31 @@ class Renderer:
                                          1 if gamma else 0, ptr(o32), ptr(o8)))
         return o32, o8
 
+    def aovs(self, width=None, height=None):
+        """Denoising AOVs of the last render (frame with is_denoising_aovs_enabled): dict of
+        depth_view (H, W), normal_roughness, base_color_metalness, motion (H, W, 4)."""
+        w = width or self.scene.width
+        h = height or self.scene.height
+        out = dict(depth_view=np.empty((h, w), np.float32),
+                   normal_roughness=np.empty((h, w, 4), np.float32),
+                   base_color_metalness=np.empty((h, w, 4), np.float32),
+                   motion=np.empty((h, w, 4), np.float32))
+        check(self._lib.agb_aov_read(self.ctx, ptr(out["depth_view"]), ptr(out["normal_roughness"]),
+                                     ptr(out["base_color_metalness"]), ptr(out["motion"])))
+        return out
+
+    def temporal_resolve(self, reset=False, alpha_min=1.0 / 16.0, alpha_max=0.6, speed_reference=6.0):
+        """Temporal resolve of the last render against the previous resolve."""
+        st = _abi.TemporalSettings(1 if reset else 0, alpha_min, alpha_max, speed_reference)
+        check(self._lib.agb_temporal_resolve(self.ctx, ctypes.byref(st)))
+
+    def temporal_read(self, width=None, height=None):
+        w = width or self.scene.width
+        h = height or self.scene.height
+        out = np.empty((h, w, 4), np.float32)
+        check(self._lib.agb_temporal_read(self.ctx, ptr(out), out.size))
+        return out
+
     def memory_bytes(self):
         b = ctypes.c_uint64()
         check(self._lib.agb_context_memory(self.ctx, ctypes.byref(b)))
@@ -178,6 +205,13 @@ def bsdf_batch(op, mats_ptr, idx_ptr, frames_ptr, v_ptr, l_ptr, rnd_ptr, n, out_
     check(library().agb_bsdf_batch(op, vp(mats_ptr), vp(idx_ptr), vp(frames_ptr), vp(v_ptr),
                                    vp(l_ptr), vp(rnd_ptr), n, vp(out_value), vp(out_dir),
                                    vp(out_pdf), vp(out_lobe), stream))
+
+
+def temporal_jitter(frame_index, phase_count=0):
+    """Halton (2, 3) camera jitter in pixels for a frame (PTRenderer.cpp:159-174)."""
+    out = (ctypes.c_float * 2)()
+    _abi.library().agb_temporal_jitter(frame_index, phase_count, out)
+    return float(out[0]), float(out[1])
 
 
 def random_stream(sample_index, width, px, py, n, out_ptr):

@@ -139,6 +139,13 @@ struct agb_context
     // Accumulation.
     uint32_t accW = 0, accH = 0;
     DevBuf accMean, accSum, accComp, lastSample;
+    // Denoising AOVs of the last render that enabled them (accW x accH).
+    DevBuf aovDepth, aovNormal, aovAlbedo, aovMotion;
+    bool aovValid = false;
+    // Temporal-resolve histories (ping-pong) and the index of the one written last.
+    DevBuf taaHistory[2];
+    uint32_t taaW = 0, taaH = 0;
+    int taaLast     = -1;
     uint32_t accumulatedSamples = 0;
     uint32_t lastAccumMode      = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -832,6 +839,21 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
     else if (ctx->accumulatedSamples != sample_start || (ctx->lastAccumMode & accumMode) != accumMode)
         return fail(AGB_ERR_INVALID_ARG, "agb_render: sample_start must continue the accumulated "
                                          "sequence in the same accumulation mode");
+    // Denoising AOVs: written by the primary paths of the call's last sample.
+    uint32_t aovSample = ~0u;
+    if (ctx->frame.is_denoising_aovs_enabled)
+    {
+        AGB_CUDA(ctx->aovDepth.ensure(size_t(pixels) * sizeof(float)), "allocate AOVs");
+        AGB_CUDA(ctx->aovNormal.ensure(size_t(pixels) * sizeof(float4)), "allocate AOVs");
+        AGB_CUDA(ctx->aovAlbedo.ensure(size_t(pixels) * sizeof(float4)), "allocate AOVs");
+        AGB_CUDA(ctx->aovMotion.ensure(size_t(pixels) * sizeof(float4)), "allocate AOVs");
+        ctx->wb.aovDepth  = ctx->aovDepth.as<float>();
+        ctx->wb.aovNormal = ctx->aovNormal.as<float4>();
+        ctx->wb.aovAlbedo = ctx->aovAlbedo.as<float4>();
+        ctx->wb.aovMotion = ctx->aovMotion.as<float4>();
+        aovSample         = sample_start + sample_count - 1;
+    }
+    ctx->aovValid = ctx->frame.is_denoising_aovs_enabled != 0;
     size_t counterWords = size_t(depth + 2) * kCounterStride;
     AGB_CUDA(cudaMemsetAsync(ctx->counters.ptr, 0, counterWords * waves * sizeof(uint32_t), ctx->stream),
         "clear counters");
@@ -857,6 +879,8 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
         wp.paths          = wp.samples * pixels;
         wp.accumMode      = accumMode;
         wp.countTraversal = ctx->counting ? 1 : 0;
+        wp.aovSample      = aovSample;
+        wp.seedOffset     = opt->seed_offset;
         wb.counters       = ctx->counters.as<uint32_t>() + counterWords * w;
         launchWave(scene, ctx->frame, wp, wb, ctx->stream, ctx->smCount, launches, marks);
         AGB_CUDA(cudaGetLastError(), "launch wave");
@@ -979,7 +1003,13 @@ AGB_API agb_status agb_post_process(agb_context* ctx, int32_t mode, const float 
     DevBuf o32, o8;
     AGB_CUDA(o32.ensure(pixels * sizeof(float4)), "allocate post output");
     AGB_CUDA(o8.ensure(pixels * sizeof(uchar4)), "allocate post output");
-    const float4* src = mode == AGB_ACCUM_KAHAN ? ctx->accSum.as<float4>() : ctx->accMean.as<float4>();
+    if (mode == AGB_POST_SOURCE_TEMPORAL && (ctx->taaLast < 0 || ctx->taaW != ctx->accW || ctx->taaH != ctx->accH))
+        return fail(AGB_ERR_NOT_READY, "agb_post_process: no temporal resolve of this size");
+    const float4* src = mode == AGB_ACCUM_KAHAN ? ctx->accSum.as<float4>()
+        : mode == AGB_POST_SOURCE_TEMPORAL      ? ctx->taaHistory[ctx->taaLast].as<float4>()
+                                                : ctx->accMean.as<float4>();
+    if (mode == AGB_POST_SOURCE_TEMPORAL)
+        mode = AGB_ACCUM_RUNNING_MEAN;
     float inv = ctx->accumulatedSamples ? 1.f / float(ctx->accumulatedSamples) : 1.f;
     AGB_CUDA(launchPostProcess(src, nullptr, mode, inv, uint32_t(pixels),
                  make_float3(brightness[0], brightness[1], brightness[2]), tone_map, gamma,
@@ -993,6 +1023,137 @@ AGB_API agb_status agb_post_process(agb_context* ctx, int32_t mode, const float 
             "read post output");
     AGB_CUDA(cudaStreamSynchronize(ctx->stream), "post-process");
     return AGB_OK;
+}
+
+AGB_API agb_status agb_aov_read(agb_context* ctx, float* depth_view, float* normal_roughness,
+    float* base_color_metalness, float* motion)
+{
+    if (!ctx || !ctx->aovValid || !ctx->aovDepth.ptr)
+        return fail(AGB_ERR_NOT_READY, "agb_aov_read: the last render did not enable the AOVs");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    size_t n = size_t(ctx->accW) * ctx->accH;
+    if (depth_view)
+        AGB_CUDA(cudaMemcpyAsync(depth_view, ctx->aovDepth.ptr, n * sizeof(float), cudaMemcpyDeviceToHost,
+                     ctx->stream), "read AOVs");
+    if (normal_roughness)
+        AGB_CUDA(cudaMemcpyAsync(normal_roughness, ctx->aovNormal.ptr, n * sizeof(float4),
+                     cudaMemcpyDeviceToHost, ctx->stream), "read AOVs");
+    if (base_color_metalness)
+        AGB_CUDA(cudaMemcpyAsync(base_color_metalness, ctx->aovAlbedo.ptr, n * sizeof(float4),
+                     cudaMemcpyDeviceToHost, ctx->stream), "read AOVs");
+    if (motion)
+        AGB_CUDA(cudaMemcpyAsync(motion, ctx->aovMotion.ptr, n * sizeof(float4), cudaMemcpyDeviceToHost,
+                     ctx->stream), "read AOVs");
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "read AOVs");
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_aov_device(agb_context* ctx, agb_aov_buffers* out)
+{
+    if (!ctx || !out)
+        return fail(AGB_ERR_INVALID_ARG, "agb_aov_device: null argument");
+    if (!ctx->aovValid || !ctx->aovDepth.ptr)
+        return fail(AGB_ERR_NOT_READY, "agb_aov_device: the last render did not enable the AOVs");
+    out->depth_view           = ctx->aovDepth.as<float>();
+    out->normal_roughness     = ctx->aovNormal.as<float>();
+    out->base_color_metalness = ctx->aovAlbedo.as<float>();
+    out->motion               = ctx->aovMotion.as<float>();
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_temporal_resolve(agb_context* ctx, const agb_temporal_settings* settings)
+{
+    if (!ctx || !settings)
+        return fail(AGB_ERR_INVALID_ARG, "agb_temporal_resolve: null argument");
+    if (!ctx->accMean.ptr || !ctx->aovValid)
+        return fail(AGB_ERR_NOT_READY, "agb_temporal_resolve: needs a render with the denoising AOVs "
+                                       "enabled (motion vectors and view depth)");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    size_t n     = size_t(ctx->accW) * ctx->accH;
+    bool resized = ctx->taaW != ctx->accW || ctx->taaH != ctx->accH || ctx->taaLast < 0;
+    if (resized)
+    {
+        for (int k = 0; k < 2; k++)
+        {
+            AGB_CUDA(ctx->taaHistory[k].ensure(n * sizeof(float4)), "allocate temporal history");
+            AGB_CUDA(cudaMemsetAsync(ctx->taaHistory[k].ptr, 0, n * sizeof(float4), ctx->stream),
+                "clear temporal history");
+        }
+        ctx->taaW    = ctx->accW;
+        ctx->taaH    = ctx->accH;
+        ctx->taaLast = 1;
+    }
+    TemporalSettings ts{ settings->is_reset || resized ? 1u : 0u, settings->blend_alpha_min,
+        settings->blend_alpha_max, settings->speed_reference };
+    int write = ctx->taaLast ^ 1;
+    AGB_CUDA(launchTemporalResolve(ctx->accMean.as<float4>(), ctx->taaHistory[ctx->taaLast].as<float4>(),
+                 ctx->aovMotion.as<float4>(), ctx->aovDepth.as<float>(), int(ctx->accW), int(ctx->accH), ts,
+                 ctx->taaHistory[write].as<float4>(), ctx->stream),
+        "temporal resolve");
+    ctx->taaLast = write;
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_temporal_read(agb_context* ctx, float* host_rgba, uint64_t capacity)
+{
+    if (!ctx || !host_rgba)
+        return fail(AGB_ERR_INVALID_ARG, "agb_temporal_read: null argument");
+    if (ctx->taaLast < 0)
+        return fail(AGB_ERR_NOT_READY, "agb_temporal_read: no temporal resolve yet");
+    size_t n = size_t(ctx->taaW) * ctx->taaH * 4;
+    if (capacity < n)
+        return fail(AGB_ERR_INVALID_ARG, "agb_temporal_read: output too small");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    AGB_CUDA(cudaMemcpyAsync(host_rgba, ctx->taaHistory[ctx->taaLast].ptr, n * sizeof(float),
+                 cudaMemcpyDeviceToHost, ctx->stream),
+        "read temporal history");
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "read temporal history");
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_temporal_resolve_batch(const float* accum, const float* history,
+    const float* motion, const float* depth_view, uint32_t width, uint32_t height,
+    const agb_temporal_settings* settings, float* out, void* cuda_stream)
+{
+    if (!settings || (uint64_t(width) * height > 0 && (!accum || !history || !motion || !depth_view || !out)))
+        return fail(AGB_ERR_INVALID_ARG, "agb_temporal_resolve_batch: null argument");
+    if (width > (1u << 15) || height > (1u << 15))
+        return fail(AGB_ERR_LIMIT, "agb_temporal_resolve_batch: image larger than 32768 pixels a side");
+    if (width == 0 || height == 0)
+        return AGB_OK;
+    TemporalSettings ts{ settings->is_reset, settings->blend_alpha_min, settings->blend_alpha_max,
+        settings->speed_reference };
+    AGB_CUDA(launchTemporalResolve(reinterpret_cast<const float4*>(accum),
+                 reinterpret_cast<const float4*>(history), reinterpret_cast<const float4*>(motion),
+                 depth_view, int(width), int(height), ts, reinterpret_cast<float4*>(out),
+                 static_cast<cudaStream_t>(cuda_stream)),
+        "agb_temporal_resolve_batch");
+    return AGB_OK;
+}
+
+AGB_API void agb_temporal_jitter(uint32_t frame_index, uint32_t phase_count, float out[2])
+{
+    // PTRenderer.cpp:81-95 (halton) and :168-174: index = frame (mod phases) + 1, centred.
+    uint32_t index = (phase_count > 0u ? frame_index % phase_count : frame_index) + 1u;
+    for (int a = 0; a < 2; a++)
+    {
+        uint32_t base = a == 0 ? 2u : 3u, i = index;
+        float result = 0.0f;
+        float scale  = 1.0f / static_cast<float>(base);
+        while (i > 0)
+        {
+            result += scale * static_cast<float>(i % base);
+            i /= base;
+            scale /= static_cast<float>(base);
+        }
+        out[a] = result - 0.5f;
+    }
 }
 
 AGB_API agb_status agb_bsdf_batch(int32_t op, const agb_material* materials,

@@ -129,6 +129,15 @@ void buildBVH2(const float* boxes, uint32_t count, int maxLeaf, int maxDepth, Bu
 // Double-precision inverse of a 3x4 affine transform rounded to float.
 void invertAffine(const float* m, float* out);
 
+// agb_temporal.cu
+struct TemporalSettings
+{
+    uint32_t isReset;
+    float blendAlphaMin, blendAlphaMax, speedReference;
+};
+cudaError_t launchTemporalResolve(const float4* accum, const float4* history, const float4* motion,
+    const float* depthView, int W, int H, const TemporalSettings& s, float4* out, cudaStream_t st);
+
 // agb_unit.cu
 cudaError_t launchBsdfBatch(int op, const agb_material* mats, const int32_t* matIndex,
     const float* frames, const float* V, const float* L, const float* rnd, int64_t n,

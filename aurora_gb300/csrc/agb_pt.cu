@@ -16,6 +16,7 @@
 // Shading arithmetic is compiled without multiply-add contraction (see the build flags) so that
 // FP32 results follow the reference's operation order.
 #include "agb_kernels.h"
+#include "agb_temporal.cuh"
 
 namespace agb
 {
@@ -72,7 +73,7 @@ __global__ void k_camera(agb_frame_data f, WaveParams wp, WaveBuffers wb)
         uint32_t pixel = p % wp.pixels;
         uint32_t k     = p / wp.pixels;
         uint32_t px = pixel % wp.width, py = pixel / wp.width;
-        Rng rng     = rngInit(wp.sampleBase + k, wp.width, px, py);
+        Rng rng     = rngInit(wp.sampleBase + k + wp.seedOffset, wp.width, px, py);
         v3 o, d;
         cameraRay(f, px, py, wp.width, wp.height, rng, o, d);
         wb.rayOrg[0][p]  = make_float4(o.x, o.y, o.z, 0.f);
@@ -82,6 +83,8 @@ __global__ void k_camera(agb_frame_data f, WaveParams wp, WaveBuffers wb)
         wb.contrib[p]    = make_float4(1.f, 1.f, 1.f, 0.f);
         wb.flags[p] = PF_PRIMARY | (uint32_t(CAMERA_RAY) << PF_RAYTYPE_SHIFT) |
             (uint32_t(NO_SECONDARY_RAY) << PF_MISLOBE_SHIFT);
+        if (wp.sampleBase + k == wp.aovSample)
+            wb.aovMotion[pixel] = make_float4(0.f, 0.f, 0.f, 0.f); // MainEntryPoints.slang:115-118
         float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
         wb.outDirect[p]    = z;
         wb.outDiffuse[p]   = z;
@@ -274,8 +277,19 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
             {
                 float4 h  = wb.hitTUV[i];
                 int32_t inst = wb.hitInst[i];
+                bool aov = primary && wp.sampleBase + p / wp.pixels == wp.aovSample;
                 if (inst < 0)
                 {
+                    if (aov)
+                    {
+                        // Miss AOVs (MainEntryPoints.slang:380-406); the guide normal faces back
+                        // along the ray.
+                        wb.aovDepth[pixel]  = f.sky_view_z;
+                        wb.aovNormal[pixel] = make_float4(-dir.x, -dir.y, -dir.z, 1.f);
+                        wb.aovAlbedo[pixel] = make_float4(0.f, 0.f, 0.f, 0.1f);
+                        wb.aovMotion[pixel] = skyMotion(f.camera_view_proj, f.camera_view_proj_prev,
+                            dir, screen.x, screen.y);
+                    }
                     v3 direct = bg ? evaluateEnvironment(s, dir, true, pixel2, screen) * contrib
                                    : splat(0.f);
                     accumulateSegment(wb, p, bounce, flags, rayType, direct, splat(0.f), clampLum);
@@ -326,6 +340,22 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
                                 saturatef(float(bounce) / 3.f));
                             m.specularRoughness = m.specularRoughness > fl ? m.specularRoughness : fl;
                             m.coatRoughness     = m.coatRoughness > fl ? m.coatRoughness : fl;
+                        }
+                        if (aov)
+                        {
+                            // Hit AOVs for every layer evaluated (HitShaderEntryPoints.slang:149-233).
+                            float4 o4 = wb.rayOrg[cur][i];
+                            v3 hw     = v3{ o4.x, o4.y, o4.z } + dir * h.x;
+                            float vz  = viewDepth(f.camera_inv_view, hw);
+                            v3 gn     = normalize(matNormal);
+                            wb.aovDepth[pixel]  = vz;
+                            wb.aovNormal[pixel] = make_float4(gn.x, gn.y, gn.z,
+                                m.specularRoughness > 0.05f ? m.specularRoughness : 0.05f);
+                            wb.aovAlbedo[pixel] = make_float4(m.baseColor.x, m.baseColor.y,
+                                m.baseColor.z, m.metalness);
+                            wb.aovMotion[pixel] = surfaceMotion(f.camera_view_proj,
+                                f.camera_view_proj_prev, f.camera_inv_view_prev, hw, vz, screen.x,
+                                screen.y);
                         }
                         v3 transparency = splat(1.f) - m.opacity;
                         P        = luminance(transparency);

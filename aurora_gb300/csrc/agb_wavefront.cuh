@@ -84,6 +84,11 @@ struct WaveBuffers
     float4* accumComp;
     float4* lastSample;
     unsigned long long* stats; // [closest rays, shadow rays, nodes, tris, overflow]
+    // Denoising AOVs (per pixel), written for one sample index (WaveParams::aovSample).
+    float* aovDepth;     // view-space depth
+    float4* aovNormal;   // guide normal xyz, roughness
+    float4* aovAlbedo;   // base colour xyz, metalness
+    float4* aovMotion;   // previous - current pixel xy, view depth change, 0
 };
 
 struct WaveParams
@@ -93,6 +98,8 @@ struct WaveParams
     uint32_t paths;               // pixels * samples
     uint32_t accumMode;           // AGB_ACCUM_* bits
     int32_t countTraversal;
+    uint32_t aovSample;           // sample index whose primary paths write the AOVs; ~0u = none
+    uint32_t seedOffset;          // added to the sample index that seeds the random streams
 };
 
 } // namespace agb

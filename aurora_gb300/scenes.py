@@ -189,22 +189,55 @@ def perspective(fovy_deg, aspect, near=0.1, far=1000.0):
     return m
 
 
+def denoising_range(view, scene_bounds):
+    """RendererBase::denoisingRange (RendererBase.cpp:206-224): farthest view-space depth of the
+    scene box, +10 %, clamped to [1, 5e8]; FP32 like glm."""
+    if scene_bounds is None:
+        return np.float32(1.0)
+    lo, hi = np.asarray(scene_bounds[0], np.float32), np.asarray(scene_bounds[1], np.float32)
+    v = np.asarray(view, np.float32)
+    zs = []
+    for c in range(8):
+        p = np.array([hi[0] if c & 1 else lo[0], hi[1] if c & 2 else lo[1],
+                      hi[2] if c & 4 else lo[2], 1.0], np.float32)
+        zs.append(np.float32(v[2] @ p))
+    depth = -np.float32(min(zs))
+    return np.float32(min(max(depth * np.float32(1.1), np.float32(1.0)), np.float32(5.0e8)))
+
+
 def frame_data(view, proj, trace_depth=5, max_luminance=1000.0, russian_roulette=True,
                rr_start_depth=3, lights=(), force_opaque_shadows=True, focal_distance=1.0,
-               lens_radius=0.0, display_errors=False, scene_bounds=None):
+               lens_radius=0.0, display_errors=False, scene_bounds=None, aovs=False, jitter=None,
+               prev=None):
     """Packs camera and options like RendererBase::updateFrameDataGPUStruct
     (RendererBase.cpp:225-295).  view / proj are math-convention 4x4 arrays (column vectors);
     lights: (direction, color, intensity, angular_diameter) tuples packed as HGIScene.cpp:118-132
-    (direction negated, cos of half the angular diameter)."""
+    (direction negated, cos of half the angular diameter).  aovs: denoising AOVs on; jitter:
+    temporal camera jitter in pixels (PTRenderer.cpp:1149-1194); prev: (view, proj, jitter) of the
+    previous frame for motion vectors (default: this frame)."""
     f = np.zeros((), dtype=_abi.FRAME_DTYPE)
     view = np.asarray(view, np.float64)
     proj = np.asarray(proj, np.float64)
     inv = np.linalg.inv(view)
     # Bytes of glm transpose(inverse(view)) = camera-to-world stored row-major.
     f["camera_view_proj"] = (proj @ view).T.reshape(-1)
-    f["camera_view_proj_prev"] = f["camera_view_proj"]
     f["camera_inv_view"] = inv.reshape(-1)
-    f["camera_inv_view_prev"] = f["camera_inv_view"]
+    if prev is None:
+        f["camera_view_proj_prev"] = f["camera_view_proj"]
+        f["camera_inv_view_prev"] = f["camera_inv_view"]
+    else:
+        pv, pp = np.asarray(prev[0], np.float64), np.asarray(prev[1], np.float64)
+        f["camera_view_proj_prev"] = (pp @ pv).T.reshape(-1)
+        f["camera_inv_view_prev"] = np.linalg.inv(pv).reshape(-1)
+        if len(prev) > 2 and prev[2] is not None:
+            f["camera_jitter_prev"] = prev[2]
+    if jitter is not None:
+        f["camera_jitter"] = jitter
+        f["is_temporal_jitter_enabled"] = 1
+        if prev is None:
+            f["camera_jitter_prev"] = jitter
+    f["is_denoising_aovs_enabled"] = 1 if aovs else 0
+    f["sky_view_z"] = -denoising_range(view, scene_bounds) * np.float32(2.0)
     f["view_size"] = (2.0 / proj[0, 0], 2.0 / proj[1, 1])
     f["is_ortho_projection"] = 1 if proj[3, 3] == 1.0 else 0
     f["focal_distance"] = focal_distance

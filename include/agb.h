@@ -263,7 +263,10 @@ typedef struct agb_render_options
     uint32_t accumulation;      /* AGB_ACCUM_* bitmask */
     uint32_t max_paths_in_flight; /* wave size in paths; 0 = default */
     int32_t env_filter_linear;  /* environment sampler: 0 nearest (Hgi default), 1 bilinear */
-    int32_t _pad[3];
+    uint32_t seed_offset;       /* added to the sample index that seeds the random streams, not to
+                                   the accumulation index (gSampleData.seedOffset,
+                                   MainEntryPoints.slang:83; PTRenderer.cpp:1008-1022) */
+    int32_t _pad[2];
 } agb_render_options;
 
 typedef struct agb_context agb_context;
@@ -402,6 +405,58 @@ AGB_API agb_status agb_accum_read(agb_context* ctx, int32_t mode, float* host_rg
 AGB_API agb_status agb_accum_device(agb_context* ctx, int32_t mode, float** device_rgba);
 /* Per-sample output of the last rendered sample (RGBA32F device buffer), like gResult. */
 AGB_API agb_status agb_last_sample_device(agb_context* ctx, float** device_rgba);
+
+/* Denoising AOVs (HitShaderEntryPoints.slang:149-233 for hits, MainEntryPoints.slang:115-118 and
+ * :380-406 for ray generation and misses), produced by agb_render when the frame has
+ * is_denoising_aovs_enabled, for the primary paths of the call's last sample (the reference keeps
+ * the data of the last sample).  width*height each, rows from the top:
+ *   depth_view            view-space depth (negative in front of the camera; sky_view_z on a miss)
+ *   normal_roughness      guide normal xyz (unencoded), max(specular roughness, 0.05); on a miss
+ *                         the reversed ray direction and 1
+ *   base_color_metalness  base colour xyz, metalness; on a miss (0, 0, 0, 0.1)
+ *   motion                previous-minus-current pixel position xy, view depth change, 0
+ * agb_aov_read copies any of them to host memory (null = skip); agb_aov_device returns the device
+ * arrays (valid until the next agb_render). */
+typedef struct agb_aov_buffers
+{
+    const float* depth_view;
+    const float* normal_roughness;
+    const float* base_color_metalness;
+    const float* motion;
+} agb_aov_buffers;
+AGB_API agb_status agb_aov_read(agb_context* ctx, float* depth_view, float* normal_roughness,
+    float* base_color_metalness, float* motion);
+AGB_API agb_status agb_aov_device(agb_context* ctx, agb_aov_buffers* out);
+
+/* Temporal resolve (DirectX/Shaders/TemporalResolve.hlsl:97-249; settings as
+ * PTRenderer.cpp:2035-2046, defaults alpha 1/16 .. 0.6 reaching the maximum at 6 pixels per
+ * frame).  Resolves the running-mean accumulation of the last render (one jittered sample per
+ * frame, camera jitter from agb_temporal_jitter) against the previous resolve, using that render's
+ * AOVs (motion vectors, view depth); the history is reset on request, on the first call and when
+ * the image size changes.  agb_temporal_read copies the resolved RGBA image; agb_post_process with
+ * AGB_POST_SOURCE_TEMPORAL post-processes it. */
+typedef struct agb_temporal_settings
+{
+    uint32_t is_reset;
+    float blend_alpha_min;
+    float blend_alpha_max;
+    float speed_reference;
+} agb_temporal_settings;
+AGB_API agb_status agb_temporal_resolve(agb_context* ctx, const agb_temporal_settings* settings);
+AGB_API agb_status agb_temporal_read(agb_context* ctx, float* host_rgba, uint64_t capacity);
+/* The temporal resolve kernel over device arrays (parity tests): accum / history / out RGBA32F,
+ * motion 4 floats and depth_view 1 float per pixel, width*height each; stream may be null. */
+AGB_API agb_status agb_temporal_resolve_batch(const float* accum, const float* history,
+    const float* motion, const float* depth_view, uint32_t width, uint32_t height,
+    const agb_temporal_settings* settings, float* out, void* cuda_stream);
+/* Halton (2, 3) camera jitter in pixels, centred on [-0.5, 0.5] (PTRenderer.cpp:81-95,159-174):
+ * index = (phase_count ? frame_index % phase_count : frame_index) + 1. */
+AGB_API void agb_temporal_jitter(uint32_t frame_index, uint32_t phase_count, float out[2]);
+/* agb_post_process source: the last temporal resolve instead of the accumulation. */
+enum
+{
+    AGB_POST_SOURCE_TEMPORAL = 4
+};
 
 /* Post-processing (HGI/Shaders/PostProcessing.glsl:37-64): brightness, optional ACES, optional
  * sRGB approximation, alpha 1.  Writes RGBA32F (out_rgba32f) and/or RGBA8 (out_rgba8) host

@@ -322,6 +322,61 @@ ORC_API void* orc_tracer_create(int precision, const Scene* s, const FrameData* 
 
 ORC_API void orc_tracer_destroy(void* t) { delete static_cast<OrcTracer*>(t); }
 
+ORC_API void orc_tracer_set_seed_offset(void* handle, uint32_t seedOffset)
+{
+    OrcTracer* t = static_cast<OrcTracer*>(handle);
+    t->f32.seedOffset = t->f64.seedOffset = seedOffset;
+}
+
+// Denoising AOV targets (width*height: depth 1 float, normal / albedo / motion 4 floats per
+// pixel) written by later renders for their last sample when the frame enables the AOVs; null
+// pointers turn them off.
+ORC_API void orc_tracer_set_aov(void* handle, float* depth, float* normal, float* albedo,
+    float* motion)
+{
+    OrcTracer* t = static_cast<OrcTracer*>(handle);
+    bool on      = depth && normal && albedo && motion;
+    t->f32.aovDepth = t->f64.aovDepth = on ? depth : nullptr;
+    t->f32.aovNormal = t->f64.aovNormal = on ? normal : nullptr;
+    t->f32.aovAlbedo = t->f64.aovAlbedo = on ? albedo : nullptr;
+    t->f32.aovMotion = t->f64.aovMotion = on ? motion : nullptr;
+}
+
+// TemporalResolve.hlsl over a whole image.  settings: isReset (as float bits of a uint), alpha
+// min, alpha max, speed reference.
+ORC_API void orc_temporal_resolve(int precision, const float* accum, const float* history,
+    const float* motion, const float* depthView, int w, int h, uint32_t isReset, float alphaMin,
+    float alphaMax, float speedReference, float* out)
+{
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++)
+        {
+            float* o = out + 4 * (size_t(y) * size_t(w) + size_t(x));
+            if (precision == 64)
+            {
+                Temporal<double>::Settings st{ isReset, alphaMin, alphaMax, speedReference };
+                double r[4];
+                Temporal<double>::resolvePixel(accum, history, motion, depthView, w, h, st, x, y, r);
+                for (int k = 0; k < 4; k++)
+                    o[k] = float(r[k]);
+            }
+            else
+            {
+                Temporal<float>::Settings st{ isReset, alphaMin, alphaMax, speedReference };
+                float r[4];
+                Temporal<float>::resolvePixel(accum, history, motion, depthView, w, h, st, x, y, r);
+                for (int k = 0; k < 4; k++)
+                    o[k] = r[k];
+            }
+        }
+}
+
+// PTRenderer.cpp:168-174
+ORC_API void orc_temporal_jitter(uint32_t frameIndex, uint32_t phaseCount, float* out)
+{
+    temporalJitter(frameIndex, phaseCount, out);
+}
+
 // Renders sampleCount samples starting at sampleStart.  Any of accumMean (running mean, FP32 as
 // the reference's accumulation pass), accumSum (FP64 sum of samples) and lastSample may be null.
 // rect (x0, y0, x1, y1) restricts the pixels, or is null.  stats[0..1] = camera-path segments and
@@ -332,6 +387,8 @@ ORC_API double orc_tracer_render(void* handle, const FrameData* f, uint32_t samp
 {
     OrcTracer* t = static_cast<OrcTracer*>(handle);
     auto t0      = std::chrono::steady_clock::now();
+    int64_t aovSample = sampleCount > 0 ? int64_t(sampleStart) + int64_t(sampleCount) - 1 : -1;
+    t->f64.aovSample = t->f32.aovSample = aovSample;
     if (t->precision == 64)
     {
         if (f)

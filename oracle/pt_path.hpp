@@ -18,6 +18,7 @@
 #include "pt_bsdf.hpp"
 #include "pt_bvh.hpp"
 #include "pt_env.hpp"
+#include "pt_temporal.hpp"
 
 namespace orc
 {
@@ -449,8 +450,63 @@ struct PathTracer
         T outputAlpha = T(0);
     };
 
-    // Closest-hit shader (HitShaderEntryPoints.slang:35-486).
-    void closestHit(Payload& p, const v3& rayDirection, const Hit& hit, v2 pixel) const
+    // Denoising AOVs of one sample per pixel (HitShaderEntryPoints.slang:149-233 for hits,
+    // MainEntryPoints.slang:380-406 for misses, MainEntryPoints.slang:115-118 at ray generation):
+    // view depth, guide normal + roughness, base colour + metalness and 2.5D motion, written while
+    // the path is primary for sampleIndex == aovSample when the frame enables them.  Null pointers
+    // or aovSample < 0 turn them off.
+    float* aovDepth   = nullptr;
+    float* aovNormal  = nullptr;
+    float* aovAlbedo  = nullptr;
+    float* aovMotion  = nullptr;
+    int64_t aovSample = -1;
+    // Added to the sample index that seeds the random streams (MainEntryPoints.slang:83).
+    uint32_t seedOffset = 0;
+
+    void writeHitAov(size_t i, const v3& rayOrigin, const v3& rayDirection, T t,
+        const Material<T>& m, const v3& materialNormal) const
+    {
+        const FrameData& f = *frame;
+        using TP           = Temporal<T>;
+        v3 hw              = rayOrigin + rayDirection * t;
+        T vz               = TP::viewZ(f.cameraInvView, hw);
+        aovDepth[i]        = float(vz);
+        v3 n               = normalize(materialNormal);
+        T rough = m.specularRoughness > T(0.05f) ? m.specularRoughness : T(0.05f);
+        float nr[4] = { float(n.x), float(n.y), float(n.z), float(rough) };
+        float al[4] = { float(m.baseColor.x), float(m.baseColor.y), float(m.baseColor.z),
+            float(m.metalness) };
+        T mv[4];
+        TP::motionVector(f.cameraViewProj, f.cameraViewProjPrev, f.cameraInvViewPrev, hw, vz,
+            T(float(screenW)), T(float(screenH)), mv);
+        for (int k = 0; k < 4; k++)
+        {
+            aovNormal[4 * i + k] = nr[k];
+            aovAlbedo[4 * i + k] = al[k];
+            aovMotion[4 * i + k] = float(mv[k]);
+        }
+    }
+    void writeSkyAov(size_t i, const v3& rayDirection) const
+    {
+        const FrameData& f = *frame;
+        aovDepth[i]        = f.skyViewZ;
+        float nr[4] = { float(-rayDirection.x), float(-rayDirection.y), float(-rayDirection.z), 1.f };
+        float al[4] = { 0.f, 0.f, 0.f, 0.1f };
+        T mv[4];
+        Temporal<T>::skyMotionVector(f.cameraViewProj, f.cameraViewProjPrev, rayDirection,
+            T(float(screenW)), T(float(screenH)), mv);
+        for (int k = 0; k < 4; k++)
+        {
+            aovNormal[4 * i + k] = nr[k];
+            aovAlbedo[4 * i + k] = al[k];
+            aovMotion[4 * i + k] = float(mv[k]);
+        }
+    }
+
+    // Closest-hit shader (HitShaderEntryPoints.slang:35-486).  aovPixel: pixel index whose AOVs
+    // this path writes, or -1.
+    void closestHit(Payload& p, const v3& rayOrigin, const v3& rayDirection, const Hit& hit,
+        v2 pixel, int64_t aovPixel) const
     {
         const FrameData& f = *frame;
         int maxTraceDepth  = f.traceDepth;
@@ -492,6 +548,8 @@ struct PathTracer
                 m.specularRoughness = m.specularRoughness > fl ? m.specularRoughness : fl;
                 m.coatRoughness     = m.coatRoughness > fl ? m.coatRoughness : fl;
             }
+            if (p.isPrimaryRay && aovPixel >= 0)
+                writeHitAov(size_t(aovPixel), rayOrigin, rayDirection, T(hit.t), m, materialNormal);
             v3 transparency = v3(1) - m.opacity;
             T P             = luminance(transparency);
             hitLayer        = random2D<T>(p.rng).x >= P;
@@ -636,13 +694,20 @@ struct PathTracer
         const FrameData& f = *frame;
         int maxTraceDepth  = f.traceDepth;
         Payload p;
-        p.rng = pcg2DInit(sampleIndex, screenW, px, py);
+        p.rng = pcg2DInit(sampleIndex + seedOffset, screenW, px, py);
         v3 rayOrigin, rayDirection;
         computeCameraRay(px, py, p.rng, rayOrigin, rayDirection);
         v3 outDirect(0), outDiffuse(0), outGlossy(0);
         T outAlpha = T(0);
         v2 pixel{T(float(px)), T(float(py))};
         v2 ss{T(float(screenW)), T(float(screenH))};
+        int64_t aovPixel = (f.isDenoisingAOVsEnabled && aovDepth && aovSample >= 0 &&
+                               int64_t(sampleIndex) == aovSample)
+            ? int64_t(py) * int64_t(screenW) + int64_t(px)
+            : int64_t(-1);
+        if (aovPixel >= 0)
+            for (int k = 0; k < 4; k++)
+                aovMotion[4 * size_t(aovPixel) + k] = 0.f;
         for (int rayDepth = 0; rayDepth <= maxTraceDepth && !p.pathEnded; rayDepth++)
         {
             if (rayDepth == maxTraceDepth)
@@ -662,7 +727,7 @@ struct PathTracer
                 Hit hit;
                 stats().raysTraced++;
                 if (caster.closest(rayOrigin, rayDirection, minT, T(INFINITY), hit))
-                    closestHit(p, rayDirection, hit, pixel);
+                    closestHit(p, rayOrigin, rayDirection, hit, pixel, aovPixel);
                 else
                 {
                     bool bg = p.isPrimaryRay || p.rayType == TRANSMISSION_LOBE ||
@@ -672,6 +737,8 @@ struct PathTracer
                         p.direct = E::evaluate(env, rayDirection, true, pixel, ss);
                         p.direct *= p.rayContribution;
                     }
+                    if (p.isPrimaryRay && aovPixel >= 0)
+                        writeSkyAov(size_t(aovPixel), rayDirection);
                     p.pathEnded = true;
                 }
                 rayOrigin    = p.nextRayOrigin;

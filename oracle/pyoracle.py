@@ -47,6 +47,12 @@ def lib():
                                         ctypes.c_int]
         L.orc_tracer_destroy.argtypes = [P]
         L.orc_fmath.argtypes = [ctypes.c_int, P, P, ctypes.c_int64, P]
+        L.orc_tracer_set_aov.argtypes = [P, P, P, P, P]
+        L.orc_tracer_set_seed_offset.argtypes = [P, ctypes.c_uint32]
+        L.orc_temporal_resolve.argtypes = [ctypes.c_int, P, P, P, P, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
+                                           ctypes.c_float, P]
+        L.orc_temporal_jitter.argtypes = [ctypes.c_uint32, ctypes.c_uint32, P]
         L.orc_tracer_render.restype = ctypes.c_double
         L.orc_tracer_render.argtypes = [P, P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, P, P,
                                         P, P, P]
@@ -203,7 +209,34 @@ class OracleScene:
             pass
 
     def render(self, sample_start, sample_count, precision=32, threads=None, brute=False,
-               want_mean=True, want_sum=False, want_last=False, rect=None, frame=None):
+               want_mean=True, want_sum=False, want_last=False, rect=None, frame=None,
+               want_aov=False, seed_offset=0):
+        """Renders with the oracle.  want_aov: also return the denoising AOVs of the last sample
+        (the frame must enable them); seed_offset: added to the sample index seeding the random
+        streams."""
+        s = self.desc
+        t = self.tracer(precision, brute)
+        lib().orc_tracer_set_seed_offset(t, seed_offset)
+        aov = None
+        if want_aov:
+            aov = dict(depth_view=np.zeros((s.height, s.width), np.float32),
+                       normal_roughness=np.zeros((s.height, s.width, 4), np.float32),
+                       base_color_metalness=np.zeros((s.height, s.width, 4), np.float32),
+                       motion=np.zeros((s.height, s.width, 4), np.float32))
+            lib().orc_tracer_set_aov(t, _p(aov["depth_view"]), _p(aov["normal_roughness"]),
+                                     _p(aov["base_color_metalness"]), _p(aov["motion"]))
+        try:
+            out = self._render(sample_start, sample_count, precision, threads, brute, want_mean,
+                               want_sum, want_last, rect, frame)
+        finally:
+            if want_aov:
+                lib().orc_tracer_set_aov(t, None, None, None, None)
+        if want_aov:
+            out["aov"] = aov
+        return out
+
+    def _render(self, sample_start, sample_count, precision, threads, brute, want_mean, want_sum,
+                want_last, rect, frame):
         s = self.desc
         n = s.width * s.height * 4
         mean = np.zeros(n, np.float32) if want_mean else None
@@ -290,6 +323,26 @@ def fmath(which, x, y=None):
     out = np.zeros_like(x)
     lib().orc_fmath(which, _p(x), _p(y), len(x), _p(out))
     return out
+
+
+def temporal_resolve(accum, history, motion, depth_view, reset=False, alpha_min=1.0 / 16.0,
+                     alpha_max=0.6, speed_reference=6.0, precision=32):
+    """TemporalResolve.hlsl over whole (H, W, 4) images; depth_view (H, W)."""
+    accum = np.ascontiguousarray(accum, np.float32)
+    history = np.ascontiguousarray(history, np.float32)
+    motion = np.ascontiguousarray(motion, np.float32)
+    depth_view = np.ascontiguousarray(depth_view, np.float32)
+    h, w = accum.shape[:2]
+    out = np.zeros((h, w, 4), np.float32)
+    lib().orc_temporal_resolve(precision, _p(accum), _p(history), _p(motion), _p(depth_view), w, h,
+                               1 if reset else 0, alpha_min, alpha_max, speed_reference, _p(out))
+    return out
+
+
+def temporal_jitter(frame_index, phase_count=0):
+    out = np.zeros(2, np.float32)
+    lib().orc_temporal_jitter(frame_index, phase_count, _p(out))
+    return float(out[0]), float(out[1])
 
 
 def rel_mse(x, ref, eps=1e-2):

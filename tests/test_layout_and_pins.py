@@ -189,3 +189,27 @@ def test_cabi_library_exports_every_declared_symbol():
     lib = ctypes.CDLL(_abi.LIB_PATH)
     for name in declared:
         assert hasattr(lib, name), name
+
+
+def test_temporal_jitter_pins(oracle):
+    """Halton (2, 3) jitter (PTRenderer.cpp:81-95,159-174) against an independent restatement in
+    Python float32, and the library's host function (no GPU work) against it."""
+    from aurora_gb300 import api, build
+    build.build()
+
+    def halton(index, base):
+        result, scale = np.float32(0.0), np.float32(1.0) / np.float32(base)
+        while index > 0:
+            result = np.float32(result + scale * np.float32(index % base))
+            index //= base
+            scale = np.float32(scale / np.float32(base))
+        return result
+
+    for frame in range(40):
+        for phases in (0, 8, 11):
+            i = (frame % phases if phases else frame) + 1
+            want = (float(np.float32(halton(i, 2) - np.float32(0.5))),
+                    float(np.float32(halton(i, 3) - np.float32(0.5))))
+            assert oracle.temporal_jitter(frame, phases) == want
+            assert api.temporal_jitter(frame, phases) == want
+    assert api.temporal_jitter(0) == (0.0, float(np.float32(1 / 3) - np.float32(0.5)))
