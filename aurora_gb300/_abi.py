@@ -174,6 +174,7 @@ SIGNATURES = {
     "agb_temporal_resolve_batch": (_I32, [_P, _P, _P, _P, _U32, _U32,
                                           ctypes.POINTER(TemporalSettings), _P, _P]),
     "agb_temporal_jitter": (None, [_U32, _U32, ctypes.POINTER(ctypes.c_float)]),
+    "agb_tc_gemm_bf16": (_I32, [_P, _P, _P, _I32, _I32, _I32, _P]),
     "agb_bsdf_batch": (_I32, [_I32, _P, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _P]),
     "agb_intersect_batch": (_I32, [_P, _P, _I64, _I32, _P, _P]),
     "agb_env_sample_batch": (_I32, [_P, _P, _I64, _P, _P, _P]),

@@ -1137,6 +1137,23 @@ AGB_API agb_status agb_temporal_resolve_batch(const float* accum, const float* h
     return AGB_OK;
 }
 
+AGB_API agb_status agb_tc_gemm_bf16(const uint16_t* a, const uint16_t* b, float* d, int32_t m,
+    int32_t n, int32_t k, void* cuda_stream)
+{
+    if (!a || !b || !d || m <= 0 || m % 128 || n < 16 || n > 256 || n % 16 || k <= 0 || k % 64)
+        return fail(AGB_ERR_INVALID_ARG, "agb_tc_gemm_bf16: M % 128, 16 <= N <= 256, N % 16, K % 64");
+    if ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(d)) & 15u)
+        return fail(AGB_ERR_INVALID_ARG, "agb_tc_gemm_bf16: pointers must be 16-byte aligned");
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    AGB_CUDA(launchTcGemm(a, b, d, m, n, k, st), "agb_tc_gemm_bf16");
+    AGB_CUDA(cudaStreamSynchronize(st), "agb_tc_gemm_bf16");
+    int flag = 0;
+    AGB_CUDA(takeTcError(&flag), "agb_tc_gemm_bf16");
+    if (flag)
+        return fail(AGB_ERR_TIMEOUT, "agb_tc_gemm_bf16: tensor-core completion wait timed out");
+    return AGB_OK;
+}
+
 AGB_API void agb_temporal_jitter(uint32_t frame_index, uint32_t phase_count, float out[2])
 {
     // PTRenderer.cpp:81-95 (halton) and :168-174: index = frame (mod phases) + 1, centred.

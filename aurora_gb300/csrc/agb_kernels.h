@@ -138,6 +138,11 @@ struct TemporalSettings
 cudaError_t launchTemporalResolve(const float4* accum, const float4* history, const float4* motion,
     const float* depthView, int W, int H, const TemporalSettings& s, float4* out, cudaStream_t st);
 
+// agb_denoise.cu
+cudaError_t launchTcGemm(const uint16_t* A, const uint16_t* B, float* D, int M, int N, int K, cudaStream_t st);
+// Reads and clears the tensor-core kernels' timeout flag (1 = a bounded wait ran out).
+cudaError_t takeTcError(int* flag);
+
 // agb_unit.cu
 cudaError_t launchBsdfBatch(int op, const agb_material* mats, const int32_t* matIndex,
     const float* frames, const float* V, const float* L, const float* rnd, int64_t n,

@@ -449,6 +449,12 @@ AGB_API agb_status agb_temporal_read(agb_context* ctx, float* host_rgba, uint64_
 AGB_API agb_status agb_temporal_resolve_batch(const float* accum, const float* history,
     const float* motion, const float* depth_view, uint32_t width, uint32_t height,
     const agb_temporal_settings* settings, float* out, void* cuda_stream);
+/* Tensor-core GEMM (tcgen05, BF16 operands, FP32 accumulation): D[M x N] = A[M x K] x B[N x K]^T,
+ * all row-major device arrays (A, B as BF16 bit patterns).  M a multiple of 128, N a multiple of
+ * 16 in [16, 256], K a positive multiple of 64.  The building block of the denoiser's
+ * convolutions, exported for its parity tests.  Synchronises the stream. */
+AGB_API agb_status agb_tc_gemm_bf16(const uint16_t* a, const uint16_t* b, float* d, int32_t m,
+    int32_t n, int32_t k, void* cuda_stream);
 /* Halton (2, 3) camera jitter in pixels, centred on [-0.5, 0.5] (PTRenderer.cpp:81-95,159-174):
  * index = (phase_count ? frame_index % phase_count : frame_index) + 1. */
 AGB_API void agb_temporal_jitter(uint32_t frame_index, uint32_t phase_count, float out[2]);
