@@ -1154,6 +1154,44 @@ AGB_API agb_status agb_tc_gemm_bf16(const uint16_t* a, const uint16_t* b, float*
     return AGB_OK;
 }
 
+AGB_API agb_status agb_conv3x3_bf16(const uint16_t* in0, const uint16_t* in1, const uint16_t* wpack,
+    const float* bias, uint16_t* out, float* out32, int32_t batch, int32_t height, int32_t width,
+    int32_t c0, int32_t c1, int32_t cout, int32_t up0, int32_t relu, void* cuda_stream)
+{
+    if (!in0 || !wpack || (c1 > 0 && !in1) || batch <= 0 || height <= 0 || width <= 0)
+        return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_bf16: null input or empty image");
+    if (c0 < 16 || c0 % 16 || c1 < 0 || c1 % 16 || cout < 16 || cout > 256 || cout % 16)
+        return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_bf16: channel counts must be multiples of 16, cout <= 256");
+    if (up0 && (height % 2 || width % 2))
+        return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_bf16: upsampled input needs even sizes");
+    if (int64_t(batch) * height * width >= (int64_t(1) << 31) / 128)
+        return fail(AGB_ERR_LIMIT, "agb_conv3x3_bf16: too many pixels");
+    uintptr_t al = reinterpret_cast<uintptr_t>(in0) | reinterpret_cast<uintptr_t>(in1) |
+        reinterpret_cast<uintptr_t>(wpack) | reinterpret_cast<uintptr_t>(out) | reinterpret_cast<uintptr_t>(out32);
+    if (al & 15u)
+        return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_bf16: pointers must be 16-byte aligned");
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    ConvLaunch c{ in0, c1 > 0 ? in1 : nullptr, wpack, bias, out, out32, batch, height, width, c0, c1, cout,
+        up0 ? 1 : 0, relu ? 1 : 0 };
+    AGB_CUDA(launchConv3x3(c, st), "agb_conv3x3_bf16");
+    AGB_CUDA(cudaStreamSynchronize(st), "agb_conv3x3_bf16");
+    int flag = 0;
+    AGB_CUDA(takeTcError(&flag), "agb_conv3x3_bf16");
+    if (flag)
+        return fail(AGB_ERR_TIMEOUT, "agb_conv3x3_bf16: tensor-core completion wait timed out");
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_pack_conv_weights(const float* w, int32_t cin, int32_t cout, int32_t flip,
+    uint16_t* out, void* cuda_stream)
+{
+    if (!w || !out || cin < 16 || cin % 16 || cout < 16 || cout % 16)
+        return fail(AGB_ERR_INVALID_ARG, "agb_pack_conv_weights: channel counts must be multiples of 16");
+    AGB_CUDA(launchPackConvWeights(w, cin, cout, flip ? 1 : 0, out, static_cast<cudaStream_t>(cuda_stream)),
+        "agb_pack_conv_weights");
+    return AGB_OK;
+}
+
 AGB_API void agb_temporal_jitter(uint32_t frame_index, uint32_t phase_count, float out[2])
 {
     // PTRenderer.cpp:81-95 (halton) and :168-174: index = frame (mod phases) + 1, centred.

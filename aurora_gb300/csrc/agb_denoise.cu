@@ -6,6 +6,8 @@
 // the threads; thread 0 issues four K16 MMAs per chunk and commits them to the stage's mbarrier,
 // which the threads wait on before refilling that stage.  The epilogue reads the accumulator rows
 // from TMEM (warp w owns lanes 32w..32w+31).
+#include <cuda_bf16.h>
+
 #include "agb_kernels.h"
 #include "agb_tc.cuh"
 
@@ -119,7 +121,223 @@ __global__ void __launch_bounds__(128) k_tc_gemm(const uint16_t* A, const uint16
         atomicExch(&g_tcError, 1);
 }
 
+// ------------------------------------------------------------------ 3x3 convolution
+// Implicit GEMM: rows = output pixels (128 per CTA), columns = output channels (Cout <= 256),
+// K = 9 taps x Cin input channels (k = tap * Cin + c; Cin and every input's channel count are
+// multiples of 16, so a K16 slice is one tap of 16 channels of one input).  Activations are NHWC
+// BF16 over a batch of images; the input is the concatenation of in0 (optionally read through a
+// nearest 2x upsample from half resolution) and in1.  Zero padding at the image border.
+//
+// Weights arrive pre-packed in the B-operand layout, slice after slice (Cout x 16 per slice), so
+// each stage's weights are one contiguous 1D bulk (TMA) copy; the activations are gathered by the
+// threads (one pixel row each, two 16-byte loads per slice) into the A layout.  Epilogue: + bias,
+// optional ReLU, BF16 round-to-nearest-even store (and an optional FP32 copy).
+
+struct ConvArgs
+{
+    const uint16_t* in0;   // [B][H0][W0][C0]; H0 = H / 2 when up0
+    const uint16_t* in1;   // [B][H][W][C1] or null
+    const uint16_t* wpack; // 9 * (C0 + C1) / 16 slices of Cout x 16
+    const float* bias;     // [Cout] or null
+    uint16_t* out;         // [B][H][W][Cout] or null
+    float* out32;          // [B][H][W][Cout] or null
+    int B, H, W, C0, C1, Cout, up0, relu;
+};
+
+constexpr int kConvStageSlices = 4;
+
+__device__ __forceinline__ void gatherSlice(const ConvArgs& a, int Cin, int slice, long p, long P,
+    uint8_t* aSlice, int row)
+{
+    uint4 v0 = make_uint4(0, 0, 0, 0), v1 = v0;
+    int k   = slice * 16;
+    int tap = k / Cin;
+    int c   = k - tap * Cin;
+    if (p < P)
+    {
+        int x  = int(p % a.W);
+        long t = p / a.W;
+        int y  = int(t % a.H);
+        int b  = int(t / a.H);
+        int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
+        if (yy >= 0 && yy < a.H && xx >= 0 && xx < a.W)
+        {
+            const uint16_t* src;
+            if (c < a.C0)
+            {
+                int h0 = a.up0 ? a.H >> 1 : a.H, w0 = a.up0 ? a.W >> 1 : a.W;
+                int y0 = a.up0 ? yy >> 1 : yy, x0 = a.up0 ? xx >> 1 : xx;
+                src = a.in0 + ((size_t(b) * h0 + y0) * w0 + x0) * a.C0 + c;
+            }
+            else
+                src = a.in1 + ((size_t(b) * a.H + yy) * a.W + xx) * a.C1 + (c - a.C0);
+            v0 = __ldg(reinterpret_cast<const uint4*>(src));
+            v1 = __ldg(reinterpret_cast<const uint4*>(src) + 1);
+        }
+    }
+    *reinterpret_cast<uint4*>(aSlice + tc::sliceOffset(row, 0)) = v0;
+    *reinterpret_cast<uint4*>(aSlice + tc::sliceOffset(row, 8)) = v1;
+}
+
+__global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t mmaBar[2], tmaBar[2];
+    __shared__ uint32_t tmemBase;
+    const int tid  = threadIdx.x;
+    const int warp = tid >> 5;
+    const int Cin  = a.C0 + a.C1;
+    const int N    = a.Cout;
+    const uint32_t aStage = kConvStageSlices * 128 * 32;
+    const uint32_t bSlice = uint32_t(N) * 32;
+    const uint32_t bStage = kConvStageSlices * bSlice;
+    uint8_t* aS[2] = { smem, smem + aStage + bStage };
+    uint8_t* bS[2] = { smem + aStage, smem + 2 * aStage + bStage };
+    const uint32_t cols = tc::tmemCols(uint32_t(N));
+    if (warp == 0)
+        tc::tmemAlloc(&tmemBase, cols);
+    if (tid == 0)
+    {
+        for (int s = 0; s < 2; s++)
+        {
+            tc::mbarInit(&mmaBar[s], 1);
+            tc::mbarInit(&tmaBar[s], 1);
+        }
+        tc::fenceMbarInit();
+    }
+    tc::fenceBeforeSync();
+    __syncthreads();
+    tc::fenceAfterSync();
+    const uint32_t tmem  = tmemBase;
+    const uint32_t idesc = tc::idescBf16(128, uint32_t(N));
+    const long P         = long(a.B) * a.H * a.W;
+    const long p         = long(blockIdx.x) * 128 + tid;
+    const int slices     = 9 * Cin / 16;
+    const int chunks     = (slices + kConvStageSlices - 1) / kConvStageSlices;
+    uint32_t mmaParity[2] = { 0, 0 }, tmaParity[2] = { 0, 0 };
+    bool ok = true;
+    for (int c = 0; c < chunks; c++)
+    {
+        const int s  = c & 1;
+        const int s0 = c * kConvStageSlices;
+        const int ns = min(kConvStageSlices, slices - s0);
+        if (c >= 2)
+        {
+            ok = tc::mbarWait(&mmaBar[s], mmaParity[s]) && ok;
+            mmaParity[s] ^= 1u;
+        }
+        if (tid == 0)
+        {
+            tc::mbarExpectTx(&tmaBar[s], uint32_t(ns) * bSlice);
+            tc::bulkLoad(bS[s], a.wpack + size_t(s0) * (bSlice / 2), uint32_t(ns) * bSlice, &tmaBar[s]);
+        }
+        for (int j = 0; j < ns; j++)
+            gatherSlice(a, Cin, s0 + j, p, P, aS[s] + j * (128 * 32), tid);
+        tc::fenceProxyAsync();
+        __syncthreads();
+        if (tid == 0)
+        {
+            ok = tc::mbarWait(&tmaBar[s], tmaParity[s]) && ok;
+            tc::fenceAfterSync();
+            for (int j = 0; j < ns; j++)
+            {
+                uint64_t ad = tc::smemDesc(tc::smemAddr(aS[s] + j * (128 * 32)), tc::kSliceLbo, tc::kSliceSbo);
+                uint64_t bd = tc::smemDesc(tc::smemAddr(bS[s] + j * bSlice), tc::kSliceLbo, tc::kSliceSbo);
+                tc::mma(tmem, ad, bd, idesc, (c > 0 || j > 0) ? 1u : 0u);
+            }
+            tc::commit(&mmaBar[s]);
+        }
+        tmaParity[s] ^= 1u;
+        __syncwarp();
+    }
+    {
+        const int sl = (chunks - 1) & 1;
+        ok           = tc::mbarWait(&mmaBar[sl], mmaParity[sl]) && ok;
+    }
+    tc::fenceAfterSync();
+    const long row = long(blockIdx.x) * 128 + warp * 32 + (tid & 31);
+    for (int c0 = 0; c0 < N; c0 += 16)
+    {
+        uint32_t r[16];
+        tc::tmemLoad16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), r);
+        tc::tmemWaitLoad();
+        if (row < P)
+        {
+            float v[16];
+#pragma unroll
+            for (int j = 0; j < 16; j++)
+            {
+                v[j] = __uint_as_float(r[j]) + (a.bias ? __ldg(a.bias + c0 + j) : 0.f);
+                if (a.relu)
+                    v[j] = fmaxf(v[j], 0.f);
+            }
+            if (a.out)
+            {
+                uint32_t w[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++)
+                    w[j] = uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(v[2 * j]))) |
+                        (uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(v[2 * j + 1]))) << 16);
+                uint4* o = reinterpret_cast<uint4*>(a.out + size_t(row) * N + c0);
+                o[0]     = make_uint4(w[0], w[1], w[2], w[3]);
+                o[1]     = make_uint4(w[4], w[5], w[6], w[7]);
+            }
+            if (a.out32)
+            {
+                float4* o = reinterpret_cast<float4*>(a.out32 + size_t(row) * N + c0);
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+            }
+        }
+    }
+    tc::fenceBeforeSync();
+    __syncthreads();
+    if (warp == 0)
+        tc::tmemDealloc(tmem, cols);
+    if (!ok && tid == 0)
+        atomicExch(&g_tcError, 1);
+}
+
+// Packs FP32 weights w[tap][ci][co] (9 x Cin x Cout) into the conv kernel's B layout (BF16).
+// flip: pack the data-gradient weights instead, w'[tap'][co][ci] = w[8 - tap'][ci][co], so that
+// k_conv3x3 over dY computes dX (the kernel's Cin is then the layer's Cout and vice versa).
+__global__ void k_pack_conv_weights(const float* w, int Cin, int Cout, int flip, uint16_t* out)
+{
+    // Packed as the kernel sees it: kCin x kCout with kCin = flip ? Cout : Cin.
+    int kCin = flip ? Cout : Cin, kCout = flip ? Cin : Cout;
+    long total = 9L * kCin * kCout;
+    for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < total; i += long(gridDim.x) * blockDim.x)
+    {
+        int n   = int(i % kCout);     // kernel output channel
+        long kk = i / kCout;          // kernel K index = tap * kCin + c
+        int tap = int(kk / kCin), c = int(kk % kCin);
+        float v = flip ? w[(size_t(8 - tap) * Cin + n) * Cout + c] : w[(size_t(tap) * Cin + c) * Cout + n];
+        int slice = int(kk / 16), kin = int(kk % 16);
+        size_t off = size_t(slice) * kCout * 16 + tc::sliceOffset(uint32_t(n), uint32_t(kin)) / 2;
+        out[off]   = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+    }
+}
+
 } // namespace
+
+cudaError_t launchConv3x3(const ConvLaunch& c, cudaStream_t st)
+{
+    ConvArgs a{ c.in0, c.in1, c.wpack, c.bias, c.out, c.out32, c.B, c.H, c.W, c.C0, c.C1, c.Cout, c.up0, c.relu };
+    size_t smem = 2 * (size_t(kConvStageSlices) * 128 * 32 + size_t(kConvStageSlices) * c.Cout * 32);
+    cudaError_t e = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess)
+        return e;
+    long P = long(c.B) * c.H * c.W;
+    k_conv3x3<<<unsigned((P + 127) / 128), 128, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launchPackConvWeights(const float* w, int Cin, int Cout, int flip, uint16_t* out, cudaStream_t st)
+{
+    k_pack_conv_weights<<<256, 256, 0, st>>>(w, Cin, Cout, flip, out);
+    return cudaGetLastError();
+}
 
 cudaError_t launchTcGemm(const uint16_t* A, const uint16_t* B, float* D, int M, int N, int K, cudaStream_t st)
 {

@@ -139,6 +139,18 @@ cudaError_t launchTemporalResolve(const float4* accum, const float4* history, co
     const float* depthView, int W, int H, const TemporalSettings& s, float4* out, cudaStream_t st);
 
 // agb_denoise.cu
+struct ConvLaunch
+{
+    const uint16_t* in0;
+    const uint16_t* in1;
+    const uint16_t* wpack;
+    const float* bias;
+    uint16_t* out;
+    float* out32;
+    int B, H, W, C0, C1, Cout, up0, relu;
+};
+cudaError_t launchConv3x3(const ConvLaunch& c, cudaStream_t st);
+cudaError_t launchPackConvWeights(const float* w, int Cin, int Cout, int flip, uint16_t* out, cudaStream_t st);
 cudaError_t launchTcGemm(const uint16_t* A, const uint16_t* B, float* D, int M, int N, int K, cudaStream_t st);
 // Reads and clears the tensor-core kernels' timeout flag (1 = a bounded wait ran out).
 cudaError_t takeTcError(int* flag);

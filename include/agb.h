@@ -455,6 +455,20 @@ AGB_API agb_status agb_temporal_resolve_batch(const float* accum, const float* h
  * convolutions, exported for its parity tests.  Synchronises the stream. */
 AGB_API agb_status agb_tc_gemm_bf16(const uint16_t* a, const uint16_t* b, float* d, int32_t m,
     int32_t n, int32_t k, void* cuda_stream);
+/* 3x3 convolution on the tensor cores (the denoiser's layer), NHWC BF16 over a batch:
+ * out[b][y][x][:] = bias + sum over taps and input channels of in[b][y+dy][x+dx][:] * w, zero
+ * padded, optional ReLU; the input is the channel concatenation of in0 (read through a nearest 2x
+ * upsample from height/2 x width/2 when up0) and in1 (may be null, c1 = 0).  c0, c1 and cout are
+ * multiples of 16 (c0 >= 16, cout <= 256); wpack is the output of agb_pack_conv_weights; out (BF16)
+ * and out32 (FP32) may each be null.  Exported for the denoiser's parity tests. */
+AGB_API agb_status agb_conv3x3_bf16(const uint16_t* in0, const uint16_t* in1, const uint16_t* wpack,
+    const float* bias, uint16_t* out, float* out32, int32_t batch, int32_t height, int32_t width,
+    int32_t c0, int32_t c1, int32_t cout, int32_t up0, int32_t relu, void* cuda_stream);
+/* Packs FP32 weights w[tap][cin][cout] (tap = 3 * (dy + 1) + (dx + 1)) for agb_conv3x3_bf16;
+ * flip != 0 packs the data-gradient convolution instead (input = dY with cout channels, output = dX
+ * with cin channels).  out holds 9 * cin * cout BF16 values. */
+AGB_API agb_status agb_pack_conv_weights(const float* w, int32_t cin, int32_t cout, int32_t flip,
+    uint16_t* out, void* cuda_stream);
 /* Halton (2, 3) camera jitter in pixels, centred on [-0.5, 0.5] (PTRenderer.cpp:81-95,159-174):
  * index = (phase_count ? frame_index % phase_count : frame_index) + 1. */
 AGB_API void agb_temporal_jitter(uint32_t frame_index, uint32_t phase_count, float out[2]);
