@@ -177,6 +177,7 @@ SIGNATURES = {
     "agb_tc_gemm_bf16": (_I32, [_P, _P, _P, _I32, _I32, _I32, _P]),
     "agb_conv3x3_bf16": (_I32, [_P, _P, _P, _P, _P, _P] + [_I32] * 8 + [_P]),
     "agb_pack_conv_weights": (_I32, [_P, _I32, _I32, _I32, _P, _P]),
+    "agb_conv3x3_wgrad_bf16": (_I32, [_P, _P, _P, _P] + [_I32] * 7 + [_P]),
     "agb_bsdf_batch": (_I32, [_I32, _P, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _P]),
     "agb_intersect_batch": (_I32, [_P, _P, _I64, _I32, _P, _P]),
     "agb_env_sample_batch": (_I32, [_P, _P, _I64, _P, _P, _P]),

@@ -1160,8 +1160,9 @@ AGB_API agb_status agb_conv3x3_bf16(const uint16_t* in0, const uint16_t* in1, co
 {
     if (!in0 || !wpack || (c1 > 0 && !in1) || batch <= 0 || height <= 0 || width <= 0)
         return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_bf16: null input or empty image");
-    if (c0 < 16 || c0 % 16 || c1 < 0 || c1 % 16 || cout < 16 || cout > 256 || cout % 16)
-        return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_bf16: channel counts must be multiples of 16, cout <= 256");
+    if (c0 < 16 || c0 % 16 || c1 < 0 || c1 % 16 || cout < 16 || cout % 16 || (cout > 256 && cout % 128) || cout > 1024)
+        return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_bf16: channel counts must be multiples of 16 (cout <= 256 "
+                                         "or a multiple of 128 up to 1024)");
     if (up0 && (height % 2 || width % 2))
         return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_bf16: upsampled input needs even sizes");
     if (int64_t(batch) * height * width >= (int64_t(1) << 31) / 128)
@@ -1179,6 +1180,34 @@ AGB_API agb_status agb_conv3x3_bf16(const uint16_t* in0, const uint16_t* in1, co
     AGB_CUDA(takeTcError(&flag), "agb_conv3x3_bf16");
     if (flag)
         return fail(AGB_ERR_TIMEOUT, "agb_conv3x3_bf16: tensor-core completion wait timed out");
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_conv3x3_wgrad_bf16(const uint16_t* in0, const uint16_t* in1, const uint16_t* dy,
+    float* dw, int32_t batch, int32_t height, int32_t width, int32_t c0, int32_t c1, int32_t cout,
+    int32_t up0, void* cuda_stream)
+{
+    if (!in0 || !dy || !dw || (c1 > 0 && !in1) || batch <= 0 || height <= 0 || width <= 0)
+        return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_wgrad_bf16: null input or empty image");
+    if (c0 < 16 || c0 % 16 || c1 < 0 || c1 % 16 || cout < 16 || cout > 256 || cout % 16 || c0 + c1 > 1024)
+        return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_wgrad_bf16: channel counts must be multiples of 16, cout <= 256");
+    if (up0 && (height % 2 || width % 2))
+        return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_wgrad_bf16: upsampled input needs even sizes");
+    uintptr_t al = reinterpret_cast<uintptr_t>(in0) | reinterpret_cast<uintptr_t>(in1) | reinterpret_cast<uintptr_t>(dy);
+    if (al & 15u)
+        return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_wgrad_bf16: pointers must be 16-byte aligned");
+    int dev = 0, sms = 0;
+    AGB_CUDA(cudaGetDevice(&dev), "agb_conv3x3_wgrad_bf16");
+    AGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "agb_conv3x3_wgrad_bf16");
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    ConvLaunch c{ in0, c1 > 0 ? in1 : nullptr, nullptr, nullptr, nullptr, nullptr, batch, height, width, c0, c1, cout,
+        up0 ? 1 : 0, 0 };
+    AGB_CUDA(launchConvWgrad(c, dy, dw, sms, st), "agb_conv3x3_wgrad_bf16");
+    AGB_CUDA(cudaStreamSynchronize(st), "agb_conv3x3_wgrad_bf16");
+    int flag = 0;
+    AGB_CUDA(takeTcError(&flag), "agb_conv3x3_wgrad_bf16");
+    if (flag)
+        return fail(AGB_ERR_TIMEOUT, "agb_conv3x3_wgrad_bf16: tensor-core completion wait timed out");
     return AGB_OK;
 }
 

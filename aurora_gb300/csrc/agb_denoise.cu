@@ -6,6 +6,8 @@
 // the threads; thread 0 issues four K16 MMAs per chunk and commits them to the stage's mbarrier,
 // which the threads wait on before refilling that stage.  The epilogue reads the accumulator rows
 // from TMEM (warp w owns lanes 32w..32w+31).
+#include <algorithm>
+
 #include <cuda_bf16.h>
 
 #include "agb_kernels.h"
@@ -142,9 +144,14 @@ struct ConvArgs
     uint16_t* out;         // [B][H][W][Cout] or null
     float* out32;          // [B][H][W][Cout] or null
     int B, H, W, C0, C1, Cout, up0, relu;
+    int nTile;             // output channels per CTA (grid.y = Cout / nTile)
 };
 
 constexpr int kConvStageSlices = 4;
+
+// Output channels per CTA for a layer with Cout channels: all of them up to the 256 accumulator
+// columns of one MMA tile, else tiles of 128.
+__host__ __device__ inline int convTile(int cout) { return cout <= 256 ? cout : 128; }
 
 __device__ __forceinline__ void gatherSlice(const ConvArgs& a, int Cin, int slice, long p, long P,
     uint8_t* aSlice, int row)
@@ -187,7 +194,8 @@ __global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a)
     const int tid  = threadIdx.x;
     const int warp = tid >> 5;
     const int Cin  = a.C0 + a.C1;
-    const int N    = a.Cout;
+    const int N    = a.nTile;
+    const int cb   = int(blockIdx.y) * N;
     const uint32_t aStage = kConvStageSlices * 128 * 32;
     const uint32_t bSlice = uint32_t(N) * 32;
     const uint32_t bStage = kConvStageSlices * bSlice;
@@ -229,7 +237,8 @@ __global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a)
         if (tid == 0)
         {
             tc::mbarExpectTx(&tmaBar[s], uint32_t(ns) * bSlice);
-            tc::bulkLoad(bS[s], a.wpack + size_t(s0) * (bSlice / 2), uint32_t(ns) * bSlice, &tmaBar[s]);
+            tc::bulkLoad(bS[s], a.wpack + (size_t(blockIdx.y) * slices + s0) * (bSlice / 2), uint32_t(ns) * bSlice,
+                &tmaBar[s]);
         }
         for (int j = 0; j < ns; j++)
             gatherSlice(a, Cin, s0 + j, p, P, aS[s] + j * (128 * 32), tid);
@@ -267,7 +276,7 @@ __global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a)
 #pragma unroll
             for (int j = 0; j < 16; j++)
             {
-                v[j] = __uint_as_float(r[j]) + (a.bias ? __ldg(a.bias + c0 + j) : 0.f);
+                v[j] = __uint_as_float(r[j]) + (a.bias ? __ldg(a.bias + cb + c0 + j) : 0.f);
                 if (a.relu)
                     v[j] = fmaxf(v[j], 0.f);
             }
@@ -278,17 +287,180 @@ __global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a)
                 for (int j = 0; j < 8; j++)
                     w[j] = uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(v[2 * j]))) |
                         (uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(v[2 * j + 1]))) << 16);
-                uint4* o = reinterpret_cast<uint4*>(a.out + size_t(row) * N + c0);
+                uint4* o = reinterpret_cast<uint4*>(a.out + size_t(row) * a.Cout + cb + c0);
                 o[0]     = make_uint4(w[0], w[1], w[2], w[3]);
                 o[1]     = make_uint4(w[4], w[5], w[6], w[7]);
             }
             if (a.out32)
             {
-                float4* o = reinterpret_cast<float4*>(a.out32 + size_t(row) * N + c0);
+                float4* o = reinterpret_cast<float4*>(a.out32 + size_t(row) * a.Cout + cb + c0);
 #pragma unroll
                 for (int j = 0; j < 4; j++)
                     o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
             }
+        }
+    }
+    tc::fenceBeforeSync();
+    __syncthreads();
+    if (warp == 0)
+        tc::tmemDealloc(tmem, cols);
+    if (!ok && tid == 0)
+        atomicExch(&g_tcError, 1);
+}
+
+// ------------------------------------------------------------------ weight gradient
+// dW[tap][ci][co] += sum over pixels p of X[p + d(tap)][ci] * dY[p][co], X = concat(up(in0), in1) as
+// in the forward pass.  GEMM with rows = input channels (128 per CTA, grid.z blocks), columns =
+// Cout, K = pixels: grid.x splits the pixels (each CTA sums its range in TMEM and adds it to dW
+// with FP32 reductions), grid.y is the tap.  NHWC stores channels contiguously but the MMA wants
+// both operands K-major (pixels contiguous), so the threads transpose while staging: thread t
+// takes pixel t % 64 of the 64-pixel chunk and half of the channel rows, loads 8 channels at a time
+// and scatters them into the operand layout.
+
+struct WgradArgs
+{
+    const uint16_t* in0;
+    const uint16_t* in1;
+    const uint16_t* dy;  // [B][H][W][Cout]
+    float* dw;           // [9][Cin][Cout], accumulated
+    int B, H, W, C0, C1, Cout, up0;
+    int chunksPerSplit;  // 64-pixel chunks per CTA
+};
+
+__device__ __forceinline__ void scatter8(uint8_t* slice, int row0, int k, uint4 v)
+{
+    const uint16_t* e = reinterpret_cast<const uint16_t*>(&v);
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+        *reinterpret_cast<uint16_t*>(slice + tc::sliceOffset(uint32_t(row0 + i), uint32_t(k))) = e[i];
+}
+
+__global__ void __launch_bounds__(128) k_conv_wgrad(WgradArgs a)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t mmaBar[2];
+    __shared__ uint32_t tmemBase;
+    const int tid  = threadIdx.x;
+    const int warp = tid >> 5;
+    const int Cin  = a.C0 + a.C1;
+    const int N    = a.Cout;
+    const uint32_t aStage = 4 * 128 * 32;
+    const uint32_t bSlice = uint32_t(N) * 32;
+    const uint32_t bStage = 4 * bSlice;
+    uint8_t* aS[2] = { smem, smem + aStage + bStage };
+    uint8_t* bS[2] = { smem + aStage, smem + 2 * aStage + bStage };
+    const long P         = long(a.B) * a.H * a.W;
+    const long total     = (P + 63) / 64;
+    const long first     = long(blockIdx.x) * a.chunksPerSplit;
+    const int chunks     = int(min(long(a.chunksPerSplit), total - first));
+    if (chunks <= 0)
+        return;
+    const uint32_t cols = tc::tmemCols(uint32_t(N));
+    if (warp == 0)
+        tc::tmemAlloc(&tmemBase, cols);
+    if (tid == 0)
+    {
+        tc::mbarInit(&mmaBar[0], 1);
+        tc::mbarInit(&mmaBar[1], 1);
+        tc::fenceMbarInit();
+    }
+    tc::fenceBeforeSync();
+    __syncthreads();
+    tc::fenceAfterSync();
+    const uint32_t tmem  = tmemBase;
+    const uint32_t idesc = tc::idescBf16(128, uint32_t(N));
+    const int tap = blockIdx.y, oy = tap / 3 - 1, ox = tap % 3 - 1;
+    const int ci0 = blockIdx.z * 128;
+    const int j   = tid & 63, hh = tid >> 6;
+    uint32_t parity[2] = { 0, 0 };
+    bool ok = true;
+    for (int c = 0; c < chunks; c++)
+    {
+        const int s = c & 1;
+        if (c >= 2)
+        {
+            ok = tc::mbarWait(&mmaBar[s], parity[s]) && ok;
+            parity[s] ^= 1u;
+        }
+        const long p = (first + c) * 64 + j;
+        uint8_t* aSl = aS[s] + (j >> 4) * (128 * 32);
+        uint8_t* bSl = bS[s] + (j >> 4) * bSlice;
+        const int k  = j & 15;
+        // A rows: input channels ci0 + hh * 64 + [0, 64) at the tap-shifted pixel.
+        bool inImg = false;
+        int b = 0, yy = 0, xx = 0;
+        if (p < P)
+        {
+            int x  = int(p % a.W);
+            long t = p / a.W;
+            int y  = int(t % a.H);
+            b      = int(t / a.H);
+            yy     = y + oy;
+            xx     = x + ox;
+            inImg  = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+        }
+#pragma unroll
+        for (int g = 0; g < 8; g++)
+        {
+            int ci  = ci0 + hh * 64 + g * 8;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (inImg && ci < Cin)
+            {
+                const uint16_t* src;
+                if (ci < a.C0)
+                {
+                    int h0 = a.up0 ? a.H >> 1 : a.H, w0 = a.up0 ? a.W >> 1 : a.W;
+                    int y0 = a.up0 ? yy >> 1 : yy, x0 = a.up0 ? xx >> 1 : xx;
+                    src = a.in0 + ((size_t(b) * h0 + y0) * w0 + x0) * a.C0 + ci;
+                }
+                else
+                    src = a.in1 + ((size_t(b) * a.H + yy) * a.W + xx) * a.C1 + (ci - a.C0);
+                v = __ldg(reinterpret_cast<const uint4*>(src));
+            }
+            scatter8(aSl, hh * 64 + g * 8, k, v);
+        }
+        // B rows: output channels hh * N / 2 + [0, N / 2) at the pixel itself.
+        for (int g = 0; g < N / 16; g++)
+        {
+            int co  = hh * (N / 2) + g * 8;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (p < P)
+                v = __ldg(reinterpret_cast<const uint4*>(a.dy + size_t(p) * N + co));
+            scatter8(bSl, co, k, v);
+        }
+        tc::fenceProxyAsync();
+        __syncthreads();
+        if (tid == 0)
+        {
+            tc::fenceAfterSync();
+#pragma unroll
+            for (int sl = 0; sl < 4; sl++)
+            {
+                uint64_t ad = tc::smemDesc(tc::smemAddr(aS[s] + sl * (128 * 32)), tc::kSliceLbo, tc::kSliceSbo);
+                uint64_t bd = tc::smemDesc(tc::smemAddr(bS[s] + sl * bSlice), tc::kSliceLbo, tc::kSliceSbo);
+                tc::mma(tmem, ad, bd, idesc, (c > 0 || sl > 0) ? 1u : 0u);
+            }
+            tc::commit(&mmaBar[s]);
+        }
+        __syncwarp();
+    }
+    {
+        const int sl = (chunks - 1) & 1;
+        ok           = tc::mbarWait(&mmaBar[sl], parity[sl]) && ok;
+    }
+    tc::fenceAfterSync();
+    const int ci = ci0 + warp * 32 + (tid & 31);
+    for (int c0 = 0; c0 < N; c0 += 16)
+    {
+        uint32_t r[16];
+        tc::tmemLoad16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), r);
+        tc::tmemWaitLoad();
+        if (ci < Cin)
+        {
+            float* dst = a.dw + (size_t(tap) * Cin + ci) * N + c0;
+#pragma unroll
+            for (int q = 0; q < 16; q++)
+                atomicAdd(dst + q, __uint_as_float(r[q]));
         }
     }
     tc::fenceBeforeSync();
@@ -314,7 +486,9 @@ __global__ void k_pack_conv_weights(const float* w, int Cin, int Cout, int flip,
         int tap = int(kk / kCin), c = int(kk % kCin);
         float v = flip ? w[(size_t(8 - tap) * Cin + n) * Cout + c] : w[(size_t(tap) * Cin + c) * Cout + n];
         int slice = int(kk / 16), kin = int(kk % 16);
-        size_t off = size_t(slice) * kCout * 16 + tc::sliceOffset(uint32_t(n), uint32_t(kin)) / 2;
+        int nt = convTile(kCout), tile = n / nt, nn = n % nt;
+        size_t slices = size_t(9) * kCin / 16;
+        size_t off = (size_t(tile) * slices + slice) * nt * 16 + tc::sliceOffset(uint32_t(nn), uint32_t(kin)) / 2;
         out[off]   = __bfloat16_as_ushort(__float2bfloat16_rn(v));
     }
 }
@@ -323,13 +497,33 @@ __global__ void k_pack_conv_weights(const float* w, int Cin, int Cout, int flip,
 
 cudaError_t launchConv3x3(const ConvLaunch& c, cudaStream_t st)
 {
-    ConvArgs a{ c.in0, c.in1, c.wpack, c.bias, c.out, c.out32, c.B, c.H, c.W, c.C0, c.C1, c.Cout, c.up0, c.relu };
-    size_t smem = 2 * (size_t(kConvStageSlices) * 128 * 32 + size_t(kConvStageSlices) * c.Cout * 32);
+    int nt = convTile(c.Cout);
+    ConvArgs a{ c.in0, c.in1, c.wpack, c.bias, c.out, c.out32, c.B, c.H, c.W, c.C0, c.C1, c.Cout, c.up0, c.relu, nt };
+    size_t smem = 2 * (size_t(kConvStageSlices) * 128 * 32 + size_t(kConvStageSlices) * nt * 32);
     cudaError_t e = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess)
         return e;
     long P = long(c.B) * c.H * c.W;
-    k_conv3x3<<<unsigned((P + 127) / 128), 128, smem, st>>>(a);
+    k_conv3x3<<<dim3(unsigned((P + 127) / 128), unsigned(c.Cout / nt)), 128, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launchConvWgrad(const ConvLaunch& c, const uint16_t* dy, float* dw, int smCount, cudaStream_t st)
+{
+    int Cin = c.C0 + c.C1;
+    WgradArgs a{ c.in0, c.in1, dy, dw, c.B, c.H, c.W, c.C0, c.C1, c.Cout, c.up0, 1 };
+    long P      = long(c.B) * c.H * c.W;
+    long chunks = (P + 63) / 64;
+    int mblocks = (Cin + 127) / 128;
+    long want   = std::max(1L, long(smCount) * 2 / (9L * mblocks));
+    long splits = std::min(chunks, want);
+    a.chunksPerSplit = int((chunks + splits - 1) / splits);
+    splits           = (chunks + a.chunksPerSplit - 1) / a.chunksPerSplit;
+    size_t smem = 2 * (size_t(4) * 128 * 32 + size_t(4) * c.Cout * 32);
+    cudaError_t e = cudaFuncSetAttribute(k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess)
+        return e;
+    k_conv_wgrad<<<dim3(unsigned(splits), 9, unsigned(mblocks)), 128, smem, st>>>(a);
     return cudaGetLastError();
 }
 

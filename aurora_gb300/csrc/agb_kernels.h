@@ -150,6 +150,9 @@ struct ConvLaunch
     int B, H, W, C0, C1, Cout, up0, relu;
 };
 cudaError_t launchConv3x3(const ConvLaunch& c, cudaStream_t st);
+// dW[tap][ci][co] += sum over pixels of X[p + d][ci] dY[p][co] (X as c.in0 / c.in1 / c.up0; c.Cout
+// the layer's output channels, at most 256).
+cudaError_t launchConvWgrad(const ConvLaunch& c, const uint16_t* dy, float* dw, int smCount, cudaStream_t st);
 cudaError_t launchPackConvWeights(const float* w, int Cin, int Cout, int flip, uint16_t* out, cudaStream_t st);
 cudaError_t launchTcGemm(const uint16_t* A, const uint16_t* B, float* D, int M, int N, int K, cudaStream_t st);
 // Reads and clears the tensor-core kernels' timeout flag (1 = a bounded wait ran out).

@@ -464,6 +464,11 @@ AGB_API agb_status agb_tc_gemm_bf16(const uint16_t* a, const uint16_t* b, float*
 AGB_API agb_status agb_conv3x3_bf16(const uint16_t* in0, const uint16_t* in1, const uint16_t* wpack,
     const float* bias, uint16_t* out, float* out32, int32_t batch, int32_t height, int32_t width,
     int32_t c0, int32_t c1, int32_t cout, int32_t up0, int32_t relu, void* cuda_stream);
+/* Weight gradient of agb_conv3x3_bf16 (same input arguments, cout <= 256): adds
+ * dw[tap][cin][cout] += sum over pixels of in[p + d(tap)][cin] * dy[p][cout] into the FP32 array dw. */
+AGB_API agb_status agb_conv3x3_wgrad_bf16(const uint16_t* in0, const uint16_t* in1, const uint16_t* dy,
+    float* dw, int32_t batch, int32_t height, int32_t width, int32_t c0, int32_t c1, int32_t cout,
+    int32_t up0, void* cuda_stream);
 /* Packs FP32 weights w[tap][cin][cout] (tap = 3 * (dy + 1) + (dx + 1)) for agb_conv3x3_bf16;
  * flip != 0 packs the data-gradient convolution instead (input = dY with cout channels, output = dX
  * with cin channels).  out holds 9 * cin * cout BF16 values. */

@@ -85,3 +85,62 @@ def test_conv3x3_data_gradient_matches_oracle(agb, case):
     err = np.abs(g32 - want) / scale
     print(f"data grad {case}: max err / sum|dy w| = {err.max():.3g}")
     assert err.max() < 1e-5
+
+
+def test_conv3x3_output_tiles_match_oracle(agb):
+    """Cout above the 256 accumulator columns of one MMA tile runs as tiles of 128 channels."""
+    rng = np.random.default_rng(7)
+    B, H, W, C0, Cout = 1, 8, 12, 32, 384
+    x0 = ref.bf16_bits(rng.normal(0, 1, (B, H, W, C0)))
+    w = ref.bf16(rng.normal(0, 0.2, (9, C0, Cout)))
+    bias = rng.normal(0, 0.1, Cout)
+    g32, _ = run_conv(agb, x0, None, w, bias, B, H, W, False, False)
+    xin = ref.from_bits(x0)
+    want = ref.conv3x3(xin, w, bias)
+    err = np.abs(g32 - want) / (ref.conv3x3(np.abs(xin), np.abs(w), np.abs(bias)) + 1e-30)
+    assert err.max() < 1e-5
+    # Data gradient of a layer with 384 input channels (the first decoder layer).
+    dy = ref.bf16_bits(rng.normal(0, 1, (B, H, W, 128)))
+    w2 = ref.bf16(rng.normal(0, 0.2, (9, 384, 128)))
+    d32, _ = run_conv(agb, dy, None, w2, None, B, H, W, False, False, flip=True)
+    want = ref.conv3x3_data_grad(ref.from_bits(dy), w2)
+    err = np.abs(d32 - want) / (ref.conv3x3_data_grad(np.abs(ref.from_bits(dy)), np.abs(w2)) + 1e-30)
+    print("384-channel tiles: max err", err.max())
+    assert err.max() < 1e-5
+
+
+WGRAD_CASES = [
+    # B, H, W, C0, C1, Cout, up0
+    (2, 16, 24, 16, 0, 32, False),
+    (1, 8, 8, 32, 16, 48, True),
+    (1, 10, 12, 256, 128, 128, True),
+    (3, 9, 14, 64, 0, 256, False),
+]
+
+
+@pytest.mark.parametrize("case", WGRAD_CASES)
+def test_conv3x3_weight_gradient_matches_oracle(agb, case):
+    import torch
+    from aurora_gb300 import _abi
+    B, H, W, C0, C1, Cout, up0 = case
+    rng = np.random.default_rng(sum(case[:6]) + 1)
+    h0, w0 = (H // 2, W // 2) if up0 else (H, W)
+    x0 = ref.bf16_bits(rng.normal(0, 1, (B, h0, w0, C0)))
+    x1 = ref.bf16_bits(rng.normal(0, 1, (B, H, W, C1))) if C1 else None
+    dy = ref.bf16_bits(rng.normal(0, 1, (B, H, W, Cout)))
+    dw = torch.full((9, C0 + C1, Cout), 0.5, dtype=torch.float32, device="cuda")
+    d0, d1, dd = to_dev(x0), (to_dev(x1) if C1 else None), to_dev(dy)
+    _abi.check(agb.agb_conv3x3_wgrad_bf16(d0.data_ptr(), d1.data_ptr() if d1 is not None else None,
+                                          dd.data_ptr(), dw.data_ptr(), B, H, W, C0, C1, Cout,
+                                          1 if up0 else 0, None))
+    g = dw.cpu().numpy().astype(np.float64) - 0.5
+    xin = ref.from_bits(x0)
+    if up0:
+        xin = ref.upsample2(xin)
+    if C1:
+        xin = np.concatenate([xin, ref.from_bits(x1)], axis=3)
+    want, _ = ref.conv3x3_weight_grad(xin, ref.from_bits(dy))
+    scale, _ = ref.conv3x3_weight_grad(np.abs(xin), np.abs(ref.from_bits(dy)))
+    err = np.abs(g - want) / (scale + 1e-30)
+    print(f"wgrad {case}: max err / sum|x dy| = {err.max():.3g}")
+    assert err.max() < 1e-5
