@@ -20,6 +20,7 @@ ERR_LIMIT = -6
 
 ACCUM_RUNNING_MEAN = 1
 ACCUM_KAHAN = 2
+ACCUM_MOMENTS = 4
 FORMAT_RGBA8 = 0
 FORMAT_RGBA32F = 1
 FORMAT_RGB32F = 2
@@ -178,6 +179,16 @@ SIGNATURES = {
     "agb_conv3x3_bf16": (_I32, [_P, _P, _P, _P, _P, _P] + [_I32] * 8 + [_P]),
     "agb_pack_conv_weights": (_I32, [_P, _I32, _I32, _I32, _P, _P]),
     "agb_conv3x3_wgrad_bf16": (_I32, [_P, _P, _P, _P] + [_I32] * 7 + [_P]),
+    "agb_denoiser_create": (_I32, [_I32, _P, _U64, ctypes.POINTER(_P)]),
+    "agb_denoiser_destroy": (_I32, [_P]),
+    "agb_denoiser_param_count": (_I32, [ctypes.POINTER(_U64)]),
+    "agb_denoiser_params": (_I32, [_P, _P, _U64]),
+    "agb_denoiser_set_params": (_I32, [_P, _P, _U64]),
+    "agb_denoiser_grads": (_I32, [_P, _P, _U64]),
+    "agb_denoiser_forward": (_I32, [_P, _P, _I32, _I32, _I32, _P]),
+    "agb_denoiser_train_step": (_I32, [_P, _P, _P, _I32, _I32, _I32, ctypes.c_float, _I32,
+                                       ctypes.POINTER(ctypes.c_float)]),
+    "agb_denoiser_features": (_I32, [_P, _P]),
     "agb_bsdf_batch": (_I32, [_I32, _P, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _P, _P]),
     "agb_intersect_batch": (_I32, [_P, _P, _I64, _I32, _P, _P]),
     "agb_env_sample_batch": (_I32, [_P, _P, _I64, _P, _P, _P]),

@@ -138,7 +138,7 @@ struct agb_context
     WaveBuffers wb{};
     // Accumulation.
     uint32_t accW = 0, accH = 0;
-    DevBuf accMean, accSum, accComp, lastSample;
+    DevBuf accMean, accSum, accComp, lastSample, accMoments;
     // Denoising AOVs of the last render that enabled them (accW x accH).
     DevBuf aovDepth, aovNormal, aovAlbedo, aovMotion;
     bool aovValid = false;
@@ -264,6 +264,8 @@ agb_status ensureAccum(agb_context* ctx, uint32_t W, uint32_t H)
     AGB_CUDA(ctx->accSum.ensure(n * sizeof(float4)), "allocate accumulation");
     AGB_CUDA(ctx->accComp.ensure(n * sizeof(float4)), "allocate accumulation");
     AGB_CUDA(ctx->lastSample.ensure(n * sizeof(float4)), "allocate accumulation");
+    AGB_CUDA(ctx->accMoments.ensure(n * sizeof(float2)), "allocate accumulation");
+    AGB_CUDA(cudaMemsetAsync(ctx->accMoments.ptr, 0, n * sizeof(float2), ctx->stream), "clear");
     AGB_CUDA(cudaMemsetAsync(ctx->accMean.ptr, 0, n * sizeof(float4), ctx->stream), "clear");
     AGB_CUDA(cudaMemsetAsync(ctx->accSum.ptr, 0, n * sizeof(float4), ctx->stream), "clear");
     AGB_CUDA(cudaMemsetAsync(ctx->accComp.ptr, 0, n * sizeof(float4), ctx->stream), "clear");
@@ -864,6 +866,7 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
     wb.accumSum   = ctx->accSum.as<float4>();
     wb.accumComp  = ctx->accComp.as<float4>();
     wb.lastSample = ctx->lastSample.as<float4>();
+    wb.accumMoments = ctx->accMoments.as<float2>();
     uint64_t launches = 0;
     ctx->marks.reset();
     KernelMarks* marks = ctx->profiling ? &ctx->marks : nullptr;
@@ -1218,6 +1221,176 @@ AGB_API agb_status agb_pack_conv_weights(const float* w, int32_t cin, int32_t co
         return fail(AGB_ERR_INVALID_ARG, "agb_pack_conv_weights: channel counts must be multiples of 16");
     AGB_CUDA(launchPackConvWeights(w, cin, cout, flip ? 1 : 0, out, static_cast<cudaStream_t>(cuda_stream)),
         "agb_pack_conv_weights");
+    return AGB_OK;
+}
+
+struct agb_denoiser
+{
+    int device          = 0;
+    cudaStream_t stream = nullptr;
+    bool ownsStream     = false;
+    UnetDenoiser net;
+    ~agb_denoiser()
+    {
+        net.release();
+        if (ownsStream && stream)
+            cudaStreamDestroy(stream);
+    }
+};
+
+namespace
+{
+agb_status denoiserCheck(agb_denoiser* dn, int32_t B, int32_t H, int32_t W, const char* what)
+{
+    if (!dn)
+        return fail(AGB_ERR_INVALID_ARG, std::string(what) + ": null denoiser");
+    if (B <= 0 || H <= 0 || W <= 0 || H % 8 || W % 8)
+        return fail(AGB_ERR_INVALID_ARG, std::string(what) + ": batch > 0, height and width multiples of 8");
+    if (int64_t(B) * H * W >= (int64_t(1) << 26))
+        return fail(AGB_ERR_LIMIT, std::string(what) + ": too many pixels per batch");
+    AGB_CUDA(cudaSetDevice(dn->device), "cudaSetDevice");
+    return AGB_OK;
+}
+agb_status tcStatus(const char* what)
+{
+    int flag = 0;
+    AGB_CUDA(takeTcError(&flag), what);
+    if (flag)
+        return fail(AGB_ERR_TIMEOUT, std::string(what) + ": tensor-core completion wait timed out");
+    return AGB_OK;
+}
+} // namespace
+
+AGB_API agb_status agb_denoiser_create(int32_t device, void* cuda_stream, uint64_t seed, agb_denoiser** out)
+{
+    if (!out)
+        return fail(AGB_ERR_INVALID_ARG, "agb_denoiser_create: out is null");
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count)
+        return fail(AGB_ERR_INVALID_ARG, "agb_denoiser_create: no CUDA device " + std::to_string(device));
+    std::unique_ptr<agb_denoiser> dn(new agb_denoiser());
+    dn->device = device;
+    AGB_CUDA(cudaSetDevice(device), "cudaSetDevice");
+    int sms = 0;
+    AGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "agb_denoiser_create");
+    if (cuda_stream)
+        dn->stream = static_cast<cudaStream_t>(cuda_stream);
+    else
+    {
+        AGB_CUDA(cudaStreamCreateWithFlags(&dn->stream, cudaStreamNonBlocking), "create stream");
+        dn->ownsStream = true;
+    }
+    AGB_CUDA(dn->net.init(seed, dn->stream, sms), "agb_denoiser_create");
+    AGB_CUDA(cudaStreamSynchronize(dn->stream), "agb_denoiser_create");
+    *out = dn.release();
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_denoiser_destroy(agb_denoiser* dn)
+{
+    if (dn)
+    {
+        cudaSetDevice(dn->device);
+        delete dn;
+    }
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_denoiser_param_count(uint64_t* count)
+{
+    if (!count)
+        return fail(AGB_ERR_INVALID_ARG, "agb_denoiser_param_count: null argument");
+    *count = UnetDenoiser::paramCount();
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_denoiser_params(agb_denoiser* dn, float* host_out, uint64_t count)
+{
+    if (!dn || !host_out || count < dn->net.nParams())
+        return fail(AGB_ERR_INVALID_ARG, "agb_denoiser_params: null argument or output too small");
+    AGB_CUDA(cudaSetDevice(dn->device), "cudaSetDevice");
+    AGB_CUDA(cudaMemcpyAsync(host_out, dn->net.params(), dn->net.nParams() * 4, cudaMemcpyDeviceToHost, dn->stream),
+        "read parameters");
+    AGB_CUDA(cudaStreamSynchronize(dn->stream), "read parameters");
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_denoiser_set_params(agb_denoiser* dn, const float* host, uint64_t count)
+{
+    if (!dn || !host || count != dn->net.nParams())
+        return fail(AGB_ERR_INVALID_ARG, "agb_denoiser_set_params: null argument or wrong count");
+    AGB_CUDA(cudaSetDevice(dn->device), "cudaSetDevice");
+    AGB_CUDA(dn->net.setParams(host), "agb_denoiser_set_params");
+    AGB_CUDA(cudaStreamSynchronize(dn->stream), "agb_denoiser_set_params");
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_denoiser_grads(agb_denoiser* dn, float* host_out, uint64_t count)
+{
+    if (!dn || !host_out || count < dn->net.nParams())
+        return fail(AGB_ERR_INVALID_ARG, "agb_denoiser_grads: null argument or output too small");
+    AGB_CUDA(cudaSetDevice(dn->device), "cudaSetDevice");
+    AGB_CUDA(cudaMemcpyAsync(host_out, dn->net.grads(), dn->net.nParams() * 4, cudaMemcpyDeviceToHost, dn->stream),
+        "read gradients");
+    AGB_CUDA(cudaStreamSynchronize(dn->stream), "read gradients");
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_denoiser_forward(agb_denoiser* dn, const uint16_t* features, int32_t batch,
+    int32_t height, int32_t width, float* out_rgba)
+{
+    agb_status st = denoiserCheck(dn, batch, height, width, "agb_denoiser_forward");
+    if (st)
+        return st;
+    if (!features || !out_rgba || ((reinterpret_cast<uintptr_t>(features) | reinterpret_cast<uintptr_t>(out_rgba)) & 15u))
+        return fail(AGB_ERR_INVALID_ARG, "agb_denoiser_forward: null or unaligned device pointer");
+    AGB_CUDA(dn->net.forward(features, batch, height, width, false), "agb_denoiser_forward");
+    AGB_CUDA(dn->net.toRadiance(out_rgba), "agb_denoiser_forward");
+    AGB_CUDA(cudaStreamSynchronize(dn->stream), "agb_denoiser_forward");
+    return tcStatus("agb_denoiser_forward");
+}
+
+AGB_API agb_status agb_denoiser_train_step(agb_denoiser* dn, const uint16_t* features,
+    const float* target_rgba, int32_t batch, int32_t height, int32_t width, float learning_rate,
+    int32_t update, float* loss)
+{
+    agb_status st = denoiserCheck(dn, batch, height, width, "agb_denoiser_train_step");
+    if (st)
+        return st;
+    if (!features || !target_rgba || ((reinterpret_cast<uintptr_t>(features) | reinterpret_cast<uintptr_t>(target_rgba)) & 15u))
+        return fail(AGB_ERR_INVALID_ARG, "agb_denoiser_train_step: null or unaligned device pointer");
+    if (!(learning_rate >= 0.f))
+        return fail(AGB_ERR_INVALID_ARG, "agb_denoiser_train_step: learning rate must be >= 0");
+    AGB_CUDA(dn->net.forward(features, batch, height, width, true), "agb_denoiser_train_step");
+    AGB_CUDA(dn->net.backward(target_rgba), "agb_denoiser_train_step");
+    if (update)
+        AGB_CUDA(dn->net.adam(learning_rate), "agb_denoiser_train_step");
+    float l = 0.f;
+    AGB_CUDA(cudaMemcpyAsync(&l, dn->net.lossDevice(), 4, cudaMemcpyDeviceToHost, dn->stream), "read loss");
+    AGB_CUDA(cudaStreamSynchronize(dn->stream), "agb_denoiser_train_step");
+    if (loss)
+        *loss = l;
+    return tcStatus("agb_denoiser_train_step");
+}
+
+AGB_API agb_status agb_denoiser_features(agb_context* ctx, uint16_t* out_features)
+{
+    if (!ctx || !out_features || (reinterpret_cast<uintptr_t>(out_features) & 15u))
+        return fail(AGB_ERR_INVALID_ARG, "agb_denoiser_features: null or unaligned argument");
+    if (!ctx->accMean.ptr || !ctx->aovValid || !(ctx->lastAccumMode & AGB_ACCUM_RUNNING_MEAN))
+        return fail(AGB_ERR_NOT_READY, "agb_denoiser_features: needs a running-mean render with the denoising "
+                                       "AOVs enabled");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    long P = long(ctx->accW) * ctx->accH;
+    const float2* mom = (ctx->lastAccumMode & AGB_ACCUM_MOMENTS) ? ctx->accMoments.as<float2>() : nullptr;
+    AGB_CUDA(launchDenoiseFeatures(ctx->accMean.as<float4>(), mom, float(ctx->accumulatedSamples),
+                 ctx->aovAlbedo.as<float4>(), ctx->aovNormal.as<float4>(), ctx->aovDepth.as<float>(),
+                 ctx->frame.sky_view_z, P, out_features, ctx->stream),
+        "agb_denoiser_features");
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "agb_denoiser_features");
     return AGB_OK;
 }
 

@@ -158,6 +158,62 @@ cudaError_t launchTcGemm(const uint16_t* A, const uint16_t* B, float* D, int M, 
 // Reads and clears the tensor-core kernels' timeout flag (1 = a bounded wait ran out).
 cudaError_t takeTcError(int* flag);
 
+// agb_unet.cu: the U-Net denoiser (layer graph, training state, elementwise kernels).
+class UnetDenoiser
+{
+public:
+    static constexpr int kLayers = 15;
+    static constexpr int kActs   = 18;
+    ~UnetDenoiser();
+    cudaError_t init(uint64_t seed, cudaStream_t st, int smCount);
+    static size_t paramCount();
+    // x: [B][H][W][16] BF16 features (H, W multiples of 8).  Keeps the activations for backward.
+    cudaError_t forward(const uint16_t* x, int B, int H, int W, bool training);
+    // After forward(training): L1 loss against target RGBA (FP32) and all parameter gradients.
+    cudaError_t backward(const float* target);
+    cudaError_t adam(float lr);
+    cudaError_t toRadiance(float* rgba);
+    cudaError_t setParams(const float* host);
+    const float* params() const { return params_; }
+    const float* grads() const { return grads_; }
+    const float* lossDevice() const { return loss_; }
+    size_t nParams() const { return nParams_; }
+    static double flopsPerPixel(bool training);
+    void release();
+
+private:
+    cudaError_t alloc(void** p, size_t bytes, std::vector<void*>& list);
+    cudaError_t repack();
+    cudaError_t ensureShape(int B, int H, int W, bool training);
+    static size_t pixels(int B, int H, int W, int level);
+    ConvLaunch layerLaunch(int i, const uint16_t* x) const;
+    cudaError_t pool(int src, int dst);
+
+    cudaStream_t stream_ = nullptr;
+    int smCount_         = 0;
+    size_t nParams_      = 0;
+    float* params_ = nullptr;
+    float* grads_  = nullptr;
+    float* adamM_  = nullptr;
+    float* adamV_  = nullptr;
+    float* loss_   = nullptr;
+    uint16_t* pack_     = nullptr;
+    uint16_t* packFlip_ = nullptr;
+    size_t wOff_[kLayers] = {}, bOff_[kLayers] = {}, packOff_[kLayers] = {};
+    uint16_t* act_[kActs] = {};
+    float* grad_[kActs]   = {};
+    float* out32_ = nullptr;
+    float* gOut_  = nullptr;
+    float* dx32_  = nullptr;
+    uint16_t* dpre_        = nullptr;
+    const uint16_t* input_ = nullptr;
+    int B_ = 0, H_ = 0, W_ = 0;
+    long step_ = 0;
+    std::vector<void*> allocs_, shapeAllocs_;
+};
+cudaError_t launchDenoiseFeatures(const float4* mean, const float2* moments, float samples, const float4* albedo,
+    const float4* normal, const float* depth, float skyZ, long P, uint16_t* out, cudaStream_t st);
+
 // agb_unit.cu
 cudaError_t launchBsdfBatch(int op, const agb_material* mats, const int32_t* matIndex,
     const float* frames, const float* V, const float* L, const float* rnd, int64_t n,

@@ -673,6 +673,9 @@ __global__ void k_finalize(agb_frame_data f, WaveParams wp, WaveBuffers wb)
             comp = wb.accumComp[pixel];
         }
         float4 res = mean;
+        float2 mom = make_float2(0.f, 0.f);
+        if ((wp.accumMode & AGB_ACCUM_MOMENTS) && wp.sampleBase > 0)
+            mom = wb.accumMoments[pixel];
         for (uint32_t k = 0; k < wp.samples; k++)
         {
             uint32_t p = k * wp.pixels + pixel;
@@ -681,6 +684,11 @@ __global__ void k_finalize(agb_frame_data f, WaveParams wp, WaveBuffers wb)
             adjustRadiance(f.max_luminance, f.is_display_errors_enabled != 0, fin);
             res = make_float4(fin.x, fin.y, fin.z, (wb.flags[p] & PF_ALPHA) ? 1.f : 0.f);
             uint32_t s = wp.sampleBase + k;
+            if (wp.accumMode & AGB_ACCUM_MOMENTS)
+            {
+                float l = luminance(fin);
+                mom     = make_float2(mom.x + l, mom.y + l * l);
+            }
             if (wp.accumMode & AGB_ACCUM_RUNNING_MEAN)
             {
                 if (s == 0)
@@ -711,6 +719,8 @@ __global__ void k_finalize(agb_frame_data f, WaveParams wp, WaveBuffers wb)
                 }
             }
         }
+        if (wp.accumMode & AGB_ACCUM_MOMENTS)
+            wb.accumMoments[pixel] = mom;
         if (wp.accumMode & AGB_ACCUM_RUNNING_MEAN)
             wb.accumMean[pixel] = mean;
         if (wp.accumMode & AGB_ACCUM_KAHAN)

@@ -83,6 +83,7 @@ struct WaveBuffers
     float4* accumSum;
     float4* accumComp;
     float4* lastSample;
+    float2* accumMoments; // sum of luminance, sum of luminance^2
     unsigned long long* stats; // [closest rays, shadow rays, nodes, tris, overflow]
     // Denoising AOVs (per pixel), written for one sample index (WaveParams::aovSample).
     float* aovDepth;     // view-space depth

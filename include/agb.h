@@ -252,7 +252,10 @@ enum
     /* FP32 running mean mix(prev, cur, 1/(n+1)) (HGI/Shaders/Accumulation.glsl:22-30). */
     AGB_ACCUM_RUNNING_MEAN = 1,
     /* FP32 Kahan-compensated sum and sample count; resolve divides. */
-    AGB_ACCUM_KAHAN = 2
+    AGB_ACCUM_KAHAN = 2,
+    /* Per-pixel sum of sample luminance and of its square (FP32), for the denoiser's variance
+     * feature. */
+    AGB_ACCUM_MOMENTS = 4
 };
 
 /* Render options beyond FrameData. */
@@ -474,6 +477,45 @@ AGB_API agb_status agb_conv3x3_wgrad_bf16(const uint16_t* in0, const uint16_t* i
  * with cin channels).  out holds 9 * cin * cout BF16 values. */
 AGB_API agb_status agb_pack_conv_weights(const float* w, int32_t cin, int32_t cout, int32_t flip,
     uint16_t* out, void* cuda_stream);
+/* ------------------------------------------------------------------------------------------ */
+/* Learned denoiser (no counterpart in the reference, whose denoiser is NVIDIA NRD): a 4-level     */
+/* U-Net on the tensor cores, trained on the renderer's own low / high sample-count pairs.        */
+/* ------------------------------------------------------------------------------------------ */
+/* Layers (3x3 convolutions, ReLU except the last), in parameter order, with (input channels ->
+ * output channels) at resolution 1 / 2^level:
+ *   0 x(16)->32 L0   1 32->32 L0   [2x2 average pool]   2 32->64 L1   3 64->64 L1   [pool]
+ *   4 64->128 L2     5 128->128 L2 [pool]                6 128->256 L3 7 256->256 L3
+ *   8 up(7)(256) + skip(5)(128) -> 128 L2   9 128->128 L2
+ *  10 up(9)(128) + skip(3)(64) -> 64 L1    11 64->64 L1
+ *  12 up(11)(64) + skip(1)(32) -> 32 L0    13 32->32 L0
+ *  14 32->16 L0 (no ReLU; channels 0-2 are added to the log1p noisy input: the prediction of
+ *     log1p(radiance))
+ * Parameters: for each layer, w[9][cin][cout] (tap = 3 * (dy + 1) + (dx + 1)) then b[cout], FP32.
+ * Features (16 BF16 channels per pixel, NHWC): log1p(noisy RGB), base colour, octahedral normal,
+ * view depth / sky depth, log1p(luminance variance), 6 zeros.  Height and width multiples of 8. */
+typedef struct agb_denoiser agb_denoiser;
+AGB_API agb_status agb_denoiser_create(int32_t device, void* cuda_stream, uint64_t seed,
+    agb_denoiser** out);
+AGB_API agb_status agb_denoiser_destroy(agb_denoiser* dn);
+AGB_API agb_status agb_denoiser_param_count(uint64_t* count);
+AGB_API agb_status agb_denoiser_params(agb_denoiser* dn, float* host_out, uint64_t count);
+AGB_API agb_status agb_denoiser_set_params(agb_denoiser* dn, const float* host, uint64_t count);
+/* Gradients of the last training step (same layout as the parameters). */
+AGB_API agb_status agb_denoiser_grads(agb_denoiser* dn, float* host_out, uint64_t count);
+/* Inference on device features [batch][height][width][16]; writes the denoised RGBA radiance
+ * (device, batch*height*width float4). */
+AGB_API agb_status agb_denoiser_forward(agb_denoiser* dn, const uint16_t* features, int32_t batch,
+    int32_t height, int32_t width, float* out_rgba);
+/* One training step on a batch: forward, L1 loss on log1p radiance against target_rgba (device,
+ * float4 per pixel), backward; update != 0 then applies Adam (beta 0.9 / 0.999, eps 1e-8) with the
+ * learning rate.  *loss receives the mean L1 loss. */
+AGB_API agb_status agb_denoiser_train_step(agb_denoiser* dn, const uint16_t* features,
+    const float* target_rgba, int32_t batch, int32_t height, int32_t width, float learning_rate,
+    int32_t update, float* loss);
+/* The 16 feature channels of the context's last render (running mean; the frame must have had
+ * is_denoising_aovs_enabled; the variance channel needs AGB_ACCUM_MOMENTS, else 0) into device
+ * memory (width*height*16 BF16). */
+AGB_API agb_status agb_denoiser_features(agb_context* ctx, uint16_t* out_features);
 /* Halton (2, 3) camera jitter in pixels, centred on [-0.5, 0.5] (PTRenderer.cpp:81-95,159-174):
  * index = (phase_count ? frame_index % phase_count : frame_index) + 1. */
 AGB_API void agb_temporal_jitter(uint32_t frame_index, uint32_t phase_count, float out[2]);

@@ -82,3 +82,112 @@ def avgpool2(x):
 
 def avgpool2_grad(d):
     return upsample2(d) * 0.25
+
+
+# ----------------------------------------------------------------------------- the U-Net
+# Activations: name -> (level, channels); layers: (in0, in1, out, up0, relu, level) in parameter
+# order, as the product's agb_unet.cu defines them.
+ACTS = {"x": (0, 16), "e0a": (0, 32), "s0": (0, 32), "p0": (1, 32), "e1a": (1, 64), "s1": (1, 64),
+        "p1": (2, 64), "e2a": (2, 128), "s2": (2, 128), "p2": (3, 128), "ba": (3, 256),
+        "bb": (3, 256), "d2a": (2, 128), "d2": (2, 128), "d1a": (1, 64), "d1": (1, 64),
+        "d0a": (0, 32), "d0": (0, 32)}
+LAYERS = [("x", None, "e0a", 0, 1, 0), ("e0a", None, "s0", 0, 1, 0),
+          ("p0", None, "e1a", 0, 1, 1), ("e1a", None, "s1", 0, 1, 1),
+          ("p1", None, "e2a", 0, 1, 2), ("e2a", None, "s2", 0, 1, 2),
+          ("p2", None, "ba", 0, 1, 3), ("ba", None, "bb", 0, 1, 3),
+          ("bb", "s2", "d2a", 1, 1, 2), ("d2a", None, "d2", 0, 1, 2),
+          ("d2", "s1", "d1a", 1, 1, 1), ("d1a", None, "d1", 0, 1, 1),
+          ("d1", "s0", "d0a", 1, 1, 0), ("d0a", None, "d0", 0, 1, 0),
+          ("d0", None, None, 0, 0, 0)]
+POOLS = {2: ("s0", "p0"), 4: ("s1", "p1"), 6: ("s2", "p2")}
+
+
+def layer_shapes():
+    out = []
+    for in0, in1, o, _, _, _ in LAYERS:
+        cin = ACTS[in0][1] + (ACTS[in1][1] if in1 else 0)
+        out.append((cin, ACTS[o][1] if o else 16))
+    return out
+
+
+def split_params(flat):
+    """Flat parameter vector -> [(w (9, cin, cout), b (cout,))]."""
+    res, off = [], 0
+    for cin, cout in layer_shapes():
+        w = flat[off:off + 9 * cin * cout].reshape(9, cin, cout)
+        off += 9 * cin * cout
+        b = flat[off:off + cout]
+        off += cout
+        res.append((np.asarray(w, np.float64), np.asarray(b, np.float64)))
+    return res
+
+
+def _layer_input(acts, in0, in1, up0):
+    x = acts[in0]
+    if up0:
+        x = upsample2(x)
+    if in1:
+        x = np.concatenate([x, acts[in1]], axis=3)
+    return x
+
+
+def unet_forward(flat, x, exact=False):
+    """x: (B, H, W, 16) BF16 values as float64.  Returns the activations (BF16-rounded where the
+    device stores them, unless exact) and the output (B, H, W, 16)."""
+    rnd = (lambda v: v) if exact else bf16
+    params = split_params(flat)
+    acts = {"x": x}
+    out = None
+    for i, (in0, in1, o, up0, relu, _) in enumerate(LAYERS):
+        if i in POOLS:
+            s, p = POOLS[i]
+            acts[p] = rnd(avgpool2(acts[s]))
+        w, b = params[i]
+        y = conv3x3(_layer_input(acts, in0, in1, up0), bf16(w), b)
+        if relu:
+            y = np.maximum(y, 0.0)
+        if o:
+            acts[o] = rnd(y)
+        else:
+            out = y
+    return acts, out
+
+
+def unet_loss_backward(flat, acts, out, target, exact=False):
+    """L1 loss on log1p radiance (prediction = out[..., :3] + x[..., :3]) and the parameter
+    gradients (flat, same layout), with the device's BF16 rounding of the per-layer gradients
+    (unless exact)."""
+    rnd = (lambda v: v) if exact else bf16
+    params = split_params(flat)
+    x = acts["x"]
+    B, H, W, _ = x.shape
+    n = B * H * W * 3
+    pred = out[..., :3] + x[..., :3]
+    t = np.log1p(np.maximum(target[..., :3], 0.0))
+    d = pred - t
+    loss = np.abs(d).sum() / n
+    g_out = np.zeros_like(out)
+    g_out[..., :3] = np.sign(d) / n
+    grads = {k: np.zeros_like(v) for k, v in acts.items() if k != "x"}
+    flat_grads = []
+    for i in range(len(LAYERS) - 1, -1, -1):
+        in0, in1, o, up0, relu, _ = LAYERS[i]
+        w, b = params[i]
+        gy = grads[o] if o else g_out
+        dpre = rnd(gy * (acts[o] > 0) if relu else gy)
+        xin = _layer_input(acts, in0, in1, up0)
+        dw, db = conv3x3_weight_grad(xin, dpre)
+        flat_grads.append((i, dw, db))
+        if i > 0:
+            dx = conv3x3_data_grad(dpre, bf16(w))
+            c0 = ACTS[in0][1]
+            g0 = dx[..., :c0]
+            grads[in0] += upsample2_grad(g0) if up0 else g0
+            if in1:
+                grads[in1] += dx[..., c0:]
+        if i in POOLS:
+            s, p = POOLS[i]
+            grads[s] += avgpool2_grad(grads[p])
+    flat_grads.sort(key=lambda t: t[0])
+    g = np.concatenate([np.concatenate([dw.reshape(-1), db]) for _, dw, db in flat_grads])
+    return loss, g
