@@ -17,6 +17,7 @@ AGB_OK = 0
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "timeout",
           -5: "not ready", -6: "limit exceeded"}
 ERR_LIMIT = -6
+ERR_INVALID_ARG, ERR_CUDA, ERR_OOM, ERR_TIMEOUT, ERR_NOT_READY = -1, -2, -3, -4, -5
 
 ACCUM_RUNNING_MEAN = 1
 ACCUM_KAHAN = 2
@@ -136,6 +137,19 @@ class TemporalSettings(ctypes.Structure):
 
 
 POST_SOURCE_TEMPORAL = 4
+SERVE_DENOISE = 1
+
+
+class ServeRequest(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_int32), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("spp", ctypes.c_uint32), ("seed_offset", ctypes.c_uint32), ("flags", ctypes.c_int32),
+                ("_pad", ctypes.c_uint32 * 2), ("frame", ctypes.c_uint8 * 512)]
+
+
+class ServeResult(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_uint64), ("status", ctypes.c_int32), ("width", ctypes.c_uint32),
+                ("height", ctypes.c_uint32), ("_pad", ctypes.c_int32), ("queue_ms", ctypes.c_double),
+                ("render_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
 
 # Every symbol include/agb.h declares, with its ctypes signature.
 _P = ctypes.c_void_p
@@ -148,6 +162,15 @@ SIGNATURES = {
     "agb_context_destroy": (_I32, [_P]),
     "agb_last_error": (ctypes.c_char_p, []),
     "agb_context_memory": (_I32, [_P, ctypes.POINTER(_U64)]),
+    "agb_view_create": (_I32, [_P, _P, ctypes.POINTER(_P)]),
+    "agb_wait_poll": (_I32, [_P]),
+    "agb_server_create": (_I32, [_I32, _U64, _I32, ctypes.POINTER(_P)]),
+    "agb_server_destroy": (_I32, [_P]),
+    "agb_server_add_scene": (_I32, [_P, _I32, _P]),
+    "agb_server_set_denoiser": (_I32, [_P, _P]),
+    "agb_server_submit": (_I32, [_P, ctypes.POINTER(ServeRequest), ctypes.POINTER(_U64)]),
+    "agb_server_wait": (_I32, [_P, _U64, _I32, ctypes.POINTER(ServeResult), _P, _U64]),
+    "agb_server_memory": (_I32, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
     "agb_set_counting": (_I32, [_P, _I32]),
     "agb_set_profiling": (_I32, [_P, _I32]),
     "agb_geometry_create": (_I32, [_P, _P, _P, _P, _P, _U32, _U32, ctypes.POINTER(_I32)]),

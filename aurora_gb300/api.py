@@ -207,6 +207,66 @@ def bsdf_batch(op, mats_ptr, idx_ptr, frames_ptr, v_ptr, l_ptr, rnd_ptr, n, out_
                                    vp(out_pdf), vp(out_lobe), stream))
 
 
+class Server:
+    """The serving loop (agb_server_*): register uploaded Renderers as scenes, submit requests,
+    wait for their images and latencies."""
+
+    def __init__(self, hbm_budget_bytes, max_slots=4, device=0):
+        self._lib = _abi.library()
+        self.handle = ctypes.c_void_p()
+        check(self._lib.agb_server_create(device, int(hbm_budget_bytes), max_slots,
+                                          ctypes.byref(self.handle)))
+        self._scenes = {}
+
+    def close(self):
+        if self.handle:
+            self._lib.agb_server_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def add_scene(self, scene_id, renderer):
+        """Registers an uploaded Renderer; returns the agb status (AGB_ERR_OOM beyond the budget)."""
+        st = self._lib.agb_server_add_scene(self.handle, scene_id, renderer.ctx)
+        if st == _abi.AGB_OK:
+            self._scenes[scene_id] = renderer
+        return st
+
+    def set_denoiser(self, handle):
+        check(self._lib.agb_server_set_denoiser(self.handle, handle))
+
+    def submit(self, scene_id, frame, width, height, spp, seed_offset=0, denoise=False):
+        r = _abi.ServeRequest()
+        r.scene, r.width, r.height, r.spp = scene_id, width, height, spp
+        r.seed_offset = seed_offset
+        r.flags = _abi.SERVE_DENOISE if denoise else 0
+        f = np.ascontiguousarray(np.asarray(frame, dtype=_abi.FRAME_DTYPE).reshape(1))
+        ctypes.memmove(r.frame, f.ctypes.data, 512)
+        rid = ctypes.c_uint64()
+        check(self._lib.agb_server_submit(self.handle, ctypes.byref(r), ctypes.byref(rid)))
+        return rid.value, (width, height)
+
+    def wait(self, ticket, timeout_ms=-1):
+        """(status, image (H, W, 4) or None, result dict)."""
+        rid, (w, h) = ticket
+        img = np.empty((h, w, 4), np.float32)
+        res = _abi.ServeResult()
+        st = self._lib.agb_server_wait(self.handle, rid, timeout_ms, ctypes.byref(res), ptr(img),
+                                       img.size)
+        info = dict(status=res.status, queue_ms=res.queue_ms, render_ms=res.render_ms,
+                    latency_ms=res.latency_ms)
+        return st, (img if st == _abi.AGB_OK else None), info
+
+    def memory(self):
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        check(self._lib.agb_server_memory(self.handle, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+
 def temporal_jitter(frame_index, phase_count=0):
     """Halton (2, 3) camera jitter in pixels for a frame (PTRenderer.cpp:159-174)."""
     out = (ctypes.c_float * 2)()

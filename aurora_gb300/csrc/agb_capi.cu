@@ -98,6 +98,10 @@ struct Image
 
 struct agb_context
 {
+    // A view (agb_view_create) renders its parent's scene with its own stream, frame and render
+    // buffers; it holds no scene data of its own.
+    agb_context* parent = nullptr;
+    int viewCount       = 0;
     int device          = 0;
     cudaStream_t stream = nullptr;
     bool ownsStream     = false;
@@ -163,6 +167,8 @@ struct agb_context
 
     DevScene scene() const
     {
+        if (parent)
+            return parent->scene();
         DevScene s{};
         s.meshes        = meshTable.as<DevMesh>();
         s.instances     = instances.as<DevInstance>();
@@ -351,9 +357,40 @@ AGB_API agb_status agb_context_destroy(agb_context* ctx)
 {
     if (!ctx)
         return AGB_OK;
+    if (ctx->viewCount > 0)
+        return fail(AGB_ERR_INVALID_ARG, "agb_context_destroy: destroy the context's views first");
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    if (ctx->parent)
+        ctx->parent->viewCount--;
     delete ctx;
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_view_create(agb_context* ctx, void* cuda_stream, agb_context** out)
+{
+    if (!ctx || !out)
+        return fail(AGB_ERR_INVALID_ARG, "agb_view_create: null argument");
+    if (ctx->parent)
+        return fail(AGB_ERR_INVALID_ARG, "agb_view_create: a view cannot have views");
+    *out = nullptr;
+    std::unique_ptr<agb_context> v(new agb_context());
+    v->parent  = ctx;
+    v->device  = ctx->device;
+    v->smCount = ctx->smCount;
+    v->envLayout = ctx->envLayout;
+    AGB_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    if (cuda_stream)
+        v->stream = static_cast<cudaStream_t>(cuda_stream);
+    else
+    {
+        AGB_CUDA(cudaStreamCreateWithFlags(&v->stream, cudaStreamNonBlocking), "create stream");
+        v->ownsStream = true;
+    }
+    AGB_CUDA(cudaEventCreate(&v->ev0), "create event");
+    AGB_CUDA(cudaEventCreate(&v->ev1), "create event");
+    ctx->viewCount++;
+    *out = v.release();
     return AGB_OK;
 }
 
@@ -365,7 +402,9 @@ AGB_API agb_status agb_context_memory(agb_context* ctx, uint64_t* bytes)
         ctx->matTex.bytes + ctx->instances.bytes + ctx->tlasNodes.bytes + ctx->tlasOrder.bytes +
         ctx->layers.bytes + ctx->alias.bytes + ctx->pathState.bytes + ctx->queues.bytes +
         ctx->counters.bytes + ctx->accMean.bytes + ctx->accSum.bytes + ctx->accComp.bytes +
-        ctx->lastSample.bytes;
+        ctx->lastSample.bytes + ctx->accMoments.bytes + ctx->aovDepth.bytes + ctx->aovNormal.bytes +
+        ctx->aovAlbedo.bytes + ctx->aovMotion.bytes + ctx->taaHistory[0].bytes + ctx->taaHistory[1].bytes +
+        uint64_t(ctx->envScratch.capacity) * 44 + ctx->stats.bytes;
     for (auto& g : ctx->geometries)
         b += g->positions.bytes + g->normals.bytes + g->texcoords.bytes + g->indices.bytes +
             g->tris.bytes + g->nodes.bytes;
@@ -397,6 +436,8 @@ AGB_API agb_status agb_geometry_create(agb_context* ctx, const float* positions,
     const float* normals, const float* texcoords, const uint32_t* indices, uint32_t vertex_count,
     uint32_t index_count, int32_t* out_geometry)
 {
+    if (ctx && ctx->parent)
+        return fail(AGB_ERR_INVALID_ARG, "agb_geometry_create: a view shares its parent's scene; change the parent");
     if (!ctx || !positions || !out_geometry)
         return fail(AGB_ERR_INVALID_ARG, "agb_geometry_create: null argument");
     if (vertex_count == 0 || index_count == 0 || index_count % 3 != 0)
@@ -505,6 +546,8 @@ AGB_API agb_status agb_geometry_create(agb_context* ctx, const float* positions,
 AGB_API agb_status agb_image_create(agb_context* ctx, const void* pixels, uint32_t width,
     uint32_t height, int32_t format, int32_t linear, int32_t* out_image)
 {
+    if (ctx && ctx->parent)
+        return fail(AGB_ERR_INVALID_ARG, "agb_image_create: a view shares its parent's scene; change the parent");
     if (!ctx || !pixels || !out_image || width == 0 || height == 0)
         return fail(AGB_ERR_INVALID_ARG, "agb_image_create: invalid argument");
     if (format != AGB_FORMAT_RGBA8_UNORM && format != AGB_FORMAT_RGBA32F && format != AGB_FORMAT_RGB32F)
@@ -550,6 +593,8 @@ AGB_API agb_status agb_image_create(agb_context* ctx, const void* pixels, uint32
 AGB_API agb_status agb_materials_set(agb_context* ctx, const agb_material* materials,
     const agb_material_textures* textures, uint32_t count)
 {
+    if (ctx && ctx->parent)
+        return fail(AGB_ERR_INVALID_ARG, "agb_materials_set: a view shares its parent's scene; change the parent");
     if (!ctx || (!materials && count))
         return fail(AGB_ERR_INVALID_ARG, "agb_materials_set: null argument");
     if (textures)
@@ -572,6 +617,8 @@ AGB_API agb_status agb_materials_set(agb_context* ctx, const agb_material* mater
 
 AGB_API agb_status agb_instances_set(agb_context* ctx, const agb_instance* inst, uint32_t count)
 {
+    if (ctx && ctx->parent)
+        return fail(AGB_ERR_INVALID_ARG, "agb_instances_set: a view shares its parent's scene; change the parent");
     if (!ctx || (!inst && count))
         return fail(AGB_ERR_INVALID_ARG, "agb_instances_set: null argument");
     if (count >= (1u << 27))
@@ -680,6 +727,8 @@ AGB_API agb_status agb_instances_set(agb_context* ctx, const agb_instance* inst,
 AGB_API agb_status agb_environment_set(agb_context* ctx, const agb_environment_data* env,
     int32_t light_image, int32_t background_image)
 {
+    if (ctx && ctx->parent)
+        return fail(AGB_ERR_INVALID_ARG, "agb_environment_set: a view shares its parent's scene; change the parent");
     if (!ctx || !env)
         return fail(AGB_ERR_INVALID_ARG, "agb_environment_set: null argument");
     if (light_image >= int32_t(ctx->images.size()) || background_image >= int32_t(ctx->images.size()))
@@ -730,6 +779,8 @@ AGB_API agb_status agb_environment_set(agb_context* ctx, const agb_environment_d
 
 AGB_API agb_status agb_set_environment_table(agb_context* ctx, int32_t layout)
 {
+    if (ctx && ctx->parent)
+        return fail(AGB_ERR_INVALID_ARG, "agb_set_environment_table: a view shares its parent's scene; change the parent");
     if (!ctx || (layout != AGB_ENV_TABLE_REFERENCE && layout != AGB_ENV_TABLE_FP64))
         return fail(AGB_ERR_INVALID_ARG, "agb_set_environment_table: bad layout");
     ctx->envLayout = layout;
@@ -813,7 +864,8 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
         return fail(AGB_ERR_NOT_READY, "agb_render: frame data not set");
     if (opt->width == 0 || opt->height == 0 || uint64_t(opt->width) * opt->height > (1ull << 26))
         return fail(AGB_ERR_INVALID_ARG, "agb_render: bad image size");
-    if (ctx->instanceCount > 0 && ctx->materialCount == 0)
+    const agb_context* sc = ctx->parent ? ctx->parent : ctx;
+    if (sc->instanceCount > 0 && sc->materialCount == 0)
         return fail(AGB_ERR_NOT_READY, "agb_render: no materials");
     agb_status st = setDevice(ctx);
     if (st)
@@ -930,6 +982,18 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
         *stats   = r;
     }
     return AGB_OK;
+}
+
+AGB_API agb_status agb_wait_poll(agb_context* ctx)
+{
+    if (!ctx)
+        return AGB_ERR_INVALID_ARG;
+    cudaError_t e = cudaStreamQuery(ctx->stream);
+    if (e == cudaSuccess)
+        return AGB_OK;
+    if (e == cudaErrorNotReady)
+        return AGB_ERR_NOT_READY;
+    return cudaFail(e, "agb_wait_poll");
 }
 
 AGB_API agb_status agb_wait(agb_context* ctx)

@@ -305,6 +305,13 @@ AGB_API agb_status agb_context_destroy(agb_context* ctx);
 AGB_API const char* agb_last_error(void);
 /* Bytes of device memory the context holds. */
 AGB_API agb_status agb_context_memory(agb_context* ctx, uint64_t* bytes);
+/* A view renders the scene of ctx with its own stream (null: a new one), frame data and render
+ * buffers (accumulation, AOVs, temporal history): several views of one resident scene render
+ * concurrently.  Every render-side call (agb_frame_set, agb_render, agb_accum_read, ...) takes a
+ * view in place of a context; scene calls on a view fail.  Views must be destroyed (with
+ * agb_context_destroy) before their context.  No counterpart in the reference (its renderer owns
+ * one render target set per scene); the serving loop uses it. */
+AGB_API agb_status agb_view_create(agb_context* ctx, void* cuda_stream, agb_context** out);
 /* Enables device-side counting of node visits / triangle tests (for the roofline). */
 AGB_API agb_status agb_set_counting(agb_context* ctx, int32_t enabled);
 /* Enables per-kernel-family device timing with CUDA events (agb_render_stats::kernel_ms). */
@@ -398,6 +405,9 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* option
     uint32_t sample_start, uint32_t sample_count, agb_render_stats* stats);
 
 /* Waits for the context stream (IRenderer::waitForTask, Aurora.h:1199). */
+/* AGB_OK when all work queued on the context (or view) has finished, AGB_ERR_NOT_READY while some
+ * is still running; never blocks. */
+AGB_API agb_status agb_wait_poll(agb_context* ctx);
 AGB_API agb_status agb_wait(agb_context* ctx);
 
 /* Copies the accumulated image to the host as RGBA32F (IRenderBuffer::data, HGIRenderBuffer.cpp).
@@ -516,6 +526,59 @@ AGB_API agb_status agb_denoiser_train_step(agb_denoiser* dn, const uint16_t* fea
  * is_denoising_aovs_enabled; the variance channel needs AGB_ACCUM_MOMENTS, else 0) into device
  * memory (width*height*16 BF16). */
 AGB_API agb_status agb_denoiser_features(agb_context* ctx, uint16_t* out_features);
+/* ------------------------------------------------------------------------------------------ */
+/* Serving loop (no counterpart in the reference, whose progressive driver renders one view at a  */
+/* time: Foundation/API/Aurora/Foundation/Timer.h:97-140, HdAuroraRenderPass.cpp:194-208).         */
+/* ------------------------------------------------------------------------------------------ */
+/* A persistent scheduler thread admits render requests of registered scenes as slots and HBM
+ * budget free up (continuous batching: requests arriving while others render are admitted at
+ * once), renders each through a pooled view of its scene on its own stream so requests overlap on
+ * the device, and records queueing, rendering and total latency.  Scenes are contexts uploaded by
+ * the caller, admitted by their HBM footprint (agb_server_add_scene fails with AGB_ERR_OOM beyond
+ * the budget); a request reserves its render memory before it starts, and one that cannot fit even
+ * with nothing else running fails with AGB_ERR_OOM.  The result is the running mean (RGBA32F) of
+ * the request's samples, or the denoised image when AGB_SERVE_DENOISE is set and a denoiser is
+ * attached (width and height multiples of 8).  Scenes must not change while the server runs;
+ * these calls return status codes only. */
+typedef struct agb_server agb_server;
+enum
+{
+    AGB_SERVE_DENOISE = 1
+};
+typedef struct agb_serve_request
+{
+    int32_t scene;
+    uint32_t width;
+    uint32_t height;
+    uint32_t spp;
+    uint32_t seed_offset;
+    int32_t flags;
+    uint32_t _pad[2];
+    agb_frame_data frame;
+} agb_serve_request;
+typedef struct agb_serve_result
+{
+    uint64_t id;
+    agb_status status;
+    uint32_t width;
+    uint32_t height;
+    int32_t _pad;
+    double queue_ms;   /* submit -> start */
+    double render_ms;  /* start -> result on the host */
+    double latency_ms; /* submit -> result on the host */
+} agb_serve_result;
+AGB_API agb_status agb_server_create(int32_t device, uint64_t hbm_budget_bytes, int32_t max_slots,
+    agb_server** out);
+AGB_API agb_status agb_server_destroy(agb_server* srv);
+AGB_API agb_status agb_server_add_scene(agb_server* srv, int32_t scene_id, agb_context* ctx);
+AGB_API agb_status agb_server_set_denoiser(agb_server* srv, agb_denoiser* dn);
+AGB_API agb_status agb_server_submit(agb_server* srv, const agb_serve_request* req, uint64_t* id);
+/* Waits (timeout_ms < 0: without limit) for a request; fills result and copies its RGBA32F image
+ * to host_rgba (may be null).  AGB_ERR_TIMEOUT when it did not finish in time (wait again); a
+ * finished request is forgotten after this call. */
+AGB_API agb_status agb_server_wait(agb_server* srv, uint64_t id, int32_t timeout_ms,
+    agb_serve_result* result, float* host_rgba, uint64_t capacity);
+AGB_API agb_status agb_server_memory(agb_server* srv, uint64_t* scene_bytes, uint64_t* render_bytes);
 /* Halton (2, 3) camera jitter in pixels, centred on [-0.5, 0.5] (PTRenderer.cpp:81-95,159-174):
  * index = (phase_count ? frame_index % phase_count : frame_index) + 1. */
 AGB_API void agb_temporal_jitter(uint32_t frame_index, uint32_t phase_count, float out[2]);
