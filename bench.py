@@ -47,7 +47,123 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--res", default=None, help="WxH override (profiling runs)")
     p.add_argument("--spp", type=int, default=None, help="samples per pixel override (profiling runs)")
+    p.add_argument("--no-denoiser", action="store_true", help="skip the denoiser measurement")
+    p.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    p.add_argument("--serve-requests", type=int, default=160)
     return p.parse_args()
+
+
+def denoiser_flops_per_pixel(training=False):
+    """2 x 9 x cin x cout per 3x3 convolution, per output pixel of its level, summed over the
+    U-Net's 15 layers (x3 for a training step: forward, data gradient, weight gradient)."""
+    layers = [(16, 32, 0), (32, 32, 0), (32, 64, 1), (64, 64, 1), (64, 128, 2), (128, 128, 2),
+              (128, 256, 3), (256, 256, 3), (384, 128, 2), (128, 128, 2), (192, 64, 1),
+              (64, 64, 1), (96, 32, 0), (32, 32, 0), (32, 16, 0)]
+    f = sum(2.0 * 9 * ci * co / 4 ** lv for ci, co, lv in layers)
+    return 3 * f if training else f
+
+
+def bench_denoiser(torch, _abi, stream, peaks):
+    """Tensor-core U-Net: 1920x1080 inference and a 4 x 256^2 training step, CUDA events on the
+    denoiser's stream after warm-up."""
+    import ctypes
+    lib = _abi.library()
+    h = ctypes.c_void_p()
+    _abi.check(lib.agb_denoiser_create(0, ctypes.c_void_p(stream.cuda_stream), 1, ctypes.byref(h)))
+    out = {}
+    try:
+        for tag, (B, H, W), train in (("inference_1080p", (1, 1080, 1920), False),
+                                      ("training_4x256", (4, 256, 256), True)):
+            x = torch.zeros((B, H, W, 16), dtype=torch.int16, device="cuda")
+            x[..., :10] = 0x3F00  # 0.5 in BF16
+            rgba = torch.zeros((B, H, W, 4), dtype=torch.float32, device="cuda")
+            loss = ctypes.c_float()
+            if train:
+                call = lambda: _abi.check(lib.agb_denoiser_train_step(
+                    h, x.data_ptr(), rgba.data_ptr(), B, H, W, 1e-4, 1, ctypes.byref(loss)))
+            else:
+                call = lambda: _abi.check(lib.agb_denoiser_forward(h, x.data_ptr(), B, H, W,
+                                                                   rgba.data_ptr()))
+            for _ in range(3):
+                call()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            n = 10
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(n):
+                call()
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / n
+            tf = denoiser_flops_per_pixel(train) * B * H * W / (ms / 1000.0) / 1e12
+            peak = peaks["bf16_tflops"] if peaks else 1900.0
+            out[tag] = {"ms": ms, "achieved": tf, "peak": peak, "unit": "TFLOP/s",
+                        "frac": tf / peak, "bound": "tensor",
+                        "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst, measured)" if peaks
+                        else "fallback 1.9 PFLOP/s"}
+    finally:
+        lib.agb_denoiser_destroy(h)
+    return out
+
+
+def bench_serving(api, _abi, n_requests, rates=(200.0, 25.0)):
+    """Serving loop on 8 resident scenes (4 of the small type, 4 instanced-icosphere scenes of the
+    large type at reduced size), Poisson arrivals, resolutions {640x360, 1280x720, 1920x1080} x
+    spp {1, 4, 16}, a Halton camera jitter per request, 150 GB HBM budget, 8 slots."""
+    from aurora_gb300 import scenes
+    rs, frames = [], []
+    for k in range(8):
+        if k % 2 == 0:
+            sc = scenes.config_small(seed=k, width=1920, height=1080, spp=1)
+        else:
+            sc = scenes.config_large(seed=k, width=1920, height=1080, spp=1, level=7, instances=16,
+                                     env_size=(512, 256))
+        r = api.Renderer()
+        r.upload(sc)
+        rs.append(r)
+        frames.append(sc.frame)
+    res_choices = [(640, 360), (1280, 720), (1920, 1080)]
+    out = {}
+    try:
+        for rate in rates:
+            rng = np.random.default_rng(7)
+            with api.Server(hbm_budget_bytes=150 << 30, max_slots=8) as srv:
+                for k, r in enumerate(rs):
+                    _abi.check(srv.add_scene(k, r))
+                tickets, paths = [], 0
+                t0 = time.perf_counter()
+                t_next = 0.0
+                for i in range(n_requests):
+                    t_next += rng.exponential(1.0 / rate)
+                    k = int(rng.integers(0, 8))
+                    w, h = res_choices[int(rng.integers(0, 3))]
+                    spp = int(rng.choice([1, 4, 16]))
+                    f = frames[k].copy()
+                    jx, jy = api.temporal_jitter(i)
+                    f["camera_jitter"] = (jx, jy)
+                    f["is_temporal_jitter_enabled"] = 1
+                    delay = t0 + t_next - time.perf_counter()
+                    if delay > 0:
+                        time.sleep(delay)
+                    tickets.append(srv.submit(k, f, w, h, spp, seed_offset=i))
+                    paths += w * h * spp
+                lat, queue = [], []
+                for t in tickets:
+                    st, img, info = srv.wait(t)
+                    _abi.check(st)
+                    lat.append(info["latency_ms"])
+                    queue.append(info["queue_ms"])
+                makespan = time.perf_counter() - t0
+            out[f"offered_{int(rate)}_rps"] = {
+                "requests": n_requests, "p50_latency_ms": float(np.percentile(lat, 50)),
+                "p99_latency_ms": float(np.percentile(lat, 99)),
+                "mean_queue_ms": float(np.mean(queue)), "frames_per_s": n_requests / makespan,
+                "path_samples_per_s": paths / makespan}
+    finally:
+        for r in rs:
+            r.close()
+    return out
 
 
 def dist_env():
@@ -331,6 +447,10 @@ def main():
         "roofline": roofline,
         "clocks": clk,
     }
+    if rank == 0 and not args.no_denoiser:
+        out["denoiser"] = bench_denoiser(torch, _abi, stream, measured_peaks())
+    if rank == 0 and not args.no_serve:
+        out["serving"] = bench_serving(api, _abi, args.serve_requests)
     if rank == 0 and not args.no_cpu_baseline:
         cpu, threads, sample = cpu_render_rate(s, args.cpu_seconds)
         out["cpu_baseline"] = {"value": cpu, "unit": UNIT, "cores": threads, "kind": "port",
