@@ -53,6 +53,17 @@ def parse_args():
     return p.parse_args()
 
 
+def closest_traffic_per_launch():
+    """DRAM bytes per k_trace_closest launch from the committed ncu summary, or None."""
+    try:
+        for line in open(os.path.join(ROOT, "profiles", "trace_closest_dram_per_launch.txt")):
+            if line.startswith("bytes_per_launch"):
+                return int(line.split()[1])
+    except OSError:
+        pass
+    return None
+
+
 def denoiser_flops_per_pixel(training=False):
     """2 x 9 x cin x cout per 3x3 convolution, per output pixel of its level, summed over the
     U-Net's 15 layers (x3 for a training step: forward, data gradient, weight gradient)."""
@@ -417,7 +428,9 @@ def main():
         "bound": "hbm", "kernel": "k_trace_closest (closest-hit BVH2 traversal)",
         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
-        "traffic": None,
+        "traffic": closest_traffic_per_launch(),
+        "traffic_unit": "bytes per launch (DRAM read + write, from the committed ncu capture)",
+        "algorithmic_bytes_per_launch": int(closest_bytes / max(1.0, kernel_count["trace_closest"] / steps)),
         "algorithmic_bytes_per_step": int(closest_bytes),
         "launches_per_step": kernel_count["trace_closest"] / steps,
         "ms_per_step": closest_ms,
