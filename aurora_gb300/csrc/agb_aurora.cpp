@@ -1,0 +1,803 @@
+// Implementation of the Aurora-style C++ interface (include/aurora_gb300.hpp) over the C ABI.
+//
+// The scene keeps Aurora's path-keyed, lazily activated resources (SceneBase.cpp): descriptors and
+// properties are recorded when set, and the first render that needs them pulls geometry and image
+// data through the client's callbacks, uploads them, and calls the completion callbacks so the
+// client may free its buffers (GeometryBase.cpp:94-112).  Frame data follows
+// RendererBase::updateFrameDataGPUStruct (RendererBase.cpp:225-295) and the HGI backend's choices
+// (opaque shadows, HGIRenderer.cpp:491); post-processing follows RendererBase.cpp:297-337.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "agb.h"
+#include "aurora_gb300.hpp"
+
+namespace agb_aurora
+{
+namespace
+{
+
+std::mutex g_logMutex;
+std::function<void(const std::string&)> g_log;
+
+void logError(const std::string& msg)
+{
+    std::lock_guard<std::mutex> g(g_logMutex);
+    if (g_log)
+        g_log(msg);
+    else
+        std::fprintf(stderr, "aurora_gb300: %s\n", msg.c_str());
+}
+
+void check(agb_status st, const std::string& what)
+{
+    if (st != AGB_OK)
+        throw Error(what + ": " + agb_last_error());
+}
+
+template <class T>
+const T* find(const Properties& p, const std::string& name)
+{
+    auto it = p.find(name);
+    return it == p.end() ? nullptr : std::get_if<T>(&it->second);
+}
+
+// glm column-major mat4 -> the 3x4 rows of the matrix (object_to_world).
+void rows3x4(const mat4& m, float out[12])
+{
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 4; c++)
+            out[4 * r + c] = m[4 * c + r];
+}
+
+// Row-major copy (the bytes of glm transpose(m)).
+void rowMajor(const mat4& m, float out[16])
+{
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++)
+            out[4 * r + c] = m[4 * c + r];
+}
+
+// Inverse of a column-major 4x4 (double precision, rounded to float), column-major out.
+bool inverse4(const mat4& m, mat4& out)
+{
+    double a[4][8];
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++)
+        {
+            a[r][c]     = m[4 * c + r];
+            a[r][c + 4] = r == c ? 1.0 : 0.0;
+        }
+    for (int c = 0; c < 4; c++)
+    {
+        int p = c;
+        for (int r = c + 1; r < 4; r++)
+            if (std::fabs(a[r][c]) > std::fabs(a[p][c]))
+                p = r;
+        if (std::fabs(a[p][c]) < 1e-300)
+            return false;
+        if (p != c)
+            for (int k = 0; k < 8; k++)
+                std::swap(a[p][k], a[c][k]);
+        double inv = 1.0 / a[c][c];
+        for (int k = 0; k < 8; k++)
+            a[c][k] *= inv;
+        for (int r = 0; r < 4; r++)
+            if (r != c)
+            {
+                double f = a[r][c];
+                for (int k = 0; k < 8; k++)
+                    a[r][k] -= f * a[c][k];
+            }
+    }
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++)
+            out[4 * c + r] = float(a[r][c + 4]);
+    return true;
+}
+
+const mat4 kIdentity = { 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1 };
+
+class Values : public IValues
+{
+public:
+    Properties props;
+    bool dirty = true;
+    void setBoolean(const std::string& n, bool v) override { props[n] = v; dirty = true; }
+    void setInt(const std::string& n, int v) override { props[n] = v; dirty = true; }
+    void setFloat(const std::string& n, float v) override { props[n] = v; dirty = true; }
+    void setFloat3(const std::string& n, const vec3& v) override { props[n] = v; dirty = true; }
+    void setMatrix(const std::string& n, const mat4& v) override { props[n] = v; dirty = true; }
+    void setString(const std::string& n, const std::string& v) override { props[n] = v; dirty = true; }
+    void clearValue(const std::string& n) override { props.erase(n); dirty = true; }
+    float asFloat(const std::string& n, float def) const
+    {
+        if (auto* f = find<float>(props, n))
+            return *f;
+        if (auto* i = find<int>(props, n))
+            return float(*i);
+        return def;
+    }
+    int asInt(const std::string& n, int def) const
+    {
+        if (auto* i = find<int>(props, n))
+            return *i;
+        if (auto* f = find<float>(props, n))
+            return int(*f);
+        return def;
+    }
+    bool asBool(const std::string& n, bool def) const
+    {
+        if (auto* b = find<bool>(props, n))
+            return *b;
+        if (auto* i = find<int>(props, n))
+            return *i != 0;
+        return def;
+    }
+    vec3 asFloat3(const std::string& n, const vec3& def) const
+    {
+        auto* v = find<vec3>(props, n);
+        return v ? *v : def;
+    }
+};
+
+class Light : public ILight
+{
+public:
+    Values v;
+    Light()
+    {
+        // Distant-light defaults (HGI/HGILight.cpp:31-38): direction normalize(-1, -0.5, -1).
+        float l = std::sqrt(1.f + 0.25f + 1.f);
+        v.setFloat3(Names::LightProperties::kDirection, { -1.f / l, -0.5f / l, -1.f / l });
+        v.setFloat3(Names::LightProperties::kColor, { 1.f, 1.f, 1.f });
+        v.setFloat(Names::LightProperties::kAngularDiameter, 0.1f);
+        v.setFloat(Names::LightProperties::kIntensity, 1.f);
+    }
+    IValues& values() override { return v; }
+};
+
+class RenderBuffer : public IRenderBuffer
+{
+public:
+    int w, h;
+    ImageFormat format;
+    std::vector<uint8_t> rgba8;
+    std::vector<float> rgba32;
+    RenderBuffer(int width, int height, ImageFormat f) : w(width), h(height), format(f)
+    {
+        if (f == ImageFormat::Integer_RGBA)
+            rgba8.assign(size_t(w) * h * 4, 0);
+        else
+            rgba32.assign(size_t(w) * h * 4, 0.f);
+    }
+    const void* data(size_t& stride, bool) override
+    {
+        stride = size_t(w) * (format == ImageFormat::Integer_RGBA ? 4 : 16);
+        return format == ImageFormat::Integer_RGBA ? static_cast<const void*>(rgba8.data())
+                                                   : static_cast<const void*>(rgba32.data());
+    }
+    int width() const override { return w; }
+    int height() const override { return h; }
+};
+
+// Standard Surface property name -> (offset in agb_material in floats, component count).
+struct MatField
+{
+    const char* name;
+    size_t offset;
+    int count;
+    bool integer;
+};
+#define AGB_MF(field, n, i) { #field, offsetof(agb_material, field), n, i }
+const MatField kMatFields[] = {
+    AGB_MF(base, 1, false), AGB_MF(base_color, 3, false), AGB_MF(diffuse_roughness, 1, false),
+    AGB_MF(metalness, 1, false), AGB_MF(specular, 1, false), AGB_MF(specular_color, 3, false),
+    AGB_MF(specular_roughness, 1, false), AGB_MF(specular_IOR, 1, false),
+    AGB_MF(specular_anisotropy, 1, false), AGB_MF(specular_rotation, 1, false),
+    AGB_MF(transmission, 1, false), AGB_MF(transmission_color, 3, false), AGB_MF(subsurface, 1, false),
+    AGB_MF(subsurface_color, 3, false), AGB_MF(subsurface_radius, 3, false),
+    AGB_MF(subsurface_scale, 1, false), AGB_MF(subsurface_anisotropy, 1, false), AGB_MF(sheen, 1, false),
+    AGB_MF(sheen_color, 3, false), AGB_MF(sheen_roughness, 1, false), AGB_MF(coat, 1, false),
+    AGB_MF(coat_color, 3, false), AGB_MF(coat_roughness, 1, false), AGB_MF(coat_anisotropy, 1, false),
+    AGB_MF(coat_rotation, 1, false), AGB_MF(coat_IOR, 1, false), AGB_MF(coat_affect_color, 1, false),
+    AGB_MF(coat_affect_roughness, 1, false), AGB_MF(emission, 1, false), AGB_MF(emission_color, 3, false),
+    AGB_MF(opacity, 3, false), AGB_MF(thin_walled, 1, true),
+};
+#undef AGB_MF
+
+// Built-in Standard Surface defaults (MaterialBase.cpp:109-167).
+agb_material defaultMaterial()
+{
+    agb_material m;
+    std::memset(&m, 0, sizeof m);
+    auto set3 = [](float* d, float a, float b, float c) { d[0] = a; d[1] = b; d[2] = c; };
+    m.base = 0.8f;
+    set3(m.base_color, 1, 1, 1);
+    m.specular = 1.f;
+    set3(m.specular_color, 1, 1, 1);
+    m.specular_roughness = 0.2f;
+    m.specular_IOR       = 1.5f;
+    set3(m.transmission_color, 1, 1, 1);
+    set3(m.subsurface_color, 1, 1, 1);
+    set3(m.subsurface_radius, 1, 1, 1);
+    m.subsurface_scale = 1.f;
+    set3(m.sheen_color, 1, 1, 1);
+    m.sheen_roughness = 0.3f;
+    set3(m.coat_color, 1, 1, 1);
+    m.coat_roughness = 0.1f;
+    m.coat_IOR       = 1.5f;
+    set3(m.emission_color, 1, 1, 1);
+    set3(m.opacity, 1, 1, 1);
+    for (float* s : { m.base_color_image_scale, m.specular_roughness_image_scale, m.emission_color_image_scale,
+             m.opacity_image_scale, m.normal_image_scale })
+        s[0] = s[1] = 1.f;
+    return m;
+}
+
+class Scene : public IScene
+{
+public:
+    struct Geometry
+    {
+        GeometryDescriptor desc;
+        int32_t handle = -1;
+        float bounds[6] = { 1e30f, 1e30f, 1e30f, -1e30f, -1e30f, -1e30f };
+    };
+    struct Image
+    {
+        ImageDescriptor desc;
+        int32_t handle = -1;
+    };
+    struct Instance
+    {
+        Path geometry;
+        Properties props;
+    };
+
+    std::map<Path, Geometry> geometries;
+    std::map<Path, Image> images;
+    std::map<Path, Properties> materials;
+    std::map<Path, Properties> environments;
+    std::vector<std::pair<Path, Instance>> instances; // insertion order
+    std::vector<std::shared_ptr<Light>> lights;
+    Path environment;
+    bool hasBounds = false;
+    vec3 bmin{}, bmax{};
+    bool dirty     = true;
+    agb_context* ctx = nullptr; // the context the scene was last activated on
+
+    void setGeometryDescriptor(const Path& p, const GeometryDescriptor& d) override
+    {
+        if (d.type != PrimitiveType::Triangles || !d.getAttributeData || d.vertexDesc.count == 0)
+            throw Error("setGeometryDescriptor: triangle geometry with vertices and a data callback required");
+        if (!d.vertexDesc.attributes.count(Names::VertexAttributes::kPosition) ||
+            d.vertexDesc.attributes.at(Names::VertexAttributes::kPosition) != AttributeFormat::Float3)
+            throw Error("setGeometryDescriptor: positions must be Float3");
+        geometries[p] = Geometry{ d, -1 };
+        dirty         = true;
+    }
+    void setImageDescriptor(const Path& p, const ImageDescriptor& d) override
+    {
+        if (!d.getData)
+            throw Error("setImageDescriptor: a data callback is required");
+        images[p] = Image{ d, -1 };
+        dirty     = true;
+    }
+    void setMaterialType(const Path& p, const std::string& type, const std::string&) override
+    {
+        if (type != Names::MaterialTypes::kBuiltIn)
+            logError("setMaterialType: only the built-in Standard Surface material is supported; " + p +
+                " uses it");
+        materials[p];
+        dirty = true;
+    }
+    void setMaterialProperties(const Path& p, const Properties& props) override
+    {
+        Properties& m = materials[p];
+        for (auto& kv : props)
+            m[kv.first] = kv.second;
+        dirty = true;
+    }
+    bool addInstance(const Path& p, const Path& geometry, const Properties& props) override
+    {
+        for (auto& kv : instances)
+            if (kv.first == p)
+            {
+                logError("addInstance: " + p + " already exists");
+                return false;
+            }
+        instances.push_back({ p, Instance{ geometry, props } });
+        dirty = true;
+        return true;
+    }
+    void setInstanceProperties(const Path& p, const Properties& props) override
+    {
+        for (auto& kv : instances)
+            if (kv.first == p)
+            {
+                for (auto& q : props)
+                    kv.second.props[q.first] = q.second;
+                dirty = true;
+                return;
+            }
+        logError("setInstanceProperties: no instance " + p);
+    }
+    void removeInstance(const Path& p) override
+    {
+        instances.erase(std::remove_if(instances.begin(), instances.end(),
+                            [&](const std::pair<Path, Instance>& kv) { return kv.first == p; }),
+            instances.end());
+        dirty = true;
+    }
+    bool setEnvironmentProperties(const Path& p, const Properties& props) override
+    {
+        Properties& e = environments[p];
+        for (auto& kv : props)
+            e[kv.first] = kv.second;
+        dirty = true;
+        return true;
+    }
+    bool setEnvironment(const Path& p) override
+    {
+        environment = p;
+        dirty       = true;
+        return true;
+    }
+    void setBounds(const vec3& mn, const vec3& mx) override
+    {
+        bmin      = mn;
+        bmax      = mx;
+        hasBounds = true;
+    }
+    ILightPtr addLightPointer(const std::string& type) override
+    {
+        if (type != Names::LightTypes::kDistantLight)
+            throw Error("addLightPointer: only " + Names::LightTypes::kDistantLight + " is supported");
+        auto l = std::make_shared<Light>();
+        lights.push_back(l);
+        return l;
+    }
+
+    // Uploads what changed to ctx (a new context re-uploads everything).
+    void activate(agb_context* c)
+    {
+        if (c != ctx)
+        {
+            for (auto& g : geometries)
+                g.second.handle = -1;
+            for (auto& i : images)
+                i.second.handle = -1;
+            ctx   = c;
+            dirty = true;
+        }
+        if (!dirty)
+            return;
+        // Geometry referenced by instances, pulled once.
+        for (auto& kv : instances)
+        {
+            auto it = geometries.find(kv.second.geometry);
+            if (it == geometries.end())
+                throw Error("render: instance " + kv.first + " refers to unknown geometry " + kv.second.geometry);
+            if (it->second.handle < 0)
+                pullGeometry(it->first, it->second);
+        }
+        std::vector<agb_material> mats(1, defaultMaterial());
+        std::map<Path, int32_t> matIndex;
+        for (auto& kv : materials)
+        {
+            agb_material m = defaultMaterial();
+            for (auto& p : kv.second)
+                applyMaterialProperty(m, p.first, p.second, kv.first);
+            matIndex[kv.first] = int32_t(mats.size());
+            mats.push_back(m);
+        }
+        check(agb_materials_set(ctx, mats.data(), nullptr, uint32_t(mats.size())), "upload materials");
+        std::vector<agb_instance> insts;
+        for (auto& kv : instances)
+        {
+            const Properties& p = kv.second.props;
+            if (auto* vis = find<bool>(p, Names::InstanceProperties::kVisible))
+                if (!*vis)
+                    continue;
+            agb_instance in;
+            std::memset(&in, 0, sizeof in);
+            in.geometry = geometries[kv.second.geometry].handle;
+            in.material = 0;
+            if (auto* mp = find<std::string>(p, Names::InstanceProperties::kMaterial))
+            {
+                auto it = matIndex.find(*mp);
+                if (it == matIndex.end())
+                    logError("instance " + kv.first + ": unknown material " + *mp + ", using the default");
+                else
+                    in.material = it->second;
+            }
+            const mat4* t = find<mat4>(p, Names::InstanceProperties::kTransform);
+            rows3x4(t ? *t : kIdentity, in.object_to_world);
+            if (p.count(Names::InstanceProperties::kMaterialLayers))
+                logError("instance " + kv.first + ": material layers are not supported by this interface");
+            insts.push_back(in);
+        }
+        check(agb_instances_set(ctx, insts.data(), uint32_t(insts.size())), "upload instances");
+        applyEnvironment();
+        dirty = false;
+    }
+
+    void pullGeometry(const Path& path, Geometry& g)
+    {
+        const GeometryDescriptor& d = g.desc;
+        size_t nv = d.vertexDesc.count, ni = d.indexCount;
+        AttributeDataMap buffers;
+        for (auto& a : d.vertexDesc.attributes)
+            buffers[a.first] = AttributeData{};
+        if (ni)
+            buffers[Names::VertexAttributes::kIndices] = AttributeData{};
+        if (!d.getAttributeData(buffers, 0, nv, 0, ni))
+            throw Error("geometry " + path + ": getAttributeData failed");
+        auto gather = [&](const std::string& name, int comps) -> std::vector<float> {
+            std::vector<float> out;
+            auto it = buffers.find(name);
+            if (it == buffers.end() || !it->second.address)
+                return out;
+            const AttributeData& a = it->second;
+            size_t stride = a.stride ? a.stride : comps * sizeof(float);
+            out.resize(nv * comps);
+            for (size_t v = 0; v < nv; v++)
+                std::memcpy(&out[v * comps], static_cast<const uint8_t*>(a.address) + a.offset + v * stride,
+                    comps * sizeof(float));
+            return out;
+        };
+        std::vector<float> pos = gather(Names::VertexAttributes::kPosition, 3);
+        if (pos.empty())
+            throw Error("geometry " + path + ": no positions");
+        std::vector<float> nrm = gather(Names::VertexAttributes::kNormal, 3);
+        std::vector<float> uv  = gather(Names::VertexAttributes::kTexCoord0, 2);
+        std::vector<uint32_t> idx;
+        if (ni)
+        {
+            const AttributeData& a = buffers[Names::VertexAttributes::kIndices];
+            if (!a.address)
+                throw Error("geometry " + path + ": no indices");
+            idx.resize(ni);
+            size_t stride = a.stride ? a.stride : sizeof(uint32_t);
+            for (size_t k = 0; k < ni; k++)
+                std::memcpy(&idx[k], static_cast<const uint8_t*>(a.address) + a.offset + k * stride, 4);
+        }
+        if (d.attributeUpdateComplete)
+            d.attributeUpdateComplete(buffers, 0, nv, 0, ni);
+        check(agb_geometry_create(ctx, pos.data(), nrm.empty() ? nullptr : nrm.data(),
+                  uv.empty() ? nullptr : uv.data(), idx.empty() ? nullptr : idx.data(), uint32_t(nv),
+                  uint32_t(ni ? ni : nv), &g.handle),
+            "geometry " + path);
+        for (size_t v = 0; v < nv; v++)
+            for (int k = 0; k < 3; k++)
+            {
+                g.bounds[k]     = std::min(g.bounds[k], pos[3 * v + k]);
+                g.bounds[3 + k] = std::max(g.bounds[3 + k], pos[3 * v + k]);
+            }
+    }
+
+    int32_t imageHandle(const Path& path)
+    {
+        auto it = images.find(path);
+        if (it == images.end())
+            throw Error("unknown image " + path);
+        Image& im = it->second;
+        if (im.handle >= 0)
+            return im.handle;
+        ImageData data;
+        if (!im.desc.getData(data) || !data.pPixelBuffer)
+            throw Error("image " + path + ": getData failed");
+        int32_t fmt = data.format == ImageFormat::Integer_RGBA ? AGB_FORMAT_RGBA8_UNORM
+            : data.format == ImageFormat::Float_RGBA           ? AGB_FORMAT_RGBA32F
+                                                               : AGB_FORMAT_RGB32F;
+        check(agb_image_create(ctx, data.pPixelBuffer, uint32_t(data.dimensions[0]), uint32_t(data.dimensions[1]),
+                  fmt, 0, &im.handle),
+            "image " + path);
+        if (im.desc.updateComplete)
+            im.desc.updateComplete(data);
+        return im.handle;
+    }
+
+    void applyEnvironment()
+    {
+        agb_environment_data e;
+        std::memset(&e, 0, sizeof e);
+        // Defaults (EnvironmentBase.cpp:33-45).
+        const Properties empty;
+        const Properties& p = environments.count(environment) ? environments[environment] : empty;
+        auto v3 = [&](const std::string& n, vec3 def, float* out) {
+            auto* v = find<vec3>(p, n);
+            vec3 x  = v ? *v : def;
+            out[0] = x[0];
+            out[1] = x[1];
+            out[2] = x[2];
+        };
+        v3(Names::EnvironmentProperties::kLightTop, { 1, 1, 1 }, e.light_top);
+        v3(Names::EnvironmentProperties::kLightBottom, { 0, 0, 0 }, e.light_bottom);
+        v3(Names::EnvironmentProperties::kBackgroundTop, { 0.02f, 0.25f, 0.60f }, e.background_top);
+        v3(Names::EnvironmentProperties::kBackgroundBottom, { 0.32f, 0.79f, 1.0f }, e.background_bottom);
+        const mat4* lt = find<mat4>(p, Names::EnvironmentProperties::kLightTransform);
+        mat4 lm        = lt ? *lt : kIdentity, lmi;
+        if (!inverse4(lm, lmi))
+            throw Error("environment: light transform is singular");
+        rowMajor(lm, e.light_transform);
+        rowMajor(lmi, e.light_transform_inv);
+        const mat4* bt = find<mat4>(p, Names::EnvironmentProperties::kBackgroundTransform);
+        rowMajor(bt ? *bt : kIdentity, e.background_transform);
+        if (auto* b = find<bool>(p, Names::EnvironmentProperties::kBackgroundUseScreen))
+            e.background_use_screen = *b ? 1 : 0;
+        int32_t light = -1, background = -1;
+        if (auto* li = find<std::string>(p, Names::EnvironmentProperties::kLightImage))
+            if (!li->empty())
+                light = imageHandle(*li);
+        if (auto* bi = find<std::string>(p, Names::EnvironmentProperties::kBackgroundImage))
+            if (!bi->empty())
+                background = imageHandle(*bi);
+        check(agb_environment_set(ctx, &e, light, background), "environment");
+    }
+
+    static void applyMaterialProperty(agb_material& m, const std::string& name, const PropertyValue& v,
+        const Path& path)
+    {
+        for (const MatField& f : kMatFields)
+        {
+            if (name != f.name)
+                continue;
+            float* dst = reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(&m) + f.offset);
+            if (f.integer)
+            {
+                int32_t iv = 0;
+                if (auto* b = std::get_if<bool>(&v))
+                    iv = *b;
+                else if (auto* i = std::get_if<int>(&v))
+                    iv = *i;
+                else
+                {
+                    logError("material " + path + ": " + name + " wants a boolean");
+                    return;
+                }
+                std::memcpy(dst, &iv, 4);
+                return;
+            }
+            if (f.count == 3)
+            {
+                if (auto* x = std::get_if<vec3>(&v))
+                {
+                    dst[0] = (*x)[0];
+                    dst[1] = (*x)[1];
+                    dst[2] = (*x)[2];
+                    return;
+                }
+            }
+            else if (auto* x = std::get_if<float>(&v))
+            {
+                dst[0] = *x;
+                return;
+            }
+            logError("material " + path + ": " + name + " has the wrong type");
+            return;
+        }
+        logError("material " + path + ": unknown property " + name);
+    }
+
+    void bounds(float out[6]) const
+    {
+        if (hasBounds)
+        {
+            for (int k = 0; k < 3; k++)
+            {
+                out[k]     = bmin[k];
+                out[3 + k] = bmax[k];
+            }
+            return;
+        }
+        for (int k = 0; k < 3; k++)
+        {
+            out[k]     = 1e30f;
+            out[3 + k] = -1e30f;
+        }
+        for (auto& kv : instances)
+        {
+            auto it = geometries.find(kv.second.geometry);
+            if (it == geometries.end() || it->second.handle < 0)
+                continue;
+            const mat4* t = find<mat4>(kv.second.props, Names::InstanceProperties::kTransform);
+            const mat4& m = t ? *t : kIdentity;
+            const float* b = it->second.bounds;
+            for (int c = 0; c < 8; c++)
+            {
+                float pt[3] = { b[(c & 1) ? 3 : 0], b[(c & 2) ? 4 : 1], b[(c & 4) ? 5 : 2] };
+                for (int r = 0; r < 3; r++)
+                {
+                    float w = m[r] * pt[0] + m[4 + r] * pt[1] + m[8 + r] * pt[2] + m[12 + r];
+                    out[r]     = std::min(out[r], w);
+                    out[3 + r] = std::max(out[3 + r], w);
+                }
+            }
+        }
+    }
+};
+
+class Renderer : public IRenderer
+{
+public:
+    agb_context* ctx = nullptr;
+    std::shared_ptr<Scene> scene;
+    TargetAssignments targets;
+    Values opts;
+    mat4 view = kIdentity, proj = kIdentity;
+    float focalDistance = 1.f, lensRadius = 0.f;
+
+    explicit Renderer(agb_context* c) : ctx(c)
+    {
+        // Option defaults (RendererBase.cpp:59-89).
+        opts.setFloat("maxLuminance", 1000.f);
+        opts.setInt("traceDepth", 5);
+        opts.setBoolean("isToneMappingEnabled", false);
+        opts.setBoolean("isGammaCorrectionEnabled", true);
+        opts.setFloat3("brightness", { 1.f, 1.f, 1.f });
+        opts.setBoolean("isRussianRouletteEnabled", true);
+        opts.setInt("russianRouletteStartDepth", 3);
+        opts.setBoolean("isDiffuseOnlyEnabled", false);
+    }
+    ~Renderer() override
+    {
+        if (ctx)
+            agb_context_destroy(ctx);
+    }
+    IScenePtr createScene() override { return std::make_shared<Scene>(); }
+    void setScene(const IScenePtr& s) override
+    {
+        scene = std::dynamic_pointer_cast<Scene>(s);
+        if (s && !scene)
+            throw Error("setScene: the scene was not created by this renderer");
+    }
+    IRenderBufferPtr createRenderBuffer(int w, int h, ImageFormat f) override
+    {
+        if (w <= 0 || h <= 0 || f == ImageFormat::Float_RGB)
+            throw Error("createRenderBuffer: positive size, Integer_RGBA or Float_RGBA");
+        return std::make_shared<RenderBuffer>(w, h, f);
+    }
+    void setTargets(const TargetAssignments& t) override { targets = t; }
+    void setOptions(const Properties& o) override
+    {
+        for (auto& kv : o)
+            opts.props[kv.first] = kv.second;
+    }
+    IValues& options() override { return opts; }
+    void setCamera(const mat4& v, const mat4& p, float fd, float lr) override
+    {
+        view          = v;
+        proj          = p;
+        focalDistance = fd;
+        lensRadius    = lr;
+    }
+
+    // RendererBase::updateFrameDataGPUStruct (RendererBase.cpp:225-295) for the current options.
+    agb_frame_data frameData(uint32_t W, uint32_t H) const
+    {
+        agb_frame_data f;
+        std::memset(&f, 0, sizeof f);
+        // view-projection: proj * view (column-major).
+        mat4 vp{};
+        for (int r = 0; r < 4; r++)
+            for (int c = 0; c < 4; c++)
+            {
+                double s = 0;
+                for (int k = 0; k < 4; k++)
+                    s += double(proj[4 * k + r]) * double(view[4 * c + k]);
+                vp[4 * c + r] = float(s);
+            }
+        std::memcpy(f.camera_view_proj, vp.data(), 64);
+        std::memcpy(f.camera_view_proj_prev, vp.data(), 64);
+        mat4 inv;
+        if (!inverse4(view, inv))
+            throw Error("setCamera: view matrix is singular");
+        rowMajor(inv, f.camera_inv_view);
+        std::memcpy(f.camera_inv_view_prev, f.camera_inv_view, 64);
+        f.view_size[0]        = float(2.0 / double(proj[0]));
+        f.view_size[1]        = float(2.0 / double(proj[5]));
+        f.is_ortho_projection = proj[15] == 1.f ? 1 : 0;
+        f.focal_distance      = focalDistance;
+        f.lens_radius         = lensRadius;
+        f.time_delta_ms       = 1000.f / 60.f;
+        float b[6];
+        scene->bounds(b);
+        bool valid = b[0] <= b[3];
+        if (valid)
+        {
+            float dx = b[3] - b[0], dy = b[4] - b[1], dz = b[5] - b[2];
+            f.scene_size = std::sqrt(dx * dx + dy * dy + dz * dz);
+        }
+        // Sky depth: twice the denoising range (RendererBase.cpp:206-224, :258).
+        float range = 1.f;
+        if (valid)
+        {
+            float zmin = 1e30f;
+            for (int c = 0; c < 8; c++)
+            {
+                float pt[3] = { b[(c & 1) ? 3 : 0], b[(c & 2) ? 4 : 1], b[(c & 4) ? 5 : 2] };
+                float z     = view[2] * pt[0] + view[6] * pt[1] + view[10] * pt[2] + view[14];
+                zmin        = std::min(zmin, z);
+            }
+            range = std::min(std::max(-zmin * 1.1f, 1.f), 5.0e8f);
+        }
+        f.sky_view_z                      = -range * 2.f;
+        f.is_force_opaque_shadows_enabled = 1;
+        f.is_diffuse_only_enabled         = opts.asBool("isDiffuseOnlyEnabled", false) ? 1 : 0;
+        f.trace_depth                     = std::max(1, std::min(10, opts.asInt("traceDepth", 5)));
+        f.max_luminance                   = opts.asFloat("maxLuminance", 1000.f);
+        f.is_russian_roulette_enabled     = opts.asBool("isRussianRouletteEnabled", true) ? 1 : 0;
+        f.russian_roulette_start_depth    = std::max(0, opts.asInt("russianRouletteStartDepth", 3));
+        // Distant lights (HGIScene.cpp:110-133): at most 4, direction negated.
+        int n = int(std::min<size_t>(scene->lights.size(), 4));
+        f.distant_light_count = n;
+        for (int i = 0; i < n; i++)
+        {
+            const Values& v = scene->lights[i]->v;
+            vec3 d = v.asFloat3(Names::LightProperties::kDirection, { 0, 0, -1 });
+            vec3 c = v.asFloat3(Names::LightProperties::kColor, { 1, 1, 1 });
+            f.distant_lights[i].cos_radius = std::cos(0.5f * v.asFloat(Names::LightProperties::kAngularDiameter, 0.1f));
+            for (int k = 0; k < 3; k++)
+            {
+                f.distant_lights[i].direction[k]           = -d[k];
+                f.distant_lights[i].color_and_intensity[k] = c[k];
+            }
+            f.distant_lights[i].color_and_intensity[3] = v.asFloat(Names::LightProperties::kIntensity, 1.f);
+        }
+        (void)W;
+        (void)H;
+        return f;
+    }
+
+    void render(uint32_t sampleStart, uint32_t sampleCount) override
+    {
+        if (!scene)
+            throw Error("render: no scene");
+        auto it = targets.find(AOV::Final);
+        if (it == targets.end() || !it->second)
+            throw Error("render: no Final target");
+        auto* target = dynamic_cast<RenderBuffer*>(it->second.get());
+        scene->activate(ctx);
+        agb_frame_data f = frameData(uint32_t(target->w), uint32_t(target->h));
+        check(agb_frame_set(ctx, &f), "render");
+        agb_render_options o;
+        std::memset(&o, 0, sizeof o);
+        o.width        = uint32_t(target->w);
+        o.height       = uint32_t(target->h);
+        o.accumulation = AGB_ACCUM_RUNNING_MEAN;
+        check(agb_render(ctx, &o, sampleStart, sampleCount, nullptr), "render");
+        vec3 br = opts.asFloat3("brightness", { 1, 1, 1 });
+        check(agb_post_process(ctx, AGB_ACCUM_RUNNING_MEAN, br.data(), opts.asBool("isToneMappingEnabled", false),
+                  opts.asBool("isGammaCorrectionEnabled", true),
+                  target->format == ImageFormat::Float_RGBA ? target->rgba32.data() : nullptr,
+                  target->format == ImageFormat::Integer_RGBA ? target->rgba8.data() : nullptr),
+            "render");
+    }
+    void waitForTask() override { check(agb_wait(ctx), "waitForTask"); }
+};
+
+} // namespace
+
+void setLogCallback(std::function<void(const std::string&)> cb)
+{
+    std::lock_guard<std::mutex> g(g_logMutex);
+    g_log = std::move(cb);
+}
+
+IRendererPtr createRenderer(IRenderer::Backend, uint32_t)
+{
+    agb_context* ctx = nullptr;
+    if (agb_context_create(0, nullptr, &ctx) != AGB_OK)
+    {
+        logError(std::string("createRenderer: ") + agb_last_error());
+        return nullptr;
+    }
+    return std::make_shared<Renderer>(ctx);
+}
+
+} // namespace agb_aurora
