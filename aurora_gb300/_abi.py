@@ -191,6 +191,7 @@ SIGNATURES = {
     "agb_accum_device": (_I32, [_P, _I32, ctypes.POINTER(_P)]),
     "agb_last_sample_device": (_I32, [_P, ctypes.POINTER(_P)]),
     "agb_post_process": (_I32, [_P, _I32, _P, _I32, _I32, _P, _P]),
+    "agb_accum_rel_mse": (_I32, [_P, _I32, _P, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
     "agb_aov_read": (_I32, [_P, _P, _P, _P, _P]),
     "agb_aov_device": (_I32, [_P, ctypes.POINTER(AovBuffers)]),
     "agb_temporal_resolve": (_I32, [_P, ctypes.POINTER(TemporalSettings)]),

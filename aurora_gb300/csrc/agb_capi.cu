@@ -1058,6 +1058,30 @@ AGB_API agb_status agb_accum_read(agb_context* ctx, int32_t mode, float* host_rg
     return AGB_OK;
 }
 
+AGB_API agb_status agb_accum_rel_mse(agb_context* ctx, int32_t mode, const float* reference_device,
+    double eps, double* out)
+{
+    if (!ctx || !reference_device || !out || !(eps > 0.0))
+        return fail(AGB_ERR_INVALID_ARG, "agb_accum_rel_mse: null argument or eps <= 0");
+    if (!ctx->accMean.ptr || (mode != AGB_ACCUM_RUNNING_MEAN && mode != AGB_ACCUM_KAHAN))
+        return fail(AGB_ERR_NOT_READY, "agb_accum_rel_mse: nothing rendered or bad mode");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    AGB_CUDA(ctx->stats.ensure(8 * sizeof(unsigned long long)), "allocate stats");
+    double* d = reinterpret_cast<double*>(ctx->stats.as<unsigned long long>() + 7);
+    uint32_t pixels = ctx->accW * ctx->accH;
+    const float4* src = mode == AGB_ACCUM_KAHAN ? ctx->accSum.as<float4>() : ctx->accMean.as<float4>();
+    float scale = (mode == AGB_ACCUM_KAHAN && ctx->accumulatedSamples) ? 1.f / float(ctx->accumulatedSamples) : 1.f;
+    AGB_CUDA(launchRelMse(src, scale, reinterpret_cast<const float4*>(reference_device), pixels, eps, d, ctx->stream),
+        "agb_accum_rel_mse");
+    double sum = 0.0;
+    AGB_CUDA(cudaMemcpyAsync(&sum, d, sizeof sum, cudaMemcpyDeviceToHost, ctx->stream), "agb_accum_rel_mse");
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "agb_accum_rel_mse");
+    *out = pixels ? sum / (3.0 * pixels) : 0.0;
+    return AGB_OK;
+}
+
 AGB_API agb_status agb_post_process(agb_context* ctx, int32_t mode, const float brightness[3],
     int32_t tone_map, int32_t gamma, float* out_rgba32f, uint8_t* out_rgba8)
 {

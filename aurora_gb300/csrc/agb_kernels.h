@@ -225,6 +225,8 @@ cudaError_t launchEnvSampleBatch(const DevScene& s, const float* rnd, int64_t n,
     float* outRadiance, float* outDir, float* outPdf, cudaStream_t st);
 cudaError_t launchRandomStream(uint32_t sampleIndex, uint32_t width, uint32_t px, uint32_t py,
     int n, float* out, cudaStream_t st);
+cudaError_t launchRelMse(const float4* accum, float scale, const float4* ref, uint32_t pixels, double eps,
+    double* out, cudaStream_t st);
 cudaError_t launchPostProcess(const float4* accum, const float* accumComp, int mode,
     float invCount, uint32_t pixels, float3 brightness, int toneMap, int gamma, float4* out32,
     uchar4* out8, cudaStream_t st);

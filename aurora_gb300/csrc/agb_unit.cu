@@ -252,4 +252,43 @@ cudaError_t launchPostProcess(const float4* accum, const float* accumComp, int m
     return cudaGetLastError();
 }
 
+// relMSE of an accumulation against a reference: mean over pixels and RGB of (x - r)^2 / (r^2 + eps),
+// x = accum * scale.  FP64 block sums, one atomic per block.
+__global__ void k_rel_mse(const float4* accum, float scale, const float4* ref, uint32_t pixels, double eps,
+    double* out)
+{
+    __shared__ double part[8];
+    double s = 0.0;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < pixels; p += gridDim.x * blockDim.x)
+    {
+        float4 a = accum[p], r = ref[p];
+        double x[3] = { double(a.x) * scale, double(a.y) * scale, double(a.z) * scale };
+        double y[3] = { r.x, r.y, r.z };
+        for (int k = 0; k < 3; k++)
+            s += (x[k] - y[k]) * (x[k] - y[k]) / (y[k] * y[k] + eps);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0)
+        part[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        double t = 0.0;
+        for (int w = 0; w < int(blockDim.x >> 5); w++)
+            t += part[w];
+        atomicAdd(out, t);
+    }
+}
+
+cudaError_t launchRelMse(const float4* accum, float scale, const float4* ref, uint32_t pixels, double eps,
+    double* out, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), st);
+    if (e != cudaSuccess)
+        return e;
+    k_rel_mse<<<304, 256, 0, st>>>(accum, scale, ref, pixels, eps, out);
+    return cudaGetLastError();
+}
+
 } // namespace agb

@@ -49,6 +49,7 @@ def parse_args():
     p.add_argument("--spp", type=int, default=None, help="samples per pixel override (profiling runs)")
     p.add_argument("--no-denoiser", action="store_true", help="skip the denoiser measurement")
     p.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    p.add_argument("--no-time-to-error", action="store_true", help="skip the time-to-relMSE measurement")
     p.add_argument("--serve-requests", type=int, default=160)
     return p.parse_args()
 
@@ -116,6 +117,32 @@ def bench_denoiser(torch, _abi, stream, peaks):
     finally:
         lib.agb_denoiser_destroy(h)
     return out
+
+
+def bench_time_to_rel_mse(torch, _abi, r, s, target=1e-3, ref_spp=2048, chunk=8, max_spp=4096):
+    """Wall time until the running image is within relMSE `target` (eps 1e-2) of a converged
+    reference of the same frame.  The reference is this renderer's own ref_spp-sample Kahan mean
+    (its agreement with the FP64 oracle is a test).  The timed loop renders `chunk` samples at a
+    time into the Kahan sum and evaluates relMSE on the GPU (agb_accum_rel_mse) after each chunk."""
+    import ctypes
+    lib = _abi.library()
+    r.set_frame(s.frame)
+    r.render(0, ref_spp, accumulation=_abi.ACCUM_KAHAN)
+    ref = torch.from_numpy(r.read(_abi.ACCUM_KAHAN).copy()).cuda()
+    torch.cuda.synchronize()
+    err = ctypes.c_double(float("inf"))
+    t0 = time.perf_counter()
+    spp = 0
+    while spp < max_spp:
+        r.render(spp, chunk, accumulation=_abi.ACCUM_KAHAN)
+        spp += chunk
+        _abi.check(lib.agb_accum_rel_mse(r.ctx, _abi.ACCUM_KAHAN, ref.data_ptr(), 1e-2, ctypes.byref(err)))
+        if err.value <= target:
+            break
+    secs = time.perf_counter() - t0
+    return {"target_rel_mse": target, "eps": 1e-2, "seconds": secs, "spp": spp,
+            "rel_mse": err.value, "reached": err.value <= target, "reference_spp": ref_spp,
+            "chunk_spp": chunk, "path_samples": s.width * s.height * spp}
 
 
 def bench_serving(api, _abi, n_requests, rates=(200.0, 25.0)):
@@ -460,6 +487,8 @@ def main():
         "roofline": roofline,
         "clocks": clk,
     }
+    if rank == 0 and not args.no_time_to_error:
+        out["time_to_rel_mse"] = bench_time_to_rel_mse(torch, _abi, r, s)
     if rank == 0 and not args.no_denoiser:
         out["denoiser"] = bench_denoiser(torch, _abi, stream, measured_peaks())
     if rank == 0 and not args.no_serve:

@@ -588,6 +588,12 @@ enum
     AGB_POST_SOURCE_TEMPORAL = 4
 };
 
+/* relMSE of the accumulation (mode as agb_accum_read) against a reference RGBA32F image in
+ * device memory: mean over pixels and RGB of (x - r)^2 / (r^2 + eps), computed on the GPU in FP64
+ * (a convergence monitor for progressive rendering). */
+AGB_API agb_status agb_accum_rel_mse(agb_context* ctx, int32_t mode, const float* reference_device,
+    double eps, double* out);
+
 /* Post-processing (HGI/Shaders/PostProcessing.glsl:37-64): brightness, optional ACES, optional
  * sRGB approximation, alpha 1.  Writes RGBA32F (out_rgba32f) and/or RGBA8 (out_rgba8) host
  * buffers. */

@@ -129,3 +129,28 @@ def test_invalid_inputs_are_rejected(agb):
         r.set_frame(s.frame)
         with pytest.raises(_abi.AgbError):
             r.render(5, 1)  # does not continue the accumulated sequence
+
+
+def test_accum_rel_mse_matches_numpy(agb, oracle):
+    """agb_accum_rel_mse (GPU, FP64) against the oracle's relMSE of the read-back image."""
+    import ctypes
+    import torch
+    from aurora_gb300 import api, scenes
+    s = scenes.config_tiny(width=40, height=30, spp=4)
+    with api.Renderer() as r:
+        r.upload(s)
+        r.render(0, 64, accumulation=_abi.ACCUM_KAHAN)
+        ref = r.read(_abi.ACCUM_KAHAN).copy()
+        r.render(0, 4, accumulation=_abi.ACCUM_KAHAN | _abi.ACCUM_RUNNING_MEAN)
+        img_k = r.read(_abi.ACCUM_KAHAN)
+        img_m = r.read(_abi.ACCUM_RUNNING_MEAN)
+        refd = torch.from_numpy(ref).cuda()
+        out = ctypes.c_double()
+        _abi.check(agb.agb_accum_rel_mse(r.ctx, _abi.ACCUM_KAHAN, refd.data_ptr(), 1e-2, ctypes.byref(out)))
+        gk = out.value
+        _abi.check(agb.agb_accum_rel_mse(r.ctx, _abi.ACCUM_RUNNING_MEAN, refd.data_ptr(), 1e-2, ctypes.byref(out)))
+        gm = out.value
+    want_k = oracle.rel_mse(img_k, ref)
+    want_m = oracle.rel_mse(img_m, ref)
+    print(f"relMSE gpu {gk:.6g} numpy {want_k:.6g}")
+    assert abs(gk - want_k) <= 1e-6 * want_k and abs(gm - want_m) <= 1e-6 * want_m
