@@ -27,6 +27,7 @@ FORMAT_RGBA32F = 1
 FORMAT_RGB32F = 2
 ENV_TABLE_REFERENCE = 0
 ENV_TABLE_FP64 = 1
+BVH_HOST, BVH_GPU = 0, 1
 ENV_NOALLOC_MAX_TEXELS = 262144  # AGB_ENV_NOALLOC_MAX_TEXELS
 TEX_BASE_COLOR, TEX_SPECULAR_ROUGHNESS, TEX_OPACITY, TEX_NORMAL, TEX_EMISSION = range(5)
 
@@ -175,6 +176,9 @@ SIGNATURES = {
     "agb_set_profiling": (_I32, [_P, _I32]),
     "agb_geometry_create": (_I32, [_P, _P, _P, _P, _P, _U32, _U32, ctypes.POINTER(_I32)]),
     "agb_image_create": (_I32, [_P, _P, _U32, _U32, _I32, _I32, ctypes.POINTER(_I32)]),
+    "agb_set_bvh_builder": (_I32, [_P, _I32]),
+    "agb_geometry_bvh": (_I32, [_P, _I32, _P, _U64, _P, _U64, ctypes.POINTER(_I32), ctypes.POINTER(_I32),
+                                ctypes.POINTER(_U32)]),
     "agb_materials_set": (_I32, [_P, _P, _P, _U32]),
     "agb_instances_set": (_I32, [_P, _P, _U32]),
     "agb_environment_set": (_I32, [_P, _P, _I32, _I32]),

@@ -40,6 +40,19 @@ class Renderer:
             pass
 
     # ------------------------------------------------------------------------- scene upload
+    def upload_geometry_only(self, s):
+        """Creates the scene's meshes (BLAS builds) and nothing else; returns their handles."""
+        self.scene = s
+        out = []
+        for m in s.meshes:
+            g = ctypes.c_int32()
+            check(self._lib.agb_geometry_create(self.ctx, ptr(m["positions"]), ptr(m["normals"]),
+                                                ptr(m["texcoords"]), ptr(m["indices"]),
+                                                len(m["positions"]), len(m["indices"]),
+                                                ctypes.byref(g)))
+            out.append(g.value)
+        return out
+
     def upload(self, s):
         """Uploads a scenes.SceneDesc: the equivalent of IScene construction + the first update."""
         lib = self._lib

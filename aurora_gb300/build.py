@@ -19,7 +19,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["agb_pt.cu", "agb_env_build.cu", "agb_env_noalloc.cu", "agb_temporal.cu", "agb_denoise.cu",
            "agb_unet.cu", "agb_unit.cu",
-           "agb_capi.cu", "agb_serve.cpp", "agb_aurora.cpp", "agb_bvh_build.cpp"]
+           "agb_capi.cu", "agb_serve.cpp", "agb_aurora.cpp", "agb_bvh_build.cpp",
+           "agb_bvh_gpu.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true",
               "-prec-sqrt=true", "-Xcompiler",

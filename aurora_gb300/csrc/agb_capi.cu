@@ -85,6 +85,7 @@ struct Geometry
 {
     DevBuf positions, normals, texcoords, indices, tris, nodes;
     DevMesh mesh{};
+    uint32_t nodeCount = 0;
     float bounds[6]; // lo, hi in object space
 };
 
@@ -129,6 +130,8 @@ struct agb_context
     int32_t envLight = -1, envBackground = -1;
     DevBuf alias;
     EnvBuildScratch envScratch;
+    GpuBvhScratch bvhScratch;
+    int32_t bvhBuilder = AGB_BVH_GPU;
     double envIntegral     = 0.0; // FP64 luminance integral
     double envShadingIntegral = 0.0;
     int32_t envLayout      = AGB_ENV_TABLE_REFERENCE;
@@ -157,6 +160,7 @@ struct agb_context
     ~agb_context()
     {
         freeEnvScratch(envScratch);
+        freeGpuBvhScratch(bvhScratch);
         if (ev0)
             cudaEventDestroy(ev0);
         if (ev1)
@@ -467,6 +471,78 @@ AGB_API agb_status agb_geometry_create(agb_context* ctx, const float* positions,
     }
     uint32_t ntri = index_count / 3;
     std::unique_ptr<Geometry> g(new Geometry());
+    if (ctx->bvhBuilder == AGB_BVH_GPU)
+    {
+        for (int k = 0; k < 3; k++)
+        {
+            g->bounds[k]     = INFINITY;
+            g->bounds[3 + k] = -INFINITY;
+        }
+        for (uint32_t v = 0; v < vertex_count; v++)
+            for (int k = 0; k < 3; k++)
+            {
+                float x = positions[3 * size_t(v) + k];
+                if (!std::isfinite(x))
+                    return fail(AGB_ERR_INVALID_ARG, "agb_geometry_create: non-finite position");
+            }
+        for (uint32_t i = 0; i < index_count; i++)
+            for (int k = 0; k < 3; k++)
+            {
+                float x          = positions[3 * size_t(idx[i]) + k];
+                g->bounds[k]     = std::min(g->bounds[k], x);
+                g->bounds[3 + k] = std::max(g->bounds[3 + k], x);
+            }
+        st = upload(ctx, g->positions, positions, size_t(vertex_count) * 3 * sizeof(float), "upload positions");
+        if (!st && normals)
+            st = upload(ctx, g->normals, normals, size_t(vertex_count) * 3 * sizeof(float), "upload normals");
+        if (!st && texcoords)
+            st = upload(ctx, g->texcoords, texcoords, size_t(vertex_count) * 2 * sizeof(float), "upload texcoords");
+        if (!st)
+            st = upload(ctx, g->indices, idx.data(), idx.size() * sizeof(uint32_t), "upload indices");
+        if (st)
+            return st;
+        AGB_CUDA(g->tris.ensure(size_t(ntri) * 3 * sizeof(float4)), "allocate triangles");
+        GpuBvhScratch& s = ctx->bvhScratch;
+        size_t capNodes  = std::max<size_t>(1, ntri);
+        if (s.nodesBytes < capNodes * sizeof(BNode))
+        {
+            cudaFree(s.nodes);
+            s.nodes      = nullptr;
+            s.nodesBytes = 0;
+            AGB_CUDA(cudaMalloc(&s.nodes, capNodes * sizeof(BNode)), "allocate BVH scratch");
+            s.nodesBytes = capNodes * sizeof(BNode);
+        }
+        int32_t root = 0, depth = 0;
+        uint32_t nodeCount = 0;
+        AGB_CUDA(buildBlasGpu(g->positions.as<float>(), g->indices.as<uint32_t>(), ntri, 34, s, s.nodes,
+                     uint32_t(capNodes), g->tris.as<float4>(), &root, &depth, &nodeCount, ctx->stream),
+            "agb_geometry_create: GPU BVH build");
+        if (depth > 34)
+            return fail(AGB_ERR_LIMIT, "agb_geometry_create: BLAS deeper than the traversal stack allows");
+        if (nodeCount)
+        {
+            AGB_CUDA(g->nodes.ensure(size_t(nodeCount) * sizeof(BNode)), "allocate BVH");
+            AGB_CUDA(cudaMemcpyAsync(g->nodes.ptr, s.nodes, size_t(nodeCount) * sizeof(BNode),
+                         cudaMemcpyDeviceToDevice, ctx->stream),
+                "copy BVH");
+        }
+        AGB_CUDA(cudaStreamSynchronize(ctx->stream), "upload geometry");
+        DevMesh& m      = g->mesh;
+        m.positions     = g->positions.as<float>();
+        m.normals       = normals ? g->normals.as<float>() : nullptr;
+        m.texcoords     = texcoords ? g->texcoords.as<float>() : nullptr;
+        m.indices       = g->indices.as<uint32_t>();
+        m.tris          = g->tris.as<float4>();
+        m.nodes         = g->nodes.as<BNode>();
+        m.vertexCount   = vertex_count;
+        m.triangleCount = ntri;
+        m.root          = root;
+        m.depth         = depth;
+        g->nodeCount    = nodeCount;
+        ctx->geometries.push_back(std::move(g));
+        *out_geometry = int32_t(ctx->geometries.size() - 1);
+        return rebuildMeshTable(ctx);
+    }
     for (int k = 0; k < 3; k++)
     {
         g->bounds[k]     = INFINITY;
@@ -538,9 +614,46 @@ AGB_API agb_status agb_geometry_create(agb_context* ctx, const float* positions,
     m.triangleCount = ntri;
     m.root          = bvh.root;
     m.depth         = bvh.depth;
+    g->nodeCount    = uint32_t(bvh.nodes.size());
     ctx->geometries.push_back(std::move(g));
     *out_geometry = int32_t(ctx->geometries.size() - 1);
     return rebuildMeshTable(ctx);
+}
+
+AGB_API agb_status agb_set_bvh_builder(agb_context* ctx, int32_t builder)
+{
+    if (!ctx || (builder != AGB_BVH_HOST && builder != AGB_BVH_GPU))
+        return fail(AGB_ERR_INVALID_ARG, "agb_set_bvh_builder: bad builder");
+    ctx->bvhBuilder = builder;
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_geometry_bvh(agb_context* ctx, int32_t geometry, float* nodes_out,
+    uint64_t node_capacity, float* tris_out, uint64_t tri_capacity, int32_t* root, int32_t* depth,
+    uint32_t* node_count)
+{
+    if (!ctx || geometry < 0 || geometry >= int32_t(ctx->geometries.size()))
+        return fail(AGB_ERR_INVALID_ARG, "agb_geometry_bvh: bad geometry");
+    const Geometry& g = *ctx->geometries[geometry];
+    if ((nodes_out && node_capacity < g.nodeCount) || (tris_out && tri_capacity < g.mesh.triangleCount))
+        return fail(AGB_ERR_INVALID_ARG, "agb_geometry_bvh: output too small");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    if (nodes_out && g.nodeCount)
+        AGB_CUDA(cudaMemcpyAsync(nodes_out, g.nodes.ptr, size_t(g.nodeCount) * sizeof(BNode), cudaMemcpyDeviceToHost,
+                     ctx->stream), "agb_geometry_bvh");
+    if (tris_out)
+        AGB_CUDA(cudaMemcpyAsync(tris_out, g.tris.ptr, size_t(g.mesh.triangleCount) * 3 * sizeof(float4),
+                     cudaMemcpyDeviceToHost, ctx->stream), "agb_geometry_bvh");
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "agb_geometry_bvh");
+    if (root)
+        *root = g.mesh.root;
+    if (depth)
+        *depth = g.mesh.depth;
+    if (node_count)
+        *node_count = g.nodeCount;
+    return AGB_OK;
 }
 
 AGB_API agb_status agb_image_create(agb_context* ctx, const void* pixels, uint32_t width,

@@ -214,6 +214,31 @@ private:
 cudaError_t launchDenoiseFeatures(const float4* mean, const float2* moments, float samples, const float4* albedo,
     const float4* normal, const float* depth, float skyZ, long P, uint16_t* out, cudaStream_t st);
 
+// agb_bvh_gpu.cu: binned-SAH BLAS build on the GPU.
+struct GpuBvhScratch
+{
+    float* boxes      = nullptr;
+    size_t boxesBytes = 0;
+    uint32_t* order   = nullptr;
+    size_t orderBytes = 0;
+    uint32_t* scratch = nullptr;
+    size_t scratchBytes = 0;
+    void* tasksA      = nullptr;
+    size_t tasksABytes = 0;
+    void* tasksB      = nullptr;
+    size_t tasksBBytes = 0;
+    void* counters    = nullptr;
+    size_t countersBytes = 0;
+    BNode* nodes      = nullptr;
+    size_t nodesBytes = 0;
+};
+// positions / indices: device arrays of the mesh.  Writes up to nodeCapacity nodes, the triangles
+// in leaf order (3 float4 each), the root ref, the depth and the interior node count.
+cudaError_t buildBlasGpu(const float* positions, const uint32_t* indices, uint32_t ntri, int maxDepth,
+    GpuBvhScratch& s, BNode* nodes, uint32_t nodeCapacity, float4* tris, int32_t* rootOut, int32_t* depthOut,
+    uint32_t* nodeCountOut, cudaStream_t st);
+void freeGpuBvhScratch(GpuBvhScratch& s);
+
 // agb_unit.cu
 cudaError_t launchBsdfBatch(int op, const agb_material* mats, const int32_t* matIndex,
     const float* frames, const float* V, const float* L, const float* rnd, int64_t n,

@@ -329,6 +329,24 @@ AGB_API agb_status agb_geometry_create(agb_context* ctx, const float* positions,
     const float* normals, const float* texcoords, const uint32_t* indices, uint32_t vertex_count,
     uint32_t index_count, int32_t* out_geometry);
 
+/* BLAS builder used by agb_geometry_create: AGB_BVH_GPU (default) builds on the GPU (binned SAH,
+ * breadth-first, one CTA per node); AGB_BVH_HOST builds on the host (binned SAH, depth first).
+ * Both produce the same node layout and depth bound; any valid BVH gives the same hits. */
+enum
+{
+    AGB_BVH_HOST = 0,
+    AGB_BVH_GPU  = 1
+};
+AGB_API agb_status agb_set_bvh_builder(agb_context* ctx, int32_t builder);
+/* Reads a geometry's BLAS back (tests, tools): nodes (16 floats each: child 0 x lo / hi, y lo / hi;
+ * child 1 the same; z lo / hi of both children; the two child refs as int bits, 2 unused), the
+ * triangles in leaf order (12 floats each: v0 with the triangle id as int bits in w, v1, v2),
+ * the root ref (a node index, or a leaf ref ~(first << 3 | count - 1)), depth and node count.
+ * Either array may be null. */
+AGB_API agb_status agb_geometry_bvh(agb_context* ctx, int32_t geometry, float* nodes_out,
+    uint64_t node_capacity, float* tris_out, uint64_t tri_capacity, int32_t* root, int32_t* depth,
+    uint32_t* node_count);
+
 /* Uploads an image (material texture or environment).  Host pixels, rows top to bottom.
  * linear: 1 bilinear, 0 nearest filtering (repeat addressing). */
 AGB_API agb_status agb_image_create(agb_context* ctx, const void* pixels, uint32_t width,
