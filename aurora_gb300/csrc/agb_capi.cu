@@ -86,6 +86,10 @@ struct Geometry
     DevBuf positions, normals, texcoords, indices, tris, nodes;
     DevMesh mesh{};
     uint32_t nodeCount = 0;
+    // Boxes that together cover the mesh (6 floats each): the child boxes of the BLAS's top
+    // levels.  Instance boxes are built from them, which is much tighter than the mesh box for
+    // rotated instances.
+    std::vector<float> cover;
     float bounds[6]; // lo, hi in object space
 };
 
@@ -283,6 +287,44 @@ agb_status ensureAccum(agb_context* ctx, uint32_t W, uint32_t H)
     ctx->accH = H;
     ctx->accumulatedSamples = 0;
     return AGB_OK;
+}
+
+// Collects the child boxes of the BLAS down to kCoverDepth levels (or to a leaf, or to a node that
+// is not among the `avail` nodes at hand) into out; a mesh whose root is a leaf keeps its bounds.
+void coverBoxes(const BNode* nodes, uint32_t avail, int32_t root, const float* bounds, std::vector<float>& out)
+{
+    const int kCoverDepth = 5;
+    out.clear();
+    if (root < 0 || uint32_t(root) >= avail)
+    {
+        out.assign(bounds, bounds + 6);
+        return;
+    }
+    struct Item
+    {
+        int32_t node;
+        int depth;
+    };
+    std::vector<Item> stack = { { root, 0 } };
+    while (!stack.empty())
+    {
+        Item it = stack.back();
+        stack.pop_back();
+        const BNode& n = nodes[it.node];
+        for (int side = 0; side < 2; side++)
+        {
+            int32_t ref     = side == 0 ? n.ref.x : n.ref.y;
+            const float4 xy = side == 0 ? n.c0xy : n.c1xy;
+            float z0 = side == 0 ? n.cz.x : n.cz.z, z1 = side == 0 ? n.cz.y : n.cz.w;
+            if (ref >= 0 && uint32_t(ref) < avail && it.depth + 1 < kCoverDepth)
+                stack.push_back({ ref, it.depth + 1 });
+            else
+            {
+                const float b[6] = { xy.x, xy.z, z0, xy.y, xy.w, z1 };
+                out.insert(out.end(), b, b + 6);
+            }
+        }
+    }
 }
 
 agb_status rebuildMeshTable(agb_context* ctx)
@@ -514,10 +556,10 @@ AGB_API agb_status agb_geometry_create(agb_context* ctx, const float* positions,
         }
         int32_t root = 0, depth = 0;
         uint32_t nodeCount = 0;
-        AGB_CUDA(buildBlasGpu(g->positions.as<float>(), g->indices.as<uint32_t>(), ntri, 34, s, s.nodes,
+        AGB_CUDA(buildBlasGpu(g->positions.as<float>(), g->indices.as<uint32_t>(), ntri, kBlasMaxDepth, s, s.nodes,
                      uint32_t(capNodes), g->tris.as<float4>(), &root, &depth, &nodeCount, ctx->stream),
             "agb_geometry_create: GPU BVH build");
-        if (depth > 34)
+        if (depth > kBlasMaxDepth)
             return fail(AGB_ERR_LIMIT, "agb_geometry_create: BLAS deeper than the traversal stack allows");
         if (nodeCount)
         {
@@ -526,7 +568,14 @@ AGB_API agb_status agb_geometry_create(agb_context* ctx, const float* positions,
                          cudaMemcpyDeviceToDevice, ctx->stream),
                 "copy BVH");
         }
+        // The builder numbers nodes level by level, so the first ones are the top of the tree.
+        std::vector<BNode> top(std::min<uint32_t>(nodeCount, 255));
+        if (!top.empty())
+            AGB_CUDA(cudaMemcpyAsync(top.data(), s.nodes, top.size() * sizeof(BNode), cudaMemcpyDeviceToHost,
+                         ctx->stream),
+                "read BVH top");
         AGB_CUDA(cudaStreamSynchronize(ctx->stream), "upload geometry");
+        coverBoxes(top.data(), uint32_t(top.size()), root, g->bounds, g->cover);
         DevMesh& m      = g->mesh;
         m.positions     = g->positions.as<float>();
         m.normals       = normals ? g->normals.as<float>() : nullptr;
@@ -575,8 +624,8 @@ AGB_API agb_status agb_geometry_create(agb_context* ctx, const float* positions,
         }
     }
     BuiltBVH bvh;
-    buildBVH2(boxes.data(), ntri, 4, 34, bvh);
-    if (bvh.depth > 34)
+    buildBVH2(boxes.data(), ntri, 4, kBlasMaxDepth, bvh);
+    if (bvh.depth > kBlasMaxDepth)
         return fail(AGB_ERR_LIMIT, "agb_geometry_create: BLAS deeper than the traversal stack allows");
     std::vector<float4> tris(size_t(ntri) * 3);
     for (uint32_t s = 0; s < ntri; s++)
@@ -615,6 +664,7 @@ AGB_API agb_status agb_geometry_create(agb_context* ctx, const float* positions,
     m.root          = bvh.root;
     m.depth         = bvh.depth;
     g->nodeCount    = uint32_t(bvh.nodes.size());
+    coverBoxes(bvh.nodes.data(), uint32_t(bvh.nodes.size()), bvh.root, g->bounds, g->cover);
     ctx->geometries.push_back(std::move(g));
     *out_geometry = int32_t(ctx->geometries.size() - 1);
     return rebuildMeshTable(ctx);
@@ -786,16 +836,20 @@ AGB_API agb_status agb_instances_set(agb_context* ctx, const agb_instance* inst,
             box[k]     = INFINITY;
             box[3 + k] = -INFINITY;
         }
-        for (int c = 0; c < 8; c++)
+        // Union of the transformed corners of the mesh's cover boxes.
+        for (size_t cb = 0; cb < g.cover.size(); cb += 6)
         {
-            float p[3] = { (c & 1) ? g.bounds[3] : g.bounds[0], (c & 2) ? g.bounds[4] : g.bounds[1],
-                (c & 4) ? g.bounds[5] : g.bounds[2] };
-            for (int r = 0; r < 3; r++)
+            const float* gb = &g.cover[cb];
+            for (int c = 0; c < 8; c++)
             {
-                float w = d.o2w[4 * r] * p[0] + d.o2w[4 * r + 1] * p[1] + d.o2w[4 * r + 2] * p[2] +
-                    d.o2w[4 * r + 3];
-                box[r]     = std::min(box[r], w);
-                box[3 + r] = std::max(box[3 + r], w);
+                float p[3] = { (c & 1) ? gb[3] : gb[0], (c & 2) ? gb[4] : gb[1], (c & 4) ? gb[5] : gb[2] };
+                for (int r = 0; r < 3; r++)
+                {
+                    float w = d.o2w[4 * r] * p[0] + d.o2w[4 * r + 1] * p[1] + d.o2w[4 * r + 2] * p[2] +
+                        d.o2w[4 * r + 3];
+                    box[r]     = std::min(box[r], w);
+                    box[3 + r] = std::max(box[3 + r], w);
+                }
             }
         }
         for (int k = 0; k < 3; k++)
@@ -806,7 +860,7 @@ AGB_API agb_status agb_instances_set(agb_context* ctx, const agb_instance* inst,
         }
     }
     BuiltBVH tl;
-    buildBVH2(boxes.data(), count, 1, 12, tl);
+    buildBVH2(boxes.data(), count, 1, kTlasMaxDepth, tl);
     // The traversal enters exactly one instance per TLAS leaf.
     auto singleLeaf = [](int32_t r) { return r >= 0 || ((uint32_t(~r) & 7u) == 0u); };
     if (!singleLeaf(tl.root))

@@ -10,7 +10,10 @@ namespace agb
 {
 
 constexpr int kTraceBlock       = 128; // threads per traversal block
-constexpr int kTraceBlocksPerSM = 8;   // 8 x 128 threads x 48 stack entries x 4 B = 192 KB / SM
+#ifndef AGB_TRACE_BLOCKS
+#define AGB_TRACE_BLOCKS 8
+#endif
+constexpr int kTraceBlocksPerSM = AGB_TRACE_BLOCKS; // x 128 threads x kStackSize entries x 4 B of shared memory per SM
 constexpr int kShadeBlock       = 128;
 #ifndef AGB_SHADE_MIN_BLOCKS
 #define AGB_SHADE_MIN_BLOCKS 16

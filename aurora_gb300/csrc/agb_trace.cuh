@@ -18,7 +18,13 @@
 namespace agb
 {
 
-constexpr int kStackSize = 48; // entries per thread; the BVH builder keeps TLAS + BLAS depth below
+#ifndef AGB_STACK_ENTRIES
+#define AGB_STACK_ENTRIES 48
+#endif
+constexpr int kStackSize = AGB_STACK_ENTRIES; // entries per thread; the BVH builder keeps TLAS + BLAS depth below
+// Depth budgets: TLAS depth 12, one instance-exit marker, one spare entry.
+constexpr int kTlasMaxDepth = 12;
+constexpr int kBlasMaxDepth = kStackSize - kTlasMaxDepth - 2;
 
 struct TraceCounters
 {
