@@ -111,6 +111,7 @@ struct agb_context
     cudaStream_t stream = nullptr;
     bool ownsStream     = false;
     int smCount         = 0;
+    size_t deviceBytes  = 0; // total device memory
     bool counting       = false;
     bool profiling      = false;
     KernelMarks marks;
@@ -211,17 +212,20 @@ agb_status setDevice(agb_context* ctx)
     return AGB_OK;
 }
 
+// Device bytes per path in flight: path state, and the ray / hit / shadow queues.
+constexpr size_t kPathStateBytes = sizeof(uint2) + sizeof(float4) * 7 + sizeof(uint32_t) * 3 +
+                                   sizeof(float4) * kMaxShadowSlots * 2 + sizeof(float4);
+constexpr size_t kPathQueueBytes = 2 * (2 * sizeof(float4) + sizeof(uint32_t)) + sizeof(float4) +
+                                   sizeof(int32_t) + sizeof(uint32_t) * kMaxShadowSlots + sizeof(uint32_t);
+
 // Carves the wave buffers for `paths` paths and `depth` bounces out of a few allocations.
 agb_status ensureWave(agb_context* ctx, size_t paths, int depth, size_t waves)
 {
     if (paths > ctx->pathCapacity)
     {
         size_t P = paths;
-        size_t stateBytes = P * (sizeof(uint2) + sizeof(float4) * 7 + sizeof(uint32_t) * 3 +
-                                    sizeof(float4) * kMaxShadowSlots * 2 + sizeof(float4));
-        size_t queueBytes = P * (2 * (2 * sizeof(float4) + sizeof(uint32_t)) + sizeof(float4) +
-                                    sizeof(int32_t) + sizeof(uint32_t) * kMaxShadowSlots +
-                                    sizeof(uint32_t)) + 1024;
+        size_t stateBytes = P * kPathStateBytes;
+        size_t queueBytes = P * kPathQueueBytes + 1024;
         AGB_CUDA(ctx->pathState.ensure(stateBytes + 4096), "allocate path state");
         AGB_CUDA(ctx->queues.ensure(queueBytes + 4096), "allocate ray queues");
         char* s = ctx->pathState.as<char>();
@@ -372,6 +376,8 @@ AGB_API agb_status agb_context_create(int32_t device, void* cuda_stream, agb_con
     AGB_CUDA(cudaSetDevice(device), "cudaSetDevice");
     AGB_CUDA(cudaDeviceGetAttribute(&ctx->smCount, cudaDevAttrMultiProcessorCount, device),
         "query SM count");
+    size_t freeBytes = 0;
+    AGB_CUDA(cudaMemGetInfo(&freeBytes, &ctx->deviceBytes), "query device memory");
     if (cuda_stream)
         ctx->stream = static_cast<cudaStream_t>(cuda_stream);
     else
@@ -424,6 +430,7 @@ AGB_API agb_status agb_view_create(agb_context* ctx, void* cuda_stream, agb_cont
     v->parent  = ctx;
     v->device  = ctx->device;
     v->smCount = ctx->smCount;
+    v->deviceBytes = ctx->deviceBytes;
     v->envLayout = ctx->envLayout;
     AGB_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     if (cuda_stream)
@@ -1043,9 +1050,25 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
             "is_force_opaque_shadows_enabled as the HGI backend does");
     uint32_t accumMode = opt->accumulation ? opt->accumulation : AGB_ACCUM_RUNNING_MEAN;
     uint32_t pixels    = opt->width * opt->height;
-    uint64_t maxPaths  = opt->max_paths_in_flight ? opt->max_paths_in_flight : (1u << 22);
-    uint32_t spw       = uint32_t(std::max<uint64_t>(1, maxPaths / pixels));
-    spw                = std::min(spw, std::max(1u, sample_count));
+    uint32_t spw = 1;
+    if (opt->max_paths_in_flight)
+    {
+        spw = uint32_t(std::max<uint64_t>(1, opt->max_paths_in_flight / pixels));
+        spw = std::min(spw, std::max(1u, sample_count));
+    }
+    else
+    {
+        // Default wave: the call's samples in as few waves as fit in an eighth of the device's
+        // memory (30 GB for 64 samples of 1920x1080 on a 288 GB device: two waves of 32), split
+        // evenly.  Fewer, larger waves keep every bounce's launch full and pay each launch's
+        // tail once per bounce instead of once per wave and bounce.
+        uint64_t budget = std::max<uint64_t>(pixels, (ctx->deviceBytes / 8) / (kPathStateBytes + kPathQueueBytes));
+        budget          = std::min<uint64_t>(budget, (1ull << 29) - 1);
+        uint32_t most   = uint32_t(std::max<uint64_t>(1, budget / pixels));
+        uint32_t count  = std::max(1u, sample_count);
+        uint32_t n      = (count + most - 1) / most;
+        spw             = (count + n - 1) / n;
+    }
     if (uint64_t(spw) * pixels >= (1ull << 29))
         return fail(AGB_ERR_LIMIT, "agb_render: wave too large");
     uint32_t waves = sample_count ? (sample_count + spw - 1) / spw : 0;

@@ -183,10 +183,11 @@ AGB_D void slab2(const SlabRay& s, float4 c0xy, float4 c1xy, float4 cz, float tm
 // Every outer iteration has three phases with uniform work inside each, so the lanes of a warp run
 // the same instructions together:
 //   node phase      lanes step through internal nodes (TLAS or BLAS).  A lane that reaches a BLAS
-//                   leaf parks it in `leaf` and keeps traversing speculatively; a lane that reaches
-//                   an instance boundary waits.  The phase ends once every lane holds a parked leaf,
+//                   leaf parks it (in `leaf`, then `leaf2`) and keeps traversing speculatively
+//                   until it holds kParkLeaves leaves and reaches another; a lane that reaches an
+//                   instance boundary waits.  The phase ends once every lane holds a parked leaf,
 //                   waits at a boundary or has finished.
-//   leaf phase      lanes with a parked leaf test its triangles.
+//   leaf phase      lanes test the triangles of their parked leaves, one triangle per iteration.
 //   boundary phase  lanes at a TLAS leaf enter its instance (object-space ray, watertight and slab
 //                   setup); lanes at kExitInstance return to the world-space ray and the TLAS.
 // Entering an instance pushes kExitInstance on the shared-memory stack; popping it restores the
@@ -204,10 +205,23 @@ constexpr int32_t kDone = int32_t(0x80000001);
 
 AGB_D bool isLeafRef(int32_t ref) { return ref < 0 && ref != kExitInstance && ref != kDone; }
 
+#ifndef AGB_TRACE_PARK
+#define AGB_TRACE_PARK 2
+#endif
+#ifndef AGB_NODE_EXIT
+#define AGB_NODE_EXIT 8
+#endif
+// Leaves a lane may park before it stops in the node phase (1 or 2).
+constexpr int kParkLeaves = AGB_TRACE_PARK;
+// The node phase also ends once fewer than this many lanes are still searching for their first
+// leaf while some lane holds a parked leaf (0: only when none is searching).
+constexpr int kNodeExitLanes = AGB_NODE_EXIT;
+
 template <bool kAnyHit, bool kCount, class Loader, class Writer>
 AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const Loader& load,
     const Writer& write, int32_t* stack, int stride, TraceCounters& cnt, bool& overflow)
 {
+    static_assert(kParkLeaves == 1 || kParkLeaves == 2, "one or two parked leaves");
     const unsigned FULL = 0xffffffffu;
     const int lane      = threadIdx.x & 31;
     bool active = false, exhausted = false;
@@ -216,7 +230,7 @@ AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const 
     float tmin = 0.f, tmax = 0.f;
     SlabRay sr;
     WtRay wr;
-    int32_t ref = kDone, leaf = 0;
+    int32_t ref = kDone, leaf = 0, leaf2 = 0;
     int sp       = 0;
     int32_t inst = -1;
     const float4* nodes = nullptr;
@@ -250,6 +264,7 @@ AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const 
                     sr       = slabSetup(o, d);
                     ref      = s.instanceCount > 0 ? s.tlasRoot : kDone;
                     leaf     = 0;
+                    leaf2    = 0;
                     sp       = 0;
                     inst     = -1;
                     nodes    = reinterpret_cast<const float4*>(s.tlas);
@@ -265,18 +280,29 @@ AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const 
         if (__all_sync(FULL, exhausted))
             break;
 
-        // Node phase: internal nodes only.  A lane stops at a BLAS leaf (parked in `leaf`; it goes
-        // on speculatively through internal nodes), at an instance boundary (TLAS leaf or
-        // kExitInstance) or at the end of its ray.
+        // Node phase: internal nodes only.  A lane stops at a BLAS leaf once it holds kParkLeaves
+        // parked leaves (until then it parks the leaf and goes on speculatively), at an instance
+        // boundary (TLAS leaf or kExitInstance) or at the end of its ray.
         for (;;)
         {
-            if (active && leaf == 0 && inst >= 0 && isLeafRef(ref))
+            if (active && inst >= 0 && isLeafRef(ref))
             {
-                leaf = ref;
-                ref  = pop();
+                if (leaf == 0)
+                {
+                    leaf = ref;
+                    ref  = pop();
+                }
+                else if (kParkLeaves > 1 && leaf2 == 0)
+                {
+                    leaf2 = ref;
+                    ref   = pop();
+                }
             }
-            bool nodeWork = active && ref >= 0;
-            if (!__any_sync(FULL, nodeWork && leaf == 0))
+            bool nodeWork      = active && ref >= 0;
+            unsigned searching = __ballot_sync(FULL, nodeWork && leaf == 0);
+            if (searching == 0)
+                break;
+            if (kNodeExitLanes > 0 && __popc(searching) < kNodeExitLanes && __any_sync(FULL, leaf != 0))
                 break;
             if (!nodeWork)
                 continue;
@@ -293,7 +319,7 @@ AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const 
                 if (sp >= kStackSize - 1)
                 {
                     overflow = true;
-                    ref = kDone, leaf = 0, sp = 0;
+                    ref = kDone, leaf = leaf2 = 0, sp = 0;
                     continue;
                 }
                 stack[sp * stride] = t0 <= t1 ? refs.y : refs.x;
@@ -306,50 +332,64 @@ AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const 
                 ref = pop();
         }
 
-        // Leaf phase.
+        // Leaf phase: one triangle per lane per iteration over the lanes' parked leaves, so lanes
+        // whose leaves hold different triangle counts do not wait for one another leaf by leaf.
+        uint32_t cur = 0, end = 0;
         if (leaf != 0)
         {
-            uint32_t code  = uint32_t(~leaf);
-            uint32_t first = code >> 3, count = (code & 7u) + 1u;
-            leaf           = 0;
-            for (uint32_t k = 0; k < count; k++)
+            uint32_t code = uint32_t(~leaf);
+            cur           = code >> 3;
+            end           = cur + (code & 7u) + 1u;
+            leaf          = 0;
+        }
+        while (__any_sync(FULL, cur < end))
+        {
+            if (cur >= end)
+                continue;
+            const float4* tp = tris + 3 * size_t(cur);
+            float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+            if (kCount)
+                cnt.tris++;
+            cur++;
+            if (cur == end && leaf2 != 0)
             {
-                const float4* tp = tris + 3 * size_t(first + k);
-                float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-                if (kCount)
-                    cnt.tris++;
-                float t, u, v;
-                if (wtIntersect(wr, a, b, c, tmin, tmax, !kAnyHit && found, t, u, v))
+                uint32_t code = uint32_t(~leaf2);
+                cur           = code >> 3;
+                end           = cur + (code & 7u) + 1u;
+                leaf2         = 0;
+            }
+            float t, u, v;
+            if (wtIntersect(wr, a, b, c, tmin, tmax, !kAnyHit && found, t, u, v))
+            {
+                int32_t prim = __float_as_int(a.w);
+                if (!found || t < tmax || inst < hit.inst || (inst == hit.inst && prim < hit.prim))
                 {
-                    int32_t prim = __float_as_int(a.w);
-                    if (!found || t < tmax || inst < hit.inst || (inst == hit.inst && prim < hit.prim))
-                    {
-                        found    = true;
-                        tmax     = t;
-                        hit.t    = t;
-                        hit.u    = u;
-                        hit.v    = v;
-                        hit.inst = inst;
-                        hit.prim = prim;
-                    }
-                    if (kAnyHit)
-                    {
-                        ref = kDone, sp = 0;
-                        break;
-                    }
+                    found    = true;
+                    tmax     = t;
+                    hit.t    = t;
+                    hit.u    = u;
+                    hit.v    = v;
+                    hit.inst = inst;
+                    hit.prim = prim;
+                }
+                if (kAnyHit)
+                {
+                    ref = kDone, sp = 0;
+                    cur = end = 0;
+                    leaf2     = 0;
                 }
             }
         }
 
         // Instance boundaries, taken together by the lanes that reached one.
-        if (active && leaf == 0 && ref == kExitInstance)
+        if (active && ref == kExitInstance)
         {
             inst  = -1;
             nodes = reinterpret_cast<const float4*>(s.tlas);
             sr    = slabSetup(o, d);
             ref   = pop();
         }
-        else if (active && leaf == 0 && inst < 0 && isLeafRef(ref))
+        else if (active && inst < 0 && isLeafRef(ref))
         {
             // TLAS leaf: one instance (the TLAS is built with single-instance leaves).
             if (sp >= kStackSize - 1)
@@ -375,7 +415,7 @@ AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const 
                 ref   = m.root;
             }
         }
-        if (active && ref == kDone && leaf == 0)
+        if (active && ref == kDone)
         {
             write(rayIdx, found, hit);
             active = false;

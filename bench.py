@@ -51,6 +51,8 @@ def parse_args():
     p.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     p.add_argument("--no-time-to-error", action="store_true", help="skip the time-to-relMSE measurement")
     p.add_argument("--serve-requests", type=int, default=160)
+    p.add_argument("--max-paths", type=int, default=0,
+                   help="paths in flight per wave (0: the library's default)")
     return p.parse_args()
 
 
@@ -380,12 +382,12 @@ def main():
 
     # Counting pass (untimed): node visits and triangle tests of exactly the timed work.
     r.set_counting(True)
-    counted = r.render(0, s.spp, stats=True)
+    counted = r.render(0, s.spp, stats=True, max_paths=args.max_paths)
     r.set_counting(False)
 
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
-        r.render(0, s.spp)
+        r.render(0, s.spp, max_paths=args.max_paths)
     r.set_profiling(True)
     torch.cuda.synchronize()
     if world > 1:
@@ -402,7 +404,7 @@ def main():
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        st = r.render(0, s.spp, stats=True)
+        st = r.render(0, s.spp, stats=True, max_paths=args.max_paths)
         e1.record(stream)
         e1.synchronize()
         step_ms.append(e0.elapsed_time(e1))
@@ -430,7 +432,7 @@ def main():
     for k in range(0 if args.no_e2e else args.warmup + args.steps):
         t0 = time.perf_counter()
         r.set_frame(frame_np)
-        r.render(0, s.spp)
+        r.render(0, s.spp, max_paths=args.max_paths)
         r.read(_abi.ACCUM_KAHAN, out=img_np)
         if k >= args.warmup:
             e2e_s.append(time.perf_counter() - t0)

@@ -264,7 +264,8 @@ typedef struct agb_render_options
     uint32_t width;
     uint32_t height;
     uint32_t accumulation;      /* AGB_ACCUM_* bitmask */
-    uint32_t max_paths_in_flight; /* wave size in paths; 0 = default */
+    uint32_t max_paths_in_flight; /* wave size in paths; 0 = the call's samples in as few waves
+                                     as fit in an eighth of the device's memory */
     int32_t env_filter_linear;  /* environment sampler: 0 nearest (Hgi default), 1 bilinear */
     uint32_t seed_offset;       /* added to the sample index that seeds the random streams, not to
                                    the accumulation index (gSampleData.seedOffset,
