@@ -151,7 +151,20 @@ AGB_D SlabRay slabSetup(v3 o, v3 d)
     s.oinv = v3{ o.x * s.inv.x, o.y * s.inv.y, o.z * s.inv.z };
     return s;
 }
-// Two child boxes of a node against [tmin, tmax]; returns entry distances.
+// Three-operand minimum / maximum (one instruction each on sm_100 and later).
+AGB_D float fmax3f(float a, float b, float c)
+{
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+AGB_D float fmin3f(float a, float b, float c)
+{
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+// Two child boxes of a node against [tmin, tmax] (tmin >= 0); returns entry distances.
 AGB_D void slab2(const SlabRay& s, float4 c0xy, float4 c1xy, float4 cz, float tmin, float tmax,
     bool& h0, bool& h1, float& t0, float& t1)
 {
@@ -159,17 +172,19 @@ AGB_D void slab2(const SlabRay& s, float4 c0xy, float4 c1xy, float4 cz, float tm
     float a0 = fmaf(c0xy.x, s.inv.x, -s.oinv.x), b0 = fmaf(c0xy.y, s.inv.x, -s.oinv.x);
     float a1 = fmaf(c0xy.z, s.inv.y, -s.oinv.y), b1 = fmaf(c0xy.w, s.inv.y, -s.oinv.y);
     float a2 = fmaf(cz.x, s.inv.z, -s.oinv.z), b2 = fmaf(cz.y, s.inv.z, -s.oinv.z);
-    float n0 = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), tmin));
-    float f0 = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tmax));
+    float n0 = fmax3f(fminf(a0, b0), fminf(a1, b1), fmaxf(fminf(a2, b2), tmin));
+    float f0 = fmin3f(fmaxf(a0, b0), fmaxf(a1, b1), fminf(fmaxf(a2, b2), tmax));
     float c0 = fmaf(c1xy.x, s.inv.x, -s.oinv.x), d0 = fmaf(c1xy.y, s.inv.x, -s.oinv.x);
     float c1 = fmaf(c1xy.z, s.inv.y, -s.oinv.y), d1 = fmaf(c1xy.w, s.inv.y, -s.oinv.y);
     float c2 = fmaf(cz.z, s.inv.z, -s.oinv.z), d2 = fmaf(cz.w, s.inv.z, -s.oinv.z);
-    float n1 = fmaxf(fmaxf(fminf(c0, d0), fminf(c1, d1)), fmaxf(fminf(c2, d2), tmin));
-    float f1 = fminf(fminf(fmaxf(c0, d0), fmaxf(c1, d1)), fminf(fmaxf(c2, d2), tmax));
-    // Conservative widening (about 8 ulp relative plus an absolute floor).
-    const float kWiden = 1.0000010f;
-    h0 = n0 * (n0 > 0.f ? 1.f / kWiden : kWiden) <= f0 * (f0 > 0.f ? kWiden : 1.f / kWiden) + 1e-30f;
-    h1 = n1 * (n1 > 0.f ? 1.f / kWiden : kWiden) <= f1 * (f1 > 0.f ? kWiden : 1.f / kWiden) + 1e-30f;
+    float n1 = fmax3f(fminf(c0, d0), fminf(c1, d1), fmaxf(fminf(c2, d2), tmin));
+    float f1 = fmin3f(fmaxf(c0, d0), fmaxf(c1, d1), fminf(fmaxf(c2, d2), tmax));
+    // Conservative widening (about 16 ulp relative plus an absolute floor).  The entry distance
+    // is at least tmin >= 0, so widening the exit distance alone covers both ends: a box whose
+    // exit lies behind the origin (f < 0) is not hit.
+    const float kWiden2 = 1.0000020f;
+    h0 = n0 <= fmaf(f0, kWiden2, 1e-30f);
+    h1 = n1 <= fmaf(f1, kWiden2, 1e-30f);
     t0 = n0;
     t1 = n1;
 }
@@ -203,7 +218,8 @@ constexpr int32_t kExitInstance = int32_t(0x80000000);
 // meshes at most 2^28 triangles.
 constexpr int32_t kDone = int32_t(0x80000001);
 
-AGB_D bool isLeafRef(int32_t ref) { return ref < 0 && ref != kExitInstance && ref != kDone; }
+// Leaf refs are the negative values above kDone (the two most negative values are the markers).
+AGB_D bool isLeafRef(int32_t ref) { return uint32_t(ref) - uint32_t(kDone + 1) < 0x7fffffffu - 1u; }
 
 #ifndef AGB_TRACE_PARK
 #define AGB_TRACE_PARK 2
@@ -211,6 +227,17 @@ AGB_D bool isLeafRef(int32_t ref) { return ref < 0 && ref != kExitInstance && re
 #ifndef AGB_NODE_EXIT
 #define AGB_NODE_EXIT 8
 #endif
+#ifndef AGB_NODE_LOAD256
+#define AGB_NODE_LOAD256 1
+#endif
+// One 32-byte read-only load (two float4) per lane: a node is two of them instead of four 16-byte
+// loads, which halves the L1 wavefronts of the divergent node fetches.  p must be 32-byte aligned.
+AGB_D void ldg256(const float4* p, float4& a, float4& b)
+{
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
 // Leaves a lane may park before it stops in the node phase (1 or 2).
 constexpr int kParkLeaves = AGB_TRACE_PARK;
 // The node phase also ends once fewer than this many lanes are still searching for their first
@@ -307,8 +334,20 @@ AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const 
             if (!nodeWork)
                 continue;
             const float4* np = nodes + 4 * size_t(ref);
-            float4 c0xy = __ldg(np), c1xy = __ldg(np + 1), cz = __ldg(np + 2);
-            int4 refs   = __ldg(reinterpret_cast<const int4*>(np + 3));
+            float4 c0xy, c1xy, cz;
+            int4 refs;
+#if AGB_NODE_LOAD256
+            ldg256(np, c0xy, c1xy);
+            {
+                float4 r4;
+                ldg256(np + 2, cz, r4);
+                refs = make_int4(__float_as_int(r4.x), __float_as_int(r4.y), __float_as_int(r4.z),
+                    __float_as_int(r4.w));
+            }
+#else
+            c0xy = __ldg(np), c1xy = __ldg(np + 1), cz = __ldg(np + 2);
+            refs = __ldg(reinterpret_cast<const int4*>(np + 3));
+#endif
             if (kCount)
                 cnt.nodes++;
             bool h0, h1;

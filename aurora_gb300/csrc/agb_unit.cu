@@ -94,7 +94,7 @@ struct BatchRayLoader
         const float* r = rays + 8 * size_t(i);
         o    = v3{ r[0], r[1], r[2] };
         d    = v3{ r[4], r[5], r[6] };
-        tmin = r[3];
+        tmin = fmaxf(r[3], 0.f); // a negative tmin is taken as 0, as TraceRay requires TMin >= 0
         tmax = r[7];
     }
 };

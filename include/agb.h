@@ -632,7 +632,8 @@ AGB_API agb_status agb_bsdf_batch(int32_t op, const agb_material* materials,
     const float* rnd, int64_t n, float* out_value, float* out_dir, float* out_pdf,
     int32_t* out_lobe, void* cuda_stream);
 
-/* Ray casts against the context's scene: rays 8 floats (origin, tmin, direction, tmax);
+/* Ray casts against the context's scene: rays 8 floats (origin, tmin, direction, tmax; a negative
+ * tmin is taken as 0);
  * out_tuv 3 floats (t or -1, u, v); out_inst_prim 2 ints.  any_hit: occlusion query.  Device. */
 AGB_API agb_status agb_intersect_batch(agb_context* ctx, const float* rays, int64_t n,
     int32_t any_hit, float* out_tuv, int32_t* out_inst_prim);
