@@ -13,7 +13,17 @@ constexpr int kTraceBlock       = 128; // threads per traversal block
 #ifndef AGB_TRACE_BLOCKS
 #define AGB_TRACE_BLOCKS 8
 #endif
-constexpr int kTraceBlocksPerSM = AGB_TRACE_BLOCKS; // x 128 threads x kStackSize entries x 4 B of shared memory per SM
+constexpr int kTraceBlocksPerSM = AGB_TRACE_BLOCKS; // x 128 threads x kSmemStack entries x 4 B of shared memory per SM
+// Dynamic shared memory of a traversal block (its threads' shared-memory stacks).
+constexpr size_t kTraceStackBytes = size_t(kSmemStack) * kTraceBlock * sizeof(int32_t);
+// Shared-memory carveout (percent of the SM's 228 KB) that holds kTraceBlocksPerSM blocks' stacks
+// (plus 1 KB reserved per block); the rest of the SM's L1 / shared storage stays L1 cache.
+inline int traceCarveoutPercent()
+{
+    size_t need = size_t(kTraceBlocksPerSM) * (kTraceStackBytes + 1024);
+    size_t pct  = (need * 100 + 228 * 1024 - 1) / (228 * 1024);
+    return int(pct > 100 ? 100 : pct);
+}
 constexpr int kShadeBlock       = 128;
 #ifndef AGB_SHADE_MIN_BLOCKS
 #define AGB_SHADE_MIN_BLOCKS 16

@@ -749,7 +749,7 @@ void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp
     launches++;
     int cur = 0;
     int depth = f.trace_depth;
-    size_t stackBytes = size_t(kStackSize) * kTraceBlock * sizeof(int32_t);
+    size_t stackBytes = kTraceStackBytes;
     for (int b = 0; b <= depth; b++)
     {
         if (b == depth)
@@ -784,11 +784,16 @@ void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp
 
 void setTraceAttributes()
 {
-    size_t stackBytes = size_t(kStackSize) * kTraceBlock * sizeof(int32_t);
-    cudaFuncSetAttribute(k_trace_closest<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(stackBytes));
-    cudaFuncSetAttribute(k_trace_closest<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(stackBytes));
-    cudaFuncSetAttribute(k_trace_shadow<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(stackBytes));
-    cudaFuncSetAttribute(k_trace_shadow<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(stackBytes));
+    int stackBytes = int(kTraceStackBytes);
+    int carveout   = traceCarveoutPercent();
+    cudaFuncSetAttribute(k_trace_closest<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, stackBytes);
+    cudaFuncSetAttribute(k_trace_closest<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, stackBytes);
+    cudaFuncSetAttribute(k_trace_shadow<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, stackBytes);
+    cudaFuncSetAttribute(k_trace_shadow<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, stackBytes);
+    cudaFuncSetAttribute(k_trace_closest<true>, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
+    cudaFuncSetAttribute(k_trace_closest<false>, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
+    cudaFuncSetAttribute(k_trace_shadow<true>, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
+    cudaFuncSetAttribute(k_trace_shadow<false>, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
 }
 
 } // namespace agb

@@ -22,6 +22,12 @@ namespace agb
 #define AGB_STACK_ENTRIES 48
 #endif
 constexpr int kStackSize = AGB_STACK_ENTRIES; // entries per thread; the BVH builder keeps TLAS + BLAS depth below
+#ifndef AGB_SMEM_STACK
+#define AGB_SMEM_STACK 24
+#endif
+// The first kSmemStack entries live in shared memory, the rest in local memory: a smaller shared
+// stack leaves more of the SM's combined L1 / shared storage to the L1 cache.
+constexpr int kSmemStack = AGB_SMEM_STACK < AGB_STACK_ENTRIES ? AGB_SMEM_STACK : AGB_STACK_ENTRIES;
 // Depth budgets: TLAS depth 12, one instance-exit marker, one spare entry.
 constexpr int kTlasMaxDepth = 12;
 constexpr int kBlasMaxDepth = kStackSize - kTlasMaxDepth - 2;
@@ -264,11 +270,21 @@ AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const 
     const float4* tris  = nullptr;
     RayHit hit;
     bool found = false;
+    int32_t spill[kStackSize > kSmemStack ? kStackSize - kSmemStack : 1];
     auto pop = [&]() -> int32_t {
         if (sp == 0)
             return kDone;
         sp--;
-        return stack[sp * stride];
+        if (kStackSize == kSmemStack || sp < kSmemStack)
+            return stack[sp * stride];
+        return spill[sp - kSmemStack];
+    };
+    auto push = [&](int32_t v) {
+        if (kStackSize == kSmemStack || sp < kSmemStack)
+            stack[sp * stride] = v;
+        else
+            spill[sp - kSmemStack] = v;
+        sp++;
     };
     for (;;)
     {
@@ -361,8 +377,7 @@ AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const 
                     ref = kDone, leaf = leaf2 = 0, sp = 0;
                     continue;
                 }
-                stack[sp * stride] = t0 <= t1 ? refs.y : refs.x;
-                sp++;
+                push(t0 <= t1 ? refs.y : refs.x);
                 ref = t0 <= t1 ? refs.x : refs.y;
             }
             else if (h0 || h1)
@@ -442,8 +457,7 @@ AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const 
                 int32_t ii     = __ldg(s.tlasOrder + first);
                 const DevInstance& in = s.instances[ii];
                 const DevMesh& m      = s.meshes[in.mesh];
-                stack[sp * stride] = kExitInstance;
-                sp++;
+                push(kExitInstance);
                 v3 oo = xfPointRn(in.w2o, o);
                 v3 od = xfVectorRn(in.w2o, d);
                 wr    = wtSetup(oo, od);

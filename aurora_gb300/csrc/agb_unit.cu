@@ -211,7 +211,7 @@ cudaError_t launchIntersectBatch(const DevScene& s, const float* rays, int64_t n
 {
     if (n <= 0)
         return cudaSuccess;
-    size_t smem = size_t(kStackSize) * kTraceBlock * sizeof(int32_t);
+    size_t smem = kTraceStackBytes;
     int64_t blocks = (n + kTraceBlock - 1) / kTraceBlock;
     int grid       = int(blocks < int64_t(smCount) * 8 ? blocks : int64_t(smCount) * 8);
     cudaError_t e = cudaMemsetAsync(work, 0, sizeof(uint32_t), st);
