@@ -6,45 +6,58 @@
 // Arithmetic follows the shader's operation order so FP32 results agree with it to rounding.
 #pragma once
 
+#include "../../include/agb.h"
 #include "agb_math.cuh"
 #include "agb_sheen_lut.cuh"
+
+// Lobe-level functions: out of line by default so that the three Standard Surface entry points
+// share one copy of each (the shading kernel's speed follows its instruction-cache footprint).
+#if defined(AGB_LOBE_INLINE)
+#define AGB_DL __device__ __forceinline__
+#else
+#define AGB_DL static __device__ __noinline__
+#endif
 
 namespace agb
 {
 
-// Material values used during shading (Shaders/Material.slang:20-57).
+// Material values used during shading (Shaders/Material.slang:20-57).  The values a texture or
+// an option can change per hit are held here; the rest are read through `b` from the material
+// block, which every lane shading that material shares in L1 (a per-lane copy of all of them
+// would sit in each thread's local memory).
 struct Mat
 {
-    float base;
+    const agb_material* b;
     v3 baseColor;
-    float diffuseRoughness;
-    float metalness;
-    v3 metalColor;
-    float specular;
-    v3 specularColor;
     float specularRoughness;
-    float specularIOR;
-    float specularAnisotropy;
-    float specularRotation;
-    float transmission;
-    v3 transmissionColor;
-    float subsurface;
-    v3 subsurfaceColor;
-    float sheen;
-    v3 sheenColor;
-    float sheenRoughness;
-    float coat;
-    v3 coatColor;
     float coatRoughness;
-    float coatAnisotropy;
-    float coatRotation;
-    float coatIOR;
-    float coatAffectColor;
-    float coatAffectRoughness;
-    float emission;
     v3 emissionColor;
     v3 opacity;
-    bool thinWalled;
+    AGB_D float base() const { return __ldg(&b->base); }
+    AGB_D float diffuseRoughness() const { return __ldg(&b->diffuse_roughness); }
+    AGB_D float metalness() const { return __ldg(&b->metalness); }
+    AGB_D float specular() const { return __ldg(&b->specular); }
+    AGB_D float specularIOR() const { return __ldg(&b->specular_IOR); }
+    AGB_D float specularAnisotropy() const { return __ldg(&b->specular_anisotropy); }
+    AGB_D float specularRotation() const { return __ldg(&b->specular_rotation); }
+    AGB_D float transmission() const { return __ldg(&b->transmission); }
+    AGB_D float subsurface() const { return __ldg(&b->subsurface); }
+    AGB_D float sheen() const { return __ldg(&b->sheen); }
+    AGB_D float sheenRoughness() const { return __ldg(&b->sheen_roughness); }
+    AGB_D float coat() const { return __ldg(&b->coat); }
+    AGB_D float coatAnisotropy() const { return __ldg(&b->coat_anisotropy); }
+    AGB_D float coatRotation() const { return __ldg(&b->coat_rotation); }
+    AGB_D float coatIOR() const { return __ldg(&b->coat_IOR); }
+    AGB_D float coatAffectColor() const { return __ldg(&b->coat_affect_color); }
+    AGB_D float coatAffectRoughness() const { return __ldg(&b->coat_affect_roughness); }
+    AGB_D float emission() const { return __ldg(&b->emission); }
+    AGB_D v3 specularColor() const { return ldg3(b->specular_color); }
+    AGB_D v3 transmissionColor() const { return ldg3(b->transmission_color); }
+    AGB_D v3 subsurfaceColor() const { return ldg3(b->subsurface_color); }
+    AGB_D v3 sheenColor() const { return ldg3(b->sheen_color); }
+    AGB_D v3 coatColor() const { return ldg3(b->coat_color); }
+    AGB_D bool thinWalled() const { return __ldg(&b->thin_walled) != 0; }
+    AGB_D v3 metalColor() const { return baseColor; } // DefaultMaterial.slang:236
 };
 
 // Shading frame.
@@ -121,7 +134,7 @@ AGB_D float ggxVNDF(v3 V, v3 H, v2 a)
     float G1 = dot(V, H) <= 0.f ? 0.f : 1.f / (1.f + ggxLambda(V, a));
     return D * G1 * VdotH / fabsf(V.z);
 }
-AGB_D v3 sampleGGXVNDF(v3 V, v2 a, v2 r)
+AGB_DL v3 sampleGGXVNDF(v3 V, v2 a, v2 r)
 {
     v3 Vh     = normalize(v3{ a.x * V.x, a.y * V.y, V.z });
     float lsq = Vh.x * Vh.x + Vh.y * Vh.y;
@@ -153,7 +166,7 @@ AGB_D v2 roughnessAniso(float roughness, float anisotropy)
 }
 AGB_D float pow5(float x) { return sqr(sqr(x)) * x; }
 AGB_D v3 mxMix(v3 bg, v3 fg, float w) { return lerp3(bg, fg, clampf(w, 0.f, 1.f)); }
-AGB_D float orenNayar(v3 L, v3 V, v3 N, float NdotL, float roughness)
+AGB_DL float orenNayar(v3 L, v3 V, v3 N, float NdotL, float roughness)
 {
     float LdotV  = dot(L, V);
     float NdotV  = fabsf(dot(N, V));
@@ -164,7 +177,7 @@ AGB_D float orenNayar(v3 L, v3 V, v3 N, float NdotL, float roughness)
     float B      = 0.45f * sigma2 / (sigma2 + 0.09f);
     return A + B * t;
 }
-AGB_D v3 diffuseReflection(v3 L, v3 V, float weight, v3 color, float roughness, v3 N)
+AGB_DL v3 diffuseReflection(v3 L, v3 V, float weight, v3 color, float roughness, v3 N)
 {
     if (weight < kFloatEps || !sameHemi(L, V, N))
         return splat(0.f);
@@ -215,12 +228,12 @@ AGB_D float energyComp(float NdotV, float roughness, float Fss)
     float Ess = dirAlbedo(NdotV, roughness, 1.f, 1.f);
     return 1.f + Fss * (1.f - Ess) / Ess;
 }
-AGB_D v3 energyComp3(float NdotV, float roughness, v3 Fss)
+AGB_DL v3 energyComp3(float NdotV, float roughness, v3 Fss)
 {
     float Ess = dirAlbedo(NdotV, roughness, 1.f, 1.f);
     return splat(1.f) + Fss * (1.f - Ess) / Ess;
 }
-AGB_D v3 dielectricReflection(v3 L, v3 V, float weight, v3 tint, float ior, v2 rough, v3 N,
+AGB_DL v3 dielectricReflection(v3 L, v3 V, float weight, v3 tint, float ior, v2 rough, v3 N,
     v3 X, v3 base)
 {
     if (weight < kFloatEps)
@@ -264,7 +277,7 @@ AGB_D v3 fresnelConductor(float c, v3 n, v3 k)
     v3 rp    = (rpa - nc2) / (rpa + nc2);
     return (rs + rp) * 0.5f;
 }
-AGB_D v3 conductorReflection(v3 L, v3 V, float weight, v3 refl, v3 edge, v2 rough, v3 N, v3 X)
+AGB_DL v3 conductorReflection(v3 L, v3 V, float weight, v3 refl, v3 edge, v2 rough, v3 N, v3 X)
 {
     if (weight < kFloatEps || !sameHemi(L, V, N))
         return splat(0.f);
@@ -303,7 +316,7 @@ AGB_D float sheenAlbedo(float cosTheta, float roughness)
     float v2_ = lerpf(agb_sheen_albedo_lut[iy2 * 16 + ix], agb_sheen_albedo_lut[iy2 * 16 + ix2], fx);
     return clampf(lerpf(v1, v2_, fy), 0.f, 1.f);
 }
-AGB_D v3 sheenReflection(v3 L, v3 V, float weight, v3 color, float roughness, v3 N, v3 base)
+AGB_DL v3 sheenReflection(v3 L, v3 V, float weight, v3 color, float roughness, v3 N, v3 base)
 {
     if (weight < kFloatEps)
         return base;
@@ -319,7 +332,7 @@ AGB_D v3 sheenReflection(v3 L, v3 V, float weight, v3 color, float roughness, v3
     float dA    = sheenAlbedo(NdotV, alpha);
     return fr * NdotL * weight + base * (1.f - dA * weight);
 }
-AGB_D v3 sheenLayer(v3 L, v3 V, float weight, v3 color, float roughness, v3 N)
+AGB_DL v3 sheenLayer(v3 L, v3 V, float weight, v3 color, float roughness, v3 N)
 {
     if (!sameHemi(L, V, N))
         return splat(0.f);
@@ -334,7 +347,7 @@ AGB_D v3 sheenLayer(v3 L, v3 V, float weight, v3 color, float roughness, v3 N)
     v3 fr       = color * D / (4.f * (NdotL + NdotV - NdotL * NdotV));
     return fr * NdotL * weight;
 }
-AGB_D v3 subsurfaceReflection(v3 L, v3 V, float weight, v3 color, v3 N)
+AGB_DL v3 subsurfaceReflection(v3 L, v3 V, float weight, v3 color, v3 N)
 {
     float NdotL = dot(L, -N);
     if (NdotL <= 0.f || weight < kFloatEps)
@@ -359,7 +372,7 @@ AGB_D v3 rotateVector(v3 v, float degrees, v3 axis)
         oc * axis.z * axis.z + c };
     return v3{ dot(r0, v), dot(r1, v), dot(r2, v) };
 }
-AGB_D v3 dielectricDiffuseLayer(v3 L, v3 V, float weight, float ior, v2 rough, v3 N, v3 albedo)
+AGB_DL v3 dielectricDiffuseLayer(v3 L, v3 V, float weight, float ior, v2 rough, v3 N, v3 albedo)
 {
     if (weight < kFloatEps || !sameHemi(L, V, N))
         return splat(0.f);
@@ -373,7 +386,7 @@ AGB_D v3 dielectricDiffuseLayer(v3 L, v3 V, float weight, float ior, v2 rough, v
     float dA    = dirAlbedo(NdotV, avgR, F0, 1.f) * comp;
     return divPi(splat(1.f - dA) * albedo * weight);
 }
-AGB_D v3 dielectricSpecularLayer(v3 L, v3 V, v3 tint, float ior, v2 rough, v3 N, v3 X)
+AGB_DL v3 dielectricSpecularLayer(v3 L, v3 V, v3 tint, float ior, v2 rough, v3 N, v3 X)
 {
     if (!sameHemi(L, V, N))
         return splat(0.f);
@@ -404,48 +417,47 @@ struct MatCommon
 AGB_D MatCommon prepare(const Mat& m, const Frame& f)
 {
     MatCommon c;
-    float carf = m.coatAffectRoughness * m.coat * m.coatRoughness;
+    float carf = m.coatAffectRoughness() * m.coat() * m.coatRoughness;
     float car  = lerpf(m.specularRoughness, 1.f, carf);
-    float gamma = clampf(m.coat, 0.f, 1.f) * m.coatAffectColor + 1.f;
-    c.subsurfaceColor = pow3(m.subsurfaceColor, gamma);
-    c.mainRough       = roughnessAniso(car, m.specularAnisotropy);
-    c.mainTangent     = rotateVector(f.X, m.specularRotation * 360.f, f.N);
-    c.coatTangent     = rotateVector(f.X, m.coatRotation * 360.f, f.N);
+    float gamma = clampf(m.coat(), 0.f, 1.f) * m.coatAffectColor() + 1.f;
+    c.subsurfaceColor = pow3(m.subsurfaceColor(), gamma);
+    c.mainRough       = roughnessAniso(car, m.specularAnisotropy());
+    c.mainTangent     = rotateVector(f.X, m.specularRotation() * 360.f, f.N);
+    c.coatTangent     = rotateVector(f.X, m.coatRotation() * 360.f, f.N);
     c.diffuseColor    = pow3(m.baseColor, gamma);
     return c;
 }
 
 // evaluateMaterial (StandardSurfaceBSDF.slang:598-718): BSDF x cosine for world V, L.
-AGB_DN v3 evaluateMaterial(const Mat& m, const Frame& f, v3 Vw, v3 Lw)
+AGB_DN v3 evaluateMaterial(const Mat& m, const MatCommon& c, const Frame& f, v3 Vw, v3 Lw)
 {
-    MatCommon c = prepare(m, f);
-    v3 dif      = diffuseReflection(Lw, Vw, m.base, c.diffuseColor, m.diffuseRoughness, f.N);
+    v3 dif      = diffuseReflection(Lw, Vw, m.base(), c.diffuseColor, m.diffuseRoughness(), f.N);
     v3 ssMix    = dif;
-    if (m.subsurface > 0.f)
-        ssMix = mxMix(dif, subsurfaceReflection(Lw, Vw, 1.f, c.subsurfaceColor, f.N), m.subsurface);
+    if (m.subsurface() > 0.f)
+        ssMix = mxMix(dif, subsurfaceReflection(Lw, Vw, 1.f, c.subsurfaceColor, f.N), m.subsurface());
     if (dot(f.N, Vw) * dot(f.N, Lw) < 0.f)
         return ssMix;
     v3 sd = ssMix;
-    if (m.sheen > 0.f)
-        sd = sheenReflection(Lw, Vw, m.sheen, m.sheenColor, m.sheenRoughness, f.N, ssMix);
-    sd *= 1.f - m.transmission;
+    if (m.sheen() > 0.f)
+        sd = sheenReflection(Lw, Vw, m.sheen(), m.sheenColor(), m.sheenRoughness(), f.N, ssMix);
+    sd *= 1.f - m.transmission();
     v3 spec = sd;
-    if (m.specular > 0.f)
-        spec = dielectricReflection(Lw, Vw, m.specular, m.specularColor, m.specularIOR,
+    if (m.specular() > 0.f)
+        spec = dielectricReflection(Lw, Vw, m.specular(), m.specularColor(), m.specularIOR(),
             c.mainRough, f.N, c.mainTangent, sd);
     v3 metalMix = spec;
-    if (m.metalness > 0.f)
+    if (m.metalness() > 0.f)
     {
-        v3 metal = conductorReflection(Lw, Vw, 1.f, m.metalColor * m.base,
-            m.specularColor * m.specular, c.mainRough, f.N, c.mainTangent);
-        metalMix = mxMix(spec, metal, m.metalness);
+        v3 metal = conductorReflection(Lw, Vw, 1.f, m.metalColor() * m.base(),
+            m.specularColor() * m.specular(), c.mainRough, f.N, c.mainTangent);
+        metalMix = mxMix(spec, metal, m.metalness());
     }
     v3 fin = metalMix;
-    if (m.coat > 0.f)
+    if (m.coat() > 0.f)
     {
-        v2 cr   = roughnessAniso(m.coatRoughness, m.coatAnisotropy);
-        v3 att  = lerp3(splat(1.f), m.coatColor, m.coat);
-        fin     = dielectricReflection(Lw, Vw, m.coat, m.coatColor, m.coatIOR, cr, f.N,
+        v2 cr   = roughnessAniso(m.coatRoughness, m.coatAnisotropy());
+        v3 att  = lerp3(splat(1.f), m.coatColor(), m.coat());
+        fin     = dielectricReflection(Lw, Vw, m.coat(), m.coatColor(), m.coatIOR(), cr, f.N,
             c.coatTangent, att * metalMix);
     }
     return fin;
@@ -456,7 +468,7 @@ AGB_D float ggxPdfForL(v3 V, v2 alpha, v3 L)
     v3 H = normalize(V + L);
     return ggxVNDF(V, H, alpha) / (4.f * dot(V, H));
 }
-AGB_D v3 sampleGGXLight(const Frame& f, v3 V, v2 alpha, v2 r, v3& Lw, float& pdf)
+AGB_DL v3 sampleGGXLight(const Frame& f, v3 V, v2 alpha, v2 r, v3& Lw, float& pdf)
 {
     bool flip = V.z <= 0.f;
     v3 H      = sampleGGXVNDF(flip ? -V : V, alpha, r);
@@ -470,7 +482,7 @@ AGB_D v3 sampleHemiTangent(v3 V, v2 r, float& pdf)
 {
     return sampleHemisphereAbout(r, v3{ 0.f, 0.f, V.z > 0.f ? 1.f : -1.f }, pdf);
 }
-AGB_D v3 computeRefraction(v3 V, float ior, bool& reflected)
+AGB_DL v3 computeRefraction(v3 V, float ior, bool& reflected)
 {
     reflected     = false;
     bool entering = V.z > 0.f;
@@ -486,7 +498,7 @@ AGB_D v3 computeRefraction(v3 V, float ior, bool& reflected)
 }
 
 // evaluateMaterialAndPDF (StandardSurfaceBSDF.slang:862-1088).
-AGB_DN v3 evaluateMaterialAndPDF(const Mat& m, const Frame& f, v3 Vw, v3 Lw, v2 rnd, float& pdf,
+AGB_DN v3 evaluateMaterialAndPDF(const Mat& m, const MatCommon& c, const Frame& f, v3 Vw, v3 Lw, v2 rnd, float& pdf,
     int& lobe)
 {
     v3 V        = toTangent(Vw, f);
@@ -494,70 +506,69 @@ AGB_DN v3 evaluateMaterialAndPDF(const Mat& m, const Frame& f, v3 Vw, v3 Lw, v2 
     float NdotV = fabsf(V.z);
     pdf         = 0.f;
     lobe        = NO_SECONDARY_RAY;
-    MatCommon c = prepare(m, f);
     v3 result;
-    float coatLum = luminance(splat(schlick(NdotV, iorToF0(m.coatIOR))) * m.coat * m.coatColor);
+    float coatLum = luminance(splat(schlick(NdotV, iorToF0(m.coatIOR()))) * m.coat() * m.coatColor());
     if (rnd.x < coatLum)
     {
-        v2 ca  = roughnessAniso(m.coatRoughness, m.coatAnisotropy);
+        v2 ca  = roughnessAniso(m.coatRoughness, m.coatAnisotropy());
         pdf    = ggxPdfForL(V, ca, L);
-        result = dielectricSpecularLayer(Lw, Vw, m.coatColor * m.coat, m.coatIOR, ca, f.N,
+        result = dielectricSpecularLayer(Lw, Vw, m.coatColor() * m.coat(), m.coatIOR(), ca, f.N,
             c.coatTangent);
         lobe   = COAT_LOBE;
     }
     else
     {
         rnd.x   = (rnd.x - coatLum) / (1.f - coatLum);
-        v2 sa   = roughnessAniso(m.specularRoughness, m.specularAnisotropy);
-        if (rnd.x < m.metalness)
+        v2 sa   = roughnessAniso(m.specularRoughness, m.specularAnisotropy());
+        if (rnd.x < m.metalness())
         {
             pdf    = ggxPdfForL(V, sa, L);
-            result = conductorReflection(Lw, Vw, 1.f, m.metalColor * m.base,
-                m.specularColor * m.specular, c.mainRough, f.N, c.mainTangent);
+            result = conductorReflection(Lw, Vw, 1.f, m.metalColor() * m.base(),
+                m.specularColor() * m.specular(), c.mainRough, f.N, c.mainTangent);
             result /= fabsf(L.z);
             lobe = METAL_LOBE;
         }
         else
         {
-            rnd.x          = (rnd.x - m.metalness) / (1.f - m.metalness);
+            rnd.x          = (rnd.x - m.metalness()) / (1.f - m.metalness());
             float specLum  = luminance(
-                splat(schlick(NdotV, iorToF0(m.specularIOR))) * m.specular * m.specularColor);
+                splat(schlick(NdotV, iorToF0(m.specularIOR()))) * m.specular() * m.specularColor());
             if (rnd.x < specLum)
             {
                 pdf    = ggxPdfForL(V, sa, L);
-                result = dielectricSpecularLayer(Lw, Vw, m.specularColor * m.specular,
-                    m.specularIOR, c.mainRough, f.N, c.mainTangent);
+                result = dielectricSpecularLayer(Lw, Vw, m.specularColor() * m.specular(),
+                    m.specularIOR(), c.mainRough, f.N, c.mainTangent);
                 result /= specLum;
                 lobe = GLOSSY_LOBE;
             }
             else
             {
                 rnd.x            = (rnd.x - specLum) / (1.f - specLum);
-                float sheenAlpha = clampf(m.sheenRoughness, kFloatEps, 1.f);
-                if (rnd.x < m.sheen)
+                float sheenAlpha = clampf(m.sheenRoughness(), kFloatEps, 1.f);
+                if (rnd.x < m.sheen())
                 {
                     v3 H   = normalize(L + V);
-                    result = sheenLayer(Lw, Vw, m.sheen, m.sheenColor, m.sheenRoughness, f.N);
+                    result = sheenLayer(Lw, Vw, m.sheen(), m.sheenColor(), m.sheenRoughness(), f.N);
                     pdf    = sheenNDF(H.z, sheenAlpha);
                     lobe   = SHEEN_LOBE;
                 }
                 else
                 {
                     pdf    = divPi(dot(f.N, Lw));
-                    result = dielectricDiffuseLayer(Lw, Vw, m.base, m.specularIOR, c.mainRough,
+                    result = dielectricDiffuseLayer(Lw, Vw, m.base(), m.specularIOR(), c.mainRough,
                         f.N, c.diffuseColor);
-                    result *= (1.f - sheenAlbedo(NdotV, sheenAlpha) * m.sheen);
+                    result *= (1.f - sheenAlbedo(NdotV, sheenAlpha) * m.sheen());
                     lobe = DIFFUSE_LOBE;
                 }
             }
         }
-        result *= lerp3(splat(1.f), m.coatColor, m.coat);
+        result *= lerp3(splat(1.f), m.coatColor(), m.coat());
     }
     return result * fabsf(L.z);
 }
 
 // sampleMaterial (StandardSurfaceBSDF.slang:1093-1372).
-AGB_DN v3 sampleMaterial(const Mat& m, const Frame& f, v3 Vw, v2 rnd, v3& Lw, float& pdf,
+AGB_DN v3 sampleMaterial(const Mat& m, const MatCommon& c, const Frame& f, v3 Vw, v2 rnd, v3& Lw, float& pdf,
     int& lobe)
 {
     v3 L;
@@ -566,15 +577,14 @@ AGB_DN v3 sampleMaterial(const Mat& m, const Frame& f, v3 Vw, v2 rnd, v3& Lw, fl
     Lw          = v3{ 1.f, 0.f, 0.f };
     pdf         = 0.f;
     lobe        = NO_SECONDARY_RAY;
-    MatCommon c = prepare(m, f);
     v3 result;
-    float coatLum = luminance(splat(schlick(NdotV, iorToF0(m.coatIOR))) * m.coat * m.coatColor);
+    float coatLum = luminance(splat(schlick(NdotV, iorToF0(m.coatIOR()))) * m.coat() * m.coatColor());
     if (rnd.x < coatLum)
     {
         rnd.x  = rnd.x / coatLum;
-        v2 ca  = roughnessAniso(m.coatRoughness, m.coatAnisotropy);
+        v2 ca  = roughnessAniso(m.coatRoughness, m.coatAnisotropy());
         L      = sampleGGXLight(f, V, ca, rnd, Lw, pdf);
-        result = dielectricSpecularLayer(Lw, Vw, m.coatColor * m.coat, m.coatIOR, ca, f.N,
+        result = dielectricSpecularLayer(Lw, Vw, m.coatColor() * m.coat(), m.coatIOR(), ca, f.N,
             c.coatTangent);
         result /= coatLum;
         lobe = COAT_LOBE;
@@ -582,75 +592,89 @@ AGB_DN v3 sampleMaterial(const Mat& m, const Frame& f, v3 Vw, v2 rnd, v3& Lw, fl
     else
     {
         rnd.x = (rnd.x - coatLum) / (1.f - coatLum);
-        v2 sa = roughnessAniso(m.specularRoughness, m.specularAnisotropy);
-        if (rnd.x < m.metalness)
+        v2 sa = roughnessAniso(m.specularRoughness, m.specularAnisotropy());
+        if (rnd.x < m.metalness())
         {
-            rnd.x  = rnd.x / m.metalness;
+            rnd.x  = rnd.x / m.metalness();
             L      = sampleGGXLight(f, V, sa, rnd, Lw, pdf);
-            result = conductorReflection(Lw, Vw, 1.f, m.metalColor * m.base,
-                m.specularColor * m.specular, c.mainRough, f.N, c.mainTangent);
+            result = conductorReflection(Lw, Vw, 1.f, m.metalColor() * m.base(),
+                m.specularColor() * m.specular(), c.mainRough, f.N, c.mainTangent);
             result /= fabsf(L.z);
             lobe = METAL_LOBE;
         }
         else
         {
-            rnd.x         = (rnd.x - m.metalness) / (1.f - m.metalness);
+            rnd.x         = (rnd.x - m.metalness()) / (1.f - m.metalness());
             float specLum = luminance(
-                splat(schlick(NdotV, iorToF0(m.specularIOR))) * m.specular * m.specularColor);
+                splat(schlick(NdotV, iorToF0(m.specularIOR()))) * m.specular() * m.specularColor());
             if (rnd.x < specLum)
             {
                 rnd.x  = rnd.x / specLum;
                 L      = sampleGGXLight(f, V, sa, rnd, Lw, pdf);
-                result = dielectricSpecularLayer(Lw, Vw, m.specularColor * m.specular,
-                    m.specularIOR, c.mainRough, f.N, c.mainTangent);
+                result = dielectricSpecularLayer(Lw, Vw, m.specularColor() * m.specular(),
+                    m.specularIOR(), c.mainRough, f.N, c.mainTangent);
                 result /= specLum;
                 lobe = GLOSSY_LOBE;
             }
             else
             {
                 rnd.x            = (rnd.x - specLum) / (1.f - specLum);
-                float sheenAlpha = clampf(m.sheenRoughness, kFloatEps, 1.f);
-                if (rnd.x < m.sheen)
+                float sheenAlpha = clampf(m.sheenRoughness(), kFloatEps, 1.f);
+                if (rnd.x < m.sheen())
                 {
-                    rnd.x  = rnd.x / m.sheen;
+                    rnd.x  = rnd.x / m.sheen();
                     L      = sampleHemiTangent(V, rnd, pdf);
                     Lw     = toWorld(L, f);
                     v3 H   = normalize(L + V);
-                    result = sheenLayer(Lw, Vw, m.sheen, m.sheenColor, m.sheenRoughness, f.N);
+                    result = sheenLayer(Lw, Vw, m.sheen(), m.sheenColor(), m.sheenRoughness(), f.N);
                     pdf    = sheenNDF(H.z, sheenAlpha);
                     lobe   = SHEEN_LOBE;
                 }
                 else
                 {
-                    rnd.x = (rnd.x - m.sheen) / (1.f - m.sheen);
-                    if (rnd.x < m.transmission)
+                    rnd.x = (rnd.x - m.sheen()) / (1.f - m.sheen());
+                    if (rnd.x < m.transmission())
                     {
                         bool reflected = false;
                         L              = -V;
-                        if (!m.thinWalled)
-                            L = computeRefraction(V, m.specularIOR, reflected);
+                        if (!m.thinWalled())
+                            L = computeRefraction(V, m.specularIOR(), reflected);
                         Lw     = toWorld(L, f);
-                        result = m.transmissionColor;
+                        result = m.transmissionColor();
                         result /= fabsf(L.z);
                         pdf  = 1.f;
                         lobe = reflected ? GLOSSY_LOBE : TRANSMISSION_LOBE;
                     }
                     else
                     {
-                        rnd.x  = (rnd.x - m.transmission) / (1.f - m.transmission);
+                        rnd.x  = (rnd.x - m.transmission()) / (1.f - m.transmission());
                         L      = sampleHemiTangent(V, rnd, pdf);
                         Lw     = toWorld(L, f);
-                        result = dielectricDiffuseLayer(Lw, Vw, m.base, m.specularIOR,
+                        result = dielectricDiffuseLayer(Lw, Vw, m.base(), m.specularIOR(),
                             c.mainRough, f.N, c.diffuseColor);
-                        result *= (1.f - sheenAlbedo(NdotV, sheenAlpha) * m.sheen);
+                        result *= (1.f - sheenAlbedo(NdotV, sheenAlpha) * m.sheen());
                         lobe = DIFFUSE_LOBE;
                     }
                 }
             }
         }
-        result *= lerp3(splat(1.f), m.coatColor, m.coat);
+        result *= lerp3(splat(1.f), m.coatColor(), m.coat());
     }
     return result * fabsf(L.z);
+}
+
+// The entry points with the shared values computed for the call (one shading point, one call).
+AGB_D v3 evaluateMaterial(const Mat& m, const Frame& f, v3 Vw, v3 Lw)
+{
+    return evaluateMaterial(m, prepare(m, f), f, Vw, Lw);
+}
+AGB_D v3 evaluateMaterialAndPDF(const Mat& m, const Frame& f, v3 Vw, v3 Lw, v2 rnd, float& pdf, int& lobe)
+{
+    return evaluateMaterialAndPDF(m, prepare(m, f), f, Vw, Lw, rnd, pdf, lobe);
+}
+AGB_D v3 sampleMaterial(const Mat& m, const Frame& f, v3 Vw, v2 rnd, v3& Lw, float& pdf, int& lobe)
+{
+    return sampleMaterial(m, prepare(m, f), f, Vw, rnd, Lw, pdf, lobe);
 }
 
 } // namespace agb

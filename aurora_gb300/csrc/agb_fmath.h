@@ -21,8 +21,16 @@
 
 #if defined(__CUDACC__)
 #define AGB_FM __host__ __device__ __forceinline__
+// The larger functions (sincos, exp2, log2, pow, atan2) can be kept out of line on the device so
+// that the shading code holds one copy of each instead of one per call site.
+#if defined(AGB_FM_OUTLINE)
+#define AGB_FMX static __host__ __device__ __noinline__
+#else
+#define AGB_FMX __host__ __device__ __forceinline__
+#endif
 #else
 #define AGB_FM inline
+#define AGB_FMX inline
 #endif
 
 namespace agb_fm
@@ -32,7 +40,7 @@ AGB_FM bool finite_(float x) { return x - x == 0.0f; }
 // Sign bit of a non-NaN float (true for -0).
 AGB_FM bool negative_(float x) { return x < 0.0f || (x == 0.0f && 1.0f / x < 0.0f); }
 
-AGB_FM void sincos(float x, float* s, float* c)
+AGB_FMX void sincos(float x, float* s, float* c)
 {
     if (!finite_(x))
     {
@@ -70,7 +78,7 @@ AGB_FM void sincos(float x, float* s, float* c)
     }
 }
 
-AGB_FM float exp2(float x)
+AGB_FMX float exp2(float x)
 {
     if (x != x)
         return x;
@@ -86,7 +94,7 @@ AGB_FM float exp2(float x)
     return ldexpf(p, int(n));
 }
 
-AGB_FM float log2(float x)
+AGB_FMX float log2(float x)
 {
     if (x != x)
         return x;
@@ -110,7 +118,7 @@ AGB_FM float log2(float x)
     return float(e) + ln * 1.442695f;
 }
 
-AGB_FM float pow(float x, float y)
+AGB_FMX float pow(float x, float y)
 {
     if (y == 1.0f)
         return x;
@@ -136,7 +144,7 @@ AGB_FM float atanSmall(float t)
                    t2 * (-6.6666670e-02f + t2 * (5.8823529e-02f + t2 * -5.2631579e-02f))))))));
 }
 
-AGB_FM float atan2(float y, float x)
+AGB_FMX float atan2(float y, float x)
 {
     if (x != x || y != y)
         return x + y;

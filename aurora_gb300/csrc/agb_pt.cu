@@ -190,12 +190,12 @@ __global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_shadow
 
 // -------------------------------------------------------------------------------- shading
 // ShadeFunctions.slang:51-89
-AGB_DN v3 shadeDistantLight(const agb_distant_light& l, const Mat& m,
+AGB_DN v3 shadeDistantLight(const agb_distant_light& l, const Mat& m, const MatCommon& mc,
     const Frame& fr, v3 V, Rng& rng, v3& dirOut)
 {
     v2 r    = random2D(rng);
     v3 L    = sampleCone(r, ld3(l.direction), l.cos_radius);
-    v3 bsdf = evaluateMaterial(m, fr, V, L);
+    v3 bsdf = evaluateMaterial(m, mc, fr, V, L);
     if (isBlack(bsdf))
     {
         dirOut = splat(0.f);
@@ -352,7 +352,7 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
                             wb.aovNormal[pixel] = make_float4(gn.x, gn.y, gn.z,
                                 m.specularRoughness > 0.05f ? m.specularRoughness : 0.05f);
                             wb.aovAlbedo[pixel] = make_float4(m.baseColor.x, m.baseColor.y,
-                                m.baseColor.z, m.metalness);
+                                m.baseColor.z, m.metalness());
                             wb.aovMotion[pixel] = surfaceMotion(f.camera_view_proj,
                                 f.camera_view_proj_prev, f.camera_inv_view_prev, hw, vz, screen.x,
                                 screen.y);
@@ -380,7 +380,10 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
                             fr.N = matNormal;
                             buildBasis(fr.N, fr.X, fr.Y);
                         }
-                        v3 emission = m.emissionColor * m.emission * lerp3(splat(1.f), m.coatColor, m.coat);
+                        // The Standard Surface values every BSDF call at this point shares
+                        // (each reference call recomputes the same values).
+                        const MatCommon mc = prepare(m, fr);
+                        v3 emission = m.emissionColor * m.emission() * lerp3(splat(1.f), m.coatColor(), m.coat());
                         v3 so = dot(V, fr.N) < 0.f ? sh.geomPosition : sh.position;
                         float4* pslot = wb.pendSlot + size_t(p) * kMaxShadowSlots;
                         float4* pdir  = wb.shDir + size_t(p) * kMaxShadowSlots;
@@ -392,7 +395,7 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
                                 if (f.distant_lights[l].color_and_intensity[3] <= 0.f)
                                     continue;
                                 v3 sd;
-                                v3 r = shadeDistantLight(f.distant_lights[l], m, fr, V, rng, sd);
+                                v3 r = shadeDistantLight(f.distant_lights[l], m, mc, fr, V, rng, sd);
                                 if (isBlack(r))
                                     continue;
                                 pslot[l] = make_float4(r.x, r.y, r.z, 0.f);
@@ -432,7 +435,7 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
                             if (f.distant_lights[idx].color_and_intensity[3] > 0.f)
                             {
                                 v3 sd;
-                                v3 r = shadeDistantLight(f.distant_lights[idx], m, fr, V, rng, sd);
+                                v3 r = shadeDistantLight(f.distant_lights[idx], m, mc, fr, V, rng, sd);
                                 r    = r / fmaxf_(selPdf, 1e-4f);
                                 if (!isBlack(r))
                                 {
@@ -449,7 +452,7 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
                             v2 rnd = random2D(rng);
                             v3 L;
                             float mpdf;
-                            v3 bsdf = sampleMaterial(m, fr, V, rnd, L, mpdf, misLobe);
+                            v3 bsdf = sampleMaterial(m, mc, fr, V, rnd, L, mpdf, misLobe);
                             if (misLobe != TRANSMISSION_LOBE)
                             {
                                 v3 lr = evaluateEnvironment(s, L, false, pixel2, screen);
@@ -466,7 +469,7 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
                                 float lpdf;
                                 lr = sampleEnvironment(s, rnd, L, lpdf);
                                 int el;
-                                bsdf = evaluateMaterialAndPDF(m, fr, V, L, rnd, mpdf, el);
+                                bsdf = evaluateMaterialAndPDF(m, mc, fr, V, L, rnd, mpdf, el);
                                 if (!isBlack(lr) && !isBlack(bsdf))
                                 {
                                     v3 res = lr * misWeight(lpdf, mpdf) * bsdf / lpdf;
@@ -488,7 +491,7 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
                             v3 L;
                             float pdf;
                             int lobe;
-                            v3 bsdf = sampleMaterial(m, fr, V, random2D(rng), L, pdf, lobe);
+                            v3 bsdf = sampleMaterial(m, mc, fr, V, random2D(rng), L, pdf, lobe);
                             if (isBlack(bsdf))
                                 nextType = NO_SECONDARY_RAY;
                             else

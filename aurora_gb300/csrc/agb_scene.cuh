@@ -216,7 +216,6 @@ AGB_D v3 xfVector(const float* m, v3 v)
     return v3{ m[0] * v.x + m[1] * v.y + m[2] * v.z, m[4] * v.x + m[5] * v.y + m[6] * v.z,
         m[8] * v.x + m[9] * v.y + m[10] * v.z };
 }
-AGB_D v3 ldg3(const float* p) { return v3{ __ldg(p), __ldg(p + 1), __ldg(p + 2) }; }
 AGB_D v3 projectOnPlane(v3 p, v3 o, v3 n) { return p - n * dot(p - o, n); }
 
 // Geometry.slang:152-265, tangent from the up vector (HGI reports no tangents).
@@ -300,35 +299,12 @@ AGB_D Mat loadMaterial(const DevScene& s, int32_t mi, const Shading& sh, v3& mat
 {
     const agb_material& b = s.materials[mi];
     Mat m;
-    m.base               = b.base;
-    m.baseColor          = ld3(b.base_color);
-    m.diffuseRoughness   = b.diffuse_roughness;
-    m.metalness          = b.metalness;
-    m.specular           = b.specular;
-    m.specularColor      = ld3(b.specular_color);
-    m.specularRoughness  = b.specular_roughness;
-    m.specularIOR        = b.specular_IOR;
-    m.specularAnisotropy = b.specular_anisotropy;
-    m.specularRotation   = b.specular_rotation;
-    m.transmission       = b.transmission;
-    m.transmissionColor  = ld3(b.transmission_color);
-    m.subsurface         = b.subsurface;
-    m.subsurfaceColor    = ld3(b.subsurface_color);
-    m.sheen              = b.sheen;
-    m.sheenColor         = ld3(b.sheen_color);
-    m.sheenRoughness     = b.sheen_roughness;
-    m.coat               = b.coat;
-    m.coatColor          = ld3(b.coat_color);
-    m.coatRoughness      = b.coat_roughness;
-    m.coatAnisotropy     = b.coat_anisotropy;
-    m.coatRotation       = b.coat_rotation;
-    m.coatIOR            = b.coat_IOR;
-    m.coatAffectColor    = b.coat_affect_color;
-    m.coatAffectRoughness = b.coat_affect_roughness;
-    m.emission           = b.emission;
-    m.emissionColor      = ld3(b.emission_color);
-    m.opacity            = ld3(b.opacity);
-    m.thinWalled         = b.thin_walled != 0;
+    m.b                 = &b;
+    m.baseColor         = ldg3(b.base_color);
+    m.specularRoughness = __ldg(&b.specular_roughness);
+    m.coatRoughness     = __ldg(&b.coat_roughness);
+    m.emissionColor     = ldg3(b.emission_color);
+    m.opacity           = ldg3(b.opacity);
     v3 rgb;
     if (b.has_base_color_image &&
         materialTexture(s, mi, AGB_TEX_BASE_COLOR, sh.uv, b.base_color_image_pivot,
@@ -358,7 +334,6 @@ AGB_D Mat loadMaterial(const DevScene& s, int32_t mi, const Shading& sh, v3& mat
         materialNormal  = normalize(sh.X * vv.x * 1.f + Bn * vv.y * 1.f + sh.N * vv.z);
         generatedNormal = true;
     }
-    m.metalColor = m.baseColor;
     return m;
 }
 

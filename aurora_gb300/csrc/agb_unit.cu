@@ -12,36 +12,12 @@ namespace
 __device__ Mat matFromBlock(const agb_material& b)
 {
     Mat m;
-    m.base               = b.base;
-    m.baseColor          = ld3(b.base_color);
-    m.diffuseRoughness   = b.diffuse_roughness;
-    m.metalness          = b.metalness;
-    m.specular           = b.specular;
-    m.specularColor      = ld3(b.specular_color);
-    m.specularRoughness  = b.specular_roughness;
-    m.specularIOR        = b.specular_IOR;
-    m.specularAnisotropy = b.specular_anisotropy;
-    m.specularRotation   = b.specular_rotation;
-    m.transmission       = b.transmission;
-    m.transmissionColor  = ld3(b.transmission_color);
-    m.subsurface         = b.subsurface;
-    m.subsurfaceColor    = ld3(b.subsurface_color);
-    m.sheen              = b.sheen;
-    m.sheenColor         = ld3(b.sheen_color);
-    m.sheenRoughness     = b.sheen_roughness;
-    m.coat               = b.coat;
-    m.coatColor          = ld3(b.coat_color);
-    m.coatRoughness      = b.coat_roughness;
-    m.coatAnisotropy     = b.coat_anisotropy;
-    m.coatRotation       = b.coat_rotation;
-    m.coatIOR            = b.coat_IOR;
-    m.coatAffectColor    = b.coat_affect_color;
-    m.coatAffectRoughness = b.coat_affect_roughness;
-    m.emission           = b.emission;
-    m.emissionColor      = ld3(b.emission_color);
-    m.opacity            = ld3(b.opacity);
-    m.thinWalled         = b.thin_walled != 0;
-    m.metalColor         = m.baseColor;
+    m.b                 = &b;
+    m.baseColor         = ld3(b.base_color);
+    m.specularRoughness = b.specular_roughness;
+    m.coatRoughness     = b.coat_roughness;
+    m.emissionColor     = ld3(b.emission_color);
+    m.opacity           = ld3(b.opacity);
     return m;
 }
 
