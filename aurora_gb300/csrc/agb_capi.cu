@@ -216,7 +216,8 @@ agb_status setDevice(agb_context* ctx)
 constexpr size_t kPathStateBytes = sizeof(uint2) + sizeof(float4) * 7 + sizeof(uint32_t) * 3 +
                                    sizeof(float4) * kMaxShadowSlots * 2 + sizeof(float4);
 constexpr size_t kPathQueueBytes = 2 * (2 * sizeof(float4) + sizeof(uint32_t)) + sizeof(float4) +
-                                   sizeof(int32_t) + sizeof(uint32_t) * kMaxShadowSlots + sizeof(uint32_t);
+                                   sizeof(int32_t) + sizeof(uint32_t) * kMaxShadowSlots + sizeof(uint32_t) +
+                                   sizeof(float4) * kShadePointWords;
 
 // Carves the wave buffers for `paths` paths and `depth` bounces out of a few allocations.
 agb_status ensureWave(agb_context* ctx, size_t paths, int depth, size_t waves)
@@ -262,6 +263,7 @@ agb_status ensureWave(agb_context* ctx, size_t paths, int depth, size_t waves)
         w.hitInst     = reinterpret_cast<int32_t*>(take(P * sizeof(int32_t)));
         w.shTag       = reinterpret_cast<uint32_t*>(take(P * kMaxShadowSlots * sizeof(uint32_t)));
         w.resolveList = reinterpret_cast<uint32_t*>(take(P * sizeof(uint32_t)));
+        w.shadePoint  = reinterpret_cast<float4*>(take(P * kShadePointWords * sizeof(float4)));
         if (size_t(s - ctx->queues.as<char>()) > ctx->queues.bytes)
             return fail(AGB_ERR_LIMIT, "internal: queue carve overflow");
         ctx->pathCapacity = P;

@@ -233,6 +233,53 @@ __device__ __forceinline__ void accumulateSegment(WaveBuffers& wb, uint32_t p, i
     *dst        = make_float4(a.x + radiance.x, a.y + radiance.y, a.z + radiance.z, 0.f);
 }
 
+// A shading point handed from k_shade to k_shade_scatter: kShadePointWords float4 per point,
+// stored word-major (word k of point j at k * stride + j) so both kernels access it coalesced.
+AGB_D void storeShadePoint(float4* sp, uint32_t stride, uint32_t j, const Mat& m, int32_t mi,
+    uint32_t slots, uint32_t p, const MatCommon& c, const Frame& fr, v3 V, v3 pos, v3 geomPos)
+{
+    float4* w = sp + j;
+    w[0 * size_t(stride)] = make_float4(m.baseColor.x, m.baseColor.y, m.baseColor.z, m.specularRoughness);
+    w[1 * size_t(stride)] = make_float4(m.coatRoughness, __int_as_float(mi), __uint_as_float(slots),
+        __uint_as_float(p));
+    w[2 * size_t(stride)] = make_float4(c.mainRough.x, c.mainRough.y, c.mainTangent.x, c.mainTangent.y);
+    w[3 * size_t(stride)] = make_float4(c.mainTangent.z, c.coatTangent.x, c.coatTangent.y, c.coatTangent.z);
+    w[4 * size_t(stride)] = make_float4(c.diffuseColor.x, c.diffuseColor.y, c.diffuseColor.z,
+        c.subsurfaceColor.x);
+    w[5 * size_t(stride)] = make_float4(c.subsurfaceColor.y, c.subsurfaceColor.z, V.x, V.y);
+    w[6 * size_t(stride)] = make_float4(V.z, fr.N.x, fr.N.y, fr.N.z);
+    w[7 * size_t(stride)] = make_float4(fr.X.x, fr.X.y, fr.X.z, fr.Y.x);
+    w[8 * size_t(stride)] = make_float4(fr.Y.y, fr.Y.z, pos.x, pos.y);
+    w[9 * size_t(stride)] = make_float4(pos.z, geomPos.x, geomPos.y, geomPos.z);
+}
+AGB_D void loadShadePoint(const DevScene& s, const float4* sp, uint32_t stride, uint32_t j, Mat& m,
+    uint32_t& slots, uint32_t& p, MatCommon& c, Frame& fr, v3& V, v3& pos, v3& geomPos)
+{
+    const float4* w = sp + j;
+    float4 a = w[0], b = w[1 * size_t(stride)], q2 = w[2 * size_t(stride)], q3 = w[3 * size_t(stride)];
+    float4 q4 = w[4 * size_t(stride)], q5 = w[5 * size_t(stride)], q6 = w[6 * size_t(stride)];
+    float4 q7 = w[7 * size_t(stride)], q8 = w[8 * size_t(stride)], q9 = w[9 * size_t(stride)];
+    m.b                 = s.materials + __float_as_int(b.y);
+    m.baseColor         = v3{ a.x, a.y, a.z };
+    m.specularRoughness = a.w;
+    m.coatRoughness     = b.x;
+    m.emissionColor     = splat(0.f); // applied by k_shade
+    m.opacity           = splat(1.f); // applied by k_shade
+    slots               = __float_as_uint(b.z);
+    p                   = __float_as_uint(b.w);
+    c.mainRough         = v2{ q2.x, q2.y };
+    c.mainTangent       = v3{ q2.z, q2.w, q3.x };
+    c.coatTangent       = v3{ q3.y, q3.z, q3.w };
+    c.diffuseColor      = v3{ q4.x, q4.y, q4.z };
+    c.subsurfaceColor   = v3{ q4.w, q5.x, q5.y };
+    V                   = v3{ q5.z, q5.w, q6.x };
+    fr.N                = v3{ q6.y, q6.z, q6.w };
+    fr.X                = v3{ q7.x, q7.y, q7.z };
+    fr.Y                = v3{ q7.w, q8.x, q8.y };
+    pos                 = v3{ q8.z, q8.w, q9.x };
+    geomPos             = v3{ q9.y, q9.z, q9.w };
+}
+
 __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene s, agb_frame_data f,
     WaveParams wp, WaveBuffers wb, int bounce, int cur, int depthLimit)
 {
@@ -249,7 +296,6 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
         uint32_t i     = base + threadIdx.x;
         bool valid     = i < n;
         bool pushNext  = false;
-        bool resolve   = false;
         uint32_t slots = 0;
         uint32_t p     = 0;
         v3 nextO = splat(0.f), nextD = splat(0.f);
@@ -306,13 +352,14 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
                     Shading sh = computeShading(s, in, uint32_t(__float_as_int(h.w)), h.y, h.z);
                     v2 baseUV  = sh.uv;
                     bool hitLayer = false;
+                    int32_t mi    = 0;
                     Mat m;
                     v3 matNormal = sh.N;
                     bool genNormal = false;
                     float P = 0.f;
                     for (int li = in.layerCount; li >= 0; li--)
                     {
-                        int32_t mi;
+                        mi = 0;
                         if (li == 0)
                         {
                             mi    = in.material;
@@ -445,107 +492,169 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
                                 }
                             }
                         }
-                        // Environment MIS (ShadeFunctions.slang:135-259): one random pair for both halves.
-                        int misLobe;
-                        bool mis = false;
-                        {
-                            v2 rnd = random2D(rng);
-                            v3 L;
-                            float mpdf;
-                            v3 bsdf = sampleMaterial(m, mc, fr, V, rnd, L, mpdf, misLobe);
-                            if (misLobe != TRANSMISSION_LOBE)
-                            {
-                                v3 lr = evaluateEnvironment(s, L, false, pixel2, screen);
-                                if (!isBlack(lr) && !isBlack(bsdf))
-                                {
-                                    float lpdf = s.env.has_light_tex && s.envLight.data
-                                        ? luminance(lr) / s.env.light_tex_luminance_integral
-                                        : divPi(0.25f);
-                                    v3 res = lr * misWeight(mpdf, lpdf) * bsdf / mpdf;
-                                    pslot[4] = make_float4(res.x, res.y, res.z, 0.f);
-                                    pdir[4]  = make_float4(L.x, L.y, L.z, 0.f);
-                                    slots |= 1u << 4;
-                                }
-                                float lpdf;
-                                lr = sampleEnvironment(s, rnd, L, lpdf);
-                                int el;
-                                bsdf = evaluateMaterialAndPDF(m, mc, fr, V, L, rnd, mpdf, el);
-                                if (!isBlack(lr) && !isBlack(bsdf))
-                                {
-                                    v3 res = lr * misWeight(lpdf, mpdf) * bsdf / lpdf;
-                                    pslot[5] = make_float4(res.x, res.y, res.z, 0.f);
-                                    pdir[5]  = make_float4(L.x, L.y, L.z, 0.f);
-                                    slots |= 1u << 5;
-                                }
-                                mis = (slots & 0x30u) != 0;
-                            }
-                        }
                         contrib *= m.opacity / (1.f - P);
-                        bool alpha = (flags & PF_ALPHA) != 0;
-                        alpha = !(!alpha && rayType == TRANSMISSION_LOBE);
-                        flags = alpha ? (flags | PF_ALPHA) : (flags & ~PF_ALPHA);
-                        // setupIndirectLightRay (ShadeFunctions.slang:263-310)
-                        int nextType;
-                        v3 nextContrib = splat(1.f);
-                        {
-                            v3 L;
-                            float pdf;
-                            int lobe;
-                            v3 bsdf = sampleMaterial(m, mc, fr, V, random2D(rng), L, pdf, lobe);
-                            if (isBlack(bsdf))
-                                nextType = NO_SECONDARY_RAY;
-                            else
-                            {
-                                bool tr = lobe == TRANSMISSION_LOBE;
-                                nextO = (dot(V, fr.N) < 0.f || tr) ? sh.geomPosition : sh.position;
-                                nextD = L;
-                                nextContrib = bsdf / pdf;
-                                nextType = lobe;
-                            }
-                        }
-                        bool ended = nextType == NO_SECONDARY_RAY;
-                        uint32_t bits = slots;
-                        if (mis)
-                        {
-                            bits |= RS_MIS;
-                            flags = pfSetMisLobe(flags, uint32_t(misLobe));
-                        }
-                        if (bounce == 0)
-                        {
-                            bits |= RS_DEPTH0;
-                            if (pfMisLobe(flags) == DIFFUSE_LOBE)
-                                bits |= RS_DIFFUSE_ROUTE;
-                        }
-                        else if (rayType == DIFFUSE_LOBE)
-                            bits |= RS_DIFFUSE_ROUTE;
-                        wb.pendEmission[p]   = make_float4(emission.x, emission.y, emission.z, 0.f);
-                        wb.pendSegContrib[p] = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
-                        wb.pendBits[p]       = bits;
-                        wb.occluded[p]       = 0u;
-                        if (slots)
-                            wb.shOrg[p] = make_float4(so.x, so.y, so.z, 0.f);
-                        flags &= ~PF_PRIMARY;
-                        if (nextType == TRANSMISSION_LOBE)
-                            flags ^= PF_INSIDE;
-                        contrib *= nextContrib;
-                        if (f.is_russian_roulette_enabled && bounce + 1 >= f.russian_roulette_start_depth)
-                        {
-                            float mx   = fmaxf_(contrib.x, fmaxf_(contrib.y, contrib.z));
-                            float surv = clampf(mx, 0.05f, 1.f);
-                            if (random2D(rng).x > surv)
-                                ended = true;
-                            else
-                                contrib = contrib / surv;
-                        }
-                        flags    = pfSetRayType(flags, uint32_t(nextType));
-                        pushNext = !ended;
-                        resolve  = true;
+                        // Hand the shading point to k_shade_scatter (environment MIS, the next
+                        // ray, Russian roulette), which runs with only those paths in its warps.
+                        wb.pendEmission[p] = make_float4(emission.x, emission.y, emission.z, 0.f);
+                        wb.shOrg[p]        = make_float4(so.x, so.y, so.z, 0.f);
+                        uint32_t j = warpAppend(wb.counters + bounce * kCounterStride + CNT_SCATTER, true);
+                        storeShadePoint(wb.shadePoint, wp.paths, j, m, mi, slots, p, mc, fr, V,
+                            sh.position, sh.geomPosition);
+                        slots = 0;
                     }
                     wb.rng[p]     = make_uint2(rng.x, rng.y);
                     wb.contrib[p] = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
                     wb.flags[p]   = flags;
                 }
             }
+        }
+        // Warp-aggregated append of the straight-through rays (all lanes of the warp reach this
+        // point together).
+        __syncwarp();
+        uint32_t slotNext = warpAppend(wb.counters + (bounce + 1) * kCounterStride + CNT_RAYS, pushNext);
+        if (pushNext)
+        {
+            wb.rayOrg[cur ^ 1][slotNext]  = make_float4(nextO.x, nextO.y, nextO.z, kRayTMin);
+            wb.rayDir[cur ^ 1][slotNext]  = make_float4(nextD.x, nextD.y, nextD.z, __int_as_float(0x7f800000));
+            wb.rayPath[cur ^ 1][slotNext] = p;
+        }
+    }
+}
+
+// Second half of the hit shading: environment MIS, the indirect ray and Russian roulette for
+// the shading points k_shade handed over (ShadeFunctions.slang:135-310,
+// HitShaderEntryPoints.slang:362-486).  Its warps hold only such points, and its code is the
+// sampling half of the BSDF, so both kernels keep a smaller instruction footprint.
+__global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade_scatter(DevScene s,
+    agb_frame_data f, WaveParams wp, WaveBuffers wb, int bounce, int cur)
+{
+    uint32_t n      = wb.counters[bounce * kCounterStride + CNT_SCATTER];
+    uint32_t stride = gridDim.x * blockDim.x;
+    v2 screen = v2{ float(wp.width), float(wp.height) };
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride)
+    {
+        uint32_t j     = base + threadIdx.x;
+        bool valid     = j < n;
+        bool pushNext  = false;
+        bool resolve   = false;
+        uint32_t slots = 0;
+        uint32_t p     = 0;
+        v3 nextO = splat(0.f), nextD = splat(0.f);
+        if (valid)
+        {
+            Mat m;
+            MatCommon mc;
+            Frame fr;
+            v3 V, shPosition, shGeomPosition;
+            loadShadePoint(s, wb.shadePoint, wp.paths, j, m, slots, p, mc, fr, V, shPosition,
+                shGeomPosition);
+            uint32_t flags = wb.flags[p];
+            float4 c4      = wb.contrib[p];
+            v3 contrib     = v3{ c4.x, c4.y, c4.z };
+            uint32_t rayType = pfRayType(flags);
+            uint32_t pixel   = p % wp.pixels;
+            v2 pixel2        = v2{ float(pixel % wp.width), float(pixel / wp.width) };
+            Rng rng;
+            {
+                uint2 r = wb.rng[p];
+                rng     = Rng{ r.x, r.y };
+            }
+            float4* pslot = wb.pendSlot + size_t(p) * kMaxShadowSlots;
+            float4* pdir  = wb.shDir + size_t(p) * kMaxShadowSlots;
+            // Environment MIS (ShadeFunctions.slang:135-259): one random pair for both halves.
+            int misLobe;
+            bool mis = false;
+            {
+                v2 rnd = random2D(rng);
+                v3 L;
+                float mpdf;
+                v3 bsdf = sampleMaterial(m, mc, fr, V, rnd, L, mpdf, misLobe);
+                if (misLobe != TRANSMISSION_LOBE)
+                {
+                    v3 lr = evaluateEnvironment(s, L, false, pixel2, screen);
+                    if (!isBlack(lr) && !isBlack(bsdf))
+                    {
+                        float lpdf = s.env.has_light_tex && s.envLight.data
+                            ? luminance(lr) / s.env.light_tex_luminance_integral
+                            : divPi(0.25f);
+                        v3 res = lr * misWeight(mpdf, lpdf) * bsdf / mpdf;
+                        pslot[4] = make_float4(res.x, res.y, res.z, 0.f);
+                        pdir[4]  = make_float4(L.x, L.y, L.z, 0.f);
+                        slots |= 1u << 4;
+                    }
+                    float lpdf;
+                    lr = sampleEnvironment(s, rnd, L, lpdf);
+                    int el;
+                    bsdf = evaluateMaterialAndPDF(m, mc, fr, V, L, rnd, mpdf, el);
+                    if (!isBlack(lr) && !isBlack(bsdf))
+                    {
+                        v3 res = lr * misWeight(lpdf, mpdf) * bsdf / lpdf;
+                        pslot[5] = make_float4(res.x, res.y, res.z, 0.f);
+                        pdir[5]  = make_float4(L.x, L.y, L.z, 0.f);
+                        slots |= 1u << 5;
+                    }
+                    mis = (slots & 0x30u) != 0;
+                }
+            }
+            bool alpha = (flags & PF_ALPHA) != 0;
+            alpha = !(!alpha && rayType == TRANSMISSION_LOBE);
+            flags = alpha ? (flags | PF_ALPHA) : (flags & ~PF_ALPHA);
+            // setupIndirectLightRay (ShadeFunctions.slang:263-310)
+            int nextType;
+            v3 nextContrib = splat(1.f);
+            {
+                v3 L;
+                float pdf;
+                int lobe;
+                v3 bsdf = sampleMaterial(m, mc, fr, V, random2D(rng), L, pdf, lobe);
+                if (isBlack(bsdf))
+                    nextType = NO_SECONDARY_RAY;
+                else
+                {
+                    bool tr = lobe == TRANSMISSION_LOBE;
+                    nextO = (dot(V, fr.N) < 0.f || tr) ? shGeomPosition : shPosition;
+                    nextD = L;
+                    nextContrib = bsdf / pdf;
+                    nextType = lobe;
+                }
+            }
+            bool ended = nextType == NO_SECONDARY_RAY;
+            uint32_t bits = slots;
+            if (mis)
+            {
+                bits |= RS_MIS;
+                flags = pfSetMisLobe(flags, uint32_t(misLobe));
+            }
+            if (bounce == 0)
+            {
+                bits |= RS_DEPTH0;
+                if (pfMisLobe(flags) == DIFFUSE_LOBE)
+                    bits |= RS_DIFFUSE_ROUTE;
+            }
+            else if (rayType == DIFFUSE_LOBE)
+                bits |= RS_DIFFUSE_ROUTE;
+            wb.pendSegContrib[p] = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
+            wb.pendBits[p]       = bits;
+            wb.occluded[p]       = 0u;
+            flags &= ~PF_PRIMARY;
+            if (nextType == TRANSMISSION_LOBE)
+                flags ^= PF_INSIDE;
+            contrib *= nextContrib;
+            if (f.is_russian_roulette_enabled && bounce + 1 >= f.russian_roulette_start_depth)
+            {
+                float mx   = fmaxf_(contrib.x, fmaxf_(contrib.y, contrib.z));
+                float surv = clampf(mx, 0.05f, 1.f);
+                if (random2D(rng).x > surv)
+                    ended = true;
+                else
+                    contrib = contrib / surv;
+            }
+            flags    = pfSetRayType(flags, uint32_t(nextType));
+            pushNext = !ended;
+            resolve  = true;
+            wb.rng[p]     = make_uint2(rng.x, rng.y);
+            wb.contrib[p] = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
+            wb.flags[p]   = flags;
         }
         // Warp-aggregated queue appends (all lanes of the warp reach this point together).
         __syncwarp();
@@ -769,6 +878,8 @@ void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp
             k_trace_closest<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, cur);
         mark(KC_SHADE);
         k_shade<<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 0);
+        mark(KC_SHADE);
+        k_shade_scatter<<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur);
         mark(KC_SHADOW);
         if (wp.countTraversal)
             k_trace_shadow<true><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b);
@@ -776,7 +887,7 @@ void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp
             k_trace_shadow<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b);
         mark(KC_RESOLVE);
         k_resolve<<<grid, 256, 0, st>>>(f, wb, b);
-        launches += 4;
+        launches += 5;
         cur ^= 1;
     }
     mark(KC_FINALIZE);

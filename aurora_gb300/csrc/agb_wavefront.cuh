@@ -8,6 +8,7 @@
 namespace agb
 {
 
+constexpr int kShadePointWords = 10; // float4 per shading point handed between the shading kernels
 constexpr int kMaxShadowSlots = 6; // up to 4 distant lights + 2 environment-MIS rays per hit
 
 // Per-bounce device counters (kCounterStride words per bounce).
@@ -18,6 +19,7 @@ enum : int
     CNT_RESOLVE       = 2, // paths with a pending record
     CNT_CLOSEST_WORK  = 3, // persistent traversal work counter (closest-hit rays)
     CNT_SHADOW_WORK   = 4, // persistent traversal work counter (shadow rays)
+    CNT_SCATTER       = 5, // shading points handed from k_shade to k_shade_scatter
     kCounterStride    = 8
 };
 
@@ -77,6 +79,7 @@ struct WaveBuffers
     float4* shDir;
     uint32_t* shTag;        // path << 3 | slot
     uint32_t* resolveList;  // paths with a pending record this bounce
+    float4* shadePoint;     // kShadePointWords float4 per shading point, word-major
     uint32_t* counters;     // per bounce: kCounterStride words (CNT_*)
     // Accumulation targets (per pixel).
     float4* accumMean;
