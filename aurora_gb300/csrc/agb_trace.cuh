@@ -244,16 +244,26 @@ AGB_D void ldg256(const float4* p, float4& a, float4& b)
         : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
         : "l"(p));
 }
-// Leaves a lane may park before it stops in the node phase (1 or 2).
-constexpr int kParkLeaves = AGB_TRACE_PARK;
+#ifndef AGB_SHADOW_PARK
+#define AGB_SHADOW_PARK AGB_TRACE_PARK
+#endif
+#ifndef AGB_SHADOW_NODE_EXIT
+#define AGB_SHADOW_NODE_EXIT AGB_NODE_EXIT
+#endif
+// Leaves a lane may park before it stops in the node phase (1 or 2): closest-hit and any-hit rays.
+constexpr int kParkLeavesClosest = AGB_TRACE_PARK;
+constexpr int kParkLeavesAny     = AGB_SHADOW_PARK;
 // The node phase also ends once fewer than this many lanes are still searching for their first
 // leaf while some lane holds a parked leaf (0: only when none is searching).
-constexpr int kNodeExitLanes = AGB_NODE_EXIT;
+constexpr int kNodeExitLanesClosest = AGB_NODE_EXIT;
+constexpr int kNodeExitLanesAny     = AGB_SHADOW_NODE_EXIT;
 
 template <bool kAnyHit, bool kCount, class Loader, class Writer>
 AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const Loader& load,
     const Writer& write, int32_t* stack, int stride, TraceCounters& cnt, bool& overflow)
 {
+    constexpr int kParkLeaves    = kAnyHit ? kParkLeavesAny : kParkLeavesClosest;
+    constexpr int kNodeExitLanes = kAnyHit ? kNodeExitLanesAny : kNodeExitLanesClosest;
     static_assert(kParkLeaves == 1 || kParkLeaves == 2, "one or two parked leaves");
     const unsigned FULL = 0xffffffffu;
     const int lane      = threadIdx.x & 31;
