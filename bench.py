@@ -56,12 +56,13 @@ def parse_args():
     return p.parse_args()
 
 
-def closest_traffic_per_launch():
-    """DRAM bytes per k_trace_closest launch from the committed ncu summary, or None."""
+def closest_dram_bytes_per_ray():
+    """DRAM bytes (read + write) per closest-hit ray of k_trace_closest from the committed ncu
+    summary, or None."""
     try:
-        for line in open(os.path.join(ROOT, "profiles", "trace_closest_dram_per_launch.txt")):
-            if line.startswith("bytes_per_launch"):
-                return int(line.split()[1])
+        for line in open(os.path.join(ROOT, "profiles", "trace_closest_dram_large_config.txt")):
+            if line.startswith("closest_bytes_per_ray"):
+                return float(line.split()[1])
     except OSError:
         pass
     return None
@@ -453,13 +454,17 @@ def main():
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     achieved = closest_bytes / (closest_ms / 1000.0) / 1e9
+    dram_per_ray = closest_dram_bytes_per_ray()
+    launches_closest = max(1.0, kernel_count["trace_closest"] / steps)
     roofline = {
         "bound": "hbm", "kernel": "k_trace_closest (closest-hit BVH2 traversal)",
         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
-        "traffic": closest_traffic_per_launch(),
-        "traffic_unit": "bytes per launch (DRAM read + write, from the committed ncu capture)",
-        "algorithmic_bytes_per_launch": int(closest_bytes / max(1.0, kernel_count["trace_closest"] / steps)),
+        "traffic": (int(dram_per_ray * counted["closest_rays"] / launches_closest)
+                    if dram_per_ray is not None else None),
+        "traffic_unit": "bytes per launch (DRAM read + write): the committed ncu capture's bytes per "
+                        "closest-hit ray x this step's closest-hit rays per launch",
+        "algorithmic_bytes_per_launch": int(closest_bytes / launches_closest),
         "algorithmic_bytes_per_step": int(closest_bytes),
         "launches_per_step": kernel_count["trace_closest"] / steps,
         "ms_per_step": closest_ms,
