@@ -643,6 +643,9 @@ public:
         opts.setBoolean("isRussianRouletteEnabled", true);
         opts.setInt("russianRouletteStartDepth", 3);
         opts.setBoolean("isDiffuseOnlyEnabled", false);
+        // The HGI backend forces opaque shadows (HGIRenderer.cpp:491); false selects the
+        // transparent (any-hit opacity) shadows of the DirectX backend.
+        opts.setBoolean("isForceOpaqueShadowsEnabled", true);
     }
     ~Renderer() override
     {
@@ -727,7 +730,7 @@ public:
             range = std::min(std::max(-zmin * 1.1f, 1.f), 5.0e8f);
         }
         f.sky_view_z                      = -range * 2.f;
-        f.is_force_opaque_shadows_enabled = 1;
+        f.is_force_opaque_shadows_enabled = opts.asBool("isForceOpaqueShadowsEnabled", true) ? 1 : 0;
         f.is_diffuse_only_enabled         = opts.asBool("isDiffuseOnlyEnabled", false) ? 1 : 0;
         f.trace_depth                     = std::max(1, std::min(10, opts.asInt("traceDepth", 5)));
         f.max_luminance                   = opts.asFloat("maxLuminance", 1000.f);

@@ -1046,10 +1046,6 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
     agb_status st = setDevice(ctx);
     if (st)
         return st;
-    if (!ctx->frame.is_force_opaque_shadows_enabled)
-        return fail(AGB_ERR_INVALID_ARG,
-            "agb_render: transparent (any-hit) shadows are not supported; set "
-            "is_force_opaque_shadows_enabled as the HGI backend does");
     uint32_t accumMode = opt->accumulation ? opt->accumulation : AGB_ACCUM_RUNNING_MEAN;
     uint32_t pixels    = opt->width * opt->height;
     uint32_t spw = 1;

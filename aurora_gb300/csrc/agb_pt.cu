@@ -7,6 +7,8 @@
 //                                               (HitShaderEntryPoints.slang:35-486,
 //                                                MainEntryPoints.slang:355-426)
 //     k_trace_shadow    shadow rays             traceShadowRay (RayTrace.slang:221-270)
+//     k_trace_shadow_transparent  the same with transparent shadows (any-hit opacity,
+//                                               HitShaderEntryPoints.slang:490-552)
 //     k_resolve         visibility x pending contributions, RayGen accumulation
 //                                               (HitShaderEntryPoints.slang:394-467,
 //                                                MainEntryPoints.slang:160-243)
@@ -152,6 +154,74 @@ struct OcclusionWriter
     }
 };
 
+// Transparent shadows (is_force_opaque_shadows_enabled = 0): the any-hit shader of
+// HitShaderEntryPoints.slang:490-552 multiplies the ray's visibility by 1 - opacity at every
+// surface it crosses and ends the ray once it is black.  Here the hits are taken nearest first,
+// each by a closest-hit traversal from just beyond the previous one, so the product has one
+// order; at most kMaxShadowHits are taken.
+constexpr int kMaxShadowHits = 4096;
+
+// Opacity the any-hit shader takes from a hit: the instance's material opacity x (1 -
+// transmission x transmission colour), 1 for an opaque material without an opacity texture.
+AGB_DN v3 shadowOpacity(const DevScene& s, const RayHit& h)
+{
+    const DevInstance& in = s.instances[h.inst];
+    const agb_material& b = s.materials[in.material];
+    bool hasOpacityImage  = s.matTex && b.has_opacity_image && s.matTex[in.material].image[AGB_TEX_OPACITY] >= 0;
+    if (b.opacity[0] == 1.f && b.opacity[1] == 1.f && b.opacity[2] == 1.f && !hasOpacityImage &&
+        b.transmission == 0.f)
+        return splat(1.f);
+    Shading sh = computeShading(s, in, uint32_t(h.prim), h.u, h.v);
+    v3 mn      = sh.N;
+    bool gen;
+    Mat m = loadMaterial(s, in.material, sh, mn, gen);
+    return m.opacity * (splat(1.f) - m.transmissionColor() * m.transmission());
+}
+
+// Shadow rays of the transparent mode; `vis` (one float4 per shadow ray: running visibility, hits
+// taken) reuses the shading-point buffer, which is free while shadow rays are traced.
+struct TransparentShadowLoader
+{
+    ShadowLoader rays;
+    float4* vis;
+    AGB_D void operator()(uint32_t i, v3& o, v3& d, float& tmin, float& tmax) const
+    {
+        rays(i, o, d, tmin, tmax);
+        vis[i] = make_float4(1.f, 1.f, 1.f, __int_as_float(0));
+    }
+};
+struct TransparentShadowWriter
+{
+    static constexpr bool kRestart = true;
+    const uint32_t* tag;
+    float4* vis;
+    float4* pendSlot;
+    // Returns false (trace on from the new tmin) while the ray is not blocked.
+    AGB_D bool operator()(const DevScene& s, uint32_t i, bool hit, const RayHit& h, float& tmin) const
+    {
+        float4 v4 = vis[i];
+        v3 v      = v3{ v4.x, v4.y, v4.z };
+        if (hit)
+        {
+            v         = v * (splat(1.f) - shadowOpacity(s, h));
+            int taken = __float_as_int(v4.w) + 1;
+            if (!isBlack(v) && taken < kMaxShadowHits)
+            {
+                vis[i] = make_float4(v.x, v.y, v.z, __int_as_float(taken));
+                tmin   = nextafterf(h.t, __int_as_float(0x7f800000));
+                return false;
+            }
+        }
+        // The slot's pending contribution times the visibility (traceShadowRay(...) * result);
+        // its occlusion bit stays clear.
+        uint32_t t = tag[i];
+        float4* ps = pendSlot + size_t(t >> 3) * kMaxShadowSlots + (t & 7u);
+        float4 c   = *ps;
+        *ps        = make_float4(v.x * c.x, v.y * c.y, v.z * c.z, c.w);
+        return true;
+    }
+};
+
 template <bool kCount>
 __global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_closest(DevScene s, WaveBuffers wb, int bounce, int cur)
 {
@@ -179,6 +249,26 @@ __global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_shadow
     persistentTrace<true, kCount>(s, n, wb.counters + bounce * kCounterStride + CNT_SHADOW_WORK,
         ShadowLoader{ wb.shTag, wb.shOrg, wb.shDir }, OcclusionWriter{ wb.shTag, wb.occluded },
         g_stack + threadIdx.x, kTraceBlock, c, overflow);
+    if (kCount)
+    {
+        atomicAdd(statPtr(wb, 5), c.nodes);
+        atomicAdd(statPtr(wb, 6), c.tris);
+    }
+    if (overflow)
+        atomicAdd(statPtr(wb, 4), 1ull);
+}
+
+template <bool kCount>
+__global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_shadow_transparent(DevScene s,
+    WaveBuffers wb, int bounce)
+{
+    uint32_t n      = wb.counters[bounce * kCounterStride + CNT_SHADOW];
+    TraceCounters c = { 0, 0 };
+    bool overflow   = false;
+    persistentTrace<false, kCount>(s, n, wb.counters + bounce * kCounterStride + CNT_SHADOW_WORK,
+        TransparentShadowLoader{ ShadowLoader{ wb.shTag, wb.shOrg, wb.shDir }, wb.shadePoint },
+        TransparentShadowWriter{ wb.shTag, wb.shadePoint, wb.pendSlot }, g_stack + threadIdx.x,
+        kTraceBlock, c, overflow);
     if (kCount)
     {
         atomicAdd(statPtr(wb, 5), c.nodes);
@@ -881,7 +971,14 @@ void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp
         mark(KC_SHADE);
         k_shade_scatter<<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur);
         mark(KC_SHADOW);
-        if (wp.countTraversal)
+        if (!f.is_force_opaque_shadows_enabled)
+        {
+            if (wp.countTraversal)
+                k_trace_shadow_transparent<true><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b);
+            else
+                k_trace_shadow_transparent<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b);
+        }
+        else if (wp.countTraversal)
             k_trace_shadow<true><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b);
         else
             k_trace_shadow<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b);
@@ -908,6 +1005,10 @@ void setTraceAttributes()
     cudaFuncSetAttribute(k_trace_closest<false>, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
     cudaFuncSetAttribute(k_trace_shadow<true>, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
     cudaFuncSetAttribute(k_trace_shadow<false>, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
+    cudaFuncSetAttribute(k_trace_shadow_transparent<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, stackBytes);
+    cudaFuncSetAttribute(k_trace_shadow_transparent<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, stackBytes);
+    cudaFuncSetAttribute(k_trace_shadow_transparent<true>, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
+    cudaFuncSetAttribute(k_trace_shadow_transparent<false>, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
 }
 
 } // namespace agb

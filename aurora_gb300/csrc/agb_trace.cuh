@@ -13,6 +13,8 @@
 // a few ulp so they never reject a hit the triangle test accepts.
 #pragma once
 
+#include <type_traits>
+
 #include "agb_scene.cuh"
 
 namespace agb
@@ -258,6 +260,20 @@ constexpr int kParkLeavesAny     = AGB_SHADOW_PARK;
 constexpr int kNodeExitLanesClosest = AGB_NODE_EXIT;
 constexpr int kNodeExitLanesAny     = AGB_SHADOW_NODE_EXIT;
 
+// A Writer whose kRestart is true is called as write(scene, ray, hit?, hit, tmin) and returns
+// false to trace the same ray again from the tmin it sets (transparent shadows walk the hits
+// along the ray this way); other writers are called as write(ray, hit?, hit) and end the ray.
+template <class W, class = void>
+struct WriterRestarts
+{
+    static constexpr bool value = false;
+};
+template <class W>
+struct WriterRestarts<W, std::void_t<decltype(W::kRestart)>>
+{
+    static constexpr bool value = W::kRestart;
+};
+
 template <bool kAnyHit, bool kCount, class Loader, class Writer>
 AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const Loader& load,
     const Writer& write, int32_t* stack, int stride, TraceCounters& cnt, bool& overflow)
@@ -270,7 +286,7 @@ AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const 
     bool active = false, exhausted = false;
     uint32_t rayIdx = 0;
     v3 o = splat(0.f), d = splat(0.f);
-    float tmin = 0.f, tmax = 0.f;
+    float tmin = 0.f, tmax = 0.f, tmaxRay = 0.f;
     SlabRay sr;
     WtRay wr;
     int32_t ref = kDone, leaf = 0, leaf2 = 0;
@@ -314,6 +330,7 @@ AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const 
                 if (rayIdx < n)
                 {
                     load(rayIdx, o, d, tmin, tmax);
+                    tmaxRay  = tmax;
                     sr       = slabSetup(o, d);
                     ref      = s.instanceCount > 0 ? s.tlasRoot : kDone;
                     leaf     = 0;
@@ -480,8 +497,28 @@ AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const 
         }
         if (active && ref == kDone)
         {
-            write(rayIdx, found, hit);
-            active = false;
+            if constexpr (WriterRestarts<Writer>::value)
+            {
+                if (write(s, rayIdx, found, hit, tmin))
+                    active = false;
+                else
+                {
+                    // Trace the ray again beyond the hit (the writer moved tmin past it).
+                    ref      = s.instanceCount > 0 ? s.tlasRoot : kDone;
+                    sp       = 0;
+                    inst     = -1;
+                    nodes    = reinterpret_cast<const float4*>(s.tlas);
+                    sr       = slabSetup(o, d);
+                    tmax     = tmaxRay;
+                    found    = false;
+                    hit.inst = hit.prim = -1;
+                }
+            }
+            else
+            {
+                write(rayIdx, found, hit);
+                active = false;
+            }
         }
     }
 }
