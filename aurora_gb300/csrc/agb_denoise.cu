@@ -153,34 +153,26 @@ constexpr int kConvStageSlices = 4;
 // columns of one MMA tile, else tiles of 128.
 __host__ __device__ inline int convTile(int cout) { return cout <= 256 ? cout : 128; }
 
-__device__ __forceinline__ void gatherSlice(const ConvArgs& a, int Cin, int slice, long p, long P,
-    uint8_t* aSlice, int row)
+// One K16 slice (16 channels c.. of tap `tap`) of this thread's output pixel (x, y, b) into row
+// `row` of the A operand; zero outside the image or for rows past the last pixel.
+__device__ __forceinline__ void gatherSlice(const ConvArgs& a, bool pixel, int x, int y, int b, int tap,
+    int c, uint8_t* aSlice, int row)
 {
     uint4 v0 = make_uint4(0, 0, 0, 0), v1 = v0;
-    int k   = slice * 16;
-    int tap = k / Cin;
-    int c   = k - tap * Cin;
-    if (p < P)
+    int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
+    if (pixel && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W)
     {
-        int x  = int(p % a.W);
-        long t = p / a.W;
-        int y  = int(t % a.H);
-        int b  = int(t / a.H);
-        int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
-        if (yy >= 0 && yy < a.H && xx >= 0 && xx < a.W)
+        const uint16_t* src;
+        if (c < a.C0)
         {
-            const uint16_t* src;
-            if (c < a.C0)
-            {
-                int h0 = a.up0 ? a.H >> 1 : a.H, w0 = a.up0 ? a.W >> 1 : a.W;
-                int y0 = a.up0 ? yy >> 1 : yy, x0 = a.up0 ? xx >> 1 : xx;
-                src = a.in0 + ((size_t(b) * h0 + y0) * w0 + x0) * a.C0 + c;
-            }
-            else
-                src = a.in1 + ((size_t(b) * a.H + yy) * a.W + xx) * a.C1 + (c - a.C0);
-            v0 = __ldg(reinterpret_cast<const uint4*>(src));
-            v1 = __ldg(reinterpret_cast<const uint4*>(src) + 1);
+            int h0 = a.up0 ? a.H >> 1 : a.H, w0 = a.up0 ? a.W >> 1 : a.W;
+            int y0 = a.up0 ? yy >> 1 : yy, x0 = a.up0 ? xx >> 1 : xx;
+            src = a.in0 + ((size_t(b) * h0 + y0) * w0 + x0) * a.C0 + c;
         }
+        else
+            src = a.in1 + ((size_t(b) * a.H + yy) * a.W + xx) * a.C1 + (c - a.C0);
+        v0 = __ldg(reinterpret_cast<const uint4*>(src));
+        v1 = __ldg(reinterpret_cast<const uint4*>(src) + 1);
     }
     *reinterpret_cast<uint4*>(aSlice + tc::sliceOffset(row, 0)) = v0;
     *reinterpret_cast<uint4*>(aSlice + tc::sliceOffset(row, 8)) = v1;
@@ -221,6 +213,18 @@ __global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a)
     const long P         = long(a.B) * a.H * a.W;
     const long p         = long(blockIdx.x) * 128 + tid;
     const int slices     = 9 * Cin / 16;
+    // This thread's output pixel, decomposed once; the slices run tap-major in order, so the
+    // (tap, channel) of the next slice follows from the current one.
+    const bool pixel = p < P;
+    int px = 0, py = 0, pb = 0;
+    if (pixel)
+    {
+        px      = int(p % a.W);
+        long pt = p / a.W;
+        py      = int(pt % a.H);
+        pb      = int(pt / a.H);
+    }
+    int gTap = 0, gC = 0;
     const int chunks     = (slices + kConvStageSlices - 1) / kConvStageSlices;
     uint32_t mmaParity[2] = { 0, 0 }, tmaParity[2] = { 0, 0 };
     bool ok = true;
@@ -241,7 +245,15 @@ __global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a)
                 &tmaBar[s]);
         }
         for (int j = 0; j < ns; j++)
-            gatherSlice(a, Cin, s0 + j, p, P, aS[s] + j * (128 * 32), tid);
+        {
+            gatherSlice(a, pixel, px, py, pb, gTap, gC, aS[s] + j * (128 * 32), tid);
+            gC += 16;
+            if (gC == Cin)
+            {
+                gC = 0;
+                gTap++;
+            }
+        }
         tc::fenceProxyAsync();
         __syncthreads();
         if (tid == 0)
