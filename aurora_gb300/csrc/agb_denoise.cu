@@ -341,10 +341,12 @@ __global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a)
 // dW[tap][ci][co] += sum over pixels p of X[p + d(tap)][ci] * dY[p][co], X = concat(up(in0), in1) as
 // in the forward pass.  GEMM with rows = input channels (128 per CTA, grid.z blocks), columns =
 // Cout, K = pixels: grid.x splits the pixels (each CTA sums its range in TMEM and adds it to dW
-// with FP32 reductions), grid.y is the tap.  NHWC stores channels contiguously but the MMA wants
-// both operands K-major (pixels contiguous), so the threads transpose while staging: thread t
-// takes pixel t % 64 of the 64-pixel chunk and half of the channel rows, loads 8 channels at a time
-// and scatters them into the operand layout.
+// with FP32 reductions), grid.y is the tap.  NHWC stores a pixel's channels contiguously, which is
+// the MN-major operand layout: both operands are staged as 16-byte rows of 8 channels of one
+// pixel, no transpose.  Core matrix (channel group m, pixel group k) of a K16 slice sits at byte
+// (m * 2 + k) * 128 with its 8 pixel rows 16 bytes apart; the MN-major descriptors give 128 (the
+// leading byte offset) between pixel groups and 256 (the stride byte offset) between channel
+// groups.
 
 struct WgradArgs
 {
@@ -356,12 +358,11 @@ struct WgradArgs
     int chunksPerSplit;  // 64-pixel chunks per CTA
 };
 
-__device__ __forceinline__ void scatter8(uint8_t* slice, int row0, int k, uint4 v)
+// Byte offset of channel group `group` (8 channels) of pixel k (k in [0, 16)) in an MN-major K16
+// slice.
+__device__ __forceinline__ uint32_t mnOffset(uint32_t group, uint32_t k)
 {
-    const uint16_t* e = reinterpret_cast<const uint16_t*>(&v);
-#pragma unroll
-    for (int i = 0; i < 8; i++)
-        *reinterpret_cast<uint16_t*>(slice + tc::sliceOffset(uint32_t(row0 + i), uint32_t(k))) = e[i];
+    return (group * 2 + (k >> 3)) * tc::kCoreBytes + (k & 7) * 16;
 }
 
 __global__ void __launch_bounds__(128) k_conv_wgrad(WgradArgs a)
@@ -397,7 +398,8 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(WgradArgs a)
     __syncthreads();
     tc::fenceAfterSync();
     const uint32_t tmem  = tmemBase;
-    const uint32_t idesc = tc::idescBf16(128, uint32_t(N));
+    // MN-major A and B (instruction descriptor bits 15 and 16).
+    const uint32_t idesc = tc::idescBf16(128, uint32_t(N)) | (1u << 15) | (1u << 16);
     const int tap = blockIdx.y, oy = tap / 3 - 1, ox = tap % 3 - 1;
     const int ci0 = blockIdx.z * 128;
     const int j   = tid & 63, hh = tid >> 6;
@@ -446,7 +448,7 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(WgradArgs a)
                     src = a.in1 + ((size_t(b) * a.H + yy) * a.W + xx) * a.C1 + (ci - a.C0);
                 v = __ldg(reinterpret_cast<const uint4*>(src));
             }
-            scatter8(aSl, hh * 64 + g * 8, k, v);
+            *reinterpret_cast<uint4*>(aSl + mnOffset(uint32_t(hh * 8 + g), uint32_t(k))) = v;
         }
         // B rows: output channels hh * N / 2 + [0, N / 2) at the pixel itself.
         for (int g = 0; g < N / 16; g++)
@@ -455,7 +457,7 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(WgradArgs a)
             uint4 v = make_uint4(0, 0, 0, 0);
             if (p < P)
                 v = __ldg(reinterpret_cast<const uint4*>(a.dy + size_t(p) * N + co));
-            scatter8(bSl, co, k, v);
+            *reinterpret_cast<uint4*>(bSl + mnOffset(uint32_t(co / 8), uint32_t(k))) = v;
         }
         tc::fenceProxyAsync();
         __syncthreads();
@@ -465,8 +467,8 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(WgradArgs a)
 #pragma unroll
             for (int sl = 0; sl < 4; sl++)
             {
-                uint64_t ad = tc::smemDesc(tc::smemAddr(aS[s] + sl * (128 * 32)), tc::kSliceLbo, tc::kSliceSbo);
-                uint64_t bd = tc::smemDesc(tc::smemAddr(bS[s] + sl * bSlice), tc::kSliceLbo, tc::kSliceSbo);
+                uint64_t ad = tc::smemDesc(tc::smemAddr(aS[s] + sl * (128 * 32)), 128, 256);
+                uint64_t bd = tc::smemDesc(tc::smemAddr(bS[s] + sl * bSlice), 128, 256);
                 tc::mma(tmem, ad, bd, idesc, (c > 0 || sl > 0) ? 1u : 0u);
             }
             tc::commit(&mmaBar[s]);
