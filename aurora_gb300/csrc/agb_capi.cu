@@ -224,6 +224,8 @@ agb_status ensureWave(agb_context* ctx, size_t paths, int depth, size_t waves)
 {
     if (paths > ctx->pathCapacity)
     {
+        // The buffers are reallocated below; if that fails the context holds none.
+        ctx->pathCapacity = 0;
         size_t P = paths;
         size_t stateBytes = P * kPathStateBytes;
         size_t queueBytes = P * kPathQueueBytes + 1024;
@@ -1056,11 +1058,18 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
     }
     else
     {
-        // Default wave: the call's samples in as few waves as fit in an eighth of the device's
-        // memory (30 GB for 64 samples of 1920x1080 on a 288 GB device: two waves of 32), split
-        // evenly.  Fewer, larger waves keep every bounce's launch full and pay each launch's
-        // tail once per bounce instead of once per wave and bounce.
-        uint64_t budget = std::max<uint64_t>(pixels, (ctx->deviceBytes / 8) / (kPathStateBytes + kPathQueueBytes));
+        // Default wave: the call's samples in as few waves as fit in half of the device memory
+        // that is free (counting this context's wave buffers as free) and at most a third of the
+        // device, split evenly: one wave of 82 GB for 64 samples of 1920x1080 on an idle 288 GB
+        // device.  Fewer, larger waves keep every bounce's launch full and pay each launch's tail
+        // once per bounce instead of once per wave and bounce.
+        size_t freeBytes = 0, totalBytes = ctx->deviceBytes;
+        if (cudaMemGetInfo(&freeBytes, &totalBytes) != cudaSuccess)
+            freeBytes = totalBytes / 4;
+        const uint64_t perPath = kPathStateBytes + kPathQueueBytes;
+        uint64_t held   = uint64_t(ctx->pathCapacity) * perPath;
+        uint64_t bytes  = std::min<uint64_t>((uint64_t(freeBytes) + held) / 2, uint64_t(totalBytes) / 3);
+        uint64_t budget = std::max<uint64_t>(pixels, bytes / perPath);
         budget          = std::min<uint64_t>(budget, (1ull << 29) - 1);
         uint32_t most   = uint32_t(std::max<uint64_t>(1, budget / pixels));
         uint32_t count  = std::max(1u, sample_count);
@@ -1069,11 +1078,21 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
     }
     if (uint64_t(spw) * pixels >= (1ull << 29))
         return fail(AGB_ERR_LIMIT, "agb_render: wave too large");
-    uint32_t waves = sample_count ? (sample_count + spw - 1) / spw : 0;
-    int depth      = ctx->frame.trace_depth;
+    int depth = ctx->frame.trace_depth;
     st = ensureAccum(ctx, opt->width, opt->height);
-    if (!st)
-        st = ensureWave(ctx, size_t(spw) * pixels, depth, std::max(1u, waves));
+    if (st)
+        return st;
+    uint32_t waves = 0;
+    for (;;)
+    {
+        waves = sample_count ? (sample_count + spw - 1) / spw : 0;
+        st    = ensureWave(ctx, size_t(spw) * pixels, depth, std::max(1u, waves));
+        if (st != AGB_ERR_OOM || opt->max_paths_in_flight || spw == 1)
+            break;
+        // The default wave did not fit after all (memory taken meanwhile): halve it.
+        cudaGetLastError();
+        spw = (spw + 1) / 2;
+    }
     if (st)
         return st;
     if (sample_start == 0)

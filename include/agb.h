@@ -265,7 +265,8 @@ typedef struct agb_render_options
     uint32_t height;
     uint32_t accumulation;      /* AGB_ACCUM_* bitmask */
     uint32_t max_paths_in_flight; /* wave size in paths; 0 = the call's samples in as few waves
-                                     as fit in an eighth of the device's memory */
+                                     as fit in half the free device memory (at most a third
+                                     of the device), halved again if allocation fails */
     int32_t env_filter_linear;  /* environment sampler: 0 nearest (Hgi default), 1 bilinear */
     uint32_t seed_offset;       /* added to the sample index that seeds the random streams, not to
                                    the accumulation index (gSampleData.seedOffset,
