@@ -19,8 +19,10 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["agb_pt.cu", "agb_env_build.cu", "agb_env_noalloc.cu", "agb_temporal.cu", "agb_denoise.cu",
            "agb_unet.cu", "agb_unit.cu",
-           "agb_capi.cu", "agb_serve.cpp", "agb_aurora.cpp", "agb_bvh_build.cpp",
+           "agb_capi.cu", "agb_serve.cpp", "agb_aurora.cpp", "agb_obj.cpp", "agb_bvh_build.cpp",
            "agb_bvh_gpu.cu"]
+CLI_SRC = os.path.join(HERE, "cli", "agb_render.cpp")
+CLI = os.path.join(BUILD, "agb_render")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true",
               "-prec-sqrt=true", "-Xcompiler",
@@ -65,6 +67,20 @@ def _compile(src, verbose):
     return obj
 
 
+def build_cli(verbose=False):
+    """The headless renderer (cli/agb_render.cpp) linked against libagb_cuda.so."""
+    deps = [CLI_SRC, LIB, os.path.join(INCLUDE, "aurora_gb300.hpp"), os.path.join(INCLUDE, "aurora_gb300_loaders.hpp")]
+    if _stale(CLI, deps):
+        gxx = shutil.which("g++") or "g++"
+        cmd = [gxx, "-std=c++17", "-O2", "-I" + INCLUDE, CLI_SRC, "-L" + BUILD, "-lagb_cuda",
+               "-Wl,-rpath," + BUILD, "-o", CLI + ".tmp"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        subprocess.check_call(cmd)
+        os.replace(CLI + ".tmp", CLI)
+    return CLI
+
+
 def build(verbose=False):
     os.makedirs(BUILD, exist_ok=True)
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
@@ -75,6 +91,7 @@ def build(verbose=False):
             print(" ".join(cmd), flush=True)
         subprocess.check_call(cmd)
         os.replace(LIB + ".tmp", LIB)
+    build_cli(verbose)
     return LIB
 
 

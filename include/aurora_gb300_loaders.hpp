@@ -1,0 +1,106 @@
+// aurora_gb300_loaders.hpp - scene and image I/O of the headless renderer (agb_render), after the
+// Plasma application's batch path (Applications/Plasma/OBJLoader.cpp, Loaders.h, Camera.cpp):
+// Wavefront OBJ + MTL files into an agb_aurora::IScene, Radiance HDR environment images, PNG /
+// PFM output, and the camera fit to the scene bounds.
+//
+// The OBJ parse restates what the reference takes from tinyobjloader: v / vt / vn / f records
+// (1-based or negative relative indices, polygons triangulated as a fan), a new shape at each
+// `o` or `g` record, `usemtl` per face, `mtllib` material files; material defaults ior 1,
+// dissolve 1, all colours 0.  The translation into Aurora objects follows OBJLoader.cpp:155-449.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "aurora_gb300.hpp"
+
+namespace agb_aurora
+{
+
+// What the reference gets from tinyobjloader.
+struct ObjMaterial
+{
+    std::string name;
+    float diffuse[3]       = { 0.f, 0.f, 0.f };
+    float specular[3]      = { 0.f, 0.f, 0.f };
+    float transmittance[3] = { 0.f, 0.f, 0.f };
+    float emission[3]      = { 0.f, 0.f, 0.f };
+    float ior              = 1.f;
+    float dissolve         = 1.f;
+    float roughness        = 0.f;
+    float metallic         = 0.f;
+    std::string diffuseTex, roughnessTex, emissiveTex, alphaTex, bumpTex, normalTex;
+};
+struct ObjIndex
+{
+    int position = -1, texcoord = -1, normal = -1; // 0-based, -1 when absent
+};
+struct ObjShape
+{
+    std::string name;
+    std::vector<ObjIndex> indices;  // three per triangle
+    std::vector<int> materialIds;   // one per triangle, -1 without usemtl
+};
+struct ObjData
+{
+    std::vector<float> positions, normals, texcoords;
+    std::vector<ObjShape> shapes;
+    std::vector<ObjMaterial> materials;
+    std::string warnings;
+};
+// Parses OBJ text; `readFile` supplies material libraries by name (relative to the OBJ file).
+AGB_CPP_API bool parseOBJ(const std::string& text,
+    const std::function<bool(const std::string&, std::string&)>& readFile, ObjData& out,
+    std::string& error);
+
+// Scene data the loader keeps alive for the renderer's pull callbacks (Plasma's SceneContents).
+struct SceneGeometryData
+{
+    std::vector<float> positions, normals, texCoords;
+    std::vector<uint32_t> indices;
+};
+struct SceneInstanceData
+{
+    Path instance, geometry, material; // material empty: the renderer's default material
+};
+struct SceneMaterialData
+{
+    Path path;
+    Properties properties;
+};
+struct SceneContents
+{
+    std::map<Path, SceneGeometryData> geometry;
+    std::vector<SceneInstanceData> instances;
+    std::vector<SceneMaterialData> materials;
+    vec3 boundsMin = { 0.f, 0.f, 0.f }, boundsMax = { 0.f, 0.f, 0.f };
+    uint32_t vertexCount = 0, triangleCount = 0;
+    std::string warnings;
+    void reset() { *this = SceneContents(); }
+};
+// The reference's translation of parsed OBJ data (OBJLoader.cpp:155-449): Standard Surface
+// properties from the MTL values, unique (position, normal, texcoord) vertices per shape,
+// normalised normals, flipped V, generated normals where the file has none, one instance per
+// shape with the material of its first face.  Texture files (map_Kd, map_Pr, map_Ke, map_d,
+// bump / norm) are not loaded: their properties are left unset, with a warning.
+AGB_CPP_API bool translateOBJ(const ObjData& obj, const std::string& filePath, SceneContents& contents);
+// loadOBJFile (OBJLoader.cpp:73-473): parse + translate + hand everything to the scene.
+AGB_CPP_API bool loadOBJFile(IScene* scene, const std::string& filePath, SceneContents& contents);
+
+// Angle-weighted smooth vertex normals (Foundation/Source/Geometry.cpp:29-99).
+AGB_CPP_API void calculateNormals(size_t vertexCount, const float* positions, size_t triangleCount,
+    const uint32_t* indices, float* normalsOut);
+
+// Radiance RGBE (.hdr) image, flat or run-length encoded scanlines, to RGB floats top row first.
+AGB_CPP_API bool loadHDRFile(const std::string& path, std::vector<float>& rgb, int& width, int& height,
+    std::string& error);
+// 8-bit RGBA PNG (stored deflate blocks) and little-endian PFM (RGB float, bottom row first).
+AGB_CPP_API bool savePNG(const std::string& path, const uint8_t* rgba, int width, int height, size_t stride);
+AGB_CPP_API bool savePFM(const std::string& path, const float* rgba, int width, int height, size_t stride);
+
+// Camera::fit (Plasma/Camera.cpp:145-178): target = box centre, eye backed off along -direction
+// until the box fills the vertical (or horizontal) field of view.
+AGB_CPP_API void fitCamera(const vec3& boundsMin, const vec3& boundsMax, const vec3& direction,
+    float fovYRadians, float aspect, vec3& eye, vec3& target);
+
+} // namespace agb_aurora

@@ -1,0 +1,158 @@
+// Test driver for include/aurora_gb300_loaders.hpp (no GPU needed): prints JSON.
+//   loader_tool obj <file.obj>                      parse + translate, no scene
+//   loader_tool hdr <file.hdr>                      width, height, RGB floats
+//   loader_tool png <out.png> <w> <h>               writes a pattern image
+//   loader_tool pfm <out.pfm> <w> <h>               writes a pattern image
+//   loader_tool fit <min xyz> <max xyz> <dir xyz> <fovY rad> <aspect>
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <variant>
+#include <vector>
+
+#include "aurora_gb300_loaders.hpp"
+
+using namespace agb_aurora;
+
+namespace
+{
+
+void printFloats(const float* v, size_t n)
+{
+    std::printf("[");
+    for (size_t i = 0; i < n; i++)
+        std::printf("%s%.9g", i ? "," : "", v[i]);
+    std::printf("]");
+}
+
+void printString(const std::string& s)
+{
+    std::printf("\"");
+    for (char c : s)
+    {
+        if (c == '"' || c == '\\')
+            std::printf("\\%c", c);
+        else if (c == '\n')
+            std::printf("\\n");
+        else
+            std::printf("%c", c);
+    }
+    std::printf("\"");
+}
+
+void printValue(const PropertyValue& v)
+{
+    if (std::holds_alternative<bool>(v))
+        std::printf("%s", std::get<bool>(v) ? "true" : "false");
+    else if (std::holds_alternative<int>(v))
+        std::printf("%d", std::get<int>(v));
+    else if (std::holds_alternative<float>(v))
+        std::printf("%.9g", std::get<float>(v));
+    else if (std::holds_alternative<vec3>(v))
+        printFloats(std::get<vec3>(v).data(), 3);
+    else if (std::holds_alternative<mat4>(v))
+        printFloats(std::get<mat4>(v).data(), 16);
+    else
+        printString(std::get<std::string>(v));
+}
+
+} // namespace
+
+int main(int argc, char** argv)
+{
+    if (argc < 3)
+        return 2;
+    std::string mode = argv[1];
+    if (mode == "obj")
+    {
+        SceneContents c;
+        bool ok = loadOBJFile(nullptr, argv[2], c);
+        std::printf("{\"ok\":%s,\"warnings\":", ok ? "true" : "false");
+        printString(c.warnings);
+        std::printf(",\"bounds\":[");
+        printFloats(c.boundsMin.data(), 3);
+        std::printf(",");
+        printFloats(c.boundsMax.data(), 3);
+        std::printf("],\"materials\":[");
+        for (size_t i = 0; i < c.materials.size(); i++)
+        {
+            std::printf("%s{\"path\":", i ? "," : "");
+            printString(c.materials[i].path);
+            std::printf(",\"properties\":{");
+            bool first = true;
+            for (auto& kv : c.materials[i].properties)
+            {
+                std::printf("%s", first ? "" : ",");
+                first = false;
+                printString(kv.first);
+                std::printf(":");
+                printValue(kv.second);
+            }
+            std::printf("}}");
+        }
+        std::printf("],\"instances\":[");
+        for (size_t i = 0; i < c.instances.size(); i++)
+        {
+            const SceneGeometryData& g = c.geometry[c.instances[i].geometry];
+            std::printf("%s{\"instance\":", i ? "," : "");
+            printString(c.instances[i].instance);
+            std::printf(",\"material\":");
+            printString(c.instances[i].material);
+            std::printf(",\"positions\":");
+            printFloats(g.positions.data(), g.positions.size());
+            std::printf(",\"normals\":");
+            printFloats(g.normals.data(), g.normals.size());
+            std::printf(",\"texcoords\":");
+            printFloats(g.texCoords.data(), g.texCoords.size());
+            std::printf(",\"indices\":[");
+            for (size_t k = 0; k < g.indices.size(); k++)
+                std::printf("%s%u", k ? "," : "", g.indices[k]);
+            std::printf("]}");
+        }
+        std::printf("],\"vertices\":%u,\"triangles\":%u}\n", c.vertexCount, c.triangleCount);
+        return 0;
+    }
+    if (mode == "hdr")
+    {
+        std::vector<float> rgb;
+        int w = 0, h = 0;
+        std::string err;
+        bool ok = loadHDRFile(argv[2], rgb, w, h, err);
+        std::printf("{\"ok\":%s,\"error\":", ok ? "true" : "false");
+        printString(err);
+        std::printf(",\"width\":%d,\"height\":%d,\"rgb\":", w, h);
+        printFloats(rgb.data(), rgb.size());
+        std::printf("}\n");
+        return 0;
+    }
+    if ((mode == "png" || mode == "pfm") && argc == 5)
+    {
+        int w = std::atoi(argv[3]), h = std::atoi(argv[4]);
+        if (mode == "png")
+        {
+            std::vector<uint8_t> px(size_t(w) * h * 4);
+            for (size_t i = 0; i < px.size(); i++)
+                px[i] = uint8_t((i * 37u + i / 7u) & 0xffu);
+            return savePNG(argv[2], px.data(), w, h, size_t(w) * 4) ? 0 : 1;
+        }
+        std::vector<float> px(size_t(w) * h * 4);
+        for (size_t i = 0; i < px.size(); i++)
+            px[i] = float(i) * 0.25f - 3.f;
+        return savePFM(argv[2], px.data(), w, h, size_t(w) * 16) ? 0 : 1;
+    }
+    if (mode == "fit" && argc == 13)
+    {
+        vec3 bmin = { float(std::atof(argv[2])), float(std::atof(argv[3])), float(std::atof(argv[4])) };
+        vec3 bmax = { float(std::atof(argv[5])), float(std::atof(argv[6])), float(std::atof(argv[7])) };
+        vec3 dir  = { float(std::atof(argv[8])), float(std::atof(argv[9])), float(std::atof(argv[10])) };
+        vec3 eye, target;
+        fitCamera(bmin, bmax, dir, float(std::atof(argv[11])), float(std::atof(argv[12])), eye, target);
+        std::printf("{\"eye\":");
+        printFloats(eye.data(), 3);
+        std::printf(",\"target\":");
+        printFloats(target.data(), 3);
+        std::printf("}\n");
+        return 0;
+    }
+    return 2;
+}
