@@ -217,7 +217,7 @@ constexpr size_t kPathStateBytes = sizeof(uint2) + sizeof(float4) * 7 + sizeof(u
                                    sizeof(float4) * kMaxShadowSlots * 2 + sizeof(float4);
 constexpr size_t kPathQueueBytes = 2 * (2 * sizeof(float4) + sizeof(uint32_t)) + sizeof(float4) +
                                    sizeof(int32_t) + sizeof(uint32_t) * kMaxShadowSlots + sizeof(uint32_t) +
-                                   sizeof(float4) * kShadePointWords;
+                                   sizeof(float4) * (kShadePointWords + kMisWords);
 
 // Carves the wave buffers for `paths` paths and `depth` bounces out of a few allocations.
 agb_status ensureWave(agb_context* ctx, size_t paths, int depth, size_t waves)
@@ -266,6 +266,7 @@ agb_status ensureWave(agb_context* ctx, size_t paths, int depth, size_t waves)
         w.shTag       = reinterpret_cast<uint32_t*>(take(P * kMaxShadowSlots * sizeof(uint32_t)));
         w.resolveList = reinterpret_cast<uint32_t*>(take(P * sizeof(uint32_t)));
         w.shadePoint  = reinterpret_cast<float4*>(take(P * kShadePointWords * sizeof(float4)));
+        w.misPoint    = reinterpret_cast<float4*>(take(P * kMisWords * sizeof(float4)));
         if (size_t(s - ctx->queues.as<char>()) > ctx->queues.bytes)
             return fail(AGB_ERR_LIMIT, "internal: queue carve overflow");
         ctx->pathCapacity = P;

@@ -611,23 +611,41 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
     }
 }
 
-// Second half of the hit shading: environment MIS, the indirect ray and Russian roulette for
-// the shading points k_shade handed over (ShadeFunctions.slang:135-310,
-// HitShaderEntryPoints.slang:362-486).  Its warps hold only such points, and its code is the
-// sampling half of the BSDF, so both kernels keep a smaller instruction footprint.
+// The hit shading after k_shade, in two kernels over the compacted shading points, each holding
+// one of the large Standard Surface entry points (the shading kernels' speed follows their
+// instruction-cache footprint):
+//   k_shade_scatter  draws the environment-MIS random pair and samples the BSDF with it
+//                    (ShadeFunctions.slang:146-163), samples the indirect ray and applies Russian
+//                    roulette (ShadeFunctions.slang:263-310, HitShaderEntryPoints.slang:362-486),
+//                    appends the next ray and hands the MIS sample to k_shade_mis;
+//   k_shade_mis      evaluates both halves of the environment MIS (ShadeFunctions.slang:135-259:
+//                    environment lookup, environment sample, evaluateMaterialAndPDF with the same
+//                    random pair), sets the pending-record bits and appends the resolve entry and
+//                    the shadow rays.
+// The random numbers are drawn in the reference's order (MIS pair, indirect pair, roulette); the
+// MIS evaluation consumes none, so running it after the indirect sampling changes no value.
+
+// MIS sample handed from k_shade_scatter to k_shade_mis: kMisWords float4 per shading point,
+// word-major like the shading point.
+AGB_D void storeMis(float4* mp, uint32_t stride, uint32_t j, v3 L, float pdf, v3 bsdf, int lobe, v2 rnd,
+    uint32_t bitsBase)
+{
+    float4* w             = mp + j;
+    w[0]                  = make_float4(L.x, L.y, L.z, pdf);
+    w[1 * size_t(stride)] = make_float4(bsdf.x, bsdf.y, bsdf.z, __int_as_float(lobe));
+    w[2 * size_t(stride)] = make_float4(rnd.x, rnd.y, __uint_as_float(bitsBase), 0.f);
+}
+
 __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade_scatter(DevScene s,
     agb_frame_data f, WaveParams wp, WaveBuffers wb, int bounce, int cur)
 {
     uint32_t n      = wb.counters[bounce * kCounterStride + CNT_SCATTER];
     uint32_t stride = gridDim.x * blockDim.x;
-    v2 screen = v2{ float(wp.width), float(wp.height) };
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride)
     {
         uint32_t j     = base + threadIdx.x;
         bool valid     = j < n;
         bool pushNext  = false;
-        bool resolve   = false;
-        uint32_t slots = 0;
         uint32_t p     = 0;
         v3 nextO = splat(0.f), nextD = splat(0.f);
         if (valid)
@@ -636,56 +654,24 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade_scatter(
             MatCommon mc;
             Frame fr;
             v3 V, shPosition, shGeomPosition;
+            uint32_t slots;
             loadShadePoint(s, wb.shadePoint, wp.paths, j, m, slots, p, mc, fr, V, shPosition,
                 shGeomPosition);
             uint32_t flags = wb.flags[p];
             float4 c4      = wb.contrib[p];
             v3 contrib     = v3{ c4.x, c4.y, c4.z };
             uint32_t rayType = pfRayType(flags);
-            uint32_t pixel   = p % wp.pixels;
-            v2 pixel2        = v2{ float(pixel % wp.width), float(pixel / wp.width) };
             Rng rng;
             {
                 uint2 r = wb.rng[p];
                 rng     = Rng{ r.x, r.y };
             }
-            float4* pslot = wb.pendSlot + size_t(p) * kMaxShadowSlots;
-            float4* pdir  = wb.shDir + size_t(p) * kMaxShadowSlots;
-            // Environment MIS (ShadeFunctions.slang:135-259): one random pair for both halves.
+            // Environment MIS, BSDF half's sample (one random pair for both halves).
+            v2 rnd = random2D(rng);
+            v3 Lmis;
+            float mpdf;
             int misLobe;
-            bool mis = false;
-            {
-                v2 rnd = random2D(rng);
-                v3 L;
-                float mpdf;
-                v3 bsdf = sampleMaterial(m, mc, fr, V, rnd, L, mpdf, misLobe);
-                if (misLobe != TRANSMISSION_LOBE)
-                {
-                    v3 lr = evaluateEnvironment(s, L, false, pixel2, screen);
-                    if (!isBlack(lr) && !isBlack(bsdf))
-                    {
-                        float lpdf = s.env.has_light_tex && s.envLight.data
-                            ? luminance(lr) / s.env.light_tex_luminance_integral
-                            : divPi(0.25f);
-                        v3 res = lr * misWeight(mpdf, lpdf) * bsdf / mpdf;
-                        pslot[4] = make_float4(res.x, res.y, res.z, 0.f);
-                        pdir[4]  = make_float4(L.x, L.y, L.z, 0.f);
-                        slots |= 1u << 4;
-                    }
-                    float lpdf;
-                    lr = sampleEnvironment(s, rnd, L, lpdf);
-                    int el;
-                    bsdf = evaluateMaterialAndPDF(m, mc, fr, V, L, rnd, mpdf, el);
-                    if (!isBlack(lr) && !isBlack(bsdf))
-                    {
-                        v3 res = lr * misWeight(lpdf, mpdf) * bsdf / lpdf;
-                        pslot[5] = make_float4(res.x, res.y, res.z, 0.f);
-                        pdir[5]  = make_float4(L.x, L.y, L.z, 0.f);
-                        slots |= 1u << 5;
-                    }
-                    mis = (slots & 0x30u) != 0;
-                }
-            }
+            v3 bsdfMis = sampleMaterial(m, mc, fr, V, rnd, Lmis, mpdf, misLobe);
             bool alpha = (flags & PF_ALPHA) != 0;
             alpha = !(!alpha && rayType == TRANSMISSION_LOBE);
             flags = alpha ? (flags | PF_ALPHA) : (flags & ~PF_ALPHA);
@@ -709,23 +695,14 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade_scatter(
                 }
             }
             bool ended = nextType == NO_SECONDARY_RAY;
-            uint32_t bits = slots;
-            if (mis)
-            {
-                bits |= RS_MIS;
-                flags = pfSetMisLobe(flags, uint32_t(misLobe));
-            }
+            // Pending-record bits that do not depend on the MIS result.
+            uint32_t bitsBase = slots;
             if (bounce == 0)
-            {
-                bits |= RS_DEPTH0;
-                if (pfMisLobe(flags) == DIFFUSE_LOBE)
-                    bits |= RS_DIFFUSE_ROUTE;
-            }
+                bitsBase |= RS_DEPTH0;
             else if (rayType == DIFFUSE_LOBE)
-                bits |= RS_DIFFUSE_ROUTE;
+                bitsBase |= RS_DIFFUSE_ROUTE;
+            storeMis(wb.misPoint, wp.paths, j, Lmis, mpdf, bsdfMis, misLobe, rnd, bitsBase);
             wb.pendSegContrib[p] = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
-            wb.pendBits[p]       = bits;
-            wb.occluded[p]       = 0u;
             flags &= ~PF_PRIMARY;
             if (nextType == TRANSMISSION_LOBE)
                 flags ^= PF_INSIDE;
@@ -741,12 +718,11 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade_scatter(
             }
             flags    = pfSetRayType(flags, uint32_t(nextType));
             pushNext = !ended;
-            resolve  = true;
             wb.rng[p]     = make_uint2(rng.x, rng.y);
             wb.contrib[p] = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
             wb.flags[p]   = flags;
         }
-        // Warp-aggregated queue appends (all lanes of the warp reach this point together).
+        // Warp-aggregated append of the next rays (all lanes of the warp reach this point together).
         __syncwarp();
         uint32_t slotNext = warpAppend(wb.counters + (bounce + 1) * kCounterStride + CNT_RAYS, pushNext);
         if (pushNext)
@@ -755,8 +731,84 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade_scatter(
             wb.rayDir[cur ^ 1][slotNext]  = make_float4(nextD.x, nextD.y, nextD.z, __int_as_float(0x7f800000));
             wb.rayPath[cur ^ 1][slotNext] = p;
         }
-        uint32_t slotRes = warpAppend(wb.counters + bounce * kCounterStride + CNT_RESOLVE, resolve);
-        if (resolve)
+    }
+}
+
+__global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade_mis(DevScene s,
+    agb_frame_data f, WaveParams wp, WaveBuffers wb, int bounce)
+{
+    uint32_t n      = wb.counters[bounce * kCounterStride + CNT_SCATTER];
+    uint32_t stride = gridDim.x * blockDim.x;
+    v2 screen = v2{ float(wp.width), float(wp.height) };
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride)
+    {
+        uint32_t j     = base + threadIdx.x;
+        bool valid     = j < n;
+        uint32_t slots = 0;
+        uint32_t p     = 0;
+        if (valid)
+        {
+            Mat m;
+            MatCommon mc;
+            Frame fr;
+            v3 V, shPosition, shGeomPosition;
+            loadShadePoint(s, wb.shadePoint, wp.paths, j, m, slots, p, mc, fr, V, shPosition,
+                shGeomPosition);
+            const float4* w = wb.misPoint + j;
+            float4 w0 = w[0], w1 = w[1 * size_t(wp.paths)], w2 = w[2 * size_t(wp.paths)];
+            v3 L          = v3{ w0.x, w0.y, w0.z };
+            float mpdf    = w0.w;
+            v3 bsdf       = v3{ w1.x, w1.y, w1.z };
+            int misLobe   = __float_as_int(w1.w);
+            v2 rnd        = v2{ w2.x, w2.y };
+            uint32_t bits = __float_as_uint(w2.z);
+            uint32_t pixel = p % wp.pixels;
+            v2 pixel2      = v2{ float(pixel % wp.width), float(pixel / wp.width) };
+            float4* pslot  = wb.pendSlot + size_t(p) * kMaxShadowSlots;
+            float4* pdir   = wb.shDir + size_t(p) * kMaxShadowSlots;
+            // Environment MIS (ShadeFunctions.slang:135-259).
+            bool mis = false;
+            if (misLobe != TRANSMISSION_LOBE)
+            {
+                v3 lr = evaluateEnvironment(s, L, false, pixel2, screen);
+                if (!isBlack(lr) && !isBlack(bsdf))
+                {
+                    float lpdf = s.env.has_light_tex && s.envLight.data
+                        ? luminance(lr) / s.env.light_tex_luminance_integral
+                        : divPi(0.25f);
+                    v3 res = lr * misWeight(mpdf, lpdf) * bsdf / mpdf;
+                    pslot[4] = make_float4(res.x, res.y, res.z, 0.f);
+                    pdir[4]  = make_float4(L.x, L.y, L.z, 0.f);
+                    slots |= 1u << 4;
+                }
+                float lpdf;
+                lr = sampleEnvironment(s, rnd, L, lpdf);
+                int el;
+                bsdf = evaluateMaterialAndPDF(m, mc, fr, V, L, rnd, mpdf, el);
+                if (!isBlack(lr) && !isBlack(bsdf))
+                {
+                    v3 res = lr * misWeight(lpdf, mpdf) * bsdf / lpdf;
+                    pslot[5] = make_float4(res.x, res.y, res.z, 0.f);
+                    pdir[5]  = make_float4(L.x, L.y, L.z, 0.f);
+                    slots |= 1u << 5;
+                }
+                mis = (slots & 0x30u) != 0;
+            }
+            bits |= slots;
+            if (mis)
+            {
+                bits |= RS_MIS;
+                wb.flags[p] = pfSetMisLobe(wb.flags[p], uint32_t(misLobe));
+            }
+            if (bounce == 0 && pfMisLobe(wb.flags[p]) == DIFFUSE_LOBE)
+                bits |= RS_DIFFUSE_ROUTE;
+            wb.pendBits[p] = bits;
+            wb.occluded[p] = 0u;
+        }
+        // Warp-aggregated appends (all lanes of the warp reach this point together).
+        __syncwarp();
+        uint32_t slotRes = warpAppend(wb.counters + bounce * kCounterStride + CNT_RESOLVE, valid);
+        if (valid)
             wb.resolveList[slotRes] = p;
         // Shadow rays: variable count per lane, warp prefix sum then one atomic.
         uint32_t cnt = __popc(slots);
@@ -774,10 +826,10 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade_scatter(
         if (lane == 31 && total)
             sbase = atomicAdd(wb.counters + bounce * kCounterStride + CNT_SHADOW, total);
         sbase = __shfl_sync(0xffffffffu, sbase, 31);
-        uint32_t w = sbase + incl - cnt;
+        uint32_t wpos = sbase + incl - cnt;
         for (uint32_t k = 0; k < uint32_t(kMaxShadowSlots); k++)
             if (slots & (1u << k))
-                wb.shTag[w++] = (p << 3) | k;
+                wb.shTag[wpos++] = (p << 3) | k;
     }
 }
 
@@ -970,6 +1022,8 @@ void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp
         k_shade<<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 0);
         mark(KC_SHADE);
         k_shade_scatter<<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur);
+        mark(KC_SHADE);
+        k_shade_mis<<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b);
         mark(KC_SHADOW);
         if (!f.is_force_opaque_shadows_enabled)
         {
@@ -984,7 +1038,7 @@ void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp
             k_trace_shadow<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b);
         mark(KC_RESOLVE);
         k_resolve<<<grid, 256, 0, st>>>(f, wb, b);
-        launches += 5;
+        launches += 6;
         cur ^= 1;
     }
     mark(KC_FINALIZE);

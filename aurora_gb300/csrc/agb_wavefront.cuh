@@ -9,6 +9,7 @@ namespace agb
 {
 
 constexpr int kShadePointWords = 10; // float4 per shading point handed between the shading kernels
+constexpr int kMisWords        = 3;  // float4 of the environment-MIS sample per shading point
 constexpr int kMaxShadowSlots = 6; // up to 4 distant lights + 2 environment-MIS rays per hit
 
 // Per-bounce device counters (kCounterStride words per bounce).
@@ -80,6 +81,7 @@ struct WaveBuffers
     uint32_t* shTag;        // path << 3 | slot
     uint32_t* resolveList;  // paths with a pending record this bounce
     float4* shadePoint;     // kShadePointWords float4 per shading point, word-major
+    float4* misPoint;       // kMisWords float4 per shading point: the environment-MIS sample
     uint32_t* counters;     // per bounce: kCounterStride words (CNT_*)
     // Accumulation targets (per pixel).
     float4* accumMean;
