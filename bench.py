@@ -20,6 +20,7 @@ steps, outside the timed region.  Device time comes from CUDA events on the rend
 """
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -122,30 +123,40 @@ def bench_denoiser(torch, _abi, stream, peaks):
     return out
 
 
-def bench_time_to_rel_mse(torch, _abi, r, s, target=1e-3, ref_spp=2048, chunk=8, max_spp=4096):
+def bench_time_to_rel_mse(torch, _abi, r, s, target=1e-3, ref_spp=4096, max_spp=8192):
     """Wall time until the running image is within relMSE `target` (eps 1e-2) of a converged
     reference of the same frame.  The reference is this renderer's own ref_spp-sample Kahan mean
-    (its agreement with the FP64 oracle is a test).  The timed loop renders `chunk` samples at a
-    time into the Kahan sum and evaluates relMSE on the GPU (agb_accum_rel_mse) after each chunk."""
+    over independent random streams (seed offset 2^24; its agreement with the FP64 oracle is a
+    test).  The timed loop renders progressively into the Kahan sum and evaluates relMSE on the
+    GPU (agb_accum_rel_mse) after each call; the next call's sample count follows the error seen so
+    far (relMSE ~ c / spp + c / ref_spp): 90 % of the predicted remainder, 8 to 128 samples,
+    a multiple of 8."""
     import ctypes
     lib = _abi.library()
     r.set_frame(s.frame)
-    r.render(0, ref_spp, accumulation=_abi.ACCUM_KAHAN)
+    r.render(0, ref_spp, accumulation=_abi.ACCUM_KAHAN, seed_offset=1 << 24)
     ref = torch.from_numpy(r.read(_abi.ACCUM_KAHAN).copy()).cuda()
     torch.cuda.synchronize()
     err = ctypes.c_double(float("inf"))
     t0 = time.perf_counter()
-    spp = 0
+    spp, chunk, calls = 0, 8, 0
     while spp < max_spp:
         r.render(spp, chunk, accumulation=_abi.ACCUM_KAHAN)
         spp += chunk
+        calls += 1
         _abi.check(lib.agb_accum_rel_mse(r.ctx, _abi.ACCUM_KAHAN, ref.data_ptr(), 1e-2, ctypes.byref(err)))
         if err.value <= target:
             break
+        c = err.value / (1.0 / spp + 1.0 / ref_spp)
+        room = target - c / ref_spp
+        need = c / room if room > 0 else max_spp
+        chunk = int(min(128, max(8, 8 * math.ceil(0.9 * (need - spp) / 8))))
+        chunk = min(chunk, max_spp - spp)
     secs = time.perf_counter() - t0
     return {"target_rel_mse": target, "eps": 1e-2, "seconds": secs, "spp": spp,
             "rel_mse": err.value, "reached": err.value <= target, "reference_spp": ref_spp,
-            "chunk_spp": chunk, "path_samples": s.width * s.height * spp}
+            "reference_seed_offset": 1 << 24, "render_calls": calls,
+            "path_samples": s.width * s.height * spp}
 
 
 def bench_serving(api, _abi, n_requests, rates=(200.0, 25.0)):
