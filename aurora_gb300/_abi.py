@@ -163,6 +163,7 @@ SIGNATURES = {
     "agb_context_destroy": (_I32, [_P]),
     "agb_last_error": (ctypes.c_char_p, []),
     "agb_context_memory": (_I32, [_P, ctypes.POINTER(_U64)]),
+    "agb_bytes_per_path": (_U64, []),
     "agb_view_create": (_I32, [_P, _P, ctypes.POINTER(_P)]),
     "agb_wait_poll": (_I32, [_P]),
     "agb_server_create": (_I32, [_I32, _U64, _I32, ctypes.POINTER(_P)]),

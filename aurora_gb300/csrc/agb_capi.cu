@@ -682,6 +682,11 @@ AGB_API agb_status agb_geometry_create(agb_context* ctx, const float* positions,
     return rebuildMeshTable(ctx);
 }
 
+AGB_API uint64_t agb_bytes_per_path(void)
+{
+    return kPathStateBytes + kPathQueueBytes;
+}
+
 AGB_API agb_status agb_set_bvh_builder(agb_context* ctx, int32_t builder)
 {
     if (!ctx || (builder != AGB_BVH_HOST && builder != AGB_BVH_GPU))

@@ -38,9 +38,8 @@ double msSince(Clock::time_point t0, Clock::time_point t1)
     return std::chrono::duration<double, std::milli>(t1 - t0).count();
 }
 
-// Paths in flight per request wave; bounds a slot's wave buffers (about 0.6 KB per path).
+// Paths in flight per request wave; bounds a slot's wave buffers (agb_bytes_per_path each).
 constexpr uint64_t kServeWavePaths = 1u << 21;
-constexpr uint64_t kBytesPerPath   = 640;
 // Per pixel: running mean, Kahan sum and compensation, last sample (16 B each), moments (8 B),
 // AOVs (52 B), temporal history (32 B).
 constexpr uint64_t kBytesPerPixel = 4 * 16 + 8 + 52 + 32;
@@ -70,7 +69,7 @@ uint64_t estimateBytes(const agb_serve_request& r)
     uint64_t pixels = uint64_t(r.width) * r.height;
     uint64_t spw    = std::max<uint64_t>(1, kServeWavePaths / std::max<uint64_t>(1, pixels));
     uint64_t paths  = std::min<uint64_t>(r.spp, spw) * pixels;
-    return pixels * kBytesPerPixel + paths * kBytesPerPath + (1u << 20);
+    return pixels * kBytesPerPixel + paths * agb_bytes_per_path() + (1u << 20);
 }
 
 } // namespace

@@ -307,6 +307,9 @@ AGB_API agb_status agb_context_destroy(agb_context* ctx);
 AGB_API const char* agb_last_error(void);
 /* Bytes of device memory the context holds. */
 AGB_API agb_status agb_context_memory(agb_context* ctx, uint64_t* bytes);
+/* Device bytes a render wave holds per path in flight (path state and ray / hit / shadow queues),
+ * for hosts that size max_paths_in_flight or budget memory themselves.  No reference counterpart. */
+AGB_API uint64_t agb_bytes_per_path(void);
 /* A view renders the scene of ctx with its own stream (null: a new one), frame data and render
  * buffers (accumulation, AOVs, temporal history): several views of one resident scene render
  * concurrently.  Every render-side call (agb_frame_set, agb_render, agb_accum_read, ...) takes a
