@@ -96,6 +96,28 @@ assert ENV_DTYPE.itemsize == 268
 
 ALIAS_DTYPE = np.dtype([("alias", "<u4"), _f("prob"), _f("pdf"), _f("_padding1")])
 
+# agb_ground_plane (IGroundPlane values, Aurora.h:780-806), 64 bytes.
+GROUND_PLANE_DTYPE = np.dtype([
+    _i("enabled"), _f("position", 3), _f("normal", 3), _f("shadow_opacity"), _f("shadow_color", 3),
+    _f("reflection_opacity"), _f("reflection_color", 3), _f("reflection_roughness"),
+])
+assert GROUND_PLANE_DTYPE.itemsize == 64
+
+
+def ground_plane(**values):
+    """An agb_ground_plane record with the reference's defaults for a new ground plane
+    (PTGroundPlane.cpp:42-51), overridden by `values`."""
+    g = np.zeros(1, GROUND_PLANE_DTYPE)
+    g["enabled"] = 1
+    g["normal"] = (0.0, 1.0, 0.0)
+    g["shadow_opacity"] = 1.0
+    g["reflection_opacity"] = 0.5
+    g["reflection_color"] = (0.5, 0.5, 0.5)
+    g["reflection_roughness"] = 0.1
+    for k, v in values.items():
+        g[k] = v
+    return g
+
 
 class Layer(ctypes.Structure):
     _fields_ = [("material", ctypes.c_int32), ("_pad", ctypes.c_int32),
@@ -183,6 +205,7 @@ SIGNATURES = {
     "agb_materials_set": (_I32, [_P, _P, _P, _U32]),
     "agb_instances_set": (_I32, [_P, _P, _U32]),
     "agb_environment_set": (_I32, [_P, _P, _I32, _I32]),
+    "agb_ground_plane_set": (_I32, [_P, _P]),
     "agb_environment_alias": (_I32, [_P, _P, _U64, ctypes.POINTER(ctypes.c_double),
                                       ctypes.POINTER(ctypes.c_double)]),
     "agb_set_environment_table": (_I32, [_P, _I32]),

@@ -92,6 +92,10 @@ class Renderer:
         check(lib.agb_environment_set(self.ctx, ptr(env.reshape(1)),
                                       imgs[s.env_light] if s.env_light >= 0 else -1,
                                       imgs[s.env_background] if s.env_background >= 0 else -1))
+        gp = getattr(s, "ground_plane", None)
+        gp = None if gp is None else np.ascontiguousarray(
+            np.asarray(gp, dtype=_abi.GROUND_PLANE_DTYPE).reshape(1))
+        check(lib.agb_ground_plane_set(self.ctx, ptr(gp)))
         self.set_frame(s.frame)
         self.scene = s
 

@@ -3,11 +3,14 @@
 // and save): load a Wavefront OBJ scene, frame the camera (or take --eye / --target), add the
 // distant light and an optional lat-long Radiance HDR environment, render --output_spp samples and
 // write the image (.png: the 8-bit post-processed buffer; .pfm: the float post-processed buffer).
+// --ground_shadow / --ground_reflection switch on Plasma's ground plane at the scene's lower bound
+// (Plasma.cpp:941-942, 989-996): matte shadow opacity 1, matte reflection opacity 0.5.
 //
 // usage: agb_render <scene.obj> --output <file.png|file.pfm> [--output_spp N] [--dims W,H]
 //          [--eye x,y,z] [--target x,y,z] [--up x,y,z] [--fov degrees] [--env file.hdr]
 //          [--lightDir x,y,z] [--lightColor r,g,b] [--lightIntensity v] [--trace-depth N]
-//          [--russian_roulette 0|1] [--gamma_correction 0|1]
+//          [--russian_roulette 0|1] [--gamma_correction 0|1] [--ground_shadow 0|1]
+//          [--ground_reflection 0|1]
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -114,7 +117,8 @@ int main(int argc, char** argv)
             "usage: agb_render <scene.obj> --output <file.png|file.pfm> [--output_spp N] [--dims W,H]\n"
             "       [--eye x,y,z] [--target x,y,z] [--up x,y,z] [--fov degrees] [--env file.hdr]\n"
             "       [--lightDir x,y,z] [--lightColor r,g,b] [--lightIntensity v] [--trace-depth N]\n"
-            "       [--russian_roulette 0|1] [--gamma_correction 0|1]\n");
+            "       [--russian_roulette 0|1] [--gamma_correction 0|1] [--ground_shadow 0|1]\n"
+            "       [--ground_reflection 0|1]\n");
         return 2;
     }
     try
@@ -177,6 +181,18 @@ int main(int argc, char** argv)
                 { { Names::EnvironmentProperties::kLightImage, std::string("/environment/image") },
                     { Names::EnvironmentProperties::kBackgroundImage, std::string("/environment/image") } });
             scene->setEnvironment("/environment");
+        }
+
+        const bool groundShadow     = a.count("ground_shadow") && std::atoi(a["ground_shadow"].c_str()) != 0;
+        const bool groundReflection = a.count("ground_reflection") && std::atoi(a["ground_reflection"].c_str()) != 0;
+        if (groundShadow || groundReflection)
+        {
+            IGroundPlanePtr ground = renderer->createGroundPlanePointer();
+            ground->values().setFloat3("position", contents.boundsMin);
+            ground->values().setBoolean("enabled", true);
+            ground->values().setFloat("shadow_opacity", groundShadow ? 1.f : 0.f);
+            ground->values().setFloat("reflection_opacity", groundReflection ? 0.5f : 0.f);
+            scene->setGroundPlanePointer(ground);
         }
 
         renderer->setScene(scene);

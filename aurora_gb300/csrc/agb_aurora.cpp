@@ -160,6 +160,44 @@ public:
     IValues& values() override { return v; }
 };
 
+class GroundPlane : public IGroundPlane
+{
+public:
+    Values v;
+    GroundPlane()
+    {
+        // PTGroundPlane.cpp:42-51.
+        v.setBoolean("enabled", true);
+        v.setFloat3("position", { 0.f, 0.f, 0.f });
+        v.setFloat3("normal", { 0.f, 1.f, 0.f });
+        v.setFloat("shadow_opacity", 1.f);
+        v.setFloat3("shadow_color", { 0.f, 0.f, 0.f });
+        v.setFloat("reflection_opacity", 0.5f);
+        v.setFloat3("reflection_color", { 0.5f, 0.5f, 0.5f });
+        v.setFloat("reflection_roughness", 0.1f);
+    }
+    IValues& values() override { return v; }
+    agb_ground_plane data() const
+    {
+        agb_ground_plane g{};
+        g.enabled = v.asBool("enabled", true) ? 1 : 0;
+        vec3 p = v.asFloat3("position", { 0.f, 0.f, 0.f }), n = v.asFloat3("normal", { 0.f, 1.f, 0.f });
+        vec3 sc = v.asFloat3("shadow_color", { 0.f, 0.f, 0.f });
+        vec3 rc = v.asFloat3("reflection_color", { 0.5f, 0.5f, 0.5f });
+        for (int k = 0; k < 3; k++)
+        {
+            g.position[k]         = p[k];
+            g.normal[k]           = n[k];
+            g.shadow_color[k]     = sc[k];
+            g.reflection_color[k] = rc[k];
+        }
+        g.shadow_opacity       = v.asFloat("shadow_opacity", 1.f);
+        g.reflection_opacity   = v.asFloat("reflection_opacity", 0.5f);
+        g.reflection_roughness = v.asFloat("reflection_roughness", 0.1f);
+        return g;
+    }
+};
+
 class RenderBuffer : public IRenderBuffer
 {
 public:
@@ -264,6 +302,7 @@ public:
     std::map<Path, Properties> environments;
     std::vector<std::pair<Path, Instance>> instances; // insertion order
     std::vector<std::shared_ptr<Light>> lights;
+    std::shared_ptr<GroundPlane> groundPlane; // null: the default, disabled plane
     Path environment;
     bool hasBounds = false;
     vec3 bmin{}, bmax{};
@@ -352,6 +391,24 @@ public:
         bmin      = mn;
         bmax      = mx;
         hasBounds = true;
+    }
+    void setGroundPlanePointer(const IGroundPlanePtr& g) override
+    {
+        groundPlane = std::dynamic_pointer_cast<GroundPlane>(g);
+        if (g && !groundPlane)
+            throw Error("setGroundPlanePointer: not a ground plane of this renderer");
+    }
+    // The ground plane's current values, read at every render as the reference's
+    // PTGroundPlane::update does (PTScene.cpp:779).
+    void applyGroundPlane()
+    {
+        if (!groundPlane)
+        {
+            check(agb_ground_plane_set(ctx, nullptr), "ground plane");
+            return;
+        }
+        agb_ground_plane g = groundPlane->data();
+        check(agb_ground_plane_set(ctx, &g), "ground plane");
     }
     ILightPtr addLightPointer(const std::string& type) override
     {
@@ -653,6 +710,7 @@ public:
             agb_context_destroy(ctx);
     }
     IScenePtr createScene() override { return std::make_shared<Scene>(); }
+    IGroundPlanePtr createGroundPlanePointer() override { return std::make_shared<GroundPlane>(); }
     void setScene(const IScenePtr& s) override
     {
         scene = std::dynamic_pointer_cast<Scene>(s);
@@ -766,6 +824,7 @@ public:
             throw Error("render: no Final target");
         auto* target = dynamic_cast<RenderBuffer*>(it->second.get());
         scene->activate(ctx);
+        scene->applyGroundPlane();
         agb_frame_data f = frameData(uint32_t(target->w), uint32_t(target->h));
         check(agb_frame_set(ctx, &f), "render");
         agb_render_options o;

@@ -140,6 +140,7 @@ struct agb_context
     double envIntegral     = 0.0; // FP64 luminance integral
     double envShadingIntegral = 0.0;
     int32_t envLayout      = AGB_ENV_TABLE_REFERENCE;
+    DevGroundPlane ground{}; // disabled until agb_ground_plane_set
 
     agb_frame_data frame{};
     bool frameSet = false;
@@ -198,7 +199,8 @@ struct agb_context
             s.envLight = images[envLight]->view;
         if (envBackground >= 0 && size_t(envBackground) < images.size())
             s.envBackground = images[envBackground]->view;
-        s.alias = alias.as<agb_alias_entry>();
+        s.alias  = alias.as<agb_alias_entry>();
+        s.ground = ground;
         return s;
     }
 };
@@ -971,6 +973,51 @@ AGB_API agb_status agb_set_environment_table(agb_context* ctx, int32_t layout)
     return AGB_OK;
 }
 
+AGB_API agb_status agb_ground_plane_set(agb_context* ctx, const agb_ground_plane* plane)
+{
+    if (ctx && ctx->parent)
+        return fail(AGB_ERR_INVALID_ARG, "agb_ground_plane_set: a view shares its parent's scene; change the parent");
+    if (!ctx)
+        return fail(AGB_ERR_INVALID_ARG, "agb_ground_plane_set: null context");
+    DevGroundPlane g{};
+    if (plane)
+    {
+        const float* n = plane->normal;
+        if (!(n[0] * n[0] + n[1] * n[1] + n[2] * n[2] > 0.f))
+            return fail(AGB_ERR_INVALID_ARG, "agb_ground_plane_set: zero or non-finite normal");
+        g.enabled = plane->enabled ? 1 : 0;
+        for (int k = 0; k < 3; k++)
+        {
+            g.position[k]        = plane->position[k];
+            g.normal[k]          = n[k];
+            g.shadowColor[k]     = plane->shadow_color[k];
+            g.reflectionColor[k] = plane->reflection_color[k];
+        }
+        g.shadowOpacity       = plane->shadow_opacity;
+        g.reflectionOpacity   = plane->reflection_opacity;
+        g.reflectionRoughness = plane->reflection_roughness;
+        // Tangent frame from the normal (PTGroundPlane.cpp:23-28): bitangent +Y unless the normal
+        // is within 0.999 of it, then +X; tangent = normalize(cross(bitangent, normal)),
+        // bitangent = cross(normal, tangent).
+        float b[3] = { 0.f, 1.f, 0.f };
+        if (!(std::fabs(n[1]) < 0.999f))
+        {
+            b[0] = 1.f;
+            b[1] = 0.f;
+        }
+        float t[3] = { b[1] * n[2] - b[2] * n[1], b[2] * n[0] - b[0] * n[2], b[0] * n[1] - b[1] * n[0] };
+        float inv  = 1.f / std::sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+        for (int k = 0; k < 3; k++)
+            g.tangent[k] = t[k] * inv;
+        const float* u = g.tangent;
+        g.bitangent[0] = n[1] * u[2] - n[2] * u[1];
+        g.bitangent[1] = n[2] * u[0] - n[0] * u[2];
+        g.bitangent[2] = n[0] * u[1] - n[1] * u[0];
+    }
+    ctx->ground = g;
+    return AGB_OK;
+}
+
 AGB_API agb_status agb_environment_alias(agb_context* ctx, agb_alias_entry* host_out,
     uint64_t capacity, double* shading_integral, double* fp64_integral)
 {
@@ -1169,11 +1216,15 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
         agb_render_stats r{};
         r.paths = uint64_t(sample_count) * pixels;
         for (uint32_t w = 0; w < waves; w++)
+        {
             for (int b = 0; b < depth; b++)
             {
                 r.closest_rays += c[counterWords * w + kCounterStride * b + CNT_RAYS];
                 r.shadow_rays += c[counterWords * w + kCounterStride * b + CNT_SHADOW];
             }
+            // Ground-plane matte-shadow rays (counter block depth + 1).
+            r.shadow_rays += c[counterWords * w + kCounterStride * (depth + 1) + CNT_SHADOW];
+        }
         r.node_visits        = s[2];
         r.tri_tests          = s[3];
         r.shadow_node_visits = s[5];

@@ -385,6 +385,9 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
     {
         uint32_t i     = base + threadIdx.x;
         bool valid     = i < n;
+        // A camera ray the ground plane turned into a reflection ray has nothing to shade here.
+        if (valid && bounce == 0 && !depthLimit && s.ground.enabled && wb.hitInst[i] == kGroundAbsorbed)
+            valid = false;
         bool pushNext  = false;
         uint32_t slots = 0;
         uint32_t p     = 0;
@@ -912,6 +915,182 @@ __device__ __forceinline__ void adjustRadiance(float maxLum, bool displayErrors,
         r = displayErrors ? v3{ 0.f, __int_as_float(0x7f800000), 0.f } : splat(0.f);
 }
 
+// ---------------------------------------------------------------------------- ground plane
+// sampleGGXSmithBRDF (BSDFCommon.slang:331-366) with anisotropy 0, tangent space: a GGX-Smith
+// VNDF half-vector (flipped for a lower-hemisphere view), the reflected direction and its PDF,
+// and the microfacet BRDF D G2 F / (4 |V.z| |L.z|) with Schlick Fresnel (BSDFCommon.slang:115-118,
+// 231-240, 310-327); black when V and L are in different hemispheres.
+AGB_D v3 sampleGGXSmithBRDF(v3 V, v3 f0, float roughness, v2 r, v3& L, float& pdf)
+{
+    float a   = fmaxf_(0.0001f, sqr(roughness)); // roughnessToAlpha, MIN_ALPHA
+    v2 alpha  = v2{ a, a };
+    bool flip = V.z <= 0.f;
+    v3 H      = sampleGGXVNDF(flip ? -V : V, alpha, r);
+    H         = flip ? -H : H;
+    L         = reflect(-V, H);
+    pdf       = ggxVNDF(V, H, alpha) / (4.f * dot(V, H));
+    if (!(V.z * L.z > 0.f))
+        return splat(0.f);
+    v3 Hn    = normalize(V + L);
+    float D  = ggxNDF(Hn, alpha);
+    float G2 = (dot(V, Hn) <= 0.f || dot(L, Hn) < 0.f)
+        ? 0.f
+        : 1.f / (1.f + ggxLambda(V, alpha) + ggxLambda(L, alpha));
+    float w  = agb_fm::pow(1.f - dot(V, Hn), 5.f);
+    v3 F     = f0 + (splat(1.f) - f0) * w;
+    return F * (D * G2) / (4.f * fabsf(V.z) * fabsf(L.z));
+}
+
+// The ground plane for the camera rays of bounce 0 (evaluateGroundPlane, GroundPlane.slang:236-289,
+// called first by the closest-hit and miss shaders while the ray is primary), after their
+// closest-hit traversal and before shading.  A ray that meets the plane from its front side
+// nearer than its hit (any distance on a miss) draws from its own random stream, in the
+// reference's order:
+//   - with probability 1 - luminance(1 - reflection opacity) it becomes a matte reflection ray
+//     (setupMatteReflectionIndirectLightRay): GGX-Smith sample about the plane's frame, the
+//     contribution scaled by bsdf cos / pdf x opacity / (1 - Pr), the guide AOVs of the plane
+//     written, the next segment appended as GROUND_PLANE_REFLECTION_RAY and the hit marked
+//     absorbed.  A black BSDF sample leaves the ray unabsorbed with only the opacity scale;
+//   - otherwise the contribution is scaled by the transparency / Pr and, with a shadow opacity,
+//     an environment sample above the plane is traced as an opaque shadow ray (shadeMatteShadow,
+//     GroundPlane.slang:71-104) in counter block `shadowBlock`; k_ground_shadow applies it.
+__global__ void k_ground(DevScene s, agb_frame_data f, WaveParams wp, WaveBuffers wb, int shadowBlock)
+{
+    const DevGroundPlane& g = s.ground;
+    uint32_t n      = wb.counters[CNT_RAYS];
+    uint32_t stride = gridDim.x * blockDim.x;
+    const v3 N = ld3(g.normal), X = ld3(g.tangent), Y = ld3(g.bitangent), P0 = ld3(g.position);
+    v2 screen  = v2{ float(wp.width), float(wp.height) };
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride)
+    {
+        uint32_t i      = base + threadIdx.x;
+        uint32_t p      = 0;
+        bool reflectRay = false, shadowRay = false;
+        v3 hitPos = splat(0.f), nextD = splat(0.f), shadowL = splat(0.f);
+        if (i < n)
+        {
+            p         = wb.rayPath[0][i];
+            float4 o4 = wb.rayOrg[0][i], d4 = wb.rayDir[0][i];
+            v3 o      = v3{ o4.x, o4.y, o4.z }, d = v3{ d4.x, d4.y, d4.z };
+            // RayTCurrent(): the hit distance, or the ray's TMax (infinity) on a miss.
+            float tCur = wb.hitInst[i] >= 0 ? wb.hitTUV[i].x : d4.w;
+            // intersectGroundPlane (GroundPlane.slang:106-131).
+            float planeDot = dot(d, N);
+            bool onPlane   = false;
+            float dist     = 0.f;
+            if (!(planeDot >= 0.f))
+            {
+                dist    = dot(P0 - o, N) / planeDot;
+                onPlane = !(dist < 0.f);
+            }
+            if (onPlane && dist < tCur)
+            {
+                hitPos = o + d * dist;
+                Rng rng;
+                {
+                    uint2 r = wb.rng[p];
+                    rng     = Rng{ r.x, r.y };
+                }
+                // setupGroundPlaneRay (GroundPlane.slang:136-193).
+                v3 color     = splat(1.f);
+                bool decided = false;
+                if (g.reflectionOpacity > 0.f)
+                {
+                    v3 transparency = splat(1.f - g.reflectionOpacity);
+                    float Pr        = luminance(transparency);
+                    if (random2D(rng).x >= Pr)
+                    {
+                        v3 V = v3{ dot(-d, X), dot(-d, Y), dot(-d, N) };
+                        v3 L;
+                        float pdf;
+                        v2 r      = random2D(rng);
+                        v3 bsdf   = sampleGGXSmithBRDF(V, ld3(g.reflectionColor), g.reflectionRoughness, r, L, pdf);
+                        bsdf      = bsdf * fabsf(L.z);
+                        if (!isBlack(bsdf))
+                        {
+                            nextD      = X * L.x + Y * L.y + N * L.z;
+                            color      = bsdf / pdf;
+                            reflectRay = true;
+                        }
+                        color   = color * (g.reflectionOpacity / (1.f - Pr));
+                        decided = true;
+                    }
+                    else
+                        color = transparency / Pr;
+                }
+                if (!decided && g.shadowOpacity > 0.f)
+                {
+                    v3 L;
+                    float pdf;
+                    sampleEnvironment(s, random2D(rng), L, pdf);
+                    // Below the plane the light casts no shadow: the shadow blend is zero and the
+                    // colour stays as it is.
+                    if (!(dot(L, N) < 0.f))
+                    {
+                        shadowRay = true;
+                        shadowL   = L;
+                    }
+                }
+                wb.rng[p]     = make_uint2(rng.x, rng.y);
+                float4 c4     = wb.contrib[p];
+                wb.contrib[p] = make_float4(c4.x * color.x, c4.y * color.y, c4.z * color.z, 0.f);
+                if (reflectRay)
+                {
+                    wb.hitInst[i] = kGroundAbsorbed;
+                    wb.flags[p]   = pfSetRayType(wb.flags[p] & ~PF_PRIMARY, GROUND_PLANE_REFLECTION_RAY);
+                    if (wp.sampleBase + p / wp.pixels == wp.aovSample)
+                    {
+                        // writeGroundPlaneGuideAOVs (GroundPlane.slang:197-233).
+                        uint32_t pixel      = p % wp.pixels;
+                        float vz            = viewDepth(f.camera_inv_view, hitPos);
+                        wb.aovDepth[pixel]  = vz;
+                        wb.aovNormal[pixel] = make_float4(N.x, N.y, N.z, fmaxf_(g.reflectionRoughness, 0.05f));
+                        wb.aovAlbedo[pixel] = make_float4(g.reflectionColor[0], g.reflectionColor[1],
+                            g.reflectionColor[2], 0.f);
+                        wb.aovMotion[pixel] = surfaceMotion(f.camera_view_proj, f.camera_view_proj_prev,
+                            f.camera_inv_view_prev, hitPos, vz, screen.x, screen.y);
+                    }
+                }
+            }
+        }
+        uint32_t slotNext = warpAppend(wb.counters + kCounterStride + CNT_RAYS, reflectRay);
+        if (reflectRay)
+        {
+            wb.rayOrg[1][slotNext]  = make_float4(hitPos.x, hitPos.y, hitPos.z, kRayTMin);
+            wb.rayDir[1][slotNext]  = make_float4(nextD.x, nextD.y, nextD.z, __int_as_float(0x7f800000));
+            wb.rayPath[1][slotNext] = p;
+        }
+        uint32_t slotShadow = warpAppend(wb.counters + shadowBlock * kCounterStride + CNT_SHADOW, shadowRay);
+        if (shadowRay)
+        {
+            wb.shOrg[p]                           = make_float4(hitPos.x, hitPos.y, hitPos.z, 0.f);
+            wb.shDir[size_t(p) * kMaxShadowSlots] = make_float4(shadowL.x, shadowL.y, shadowL.z, 0.f);
+            wb.shTag[slotShadow]                  = p << 3;
+            wb.occluded[p]                        = 0u;
+        }
+    }
+}
+
+// The matte shadow of the ground plane (GroundPlane.slang:171-182): a camera ray whose opaque
+// shadow ray was blocked has its contribution scaled by lerp(1, shadow colour, luminance(1 - 0) x
+// shadow opacity); an unblocked one by lerp(1, shadow colour, 0) = 1.
+__global__ void k_ground_shadow(DevScene s, WaveBuffers wb, int shadowBlock)
+{
+    const DevGroundPlane& g = s.ground;
+    uint32_t n      = wb.counters[shadowBlock * kCounterStride + CNT_SHADOW];
+    uint32_t stride = gridDim.x * blockDim.x;
+    v3 blend = lerp3(splat(1.f), ld3(g.shadowColor), luminance(splat(1.f) - splat(0.f)) * g.shadowOpacity);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        uint32_t p = wb.shTag[i] >> 3;
+        if (wb.occluded[p] & 1u)
+        {
+            float4 c4     = wb.contrib[p];
+            wb.contrib[p] = make_float4(c4.x * blend.x, c4.y * blend.y, c4.z * blend.z, 0.f);
+        }
+    }
+}
+
 // Per pixel: final radiance of each sample of the wave in sample order, then accumulation.
 __global__ void k_finalize(agb_frame_data f, WaveParams wp, WaveBuffers wb)
 {
@@ -1018,6 +1197,21 @@ void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp
             k_trace_closest<true><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, cur);
         else
             k_trace_closest<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, cur);
+        if (b == 0 && s.ground.enabled)
+        {
+            // Ground plane before the camera rays are shaded; its shadow rays use the spare
+            // counter block depth + 1.
+            mark(KC_SHADE);
+            k_ground<<<grid, 256, 0, st>>>(s, f, wp, wb, depth + 1);
+            mark(KC_SHADOW);
+            if (wp.countTraversal)
+                k_trace_shadow<true><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, depth + 1);
+            else
+                k_trace_shadow<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, depth + 1);
+            mark(KC_SHADE);
+            k_ground_shadow<<<grid, 256, 0, st>>>(s, wb, depth + 1);
+            launches += 3;
+        }
         mark(KC_SHADE);
         k_shade<<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 0);
         mark(KC_SHADE);

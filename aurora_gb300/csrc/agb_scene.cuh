@@ -63,6 +63,22 @@ struct DevInstance
     int32_t layerOffset; // into DevScene::layers
 };
 
+// Ground plane constants (the GroundPlane struct of GroundPlane.slang; PTGroundPlane.cpp:62-83):
+// the caller's properties plus the tangent frame built from the normal.
+struct DevGroundPlane
+{
+    int32_t enabled;
+    float position[3];
+    float normal[3];
+    float tangent[3];
+    float bitangent[3];
+    float shadowOpacity;
+    float shadowColor[3];
+    float reflectionOpacity;
+    float reflectionColor[3];
+    float reflectionRoughness;
+};
+
 struct DevScene
 {
     const DevMesh* meshes;
@@ -82,6 +98,7 @@ struct DevScene
     DevImage envLight;        // data null when absent
     DevImage envBackground;   // data null when absent
     const agb_alias_entry* alias;
+    DevGroundPlane ground;
 };
 
 // -------------------------------------------------------------------------- texture sampling

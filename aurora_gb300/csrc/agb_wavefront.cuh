@@ -11,6 +11,8 @@ namespace agb
 constexpr int kShadePointWords = 10; // float4 per shading point handed between the shading kernels
 constexpr int kMisWords        = 3;  // float4 of the environment-MIS sample per shading point
 constexpr int kMaxShadowSlots = 6; // up to 4 distant lights + 2 environment-MIS rays per hit
+// hitInst value of a camera ray absorbed by the ground plane's matte reflection: k_shade skips it.
+constexpr int32_t kGroundAbsorbed = -2;
 
 // Per-bounce device counters (kCounterStride words per bounce).
 enum : int

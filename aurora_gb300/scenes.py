@@ -311,6 +311,7 @@ class SceneDesc:
         self.env = environment()
         self.env_light = -1     # image index
         self.env_background = -1
+        self.ground_plane = None  # GROUND_PLANE_DTYPE record (_abi.ground_plane()) or None
         self.frame = None
         self.width = 0
         self.height = 0

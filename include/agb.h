@@ -211,6 +211,24 @@ typedef struct agb_alias_entry
     float _padding1;
 } agb_alias_entry;
 
+/* Ground plane (IGroundPlane, Aurora.h:780-806; the GPU constant data of PTGroundPlane.cpp:62-83):
+ * an invisible plane that catches matte shadows of the environment light and a matte GGX
+ * reflection, seen by camera rays only (GroundPlane.slang).  The side the normal points away from
+ * is not rendered.  Defaults of a new ground plane (PTGroundPlane.cpp:42-51): enabled, position
+ * 0, normal +Y, shadow opacity 1, shadow colour 0, reflection opacity 0.5, reflection colour 0.5,
+ * reflection roughness 0.1.  The tangent frame is built from the normal. */
+typedef struct agb_ground_plane
+{
+    int32_t enabled;
+    float position[3];
+    float normal[3];
+    float shadow_opacity;
+    float shadow_color[3];
+    float reflection_opacity;
+    float reflection_color[3];
+    float reflection_roughness;
+} agb_ground_plane;
+
 /* ------------------------------------------------------------------------------------------ */
 /* Scene description.                                                                          */
 /* ------------------------------------------------------------------------------------------ */
@@ -373,6 +391,9 @@ AGB_API agb_status agb_instances_set(agb_context* ctx, const agb_instance* insta
  * light_tex_luminance_integral. */
 AGB_API agb_status agb_environment_set(agb_context* ctx, const agb_environment_data* env,
     int32_t light_image, int32_t background_image);
+/* Sets the scene's ground plane (IScene::setGroundPlanePointer, PTScene.cpp:660-667); null
+ * removes it (the renderer's default plane is disabled, PTRenderer.cpp:713-727). */
+AGB_API agb_status agb_ground_plane_set(agb_context* ctx, const agb_ground_plane* plane);
 /* Reads back the environment alias table (width*height entries), the luminance integral the
  * shading divides by, and the FP64 luminance integral (either pointer may be null). */
 AGB_API agb_status agb_environment_alias(agb_context* ctx, agb_alias_entry* host_out,

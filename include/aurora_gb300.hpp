@@ -178,6 +178,17 @@ public:
 };
 using ILightPtr = std::shared_ptr<ILight>;
 
+// Ground plane (Aurora.h:780-806): values "enabled" (bool), "position", "normal" (float3),
+// "shadow_opacity", "reflection_opacity", "reflection_roughness" (float), "shadow_color",
+// "reflection_color" (float3); defaults as PTGroundPlane.cpp:42-51.
+class IGroundPlane
+{
+public:
+    virtual IValues& values()   = 0;
+    virtual ~IGroundPlane()     = default;
+};
+using IGroundPlanePtr = std::shared_ptr<IGroundPlane>;
+
 // A render target (Aurora.h:714-747): RGBA8 (Integer_RGBA) or RGBA32F (Float_RGBA).
 class IRenderBuffer
 {
@@ -207,6 +218,8 @@ public:
     virtual bool setEnvironment(const Path& environment)                                  = 0;
     virtual void setBounds(const vec3& min, const vec3& max)                              = 0;
     virtual ILightPtr addLightPointer(const std::string& lightType)                       = 0;
+    // Null restores the renderer's default ground plane, which is disabled (PTScene.cpp:660-667).
+    virtual void setGroundPlanePointer(const IGroundPlanePtr& pGroundPlane)               = 0;
     virtual ~IScene() = default;
 };
 using IScenePtr = std::shared_ptr<IScene>;
@@ -227,6 +240,7 @@ public:
         CUDA
     };
     virtual IScenePtr createScene()                                                   = 0;
+    virtual IGroundPlanePtr createGroundPlanePointer()                                = 0;
     virtual void setScene(const IScenePtr& pScene)                                    = 0;
     virtual IRenderBufferPtr createRenderBuffer(int width, int height, ImageFormat format) = 0;
     virtual void setTargets(const TargetAssignments& targetAssignments)               = 0;

@@ -172,6 +172,8 @@ ORC_API int orc_layout(int which)
         return int(sizeof(Scene));
     case 7:
         return int(sizeof(Layer));
+    case 8:
+        return int(sizeof(GroundPlaneData));
     default:
         return -1;
     }
@@ -326,6 +328,14 @@ ORC_API void orc_tracer_set_seed_offset(void* handle, uint32_t seedOffset)
 {
     OrcTracer* t = static_cast<OrcTracer*>(handle);
     t->f32.seedOffset = t->f64.seedOffset = seedOffset;
+}
+
+// The scene's ground plane (null: none), restated in GroundPlane.slang's order by the tracer.
+ORC_API void orc_tracer_set_ground_plane(void* handle, const GroundPlaneData* g)
+{
+    OrcTracer* t = static_cast<OrcTracer*>(handle);
+    t->f32.setGroundPlane(g);
+    t->f64.setGroundPlane(g);
 }
 
 // Denoising AOV targets (width*height: depth 1 float, normal / albedo / motion 4 floats per

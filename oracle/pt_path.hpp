@@ -81,6 +81,20 @@ struct Scene
     const AliasEntry* envAlias       = nullptr;
 };
 
+// Ground plane: the layout of the C ABI's agb_ground_plane (the caller's IGroundPlane values,
+// Aurora.h:780-806; PTGroundPlane.cpp:62-83).  enabled == 0: no ground plane.
+struct GroundPlaneData
+{
+    int32_t enabled           = 0;
+    float position[3]         = { 0.f, 0.f, 0.f };
+    float normal[3]           = { 0.f, 1.f, 0.f };
+    float shadowOpacity       = 1.f;
+    float shadowColor[3]      = { 0.f, 0.f, 0.f };
+    float reflectionOpacity   = 0.5f;
+    float reflectionColor[3]  = { 0.5f, 0.5f, 0.5f };
+    float reflectionRoughness = 0.1f;
+};
+
 template <class T>
 struct PathTracer
 {
@@ -118,6 +132,36 @@ struct PathTracer
         env.lightImage = s->envLight;
         env.background = s->envBackground;
         env.alias      = s->envAlias;
+    }
+
+    // The scene's ground plane and the tangent frame the host builds from its normal
+    // (PTGroundPlane.cpp:23-28, in FP32 as the constant buffer holds it).
+    GroundPlaneData ground;
+    float groundTangent[3]   = { 1.f, 0.f, 0.f };
+    float groundBitangent[3] = { 0.f, 0.f, 1.f };
+    void setGroundPlane(const GroundPlaneData* g)
+    {
+        ground = g ? *g : GroundPlaneData{};
+        if (!g)
+        {
+            ground.enabled = 0;
+            return;
+        }
+        const float* n = ground.normal;
+        float b[3]     = { 0.f, 1.f, 0.f };
+        if (!(std::fabs(n[1]) < 0.999f))
+        {
+            b[0] = 1.f;
+            b[1] = 0.f;
+        }
+        float t[3] = { b[1] * n[2] - b[2] * n[1], b[2] * n[0] - b[0] * n[2], b[0] * n[1] - b[1] * n[0] };
+        float inv  = 1.f / std::sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+        for (int k = 0; k < 3; k++)
+            groundTangent[k] = t[k] * inv;
+        const float* u     = groundTangent;
+        groundBitangent[0] = n[1] * u[2] - n[2] * u[1];
+        groundBitangent[1] = n[2] * u[0] - n[0] * u[2];
+        groundBitangent[2] = n[0] * u[1] - n[1] * u[0];
     }
 
     // RayTrace.slang:130-182
@@ -503,6 +547,146 @@ struct PathTracer
         }
     }
 
+    // sampleGGXSmithBRDF (BSDFCommon.slang:331-366) with anisotropy 0: roughnessToAlpha
+    // (BSDFCommon.slang:194-204), the VNDF half-vector flipped for a lower-hemisphere view, the
+    // reflected direction and its PDF, then evaluateGGXSmithBRDF (BSDFCommon.slang:310-327:
+    // D G2 F / (4 |V.z| |L.z|), Schlick Fresnel BSDFCommon.slang:115-118, Smith G2 :231-240).
+    static v3 sampleGGXSmithBRDF(const v3& V, const v3& f0, T roughness, v2 random, v3& L, T& pdf)
+    {
+        T a       = B::fmax_(T(0.0001f), roughness * roughness);
+        v2 alpha(a * (T(1) + T(0)), a * (T(1) - T(0)));
+        bool flip = V.z <= T(0);
+        v3 H      = B::sampleGGXSmithVNDF(flip ? -V : V, alpha, random);
+        H         = flip ? -H : H;
+        L         = reflect(-V, H);
+        T denom   = T(4) * dot(V, H);
+        pdf       = B::evaluateGGXSmithVNDF(V, H, alpha) / denom;
+        if (!(V.z * L.z > T(0)))
+            return v3(0);
+        v3 Hn = normalize(V + L);
+        T D   = B::evaluateGGXNDF(Hn, alpha);
+        T G2  = (dot(V, Hn) <= T(0) || dot(L, Hn) < T(0))
+            ? T(0)
+            : T(1) / (T(1) + B::lambda(V, alpha) + B::lambda(L, alpha));
+        v3 F  = lerp(f0, v3(1), tpow(T(1) - dot(V, Hn), T(5)));
+        return F * (D * G2) / (T(4) * std::fabs(V.z) * std::fabs(L.z));
+    }
+
+    // writeGroundPlaneGuideAOVs (GroundPlane.slang:197-233).
+    void writeGroundAov(size_t i, const v3& pos) const
+    {
+        const FrameData& f = *frame;
+        using TP           = Temporal<T>;
+        T vz               = TP::viewZ(f.cameraInvView, pos);
+        aovDepth[i]        = float(vz);
+        const GroundPlaneData& g = ground;
+        float rough = g.reflectionRoughness > 0.05f ? g.reflectionRoughness : 0.05f;
+        float nr[4] = { g.normal[0], g.normal[1], g.normal[2], rough };
+        float al[4] = { g.reflectionColor[0], g.reflectionColor[1], g.reflectionColor[2], 0.f };
+        T mv[4];
+        TP::motionVector(f.cameraViewProj, f.cameraViewProjPrev, f.cameraInvViewPrev, pos, vz,
+            T(float(screenW)), T(float(screenH)), mv);
+        for (int k = 0; k < 4; k++)
+        {
+            aovNormal[4 * i + k] = nr[k];
+            aovAlbedo[4 * i + k] = al[k];
+            aovMotion[4 * i + k] = float(mv[k]);
+        }
+    }
+
+    // evaluateGroundPlane (GroundPlane.slang:236-289), run first by the closest-hit and miss
+    // shaders: tCurrent is RayTCurrent() (the hit distance, infinity on a miss).  Returns true when
+    // the ray was absorbed, i.e. continues as a matte reflection ray.
+    bool evaluateGroundPlane(Payload& p, const v3& rayOrigin, const v3& rayDirection, T tCurrent,
+        int64_t aovPixel) const
+    {
+        const GroundPlaneData& g = ground;
+        if (!p.isPrimaryRay || !g.enabled)
+            return false;
+        // intersectGroundPlane (GroundPlane.slang:106-131).
+        v3 N       = v3::from(g.normal);
+        T planeDot = dot(rayDirection, N);
+        if (planeDot >= T(0))
+            return false;
+        T dist = dot(v3::from(g.position) - rayOrigin, N) / planeDot;
+        if (dist < T(0))
+            return false;
+        v3 pos = rayOrigin + rayDirection * dist;
+        if (!(dist < tCurrent))
+            return false;
+        // setupGroundPlaneRay (GroundPlane.slang:136-193).
+        v3 X = v3::from(groundTangent), Y = v3::from(groundBitangent);
+        v3 color(1), nextDir(0), nextOrg(0);
+        int rayType = CAMERA_RAY;
+        bool chosen = false;
+        if (g.reflectionOpacity > 0.f)
+        {
+            v3 transparency = v3(T(1) - T(g.reflectionOpacity));
+            T Pr            = luminance(transparency);
+            if (random2D<T>(p.rng).x >= Pr)
+            {
+                // setupMatteReflectionIndirectLightRay (GroundPlane.slang:26-67).
+                v3 V = B::worldToTangent(-rayDirection, X, Y, N);
+                v3 L;
+                T pdf;
+                v2 random = random2D<T>(p.rng);
+                v3 bsdf   = sampleGGXSmithBRDF(V, v3::from(g.reflectionColor), T(g.reflectionRoughness),
+                    random, L, pdf);
+                bsdf *= std::fabs(L.z);
+                if (isBlack(bsdf))
+                {
+                    rayType = NO_SECONDARY_RAY;
+                    color   = v3(1);
+                }
+                else
+                {
+                    nextOrg = pos;
+                    nextDir = B::tangentToWorld(L, X, Y, N);
+                    color   = bsdf / pdf;
+                    rayType = GROUND_PLANE_REFLECTION_RAY;
+                }
+                color *= T(g.reflectionOpacity) / (T(1) - Pr);
+                chosen = true;
+            }
+            else
+                color = transparency / Pr;
+        }
+        if (!chosen && g.shadowOpacity > 0.f)
+        {
+            // shadeMatteShadow (GroundPlane.slang:71-104): always an opaque shadow ray.
+            v3 L;
+            T pdf;
+            E::sampleEnvironment(env, random2D<T>(p.rng), L, pdf);
+            v3 shadowRGB(0);
+            T shadowA = T(0);
+            if (!(dot(L, N) < T(0)))
+            {
+                v3 vis(1);
+                if (1 != frame->traceDepth + 1)
+                {
+                    stats().shadowRaysTraced++;
+                    vis = caster.occluded(pos, L, Consts<T>::RAY_TMIN, T(INFINITY)) ? v3(0) : v3(1);
+                }
+                shadowRGB = v3::from(g.shadowColor);
+                shadowA   = luminance(v3(1) - vis) * T(g.shadowOpacity);
+            }
+            color *= lerp(v3(1), shadowRGB, shadowA);
+        }
+        if (rayType == GROUND_PLANE_REFLECTION_RAY)
+        {
+            if (aovPixel >= 0)
+                writeGroundAov(size_t(aovPixel), pos);
+            p.nextRayType      = GROUND_PLANE_REFLECTION_RAY;
+            p.rayContribution *= color;
+            p.nextRayDirection = nextDir;
+            p.nextRayOrigin    = nextOrg;
+            p.isPrimaryRay     = false;
+            return true;
+        }
+        p.rayContribution *= color;
+        return false;
+    }
+
     // Closest-hit shader (HitShaderEntryPoints.slang:35-486).  aovPixel: pixel index whose AOVs
     // this path writes, or -1.
     void closestHit(Payload& p, const v3& rayOrigin, const v3& rayDirection, const Hit& hit,
@@ -511,6 +695,8 @@ struct PathTracer
         const FrameData& f = *frame;
         int maxTraceDepth  = f.traceDepth;
         v3 nextRayContribution(1);
+        if (evaluateGroundPlane(p, rayOrigin, rayDirection, T(hit.t), aovPixel))
+            return;
         v3 V              = -rayDirection;
         ShadingData<T> sh = computeShadingData(hit.inst, uint32_t(hit.prim), T(hit.u), T(hit.v));
         const Instance& in = scene->instances[hit.inst];
@@ -728,7 +914,7 @@ struct PathTracer
                 stats().raysTraced++;
                 if (caster.closest(rayOrigin, rayDirection, minT, T(INFINITY), hit))
                     closestHit(p, rayOrigin, rayDirection, hit, pixel, aovPixel);
-                else
+                else if (!evaluateGroundPlane(p, rayOrigin, rayDirection, T(INFINITY), aovPixel))
                 {
                     bool bg = p.isPrimaryRay || p.rayType == TRANSMISSION_LOBE ||
                         p.rayType == GROUND_PLANE_REFLECTION_RAY;

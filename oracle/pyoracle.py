@@ -49,6 +49,7 @@ def lib():
         L.orc_fmath.argtypes = [ctypes.c_int, P, P, ctypes.c_int64, P]
         L.orc_tracer_set_aov.argtypes = [P, P, P, P, P]
         L.orc_tracer_set_seed_offset.argtypes = [P, ctypes.c_uint32]
+        L.orc_tracer_set_ground_plane.argtypes = [P, P]
         L.orc_temporal_resolve.argtypes = [ctypes.c_int, P, P, P, P, ctypes.c_int, ctypes.c_int,
                                            ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
                                            ctypes.c_float, P]
@@ -192,9 +193,13 @@ class OracleScene:
         if not hasattr(self, "_tracers"):
             self._tracers = {}
         if key not in self._tracers:
-            self._tracers[key] = lib().orc_tracer_create(precision, ctypes.byref(self.scene),
-                                                         _p(self.frame), self.desc.width,
-                                                         self.desc.height, 1 if brute else 0)
+            t = lib().orc_tracer_create(precision, ctypes.byref(self.scene), _p(self.frame),
+                                        self.desc.width, self.desc.height, 1 if brute else 0)
+            gp = getattr(self.desc, "ground_plane", None)
+            if gp is not None:
+                self._ground = np.ascontiguousarray(gp).reshape(1).copy()
+                lib().orc_tracer_set_ground_plane(t, _p(self._ground))
+            self._tracers[key] = t
         return self._tracers[key]
 
     def close(self):

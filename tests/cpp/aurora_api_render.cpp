@@ -14,6 +14,8 @@
 //   u32 lights; per light: f32 direction[3], color[3], intensity, angular diameter
 //   f32 light top[3], light bottom[3], background top[3], background bottom[3]
 //   u8 has environment image; if set: u32 width, height, f32 rgb[3 * width * height]
+//   optional: u8 has ground plane; if set: i32 enabled, f32 position[3], normal[3], shadow
+//     opacity, shadow colour[3], reflection opacity, reflection colour[3], reflection roughness
 // Output: u32 width, height, then f32 RGBA rows top to bottom.
 #include <cstdio>
 #include <cstring>
@@ -205,6 +207,24 @@ int main(int argc, char** argv)
         }
         scene->setEnvironmentProperties("/environment", envProps);
         scene->setEnvironment("/environment");
+        if (r.pos < r.buf.size() && r.get<uint8_t>())
+        {
+            IGroundPlanePtr ground = renderer->createGroundPlanePointer();
+            IValues& gv            = ground->values();
+            gv.setBoolean("enabled", r.get<int32_t>() != 0);
+            auto f3 = [&r]() {
+                auto a = r.array<float>(3);
+                return vec3{ a[0], a[1], a[2] };
+            };
+            gv.setFloat3("position", f3());
+            gv.setFloat3("normal", f3());
+            gv.setFloat("shadow_opacity", r.get<float>());
+            gv.setFloat3("shadow_color", f3());
+            gv.setFloat("reflection_opacity", r.get<float>());
+            gv.setFloat3("reflection_color", f3());
+            gv.setFloat("reflection_roughness", r.get<float>());
+            scene->setGroundPlanePointer(ground);
+        }
 
         renderer->setScene(scene);
         renderer->setOptions({ { "traceDepth", int(depth) } });

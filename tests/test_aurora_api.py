@@ -38,7 +38,7 @@ def test_cpp_client_builds_and_links():
 
 
 def write_scene(path, s, view, proj, lights, depth):
-    from aurora_gb300 import scenes
+    from aurora_gb300 import _abi, scenes
     b = bytearray(b"AGBS")
     b += struct.pack("<5I", 1, s.width, s.height, s.spp, depth)
     b += np.asarray(view, np.float32).T.tobytes()   # column-major
@@ -82,14 +82,28 @@ def write_scene(path, s, view, proj, lights, depth):
         b += np.asarray(im["pixels"], np.float32)[..., :3].tobytes()
     else:
         b += struct.pack("<B", 0)
+    gp = getattr(s, "ground_plane", None)
+    if gp is not None:
+        b += struct.pack("<B", 1) + np.asarray(gp, _abi.GROUND_PLANE_DTYPE).reshape(1).tobytes()
     open(path, "wb").write(bytes(b))
 
 
 @pytest.mark.gpu
-def test_cpp_interface_render_matches_c_abi(agb, oracle):
+@pytest.mark.parametrize("ground", [False, True])
+def test_cpp_interface_render_matches_c_abi(agb, oracle, ground):
+    """The same frame through the C++ interface and through the C ABI; with `ground`, the floor
+    quad is replaced by a ground plane (IRenderer::createGroundPlanePointer,
+    IScene::setGroundPlanePointer) with non-default values."""
     from aurora_gb300 import _abi, api, scenes
     exe = build_client()
     s = scenes.config_tiny(width=48, height=32, spp=8, lights=False)
+    if ground:
+        s.instances = s.instances[:4]   # the spheres (mesh 0); the floor quad is not referenced
+        s.meshes = s.meshes[:1]
+        s.ground_plane = _abi.ground_plane(position=(0.0, 0.05, 0.0), shadow_opacity=0.7,
+                                           shadow_color=(0.1, 0.2, 0.3), reflection_opacity=0.4,
+                                           reflection_color=(0.8, 0.6, 0.4),
+                                           reflection_roughness=0.2)
     # Matrices as the client holds them (FP32); angular diameter 0 so cos(radius) = 1 exactly.
     view = np.asarray(scenes.look_at((0.4, 3.0, 7.0), (0.0, 0.8, 0.0)), np.float32)
     proj = np.asarray(scenes.perspective(45.0, s.width / s.height), np.float32)

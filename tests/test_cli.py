@@ -36,7 +36,11 @@ def write_obj(path, meshes):
         "newmtl floor\nKd 0.7 0.7 0.6\nPm 0.5\nPr 0.6\nd 0.8\n")
 
 
-def test_cli_render_matches_c_abi(agb, oracle):
+@pytest.mark.parametrize("ground", [False, True])
+def test_cli_render_matches_c_abi(agb, oracle, ground):
+    """With `ground`, the floor quad gives way to the CLI's ground plane (--ground_shadow 1
+    --ground_reflection 1: Plasma's plane at the scene's lower bound, shadow opacity 1,
+    reflection opacity 0.5)."""
     from aurora_gb300 import _abi, api, build, scenes
     build.build()
     exe = build.CLI
@@ -46,14 +50,18 @@ def test_cli_render_matches_c_abi(agb, oracle):
     env = scenes.hdr_env(32, 16, 5, sigma=1.0, suns=1, sun_radiance=200.0, sun_radius=1.5)[..., :3]
     with tempfile.TemporaryDirectory() as tmp:
         obj = os.path.join(tmp, "scene.obj")
-        write_obj(obj, [("ball", "blue", sp, sn, st, si), ("ground", "floor", qp, qn, qt, qi)])
+        meshes = [("ball", "blue", sp, sn, st, si)]
+        if not ground:
+            meshes.append(("ground", "floor", qp, qn, qt, qi))
+        write_obj(obj, meshes)
         enc = np.array([[rgbe(px) for px in row] for row in env], np.uint8)
         hdr = os.path.join(tmp, "env.hdr")
         open(hdr, "wb").write(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y 16 +X 32\n" + enc.tobytes())
         out = os.path.join(tmp, "out.pfm")
         res = subprocess.run([exe, obj, "--output", out, "--dims", "64,48", "--output_spp", "8",
                               "--eye", "0.4,3,7", "--target", "0,0.8,0", "--fov", "45", "--env", hdr,
-                              "--lightDir", "0.3,-1,-0.2", "--lightIntensity", "2", "--trace-depth", "4"],
+                              "--lightDir", "0.3,-1,-0.2", "--lightIntensity", "2", "--trace-depth", "4"]
+                             + (["--ground_shadow", "1", "--ground_reflection", "1"] if ground else []),
                              capture_output=True, text=True)
         assert res.returncode == 0, res.stderr
         mats = {k: np.array(re.search(rf"agb_render: {k}(( \S+){{16}})", res.stderr).group(1).split(),
@@ -83,6 +91,9 @@ def test_cli_render_matches_c_abi(agb, oracle):
     frame = scenes.frame_data(mats["view"].astype(np.float64), mats["proj"].astype(np.float64), trace_depth=4,
                               lights=[(tuple(d), (1.0, 1.0, 1.0), 2.0, 0.1)], scene_bounds=s.bounds())
     s.frame = frame
+    if ground:
+        s.ground_plane = _abi.ground_plane(position=scene["bounds"][0], shadow_opacity=1.0,
+                                           reflection_opacity=0.5)
     with api.Renderer() as r:
         r.upload(s)
         r.render(0, 8, accumulation=_abi.ACCUM_RUNNING_MEAN)

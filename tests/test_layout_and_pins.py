@@ -58,6 +58,7 @@ def test_oracle_layouts_match_abi(oracle):
     assert L.orc_layout(5) == ctypes.sizeof(oracle.Image)
     assert L.orc_layout(6) == ctypes.sizeof(oracle.Scene)
     assert L.orc_layout(7) == ctypes.sizeof(oracle.Layer)
+    assert L.orc_layout(8) == _abi.GROUND_PLANE_DTYPE.itemsize
 
 
 def test_oracle_alias_table_matches_reference_fixtures(oracle):
