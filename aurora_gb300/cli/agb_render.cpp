@@ -1,16 +1,19 @@
 // agb_render: headless renderer over the Aurora-style C++ interface, after the Plasma
 // application's batch mode (Applications/Plasma/Plasma.cpp:421-465 options, :778-790 render once
-// and save): load a Wavefront OBJ scene, frame the camera (or take --eye / --target), add the
+// and save): load a Wavefront OBJ or glTF 2.0 (.gltf / .glb) scene, frame the camera (or take
+// --eye / --target, or --camera N for the file's N-th camera as Plasma's camera switch applies
+// it, Plasma.cpp:1902-1935: its view, its vertical field of view, aspect ratio and depth range;
+// orthographic cameras as glm::ortho(-xmag, xmag, -ymag, ymag, znear, zfar)), add the
 // distant light and an optional lat-long Radiance HDR environment, render --output_spp samples and
 // write the image (.png: the 8-bit post-processed buffer; .pfm: the float post-processed buffer).
 // --ground_shadow / --ground_reflection switch on Plasma's ground plane at the scene's lower bound
 // (Plasma.cpp:941-942, 989-996): matte shadow opacity 1, matte reflection opacity 0.5.
 //
-// usage: agb_render <scene.obj> --output <file.png|file.pfm> [--output_spp N] [--dims W,H]
+// usage: agb_render <scene.obj|.gltf|.glb> --output <file.png|file.pfm> [--output_spp N] [--dims W,H]
 //          [--eye x,y,z] [--target x,y,z] [--up x,y,z] [--fov degrees] [--env file.hdr]
 //          [--lightDir x,y,z] [--lightColor r,g,b] [--lightIntensity v] [--trace-depth N]
 //          [--russian_roulette 0|1] [--gamma_correction 0|1] [--ground_shadow 0|1]
-//          [--ground_reflection 0|1]
+//          [--ground_reflection 0|1] [--camera N]
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -114,11 +117,11 @@ int main(int argc, char** argv)
     if (scenePath.empty() || !a.count("output"))
     {
         std::fprintf(stderr,
-            "usage: agb_render <scene.obj> --output <file.png|file.pfm> [--output_spp N] [--dims W,H]\n"
+            "usage: agb_render <scene.obj|.gltf|.glb> --output <file.png|file.pfm> [--output_spp N] [--dims W,H]\n"
             "       [--eye x,y,z] [--target x,y,z] [--up x,y,z] [--fov degrees] [--env file.hdr]\n"
             "       [--lightDir x,y,z] [--lightColor r,g,b] [--lightIntensity v] [--trace-depth N]\n"
             "       [--russian_roulette 0|1] [--gamma_correction 0|1] [--ground_shadow 0|1]\n"
-            "       [--ground_reflection 0|1]\n");
+            "       [--ground_reflection 0|1] [--camera N]\n");
         return 2;
     }
     try
@@ -142,7 +145,8 @@ int main(int argc, char** argv)
             throw Error("no GB300 renderer available");
         IScenePtr scene = renderer->createScene();
         SceneContents contents;
-        if (!loadOBJFile(scene.get(), scenePath, contents))
+        const bool gltf = endsWith(scenePath, ".gltf") || endsWith(scenePath, ".glb");
+        if (!(gltf ? loadglTFFile(scene.get(), scenePath, contents) : loadOBJFile(scene.get(), scenePath, contents)))
             throw Error("cannot load " + scenePath + (contents.warnings.empty() ? "" : ": " + contents.warnings));
         if (!contents.warnings.empty())
             std::fprintf(stderr, "%s", contents.warnings.c_str());
@@ -211,7 +215,30 @@ int main(int argc, char** argv)
         IRenderBufferPtr target_ =
             renderer->createRenderBuffer(width, height, pfm ? ImageFormat::Float_RGBA : ImageFormat::Integer_RGBA);
         renderer->setTargets({ { AOV::Final, target_ } });
-        const mat4 view = lookAt(eye, target, up), proj = perspective(fovY, aspect, 0.1f, 1000.f);
+        mat4 view = lookAt(eye, target, up), proj = perspective(fovY, aspect, 0.1f, 1000.f);
+        if (a.count("camera"))
+        {
+            int k = std::atoi(a["camera"].c_str());
+            if (k < 1 || size_t(k) > contents.cameras.size())
+                throw Error("--camera " + a["camera"] + ": the scene has " + std::to_string(contents.cameras.size()) +
+                    " camera(s)");
+            const SceneCamera& c = contents.cameras[size_t(k - 1)];
+            view                 = c.viewMatrix;
+            float zn = c.znear > 0.f ? c.znear : 0.1f, zf = c.zfar > zn ? c.zfar : 1000.f;
+            if (c.type == SceneCamera::Perspective)
+                proj = perspective(c.yfov > 0.f ? c.yfov : fovY, c.aspectRatio > 0.f ? c.aspectRatio : aspect, zn, zf);
+            else
+            {
+                if (!(c.xmag > 0.f && c.ymag > 0.f))
+                    throw Error("--camera " + a["camera"] + ": orthographic camera without a magnification");
+                proj     = mat4{};
+                proj[0]  = 1.f / c.xmag;
+                proj[5]  = 1.f / c.ymag;
+                proj[10] = -2.f / (zf - zn);
+                proj[14] = -(zf + zn) / (zf - zn);
+                proj[15] = 1.f;
+            }
+        }
         renderer->setCamera(view, proj);
         renderer->render(0, uint32_t(spp));
         renderer->waitForTask();

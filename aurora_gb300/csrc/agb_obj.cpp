@@ -478,8 +478,14 @@ bool loadOBJFile(IScene* scene, const std::string& filePath, SceneContents& cont
     }
     if (!translateOBJ(obj, filePath, contents))
         return false;
+    addContentsToScene(scene, contents);
+    return true;
+}
+
+void addContentsToScene(IScene* scene, SceneContents& contents)
+{
     if (!scene)
-        return true;
+        return;
     for (const SceneMaterialData& m : contents.materials)
     {
         scene->setMaterialType(m.path);
@@ -504,14 +510,12 @@ bool loadOBJFile(IScene* scene, const std::string& filePath, SceneContents& cont
             return true;
         };
         scene->setGeometryDescriptor(inst.geometry, d);
-        Properties props = { { Names::InstanceProperties::kTransform,
-            mat4{ 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1 } } };
+        Properties props = { { Names::InstanceProperties::kTransform, inst.transform } };
         if (!inst.material.empty())
             props[Names::InstanceProperties::kMaterial] = inst.material;
         scene->addInstance(inst.instance, inst.geometry, props);
     }
     scene->setBounds(contents.boundsMin, contents.boundsMax);
-    return true;
 }
 
 bool loadHDRFile(const std::string& path, std::vector<float>& rgb, int& width, int& height, std::string& error)

@@ -62,15 +62,32 @@ struct SceneGeometryData
 struct SceneInstanceData
 {
     Path instance, geometry, material; // material empty: the renderer's default material
+    mat4 transform = { 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1 }; // column-major
 };
 struct SceneMaterialData
 {
     Path path;
     Properties properties;
 };
+// A camera of a glTF file (Plasma's SceneCamera, SceneContents.h:27-61).
+struct SceneCamera
+{
+    enum Type
+    {
+        Perspective,
+        Orthographic
+    };
+    Type type = Perspective;
+    std::string name;
+    mat4 viewMatrix = { 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1 }; // column-major
+    float yfov = 0.f, aspectRatio = 0.f; // perspective
+    float xmag = 0.f, ymag = 0.f;        // orthographic
+    float znear = 0.f, zfar = 0.f;
+};
 struct SceneContents
 {
     std::map<Path, SceneGeometryData> geometry;
+    std::vector<SceneCamera> cameras;
     std::vector<SceneInstanceData> instances;
     std::vector<SceneMaterialData> materials;
     vec3 boundsMin = { 0.f, 0.f, 0.f }, boundsMax = { 0.f, 0.f, 0.f };
@@ -86,6 +103,26 @@ struct SceneContents
 AGB_CPP_API bool translateOBJ(const ObjData& obj, const std::string& filePath, SceneContents& contents);
 // loadOBJFile (OBJLoader.cpp:73-473): parse + translate + hand everything to the scene.
 AGB_CPP_API bool loadOBJFile(IScene* scene, const std::string& filePath, SceneContents& contents);
+
+// Hands loaded contents to a scene: materials, geometry descriptors that pull from `contents`
+// (which must outlive the scene's use of them), instances with their transforms, bounds.
+AGB_CPP_API void addContentsToScene(IScene* scene, SceneContents& contents);
+
+// glTF 2.0 (.gltf with embedded or external buffers, .glb) after the reference's loader
+// (Applications/Plasma/glTFLoader.cpp:26-436; the file parse restates what it takes from
+// tinygltf): every scene's nodes, recursively, with matrix or TRS transforms accumulated from
+// the parents; each TRIANGLES primitive with FLOAT positions becomes one geometry
+// (`<file>:gltfGeom:<n>`) and one instance (`<file>:gltfInst:<n>`) with the node's world
+// transform; NORMAL and TEXCOORD_0 when present (FLOAT), normals generated otherwise, unsigned
+// 8/16/32-bit indices or a sequential list; one material per glTF material
+// (`<file>:gltfMat:<i>`) with base_color, metalness and specular_roughness from
+// pbrMetallicRoughness (glTF defaults 1, 1, 1); camera nodes collected with the inverse of the
+// node's own transform as the view.  The AURORA_materials_materialX node extension is not
+// supported: such nodes take their glTF material, with a warning.  With a null scene the contents
+// are filled and no scene is touched.
+AGB_CPP_API bool loadglTFFile(IScene* scene, const std::string& filePath, SceneContents& contents);
+// Writes the contents' cameras as a glTF file of camera nodes (glTFLoader.cpp:438-492).
+AGB_CPP_API bool saveglTFFile(const std::string& filePath, const SceneContents& contents);
 
 // Angle-weighted smooth vertex normals (Foundation/Source/Geometry.cpp:29-99).
 AGB_CPP_API void calculateNormals(size_t vertexCount, const float* positions, size_t triangleCount,

@@ -1,5 +1,7 @@
 // Test driver for include/aurora_gb300_loaders.hpp (no GPU needed): prints JSON.
 //   loader_tool obj <file.obj>                      parse + translate, no scene
+//   loader_tool gltf <file.gltf|file.glb>           parse + translate, no scene
+//   loader_tool gltfsave <out.gltf> <in.gltf>       the input's cameras written as a glTF file
 //   loader_tool hdr <file.hdr>                      width, height, RGB floats
 //   loader_tool png <out.png> <w> <h>               writes a pattern image
 //   loader_tool pfm <out.pfm> <w> <h>               writes a pattern image
@@ -63,10 +65,18 @@ int main(int argc, char** argv)
     if (argc < 3)
         return 2;
     std::string mode = argv[1];
-    if (mode == "obj")
+    if (mode == "gltfsave" && argc == 4)
+    {
+        // Loads the cameras of argv[3] and writes them to argv[2].
+        SceneContents c;
+        if (!loadglTFFile(nullptr, argv[3], c))
+            return 1;
+        return saveglTFFile(argv[2], c) ? 0 : 1;
+    }
+    if (mode == "obj" || mode == "gltf")
     {
         SceneContents c;
-        bool ok = loadOBJFile(nullptr, argv[2], c);
+        bool ok = mode == "obj" ? loadOBJFile(nullptr, argv[2], c) : loadglTFFile(nullptr, argv[2], c);
         std::printf("{\"ok\":%s,\"warnings\":", ok ? "true" : "false");
         printString(c.warnings);
         std::printf(",\"bounds\":[");
@@ -98,6 +108,10 @@ int main(int argc, char** argv)
             printString(c.instances[i].instance);
             std::printf(",\"material\":");
             printString(c.instances[i].material);
+            std::printf(",\"geometry\":");
+            printString(c.instances[i].geometry);
+            std::printf(",\"transform\":");
+            printFloats(c.instances[i].transform.data(), 16);
             std::printf(",\"positions\":");
             printFloats(g.positions.data(), g.positions.size());
             std::printf(",\"normals\":");
@@ -108,6 +122,19 @@ int main(int argc, char** argv)
             for (size_t k = 0; k < g.indices.size(); k++)
                 std::printf("%s%u", k ? "," : "", g.indices[k]);
             std::printf("]}");
+        }
+        std::printf("],\"cameras\":[");
+        for (size_t i = 0; i < c.cameras.size(); i++)
+        {
+            const SceneCamera& k = c.cameras[i];
+            std::printf("%s{\"name\":", i ? "," : "");
+            printString(k.name);
+            std::printf(",\"type\":\"%s\",\"view\":", k.type == SceneCamera::Perspective ? "perspective" : "orthographic");
+            printFloats(k.viewMatrix.data(), 16);
+            float v[6] = { k.yfov, k.aspectRatio, k.xmag, k.ymag, k.znear, k.zfar };
+            std::printf(",\"values\":");
+            printFloats(v, 6);
+            std::printf("}");
         }
         std::printf("],\"vertices\":%u,\"triangles\":%u}\n", c.vertexCount, c.triangleCount);
         return 0;

@@ -102,3 +102,94 @@ def test_cli_render_matches_c_abi(agb, oracle, ground):
     print(f"CLI vs C ABI: relMSE {err:.3g}, identical pixels {np.mean(np.all(img == ref[..., :3], axis=2)):.4f}")
     assert err < 1e-6
     assert img.max() > 0
+
+
+def test_cli_gltf_camera_render_matches_c_abi(agb, oracle):
+    """A .glb scene (a TRS-transformed sphere over a matrix-transformed floor, two
+    pbrMetallicRoughness materials, a perspective camera node) rendered by the CLI from the file's
+    camera (--camera 1) must match the loader's contents rendered through the C ABI."""
+    from aurora_gb300 import _abi, api, build, scenes
+    from test_gltf import Builder, sphere, write
+    build.build()
+    exe = build.CLI
+    b = Builder()
+    sp, sn, st, si = sphere(24, 12)
+    qp, qn, qt, qi = [np.asarray(a) for a in scenes.quad(4.0)]
+    prims = [
+        {"attributes": {"POSITION": b.accessor(sp, "VEC3"), "NORMAL": b.accessor(sn, "VEC3"),
+                        "TEXCOORD_0": b.accessor(st, "VEC2")},
+         "indices": b.accessor(si.astype(np.uint32), "SCALAR", ctype=5125), "material": 0},
+        {"attributes": {"POSITION": b.accessor(np.float32(qp), "VEC3"),
+                        "NORMAL": b.accessor(np.float32(qn), "VEC3")},
+         "indices": b.accessor(np.asarray(qi, np.uint16), "SCALAR", ctype=5123), "material": 1},
+    ]
+    doc = {
+        "asset": {"version": "2.0"}, "scenes": [{"nodes": [0, 1, 2]}],
+        "nodes": [
+            {"mesh": 0, "translation": [0.2, 1.0, 0.1], "rotation": [0, 0.2588190, 0, 0.9659258],
+             "scale": [1.0, 0.8, 1.0]},
+            {"mesh": 1, "matrix": [1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, -0.05, 0, 1]},
+            {"name": "view", "camera": 0, "translation": [0.5, 2.5, 6.5],
+             "rotation": [-0.1736482, 0, 0, 0.9848078]},
+        ],
+        "meshes": [{"primitives": [prims[0]]}, {"primitives": [prims[1]]}],
+        "materials": [
+            {"pbrMetallicRoughness": {"baseColorFactor": [0.9, 0.3, 0.2, 1], "metallicFactor": 0.0,
+                                      "roughnessFactor": 0.35}},
+            {"pbrMetallicRoughness": {"baseColorFactor": [0.6, 0.6, 0.5, 1], "metallicFactor": 0.5,
+                                      "roughnessFactor": 0.7}},
+        ],
+        "cameras": [{"type": "perspective",
+                     "perspective": {"yfov": 0.8, "aspectRatio": 64 / 48, "znear": 0.1, "zfar": 200}}],
+        "bufferViews": b.views, "accessors": b.accessors, "buffers": [{"byteLength": len(b.blob)}],
+    }
+    env = scenes.hdr_env(32, 16, 5, sigma=1.0, suns=1, sun_radiance=200.0, sun_radius=1.5)[..., :3]
+    with tempfile.TemporaryDirectory() as tmp:
+        glb = write(tmp, "glb", doc, bytes(b.blob))
+        enc = np.array([[rgbe(px) for px in row] for row in env], np.uint8)
+        hdr = os.path.join(tmp, "env.hdr")
+        open(hdr, "wb").write(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y 16 +X 32\n" + enc.tobytes())
+        out = os.path.join(tmp, "out.pfm")
+        res = subprocess.run([exe, glb, "--output", out, "--dims", "64,48", "--output_spp", "8",
+                              "--camera", "1", "--env", hdr, "--lightDir", "0.3,-1,-0.2",
+                              "--lightIntensity", "2", "--trace-depth", "4"], capture_output=True, text=True)
+        assert res.returncode == 0, res.stderr
+        mats = {k: np.array(re.search(rf"agb_render: {k}(( \S+){{16}})", res.stderr).group(1).split(),
+                            np.float32).reshape(4, 4).T for k in ("view", "proj")}
+        data = open(out, "rb").read()
+        head = b"PF\n64 48\n-1.0\n"
+        img = np.frombuffer(data[len(head):], "<f4").reshape(48, 64, 3)[::-1]
+        scene = loader("gltf", glb)
+        env_f = np.reshape(loader("hdr", hdr)["rgb"], (16, 32, 3)).astype(np.float32)
+    cam = np.float32(scene["cameras"][0]["view"]).reshape(4, 4).T
+    np.testing.assert_array_equal(mats["view"], cam)
+    s = scenes.SceneDesc("cli-gltf")
+    names = {m["path"]: k for k, m in enumerate(scene["materials"])}
+    s.materials = scenes.materials(len(names))
+    for m in scene["materials"]:
+        for key, v in m["properties"].items():
+            s.materials[key][names[m["path"]]] = v
+    for inst in scene["instances"]:
+        tc = inst["texcoords"]
+        mesh = s.add_mesh(np.reshape(inst["positions"], (-1, 3)), np.reshape(inst["normals"], (-1, 3)),
+                          np.reshape(tc, (-1, 2)) if tc else None, np.array(inst["indices"], np.uint32))
+        xf = np.float32(inst["transform"]).reshape(4, 4).T[:3].reshape(-1)
+        s.instances.append(dict(mesh=mesh, material=names[inst["material"]], xform=xf, layers=[]))
+    img_id = s.add_image(env_f, _abi.FORMAT_RGB32F)
+    s.env_light = img_id
+    s.env_background = img_id
+    s.width, s.height, s.spp = 64, 48, 8
+    d = np.float32([0.3, -1, -0.2])
+    d = d / np.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])
+    s.frame = scenes.frame_data(mats["view"].astype(np.float64), mats["proj"].astype(np.float64),
+                                trace_depth=4, lights=[(tuple(d), (1.0, 1.0, 1.0), 2.0, 0.1)],
+                                scene_bounds=s.bounds())
+    with api.Renderer() as r:
+        r.upload(s)
+        r.render(0, 8, accumulation=_abi.ACCUM_RUNNING_MEAN)
+        ref, _ = r.post_process(mode=_abi.ACCUM_RUNNING_MEAN)
+    err = oracle.rel_mse(img, ref[..., :3])
+    print(f"CLI (glTF, file camera) vs C ABI: relMSE {err:.3g}, "
+          f"identical pixels {np.mean(np.all(img == ref[..., :3], axis=2)):.4f}")
+    assert err < 1e-6
+    assert img.max() > 0
