@@ -14,6 +14,7 @@
 
 #include "agb.h"
 #include "aurora_gb300.hpp"
+#include "aurora_gb300_loaders.hpp"
 
 namespace agb_aurora
 {
@@ -326,12 +327,27 @@ public:
         images[p] = Image{ d, -1 };
         dirty     = true;
     }
-    void setMaterialType(const Path& p, const std::string& type, const std::string&) override
+    void setMaterialType(const Path& p, const std::string& type, const std::string& document) override
     {
-        if (type != Names::MaterialTypes::kBuiltIn)
-            logError("setMaterialType: only the built-in Standard Surface material is supported; " + p +
-                " uses it");
-        materials[p];
+        Properties& m = materials[p];
+        if (type == Names::MaterialTypes::kMaterialX || type == Names::MaterialTypes::kMaterialXPath)
+        {
+            // The document's standard_surface constants become the material's values; properties
+            // set afterwards override them.
+            Properties fromDoc;
+            std::string warnings;
+            bool ok = type == Names::MaterialTypes::kMaterialX
+                ? materialXToProperties(document, fromDoc, warnings)
+                : materialXFileToProperties(document, fromDoc, warnings);
+            if (!warnings.empty())
+                logError("setMaterialType " + p + ": " + warnings);
+            if (ok)
+                for (auto& kv : fromDoc)
+                    m[kv.first] = kv.second;
+        }
+        else if (type != Names::MaterialTypes::kBuiltIn)
+            logError("setMaterialType: unknown material type " + type + "; " + p +
+                " uses the built-in Standard Surface material");
         dirty = true;
     }
     void setMaterialProperties(const Path& p, const Properties& props) override

@@ -860,12 +860,33 @@ void loadNode(Model& m, int nodeIdx, const mat4& parent, SceneContents& contents
             inst.instance  = instPath;
             inst.geometry  = geomPath;
             inst.transform = local;
+            // Priority 1: the node's AURORA_materials_materialX extension; 2: the glTF material.
             const Json* ext = node.get("extensions");
-            if (ext && ext->get("AURORA_materials_materialX"))
-                m.warnings += "node " + std::to_string(nodeIdx) +
-                    ": MaterialX materials are not supported; using the glTF material\n";
+            const Json* mx  = ext ? ext->get("AURORA_materials_materialX") : nullptr;
+            if (mx && mx->kind == Json::Object && !mx->str("materialXFile").empty())
+            {
+                const std::string file = dirOf(m.filePath) + mx->str("materialXFile");
+                const Path path        = "AURORA_mtlx:" + file;
+                bool known             = false;
+                for (const SceneMaterialData& md : contents.materials)
+                    known = known || md.path == path;
+                if (known)
+                    inst.material = path;
+                else
+                {
+                    SceneMaterialData md;
+                    md.path = path;
+                    if (materialXFileToProperties(file, md.properties, m.warnings))
+                    {
+                        contents.materials.push_back(md);
+                        inst.material = path;
+                    }
+                    else
+                        m.warnings += "node " + std::to_string(nodeIdx) + ": using the glTF material\n";
+                }
+            }
             int mi = prim.integer("material", -1);
-            if (mi >= 0 && size_t(mi) < materialPaths.size())
+            if (inst.material.empty() && mi >= 0 && size_t(mi) < materialPaths.size())
                 inst.material = materialPaths[size_t(mi)];
             contents.instances.push_back(inst);
             contents.vertexCount += vertexCount;

@@ -94,6 +94,10 @@ inline const std::string kColor("color");
 namespace MaterialTypes
 {
 inline const std::string kBuiltIn("BuiltIn");
+// A MaterialX document (the string) or the path of a .mtlx file (AuroraNames.cpp:48-50): a
+// standard_surface with constant inputs, read into the built-in material's properties.
+inline const std::string kMaterialX("MaterialX");
+inline const std::string kMaterialXPath("MaterialXPath");
 } // namespace MaterialTypes
 } // namespace Names
 

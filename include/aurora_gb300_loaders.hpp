@@ -117,12 +117,23 @@ AGB_CPP_API void addContentsToScene(IScene* scene, SceneContents& contents);
 // 8/16/32-bit indices or a sequential list; one material per glTF material
 // (`<file>:gltfMat:<i>`) with base_color, metalness and specular_roughness from
 // pbrMetallicRoughness (glTF defaults 1, 1, 1); camera nodes collected with the inverse of the
-// node's own transform as the view.  The AURORA_materials_materialX node extension is not
-// supported: such nodes take their glTF material, with a warning.  With a null scene the contents
-// are filled and no scene is touched.
+// node's own transform as the view.  A node's AURORA_materials_materialX extension names a .mtlx
+// file beside the glTF file that gives the node's material (`AURORA_mtlx:<file>`, read with
+// materialXFileToProperties); when it cannot be read the glTF material is used, with a warning.
+// With a null scene the contents are filled and no scene is touched.
 AGB_CPP_API bool loadglTFFile(IScene* scene, const std::string& filePath, SceneContents& contents);
 // Writes the contents' cameras as a glTF file of camera nodes (glTFLoader.cpp:438-492).
 AGB_CPP_API bool saveglTFFile(const std::string& filePath, const SceneContents& contents);
+
+// MaterialX (the reference generates shader code from the document, Source/MaterialX/
+// MaterialGenerator.cpp:30-120 mapping standard_surface inputs to its material fields): here a
+// document whose surface shader -- the surfaceshader input of its first surfacematerial, else its
+// first standard_surface node -- is a standard_surface becomes the built-in material's
+// properties, one per constant input (float, integer, boolean, color3 / vector3, the rgb of
+// color4) under the input's name.  Inputs connected to node graphs keep their defaults and other
+// surface shaders are refused, each with a warning.
+AGB_CPP_API bool materialXToProperties(const std::string& document, Properties& properties, std::string& warnings);
+AGB_CPP_API bool materialXFileToProperties(const std::string& path, Properties& properties, std::string& warnings);
 
 // Angle-weighted smooth vertex normals (Foundation/Source/Geometry.cpp:29-99).
 AGB_CPP_API void calculateNormals(size_t vertexCount, const float* positions, size_t triangleCount,

@@ -9,7 +9,7 @@
 //   u32 meshes; per mesh: u32 vertices, indices, f32 positions[3v], u8 has normals + f32[3v],
 //     u8 has uvs + f32[2v], u32 indices[i]
 //   u32 materials; per material: u32 properties; per property: u8 name length, name, u8 kind
-//     (1 float, 3 float3, 2 bool), values
+//     (1 float, 3 float3, 2 bool), values; or u32 0xFFFFFFFF, u32 length, a MaterialX document
 //   u32 instances; per instance: u32 mesh, u32 material, f32 transform[16] (column-major)
 //   u32 lights; per light: f32 direction[3], color[3], intensity, angular diameter
 //   f32 light top[3], light bottom[3], background top[3], background bottom[3]
@@ -138,6 +138,14 @@ int main(int argc, char** argv)
         {
             Properties props;
             uint32_t np = r.get<uint32_t>();
+            if (np == 0xFFFFFFFFu)
+            {
+                // A MaterialX document instead of a property list.
+                auto doc = r.array<char>(r.get<uint32_t>());
+                Path path = "/material/" + std::to_string(m);
+                scene->setMaterialType(path, Names::MaterialTypes::kMaterialX, std::string(doc.begin(), doc.end()));
+                continue;
+            }
             for (uint32_t k = 0; k < np; k++)
             {
                 auto nameChars = r.array<char>(r.get<uint8_t>());

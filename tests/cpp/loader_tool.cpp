@@ -2,6 +2,7 @@
 //   loader_tool obj <file.obj>                      parse + translate, no scene
 //   loader_tool gltf <file.gltf|file.glb>           parse + translate, no scene
 //   loader_tool gltfsave <out.gltf> <in.gltf>       the input's cameras written as a glTF file
+//   loader_tool mtlx <file.mtlx>                    standard_surface constants as properties
 //   loader_tool hdr <file.hdr>                      width, height, RGB floats
 //   loader_tool png <out.png> <w> <h>               writes a pattern image
 //   loader_tool pfm <out.pfm> <w> <h>               writes a pattern image
@@ -65,6 +66,26 @@ int main(int argc, char** argv)
     if (argc < 3)
         return 2;
     std::string mode = argv[1];
+    if (mode == "mtlx")
+    {
+        Properties props;
+        std::string warnings;
+        bool ok = materialXFileToProperties(argv[2], props, warnings);
+        std::printf("{\"ok\":%s,\"warnings\":", ok ? "true" : "false");
+        printString(warnings);
+        std::printf(",\"properties\":{");
+        bool first = true;
+        for (auto& kv : props)
+        {
+            std::printf("%s", first ? "" : ",");
+            first = false;
+            printString(kv.first);
+            std::printf(":");
+            printValue(kv.second);
+        }
+        std::printf("}}\n");
+        return 0;
+    }
     if (mode == "gltfsave" && argc == 4)
     {
         // Loads the cameras of argv[3] and writes them to argv[2].

@@ -37,7 +37,29 @@ def test_cpp_client_builds_and_links():
     assert os.access(build_client(), os.X_OK)
 
 
-def write_scene(path, s, view, proj, lights, depth):
+def materialx_document(mat, keys, name):
+    """The material as a MaterialX standard_surface with one constant input per property (values
+    printed with 9 significant digits, so each float reads back exactly)."""
+    lines = ['<?xml version="1.0"?>', '<materialx version="1.38" colorspace="lin_rec709">',
+             f'  <!-- {name}: constants only -->',
+             f'  <standard_surface name="SR_{name}" type="surfaceshader">']
+    for k in keys:
+        v = mat[k]
+        if k == "thin_walled":
+            lines.append(f'    <input name="{k}" type="boolean" value="{"true" if int(v) else "false"}" />')
+        elif np.ndim(v):
+            lines.append(f'    <input name="{k}" type="color3" value="' +
+                         ", ".join("%.9g" % np.float32(x) for x in v) + '" />')
+        else:
+            lines.append(f'    <input name="{k}" type="float" value="{"%.9g" % np.float32(v)}" />')
+    lines += ['  </standard_surface>',
+              f'  <surfacematerial name="M_{name}" type="material">',
+              f'    <input name="surfaceshader" type="surfaceshader" nodename="SR_{name}" />',
+              '  </surfacematerial>', '</materialx>']
+    return "\n".join(lines)
+
+
+def write_scene(path, s, view, proj, lights, depth, mtlx=False):
     from aurora_gb300 import _abi, scenes
     b = bytearray(b"AGBS")
     b += struct.pack("<5I", 1, s.width, s.height, s.spp, depth)
@@ -53,8 +75,12 @@ def write_scene(path, s, view, proj, lights, depth):
                 b += np.asarray(m[key], np.float32).tobytes()
         b += np.asarray(m["indices"], np.uint32).tobytes()
     b += struct.pack("<I", len(s.materials))
-    for mat in s.materials:
+    for mi, mat in enumerate(s.materials):
         props = list(scenes._DEFAULTS.keys())
+        if mtlx:
+            doc = materialx_document(mat, props, f"m{mi}").encode()
+            b += struct.pack("<II", 0xFFFFFFFF, len(doc)) + doc
+            continue
         b += struct.pack("<I", len(props))
         for k in props:
             b += struct.pack("<B", len(k)) + k.encode()
@@ -89,11 +115,12 @@ def write_scene(path, s, view, proj, lights, depth):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("ground", [False, True])
-def test_cpp_interface_render_matches_c_abi(agb, oracle, ground):
+@pytest.mark.parametrize("ground,mtlx", [(False, False), (True, False), (False, True)])
+def test_cpp_interface_render_matches_c_abi(agb, oracle, ground, mtlx):
     """The same frame through the C++ interface and through the C ABI; with `ground`, the floor
     quad is replaced by a ground plane (IRenderer::createGroundPlanePointer,
-    IScene::setGroundPlanePointer) with non-default values."""
+    IScene::setGroundPlanePointer) with non-default values; with `mtlx`, every material reaches the
+    interface as a MaterialX standard_surface document (setMaterialType(path, "MaterialX", doc))."""
     from aurora_gb300 import _abi, api, scenes
     exe = build_client()
     s = scenes.config_tiny(width=48, height=32, spp=8, lights=False)
@@ -111,7 +138,7 @@ def test_cpp_interface_render_matches_c_abi(agb, oracle, ground):
     depth = 4
     with tempfile.TemporaryDirectory() as tmp:
         scene_file, out_file = os.path.join(tmp, "scene.bin"), os.path.join(tmp, "out.bin")
-        write_scene(scene_file, s, view, proj, lights, depth)
+        write_scene(scene_file, s, view, proj, lights, depth, mtlx=mtlx)
         subprocess.check_call([exe, scene_file, out_file])
         raw = open(out_file, "rb").read()
     w, h = struct.unpack("<2I", raw[:8])

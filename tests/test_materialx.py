@@ -1,0 +1,100 @@
+"""MaterialX documents with a standard_surface of constant inputs (include/aurora_gb300_loaders.hpp,
+materialXToProperties) on the CPU: the properties they give, what is refused with a warning, and
+the glTF AURORA_materials_materialX node extension that names such a file."""
+import json
+import os
+import tempfile
+
+import numpy as np
+
+from test_loaders import run
+
+GOLD = """<?xml version="1.0"?>
+<materialx version="1.38" colorspace="lin_rec709">
+  <!-- a standard_surface reached through its surfacematerial -->
+  <standard_surface name="SR_gold" type="surfaceshader">
+    <input name="base" type="float" value="1" />
+    <input name="base_color" type="color3" value="0.944, 0.776, 0.373" />
+    <input name="metalness" type="float" value="1" />
+    <input name="specular_roughness" type="float" value="0.25"/>
+    <input name="thin_walled" type="boolean" value="true" />
+    <input name="coat_color" type="color4" value="0.5,0.25,0.125,1" />
+    <input name="specular_IOR" type="float" />
+  </standard_surface>
+  <standard_surface name="SR_unused" type="surfaceshader">
+    <input name="base" type="float" value="0.1" />
+  </standard_surface>
+  <surfacematerial name="Gold" type="material">
+    <input name="surfaceshader" type="surfaceshader" nodename="SR_gold" />
+  </surfacematerial>
+</materialx>
+"""
+
+
+def props(text, name="m.mtlx"):
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, name)
+        open(path, "w").write(text)
+        return run("mtlx", path)
+
+
+def test_standard_surface_constants_become_properties():
+    out = props(GOLD)
+    assert out["ok"], out["warnings"]
+    p = out["properties"]
+    assert set(p) == {"base", "base_color", "metalness", "specular_roughness", "thin_walled", "coat_color"}
+    assert p["base"] == 1.0 and p["metalness"] == 1.0 and p["thin_walled"] is True
+    np.testing.assert_array_equal(np.float32(p["base_color"]), np.float32([0.944, 0.776, 0.373]))
+    assert np.float32(p["specular_roughness"]) == np.float32(0.25)
+    np.testing.assert_array_equal(np.float32(p["coat_color"]), np.float32([0.5, 0.25, 0.125]))
+
+
+def test_bare_standard_surface_entities_and_single_quotes():
+    doc = ("<materialx version='1.38'><standard_surface name='a&amp;b' type='surfaceshader'>"
+           "<input name='emission' type='float' value='2.5'/>"
+           "<input name='emission_color' type='vector3' value='1 0.5 0.25'/>"
+           "</standard_surface></materialx>")
+    out = props(doc)
+    assert out["ok"], out["warnings"]
+    assert out["properties"]["emission"] == 2.5
+    assert out["properties"]["emission_color"] == [1.0, 0.5, 0.25]
+
+
+def test_refusals_and_warnings():
+    graph = GOLD.replace('<input name="metalness" type="float" value="1" />',
+                         '<input name="metalness" type="float" nodename="noise1" />')
+    out = props(graph)
+    assert out["ok"] and "metalness" not in out["properties"]
+    assert "node graph" in out["warnings"]
+    other = ('<materialx version="1.38"><open_pbr_surface name="S" type="surfaceshader"/>'
+             '<surfacematerial name="M" type="material"><input name="surfaceshader" '
+             'type="surfaceshader" nodename="S"/></surfacematerial></materialx>')
+    out = props(other)
+    assert not out["ok"] and "open_pbr_surface" in out["warnings"]
+    for bad, why in (("<materialx><standard_surface name='x'></materialx>", "mismatched end tag"),
+                     ("<mtlx/>", "not <materialx>"),
+                     ("<materialx/>", "no surface shader")):
+        out = props(bad)
+        assert not out["ok"] and why in out["warnings"], (bad, out["warnings"])
+    out = props(GOLD.replace('type="color3" value="0.944, 0.776, 0.373"',
+                             'type="color3" value="0.944, 0.776, 0.373" colorspace="srgb_texture"'))
+    assert out["ok"] and "colour space srgb_texture" in out["warnings"]
+
+
+def test_gltf_materialx_extension():
+    from test_gltf import make_doc, write
+    doc, blob, _ = make_doc()
+    with tempfile.TemporaryDirectory() as tmp:
+        open(os.path.join(tmp, "x.mtlx"), "w").write(GOLD)
+        path = write(tmp, "glb", doc, blob)
+        out = run("gltf", path)
+        mtlx = os.path.join(tmp, "x.mtlx")
+        assert out["ok"] and "MaterialX" not in out["warnings"]
+        assert out["instances"][0]["material"] == "AURORA_mtlx:" + mtlx
+        m = {x["path"]: x["properties"] for x in out["materials"]}["AURORA_mtlx:" + mtlx]
+        assert m["metalness"] == 1.0 and m["thin_walled"] is True
+        # without the file the node falls back to its glTF material, with a warning
+        os.remove(mtlx)
+        out = run("gltf", path)
+        assert out["ok"] and "cannot read MaterialX file" in out["warnings"]
+        assert out["instances"][0]["material"].endswith(":gltfMat:1")
