@@ -36,7 +36,7 @@ def nvcc():
 
 def _headers():
     out = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
-    out.append(os.path.join(INCLUDE, "agb.h"))
+    out += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith((".h", ".hpp"))]
     return out
 
 

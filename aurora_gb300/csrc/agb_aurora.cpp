@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <list>
 #include <mutex>
 
 #include "agb.h"
@@ -245,7 +246,33 @@ const MatField kMatFields[] = {
     AGB_MF(coat_rotation, 1, false), AGB_MF(coat_IOR, 1, false), AGB_MF(coat_affect_color, 1, false),
     AGB_MF(coat_affect_roughness, 1, false), AGB_MF(emission, 1, false), AGB_MF(emission_color, 3, false),
     AGB_MF(opacity, 3, false), AGB_MF(thin_walled, 1, true),
+    // Texture transforms (MaterialBase.cpp:61-86).
+    AGB_MF(base_color_image_offset, 2, false), AGB_MF(base_color_image_scale, 2, false),
+    AGB_MF(base_color_image_pivot, 2, false), AGB_MF(base_color_image_rotation, 1, false),
+    AGB_MF(specular_roughness_image_offset, 2, false), AGB_MF(specular_roughness_image_scale, 2, false),
+    AGB_MF(specular_roughness_image_pivot, 2, false), AGB_MF(specular_roughness_image_rotation, 1, false),
+    AGB_MF(emission_color_image_offset, 2, false), AGB_MF(emission_color_image_scale, 2, false),
+    AGB_MF(emission_color_image_pivot, 2, false), AGB_MF(emission_color_image_rotation, 1, false),
+    AGB_MF(opacity_image_offset, 2, false), AGB_MF(opacity_image_scale, 2, false),
+    AGB_MF(opacity_image_pivot, 2, false), AGB_MF(opacity_image_rotation, 1, false),
+    AGB_MF(normal_image_offset, 2, false), AGB_MF(normal_image_scale, 2, false),
+    AGB_MF(normal_image_pivot, 2, false), AGB_MF(normal_image_rotation, 1, false),
 };
+// Texture properties (MaterialBase.cpp:91-95, 199-213): the image path, its texture slot and the
+// material block's has_<name> flag, set when the texture is present.
+struct TexField
+{
+    const char* name;
+    int slot;
+    size_t hasOffset;
+};
+#define AGB_TF(field, slot) { #field, slot, offsetof(agb_material, has_##field) }
+const TexField kTexFields[] = {
+    AGB_TF(base_color_image, AGB_TEX_BASE_COLOR), AGB_TF(specular_roughness_image, AGB_TEX_SPECULAR_ROUGHNESS),
+    AGB_TF(opacity_image, AGB_TEX_OPACITY), AGB_TF(normal_image, AGB_TEX_NORMAL),
+    AGB_TF(emission_color_image, AGB_TEX_EMISSION),
+};
+#undef AGB_TF
 #undef AGB_MF
 
 // Built-in Standard Surface defaults (MaterialBase.cpp:109-167).
@@ -289,7 +316,8 @@ public:
     struct Image
     {
         ImageDescriptor desc;
-        int32_t handle = -1;
+        int32_t handle    = -1; // environment use: nearest filtering
+        int32_t texHandle = -1; // material textures: the default sampler's bilinear filtering
     };
     struct Instance
     {
@@ -301,6 +329,7 @@ public:
     std::map<Path, Image> images;
     std::map<Path, Properties> materials;
     std::map<Path, Properties> environments;
+    std::map<Path, Properties> samplers;
     std::vector<std::pair<Path, Instance>> instances; // insertion order
     std::vector<std::shared_ptr<Light>> lights;
     std::shared_ptr<GroundPlane> groundPlane; // null: the default, disabled plane
@@ -348,6 +377,13 @@ public:
         else if (type != Names::MaterialTypes::kBuiltIn)
             logError("setMaterialType: unknown material type " + type + "; " + p +
                 " uses the built-in Standard Surface material");
+        dirty = true;
+    }
+    void setSamplerProperties(const Path& p, const Properties& props) override
+    {
+        Properties& m = samplers[p];
+        for (auto& kv : props)
+            m[kv.first] = kv.second;
         dirty = true;
     }
     void setMaterialProperties(const Path& p, const Properties& props) override
@@ -443,7 +479,7 @@ public:
             for (auto& g : geometries)
                 g.second.handle = -1;
             for (auto& i : images)
-                i.second.handle = -1;
+                i.second.handle = i.second.texHandle = -1;
             ctx   = c;
             dirty = true;
         }
@@ -459,16 +495,31 @@ public:
                 pullGeometry(it->first, it->second);
         }
         std::vector<agb_material> mats(1, defaultMaterial());
+        std::vector<agb_material_textures> texs(1);
         std::map<Path, int32_t> matIndex;
+        bool anyTexture = false;
         for (auto& kv : materials)
         {
             agb_material m = defaultMaterial();
+            agb_material_textures t;
+            for (int k = 0; k < AGB_TEX_SLOTS; k++)
+                t.image[k] = -1;
             for (auto& p : kv.second)
+            {
+                if (applyTextureProperty(m, t, p.first, p.second, kv.first))
+                    continue;
                 applyMaterialProperty(m, p.first, p.second, kv.first);
+            }
+            for (int k = 0; k < AGB_TEX_SLOTS; k++)
+                anyTexture = anyTexture || t.image[k] >= 0;
             matIndex[kv.first] = int32_t(mats.size());
             mats.push_back(m);
+            texs.push_back(t);
         }
-        check(agb_materials_set(ctx, mats.data(), nullptr, uint32_t(mats.size())), "upload materials");
+        for (int k = 0; k < AGB_TEX_SLOTS; k++)
+            texs[0].image[k] = -1;
+        check(agb_materials_set(ctx, mats.data(), anyTexture ? texs.data() : nullptr, uint32_t(mats.size())),
+            "upload materials");
         std::vector<agb_instance> insts;
         for (auto& kv : instances)
         {
@@ -490,11 +541,49 @@ public:
             }
             const mat4* t = find<mat4>(p, Names::InstanceProperties::kTransform);
             rows3x4(t ? *t : kIdentity, in.object_to_world);
-            if (p.count(Names::InstanceProperties::kMaterialLayers))
-                logError("instance " + kv.first + ": material layers are not supported by this interface");
+            // Material layers (Resources.cpp:318-335; PTScene.cpp:1051-1166): layer i is the
+            // material of layer_materials[i] with the texture coordinates of the geometry
+            // layer_geometry[i], one per vertex of the instance's geometry.
+            const Strings* lm = find<Strings>(p, Names::InstanceProperties::kMaterialLayers);
+            const Strings* lg = find<Strings>(p, Names::InstanceProperties::kGeometryLayers);
+            if (lm && !lm->empty())
+            {
+                layerSets.emplace_back();
+                std::vector<agb_layer>& ls = layerSets.back();
+                const Geometry& base       = geometries[kv.second.geometry];
+                for (size_t li = 0; li < lm->size(); li++)
+                {
+                    auto mit = matIndex.find((*lm)[li]);
+                    if (mit == matIndex.end())
+                    {
+                        logError("instance " + kv.first + ": unknown layer material " + (*lm)[li]);
+                        continue;
+                    }
+                    if (!lg || li >= lg->size())
+                    {
+                        logError("instance " + kv.first + ": layer " + std::to_string(li) + " has no geometry");
+                        continue;
+                    }
+                    const std::vector<float>* uv = layerTexcoords((*lg)[li], base.desc.vertexDesc.count);
+                    if (!uv)
+                    {
+                        logError("instance " + kv.first + ": layer geometry " + (*lg)[li] +
+                            " needs texture coordinates for every vertex of " + kv.second.geometry);
+                        continue;
+                    }
+                    agb_layer l{};
+                    l.material  = mit->second;
+                    l.texcoords = uv->data();
+                    ls.push_back(l);
+                }
+                in.layer_count = int32_t(ls.size());
+                in.layers      = ls.empty() ? nullptr : ls.data();
+            }
             insts.push_back(in);
         }
         check(agb_instances_set(ctx, insts.data(), uint32_t(insts.size())), "upload instances");
+        layerSets.clear();
+        layerUVs.clear();
         applyEnvironment();
         dirty = false;
     }
@@ -575,6 +664,132 @@ public:
         return im.handle;
     }
 
+    // Layer arrays and layer texture coordinates of the activation in progress.
+    std::list<std::vector<agb_layer>> layerSets;
+    std::map<Path, std::vector<float>> layerUVs;
+
+    // The texture coordinates of a layer geometry, pulled from its descriptor; null unless it
+    // has one pair per vertex of a geometry with `vertexCount` vertices.
+    const std::vector<float>* layerTexcoords(const Path& path, size_t vertexCount)
+    {
+        auto cached = layerUVs.find(path);
+        if (cached != layerUVs.end())
+            return cached->second.size() == vertexCount * 2 ? &cached->second : nullptr;
+        std::vector<float>& uv = layerUVs[path];
+        auto it = geometries.find(path);
+        if (it == geometries.end())
+            return nullptr;
+        const GeometryDescriptor& d = it->second.desc;
+        if (!d.vertexDesc.attributes.count(Names::VertexAttributes::kTexCoord0) || d.vertexDesc.count != vertexCount)
+            return nullptr;
+        AttributeDataMap buffers;
+        buffers[Names::VertexAttributes::kTexCoord0] = AttributeData{};
+        if (!d.getAttributeData(buffers, 0, d.vertexDesc.count, 0, 0))
+            return nullptr;
+        const AttributeData& a = buffers[Names::VertexAttributes::kTexCoord0];
+        if (a.address)
+        {
+            size_t stride = a.stride ? a.stride : 2 * sizeof(float);
+            uv.resize(vertexCount * 2);
+            for (size_t v = 0; v < vertexCount; v++)
+                std::memcpy(&uv[v * 2], static_cast<const uint8_t*>(a.address) + a.offset + v * stride,
+                    2 * sizeof(float));
+        }
+        if (d.attributeUpdateComplete)
+            d.attributeUpdateComplete(buffers, 0, d.vertexDesc.count, 0, 0);
+        return uv.size() == vertexCount * 2 ? &uv : nullptr;
+    }
+
+    // A material texture: bilinear filtering (the default sampler, HGIRenderer.cpp:108-112); an
+    // 8-bit image with `linearize` set is decoded from sRGB to linear values first, as an sRGB
+    // texture format decodes it.
+    int32_t textureHandle(const Path& path)
+    {
+        auto it = images.find(path);
+        if (it == images.end())
+            throw Error("unknown image " + path);
+        Image& im = it->second;
+        if (im.texHandle >= 0)
+            return im.texHandle;
+        ImageData data;
+        if (!im.desc.getData(data) || !data.pPixelBuffer)
+            throw Error("image " + path + ": getData failed");
+        const uint32_t w = uint32_t(data.dimensions[0]), h = uint32_t(data.dimensions[1]);
+        if (data.format == ImageFormat::Integer_RGBA && im.desc.linearize)
+        {
+            std::vector<float> px(size_t(w) * h * 4);
+            size_t row = data.bytesPerRow ? data.bytesPerRow : size_t(w) * 4;
+            for (uint32_t y = 0; y < h; y++)
+                for (uint32_t x = 0; x < w; x++)
+                {
+                    const uint8_t* s8 = static_cast<const uint8_t*>(data.pPixelBuffer) + y * row + x * 4;
+                    float* d          = &px[(size_t(y) * w + x) * 4];
+                    for (int c = 0; c < 3; c++)
+                    {
+                        double v = double(s8[c]) / 255.0;
+                        d[c] = float(v <= 0.04045 ? v / 12.92 : std::pow((v + 0.055) / 1.055, 2.4));
+                    }
+                    d[3] = float(s8[3]) / 255.f;
+                }
+            check(agb_image_create(ctx, px.data(), w, h, AGB_FORMAT_RGBA32F, 1, &im.texHandle), "image " + path);
+        }
+        else
+        {
+            int32_t fmt = data.format == ImageFormat::Integer_RGBA ? AGB_FORMAT_RGBA8_UNORM
+                : data.format == ImageFormat::Float_RGBA           ? AGB_FORMAT_RGBA32F
+                                                                   : AGB_FORMAT_RGB32F;
+            check(agb_image_create(ctx, data.pPixelBuffer, w, h, fmt, 1, &im.texHandle), "image " + path);
+        }
+        if (im.desc.updateComplete)
+            im.desc.updateComplete(data);
+        return im.texHandle;
+    }
+
+    // Texture image and sampler properties; false for any other property.
+    bool applyTextureProperty(agb_material& m, agb_material_textures& t, const std::string& name,
+        const PropertyValue& v, const Path& path)
+    {
+        for (const TexField& f : kTexFields)
+        {
+            if (name == f.name)
+            {
+                auto* ip = std::get_if<std::string>(&v);
+                if (!ip)
+                {
+                    logError("material " + path + ": " + name + " wants an image path");
+                    return true;
+                }
+                int32_t has = 0;
+                if (!ip->empty())
+                {
+                    t.image[f.slot] = textureHandle(*ip);
+                    has             = 1;
+                }
+                std::memcpy(reinterpret_cast<uint8_t*>(&m) + f.hasOffset, &has, 4);
+                return true;
+            }
+            if (name == std::string(f.name) + "_sampler")
+            {
+                auto* sp = std::get_if<std::string>(&v);
+                if (sp && !sp->empty())
+                {
+                    auto it = samplers.find(*sp);
+                    if (it == samplers.end())
+                        logError("material " + path + ": unknown sampler " + *sp);
+                    else
+                        for (const std::string& k :
+                            { Names::SamplerProperties::kAddressModeU, Names::SamplerProperties::kAddressModeV })
+                            if (auto* mode = find<std::string>(it->second, k))
+                                if (*mode != Names::AddressModes::kWrap)
+                                    logError("sampler " + *sp + ": address mode " + *mode +
+                                        " is sampled with wrapping");
+                }
+                return true;
+            }
+        }
+        return false;
+    }
+
     void applyEnvironment()
     {
         agb_environment_data e;
@@ -643,6 +858,15 @@ public:
                     dst[0] = (*x)[0];
                     dst[1] = (*x)[1];
                     dst[2] = (*x)[2];
+                    return;
+                }
+            }
+            else if (f.count == 2)
+            {
+                if (auto* x = std::get_if<vec2>(&v))
+                {
+                    dst[0] = (*x)[0];
+                    dst[1] = (*x)[1];
                     return;
                 }
             }

@@ -36,8 +36,10 @@ namespace agb_aurora
 
 using Path  = std::string;
 using Paths = std::vector<Path>;
+using vec2  = std::array<float, 2>;
 using vec3  = std::array<float, 3>;
 using mat4  = std::array<float, 16>;
+using Strings = std::vector<std::string>;
 
 struct Error : std::runtime_error
 {
@@ -47,7 +49,7 @@ struct Error : std::runtime_error
 AGB_CPP_API void setLogCallback(std::function<void(const std::string&)> cb);
 
 // A property value (Aurora.h:125-300, reduced to the kinds this path uses).
-using PropertyValue = std::variant<bool, int, float, vec3, mat4, std::string>;
+using PropertyValue = std::variant<bool, int, float, vec2, vec3, mat4, std::string, Strings>;
 using Properties    = std::map<std::string, PropertyValue>;
 
 // Property names (AuroraNames.cpp).
@@ -80,6 +82,19 @@ inline const std::string kNormal("normal");
 inline const std::string kTexCoord0("tcoord0");
 inline const std::string kIndices("indices");
 } // namespace VertexAttributes
+namespace SamplerProperties
+{
+inline const std::string kAddressModeU("AddressModeU");
+inline const std::string kAddressModeV("AddressModeV");
+} // namespace SamplerProperties
+namespace AddressModes
+{
+inline const std::string kWrap("Wrap");
+inline const std::string kMirror("Mirror");
+inline const std::string kClamp("Clamp");
+inline const std::string kBorder("Border");
+inline const std::string kMirrorOnce("MirrorOnce");
+} // namespace AddressModes
 namespace LightTypes
 {
 inline const std::string kDistantLight("DistantLight");
@@ -214,7 +229,14 @@ public:
     virtual void setMaterialType(const Path& atPath,
         const std::string& materialType = Names::MaterialTypes::kBuiltIn,
         const std::string& document     = "Default")                                      = 0;
+    // Material properties are the Standard Surface names (MaterialBase.cpp), with textures as
+    // image paths: base_color_image, specular_roughness_image, opacity_image, normal_image,
+    // emission_color_image, each with <name>_offset / _scale / _pivot (vec2), _rotation (float)
+    // and _sampler (a sampler path).
     virtual void setMaterialProperties(const Path& path, const Properties& materialProperties) = 0;
+    // Samplers (Aurora.h:922): AddressModeU / AddressModeV.  Textures here wrap (the reference's
+    // default sampler); other modes are reported and sampled with wrapping.
+    virtual void setSamplerProperties(const Path& atPath, const Properties& props)      = 0;
     virtual bool addInstance(const Path& path, const Path& geometry, const Properties& properties = {}) = 0;
     virtual void setInstanceProperties(const Path& path, const Properties& instanceProperties) = 0;
     virtual void removeInstance(const Path& path)                                         = 0;

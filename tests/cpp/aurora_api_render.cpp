@@ -5,12 +5,16 @@
 //
 // usage: aurora_api_render <scene file> <output file>
 // Scene file (little-endian), written by tests/test_aurora_api.py:
-//   "AGBS", u32 version 1, u32 width, height, spp, trace depth, f32 view[16], proj[16] (column-major)
+//   "AGBS", u32 version (1 or 2), u32 width, height, spp, trace depth, f32 view[16], proj[16]
+//     (column-major)
 //   u32 meshes; per mesh: u32 vertices, indices, f32 positions[3v], u8 has normals + f32[3v],
 //     u8 has uvs + f32[2v], u32 indices[i]
+//   version 2: u32 images; per image: u32 width, height, u8 linearize, u8 rgba[4 * w * h]
 //   u32 materials; per material: u32 properties; per property: u8 name length, name, u8 kind
-//     (1 float, 3 float3, 2 bool), values; or u32 0xFFFFFFFF, u32 length, a MaterialX document
-//   u32 instances; per instance: u32 mesh, u32 material, f32 transform[16] (column-major)
+//     (1 float, 3 float3, 2 bool, 4 string: u8 length + chars, 5 float2), values; or
+//     u32 0xFFFFFFFF, u32 length, a MaterialX document
+//   u32 instances; per instance: u32 mesh, u32 material, f32 transform[16] (column-major);
+//     version 2: u32 layers; per layer: u32 material, u32 mesh with the layer's texcoords
 //   u32 lights; per light: f32 direction[3], color[3], intensity, angular diameter
 //   f32 light top[3], light bottom[3], background top[3], background bottom[3]
 //   u8 has environment image; if set: u32 width, height, f32 rgb[3 * width * height]
@@ -84,8 +88,11 @@ int main(int argc, char** argv)
                 throw Error("cannot read scene file");
             std::fclose(f);
         }
-        if (r.array<char>(4) != std::vector<char>{ 'A', 'G', 'B', 'S' } || r.get<uint32_t>() != 1)
-            throw Error("not a version 1 scene file");
+        if (r.array<char>(4) != std::vector<char>{ 'A', 'G', 'B', 'S' })
+            throw Error("not a scene file");
+        const uint32_t version = r.get<uint32_t>();
+        if (version != 1 && version != 2)
+            throw Error("not a version 1 or 2 scene file");
         uint32_t width = r.get<uint32_t>(), height = r.get<uint32_t>(), spp = r.get<uint32_t>();
         uint32_t depth = r.get<uint32_t>();
         mat4 view, proj;
@@ -133,6 +140,32 @@ int main(int argc, char** argv)
             };
             scene->setGeometryDescriptor("/mesh/" + std::to_string(m), d);
         }
+        // Version 2: RGBA8 images /image/<k> for material textures.
+        struct Img
+        {
+            uint32_t w = 0, h = 0;
+            std::vector<uint8_t> px;
+        };
+        std::vector<Img> imgs(version >= 2 ? r.get<uint32_t>() : 0);
+        for (size_t k = 0; k < imgs.size(); k++)
+        {
+            Img& im       = imgs[k];
+            im.w          = r.get<uint32_t>();
+            im.h          = r.get<uint32_t>();
+            bool linearize = r.get<uint8_t>() != 0;
+            im.px         = r.array<uint8_t>(size_t(im.w) * im.h * 4);
+            ImageDescriptor id;
+            id.linearize = linearize;
+            id.getData   = [&im](ImageData& d) {
+                d.pPixelBuffer = im.px.data();
+                d.bytesPerRow  = size_t(im.w) * 4;
+                d.bufferSize   = im.px.size();
+                d.dimensions   = { int(im.w), int(im.h) };
+                d.format       = ImageFormat::Integer_RGBA;
+                return true;
+            };
+            scene->setImageDescriptor("/image/" + std::to_string(k), id);
+        }
         uint32_t nm = r.get<uint32_t>();
         for (uint32_t m = 0; m < nm; m++)
         {
@@ -158,6 +191,16 @@ int main(int argc, char** argv)
                     auto v = r.array<float>(3);
                     props[name] = vec3{ v[0], v[1], v[2] };
                 }
+                else if (kind == 4)
+                {
+                    auto chars  = r.array<char>(r.get<uint8_t>());
+                    props[name] = std::string(chars.begin(), chars.end());
+                }
+                else if (kind == 5)
+                {
+                    auto v      = r.array<float>(2);
+                    props[name] = vec2{ v[0], v[1] };
+                }
                 else
                     props[name] = r.get<uint8_t>() != 0;
             }
@@ -172,9 +215,25 @@ int main(int argc, char** argv)
             auto t = r.array<float>(16);
             mat4 tm;
             std::memcpy(tm.data(), t.data(), 64);
-            scene->addInstance("/instance/" + std::to_string(i), "/mesh/" + std::to_string(mesh),
-                { { Names::InstanceProperties::kMaterial, std::string("/material/" + std::to_string(mat)) },
-                    { Names::InstanceProperties::kTransform, tm } });
+            Properties ip = { { Names::InstanceProperties::kMaterial, std::string("/material/" + std::to_string(mat)) },
+                { Names::InstanceProperties::kTransform, tm } };
+            if (version >= 2)
+            {
+                // Material layers: (layer material, mesh holding the layer's texture coordinates).
+                Strings lm, lg;
+                uint32_t nlayer = r.get<uint32_t>();
+                for (uint32_t k = 0; k < nlayer; k++)
+                {
+                    lm.push_back("/material/" + std::to_string(r.get<uint32_t>()));
+                    lg.push_back("/mesh/" + std::to_string(r.get<uint32_t>()));
+                }
+                if (nlayer)
+                {
+                    ip[Names::InstanceProperties::kMaterialLayers] = lm;
+                    ip[Names::InstanceProperties::kGeometryLayers] = lg;
+                }
+            }
+            scene->addInstance("/instance/" + std::to_string(i), "/mesh/" + std::to_string(mesh), ip);
         }
         uint32_t nl = r.get<uint32_t>();
         for (uint32_t l = 0; l < nl; l++)

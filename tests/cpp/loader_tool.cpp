@@ -51,8 +51,21 @@ void printValue(const PropertyValue& v)
         std::printf("%d", std::get<int>(v));
     else if (std::holds_alternative<float>(v))
         std::printf("%.9g", std::get<float>(v));
+    else if (std::holds_alternative<vec2>(v))
+        printFloats(std::get<vec2>(v).data(), 2);
     else if (std::holds_alternative<vec3>(v))
         printFloats(std::get<vec3>(v).data(), 3);
+    else if (std::holds_alternative<Strings>(v))
+    {
+        std::printf("[");
+        const Strings& list = std::get<Strings>(v);
+        for (size_t i = 0; i < list.size(); i++)
+        {
+            std::printf("%s", i ? "," : "");
+            printString(list[i]);
+        }
+        std::printf("]");
+    }
     else if (std::holds_alternative<mat4>(v))
         printFloats(std::get<mat4>(v).data(), 16);
     else

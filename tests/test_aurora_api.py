@@ -59,14 +59,37 @@ def materialx_document(mat, keys, name):
     return "\n".join(lines)
 
 
+TEX_NAMES = {0: "base_color_image", 1: "specular_roughness_image", 2: "opacity_image",
+             3: "normal_image", 4: "emission_color_image"}
+
+
 def write_scene(path, s, view, proj, lights, depth, mtlx=False):
+    """The scene file tests/cpp/aurora_api_render.cpp reads: version 2 when the scene has material
+    textures or layers (images, texture properties, per-instance layer lists; each distinct
+    layer UV set becomes one more mesh with the base mesh's geometry)."""
     from aurora_gb300 import _abi, scenes
+    layered = any(inst.get("layers") for inst in s.instances)
+    textured = s.textures is not None and bool((np.asarray(s.textures["image"]) >= 0).any())
+    version = 2 if (layered or textured) else 1
+    meshes = [dict(m) for m in s.meshes]
+    layer_mesh, inst_layers = {}, []
+    for inst in s.instances:
+        ls = []
+        for mat, uv in inst.get("layers") or []:
+            key = (inst["mesh"], np.ascontiguousarray(uv, np.float32).tobytes())
+            if key not in layer_mesh:
+                base = s.meshes[inst["mesh"]]
+                layer_mesh[key] = len(meshes)
+                meshes.append(dict(positions=base["positions"], normals=None,
+                                   texcoords=np.ascontiguousarray(uv, np.float32), indices=base["indices"]))
+            ls.append((mat, layer_mesh[key]))
+        inst_layers.append(ls)
     b = bytearray(b"AGBS")
-    b += struct.pack("<5I", 1, s.width, s.height, s.spp, depth)
+    b += struct.pack("<5I", version, s.width, s.height, s.spp, depth)
     b += np.asarray(view, np.float32).T.tobytes()   # column-major
     b += np.asarray(proj, np.float32).T.tobytes()
-    b += struct.pack("<I", len(s.meshes))
-    for m in s.meshes:
+    b += struct.pack("<I", len(meshes))
+    for m in meshes:
         b += struct.pack("<2I", len(m["positions"]), len(m["indices"]))
         b += np.asarray(m["positions"], np.float32).tobytes()
         for key in ("normals", "texcoords"):
@@ -74,6 +97,14 @@ def write_scene(path, s, view, proj, lights, depth, mtlx=False):
             if m[key] is not None:
                 b += np.asarray(m[key], np.float32).tobytes()
         b += np.asarray(m["indices"], np.uint32).tobytes()
+    if version >= 2:
+        b += struct.pack("<I", len(s.images))
+        for im in s.images:
+            px = np.asarray(im["pixels"])
+            if im["format"] != _abi.FORMAT_RGBA8:
+                px = np.zeros((im["height"], im["width"], 4), np.uint8)   # textures only; unused here
+            # linearize off: the C ABI samples the bytes as they are
+            b += struct.pack("<2IB", im["width"], im["height"], 0) + np.ascontiguousarray(px, np.uint8).tobytes()
     b += struct.pack("<I", len(s.materials))
     for mi, mat in enumerate(s.materials):
         props = list(scenes._DEFAULTS.keys())
@@ -81,7 +112,14 @@ def write_scene(path, s, view, proj, lights, depth, mtlx=False):
             doc = materialx_document(mat, props, f"m{mi}").encode()
             b += struct.pack("<II", 0xFFFFFFFF, len(doc)) + doc
             continue
-        b += struct.pack("<I", len(props))
+        tex = []
+        if textured:
+            for slot, name in TEX_NAMES.items():
+                img = int(s.textures["image"][mi, slot])
+                if img >= 0:
+                    tex.append((name, img))
+        count = len(props) + sum(5 for _ in tex)
+        b += struct.pack("<I", count)
         for k in props:
             b += struct.pack("<B", len(k)) + k.encode()
             v = mat[k]
@@ -91,11 +129,23 @@ def write_scene(path, s, view, proj, lights, depth, mtlx=False):
                 b += struct.pack("<B3f", 3, *[float(x) for x in v])
             else:
                 b += struct.pack("<Bf", 1, float(v))
+        for name, img in tex:
+            ipath = f"/image/{img}".encode()
+            b += struct.pack("<B", len(name)) + name.encode() + struct.pack("<BB", 4, len(ipath)) + ipath
+            for suffix in ("_offset", "_scale", "_pivot"):
+                k = name + suffix
+                b += struct.pack("<B", len(k)) + k.encode() + struct.pack("<B2f", 5, *map(float, mat[k]))
+            k = name + "_rotation"
+            b += struct.pack("<B", len(k)) + k.encode() + struct.pack("<Bf", 1, float(mat[k]))
     b += struct.pack("<I", len(s.instances))
-    for inst in s.instances:
+    for inst, ls in zip(s.instances, inst_layers):
         m4 = np.eye(4, dtype=np.float32)
         m4[:3, :] = np.asarray(inst["xform"], np.float32).reshape(3, 4)
         b += struct.pack("<2I", inst["mesh"], inst["material"]) + m4.T.tobytes()
+        if version >= 2:
+            b += struct.pack("<I", len(ls))
+            for mat, mesh in ls:
+                b += struct.pack("<2I", mat, mesh)
     b += struct.pack("<I", len(lights))
     for d, c, i, a in lights:
         b += struct.pack("<8f", *d, *c, i, a)
@@ -155,3 +205,54 @@ def test_cpp_interface_render_matches_c_abi(agb, oracle, ground, mtlx):
           f"identical pixels {np.mean(np.all(img == ref, axis=2)):.4f}")
     assert err < 1e-10
     assert np.abs(img[..., :3]).max() > 0
+
+
+@pytest.mark.gpu
+def test_cpp_interface_textures_and_layers_match_c_abi(agb, oracle):
+    """Material textures (image paths, a transformed base-colour texture), samplers and material
+    layers (layer_materials / layer_geometry, the layer's UVs from a geometry of its own) through
+    the C++ interface, against the same scene through the C ABI."""
+    from aurora_gb300 import _abi, api, scenes
+    exe = build_client()
+    s = scenes.config_layered(width=64, height=48, spp=4, trace_depth=4, blas=2, instances=6,
+                              tri_range=(200, 1000), decal_size=64)
+    color_img = int(s.textures["image"][6, _abi.TEX_BASE_COLOR])
+    s.materials["has_base_color_image"][0] = 1
+    s.textures["image"][0, _abi.TEX_BASE_COLOR] = color_img
+    s.materials["base_color_image_scale"][0] = (2.0, 0.5)
+    s.materials["base_color_image_offset"][0] = (0.1, 0.2)
+    s.materials["base_color_image_pivot"][0] = (0.5, 0.5)
+    s.materials["base_color_image_rotation"][0] = 0.3
+    view = np.asarray(scenes.look_at((0.0, 15.0, 60.0), (0.0, 0.0, 0.0)), np.float32)
+    proj = np.asarray(scenes.perspective(45.0, s.width / s.height), np.float32)
+    depth = 4
+    with tempfile.TemporaryDirectory() as tmp:
+        scene_file, out_file = os.path.join(tmp, "scene.bin"), os.path.join(tmp, "out.bin")
+        write_scene(scene_file, s, view, proj, [], depth)
+        subprocess.check_call([exe, scene_file, out_file])
+        raw = open(out_file, "rb").read()
+    w, h = struct.unpack("<2I", raw[:8])
+    img = np.frombuffer(raw[8:], np.float32).reshape(h, w, 4)
+    frame = scenes.frame_data(view.astype(np.float64), proj.astype(np.float64), trace_depth=depth,
+                              lights=[], scene_bounds=s.bounds())
+    with api.Renderer() as r:
+        r.upload(s)
+        r.set_frame(frame)
+        r.render(0, s.spp, accumulation=_abi.ACCUM_RUNNING_MEAN)
+        ref, _ = r.post_process(mode=_abi.ACCUM_RUNNING_MEAN)
+    # Without the textures and layers the image differs: they reach the renderer.
+    bare = scenes.config_layered(width=64, height=48, spp=4, trace_depth=4, blas=2, instances=6,
+                                 tri_range=(200, 1000), decal_size=64)
+    for inst in bare.instances:
+        inst["layers"] = []
+    with api.Renderer() as r:
+        r.upload(bare)
+        r.set_frame(frame)
+        r.render(0, s.spp, accumulation=_abi.ACCUM_RUNNING_MEAN)
+        plain, _ = r.post_process(mode=_abi.ACCUM_RUNNING_MEAN)
+    err = oracle.rel_mse(img, ref)
+    changed = np.mean(np.any(plain != ref, axis=2))
+    print(f"C++ interface (textures, layers) vs C ABI: relMSE {err:.3g}, identical pixels "
+          f"{np.mean(np.all(img == ref, axis=2)):.4f}; pixels the layers and textures change {changed:.3f}")
+    assert err < 1e-10
+    assert changed > 0.05
