@@ -19,7 +19,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["agb_pt.cu", "agb_env_build.cu", "agb_env_noalloc.cu", "agb_temporal.cu", "agb_denoise.cu",
            "agb_unet.cu", "agb_unit.cu",
-           "agb_capi.cu", "agb_serve.cpp", "agb_aurora.cpp", "agb_obj.cpp", "agb_gltf.cpp", "agb_mtlx.cpp", "agb_bvh_build.cpp",
+           "agb_capi.cu", "agb_serve.cpp", "agb_aurora.cpp", "agb_obj.cpp", "agb_gltf.cpp", "agb_mtlx.cpp", "agb_image_io.cpp", "agb_bvh_build.cpp",
            "agb_bvh_gpu.cu"]
 CLI_SRC = os.path.join(HERE, "cli", "agb_render.cpp")
 CLI = os.path.join(BUILD, "agb_render")

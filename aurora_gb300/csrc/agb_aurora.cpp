@@ -356,6 +356,58 @@ public:
         images[p] = Image{ d, -1 };
         dirty     = true;
     }
+    // The file is read when the image is first used and released once uploaded (the scene keeps
+    // the path, so a context change reads it again).
+    void setImageFromFilePath(const Path& p, const std::string& filePath, bool linearize, bool) override
+    {
+        struct FileImage
+        {
+            std::vector<uint8_t> rgba8;
+            std::vector<float> rgb32;
+            int w = 0, h = 0;
+        };
+        const std::string file = filePath.empty() ? p : filePath;
+        auto store             = std::make_shared<FileImage>();
+        ImageDescriptor d;
+        d.linearize = linearize;
+        d.getData   = [file, store](ImageData& out) {
+            const bool hdr = file.size() >= 4 && (file.compare(file.size() - 4, 4, ".hdr") == 0 ||
+                                                     file.compare(file.size() - 4, 4, ".HDR") == 0);
+            if (store->rgba8.empty() && store->rgb32.empty())
+            {
+                std::string err;
+                bool ok = hdr ? loadHDRFile(file, store->rgb32, store->w, store->h, err)
+                              : loadPNGFile(file, store->rgba8, store->w, store->h, err);
+                if (!ok)
+                {
+                    logError("image " + file + ": " + err);
+                    return false;
+                }
+            }
+            out.dimensions = { store->w, store->h };
+            if (hdr)
+            {
+                out.pPixelBuffer = store->rgb32.data();
+                out.bytesPerRow  = size_t(store->w) * 12;
+                out.bufferSize   = store->rgb32.size() * 4;
+                out.format       = ImageFormat::Float_RGB;
+            }
+            else
+            {
+                out.pPixelBuffer = store->rgba8.data();
+                out.bytesPerRow  = size_t(store->w) * 4;
+                out.bufferSize   = store->rgba8.size();
+                out.format       = ImageFormat::Integer_RGBA;
+            }
+            return true;
+        };
+        d.updateComplete = [store](const ImageData&) {
+            std::vector<uint8_t>().swap(store->rgba8);
+            std::vector<float>().swap(store->rgb32);
+        };
+        images[p] = Image{ d, -1, -1 };
+        dirty     = true;
+    }
     void setMaterialType(const Path& p, const std::string& type, const std::string& document) override
     {
         Properties& m = materials[p];

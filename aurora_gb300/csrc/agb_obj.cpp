@@ -354,11 +354,23 @@ bool translateOBJ(const ObjData& obj, const std::string& filePath, SceneContents
         if (length3(transmissionColor) == 0.0f)
             transmissionColor = { 1.f, 1.f, 1.f };
         vec3 emissionColor = sRGBToLinear3(m.emission);
-        for (const std::string* tex : { &m.diffuseTex, &m.roughnessTex, &m.emissiveTex, &m.alphaTex,
-                 &m.bumpTex, &m.normalTex })
-            if (!tex->empty())
-                contents.warnings += "texture '" + *tex + "' of material '" + m.name + "' not loaded\n";
-        float emission = length3(emissionColor) != 0.0f ? 1.0f : 0.0f;
+        // ImageCache::getImage (Loaders.h:22-38): one image path per (file, linearize).
+        auto image = [&](const std::string& name, bool linearize) -> Path {
+            if (name.empty())
+                return Path();
+            Path p = "PlasmaImage/" + name + ":linearize:" + std::to_string(linearize ? 1 : 0);
+            for (const SceneImageData& im : contents.images)
+                if (im.path == p)
+                    return p;
+            contents.images.push_back(SceneImageData{ p, directoryOf(filePath) + name, linearize });
+            return p;
+        };
+        Path baseColorImage         = image(m.diffuseTex, true);
+        Path specularRoughnessImage = image(m.roughnessTex, false);
+        Path emissionColorImage     = image(m.emissiveTex, true);
+        Path opacityImage           = image(m.alphaTex, false);
+        Path normalImage            = image(m.normalTex.empty() ? m.bumpTex : m.normalTex, false);
+        float emission = (!emissionColorImage.empty() || length3(emissionColor) != 0.0f) ? 1.0f : 0.0f;
         SceneMaterialData md;
         md.path       = filePath + "-" + m.name + ":OBJFileMaterial-" + std::to_string(mtlCount++);
         md.properties = {
@@ -372,6 +384,11 @@ bool translateOBJ(const ObjData& obj, const std::string& filePath, SceneContents
             { "emission", emission },
             { "emission_color", emissionColor },
             { "opacity", vec3{ 1.f, 1.f, 1.f } },
+            { "base_color_image", baseColorImage },
+            { "specular_roughness_image", specularRoughnessImage },
+            { "emission_color_image", emissionColorImage },
+            { "opacity_image", opacityImage },
+            { "normal_image", normalImage },
         };
         materialPaths.push_back(md.path);
         contents.materials.push_back(std::move(md));
@@ -486,6 +503,8 @@ void addContentsToScene(IScene* scene, SceneContents& contents)
 {
     if (!scene)
         return;
+    for (const SceneImageData& im : contents.images)
+        scene->setImageFromFilePath(im.path, im.file, im.linearize);
     for (const SceneMaterialData& m : contents.materials)
     {
         scene->setMaterialType(m.path);

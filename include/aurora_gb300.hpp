@@ -226,6 +226,11 @@ class IScene
 public:
     virtual void setGeometryDescriptor(const Path& atPath, const GeometryDescriptor& desc) = 0;
     virtual void setImageDescriptor(const Path& atPath, const ImageDescriptor& desc)       = 0;
+    // An image read from a file when first used (Aurora.h:905-914): PNG (8 or 16 bits, grey,
+    // grey + alpha, RGB, RGBA or palette, non-interlaced) or Radiance HDR; an empty filePath
+    // reads atPath.  linearize: 8-bit texels are sRGB encoded.
+    virtual void setImageFromFilePath(const Path& atPath, const std::string& filePath = "",
+        bool linearize = true, bool isEnvironment = false)                                = 0;
     virtual void setMaterialType(const Path& atPath,
         const std::string& materialType = Names::MaterialTypes::kBuiltIn,
         const std::string& document     = "Default")                                      = 0;

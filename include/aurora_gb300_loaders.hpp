@@ -69,6 +69,13 @@ struct SceneMaterialData
     Path path;
     Properties properties;
 };
+// An image file a material refers to, handed to IScene::setImageFromFilePath.
+struct SceneImageData
+{
+    Path path;
+    std::string file;
+    bool linearize = true;
+};
 // A camera of a glTF file (Plasma's SceneCamera, SceneContents.h:27-61).
 struct SceneCamera
 {
@@ -90,6 +97,7 @@ struct SceneContents
     std::vector<SceneCamera> cameras;
     std::vector<SceneInstanceData> instances;
     std::vector<SceneMaterialData> materials;
+    std::vector<SceneImageData> images;
     vec3 boundsMin = { 0.f, 0.f, 0.f }, boundsMax = { 0.f, 0.f, 0.f };
     uint32_t vertexCount = 0, triangleCount = 0;
     std::string warnings;
@@ -98,8 +106,10 @@ struct SceneContents
 // The reference's translation of parsed OBJ data (OBJLoader.cpp:155-449): Standard Surface
 // properties from the MTL values, unique (position, normal, texcoord) vertices per shape,
 // normalised normals, flipped V, generated normals where the file has none, one instance per
-// shape with the material of its first face.  Texture files (map_Kd, map_Pr, map_Ke, map_d,
-// bump / norm) are not loaded: their properties are left unset, with a warning.
+// shape with the material of its first face.  Texture files (map_Kd and map_Ke decoded from
+// sRGB, map_Pr, map_d and norm / bump linear; OBJLoader.cpp:176-227) become image paths
+// `PlasmaImage/<file>:linearize:<0|1>` listed in contents.images, the file resolved beside the
+// OBJ file; emission is 1 when there is an emission colour image.
 AGB_CPP_API bool translateOBJ(const ObjData& obj, const std::string& filePath, SceneContents& contents);
 // loadOBJFile (OBJLoader.cpp:73-473): parse + translate + hand everything to the scene.
 AGB_CPP_API bool loadOBJFile(IScene* scene, const std::string& filePath, SceneContents& contents);
@@ -138,6 +148,14 @@ AGB_CPP_API bool materialXFileToProperties(const std::string& path, Properties& 
 // Angle-weighted smooth vertex normals (Foundation/Source/Geometry.cpp:29-99).
 AGB_CPP_API void calculateNormals(size_t vertexCount, const float* positions, size_t triangleCount,
     const uint32_t* indices, float* normalsOut);
+
+// PNG files to 8-bit RGBA, top row first (agb_image_io.cpp: zlib / DEFLATE and the scanline
+// filters restated from RFC 1950 / 1951 and the PNG specification): grey, grey + alpha, RGB, RGBA
+// and palette images at 1-16 bits, non-interlaced.
+AGB_CPP_API bool decodePNG(const std::string& data, std::vector<uint8_t>& rgba, int& width, int& height,
+    std::string& error);
+AGB_CPP_API bool loadPNGFile(const std::string& path, std::vector<uint8_t>& rgba, int& width, int& height,
+    std::string& error);
 
 // Radiance RGBE (.hdr) image, flat or run-length encoded scanlines, to RGB floats top row first.
 AGB_CPP_API bool loadHDRFile(const std::string& path, std::vector<float>& rgb, int& width, int& height,

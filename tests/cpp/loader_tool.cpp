@@ -3,6 +3,7 @@
 //   loader_tool gltf <file.gltf|file.glb>           parse + translate, no scene
 //   loader_tool gltfsave <out.gltf> <in.gltf>       the input's cameras written as a glTF file
 //   loader_tool mtlx <file.mtlx>                    standard_surface constants as properties
+//   loader_tool pngread <file.png>                  decoded 8-bit RGBA
 //   loader_tool hdr <file.hdr>                      width, height, RGB floats
 //   loader_tool png <out.png> <w> <h>               writes a pattern image
 //   loader_tool pfm <out.pfm> <w> <h>               writes a pattern image
@@ -79,6 +80,20 @@ int main(int argc, char** argv)
     if (argc < 3)
         return 2;
     std::string mode = argv[1];
+    if (mode == "pngread")
+    {
+        std::vector<uint8_t> rgba;
+        int w = 0, h = 0;
+        std::string err;
+        bool ok = loadPNGFile(argv[2], rgba, w, h, err);
+        std::printf("{\"ok\":%s,\"error\":", ok ? "true" : "false");
+        printString(err);
+        std::printf(",\"width\":%d,\"height\":%d,\"rgba\":[", w, h);
+        for (size_t i = 0; i < rgba.size(); i++)
+            std::printf("%s%u", i ? "," : "", unsigned(rgba[i]));
+        std::printf("]}\n");
+        return 0;
+    }
     if (mode == "mtlx")
     {
         Properties props;
@@ -156,6 +171,15 @@ int main(int argc, char** argv)
             for (size_t k = 0; k < g.indices.size(); k++)
                 std::printf("%s%u", k ? "," : "", g.indices[k]);
             std::printf("]}");
+        }
+        std::printf("],\"images\":[");
+        for (size_t i = 0; i < c.images.size(); i++)
+        {
+            std::printf("%s{\"path\":", i ? "," : "");
+            printString(c.images[i].path);
+            std::printf(",\"file\":");
+            printString(c.images[i].file);
+            std::printf(",\"linearize\":%s}", c.images[i].linearize ? "true" : "false");
         }
         std::printf("],\"cameras\":[");
         for (size_t i = 0; i < c.cameras.size(); i++)

@@ -36,11 +36,12 @@ def write_obj(path, meshes):
         "newmtl floor\nKd 0.7 0.7 0.6\nPm 0.5\nPr 0.6\nd 0.8\n")
 
 
-@pytest.mark.parametrize("ground", [False, True])
-def test_cli_render_matches_c_abi(agb, oracle, ground):
+@pytest.mark.parametrize("ground,texture", [(False, False), (True, False), (False, True)])
+def test_cli_render_matches_c_abi(agb, oracle, ground, texture):
     """With `ground`, the floor quad gives way to the CLI's ground plane (--ground_shadow 1
     --ground_reflection 1: Plasma's plane at the scene's lower bound, shadow opacity 1,
-    reflection opacity 0.5)."""
+    reflection opacity 0.5).  With `texture`, the floor's MTL record names a PNG (map_Kd), which
+    the C ABI side receives decoded from sRGB with the same formula."""
     from aurora_gb300 import _abi, api, build, scenes
     build.build()
     exe = build.CLI
@@ -54,6 +55,12 @@ def test_cli_render_matches_c_abi(agb, oracle, ground):
         if not ground:
             meshes.append(("ground", "floor", qp, qn, qt, qi))
         write_obj(obj, meshes)
+        if texture:
+            from test_loaders import png_bytes
+            tex_px = np.random.default_rng(9).integers(0, 256, (16, 24, 3))
+            open(os.path.join(tmp, "floor.png"), "wb").write(png_bytes(tex_px, 2, 8, [0, 1, 4]))
+            with open(os.path.join(tmp, "scene.mtl"), "a") as f:
+                f.write("map_Kd floor.png\n")
         enc = np.array([[rgbe(px) for px in row] for row in env], np.uint8)
         hdr = os.path.join(tmp, "env.hdr")
         open(hdr, "wb").write(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y 16 +X 32\n" + enc.tobytes())
@@ -71,17 +78,30 @@ def test_cli_render_matches_c_abi(agb, oracle, ground):
         img = np.frombuffer(data[len(head):], "<f4").reshape(48, 64, 3)[::-1]
         scene = loader("obj", obj)
         env_f = np.reshape(loader("hdr", hdr)["rgb"], (16, 32, 3)).astype(np.float32)
+        tex = loader("pngread", os.path.join(tmp, "floor.png")) if texture else None
     s = scenes.SceneDesc("cli")
     names = {m["path"]: k for k, m in enumerate(scene["materials"])}
     s.materials = scenes.materials(len(names))
     for m in scene["materials"]:
         for key, v in m["properties"].items():
-            s.materials[key][names[m["path"]]] = v
+            if not key.endswith("_image"):      # texture paths: bound below
+                s.materials[key][names[m["path"]]] = v
     for inst in scene["instances"]:
         mesh = s.add_mesh(np.reshape(inst["positions"], (-1, 3)), np.reshape(inst["normals"], (-1, 3)),
                           np.reshape(inst["texcoords"], (-1, 2)), np.array(inst["indices"], np.uint32))
         s.instances.append(dict(mesh=mesh, material=names[inst["material"]],
                                 xform=np.eye(4, dtype=np.float32)[:3].reshape(-1), layers=[]))
+    if texture:
+        # The C++ interface's decode of an sRGB 8-bit texture: v / 12.92 or ((v + 0.055) / 1.055)^2.4
+        # in double precision, alpha / 255.
+        rgba = np.float64(np.reshape(tex["rgba"], (tex["height"], tex["width"], 4))) / 255.0
+        lin = np.where(rgba <= 0.04045, rgba / 12.92, ((rgba + 0.055) / 1.055) ** 2.4)
+        lin[..., 3] = rgba[..., 3]
+        tex_id = s.add_image(lin.astype(np.float32), _abi.FORMAT_RGBA32F, linear=True)
+        s.textures = scenes.no_textures(len(names))
+        floor = [m["path"] for m in scene["materials"] if m["properties"].get("base_color_image")][0]
+        s.materials["has_base_color_image"][names[floor]] = 1
+        s.textures["image"][names[floor], _abi.TEX_BASE_COLOR] = tex_id
     img_id = s.add_image(env_f, _abi.FORMAT_RGB32F)
     s.env_light = img_id
     s.env_background = img_id
@@ -168,7 +188,8 @@ def test_cli_gltf_camera_render_matches_c_abi(agb, oracle):
     s.materials = scenes.materials(len(names))
     for m in scene["materials"]:
         for key, v in m["properties"].items():
-            s.materials[key][names[m["path"]]] = v
+            if not key.endswith("_image"):      # texture paths: bound below
+                s.materials[key][names[m["path"]]] = v
     for inst in scene["instances"]:
         tc = inst["texcoords"]
         mesh = s.add_mesh(np.reshape(inst["positions"], (-1, 3)), np.reshape(inst["normals"], (-1, 3)),

@@ -105,7 +105,11 @@ def test_obj_translation_follows_reference_loader():
     assert g["transmission_color"] == [1.0, 1.0, 1.0]                 # black Tf -> white
     assert g["emission"] == 1.0
     np.testing.assert_array_equal(np.float32(g["emission_color"]), srgb_to_linear([0.5, 0.25, 0.0]))
-    assert "texture.png" in r["warnings"]
+    # map_Kd: an sRGB image path (ImageCache::getImage), the file beside the OBJ file.
+    assert g["base_color_image"] == "PlasmaImage/texture.png:linearize:1"
+    assert p["base_color_image"] == "" and g["opacity_image"] == "" and g["normal_image"] == ""
+    assert r["images"] == [{"path": "PlasmaImage/texture.png:linearize:1",
+                            "file": os.path.join(os.path.dirname(path), "texture.png"), "linearize": True}]
     assert red["path"].endswith("-red:OBJFileMaterial-0") and glass["path"].endswith("-glass:OBJFileMaterial-1")
 
     quad, tri = r["instances"]
@@ -260,3 +264,103 @@ def test_camera_fit():
     dist = (dims[0] if wide else dims[1]) / (2 * np.tan(half)) + dims[2] / 2
     np.testing.assert_allclose(r["target"], target, rtol=1e-6)
     np.testing.assert_allclose(r["eye"], target - dist * f, rtol=1e-5)
+
+
+def png_bytes(pixels, color, depth, filters, level=9, palette=None, trns=None):
+    """A PNG of `pixels` (H x W x channels samples, unsigned) with the given filter type per row
+    (the filters applied here as the encoder would), compressed by zlib at `level`."""
+    h, w = pixels.shape[:2]
+    ch = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[color]
+    bpp_bits = ch * depth
+    rows = []
+    for y in range(h):
+        if depth >= 8:
+            row = pixels[y].reshape(-1).astype(">u2" if depth == 16 else np.uint8).tobytes()
+        else:
+            bits = "".join(format(int(v), f"0{depth}b") for v in pixels[y].reshape(-1))
+            bits += "0" * (-len(bits) % 8)
+            row = bytes(int(bits[i:i + 8], 2) for i in range(0, len(bits), 8))
+        rows.append(np.frombuffer(row, np.uint8).astype(np.int32))
+    bpp = max(1, bpp_bits // 8)
+    out = bytearray()
+    prev = np.zeros_like(rows[0])
+    for y, cur in enumerate(rows):
+        f = filters[y % len(filters)]
+        a = np.concatenate([np.zeros(bpp, np.int32), cur[:-bpp]])
+        c = np.concatenate([np.zeros(bpp, np.int32), prev[:-bpp]])
+        b = prev
+        if f == 0:
+            enc = cur
+        elif f == 1:
+            enc = cur - a
+        elif f == 2:
+            enc = cur - b
+        elif f == 3:
+            enc = cur - (a + b) // 2
+        else:
+            p = a + b - c
+            pa, pb, pc = np.abs(p - a), np.abs(p - b), np.abs(p - c)
+            pred = np.where((pa <= pb) & (pa <= pc), a, np.where(pb <= pc, b, c))
+            enc = cur - pred
+        out += bytes([f]) + (enc % 256).astype(np.uint8).tobytes()
+        prev = cur
+
+    def chunk(t, body):
+        return struct.pack(">I", len(body)) + t + body + struct.pack(">I", zlib.crc32(t + body) & 0xffffffff)
+
+    png = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, color, 0, 0, 0))
+    if palette is not None:
+        png += chunk(b"PLTE", bytes(palette))
+    if trns is not None:
+        png += chunk(b"tRNS", bytes(trns))
+    data = zlib.compress(bytes(out), level)
+    return png + chunk(b"IDAT", data[:len(data) // 2]) + chunk(b"IDAT", data[len(data) // 2:]) + chunk(b"IEND", b"")
+
+
+def test_png_decoder_matches_restatement():
+    """Every colour type and bit depth the decoder takes, all five filters, stored / fixed /
+    dynamic DEFLATE blocks (zlib levels 0, 1, 9) and a split IDAT, against the expected RGBA."""
+    rng = np.random.default_rng(5)
+    cases = []
+    for color, depth in ((0, 1), (0, 2), (0, 4), (0, 8), (0, 16), (2, 8), (2, 16), (3, 1), (3, 4), (3, 8),
+                         (4, 8), (4, 16), (6, 8), (6, 16)):
+        h, w = 7, 13
+        ch = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[color]
+        hi = (1 << depth) - 1
+        px = rng.integers(0, hi + 1, (h, w, ch))
+        palette = trns = None
+        if color == 3:
+            n = hi + 1
+            palette = rng.integers(0, 256, 3 * n).tolist()
+            trns = rng.integers(0, 256, n // 2).tolist()
+        cases.append((color, depth, px, palette, trns))
+    with tempfile.TemporaryDirectory() as tmp:
+        for k, (color, depth, px, palette, trns) in enumerate(cases):
+            for level in (0, 1, 9):
+                path = os.path.join(tmp, f"t{k}_{level}.png")
+                open(path, "wb").write(png_bytes(px, color, depth, [0, 1, 2, 3, 4], level, palette, trns))
+                r = run("pngread", path)
+                assert r["ok"], (color, depth, r["error"])
+                got = np.uint8(r["rgba"]).reshape(px.shape[0], px.shape[1], 4)
+                if color == 3:
+                    pal = np.uint8(palette).reshape(-1, 3)
+                    alpha = np.full(len(pal), 255, np.uint8)
+                    alpha[:len(trns)] = trns
+                    want = np.concatenate([pal[px[..., 0]], alpha[px[..., 0]][..., None]], axis=2)
+                else:
+                    # samples to 8 bits: 16-bit keeps the high byte, low-depth grey is scaled
+                    s8 = px >> 8 if depth == 16 else (px * 255 // ((1 << depth) - 1) if depth < 8 else px)
+                    opaque = np.full(px.shape[:2] + (1,), 255)
+                    if color in (0, 4):
+                        alpha = s8[..., 1:2] if color == 4 else opaque
+                        want = np.concatenate([s8[..., :1]] * 3 + [alpha], axis=2)
+                    else:
+                        alpha = s8[..., 3:4] if color == 6 else opaque
+                        want = np.concatenate([s8[..., :3], alpha], axis=2)
+                np.testing.assert_array_equal(got, np.uint8(want), err_msg=f"color {color} depth {depth} level {level}")
+        bad = os.path.join(tmp, "bad.png")
+        data = png_bytes(cases[5][2], 2, 8, [0])
+        open(bad, "wb").write(data[:60])
+        assert not run("pngread", bad)["ok"]
+        open(bad, "wb").write(b"GIF89a")
+        assert "not a PNG" in run("pngread", bad)["error"]
