@@ -1221,9 +1221,8 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
             {
                 r.closest_rays += c[counterWords * w + kCounterStride * b + CNT_RAYS];
                 r.shadow_rays += c[counterWords * w + kCounterStride * b + CNT_SHADOW];
+                r.shadow_rays += c[counterWords * w + kCounterStride * b + CNT_GROUND_SHADOW];
             }
-            // Ground-plane matte-shadow rays (counter block depth + 1).
-            r.shadow_rays += c[counterWords * w + kCounterStride * (depth + 1) + CNT_SHADOW];
         }
         r.node_visits        = s[2];
         r.tri_tests          = s[3];

@@ -240,13 +240,16 @@ __global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_closes
         atomicAdd(statPtr(wb, 4), 1ull);
 }
 
+// Opaque shadow rays of the bounce's counter block: the shading's (CNT_SHADOW / CNT_SHADOW_WORK)
+// or the ground plane's (CNT_GROUND_SHADOW / CNT_GROUND_WORK).
 template <bool kCount>
-__global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_shadow(DevScene s, WaveBuffers wb, int bounce)
+__global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_shadow(DevScene s, WaveBuffers wb,
+    int bounce, int countSlot, int workSlot)
 {
-    uint32_t n      = wb.counters[bounce * kCounterStride + CNT_SHADOW];
+    uint32_t n      = wb.counters[bounce * kCounterStride + countSlot];
     TraceCounters c = { 0, 0 };
     bool overflow   = false;
-    persistentTrace<true, kCount>(s, n, wb.counters + bounce * kCounterStride + CNT_SHADOW_WORK,
+    persistentTrace<true, kCount>(s, n, wb.counters + bounce * kCounterStride + workSlot,
         ShadowLoader{ wb.shTag, wb.shOrg, wb.shDir }, OcclusionWriter{ wb.shTag, wb.occluded },
         g_stack + threadIdx.x, kTraceBlock, c, overflow);
     if (kCount)
@@ -386,7 +389,7 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
         uint32_t i     = base + threadIdx.x;
         bool valid     = i < n;
         // A camera ray the ground plane turned into a reflection ray has nothing to shade here.
-        if (valid && bounce == 0 && !depthLimit && s.ground.enabled && wb.hitInst[i] == kGroundAbsorbed)
+        if (valid && !depthLimit && s.ground.enabled && wb.hitInst[i] == kGroundAbsorbed)
             valid = false;
         bool pushNext  = false;
         uint32_t slots = 0;
@@ -941,8 +944,9 @@ AGB_D v3 sampleGGXSmithBRDF(v3 V, v3 f0, float roughness, v2 r, v3& L, float& pd
     return F * (D * G2) / (4.f * fabsf(V.z) * fabsf(L.z));
 }
 
-// The ground plane for the camera rays of bounce 0 (evaluateGroundPlane, GroundPlane.slang:236-289,
-// called first by the closest-hit and miss shaders while the ray is primary), after their
+// The ground plane for the primary rays of a bounce (evaluateGroundPlane, GroundPlane.slang:236-289,
+// called first by the closest-hit and miss shaders while the ray is primary: the camera rays and
+// the rays that passed through a transparent surface since, which stay primary), after their
 // closest-hit traversal and before shading.  A ray that meets the plane from its front side
 // nearer than its hit (any distance on a miss) draws from its own random stream, in the
 // reference's order:
@@ -953,11 +957,12 @@ AGB_D v3 sampleGGXSmithBRDF(v3 V, v3 f0, float roughness, v2 r, v3& L, float& pd
 //     absorbed.  A black BSDF sample leaves the ray unabsorbed with only the opacity scale;
 //   - otherwise the contribution is scaled by the transparency / Pr and, with a shadow opacity,
 //     an environment sample above the plane is traced as an opaque shadow ray (shadeMatteShadow,
-//     GroundPlane.slang:71-104) in counter block `shadowBlock`; k_ground_shadow applies it.
-__global__ void k_ground(DevScene s, agb_frame_data f, WaveParams wp, WaveBuffers wb, int shadowBlock)
+//     GroundPlane.slang:71-104; counter CNT_GROUND_SHADOW of the bounce) whose colour factor
+//     waits in the path's first pending slot until k_ground_shadow applies it.
+__global__ void k_ground(DevScene s, agb_frame_data f, WaveParams wp, WaveBuffers wb, int bounce, int cur)
 {
     const DevGroundPlane& g = s.ground;
-    uint32_t n      = wb.counters[CNT_RAYS];
+    uint32_t n      = wb.counters[bounce * kCounterStride + CNT_RAYS];
     uint32_t stride = gridDim.x * blockDim.x;
     const v3 N = ld3(g.normal), X = ld3(g.tangent), Y = ld3(g.bitangent), P0 = ld3(g.position);
     v2 screen  = v2{ float(wp.width), float(wp.height) };
@@ -969,8 +974,8 @@ __global__ void k_ground(DevScene s, agb_frame_data f, WaveParams wp, WaveBuffer
         v3 hitPos = splat(0.f), nextD = splat(0.f), shadowL = splat(0.f);
         if (i < n)
         {
-            p         = wb.rayPath[0][i];
-            float4 o4 = wb.rayOrg[0][i], d4 = wb.rayDir[0][i];
+            p         = wb.rayPath[cur][i];
+            float4 o4 = wb.rayOrg[cur][i], d4 = wb.rayDir[cur][i];
             v3 o      = v3{ o4.x, o4.y, o4.z }, d = v3{ d4.x, d4.y, d4.z };
             // RayTCurrent(): the hit distance, or the ray's TMax (infinity) on a miss.
             float tCur = wb.hitInst[i] >= 0 ? wb.hitTUV[i].x : d4.w;
@@ -983,7 +988,7 @@ __global__ void k_ground(DevScene s, agb_frame_data f, WaveParams wp, WaveBuffer
                 dist    = dot(P0 - o, N) / planeDot;
                 onPlane = !(dist < 0.f);
             }
-            if (onPlane && dist < tCur)
+            if ((wb.flags[p] & PF_PRIMARY) && onPlane && dist < tCur)
             {
                 hitPos = o + d * dist;
                 Rng rng;
@@ -1031,9 +1036,14 @@ __global__ void k_ground(DevScene s, agb_frame_data f, WaveParams wp, WaveBuffer
                         shadowL   = L;
                     }
                 }
-                wb.rng[p]     = make_uint2(rng.x, rng.y);
-                float4 c4     = wb.contrib[p];
-                wb.contrib[p] = make_float4(c4.x * color.x, c4.y * color.y, c4.z * color.z, 0.f);
+                wb.rng[p] = make_uint2(rng.x, rng.y);
+                if (shadowRay)
+                    wb.pendSlot[size_t(p) * kMaxShadowSlots] = make_float4(color.x, color.y, color.z, 0.f);
+                else
+                {
+                    float4 c4     = wb.contrib[p];
+                    wb.contrib[p] = make_float4(c4.x * color.x, c4.y * color.y, c4.z * color.z, 0.f);
+                }
                 if (reflectRay)
                 {
                     wb.hitInst[i] = kGroundAbsorbed;
@@ -1053,14 +1063,14 @@ __global__ void k_ground(DevScene s, agb_frame_data f, WaveParams wp, WaveBuffer
                 }
             }
         }
-        uint32_t slotNext = warpAppend(wb.counters + kCounterStride + CNT_RAYS, reflectRay);
+        uint32_t slotNext = warpAppend(wb.counters + (bounce + 1) * kCounterStride + CNT_RAYS, reflectRay);
         if (reflectRay)
         {
-            wb.rayOrg[1][slotNext]  = make_float4(hitPos.x, hitPos.y, hitPos.z, kRayTMin);
-            wb.rayDir[1][slotNext]  = make_float4(nextD.x, nextD.y, nextD.z, __int_as_float(0x7f800000));
-            wb.rayPath[1][slotNext] = p;
+            wb.rayOrg[cur ^ 1][slotNext]  = make_float4(hitPos.x, hitPos.y, hitPos.z, kRayTMin);
+            wb.rayDir[cur ^ 1][slotNext]  = make_float4(nextD.x, nextD.y, nextD.z, __int_as_float(0x7f800000));
+            wb.rayPath[cur ^ 1][slotNext] = p;
         }
-        uint32_t slotShadow = warpAppend(wb.counters + shadowBlock * kCounterStride + CNT_SHADOW, shadowRay);
+        uint32_t slotShadow = warpAppend(wb.counters + bounce * kCounterStride + CNT_GROUND_SHADOW, shadowRay);
         if (shadowRay)
         {
             wb.shOrg[p]                           = make_float4(hitPos.x, hitPos.y, hitPos.z, 0.f);
@@ -1071,23 +1081,25 @@ __global__ void k_ground(DevScene s, agb_frame_data f, WaveParams wp, WaveBuffer
     }
 }
 
-// The matte shadow of the ground plane (GroundPlane.slang:171-182): a camera ray whose opaque
-// shadow ray was blocked has its contribution scaled by lerp(1, shadow colour, luminance(1 - 0) x
-// shadow opacity); an unblocked one by lerp(1, shadow colour, 0) = 1.
-__global__ void k_ground_shadow(DevScene s, WaveBuffers wb, int shadowBlock)
+// The matte shadow of the ground plane (GroundPlane.slang:171-182): the waiting colour factor is
+// scaled by lerp(1, shadow colour, luminance(1 - 0) x shadow opacity) when the opaque shadow ray
+// was blocked (by lerp(1, shadow colour, 0) = 1 otherwise), then multiplies the contribution, in
+// the reference's order (contribution x (colour x blend)).
+__global__ void k_ground_shadow(DevScene s, WaveBuffers wb, int bounce)
 {
     const DevGroundPlane& g = s.ground;
-    uint32_t n      = wb.counters[shadowBlock * kCounterStride + CNT_SHADOW];
+    uint32_t n      = wb.counters[bounce * kCounterStride + CNT_GROUND_SHADOW];
     uint32_t stride = gridDim.x * blockDim.x;
     v3 blend = lerp3(splat(1.f), ld3(g.shadowColor), luminance(splat(1.f) - splat(0.f)) * g.shadowOpacity);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
     {
         uint32_t p = wb.shTag[i] >> 3;
+        float4 f4  = wb.pendSlot[size_t(p) * kMaxShadowSlots];
+        v3 color   = v3{ f4.x, f4.y, f4.z };
         if (wb.occluded[p] & 1u)
-        {
-            float4 c4     = wb.contrib[p];
-            wb.contrib[p] = make_float4(c4.x * blend.x, c4.y * blend.y, c4.z * blend.z, 0.f);
-        }
+            color = color * blend;
+        float4 c4     = wb.contrib[p];
+        wb.contrib[p] = make_float4(c4.x * color.x, c4.y * color.y, c4.z * color.z, 0.f);
     }
 }
 
@@ -1197,19 +1209,20 @@ void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp
             k_trace_closest<true><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, cur);
         else
             k_trace_closest<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, cur);
-        if (b == 0 && s.ground.enabled)
+        if (s.ground.enabled)
         {
-            // Ground plane before the camera rays are shaded; its shadow rays use the spare
-            // counter block depth + 1.
+            // Ground plane for the bounce's primary rays before they are shaded.
             mark(KC_SHADE);
-            k_ground<<<grid, 256, 0, st>>>(s, f, wp, wb, depth + 1);
+            k_ground<<<grid, 256, 0, st>>>(s, f, wp, wb, b, cur);
             mark(KC_SHADOW);
             if (wp.countTraversal)
-                k_trace_shadow<true><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, depth + 1);
+                k_trace_shadow<true><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, CNT_GROUND_SHADOW,
+                    CNT_GROUND_WORK);
             else
-                k_trace_shadow<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, depth + 1);
+                k_trace_shadow<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, CNT_GROUND_SHADOW,
+                    CNT_GROUND_WORK);
             mark(KC_SHADE);
-            k_ground_shadow<<<grid, 256, 0, st>>>(s, wb, depth + 1);
+            k_ground_shadow<<<grid, 256, 0, st>>>(s, wb, b);
             launches += 3;
         }
         mark(KC_SHADE);
@@ -1227,9 +1240,9 @@ void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp
                 k_trace_shadow_transparent<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b);
         }
         else if (wp.countTraversal)
-            k_trace_shadow<true><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b);
+            k_trace_shadow<true><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, CNT_SHADOW, CNT_SHADOW_WORK);
         else
-            k_trace_shadow<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b);
+            k_trace_shadow<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, CNT_SHADOW, CNT_SHADOW_WORK);
         mark(KC_RESOLVE);
         k_resolve<<<grid, 256, 0, st>>>(f, wb, b);
         launches += 6;

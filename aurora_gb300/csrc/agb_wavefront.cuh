@@ -23,6 +23,8 @@ enum : int
     CNT_CLOSEST_WORK  = 3, // persistent traversal work counter (closest-hit rays)
     CNT_SHADOW_WORK   = 4, // persistent traversal work counter (shadow rays)
     CNT_SCATTER       = 5, // shading points handed from k_shade to k_shade_scatter
+    CNT_GROUND_SHADOW = 6, // ground-plane matte-shadow rays of the bounce's primary rays
+    CNT_GROUND_WORK   = 7, // persistent traversal work counter (ground-plane shadow rays)
     kCounterStride    = 8
 };
 

@@ -52,6 +52,8 @@ def parse_args():
     p.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     p.add_argument("--no-time-to-error", action="store_true", help="skip the time-to-relMSE measurement")
     p.add_argument("--serve-requests", type=int, default=160)
+    p.add_argument("--ground-plane", action="store_true",
+                   help="add a ground plane (the reference's defaults) under the scene (overhead runs)")
     p.add_argument("--max-paths", type=int, default=0,
                    help="paths in flight per wave (0: the library's default)")
     return p.parse_args()
@@ -253,7 +255,9 @@ def workload(s, name):
             "trace_depth": int(s.frame["trace_depth"]), "unique_triangles": s.unique_triangles,
             "instances": len(s.instances), "instanced_triangles": s.triangle_count,
             "seed": 0, "accumulation": "FP32 running mean + Kahan-compensated sum",
-            "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas"}
+            "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas",
+            **({"ground_plane": "enabled (defaults) at the scene's lower bound"}
+               if getattr(s, "ground_plane", None) is not None else {})}
 
 
 class ClockSampler:
@@ -393,6 +397,8 @@ def main():
     from aurora_gb300 import _abi, api, build
     build.build()
     s = make_scene(args.config, args.res, args.spp)
+    if args.ground_plane:
+        s.ground_plane = _abi.ground_plane(position=(0.0, float(s.bounds()[0][1]), 0.0))
     stream = torch.cuda.Stream()
     r = api.Renderer(local, stream=stream.cuda_stream)
     r.upload(s)

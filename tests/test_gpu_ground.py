@@ -120,3 +120,25 @@ def test_ground_plane_rejects_zero_normal(agb):
         code = _abi.library().agb_ground_plane_set(r.ctx, _abi.ptr(g))
         assert code == _abi.ERR_INVALID_ARG
         assert _abi.library().agb_ground_plane_set(r.ctx, None) == 0
+
+
+def test_ground_plane_with_transparent_shadows_and_small_waves(agb, oracle):
+    """The plane's matte shadow ray is always opaque (shadeMatteShadow is called with true), also
+    when the frame traces transparent shadows; and splitting the frame into waves of a few paths
+    (each wave with its own counter blocks) changes no pixel."""
+    from aurora_gb300 import api
+    s = ground_scene(reflection_opacity=0.35, shadow_opacity=0.9)
+    s.materials["opacity"][0] = (0.5, 0.3, 0.8)
+    f = np.asarray(s.frame).copy()
+    f["is_force_opaque_shadows_enabled"] = 0
+    s.frame = f
+    g = render_gpu(s, 4)
+    o = oracle.OracleScene(s).render(0, 4)
+    print("transparent shadows + ground plane: identical pixels",
+          np.mean(np.all(g["mean"] == o["mean"], axis=2)))
+    np.testing.assert_array_equal(g["mean"], o["mean"])
+    with api.Renderer() as r:
+        r.upload(s)
+        r.render(0, 4, max_paths=s.width * s.height // 3)
+        small = r.read(_abi.ACCUM_RUNNING_MEAN)
+    np.testing.assert_array_equal(small, g["mean"])
