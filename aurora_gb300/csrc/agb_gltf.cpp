@@ -542,8 +542,16 @@ struct Model
         const std::vector<Json>& accs = doc.arr("accessors");
         if (accessor < 0 || size_t(accessor) >= accs.size())
             return false;
-        acc       = &accs[size_t(accessor)];
-        count     = size_t(acc->num("count", 0));
+        acc = &accs[size_t(accessor)];
+        // Sizes as JSON numbers: refuse negative or absurd values before converting them.
+        auto size = [](double v, size_t& out) {
+            if (!(v >= 0.0 && v <= 4294967295.0))
+                return false;
+            out = size_t(v);
+            return true;
+        };
+        if (!size(acc->num("count", 0), count))
+            return false;
         int bvIdx = acc->integer("bufferView", -1);
         const std::vector<Json>& views = doc.arr("bufferViews");
         if (bvIdx < 0 || size_t(bvIdx) >= views.size())
@@ -553,9 +561,10 @@ struct Model
         if (bIdx < 0 || size_t(bIdx) >= buffers.size())
             return false;
         const std::string& buf = buffers[size_t(bIdx)];
-        size_t bvOffset = size_t(bv.num("byteOffset", 0)), bvLength = size_t(bv.num("byteLength", 0));
-        size_t accOffset = size_t(acc->num("byteOffset", 0));
-        stride           = size_t(bv.num("byteStride", 0));
+        size_t bvOffset, bvLength, accOffset;
+        if (!size(bv.num("byteOffset", 0), bvOffset) || !size(bv.num("byteLength", 0), bvLength) ||
+            !size(acc->num("byteOffset", 0), accOffset) || !size(bv.num("byteStride", 0), stride))
+            return false;
         if (!stride)
             stride = size_t(elementSize);
         if (bvOffset + bvLength > buf.size() || bvOffset + bvLength < bvOffset)
@@ -733,8 +742,8 @@ bool loadModel(const std::string& path, Model& m, std::string& error)
             error = "cannot read buffer " + uri;
             return false;
         }
-        size_t length = size_t(b.num("byteLength", double(bytes.size())));
-        if (bytes.size() < length)
+        double lengthValue = b.num("byteLength", double(bytes.size()));
+        if (!(lengthValue >= 0.0) || lengthValue > double(bytes.size()))
         {
             error = "buffer " + uri + " is shorter than its byteLength";
             return false;
