@@ -387,6 +387,11 @@ bool decodePNG(const std::string& data, std::vector<uint8_t>& rgba, int& width, 
     const size_t bitsPerPixel = size_t(channels) * size_t(depth);
     const size_t stride       = (size_t(w) * bitsPerPixel + 7) / 8;
     const size_t bpp          = (bitsPerPixel + 7) / 8; // filter byte distance
+    if ((stride + 1) * size_t(h) > (size_t(1) << 30))
+    {
+        error = "PNG image too large (more than 1 GiB of scanlines)";
+        return false;
+    }
     std::vector<uint8_t> raw;
     raw.reserve((stride + 1) * h);
     if (!zlibInflate(idat.data(), idat.size(), raw, (stride + 1) * h, error))
