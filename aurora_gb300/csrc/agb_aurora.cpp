@@ -214,6 +214,20 @@ public:
         else
             rgba32.assign(size_t(w) * h * 4, 0.f);
     }
+    IBufferPtr asReadable(size_t& stride) override
+    {
+        struct Copy : IBuffer
+        {
+            std::vector<uint8_t> bytes;
+            const void* data() override { return bytes.data(); }
+        };
+        auto c           = std::make_shared<Copy>();
+        const void* src  = data(stride, false);
+        size_t n         = stride * size_t(h);
+        c->bytes.assign(static_cast<const uint8_t*>(src), static_cast<const uint8_t*>(src) + n);
+        return c;
+    }
+    IBufferPtr asShared() override { return nullptr; }
     const void* data(size_t& stride, bool) override
     {
         stride = size_t(w) * (format == ImageFormat::Integer_RGBA ? 4 : 16);
@@ -1133,6 +1147,11 @@ public:
             "render");
     }
     void waitForTask() override { check(agb_wait(ctx), "waitForTask"); }
+    const std::vector<std::string>& builtInMaterials() override
+    {
+        static const std::vector<std::string> kNone;
+        return kNone;
+    }
 };
 
 } // namespace

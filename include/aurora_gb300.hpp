@@ -212,8 +212,21 @@ using IGroundPlanePtr = std::shared_ptr<IGroundPlane>;
 class IRenderBuffer
 {
 public:
+    // A readable (or shareable) buffer held for as long as the pointer lives (Aurora.h:720-733).
+    class IBuffer
+    {
+    public:
+        virtual const void* data() = 0;
+        virtual const void* handle() { return nullptr; }
+        virtual ~IBuffer() = default;
+    };
+    using IBufferPtr = std::shared_ptr<IBuffer>;
     // The pixels of the last render; stride receives the bytes per row.
     virtual const void* data(size_t& stride, bool removePadding = false) = 0;
+    // The pixels of the last render in a buffer of their own (a copy: later renders leave it).
+    virtual IBufferPtr asReadable(size_t& stride) = 0;
+    // Shareable GPU memory of the target: none here (post-processing writes host memory), null.
+    virtual IBufferPtr asShared() = 0;
     virtual int width() const                                           = 0;
     virtual int height() const                                          = 0;
     virtual ~IRenderBuffer() = default;
@@ -281,6 +294,9 @@ public:
         float lensRadius = 0.0f)                                                      = 0;
     virtual void render(uint32_t sampleStart = 0, uint32_t sampleCount = 1)           = 0;
     virtual void waitForTask()                                                        = 0;
+    // Built-in material types beyond the default Standard Surface: none, as in the HGI
+    // backend (HGIRenderer.cpp:622-627).
+    virtual const std::vector<std::string>& builtInMaterials()                       = 0;
     virtual ~IRenderer() = default;
 };
 using IRendererPtr = std::shared_ptr<IRenderer>;

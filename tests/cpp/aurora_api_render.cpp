@@ -304,6 +304,13 @@ int main(int argc, char** argv)
             throw Error("attributeUpdateComplete was not called for every mesh");
         size_t stride = 0;
         const float* px = static_cast<const float*>(target->data(stride));
+        // asReadable: a copy of the same pixels; asShared: no shareable GPU image here.
+        size_t readStride = 0;
+        IRenderBuffer::IBufferPtr readable = target->asReadable(readStride);
+        if (!readable || readStride != stride || std::memcmp(readable->data(), px, stride * height) != 0)
+            throw Error("asReadable differs from data()");
+        if (target->asShared() || !renderer->builtInMaterials().empty())
+            throw Error("unexpected shared buffer or built-in materials");
         FILE* o = std::fopen(argv[2], "wb");
         if (!o)
             throw Error("cannot write output");
