@@ -431,14 +431,19 @@ public:
             // set afterwards override them.
             Properties fromDoc;
             std::string warnings;
+            std::vector<MaterialXImage> imgs;
             bool ok = type == Names::MaterialTypes::kMaterialX
-                ? materialXToProperties(document, fromDoc, warnings)
-                : materialXFileToProperties(document, fromDoc, warnings);
+                ? materialXToProperties(document, "", fromDoc, warnings, imgs)
+                : materialXFileToProperties(document, fromDoc, warnings, &imgs);
             if (!warnings.empty())
                 logError("setMaterialType " + p + ": " + warnings);
             if (ok)
+            {
+                for (const MaterialXImage& im : imgs)
+                    setImageFromFilePath(im.image, im.file, im.linearize, false);
                 for (auto& kv : fromDoc)
                     m[kv.first] = kv.second;
+            }
         }
         else if (type != Names::MaterialTypes::kBuiltIn)
             logError("setMaterialType: unknown material type " + type + "; " + p +

@@ -885,8 +885,17 @@ void loadNode(Model& m, int nodeIdx, const mat4& parent, SceneContents& contents
                 {
                     SceneMaterialData md;
                     md.path = path;
-                    if (materialXFileToProperties(file, md.properties, m.warnings))
+                    std::vector<MaterialXImage> imgs;
+                    if (materialXFileToProperties(file, md.properties, m.warnings, &imgs))
                     {
+                        for (const MaterialXImage& im : imgs)
+                        {
+                            bool have = false;
+                            for (const SceneImageData& d : contents.images)
+                                have = have || d.path == im.image;
+                            if (!have)
+                                contents.images.push_back(SceneImageData{ im.image, im.file, im.linearize });
+                        }
                         contents.materials.push_back(md);
                         inst.material = path;
                     }

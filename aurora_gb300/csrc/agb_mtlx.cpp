@@ -225,9 +225,67 @@ const XmlElement* findChild(const XmlElement& root, const std::string& elementNa
     return nullptr;
 }
 
+// The texture slots a standard_surface input can take from an image node (MaterialBase.cpp:91-95).
+const char* textureSlot(const std::string& input)
+{
+    if (input == "base_color")
+        return "base_color_image";
+    if (input == "specular_roughness")
+        return "specular_roughness_image";
+    if (input == "emission_color")
+        return "emission_color_image";
+    if (input == "opacity")
+        return "opacity_image";
+    return nullptr;
+}
+
+const XmlElement* findNamed(const XmlElement& scope, const std::string& name)
+{
+    for (auto& c : scope.children)
+        if (c->attr("name") == name)
+            return c.get();
+    return nullptr;
+}
+
+// The image or tiledimage node an input is connected to: directly (nodename) or through a node
+// graph's output; null otherwise.
+const XmlElement* connectedImage(const XmlElement& root, const XmlElement& in)
+{
+    const XmlElement* node = nullptr;
+    if (in.has("nodegraph"))
+    {
+        const XmlElement* graph = findNamed(root, in.attr("nodegraph"));
+        if (!graph)
+            return nullptr;
+        const XmlElement* out = nullptr;
+        for (auto& c : graph->children)
+            if (c->name == "output" && (!in.has("output") || c->attr("name") == in.attr("output")))
+            {
+                out = c.get();
+                break;
+            }
+        if (!out || !out->has("nodename"))
+            return nullptr;
+        node = findNamed(*graph, out->attr("nodename"));
+    }
+    else if (in.has("nodename"))
+        node = findNamed(root, in.attr("nodename"));
+    return node && (node->name == "image" || node->name == "tiledimage") ? node : nullptr;
+}
+
 } // namespace
 
 bool materialXToProperties(const std::string& document, Properties& properties, std::string& warnings)
+{
+    std::vector<MaterialXImage> images;
+    bool ok = materialXToProperties(document, "", properties, warnings, images);
+    if (!images.empty())
+        warnings += "MaterialX image files are not loaded without a scene\n";
+    return ok;
+}
+
+bool materialXToProperties(const std::string& document, const std::string& baseDirectory,
+    Properties& properties, std::string& warnings, std::vector<MaterialXImage>& images)
 {
     XmlElement root;
     std::string error;
@@ -280,6 +338,40 @@ bool materialXToProperties(const std::string& document, Properties& properties, 
         const std::string n = in->attr("name"), type = in->attr("type");
         if (in->has("nodename") || in->has("nodegraph") || in->has("output") || in->has("interfacename"))
         {
+            // An image (or tiledimage) node feeding a texturable input becomes that input's
+            // texture: the file (sRGB-decoded when its colour space is srgb_texture), with a
+            // tiledimage's uvtiling / uvoffset as the texture scale / offset.
+            const XmlElement* img = connectedImage(root, *in);
+            const char* slot      = textureSlot(n);
+            const XmlElement* file = nullptr;
+            if (img)
+                for (auto& c : img->children)
+                    if (c->name == "input" && c->attr("name") == "file" && c->has("value"))
+                        file = c.get();
+            if (slot && file)
+            {
+                std::string path = file->attr("value");
+                if (!path.empty() && path[0] != '/' && !baseDirectory.empty())
+                    path = baseDirectory + path;
+                const std::string space = file->has("colorspace") ? file->attr("colorspace")
+                    : img->has("colorspace")                       ? img->attr("colorspace")
+                                                                   : docSpace;
+                const bool linearize = space == "srgb_texture";
+                const Path image     = "MaterialXImage/" + path + ":linearize:" + (linearize ? "1" : "0");
+                images.push_back(MaterialXImage{ slot, image, path, linearize });
+                properties[slot] = image;
+                for (auto& c : img->children)
+                {
+                    if (c->name != "input" || !c->has("value"))
+                        continue;
+                    std::vector<float> f = numbers(c->attr("value"));
+                    if (c->attr("name") == "uvtiling" && f.size() == 2)
+                        properties[std::string(slot) + "_scale"] = vec2{ f[0], f[1] };
+                    else if (c->attr("name") == "uvoffset" && f.size() == 2)
+                        properties[std::string(slot) + "_offset"] = vec2{ f[0], f[1] };
+                }
+                continue;
+            }
             warnings += "MaterialX input '" + n + "' is connected to a node graph, which is not supported; " +
                 "its default is used\n";
             continue;
@@ -307,7 +399,8 @@ bool materialXToProperties(const std::string& document, Properties& properties, 
     return true;
 }
 
-bool materialXFileToProperties(const std::string& path, Properties& properties, std::string& warnings)
+bool materialXFileToProperties(const std::string& path, Properties& properties, std::string& warnings,
+    std::vector<MaterialXImage>* images)
 {
     std::ifstream f(path, std::ios::binary);
     if (!f)
@@ -317,7 +410,15 @@ bool materialXFileToProperties(const std::string& path, Properties& properties, 
     }
     std::ostringstream s;
     s << f.rdbuf();
-    return materialXToProperties(s.str(), properties, warnings);
+    // Image files are found beside the document (the reference prefixes relative texture paths
+    // with the document's folder, glTFLoader.cpp:310-327).
+    size_t k = path.find_last_of("/\\");
+    std::string dir = k == std::string::npos ? std::string() : path.substr(0, k + 1);
+    std::vector<MaterialXImage> local;
+    bool ok = materialXToProperties(s.str(), dir, properties, warnings, images ? *images : local);
+    if (!images && !local.empty())
+        warnings += "MaterialX image files are not loaded without a scene\n";
+    return ok;
 }
 
 } // namespace agb_aurora

@@ -140,10 +140,25 @@ AGB_CPP_API bool saveglTFFile(const std::string& filePath, const SceneContents& 
 // document whose surface shader -- the surfaceshader input of its first surfacematerial, else its
 // first standard_surface node -- is a standard_surface becomes the built-in material's
 // properties, one per constant input (float, integer, boolean, color3 / vector3, the rgb of
-// color4) under the input's name.  Inputs connected to node graphs keep their defaults and other
-// surface shaders are refused, each with a warning.
+// color4) under the input's name.  An image or tiledimage node (directly or as a node graph's
+// output) feeding base_color, specular_roughness, emission_color or opacity becomes that
+// texture: `<input>_image` = an image path for the file (relative paths against baseDirectory),
+// listed in `images` with linearize for the srgb_texture colour space, uvtiling / uvoffset as the texture
+// scale / offset.  Other connected inputs keep their defaults and other surface shaders are
+// refused, each with a warning.
+struct MaterialXImage
+{
+    std::string property; // e.g. base_color_image
+    Path image;           // the image path the property names: MaterialXImage/<file>:linearize:<0|1>
+    std::string file;
+    bool linearize = false;
+};
+AGB_CPP_API bool materialXToProperties(const std::string& document, const std::string& baseDirectory,
+    Properties& properties, std::string& warnings, std::vector<MaterialXImage>& images);
+// Without a scene to load image files into: connected images are reported.
 AGB_CPP_API bool materialXToProperties(const std::string& document, Properties& properties, std::string& warnings);
-AGB_CPP_API bool materialXFileToProperties(const std::string& path, Properties& properties, std::string& warnings);
+AGB_CPP_API bool materialXFileToProperties(const std::string& path, Properties& properties, std::string& warnings,
+    std::vector<MaterialXImage>* images = nullptr);
 
 // Angle-weighted smooth vertex normals (Foundation/Source/Geometry.cpp:29-99).
 AGB_CPP_API void calculateNormals(size_t vertexCount, const float* positions, size_t triangleCount,

@@ -98,9 +98,22 @@ int main(int argc, char** argv)
     {
         Properties props;
         std::string warnings;
-        bool ok = materialXFileToProperties(argv[2], props, warnings);
+        std::vector<MaterialXImage> images;
+        bool ok = materialXFileToProperties(argv[2], props, warnings, &images);
         std::printf("{\"ok\":%s,\"warnings\":", ok ? "true" : "false");
         printString(warnings);
+        std::printf(",\"images\":[");
+        for (size_t i = 0; i < images.size(); i++)
+        {
+            std::printf("%s{\"property\":", i ? "," : "");
+            printString(images[i].property);
+            std::printf(",\"image\":");
+            printString(images[i].image);
+            std::printf(",\"file\":");
+            printString(images[i].file);
+            std::printf(",\"linearize\":%s}", images[i].linearize ? "true" : "false");
+        }
+        std::printf("]");
         std::printf(",\"properties\":{");
         bool first = true;
         for (auto& kv : props)

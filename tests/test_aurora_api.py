@@ -37,13 +37,20 @@ def test_cpp_client_builds_and_links():
     assert os.access(build_client(), os.X_OK)
 
 
-def materialx_document(mat, keys, name):
+def materialx_document(mat, keys, name, textures=()):
     """The material as a MaterialX standard_surface with one constant input per property (values
-    printed with 9 significant digits, so each float reads back exactly)."""
+    printed with 9 significant digits, so each float reads back exactly); `textures`: (input,
+    PNG file) pairs wired through a node graph's tiledimage with the material's texture scale and
+    offset."""
     lines = ['<?xml version="1.0"?>', '<materialx version="1.38" colorspace="lin_rec709">',
-             f'  <!-- {name}: constants only -->',
+             f'  <!-- {name} -->',
              f'  <standard_surface name="SR_{name}" type="surfaceshader">']
+    wired = {inp for inp, _ in textures}
+    for inp, _ in textures:
+        lines.append(f'    <input name="{inp}" type="color3" nodegraph="NG_{name}" output="out_{inp}" />')
     for k in keys:
+        if k in wired:
+            continue
         v = mat[k]
         if k == "thin_walled":
             lines.append(f'    <input name="{k}" type="boolean" value="{"true" if int(v) else "false"}" />')
@@ -52,8 +59,20 @@ def materialx_document(mat, keys, name):
                          ", ".join("%.9g" % np.float32(x) for x in v) + '" />')
         else:
             lines.append(f'    <input name="{k}" type="float" value="{"%.9g" % np.float32(v)}" />')
-    lines += ['  </standard_surface>',
-              f'  <surfacematerial name="M_{name}" type="material">',
+    lines.append('  </standard_surface>')
+    if textures:
+        lines.append(f'  <nodegraph name="NG_{name}">')
+        for inp, file in textures:
+            sc = ", ".join("%.9g" % np.float32(x) for x in mat[inp + "_image_scale"])
+            of = ", ".join("%.9g" % np.float32(x) for x in mat[inp + "_image_offset"])
+            lines += [f'    <tiledimage name="img_{inp}" type="color3">',
+                      f'      <input name="file" type="filename" value="{file}" colorspace="lin_rec709" />',
+                      f'      <input name="uvtiling" type="vector2" value="{sc}" />',
+                      f'      <input name="uvoffset" type="vector2" value="{of}" />',
+                      '    </tiledimage>',
+                      f'    <output name="out_{inp}" type="color3" nodename="img_{inp}" />']
+        lines.append('  </nodegraph>')
+    lines += [f'  <surfacematerial name="M_{name}" type="material">',
               f'    <input name="surfaceshader" type="surfaceshader" nodename="SR_{name}" />',
               '  </surfacematerial>', '</materialx>']
     return "\n".join(lines)
@@ -109,7 +128,17 @@ def write_scene(path, s, view, proj, lights, depth, mtlx=False):
     for mi, mat in enumerate(s.materials):
         props = list(scenes._DEFAULTS.keys())
         if mtlx:
-            doc = materialx_document(mat, props, f"m{mi}").encode()
+            tex = []
+            if textured:
+                from test_loaders import png_bytes
+                for slot, name in TEX_NAMES.items():
+                    img = int(s.textures["image"][mi, slot])
+                    if img >= 0:
+                        png = os.path.join(os.path.dirname(path), f"tex{img}.png")
+                        if not os.path.exists(png):
+                            open(png, "wb").write(png_bytes(np.asarray(s.images[img]["pixels"]), 6, 8, [0]))
+                        tex.append((name[:-len("_image")], png))
+            doc = materialx_document(mat, props, f"m{mi}", tex).encode()
             b += struct.pack("<II", 0xFFFFFFFF, len(doc)) + doc
             continue
         tex = []
@@ -208,10 +237,12 @@ def test_cpp_interface_render_matches_c_abi(agb, oracle, ground, mtlx):
 
 
 @pytest.mark.gpu
-def test_cpp_interface_textures_and_layers_match_c_abi(agb, oracle):
+@pytest.mark.parametrize("mtlx", [False, True])
+def test_cpp_interface_textures_and_layers_match_c_abi(agb, oracle, mtlx):
     """Material textures (image paths, a transformed base-colour texture), samplers and material
     layers (layer_materials / layer_geometry, the layer's UVs from a geometry of its own) through
-    the C++ interface, against the same scene through the C ABI."""
+    the C++ interface, against the same scene through the C ABI; with `mtlx`, the materials are
+    MaterialX documents whose textures are PNG files behind node-graph tiledimages."""
     from aurora_gb300 import _abi, api, scenes
     exe = build_client()
     s = scenes.config_layered(width=64, height=48, spp=4, trace_depth=4, blas=2, instances=6,
@@ -221,14 +252,15 @@ def test_cpp_interface_textures_and_layers_match_c_abi(agb, oracle):
     s.textures["image"][0, _abi.TEX_BASE_COLOR] = color_img
     s.materials["base_color_image_scale"][0] = (2.0, 0.5)
     s.materials["base_color_image_offset"][0] = (0.1, 0.2)
-    s.materials["base_color_image_pivot"][0] = (0.5, 0.5)
-    s.materials["base_color_image_rotation"][0] = 0.3
+    if not mtlx:  # a tiledimage has no pivot or rotation
+        s.materials["base_color_image_pivot"][0] = (0.5, 0.5)
+        s.materials["base_color_image_rotation"][0] = 0.3
     view = np.asarray(scenes.look_at((0.0, 15.0, 60.0), (0.0, 0.0, 0.0)), np.float32)
     proj = np.asarray(scenes.perspective(45.0, s.width / s.height), np.float32)
     depth = 4
     with tempfile.TemporaryDirectory() as tmp:
         scene_file, out_file = os.path.join(tmp, "scene.bin"), os.path.join(tmp, "out.bin")
-        write_scene(scene_file, s, view, proj, [], depth)
+        write_scene(scene_file, s, view, proj, [], depth, mtlx=mtlx)
         subprocess.check_call([exe, scene_file, out_file])
         raw = open(out_file, "rb").read()
     w, h = struct.unpack("<2I", raw[:8])

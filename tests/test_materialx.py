@@ -1,6 +1,7 @@
-"""MaterialX documents with a standard_surface of constant inputs (include/aurora_gb300_loaders.hpp,
-materialXToProperties) on the CPU: the properties they give, what is refused with a warning, and
-the glTF AURORA_materials_materialX node extension that names such a file."""
+"""MaterialX documents with a standard_surface of constant inputs and image textures
+(include/aurora_gb300_loaders.hpp, materialXToProperties) on the CPU: the properties they give,
+what is refused with a warning, and the glTF AURORA_materials_materialX node extension that names
+such a file."""
 import json
 import os
 import tempfile
@@ -98,3 +99,44 @@ def test_gltf_materialx_extension():
         out = run("gltf", path)
         assert out["ok"] and "cannot read MaterialX file" in out["warnings"]
         assert out["instances"][0]["material"].endswith(":gltfMat:1")
+
+
+def test_image_nodes_become_textures():
+    """base_color through a node graph's tiledimage (sRGB file, tiling and offset), opacity
+    straight from an image node; an image feeding metalness (no texture slot) is refused."""
+    doc = """<?xml version="1.0"?>
+<materialx version="1.38" colorspace="lin_rec709">
+  <nodegraph name="NG">
+    <tiledimage name="wood" type="color3">
+      <input name="file" type="filename" value="textures/wood.png" colorspace="srgb_texture" />
+      <input name="uvtiling" type="vector2" value="4, 2" />
+      <input name="uvoffset" type="vector2" value="0.25, 0.5" />
+    </tiledimage>
+    <output name="out" type="color3" nodename="wood" />
+  </nodegraph>
+  <image name="mask" type="color3">
+    <input name="file" type="filename" value="/abs/mask.png" />
+  </image>
+  <standard_surface name="S" type="surfaceshader">
+    <input name="base_color" type="color3" nodegraph="NG" output="out" />
+    <input name="opacity" type="color3" nodename="mask" />
+    <input name="metalness" type="float" nodename="mask" />
+    <input name="specular_roughness" type="float" value="0.5" />
+  </standard_surface>
+</materialx>
+"""
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "m.mtlx")
+        open(path, "w").write(doc)
+        out = run("mtlx", path)
+    assert out["ok"], out["warnings"]
+    wood = os.path.join(tmp, "textures/wood.png")
+    p = out["properties"]
+    assert p["base_color_image"] == f"MaterialXImage/{wood}:linearize:1"
+    assert p["base_color_image_scale"] == [4.0, 2.0] and p["base_color_image_offset"] == [0.25, 0.5]
+    assert p["opacity_image"] == "MaterialXImage//abs/mask.png:linearize:0"
+    assert "metalness" not in p and "'metalness' is connected" in out["warnings"]
+    assert p["specular_roughness"] == 0.5
+    assert out["images"] == [
+        {"property": "base_color_image", "image": p["base_color_image"], "file": wood, "linearize": True},
+        {"property": "opacity_image", "image": p["opacity_image"], "file": "/abs/mask.png", "linearize": False}]
