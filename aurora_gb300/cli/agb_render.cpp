@@ -13,7 +13,10 @@
 //          [--eye x,y,z] [--target x,y,z] [--up x,y,z] [--fov degrees] [--env file.hdr]
 //          [--lightDir x,y,z] [--lightColor r,g,b] [--lightIntensity v] [--trace-depth N]
 //          [--russian_roulette 0|1] [--gamma_correction 0|1] [--ground_shadow 0|1]
-//          [--ground_reflection 0|1] [--camera N]
+//          [--ground_reflection 0|1] [--camera N] [--mtlx file.mtlx] [--loadMtlXForObj 1]
+// --mtlx applies a MaterialX document to every instance (Plasma::applyMaterialXFile,
+// Plasma.cpp:1674-1703); --loadMtlXForObj takes <material>.mtlx beside an OBJ file for its OBJ
+// materials (Plasma.cpp:600-605).
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -121,7 +124,7 @@ int main(int argc, char** argv)
             "       [--eye x,y,z] [--target x,y,z] [--up x,y,z] [--fov degrees] [--env file.hdr]\n"
             "       [--lightDir x,y,z] [--lightColor r,g,b] [--lightIntensity v] [--trace-depth N]\n"
             "       [--russian_roulette 0|1] [--gamma_correction 0|1] [--ground_shadow 0|1]\n"
-            "       [--ground_reflection 0|1] [--camera N]\n");
+            "       [--ground_reflection 0|1] [--camera N] [--mtlx file.mtlx] [--loadMtlXForObj 1]\n");
         return 2;
     }
     try
@@ -145,11 +148,20 @@ int main(int argc, char** argv)
             throw Error("no GB300 renderer available");
         IScenePtr scene = renderer->createScene();
         SceneContents contents;
+        if (a.count("loadMtlXForObj"))
+            loadMaterialXForOBJMaterials(std::atoi(a["loadMtlXForObj"].c_str()) != 0);
         const bool gltf = endsWith(scenePath, ".gltf") || endsWith(scenePath, ".glb");
         if (!(gltf ? loadglTFFile(scene.get(), scenePath, contents) : loadOBJFile(scene.get(), scenePath, contents)))
             throw Error("cannot load " + scenePath + (contents.warnings.empty() ? "" : ": " + contents.warnings));
         if (!contents.warnings.empty())
             std::fprintf(stderr, "%s", contents.warnings.c_str());
+        if (a.count("mtlx"))
+        {
+            const Path material = "PlasmaMaterialX:" + a["mtlx"];
+            scene->setMaterialType(material, Names::MaterialTypes::kMaterialXPath, a["mtlx"]);
+            for (const SceneInstanceData& inst : contents.instances)
+                scene->setInstanceProperties(inst.instance, { { Names::InstanceProperties::kMaterial, material } });
+        }
 
         vec3 eye, target;
         fitCamera(contents.boundsMin, contents.boundsMax, { 0.f, 0.f, -1.f }, fovY, aspect, eye, target);

@@ -338,6 +338,13 @@ void calculateNormals(size_t vertexCount, const float* positions, size_t triangl
     }
 }
 
+namespace
+{
+bool gMaterialXForOBJ = false;
+}
+
+void loadMaterialXForOBJMaterials(bool enabled) { gMaterialXForOBJ = enabled; }
+
 bool translateOBJ(const ObjData& obj, const std::string& filePath, SceneContents& contents)
 {
     contents.reset();
@@ -345,6 +352,24 @@ bool translateOBJ(const ObjData& obj, const std::string& filePath, SceneContents
     int mtlCount = 0;
     for (const ObjMaterial& m : obj.materials)
     {
+        if (gMaterialXForOBJ && !m.name.empty())
+        {
+            const std::string mtlx = directoryOf(filePath) + m.name + ".mtlx";
+            if (std::ifstream(mtlx).good())
+            {
+                SceneMaterialData md;
+                md.path = filePath + "-" + m.name + ":MaterialX-" + std::to_string(mtlCount++);
+                std::vector<MaterialXImage> imgs;
+                if (materialXFileToProperties(mtlx, md.properties, contents.warnings, &imgs))
+                {
+                    for (const MaterialXImage& im : imgs)
+                        contents.images.push_back(SceneImageData{ im.image, im.file, im.linearize });
+                    materialPaths.push_back(md.path);
+                    contents.materials.push_back(std::move(md));
+                    continue;
+                }
+            }
+        }
         // OBJLoader.cpp:155-232: Standard Surface values from the MTL record.
         vec3 baseColor         = sRGBToLinear3(m.diffuse);
         vec3 specularColor     = sRGBToLinear3(m.specular);

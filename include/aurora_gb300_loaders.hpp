@@ -111,6 +111,9 @@ struct SceneContents
 // `PlasmaImage/<file>:linearize:<0|1>` listed in contents.images, the file resolved beside the
 // OBJ file; emission is 1 when there is an emission colour image.
 AGB_CPP_API bool translateOBJ(const ObjData& obj, const std::string& filePath, SceneContents& contents);
+// With this set, an OBJ material whose name has a .mtlx file beside the OBJ file takes that
+// MaterialX document instead (OBJLoader.cpp:124-150, Plasma's --loadMtlXForObj); off by default.
+AGB_CPP_API void loadMaterialXForOBJMaterials(bool enabled);
 // loadOBJFile (OBJLoader.cpp:73-473): parse + translate + hand everything to the scene.
 AGB_CPP_API bool loadOBJFile(IScene* scene, const std::string& filePath, SceneContents& contents);
 

@@ -1,6 +1,7 @@
 // Test driver for include/aurora_gb300_loaders.hpp (no GPU needed): prints JSON.
 //   loader_tool obj <file.obj>                      parse + translate, no scene
 //   loader_tool gltf <file.gltf|file.glb>           parse + translate, no scene
+//   loader_tool objmtlx <file.obj>                  as obj, with <material>.mtlx files beside it
 //   loader_tool gltfsave <out.gltf> <in.gltf>       the input's cameras written as a glTF file
 //   loader_tool mtlx <file.mtlx>                    standard_surface constants as properties
 //   loader_tool pngread <file.png>                  decoded 8-bit RGBA
@@ -135,10 +136,11 @@ int main(int argc, char** argv)
             return 1;
         return saveglTFFile(argv[2], c) ? 0 : 1;
     }
-    if (mode == "obj" || mode == "gltf")
+    if (mode == "obj" || mode == "gltf" || mode == "objmtlx")
     {
         SceneContents c;
-        bool ok = mode == "obj" ? loadOBJFile(nullptr, argv[2], c) : loadglTFFile(nullptr, argv[2], c);
+        loadMaterialXForOBJMaterials(mode == "objmtlx");
+        bool ok = mode != "gltf" ? loadOBJFile(nullptr, argv[2], c) : loadglTFFile(nullptr, argv[2], c);
         std::printf("{\"ok\":%s,\"warnings\":", ok ? "true" : "false");
         printString(c.warnings);
         std::printf(",\"bounds\":[");

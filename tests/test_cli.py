@@ -36,12 +36,14 @@ def write_obj(path, meshes):
         "newmtl floor\nKd 0.7 0.7 0.6\nPm 0.5\nPr 0.6\nd 0.8\n")
 
 
-@pytest.mark.parametrize("ground,texture", [(False, False), (True, False), (False, True)])
-def test_cli_render_matches_c_abi(agb, oracle, ground, texture):
+@pytest.mark.parametrize("ground,texture,mtlx", [(False, False, False), (True, False, False),
+                                                 (False, True, False), (False, False, True)])
+def test_cli_render_matches_c_abi(agb, oracle, ground, texture, mtlx):
     """With `ground`, the floor quad gives way to the CLI's ground plane (--ground_shadow 1
     --ground_reflection 1: Plasma's plane at the scene's lower bound, shadow opacity 1,
     reflection opacity 0.5).  With `texture`, the floor's MTL record names a PNG (map_Kd), which
-    the C ABI side receives decoded from sRGB with the same formula."""
+    the C ABI side receives decoded from sRGB with the same formula.  With `mtlx`, --mtlx applies
+    a MaterialX standard_surface to every instance (Plasma::applyMaterialXFile)."""
     from aurora_gb300 import _abi, api, build, scenes
     build.build()
     exe = build.CLI
@@ -65,10 +67,18 @@ def test_cli_render_matches_c_abi(agb, oracle, ground, texture):
         hdr = os.path.join(tmp, "env.hdr")
         open(hdr, "wb").write(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y 16 +X 32\n" + enc.tobytes())
         out = os.path.join(tmp, "out.pfm")
+        mtlx_file = os.path.join(tmp, "gold.mtlx")
+        open(mtlx_file, "w").write(
+            '<materialx version="1.38"><standard_surface name="S" type="surfaceshader">'
+            '<input name="base_color" type="color3" value="0.944, 0.776, 0.373"/>'
+            '<input name="metalness" type="float" value="1"/>'
+            '<input name="specular_roughness" type="float" value="0.25"/>'
+            '<input name="coat" type="float" value="0.5"/></standard_surface></materialx>')
         res = subprocess.run([exe, obj, "--output", out, "--dims", "64,48", "--output_spp", "8",
                               "--eye", "0.4,3,7", "--target", "0,0.8,0", "--fov", "45", "--env", hdr,
                               "--lightDir", "0.3,-1,-0.2", "--lightIntensity", "2", "--trace-depth", "4"]
-                             + (["--ground_shadow", "1", "--ground_reflection", "1"] if ground else []),
+                             + (["--ground_shadow", "1", "--ground_reflection", "1"] if ground else [])
+                             + (["--mtlx", mtlx_file] if mtlx else []),
                              capture_output=True, text=True)
         assert res.returncode == 0, res.stderr
         mats = {k: np.array(re.search(rf"agb_render: {k}(( \S+){{16}})", res.stderr).group(1).split(),
@@ -91,6 +101,15 @@ def test_cli_render_matches_c_abi(agb, oracle, ground, texture):
                           np.reshape(inst["texcoords"], (-1, 2)), np.array(inst["indices"], np.uint32))
         s.instances.append(dict(mesh=mesh, material=names[inst["material"]],
                                 xform=np.eye(4, dtype=np.float32)[:3].reshape(-1), layers=[]))
+    if mtlx:
+        gold = len(s.materials)
+        s.materials = np.concatenate([s.materials, scenes.materials(1)])
+        s.materials["base_color"][gold] = (0.944, 0.776, 0.373)
+        s.materials["metalness"][gold] = 1.0
+        s.materials["specular_roughness"][gold] = 0.25
+        s.materials["coat"][gold] = 0.5
+        for inst in s.instances:
+            inst["material"] = gold
     if texture:
         # The C++ interface's decode of an sRGB 8-bit texture: v / 12.92 or ((v + 0.055) / 1.055)^2.4
         # in double precision, alpha / 255.

@@ -140,3 +140,19 @@ def test_image_nodes_become_textures():
     assert out["images"] == [
         {"property": "base_color_image", "image": p["base_color_image"], "file": wood, "linearize": True},
         {"property": "opacity_image", "image": p["opacity_image"], "file": "/abs/mask.png", "linearize": False}]
+
+
+def test_obj_materials_from_materialx_files():
+    """--loadMtlXForObj: an OBJ material with <name>.mtlx beside the OBJ file takes the document
+    (OBJLoader.cpp:124-150); without the option, or without the file, the MTL record is used."""
+    from test_loaders import write_scene
+    with tempfile.TemporaryDirectory() as tmp:
+        path = write_scene(tmp)
+        open(os.path.join(tmp, "red.mtlx"), "w").write(GOLD)
+        on = run("objmtlx", path)
+        off = run("obj", path)
+    red_on, glass_on = on["materials"]
+    assert red_on["path"].endswith("-red:MaterialX-0") and red_on["properties"]["metalness"] == 1.0
+    assert glass_on["path"].endswith("-glass:OBJFileMaterial-1")
+    assert off["materials"][0]["path"].endswith("-red:OBJFileMaterial-0")
+    assert on["instances"][0]["material"] == red_on["path"]
