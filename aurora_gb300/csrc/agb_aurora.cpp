@@ -331,7 +331,7 @@ public:
     {
         ImageDescriptor desc;
         int32_t handle    = -1; // environment use: nearest filtering
-        int32_t texHandle = -1; // material textures: the default sampler's bilinear filtering
+        int32_t texHandle[2] = { -1, -1 }; // material textures: nearest, bilinear filtering
     };
     struct Instance
     {
@@ -439,8 +439,14 @@ public:
                 logError("setMaterialType " + p + ": " + warnings);
             if (ok)
             {
+                // MaterialX image nodes filter linearly (their filtertype default): a sampler of
+                // the material's own.
                 for (const MaterialXImage& im : imgs)
+                {
                     setImageFromFilePath(im.image, im.file, im.linearize, false);
+                    samplers["MaterialXSampler"];
+                    m[im.property + "_sampler"] = std::string("MaterialXSampler");
+                }
                 for (auto& kv : fromDoc)
                     m[kv.first] = kv.second;
             }
@@ -550,7 +556,7 @@ public:
             for (auto& g : geometries)
                 g.second.handle = -1;
             for (auto& i : images)
-                i.second.handle = i.second.texHandle = -1;
+                i.second.handle = i.second.texHandle[0] = i.second.texHandle[1] = -1;
             ctx   = c;
             dirty = true;
         }
@@ -577,7 +583,7 @@ public:
                 t.image[k] = -1;
             for (auto& p : kv.second)
             {
-                if (applyTextureProperty(m, t, p.first, p.second, kv.first))
+                if (applyTextureProperty(m, t, p.first, p.second, kv.first, kv.second))
                     continue;
                 applyMaterialProperty(m, p.first, p.second, kv.first);
             }
@@ -771,17 +777,20 @@ public:
         return uv.size() == vertexCount * 2 ? &uv : nullptr;
     }
 
-    // A material texture: bilinear filtering (the default sampler, HGIRenderer.cpp:108-112); an
-    // 8-bit image with `linearize` set is decoded from sRGB to linear values first, as an sRGB
-    // texture format decodes it.
-    int32_t textureHandle(const Path& path)
+    // A material texture: nearest filtering with the renderer's default sampler
+    // (HGIRenderer.cpp:108-112, HgiSamplerDesc's default filters), bilinear with a sampler of the
+    // material's own (HGISampler.cpp:21-41; HGIScene.cpp:249-251, 512); an 8-bit image with
+    // `linearize` set is decoded from sRGB to linear values first, as an sRGB texture format
+    // decodes it.
+    int32_t textureHandle(const Path& path, bool bilinear)
     {
         auto it = images.find(path);
         if (it == images.end())
             throw Error("unknown image " + path);
-        Image& im = it->second;
-        if (im.texHandle >= 0)
-            return im.texHandle;
+        Image& im       = it->second;
+        int32_t& handle = im.texHandle[bilinear ? 1 : 0];
+        if (handle >= 0)
+            return handle;
         ImageData data;
         if (!im.desc.getData(data) || !data.pPixelBuffer)
             throw Error("image " + path + ": getData failed");
@@ -802,23 +811,24 @@ public:
                     }
                     d[3] = float(s8[3]) / 255.f;
                 }
-            check(agb_image_create(ctx, px.data(), w, h, AGB_FORMAT_RGBA32F, 1, &im.texHandle), "image " + path);
+            check(agb_image_create(ctx, px.data(), w, h, AGB_FORMAT_RGBA32F, bilinear ? 1 : 0, &handle),
+                "image " + path);
         }
         else
         {
             int32_t fmt = data.format == ImageFormat::Integer_RGBA ? AGB_FORMAT_RGBA8_UNORM
                 : data.format == ImageFormat::Float_RGBA           ? AGB_FORMAT_RGBA32F
                                                                    : AGB_FORMAT_RGB32F;
-            check(agb_image_create(ctx, data.pPixelBuffer, w, h, fmt, 1, &im.texHandle), "image " + path);
+            check(agb_image_create(ctx, data.pPixelBuffer, w, h, fmt, bilinear ? 1 : 0, &handle), "image " + path);
         }
         if (im.desc.updateComplete)
             im.desc.updateComplete(data);
-        return im.texHandle;
+        return handle;
     }
 
     // Texture image and sampler properties; false for any other property.
     bool applyTextureProperty(agb_material& m, agb_material_textures& t, const std::string& name,
-        const PropertyValue& v, const Path& path)
+        const PropertyValue& v, const Path& path, const Properties& all)
     {
         for (const TexField& f : kTexFields)
         {
@@ -833,7 +843,9 @@ public:
                 int32_t has = 0;
                 if (!ip->empty())
                 {
-                    t.image[f.slot] = textureHandle(*ip);
+                    const std::string* sampler = find<std::string>(all, std::string(f.name) + "_sampler");
+                    bool bilinear = sampler && !sampler->empty() && samplers.count(*sampler);
+                    t.image[f.slot] = textureHandle(*ip, bilinear);
                     has             = 1;
                 }
                 std::memcpy(reinterpret_cast<uint8_t*>(&m) + f.hasOffset, &has, 4);

@@ -252,8 +252,10 @@ public:
     // emission_color_image, each with <name>_offset / _scale / _pivot (vec2), _rotation (float)
     // and _sampler (a sampler path).
     virtual void setMaterialProperties(const Path& path, const Properties& materialProperties) = 0;
-    // Samplers (Aurora.h:922): AddressModeU / AddressModeV.  Textures here wrap (the reference's
-    // default sampler); other modes are reported and sampled with wrapping.
+    // Samplers (Aurora.h:922): AddressModeU / AddressModeV.  A texture without a sampler uses the
+    // renderer's default one (nearest filtering, wrap); a texture with a sampler set here filters
+    // bilinearly (HGISampler.cpp:21-41).  Address modes other than Wrap are reported and sampled
+    // with wrapping.
     virtual void setSamplerProperties(const Path& atPath, const Properties& props)      = 0;
     virtual bool addInstance(const Path& path, const Path& geometry, const Properties& properties = {}) = 0;
     virtual void setInstanceProperties(const Path& path, const Properties& instanceProperties) = 0;

@@ -166,6 +166,8 @@ int main(int argc, char** argv)
             };
             scene->setImageDescriptor("/image/" + std::to_string(k), id);
         }
+        if (version >= 2)
+            scene->setSamplerProperties("/sampler/linear", {}); // a material sampler: bilinear, wrap
         uint32_t nm = r.get<uint32_t>();
         for (uint32_t m = 0; m < nm; m++)
         {

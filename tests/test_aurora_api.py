@@ -147,7 +147,9 @@ def write_scene(path, s, view, proj, lights, depth, mtlx=False):
                 img = int(s.textures["image"][mi, slot])
                 if img >= 0:
                     tex.append((name, img))
-        count = len(props) + sum(5 for _ in tex)
+        # a bilinear image gets a sampler of the material's own (the default sampler is nearest)
+        linear = {img: bool(s.images[img]["linear"]) for _, img in tex}
+        count = len(props) + sum(6 if linear[img] else 5 for _, img in tex)
         b += struct.pack("<I", count)
         for k in props:
             b += struct.pack("<B", len(k)) + k.encode()
@@ -166,6 +168,9 @@ def write_scene(path, s, view, proj, lights, depth, mtlx=False):
                 b += struct.pack("<B", len(k)) + k.encode() + struct.pack("<B2f", 5, *map(float, mat[k]))
             k = name + "_rotation"
             b += struct.pack("<B", len(k)) + k.encode() + struct.pack("<Bf", 1, float(mat[k]))
+            if linear[img]:
+                k, sp = name + "_sampler", b"/sampler/linear"
+                b += struct.pack("<B", len(k)) + k.encode() + struct.pack("<BB", 4, len(sp)) + sp
     b += struct.pack("<I", len(s.instances))
     for inst, ls in zip(s.instances, inst_layers):
         m4 = np.eye(4, dtype=np.float32)

@@ -116,7 +116,8 @@ def test_cli_render_matches_c_abi(agb, oracle, ground, texture, mtlx):
         rgba = np.float64(np.reshape(tex["rgba"], (tex["height"], tex["width"], 4))) / 255.0
         lin = np.where(rgba <= 0.04045, rgba / 12.92, ((rgba + 0.055) / 1.055) ** 2.4)
         lin[..., 3] = rgba[..., 3]
-        tex_id = s.add_image(lin.astype(np.float32), _abi.FORMAT_RGBA32F, linear=True)
+        # no sampler in an MTL file: the renderer's default sampler, nearest filtering
+        tex_id = s.add_image(lin.astype(np.float32), _abi.FORMAT_RGBA32F, linear=False)
         s.textures = scenes.no_textures(len(names))
         floor = [m["path"] for m in scene["materials"] if m["properties"].get("base_color_image")][0]
         s.materials["has_base_color_image"][names[floor]] = 1
