@@ -29,6 +29,7 @@ ENV_TABLE_REFERENCE = 0
 ENV_TABLE_FP64 = 1
 BVH_HOST, BVH_GPU = 0, 1
 ENV_NOALLOC_MAX_TEXELS = 262144  # AGB_ENV_NOALLOC_MAX_TEXELS
+WAVE_LARGEST = 0xFFFFFFFF  # AGB_WAVE_LARGEST: waves from half the free device memory
 TEX_BASE_COLOR, TEX_SPECULAR_ROUGHNESS, TEX_OPACITY, TEX_NORMAL, TEX_EMISSION = range(5)
 
 

@@ -12,6 +12,7 @@
 #include <cstring>
 #include <list>
 #include <mutex>
+#include <set>
 
 #include "agb.h"
 #include "aurora_gb300.hpp"
@@ -344,6 +345,8 @@ public:
     std::map<Path, Properties> materials;
     std::map<Path, Properties> environments;
     std::map<Path, Properties> samplers;
+    // Per material: texture properties fed by MaterialX image nodes (sampled bilinearly).
+    std::map<Path, std::set<std::string>> materialXBilinear;
     std::vector<std::pair<Path, Instance>> instances; // insertion order
     std::vector<std::shared_ptr<Light>> lights;
     std::shared_ptr<GroundPlane> groundPlane; // null: the default, disabled plane
@@ -367,7 +370,7 @@ public:
     {
         if (!d.getData)
             throw Error("setImageDescriptor: a data callback is required");
-        images[p] = Image{ d, -1 };
+        images[p] = Image{ d };
         dirty     = true;
     }
     // The file is read when the image is first used and released once uploaded (the scene keeps
@@ -419,7 +422,7 @@ public:
             std::vector<uint8_t>().swap(store->rgba8);
             std::vector<float>().swap(store->rgb32);
         };
-        images[p] = Image{ d, -1, -1 };
+        images[p] = Image{ d }; // both texture handles start unset (-1)
         dirty     = true;
     }
     void setMaterialType(const Path& p, const std::string& type, const std::string& document) override
@@ -439,13 +442,15 @@ public:
                 logError("setMaterialType " + p + ": " + warnings);
             if (ok)
             {
-                // MaterialX image nodes filter linearly (their filtertype default): a sampler of
-                // the material's own.
+                // MaterialX image nodes filter linearly (their filtertype default).  The slots are
+                // kept apart from the user's samplers, so no sampler name is taken; their address
+                // modes (uaddressmode / vaddressmode) are not read: the device wraps.
+                std::set<std::string>& lin = materialXBilinear[p];
+                lin.clear();
                 for (const MaterialXImage& im : imgs)
                 {
                     setImageFromFilePath(im.image, im.file, im.linearize, false);
-                    samplers["MaterialXSampler"];
-                    m[im.property + "_sampler"] = std::string("MaterialXSampler");
+                    lin.insert(im.property);
                 }
                 for (auto& kv : fromDoc)
                     m[kv.first] = kv.second;
@@ -845,6 +850,9 @@ public:
                 {
                     const std::string* sampler = find<std::string>(all, std::string(f.name) + "_sampler");
                     bool bilinear = sampler && !sampler->empty() && samplers.count(*sampler);
+                    auto mx       = materialXBilinear.find(path);
+                    if (mx != materialXBilinear.end() && mx->second.count(f.name))
+                        bilinear = true;
                     t.image[f.slot] = textureHandle(*ip, bilinear);
                     has             = 1;
                 }

@@ -1104,24 +1104,29 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
     uint32_t accumMode = opt->accumulation ? opt->accumulation : AGB_ACCUM_RUNNING_MEAN;
     uint32_t pixels    = opt->width * opt->height;
     uint32_t spw = 1;
-    if (opt->max_paths_in_flight)
+    const bool explicitWave = opt->max_paths_in_flight && opt->max_paths_in_flight != AGB_WAVE_LARGEST;
+    if (explicitWave)
     {
         spw = uint32_t(std::max<uint64_t>(1, opt->max_paths_in_flight / pixels));
         spw = std::min(spw, std::max(1u, sample_count));
     }
     else
     {
-        // Default wave: the call's samples in as few waves as fit in half of the device memory
-        // that is free (counting this context's wave buffers as free) and at most a third of the
-        // device, split evenly: one wave of 82 GB for 64 samples of 1920x1080 on an idle 288 GB
-        // device.  Fewer, larger waves keep every bounce's launch full and pay each launch's tail
-        // once per bounce instead of once per wave and bounce.
+        // The call's samples in as few waves as fit, split evenly.  Default: wave buffers of at
+        // most AGB_WAVE_DEFAULT_BYTES (a library that shares the device with its host takes a
+        // bounded amount).  AGB_WAVE_LARGEST: half of the device memory that is free (counting
+        // this context's wave buffers as free) and at most a third of the device: one wave of
+        // 82 GB for 64 samples of 1920x1080 on an idle 288 GB device.  Fewer, larger waves keep
+        // every bounce's launch full and pay each launch's tail once per bounce instead of once
+        // per wave and bounce (about 4 % at that size).
         size_t freeBytes = 0, totalBytes = ctx->deviceBytes;
         if (cudaMemGetInfo(&freeBytes, &totalBytes) != cudaSuccess)
             freeBytes = totalBytes / 4;
         const uint64_t perPath = kPathStateBytes + kPathQueueBytes;
         uint64_t held   = uint64_t(ctx->pathCapacity) * perPath;
         uint64_t bytes  = std::min<uint64_t>((uint64_t(freeBytes) + held) / 2, uint64_t(totalBytes) / 3);
+        if (!opt->max_paths_in_flight)
+            bytes = std::min<uint64_t>(bytes, AGB_WAVE_DEFAULT_BYTES);
         uint64_t budget = std::max<uint64_t>(pixels, bytes / perPath);
         budget          = std::min<uint64_t>(budget, (1ull << 29) - 1);
         uint32_t most   = uint32_t(std::max<uint64_t>(1, budget / pixels));
@@ -1140,7 +1145,7 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
     {
         waves = sample_count ? (sample_count + spw - 1) / spw : 0;
         st    = ensureWave(ctx, size_t(spw) * pixels, depth, std::max(1u, waves));
-        if (st != AGB_ERR_OOM || opt->max_paths_in_flight || spw == 1)
+        if (st != AGB_ERR_OOM || explicitWave || spw == 1)
             break;
         // The default wave did not fit after all (memory taken meanwhile): halve it.
         cudaGetLastError();

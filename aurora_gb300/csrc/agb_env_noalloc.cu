@@ -10,8 +10,6 @@
 // The array lives in this file alone so that only processes that use this entry point carry it:
 // the CUDA driver reserves a module's __device__ storage when it loads the module (at context
 // creation with eager module loading, on first use with lazy loading).
-#include <atomic>
-
 #include "agb_kernels.h"
 
 namespace agb
@@ -38,9 +36,6 @@ constexpr size_t kOffBlockCnt  = alignUp(kOffBlockSums + sizeof(double) * (kTile
 constexpr size_t kOffRowSA     = alignUp(kOffBlockCnt + sizeof(uint32_t) * (kTiles + 8));
 constexpr size_t kScratchBytes = alignUp(kOffRowSA + sizeof(float) * (size_t(kMax) + 16));
 
-constexpr int kCachedDevices = 64;
-std::atomic<unsigned char*> g_scratchAddress[kCachedDevices];
-
 } // namespace
 
 // Nothing in it has to start at zero: every kernel of the build writes each scratch entry it
@@ -50,28 +45,16 @@ static __device__ __align__(256) unsigned char g_envNoAllocScratch[kScratchBytes
 namespace
 {
 
-// Device address of the scratch on the current device; looked up once per device.
+// Device address of the scratch in the current device's context.  Looked up on every call (the
+// lookup allocates nothing): a cached address would outlive a context reset (cudaDeviceReset, or
+// a primary context released and retained again), after which the module's storage is reloaded
+// at another address.
 cudaError_t scratchAddress(unsigned char** out)
 {
-    int dev        = 0;
-    cudaError_t e  = cudaGetDevice(&dev);
-    if (e != cudaSuccess)
-        return e;
-    if (dev >= 0 && dev < kCachedDevices)
-    {
-        unsigned char* p = g_scratchAddress[dev].load(std::memory_order_acquire);
-        if (p)
-        {
-            *out = p;
-            return cudaSuccess;
-        }
-    }
     unsigned char* p = nullptr;
-    e = cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_envNoAllocScratch);
+    cudaError_t e    = cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_envNoAllocScratch);
     if (e != cudaSuccess)
         return e;
-    if (dev >= 0 && dev < kCachedDevices)
-        g_scratchAddress[dev].store(p, std::memory_order_release);
     *out = p;
     return cudaSuccess;
 }

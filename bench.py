@@ -54,8 +54,13 @@ def parse_args():
     p.add_argument("--serve-requests", type=int, default=160)
     p.add_argument("--ground-plane", action="store_true",
                    help="add a ground plane (the reference's defaults) under the scene (overhead runs)")
-    p.add_argument("--max-paths", type=int, default=0,
-                   help="paths in flight per wave (0: the library's default)")
+    p.add_argument("--max-paths", type=int, default=0xFFFFFFFF,
+                   help="paths in flight per wave (0: the library's bounded default of 8 GiB of "
+                        "wave buffers; default here 0xFFFFFFFF = AGB_WAVE_LARGEST, waves sized "
+                        "from half the free device memory)")
+    p.add_argument("--oracle-rows", type=int, default=8,
+                   help="rows of the frame rendered by the FP64 oracle at the step's samples for "
+                        "the reported relMSE (0: skip)")
     return p.parse_args()
 
 
@@ -348,6 +353,28 @@ def cpu_render_rate(s, seconds):
         f"1-{spp}), {paths} path samples, {r['seconds']:.1f} s, FP32 oracle, BVH build excluded")
 
 
+def rel_mse_vs_fp64_oracle(s, img, rows, threads=None):
+    """relMSE (eps 1e-2) of the renderer's image of the step (sum / n, the step's own samples
+    0..spp-1) against the FP64 oracle's render of the same samples over a band of `rows` rows
+    through the middle of the frame: the error of the benchmarked result itself."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    o = pyoracle.OracleScene(s)
+    y0 = s.height // 2 - rows // 2
+    rect = (0, y0, s.width, y0 + rows)
+    t0 = time.perf_counter()
+    ref = o.render(0, s.spp, precision=64, want_sum=True, want_mean=False, rect=rect,
+                   threads=threads)
+    secs = time.perf_counter() - t0
+    o.close()
+    band = slice(y0, y0 + rows)
+    err = pyoracle.rel_mse(img[band], ref["sum"][band] / s.spp)
+    return {"rel_mse": err, "eps": 1e-2, "bar": 1e-3, "within_bar": err <= 1e-3,
+            "oracle": "FP64 CPU restatement of the reference shaders, same sample streams",
+            "rows": [y0, y0 + rows], "spp": s.spp, "pixels": s.width * rows,
+            "oracle_seconds": secs}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -503,7 +530,11 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": workload(s, args.config),
+        "config": {**workload(s, args.config),
+                   "wave": ("largest (AGB_WAVE_LARGEST: half the free device memory)"
+                            if args.max_paths == 0xFFFFFFFF else
+                            "library default (8 GiB of wave buffers)" if args.max_paths == 0 else
+                            f"{args.max_paths} paths")},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(_abi.FRAME_DTYPE.itemsize),
                 "d2h_bytes_per_step": int(s.width * s.height * 16),
                 "ms_per_step": 1000.0 * e2e_time / args.steps},
@@ -517,6 +548,9 @@ def main():
         "roofline": roofline,
         "clocks": clk,
     }
+    if world == 1 and args.oracle_rows > 0:
+        out["rel_mse_vs_fp64_oracle"] = rel_mse_vs_fp64_oracle(
+            s, r.read(_abi.ACCUM_KAHAN).copy(), args.oracle_rows)
     if world == 1 and not args.no_time_to_error:
         out["time_to_rel_mse"] = bench_time_to_rel_mse(torch, _abi, r, s)
     if world == 1 and not args.no_denoiser:

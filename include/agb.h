@@ -276,6 +276,10 @@ enum
     AGB_ACCUM_MOMENTS = 4
 };
 
+/* Wave sizing (agb_render_options.max_paths_in_flight). */
+#define AGB_WAVE_LARGEST 0xFFFFFFFFu
+#define AGB_WAVE_DEFAULT_BYTES (8ull << 30)
+
 /* Render options beyond FrameData. */
 typedef struct agb_render_options
 {
@@ -283,8 +287,10 @@ typedef struct agb_render_options
     uint32_t height;
     uint32_t accumulation;      /* AGB_ACCUM_* bitmask */
     uint32_t max_paths_in_flight; /* wave size in paths; 0 = the call's samples in as few waves
-                                     as fit in half the free device memory (at most a third
-                                     of the device), halved again if allocation fails */
+                                     as fit in AGB_WAVE_DEFAULT_BYTES of wave buffers;
+                                     AGB_WAVE_LARGEST = as few waves as fit in half the free
+                                     device memory (at most a third of the device); either is
+                                     halved again if allocation fails */
     int32_t env_filter_linear;  /* environment sampler: 0 nearest (Hgi default), 1 bilinear */
     uint32_t seed_offset;       /* added to the sample index that seeds the random streams, not to
                                    the accumulation index (gSampleData.seedOffset,
@@ -425,8 +431,9 @@ AGB_API agb_status agb_set_environment_table(agb_context* ctx, int32_t layout);
  * Scratch is one fixed array in the library's device image (about 12.6 MB, reserved by the CUDA
  * driver when it loads this part of the library), so width*height is at most
  * AGB_ENV_NOALLOC_MAX_TEXELS; larger images are rejected with AGB_ERR_LIMIT.  Works on the
- * current device.  The first call on each device does one-time setup (it looks up the scratch
- * address, which can make the driver load the module): make it before any stream capture.
+ * current device.  Each call looks up the scratch address in the current context (no
+ * allocation), so a context reset (cudaDeviceReset) is followed correctly; the first call on a
+ * device can make the driver load this part of the library: make it before any stream capture.
  * Returns after the stream has finished the build.  All calls on a device share the one scratch
  * array: calls that overlap in time (two host threads, or two streams) race and corrupt each
  * other's tables, so callers serialise them. */

@@ -13,7 +13,10 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_SOURCE = "/root/reference/Libraries/Aurora/Source"
+# The reference checkout this recipe compiles from (read-only; absent on machines that only run the
+# built files).  AURORA_REFERENCE_ROOT overrides the default location.
+REFERENCE_ROOT = os.environ.get("AURORA_REFERENCE_ROOT", "/root/reference")
+REFERENCE_SOURCE = os.path.join(REFERENCE_ROOT, "Libraries", "Aurora", "Source")
 
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-pthread",
             "-fvisibility=hidden"]

@@ -3,7 +3,10 @@
 // and instances through property maps, distant lights through ILight values, the environment
 // through its properties, the camera through setCamera, then render() into an RGBA32F target.
 //
-// usage: aurora_api_render <scene file> <output file>
+// usage: aurora_api_render <scene file> <output file> [--late-materials]
+// --late-materials: the scene is first rendered (1 sample) with its materials unset, then the
+//   materials (and the images they name, MaterialX file images included) are set and the frame is
+//   rendered again from sample 0: resources added to a scene after its first activation.
 // Scene file (little-endian), written by tests/test_aurora_api.py:
 //   "AGBS", u32 version (1 or 2), u32 width, height, spp, trace depth, f32 view[16], proj[16]
 //     (column-major)
@@ -23,6 +26,7 @@
 // Output: u32 width, height, then f32 RGBA rows top to bottom.
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -69,11 +73,12 @@ struct Mesh
 
 int main(int argc, char** argv)
 {
-    if (argc != 3)
+    if (argc != 3 && !(argc == 4 && std::string(argv[3]) == "--late-materials"))
     {
-        std::fprintf(stderr, "usage: %s scene output\n", argv[0]);
+        std::fprintf(stderr, "usage: %s scene output [--late-materials]\n", argv[0]);
         return 2;
     }
+    const bool lateMaterials = argc == 4;
     try
     {
         Reader r;
@@ -168,6 +173,7 @@ int main(int argc, char** argv)
         }
         if (version >= 2)
             scene->setSamplerProperties("/sampler/linear", {}); // a material sampler: bilinear, wrap
+        std::vector<std::function<void()>> materialOps; // applied before or after a first render
         uint32_t nm = r.get<uint32_t>();
         for (uint32_t m = 0; m < nm; m++)
         {
@@ -178,7 +184,10 @@ int main(int argc, char** argv)
                 // A MaterialX document instead of a property list.
                 auto doc = r.array<char>(r.get<uint32_t>());
                 Path path = "/material/" + std::to_string(m);
-                scene->setMaterialType(path, Names::MaterialTypes::kMaterialX, std::string(doc.begin(), doc.end()));
+                std::string text(doc.begin(), doc.end());
+                materialOps.push_back([scene, path, text]() {
+                    scene->setMaterialType(path, Names::MaterialTypes::kMaterialX, text);
+                });
                 continue;
             }
             for (uint32_t k = 0; k < np; k++)
@@ -207,9 +216,14 @@ int main(int argc, char** argv)
                     props[name] = r.get<uint8_t>() != 0;
             }
             Path path = "/material/" + std::to_string(m);
-            scene->setMaterialType(path);
-            scene->setMaterialProperties(path, props);
+            materialOps.push_back([scene, path, props]() {
+                scene->setMaterialType(path);
+                scene->setMaterialProperties(path, props);
+            });
         }
+        if (!lateMaterials)
+            for (auto& op : materialOps)
+                op();
         uint32_t ninst = r.get<uint32_t>();
         for (uint32_t i = 0; i < ninst; i++)
         {
@@ -300,9 +314,16 @@ int main(int argc, char** argv)
         IRenderBufferPtr target = renderer->createRenderBuffer(int(width), int(height), ImageFormat::Float_RGBA);
         renderer->setTargets({ { AOV::Final, target } });
         renderer->setCamera(view, proj);
+        if (lateMaterials)
+        {
+            renderer->render(0, 1);
+            renderer->waitForTask();
+            for (auto& op : materialOps)
+                op();
+        }
         renderer->render(0, spp);
         renderer->waitForTask();
-        if (released != meshes.size())
+        if (lateMaterials ? released < meshes.size() : released != meshes.size())
             throw Error("attributeUpdateComplete was not called for every mesh");
         size_t stride = 0;
         const float* px = static_cast<const float*>(target->data(stride));

@@ -20,8 +20,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference"
 sys.path.insert(0, os.path.join(REPO, "oracle"))
+from build_oracle import REFERENCE_ROOT as REF  # noqa: E402
 
 
 def material_layout():

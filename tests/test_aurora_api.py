@@ -242,12 +242,15 @@ def test_cpp_interface_render_matches_c_abi(agb, oracle, ground, mtlx):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("mtlx", [False, True])
-def test_cpp_interface_textures_and_layers_match_c_abi(agb, oracle, mtlx):
+@pytest.mark.parametrize("mtlx,late", [(False, False), (True, False), (False, True), (True, True)])
+def test_cpp_interface_textures_and_layers_match_c_abi(agb, oracle, mtlx, late):
     """Material textures (image paths, a transformed base-colour texture), samplers and material
     layers (layer_materials / layer_geometry, the layer's UVs from a geometry of its own) through
     the C++ interface, against the same scene through the C ABI; with `mtlx`, the materials are
-    MaterialX documents whose textures are PNG files behind node-graph tiledimages."""
+    MaterialX documents whose textures are PNG files behind node-graph tiledimages.  With `late`,
+    the client renders once before it sets the materials, so their images (two PNG files, sampled
+    bilinearly, in the MaterialX case) are uploaded after the environment image took the
+    context's first image handle."""
     from aurora_gb300 import _abi, api, scenes
     exe = build_client()
     s = scenes.config_layered(width=64, height=48, spp=4, trace_depth=4, blas=2, instances=6,
@@ -266,7 +269,7 @@ def test_cpp_interface_textures_and_layers_match_c_abi(agb, oracle, mtlx):
     with tempfile.TemporaryDirectory() as tmp:
         scene_file, out_file = os.path.join(tmp, "scene.bin"), os.path.join(tmp, "out.bin")
         write_scene(scene_file, s, view, proj, [], depth, mtlx=mtlx)
-        subprocess.check_call([exe, scene_file, out_file])
+        subprocess.check_call([exe, scene_file, out_file] + (["--late-materials"] if late else []))
         raw = open(out_file, "rb").read()
     w, h = struct.unpack("<2I", raw[:8])
     img = np.frombuffer(raw[8:], np.float32).reshape(h, w, 4)

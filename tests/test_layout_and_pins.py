@@ -172,7 +172,8 @@ def test_sheen_tables_identical():
     b = numbers(os.path.join(ROOT, "aurora_gb300", "csrc", "agb_sheen_lut.cuh"))
     assert a.shape == (256,)
     np.testing.assert_array_equal(a, b)
-    ref = "/root/reference/Libraries/Aurora/Source/Shaders/StandardSurfaceBSDF.slang"
+    from build_oracle import REFERENCE_SOURCE
+    ref = os.path.join(REFERENCE_SOURCE, "Shaders", "StandardSurfaceBSDF.slang")
     if os.path.exists(ref):
         src = open(ref).read()
         m = re.search(r"u_sheenAlbedo\[[^\]]*\] = \{(.*?)\};", src, re.S)
