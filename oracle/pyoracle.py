@@ -61,6 +61,87 @@ def lib():
     return _lib
 
 
+_ref_lib = False
+
+
+def ref_lib():
+    """The reference's own shader functions compiled as host C++ (oracle/_ref/libshaders_ref.so,
+    built from the reference tree by build_oracle.build_reference_shaders), or None where the
+    reference tree is absent."""
+    global _ref_lib
+    if _ref_lib is False:
+        path = build_oracle.build_reference_shaders()
+        if path is None:
+            _ref_lib = None
+        else:
+            L = ctypes.CDLL(path)
+            P = ctypes.c_void_p
+            for prec in (32, 64):
+                getattr(L, f"ref{prec}_bsdf_batch").argtypes = [ctypes.c_int, ctypes.c_int, P, P, P, P,
+                                                                P, P, ctypes.c_int64, P, P, P, P]
+                getattr(L, f"ref{prec}_env_sample").argtypes = [P, P, ctypes.c_uint32, ctypes.c_uint32,
+                                                                P, P, ctypes.c_int64, P, P, P]
+                getattr(L, f"ref{prec}_env_evaluate").argtypes = [P, P, ctypes.c_uint32, ctypes.c_uint32,
+                                                                  P, ctypes.c_uint32, ctypes.c_uint32,
+                                                                  ctypes.c_int, P, P, ctypes.c_int64, P]
+                getattr(L, f"ref{prec}_random_stream").argtypes = [ctypes.c_uint32] * 4 + [ctypes.c_int, P]
+            _ref_lib = L
+    return _ref_lib
+
+
+def ref_bsdf_batch(op, mats, mat_index, frames, V, L, rnd, precision=32, denoising_aovs=False):
+    """StandardSurfaceBSDF.slang's evaluateMaterial (op 0), sampleMaterial (1) and
+    evaluateMaterialAndPDF (2) from the reference source itself, FP32 or FP64."""
+    n = len(mat_index)
+    val = np.zeros((n, 3), np.float32)
+    d = np.zeros((n, 3), np.float32)
+    pdf = np.zeros(n, np.float32)
+    lobe = np.zeros(n, np.int32)
+    c = np.ascontiguousarray
+    getattr(ref_lib(), f"ref{precision}_bsdf_batch")(
+        op, 1 if denoising_aovs else 0, _p(c(mats)), _p(c(mat_index, np.int32)),
+        _p(c(frames, np.float32)), _p(c(V, np.float32)),
+        _p(None if L is None else c(L, np.float32)), _p(None if rnd is None else c(rnd, np.float32)),
+        n, _p(val), _p(d), _p(pdf), _p(lobe))
+    return val, d, pdf, lobe
+
+
+def ref_env_sample(env, light_rgba, alias, rnd, precision=32):
+    """Environment.slang's sampleEnvironment from the reference source."""
+    light_rgba = np.ascontiguousarray(light_rgba, np.float32)
+    h, w = light_rgba.shape[:2]
+    n = len(rnd)
+    r = np.zeros((n, 3), np.float32)
+    d = np.zeros((n, 3), np.float32)
+    pdf = np.zeros(n, np.float32)
+    getattr(ref_lib(), f"ref{precision}_env_sample")(
+        _p(np.ascontiguousarray(env)), _p(light_rgba), w, h, _p(np.ascontiguousarray(alias)),
+        _p(np.ascontiguousarray(rnd, np.float32)), n, _p(r), _p(d), _p(pdf))
+    return r, d, pdf
+
+
+def ref_env_evaluate(env, light_rgba, background_rgba, dirs, as_background, linear=False,
+                     precision=32):
+    """Environment.slang's evaluateEnvironment from the reference source."""
+    light_rgba = np.ascontiguousarray(light_rgba, np.float32)
+    background_rgba = np.ascontiguousarray(background_rgba, np.float32)
+    n = len(dirs)
+    out = np.zeros((n, 3), np.float32)
+    getattr(ref_lib(), f"ref{precision}_env_evaluate")(
+        _p(np.ascontiguousarray(env)), _p(light_rgba), light_rgba.shape[1], light_rgba.shape[0],
+        _p(background_rgba), background_rgba.shape[1], background_rgba.shape[0], 1 if linear else 0,
+        _p(np.ascontiguousarray(dirs, np.float32)), _p(np.ascontiguousarray(as_background, np.int32)),
+        n, _p(out))
+    return out
+
+
+def ref_random_stream(sample_index, width, px, py, n):
+    """Random.slang's pcg2DInit + random2D from the reference source (FP32)."""
+    out = np.zeros((n, 2), np.float32)
+    ref_lib().ref32_random_stream(sample_index, width, px, py, n, _p(out))
+    return out
+
+
 def _p(a):
     return None if a is None else ctypes.c_void_p(a.ctypes.data)
 

@@ -9,6 +9,11 @@ tree exists; the fixtures travel, the reference does not).
   alias_ref.npz         alias tables and luminance integrals from the reference's own
                         AliasMap::build (AliasMap.cpp:71-166), compiled in place by
                         oracle/build_oracle.py, on seeded environment images.
+  shaders_ref.npz       outputs of the reference's own shader functions compiled as host C++
+                        (oracle/build_oracle.py build_reference_shaders): Standard Surface
+                        evaluateMaterial / sampleMaterial / evaluateMaterialAndPDF on 4096 seeded
+                        cases (inputs stored) with the per-case tolerances of tests/bsdf_cases.py,
+                        sampleEnvironment on a seeded 64x32 environment, and random2D streams.
 """
 import ctypes
 import json
@@ -20,6 +25,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+sys.path.insert(0, os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(REPO, "oracle"))
 from build_oracle import REFERENCE_ROOT as REF  # noqa: E402
 
@@ -96,8 +103,44 @@ def alias_tables():
     return out
 
 
+def shader_references(n=4096, seed=2024):
+    import pyoracle
+    from aurora_gb300 import scenes
+    from bsdf_cases import make_cases, tolerances
+    assert pyoracle.ref_lib() is not None, "the reference tree is needed"
+    m, idx, frames, V, L, rnd = make_cases(n, seed)
+    out = dict(materials=m.view(np.uint8).copy(), idx=idx, frames=frames, V=V, L=L, rnd=rnd)
+    for op in (0, 1, 2):
+        r32, r64, tol = tolerances(pyoracle.ref_bsdf_batch, op, m, idx, frames, V, L, rnd)
+        for tag, r in (("ref32", r32), ("ref64", r64)):
+            for k, name in enumerate(("value", "dir", "pdf", "lobe")):
+                out[f"op{op}_{tag}_{name}"] = r[k]
+        out[f"op{op}_tol"] = tol
+    img = scenes.hdr_env(64, 32, 3, sigma=1.0, suns=1, sun_radiance=200.0, sun_radius=1.5)
+    rgba = np.ones((32, 64, 4), np.float32)
+    rgba[..., :3] = img
+    alias, integral = pyoracle.alias_build(img)
+    env = np.ascontiguousarray(scenes.environment()).reshape(1).copy()
+    env["has_light_tex"] = 1
+    env["light_tex_luminance_integral"] = integral
+    env_rnd = np.random.default_rng(seed + 1).uniform(size=(n, 2)).astype(np.float32)
+    er, ed, ep = pyoracle.ref_env_sample(env, rgba, alias, env_rnd)
+    out.update(env_image=img, env_alias=alias.view(np.uint8).copy(), env_integral=np.float64(integral),
+               env_data=env.view(np.uint8).copy(), env_rnd=env_rnd, env_radiance=er, env_dir=ed,
+               env_pdf=ep)
+    streams = []
+    for sample, width, px, py in ((0, 512, 0, 0), (7, 512, 511, 3), (63, 1920, 1000, 540),
+                                  (4095, 3840, 3839, 2159), (1 << 24, 64, 5, 9)):
+        streams.append(pyoracle.ref_random_stream(sample, width, px, py, 16))
+    out["random_args"] = np.array([(0, 512, 0, 0), (7, 512, 511, 3), (63, 1920, 1000, 540),
+                                   (4095, 3840, 3839, 2159), (1 << 24, 64, 5, 9)], np.uint32)
+    out["random_streams"] = np.stack(streams)
+    return out
+
+
 if __name__ == "__main__":
     json.dump(material_layout(), open(os.path.join(HERE, "material_layout.json"), "w"), indent=1)
     json.dump(frame_layout(), open(os.path.join(HERE, "frame_layout.json"), "w"), indent=1)
     np.savez_compressed(os.path.join(HERE, "alias_ref.npz"), **alias_tables())
+    np.savez_compressed(os.path.join(HERE, "shaders_ref.npz"), **shader_references())
     print("golden fixtures written")
