@@ -203,6 +203,8 @@ SIGNATURES = {
     "agb_set_bvh_builder": (_I32, [_P, _I32]),
     "agb_geometry_bvh": (_I32, [_P, _I32, _P, _U64, _P, _U64, ctypes.POINTER(_I32), ctypes.POINTER(_I32),
                                 ctypes.POINTER(_U32)]),
+    "agb_tlas_read": (_I32, [_P, _P, _U64, _P, _U64, ctypes.POINTER(_I32), ctypes.POINTER(_I32),
+                             ctypes.POINTER(_U32)]),
     "agb_materials_set": (_I32, [_P, _P, _P, _U32]),
     "agb_instances_set": (_I32, [_P, _P, _U32]),
     "agb_environment_set": (_I32, [_P, _P, _I32, _I32]),
@@ -216,6 +218,7 @@ SIGNATURES = {
     "agb_frame_set": (_I32, [_P, _P]),
     "agb_render": (_I32, [_P, ctypes.POINTER(RenderOptions), _U32, _U32, ctypes.POINTER(RenderStats)]),
     "agb_wait": (_I32, [_P]),
+    "agb_accum_read_rect": (_I32, [_P, _I32, _U32, _U32, _U32, _U32, _P, _U64]),
     "agb_accum_read": (_I32, [_P, _I32, _P, _U64]),
     "agb_accum_device": (_I32, [_P, _I32, ctypes.POINTER(_P)]),
     "agb_last_sample_device": (_I32, [_P, ctypes.POINTER(_P)]),

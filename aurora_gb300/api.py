@@ -132,6 +132,13 @@ class Renderer:
     def set_profiling(self, enabled):
         check(self._lib.agb_set_profiling(self.ctx, 1 if enabled else 0))
 
+    def read_rect(self, rect, mode=_abi.ACCUM_KAHAN):
+        """The accumulated image over rect = (x0, y0, x1, y1) (agb_accum_read_rect)."""
+        x0, y0, x1, y1 = (int(v) for v in rect)
+        out = np.empty((y1 - y0, x1 - x0, 4), np.float32)
+        check(self._lib.agb_accum_read_rect(self.ctx, mode, x0, y0, x1 - x0, y1 - y0, ptr(out), out.size))
+        return out
+
     def read(self, mode=_abi.ACCUM_RUNNING_MEAN, width=None, height=None, out=None):
         w = width or self.scene.width
         h = height or self.scene.height

@@ -112,7 +112,7 @@ void buildBVH2(const float* boxesIn, uint32_t n, int maxLeaf, int maxDepth, Buil
             continue;
         uint32_t first = nd.first, count = nd.count;
         uint32_t mid   = first;
-        bool forceMedian = it.depth + ceilLog2((count + 3) / 4) + 2 >= maxDepth;
+        bool forceMedian = it.depth + ceilLog2((count + maxLeaf - 1) / maxLeaf) + 2 >= maxDepth;
         int bestAxis = -1, bestSplit = -1;
         float bestCost = INFINITY;
         if (!forceMedian)

@@ -1,19 +1,20 @@
-// GPU binned-SAH BVH2 builder for triangle meshes (BLAS), producing the same 64-byte node layout
-// and leaf encoding as the host builder (agb_bvh_build.cpp), which stays in use for the TLAS.
+// GPU binned-SAH BVH2 builder, producing the same 64-byte node layout and leaf encoding as the host
+// builder (agb_bvh_build.cpp): over the triangles of a mesh (BLAS, leaves of at most 4 triangles)
+// and over instance boxes (TLAS, one instance per leaf).
 //
 // Top-down, one level of the tree per launch, one CTA per node (task) of the level:
 //   1. the CTA reduces its primitives' box and centroid box and writes the box into its parent's
 //      child slot (the node layout keeps both child boxes in the parent);
-//   2. a node of at most 4 triangles becomes a leaf (ref ~(first << 3 | count - 1));
+//   2. a node of at most leafMax primitives becomes a leaf (ref ~(first << 3 | count - 1));
 //   3. otherwise 16 bins per axis over the centroid box collect counts and boxes (shared-memory
 //      atomics on order-preserving integer encodings of the floats); one thread per axis sweeps the
-//      15 split planes with the SAH cost area(L) n(L) + area(R) n(R); the node stays a leaf when
-//      it holds at most 4 triangles and no split beats area(node) n(node), like the host builder;
+//      15 split planes with the SAH cost area(L) n(L) + area(R) n(R);
 //   4. the CTA partitions its range of the primitive order stably and in place (ballot ranks per
 //      warp, warp offsets through shared memory, a scratch copy of the range), allocates its node
 //      id and appends its two children to the next level's task list.
 // Nodes that could exceed the depth budget (the traversal stack holds 48 entries for TLAS + BLAS)
-// split at their index midpoint, which halves every subtree and bounds the depth.
+// split at their index midpoint, which halves every subtree and bounds the depth: the tree is then
+// at most maxDepth deep whenever ceil(log2(count / leafMax)) + 2 <= maxDepth.
 #include <algorithm>
 
 #include "agb_kernels.h"
@@ -25,7 +26,7 @@ namespace
 
 constexpr int kBins        = 16;
 constexpr int kBuildThreads = 128;
-constexpr int kBuildLeaf   = 4;
+constexpr int kBlasLeaf    = 4;
 
 struct BuildTask
 {
@@ -88,7 +89,7 @@ __device__ void blockBox(float v[6], float* s)
 __global__ void __launch_bounds__(kBuildThreads) k_bvh_level(const float* boxes, uint32_t* order,
     uint32_t* scratch, const BuildTask* tasks, BuildTask* next, uint32_t* nextCount, BNode* nodes,
     uint32_t* nodeCount, int32_t* rootRef, uint32_t* depthSeen, uint32_t nodeCapacity, int maxDepth,
-    int* err)
+    uint32_t leafMax, int* err)
 {
     const BuildTask t = tasks[blockIdx.x];
     const int tid     = threadIdx.x;
@@ -153,12 +154,12 @@ __global__ void __launch_bounds__(kBuildThreads) k_bvh_level(const float* boxes,
                 *rootRef = ref;
         }
     };
-    if (t.count <= uint32_t(kBuildLeaf))
+    if (t.count <= leafMax)
     {
         makeLeaf();
         return;
     }
-    const bool forceMid = t.depth + ceilLog2((t.count + 3) / 4) + 2 >= maxDepth;
+    const bool forceMid = t.depth + ceilLog2((t.count + leafMax - 1) / leafMax) + 2 >= maxDepth;
     // 3. Binned SAH.
     if (tid < 3 * kBins)
     {
@@ -251,9 +252,7 @@ __global__ void __launch_bounds__(kBuildThreads) k_bvh_level(const float* boxes,
         for (int a = 0; a < 3; a++)
             if (bestSplit[a] >= 0 && (best < 0 || bestCost[a] < bestCost[best]))
                 best = a;
-        if (!forceMid && t.count <= uint32_t(kBuildLeaf) && (best < 0 || bestCost[best] >= boxArea(box, box + 3) * float(t.count)))
-            mode = 0; // leaf
-        else if (best >= 0)
+        if (best >= 0)
         {
             mode     = 1; // SAH split
             axisSel  = best;
@@ -263,11 +262,6 @@ __global__ void __launch_bounds__(kBuildThreads) k_bvh_level(const float* boxes,
             mode = 2; // index midpoint
     }
     __syncthreads();
-    if (mode == 0)
-    {
-        makeLeaf();
-        return;
-    }
     // 4. Stable in-place partition through the scratch copy of the range.
     uint32_t nLeft = t.count / 2;
     if (mode == 1)
@@ -400,40 +394,45 @@ __global__ void k_reorder_tris(const float* positions, const uint32_t* indices, 
     }
 }
 
-} // namespace
+cudaError_t growScratch(void** p, size_t& cap, size_t bytes)
+{
+    if (cap >= bytes)
+        return cudaSuccess;
+    cudaFree(*p);
+    *p  = nullptr;
+    cap = 0;
+    cudaError_t r = cudaMalloc(p, bytes);
+    if (r == cudaSuccess)
+        cap = bytes;
+    return r;
+}
 
-cudaError_t buildBlasGpu(const float* positions, const uint32_t* indices, uint32_t ntri, int maxDepth,
-    GpuBvhScratch& s, BNode* nodes, uint32_t nodeCapacity, float4* tris, int32_t* rootOut, int32_t* depthOut,
-    uint32_t* nodeCountOut, cudaStream_t st)
+// Scratch for n primitives (their boxes are written into s.boxes by the caller).
+cudaError_t reserve(GpuBvhScratch& s, size_t n)
 {
     cudaError_t e;
-    auto grow = [&](void** p, size_t& cap, size_t bytes) -> cudaError_t {
-        if (cap >= bytes)
-            return cudaSuccess;
-        cudaFree(*p);
-        *p  = nullptr;
-        cap = 0;
-        cudaError_t r = cudaMalloc(p, bytes);
-        if (r == cudaSuccess)
-            cap = bytes;
-        return r;
-    };
-    size_t n = ntri;
-    if ((e = grow(reinterpret_cast<void**>(&s.boxes), s.boxesBytes, n * 24)) != cudaSuccess ||
-        (e = grow(reinterpret_cast<void**>(&s.order), s.orderBytes, n * 4)) != cudaSuccess ||
-        (e = grow(reinterpret_cast<void**>(&s.scratch), s.scratchBytes, n * 4)) != cudaSuccess ||
-        (e = grow(reinterpret_cast<void**>(&s.tasksA), s.tasksABytes, (n + 2) * sizeof(BuildTask))) != cudaSuccess ||
-        (e = grow(reinterpret_cast<void**>(&s.tasksB), s.tasksBBytes, (n + 2) * sizeof(BuildTask))) != cudaSuccess ||
-        (e = grow(reinterpret_cast<void**>(&s.counters), s.countersBytes, 64)) != cudaSuccess)
+    if ((e = growScratch(reinterpret_cast<void**>(&s.boxes), s.boxesBytes, n * 24)) != cudaSuccess ||
+        (e = growScratch(reinterpret_cast<void**>(&s.order), s.orderBytes, n * 4)) != cudaSuccess ||
+        (e = growScratch(reinterpret_cast<void**>(&s.scratch), s.scratchBytes, n * 4)) != cudaSuccess ||
+        (e = growScratch(&s.tasksA, s.tasksABytes, (n + 2) * sizeof(BuildTask))) != cudaSuccess ||
+        (e = growScratch(&s.tasksB, s.tasksBBytes, (n + 2) * sizeof(BuildTask))) != cudaSuccess ||
+        (e = growScratch(&s.counters, s.countersBytes, 64)) != cudaSuccess)
         return e;
-    unsigned g = unsigned(std::min<size_t>((n + 255) / 256, 4096));
-    k_tri_boxes<<<g, 256, 0, st>>>(positions, indices, ntri, s.boxes);
-    k_iota<<<g, 256, 0, st>>>(s.order, ntri);
+    return cudaSuccess;
+}
+
+// The level-by-level build over s.boxes (n primitives); s.order ends in leaf order.
+cudaError_t buildLevels(uint32_t n, uint32_t leafMax, int maxDepth, GpuBvhScratch& s, BNode* nodes,
+    uint32_t nodeCapacity, int32_t* rootOut, int32_t* depthOut, uint32_t* nodeCountOut, cudaStream_t st)
+{
+    cudaError_t e;
+    unsigned g = unsigned(std::min<size_t>((size_t(n) + 255) / 256, 4096));
+    k_iota<<<g, 256, 0, st>>>(s.order, n);
     // counters: [0] next task count, [1] node count, [2] root ref, [3] depth seen, [4] error
     uint32_t* cnt = static_cast<uint32_t*>(s.counters);
     if ((e = cudaMemsetAsync(cnt, 0, 64, st)) != cudaSuccess)
         return e;
-    BuildTask root{ 0, ntri, -1, 0, 0 };
+    BuildTask root{ 0, n, -1, 0, 0 };
     BuildTask* cur = static_cast<BuildTask*>(s.tasksA);
     BuildTask* nxt = static_cast<BuildTask*>(s.tasksB);
     if ((e = cudaMemcpyAsync(cur, &root, sizeof root, cudaMemcpyHostToDevice, st)) != cudaSuccess)
@@ -446,7 +445,7 @@ cudaError_t buildBlasGpu(const float* positions, const uint32_t* indices, uint32
         if ((e = cudaMemsetAsync(cnt, 0, 4, st)) != cudaSuccess)
             return e;
         k_bvh_level<<<taskCount, kBuildThreads, 0, st>>>(s.boxes, s.order, s.scratch, cur, nxt, cnt, nodes,
-            cnt + 1, reinterpret_cast<int32_t*>(cnt + 2), cnt + 3, nodeCapacity, maxDepth,
+            cnt + 1, reinterpret_cast<int32_t*>(cnt + 2), cnt + 3, nodeCapacity, maxDepth, leafMax,
             reinterpret_cast<int*>(cnt + 4));
         if ((e = cudaGetLastError()) != cudaSuccess)
             return e;
@@ -461,11 +460,43 @@ cudaError_t buildBlasGpu(const float* positions, const uint32_t* indices, uint32
         return e;
     if (h[4])
         return cudaErrorInvalidValue;
-    k_reorder_tris<<<g, 256, 0, st>>>(positions, indices, s.order, ntri, tris);
     *nodeCountOut = h[1];
     *rootOut      = int32_t(h[2]);
     *depthOut     = int32_t(h[3]);
+    return cudaSuccess;
+}
+
+} // namespace
+
+cudaError_t buildBlasGpu(const float* positions, const uint32_t* indices, uint32_t ntri, int maxDepth,
+    GpuBvhScratch& s, BNode* nodes, uint32_t nodeCapacity, float4* tris, int32_t* rootOut, int32_t* depthOut,
+    uint32_t* nodeCountOut, cudaStream_t st)
+{
+    cudaError_t e = reserve(s, ntri);
+    if (e != cudaSuccess)
+        return e;
+    unsigned g = unsigned(std::min<size_t>((size_t(ntri) + 255) / 256, 4096));
+    k_tri_boxes<<<g, 256, 0, st>>>(positions, indices, ntri, s.boxes);
+    if ((e = buildLevels(ntri, kBlasLeaf, maxDepth, s, nodes, nodeCapacity, rootOut, depthOut, nodeCountOut,
+             st)) != cudaSuccess)
+        return e;
+    k_reorder_tris<<<g, 256, 0, st>>>(positions, indices, s.order, ntri, tris);
     return cudaGetLastError();
+}
+
+cudaError_t buildTlasGpu(const float* boxesHost, uint32_t count, int maxDepth, GpuBvhScratch& s, BNode* nodes,
+    uint32_t nodeCapacity, int32_t* orderOut, int32_t* rootOut, int32_t* depthOut, uint32_t* nodeCountOut,
+    cudaStream_t st)
+{
+    cudaError_t e = reserve(s, count);
+    if (e != cudaSuccess)
+        return e;
+    if ((e = cudaMemcpyAsync(s.boxes, boxesHost, size_t(count) * 24, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return e;
+    if ((e = buildLevels(count, 1, maxDepth, s, nodes, nodeCapacity, rootOut, depthOut, nodeCountOut, st)) !=
+        cudaSuccess)
+        return e;
+    return cudaMemcpyAsync(orderOut, s.order, size_t(count) * 4, cudaMemcpyDeviceToDevice, st);
 }
 
 void freeGpuBvhScratch(GpuBvhScratch& s)

@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <string>
 #include <vector>
@@ -130,6 +131,7 @@ struct agb_context
     uint32_t instanceCount = 0;
     int32_t tlasRoot       = 0;
     int32_t tlasDepth      = 0;
+    uint32_t tlasNodeCount = 0;
 
     agb_environment_data env{};
     int32_t envLight = -1, envBackground = -1;
@@ -725,6 +727,32 @@ AGB_API agb_status agb_geometry_bvh(agb_context* ctx, int32_t geometry, float* n
     return AGB_OK;
 }
 
+AGB_API agb_status agb_tlas_read(agb_context* ctx, float* nodes_out, uint64_t node_capacity,
+    int32_t* order_out, uint64_t order_capacity, int32_t* root, int32_t* depth, uint32_t* node_count)
+{
+    if (!ctx || ctx->parent)
+        return fail(AGB_ERR_INVALID_ARG, "agb_tlas_read: a context with a scene is required");
+    if ((nodes_out && node_capacity < ctx->tlasNodeCount) || (order_out && order_capacity < ctx->instanceCount))
+        return fail(AGB_ERR_INVALID_ARG, "agb_tlas_read: output too small");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    if (nodes_out && ctx->tlasNodeCount)
+        AGB_CUDA(cudaMemcpyAsync(nodes_out, ctx->tlasNodes.ptr, size_t(ctx->tlasNodeCount) * sizeof(BNode),
+                     cudaMemcpyDeviceToHost, ctx->stream), "agb_tlas_read");
+    if (order_out && ctx->instanceCount)
+        AGB_CUDA(cudaMemcpyAsync(order_out, ctx->tlasOrder.ptr, size_t(ctx->instanceCount) * sizeof(int32_t),
+                     cudaMemcpyDeviceToHost, ctx->stream), "agb_tlas_read");
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "agb_tlas_read");
+    if (root)
+        *root = ctx->tlasRoot;
+    if (depth)
+        *depth = ctx->tlasDepth;
+    if (node_count)
+        *node_count = ctx->tlasNodeCount;
+    return AGB_OK;
+}
+
 AGB_API agb_status agb_image_create(agb_context* ctx, const void* pixels, uint32_t width,
     uint32_t height, int32_t format, int32_t linear, int32_t* out_image)
 {
@@ -811,6 +839,7 @@ AGB_API agb_status agb_instances_set(agb_context* ctx, const agb_instance* inst,
     std::vector<DevInstance> di(count);
     std::vector<DevLayer> dl;
     std::vector<std::unique_ptr<DevBuf>> uvs;
+    std::map<std::pair<const float*, size_t>, const float*> uvUploads;
     std::vector<float> boxes(size_t(count) * 6);
     for (uint32_t i = 0; i < count; i++)
     {
@@ -840,14 +869,26 @@ AGB_API agb_status agb_instances_set(agb_context* ctx, const agb_instance* inst,
             const agb_layer& L = s.layers[l];
             if (L.material < 0 || uint32_t(L.material) >= ctx->materialCount || !L.texcoords)
                 return fail(AGB_ERR_INVALID_ARG, "agb_instances_set: bad layer material or UVs");
-            std::unique_ptr<DevBuf> b(new DevBuf());
-            st = upload(ctx, *b, L.texcoords, size_t(g.mesh.vertexCount) * 2 * sizeof(float), "upload layer UVs");
-            if (st)
-                return st;
+            // Instances that share a layer UV array (one per BLAS, typically) share its upload.
+            const size_t bytes = size_t(g.mesh.vertexCount) * 2 * sizeof(float);
+            auto key           = std::make_pair(L.texcoords, bytes);
+            auto hit           = uvUploads.find(key);
+            const float* dev   = nullptr;
+            if (hit != uvUploads.end())
+                dev = hit->second;
+            else
+            {
+                std::unique_ptr<DevBuf> b(new DevBuf());
+                st = upload(ctx, *b, L.texcoords, bytes, "upload layer UVs");
+                if (st)
+                    return st;
+                dev = b->as<float>();
+                uvUploads.emplace(key, dev);
+                uvs.push_back(std::move(b));
+            }
             // Layers are applied outermost first: the reference loops li = count .. 1 over
             // layer index li - 1, so store them in the given order.
-            dl.push_back(DevLayer{ L.material, 0, b->as<float>() });
-            uvs.push_back(std::move(b));
+            dl.push_back(DevLayer{ L.material, 0, dev });
         }
         float* box = &boxes[6 * size_t(i)];
         for (int k = 0; k < 3; k++)
@@ -878,35 +919,61 @@ AGB_API agb_status agb_instances_set(agb_context* ctx, const agb_instance* inst,
             box[3 + k] += pad;
         }
     }
-    BuiltBVH tl;
-    buildBVH2(boxes.data(), count, 1, kTlasMaxDepth, tl);
-    // The traversal enters exactly one instance per TLAS leaf.
-    auto singleLeaf = [](int32_t r) { return r >= 0 || ((uint32_t(~r) & 7u) == 0u); };
-    if (!singleLeaf(tl.root))
-        return fail(AGB_ERR_LIMIT, "agb_instances_set: TLAS leaf with more than one instance");
-    for (const BNode& nd : tl.nodes)
-        if (!singleLeaf(nd.ref.x) || !singleLeaf(nd.ref.y))
-            return fail(AGB_ERR_LIMIT, "agb_instances_set: TLAS leaf with more than one instance");
+    // TLAS depth budget: the traversal stack holds the TLAS path, an instance-exit marker and the
+    // deepest BLAS path.  Near the budget the builders split at the index midpoint, so any tree
+    // with ceil(log2(count)) + 2 levels to spare fits; beyond that the stack cannot hold the scene.
     int maxBlas = 0;
     for (auto& g : ctx->geometries)
         maxBlas = std::max(maxBlas, g->mesh.depth);
-    if (tl.depth + maxBlas + 2 > kStackSize)
-        return fail(AGB_ERR_LIMIT, "agb_instances_set: TLAS + BLAS depth exceeds the traversal stack");
-    std::vector<int32_t> order(tl.order.begin(), tl.order.end());
+    const int tlasBudget = kStackSize - 2 - maxBlas;
+    int need = 0;
+    while ((1u << need) < count)
+        need++;
+    if (count > 1 && need + 2 > tlasBudget)
+        return fail(AGB_ERR_LIMIT, "agb_instances_set: " + std::to_string(count) +
+            " instances need a TLAS deeper than the traversal stack leaves beside the deepest BLAS (" +
+            std::to_string(maxBlas) + " levels)");
     st = upload(ctx, ctx->instances, di.data(), di.size() * sizeof(DevInstance), "upload instances");
-    if (!st && !tl.nodes.empty())
-        st = upload(ctx, ctx->tlasNodes, tl.nodes.data(), tl.nodes.size() * sizeof(BNode), "upload TLAS");
-    if (!st)
-        st = upload(ctx, ctx->tlasOrder, order.data(), order.size() * sizeof(int32_t), "upload TLAS order");
     if (!st && !dl.empty())
         st = upload(ctx, ctx->layers, dl.data(), dl.size() * sizeof(DevLayer), "upload layers");
     if (st)
         return st;
+    int32_t tlasRoot = 0, tlasDepth = 0;
+    uint32_t nodeCount = 0;
+    if (ctx->bvhBuilder == AGB_BVH_GPU && count > 0)
+    {
+        // Binned SAH over the instance boxes on the GPU (the BLAS builder's kernel, one instance
+        // per leaf); nodes and leaf order are written straight into the scene's arrays.
+        AGB_CUDA(ctx->tlasNodes.ensure(std::max<size_t>(1, count) * sizeof(BNode)), "allocate TLAS");
+        AGB_CUDA(ctx->tlasOrder.ensure(size_t(count) * sizeof(int32_t)), "allocate TLAS order");
+        AGB_CUDA(buildTlasGpu(boxes.data(), count, tlasBudget, ctx->bvhScratch, ctx->tlasNodes.as<BNode>(),
+                     std::max<uint32_t>(1, count), ctx->tlasOrder.as<int32_t>(), &tlasRoot, &tlasDepth,
+                     &nodeCount, ctx->stream),
+            "agb_instances_set: GPU TLAS build");
+    }
+    else
+    {
+        BuiltBVH tl;
+        buildBVH2(boxes.data(), count, 1, tlasBudget, tl);
+        std::vector<int32_t> order(tl.order.begin(), tl.order.end());
+        if (!tl.nodes.empty())
+            st = upload(ctx, ctx->tlasNodes, tl.nodes.data(), tl.nodes.size() * sizeof(BNode), "upload TLAS");
+        if (!st)
+            st = upload(ctx, ctx->tlasOrder, order.data(), order.size() * sizeof(int32_t), "upload TLAS order");
+        if (st)
+            return st;
+        tlasRoot  = tl.root;
+        tlasDepth = tl.depth;
+        nodeCount = uint32_t(tl.nodes.size());
+    }
+    if (tlasDepth + maxBlas + 2 > kStackSize)
+        return fail(AGB_ERR_LIMIT, "agb_instances_set: TLAS + BLAS depth exceeds the traversal stack");
     AGB_CUDA(cudaStreamSynchronize(ctx->stream), "upload instances");
     ctx->layerUVs      = std::move(uvs);
     ctx->instanceCount = count;
-    ctx->tlasRoot      = tl.root;
-    ctx->tlasDepth     = tl.depth;
+    ctx->tlasRoot      = tlasRoot;
+    ctx->tlasDepth     = tlasDepth;
+    ctx->tlasNodeCount = nodeCount;
     return AGB_OK;
 }
 
@@ -1317,6 +1384,38 @@ AGB_API agb_status agb_accum_read(agb_context* ctx, int32_t mode, float* host_rg
     AGB_CUDA(cudaMemcpyAsync(host_rgba, src, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream),
         "read accumulation");
     AGB_CUDA(cudaStreamSynchronize(ctx->stream), "read accumulation");
+    if (mode == AGB_ACCUM_KAHAN && ctx->accumulatedSamples)
+    {
+        float inv = 1.f / float(ctx->accumulatedSamples);
+        for (size_t i = 0; i < n; i++)
+            host_rgba[i] *= inv;
+    }
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_accum_read_rect(agb_context* ctx, int32_t mode, uint32_t x0, uint32_t y0,
+    uint32_t width, uint32_t height, float* host_rgba, uint64_t capacity_floats)
+{
+    if (!ctx || !host_rgba || !ctx->accMean.ptr)
+        return fail(AGB_ERR_NOT_READY, "agb_accum_read_rect: nothing rendered");
+    if (width == 0 || height == 0 || uint64_t(x0) + width > ctx->accW || uint64_t(y0) + height > ctx->accH)
+        return fail(AGB_ERR_INVALID_ARG, "agb_accum_read_rect: rectangle outside the image");
+    size_t n = size_t(width) * height * 4;
+    if (capacity_floats < n)
+        return fail(AGB_ERR_INVALID_ARG, "agb_accum_read_rect: buffer too small");
+    if (mode != AGB_ACCUM_RUNNING_MEAN && mode != AGB_ACCUM_KAHAN)
+        return fail(AGB_ERR_INVALID_ARG, "agb_accum_read_rect: bad mode");
+    if (!(ctx->lastAccumMode & uint32_t(mode)))
+        return fail(AGB_ERR_NOT_READY, "agb_accum_read_rect: mode was not accumulated");
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    const float4* src = (mode == AGB_ACCUM_KAHAN ? ctx->accSum.as<float4>() : ctx->accMean.as<float4>()) +
+        size_t(y0) * ctx->accW + x0;
+    AGB_CUDA(cudaMemcpy2DAsync(host_rgba, size_t(width) * sizeof(float4), src, size_t(ctx->accW) * sizeof(float4),
+                 size_t(width) * sizeof(float4), height, cudaMemcpyDeviceToHost, ctx->stream),
+        "read accumulation rectangle");
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "read accumulation rectangle");
     if (mode == AGB_ACCUM_KAHAN && ctx->accumulatedSamples)
     {
         float inv = 1.f / float(ctx->accumulatedSamples);

@@ -250,6 +250,11 @@ struct GpuBvhScratch
 cudaError_t buildBlasGpu(const float* positions, const uint32_t* indices, uint32_t ntri, int maxDepth,
     GpuBvhScratch& s, BNode* nodes, uint32_t nodeCapacity, float4* tris, int32_t* rootOut, int32_t* depthOut,
     uint32_t* nodeCountOut, cudaStream_t st);
+// TLAS over count instance boxes (6 floats each, host memory; staged through the scratch): one
+// instance per leaf; orderOut (device, count entries) gets the instance index of each leaf slot.
+cudaError_t buildTlasGpu(const float* boxesHost, uint32_t count, int maxDepth, GpuBvhScratch& s, BNode* nodes,
+    uint32_t nodeCapacity, int32_t* orderOut, int32_t* rootOut, int32_t* depthOut, uint32_t* nodeCountOut,
+    cudaStream_t st);
 void freeGpuBvhScratch(GpuBvhScratch& s);
 
 // agb_unit.cu

@@ -30,7 +30,9 @@ constexpr int kStackSize = AGB_STACK_ENTRIES; // entries per thread; the BVH bui
 // The first kSmemStack entries live in shared memory, the rest in local memory: a smaller shared
 // stack leaves more of the SM's combined L1 / shared storage to the L1 cache.
 constexpr int kSmemStack = AGB_SMEM_STACK < AGB_STACK_ENTRIES ? AGB_SMEM_STACK : AGB_STACK_ENTRIES;
-// Depth budgets: TLAS depth 12, one instance-exit marker, one spare entry.
+// Depth budgets: a BLAS is built at most kBlasMaxDepth deep, which leaves at least kTlasMaxDepth
+// levels of the stack to the TLAS beside one instance-exit marker and a spare entry; the TLAS
+// builder takes whatever the deepest BLAS of the scene leaves (agb_instances_set).
 constexpr int kTlasMaxDepth = 12;
 constexpr int kBlasMaxDepth = kStackSize - kTlasMaxDepth - 2;
 

@@ -13,9 +13,12 @@ and the CPU oracle render byte-identical inputs on any machine.
                       instanced 64x with random rigid transforms in a 100^3 box; coat ~ U[0,1],
                       transmission 1 (IOR 1.5) on 10% of instances; 2048x1024 RGB32F environment
                       with log-normal(0, 2) texels plus 4 sun-like hot spots.
-  config_layered    : stress with layered materials: distinct BLASes instanced many times, each
-                      instance with a base material and an alpha-masked decal layer (RGBA8 noise
-                      texture), progressive accumulation (sizes are parameters).
+  config_layered    : layered materials at small sizes (parity tests): distinct BLASes instanced
+                      several times, each instance with a base material and an alpha-masked decal
+                      layer (RGBA8 noise texture).
+  config_stress     : plain method, stress with layered materials and accumulation (3840x2160,
+                      progressive to 4096 spp): 16 BLAS of 10K-500K triangles, 1000 instances with
+                      a decal layer each (1024^2 RGBA8 noise texture).
 """
 import math
 
@@ -157,6 +160,46 @@ def icosphere(level, radius=1.0, displacement=0.0, seed=0):
     u = np.arctan2(dirs[:, 0], -dirs[:, 2]) / (2 * math.pi) + 0.5
     v = -np.arcsin(np.clip(dirs[:, 1], -1, 1)) / math.pi + 0.5
     uv = np.stack([u, v], axis=1)
+    return (pos.astype(np.float32), nrm.astype(np.float32), uv.astype(np.float32),
+            tris.astype(np.uint32).reshape(-1))
+
+
+def lumpy_sphere(target_triangles, radius=1.0, displacement=0.0, seed=0):
+    """UV sphere of about `target_triangles` triangles (segments = 2 x rings), vertices displaced
+    radially by radius * N(0, displacement) (the seam column and each pole share one value, so the
+    surface stays closed); normals are area-weighted face normals.  Vectorised: 500K triangles in
+    well under a second."""
+    seg = max(8, int(round(math.sqrt(target_triangles) + 1.0)))
+    seg += seg % 2
+    rings = seg // 2
+    v = np.arange(rings + 1) / rings
+    u = np.arange(seg + 1) / seg
+    theta = v[:, None] * math.pi
+    phi = u[None, :] * 2.0 * math.pi
+    dirs = np.stack([np.sin(theta) * np.cos(phi), np.cos(theta) * np.ones_like(phi),
+                     np.sin(theta) * np.sin(phi)], axis=-1)
+    rng = np.random.default_rng(seed)
+    d = rng.normal(0.0, displacement, (rings + 1, seg)) if displacement else np.zeros((rings + 1, seg))
+    d[0, :] = d[0, 0]
+    d[-1, :] = d[-1, 0]
+    d = np.concatenate([d, d[:, :1]], axis=1)
+    pos = (dirs * (radius * (1.0 + d))[..., None]).reshape(-1, 3)
+    uv = np.stack(np.broadcast_arrays(u[None, :], v[:, None]), axis=-1).reshape(-1, 2)
+    row = seg + 1
+    r, c = np.meshgrid(np.arange(rings), np.arange(seg), indexing="ij")
+    a = r * row + c
+    b = a + row
+    t1 = np.stack([a, b, a + 1], axis=-1)[r != 0]
+    t2 = np.stack([a + 1, b, b + 1], axis=-1)[r != rings - 1]
+    tris = np.concatenate([t1, t2]).astype(np.int64)
+    e1 = pos[tris[:, 1]] - pos[tris[:, 0]]
+    e2 = pos[tris[:, 2]] - pos[tris[:, 0]]
+    fn = np.cross(e1, e2)
+    nrm = np.zeros_like(pos)
+    for k in range(3):
+        np.add.at(nrm, tris[:, k], fn)
+    ln = np.linalg.norm(nrm, axis=1, keepdims=True)
+    nrm = np.where(ln > 0, nrm / np.maximum(ln, 1e-30), dirs.reshape(-1, 3))
     return (pos.astype(np.float32), nrm.astype(np.float32), uv.astype(np.float32),
             tris.astype(np.uint32).reshape(-1))
 
@@ -464,6 +507,50 @@ def config_layered(seed=0, width=960, height=540, spp=64, trace_depth=5, blas=4,
     s.env_background = img
     s.width, s.height, s.spp = width, height, spp
     view = look_at((0.0, 15.0, 60.0), (0.0, 0.0, 0.0))
+    proj = perspective(45.0, width / height)
+    s.frame = frame_data(view, proj, trace_depth=trace_depth, scene_bounds=s.bounds())
+    return s
+
+
+def config_stress(seed=0, width=3840, height=2160, spp=4096, trace_depth=5, blas=16, instances=1000,
+                  tri_range=(10_000, 500_000), decal_size=1024, box=120.0):
+    """Plain method, stress with layered materials and accumulation, at the stated shape by
+    default: `blas` distinct BLASes whose triangle counts are evenly spaced over `tri_range`
+    (16 x 10K-500K: 4.08M unique triangles -- the per-BLAS range caps the total at 8M, below the
+    "~20M" the configuration also names), `instances` instances with random rigid transforms in a
+    `box`^3 volume, each with a base Standard Surface material and an alpha-masked decal layer (a
+    `decal_size`^2 RGBA8 noise colour texture and its mask), 3840x2160, accumulated progressively
+    to `spp` samples (Kahan-compensated sums).  Smaller sizes keep the same structure for tests."""
+    s = SceneDesc(f"stress: {blas} BLAS x {instances} instances with decal layers, {width}x{height}")
+    rng = np.random.default_rng(seed)
+    counts = np.linspace(tri_range[0], tri_range[1], blas).round().astype(int) if blas > 1 else \
+        np.array([tri_range[0]])
+    meshes = [s.add_mesh(*lumpy_sphere(int(c), radius=2.0, displacement=0.005, seed=seed + 100 + b))
+              for b, c in enumerate(counts)]
+    rgba, opacity = noise_decal(decal_size, seed + 3)
+    color_img = s.add_image(rgba, _abi.FORMAT_RGBA8, linear=True)
+    mask_img = s.add_image(opacity, _abi.FORMAT_RGBA8, linear=True)
+    s.materials = materials(instances + 1)
+    s.materials["base_color"][:instances] = rng.uniform(0.1, 0.9, (instances, 3))
+    s.materials["metalness"][:instances] = (rng.uniform(size=instances) < 0.3).astype(np.float32)
+    s.materials["specular_roughness"][:instances] = rng.uniform(0.05, 0.6, instances)
+    decal = instances
+    s.materials["has_base_color_image"][decal] = 1
+    s.materials["has_opacity_image"][decal] = 1
+    s.textures = no_textures(instances + 1)
+    s.textures["image"][decal, _abi.TEX_BASE_COLOR] = color_img
+    s.textures["image"][decal, _abi.TEX_OPACITY] = mask_img
+    layer_uv = [np.ascontiguousarray(s.meshes[m]["texcoords"] * np.float32(3.0), np.float32) for m in meshes]
+    for k in range(instances):
+        b = int(rng.integers(0, blas))
+        s.instances.append(dict(mesh=meshes[b], material=k, xform=random_rigid(rng, box),
+                                layers=[(decal, layer_uv[b])]))
+    img = s.add_image(hdr_env(256, 128, seed + 4, sigma=1.0, suns=2, sun_radiance=500.0,
+                              sun_radius=2.0), _abi.FORMAT_RGB32F)
+    s.env_light = img
+    s.env_background = img
+    s.width, s.height, s.spp = width, height, spp
+    view = look_at((0.0, 0.25 * box, 1.4 * box), (0.0, 0.0, 0.0))
     proj = perspective(45.0, width / height)
     s.frame = frame_data(view, proj, trace_depth=trace_depth, scene_bounds=s.bounds())
     return s

@@ -42,7 +42,14 @@ def parse_args():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--config", default="large", choices=["large", "small"])
+    p.add_argument("--config", default="large", choices=["large", "small", "stress"],
+                   help="large: the headline configuration; small: the CPU-runnable one; stress: "
+                        "3840x2160 layered-material progressive accumulation (a step = one "
+                        "progressive call of --stress-chunk samples, default 64 steps = 4096 spp)")
+    p.add_argument("--stress-chunk", type=int, default=64)
+    p.add_argument("--stress-crop", type=int, default=32,
+                   help="side of the centred square the FP64 oracle renders at the full sample count "
+                        "for the stress configuration's relMSE series (0: skip)")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -248,6 +255,8 @@ def make_scene(name, res=None, spp=None):
         kw.update(spp=spp)
     if name == "small":
         return scenes.config_small(seed=0, **kw)
+    if name == "stress":
+        return scenes.config_stress(seed=0, **kw)
     return scenes.config_large(seed=0, **kw)
 
 
@@ -375,6 +384,112 @@ def rel_mse_vs_fp64_oracle(s, img, rows, threads=None):
             "oracle_seconds": secs}
 
 
+def run_stress(args):
+    """Stress configuration (3840x2160; 16 BLAS of 10K-500K triangles, 1000 instances with a decal
+    layer; Kahan-compensated progressive accumulation).  Warm-up: W calls of one chunk from sample
+    0.  Timed: K progressive calls of `--stress-chunk` samples continuing the accumulation (the
+    default K = 64 reaches 4096 spp); per call the frame data goes up from pinned host memory and the
+    whole running image (Kahan sum / n) comes back into pinned host memory, both inside the e2e wall
+    time; `value` is from CUDA events around the renders alone.  After every call the relMSE of a
+    centred crop against the FP64 oracle's render of the same crop at the full sample count (the
+    same sample streams) is recorded: the convergence series."""
+    import torch
+    from aurora_gb300 import _abi, api, build
+    build.build()
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    chunk, steps = args.stress_chunk, args.steps
+    total = chunk * steps
+    t0 = time.perf_counter()
+    s = make_scene("stress", args.res, total)
+    gen_s = time.perf_counter() - t0
+    stream = torch.cuda.Stream()
+    r = api.Renderer(local, stream=stream.cuda_stream)
+    t0 = time.perf_counter()
+    r.upload(s)
+    upload_s = time.perf_counter() - t0
+    acc = _abi.ACCUM_KAHAN | _abi.ACCUM_RUNNING_MEAN
+    for _ in range(args.warmup):
+        r.render(0, chunk, accumulation=acc, max_paths=args.max_paths)
+    r.set_profiling(True)
+    frame_host = torch.from_numpy(np.frombuffer(np.ascontiguousarray(s.frame).tobytes(),
+                                                np.uint8).copy()).pin_memory()
+    frame_np = frame_host.numpy().view(_abi.FRAME_DTYPE)
+    img_host = torch.empty((s.height, s.width, 4), dtype=torch.float32).pin_memory()
+    img_np = img_host.numpy()
+    c = args.stress_crop
+    x0, y0 = s.width // 2 - c // 2, s.height // 2 - c // 2
+    crops = []
+    clocks = ClockSampler(local)
+    torch.cuda.synchronize()
+    clocks.start()
+    render_ms, launches = 0.0, 0
+    kernel_ms = {k: 0.0 for k in _abi.KERNEL_FAMILIES}
+    wall0 = time.perf_counter()
+    for k in range(steps):
+        r.set_frame(frame_np)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = r.render(k * chunk, chunk, accumulation=acc, stats=True, max_paths=args.max_paths)
+        e1.record(stream)
+        r.read(_abi.ACCUM_KAHAN, out=img_np)
+        e1.synchronize()
+        render_ms += e0.elapsed_time(e1)
+        launches += st["kernel_launches"]
+        for f in _abi.KERNEL_FAMILIES:
+            kernel_ms[f] += st["kernel_ms"][f]
+        if c > 0:
+            crops.append(img_np[y0:y0 + c, x0:x0 + c].copy())
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    paths = s.width * s.height * total
+    out = {
+        "metric": METRIC, "value": paths / (render_ms / 1000.0), "unit": UNIT, "n_gpus": 1,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": render_ms / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "plain method, stress with layered materials and accumulation: 16 BLAS "
+                               "of 10K-500K triangles (4.09M unique), 1000 instances with an "
+                               "alpha-masked decal layer (1024^2 RGBA8), 3840x2160, progressive to "
+                               f"{total} spp, Kahan-compensated FP32",
+                   "width": s.width, "height": s.height, "spp": total, "chunk_spp": chunk,
+                   "trace_depth": int(s.frame["trace_depth"]), "unique_triangles": s.unique_triangles,
+                   "instances": len(s.instances), "instanced_triangles": s.triangle_count,
+                   "seed": 0, "l2": "inputs larger than L2 (scene and wave state)",
+                   "scene_generation_s": gen_s, "upload_and_build_s": upload_s},
+        "e2e": {"value": paths / wall, "unit": UNIT,
+                "h2d_bytes_per_step": int(_abi.FRAME_DTYPE.itemsize),
+                "d2h_bytes_per_step": int(s.width * s.height * 16), "ms_per_step": 1000.0 * wall / steps},
+        "gpu_launches": int(launches),
+        "kernel_ms_per_step": {f: v / steps for f, v in kernel_ms.items()},
+        "clocks": clk,
+    }
+    r.close()
+    if c > 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+        o = pyoracle.OracleScene(s)
+        rect = (x0, y0, x0 + c, y0 + c)
+        t0 = time.perf_counter()
+        half = total // 2
+        a = o.render(0, half, precision=64, want_sum=True, want_mean=False, rect=rect)["sum"]
+        b = o.render(half, total - half, precision=64, want_sum=True, want_mean=False, rect=rect)["sum"]
+        oracle_s = time.perf_counter() - t0
+        o.close()
+        ref = ((a + b) / total)[y0:y0 + c, x0:x0 + c]
+        noise = pyoracle.rel_mse(a[y0:y0 + c, x0:x0 + c] / half,
+                                 b[y0:y0 + c, x0:x0 + c] / (total - half)) / 4
+        series = [[chunk * (k + 1), pyoracle.rel_mse(img, ref)] for k, img in enumerate(crops)]
+        out["rel_mse_vs_fp64_oracle"] = {
+            "series": series, "eps": 1e-2, "every_spp": chunk, "crop": list(rect),
+            "reference": f"FP64 oracle, the same {total} sample streams",
+            "reference_noise_rel_mse": noise, "final": series[-1][1],
+            "first_spp_within_1e-3": next((n for n, e in series if e <= 1e-3), None),
+            "oracle_seconds": oracle_s}
+    print(json.dumps(out))
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -414,6 +529,9 @@ def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.config == "stress":
+        run_stress(args)
         return
     rank, world, local = dist_env()
     import torch

@@ -358,9 +358,14 @@ AGB_API agb_status agb_geometry_create(agb_context* ctx, const float* positions,
     const float* normals, const float* texcoords, const uint32_t* indices, uint32_t vertex_count,
     uint32_t index_count, int32_t* out_geometry);
 
-/* BLAS builder used by agb_geometry_create: AGB_BVH_GPU (default) builds on the GPU (binned SAH,
- * breadth-first, one CTA per node); AGB_BVH_HOST builds on the host (binned SAH, depth first).
- * Both produce the same node layout and depth bound; any valid BVH gives the same hits. */
+/* BVH builder used by agb_geometry_create (BLAS) and agb_instances_set (TLAS; replaces the
+ * acceleration-structure builds the reference hands to the driver, HGI/HGIGeometry.cpp:127-160,
+ * HGI/HGIScene.cpp:377-420): AGB_BVH_GPU (default) builds on the GPU (binned SAH, breadth-first,
+ * one CTA per node); AGB_BVH_HOST builds on the host (binned SAH, depth first).  The TLAS has one
+ * instance per leaf and takes the depth the deepest BLAS leaves on the traversal stack (splits
+ * fall back to the index midpoint near that budget); a scene whose instance count needs more
+ * levels than that is refused with AGB_ERR_LIMIT.  Both builders produce the same node layout
+ * and depth bound; any valid BVH gives the same hits. */
 enum
 {
     AGB_BVH_HOST = 0,
@@ -375,6 +380,12 @@ AGB_API agb_status agb_set_bvh_builder(agb_context* ctx, int32_t builder);
 AGB_API agb_status agb_geometry_bvh(agb_context* ctx, int32_t geometry, float* nodes_out,
     uint64_t node_capacity, float* tris_out, uint64_t tri_capacity, int32_t* root, int32_t* depth,
     uint32_t* node_count);
+
+/* Reads the context's TLAS back (tests, tools): nodes as agb_geometry_bvh writes them, the
+ * instance index of each leaf slot (a leaf ref ~(slot << 3) names slot), root ref, depth, node
+ * count.  Either array may be null.  No reference counterpart (the driver owns its TLAS). */
+AGB_API agb_status agb_tlas_read(agb_context* ctx, float* nodes_out, uint64_t node_capacity,
+    int32_t* order_out, uint64_t order_capacity, int32_t* root, int32_t* depth, uint32_t* node_count);
 
 /* Uploads an image (material texture or environment).  Host pixels, rows top to bottom.
  * linear: 1 bilinear, 0 nearest filtering (repeat addressing). */
@@ -465,6 +476,10 @@ AGB_API agb_status agb_wait(agb_context* ctx);
  * mode: AGB_ACCUM_RUNNING_MEAN reads the running mean; AGB_ACCUM_KAHAN reads sum / count. */
 AGB_API agb_status agb_accum_read(agb_context* ctx, int32_t mode, float* host_rgba,
     uint64_t capacity_floats);
+/* The same for a rectangle of the image (x0, y0, width, height), rows top to bottom: progressive
+ * callers that track part of a large frame read only that part (no reference counterpart). */
+AGB_API agb_status agb_accum_read_rect(agb_context* ctx, int32_t mode, uint32_t x0, uint32_t y0,
+    uint32_t width, uint32_t height, float* host_rgba, uint64_t capacity_floats);
 /* Device pointer to the accumulation buffer of a mode (RGBA32F, width*height*4 floats). */
 AGB_API agb_status agb_accum_device(agb_context* ctx, int32_t mode, float** device_rgba);
 /* Per-sample output of the last rendered sample (RGBA32F device buffer), like gResult. */

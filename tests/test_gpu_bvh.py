@@ -139,3 +139,86 @@ def test_gpu_bvh_build_time_1m_triangles(agb):
     print(f"1.31M-triangle BLAS: host {out[_abi.BVH_HOST] * 1e3:.0f} ms, gpu {out[_abi.BVH_GPU] * 1e3:.0f} ms "
           f"(both include the upload)")
     assert out[_abi.BVH_GPU] < out[_abi.BVH_HOST]
+
+
+def read_tlas(r):
+    lib = r._lib
+    root, depth, nn = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_uint32()
+    _abi.check(lib.agb_tlas_read(r.ctx, None, 0, None, 0, ctypes.byref(root), ctypes.byref(depth),
+                                 ctypes.byref(nn)))
+    n = len(r.scene.instances)
+    nodes = np.zeros((max(nn.value, 1), 16), np.float32)
+    order = np.zeros(n, np.int32)
+    _abi.check(lib.agb_tlas_read(r.ctx, nodes.ctypes.data, nodes.shape[0], order.ctypes.data, n,
+                                 None, None, None))
+    return nodes[:nn.value], order, root.value, depth.value
+
+
+def check_tlas(s, nodes, order, root, depth):
+    """One instance per leaf, every instance in exactly one leaf, each leaf box containing its
+    instance's world-space vertices, each interior box containing its children's, depth as
+    reported."""
+    n = len(s.instances)
+    assert sorted(order.tolist()) == list(range(n))
+    world = []
+    for inst in s.instances:
+        p = s.meshes[inst["mesh"]]["positions"].astype(np.float64)
+        m = np.asarray(inst["xform"], np.float64).reshape(3, 4)
+        w = p @ m[:, :3].T + m[:, 3]
+        world.append((w.min(0), w.max(0)))
+    refs = nodes[:, 12:14].view(np.int32) if len(nodes) else np.zeros((0, 2), np.int32)
+    seen = np.zeros(n, np.int32)
+    max_depth = [0]
+
+    def visit(ref, d, lo_box, hi_box):
+        max_depth[0] = max(max_depth[0], d)
+        if ref < 0:
+            code = ~ref
+            slot, count = code >> 3, (code & 7) + 1
+            assert count == 1
+            inst = order[slot]
+            seen[inst] += 1
+            if lo_box is not None:
+                lo, hi = world[inst]
+                assert (lo_box <= lo + 1e-4 * (1 + np.abs(lo))).all() and \
+                    (hi_box >= hi - 1e-4 * (1 + np.abs(hi))).all()
+            return
+        nd = nodes[ref]
+        boxes = [(np.array([nd[0], nd[2], nd[8]]), np.array([nd[1], nd[3], nd[9]])),
+                 (np.array([nd[4], nd[6], nd[10]]), np.array([nd[5], nd[7], nd[11]]))]
+        for side in (0, 1):
+            lo, hi = boxes[side]
+            if lo_box is not None:
+                assert (lo >= lo_box).all() and (hi <= hi_box).all()
+            visit(int(refs[ref][side]), d + 1, lo, hi)
+
+    visit(root, 0, None, None)
+    assert (seen == 1).all()
+    assert max_depth[0] == depth
+
+
+@pytest.mark.parametrize("instances", [1, 2, 1000, 5000])
+def test_tlas_gpu_and_host_valid_and_render_identically(agb, oracle, instances):
+    """TLAS over many instances built by the GPU builder (the BLAS kernel over instance boxes) and
+    by the host builder: both valid; renders through either identical to each other and to the
+    oracle; 5000 instances need more than the former fixed 12-level TLAS budget."""
+    from aurora_gb300 import api, scenes
+    s = scenes.config_stress(width=64, height=48, spp=2, blas=3, instances=instances,
+                             tri_range=(200, 2000), decal_size=64, box=60.0 if instances > 2 else 6.0)
+    imgs, depths = [], []
+    for builder in (_abi.BVH_HOST, _abi.BVH_GPU):
+        with api.Renderer() as r:
+            _abi.check(r._lib.agb_set_bvh_builder(r.ctx, builder))
+            r.upload(s)
+            nodes, order, root, depth = read_tlas(r)
+            check_tlas(s, nodes, order, root, depth)
+            depths.append(depth)
+            r.render(0, s.spp)
+            imgs.append(r.read(_abi.ACCUM_RUNNING_MEAN))
+    o = oracle.OracleScene(s).render(0, s.spp)["mean"]
+    print(f"{instances} instances: TLAS depth host {depths[0]} gpu {depths[1]}; relMSE vs oracle "
+          f"{oracle.rel_mse(imgs[1], o):.3g}")
+    np.testing.assert_array_equal(imgs[0], imgs[1])
+    assert oracle.rel_mse(imgs[1], o) < 1e-9
+    if instances == 5000:
+        assert depths[1] > 12

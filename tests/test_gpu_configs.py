@@ -80,3 +80,33 @@ def test_large_config_band_at_stated_shape(agb, oracle):
     assert err32 < FP32_BAR
     assert np.isfinite(err64)
     assert lit > 0.9
+
+
+def test_stress_config_crop_at_stated_shape(agb, oracle):
+    """Stress configuration at its stated shape (3840x2160; 16 BLAS of 10K-500K triangles, 1000
+    instances with an alpha-masked decal layer on a 1024^2 RGBA8 texture each): the whole frame at
+    2 spp on the device, a 64x48 crop of it against the FP32 oracle (relMSE below 1e-9) with the
+    FP64 oracle's relMSE printed."""
+    from aurora_gb300 import scenes
+    s = scenes.config_stress(spp=2)
+    assert (s.width, s.height, len(s.instances), len(s.meshes)) == (3840, 2160, 1000, 16)
+    tri = [len(m["indices"]) // 3 for m in s.meshes]
+    assert min(tri) >= 10_000 * 0.98 and max(tri) <= 500_000 * 1.02
+    assert s.images[0]["width"] == s.images[0]["height"] == 1024
+    spp = 2
+    g, gk = gpu_render(s, spp)
+    x0, y0 = s.width // 2 - 32, s.height // 2 - 24
+    rect = (x0, y0, x0 + 64, y0 + 48)
+    o = oracle.OracleScene(s)
+    o32 = o.render(0, spp, precision=32, want_sum=True, rect=rect)
+    o64 = o.render(0, spp, precision=64, want_sum=True, rect=rect)
+    o.close()
+    crop = (slice(y0, y0 + 48), slice(x0, x0 + 64))
+    err32 = oracle.rel_mse(g[crop], o32["mean"][crop])
+    same = np.mean(np.all(g[crop] == o32["mean"][crop], axis=2))
+    err64 = oracle.rel_mse(gk[crop], o64["sum"][crop] / spp)
+    print(f"stress 3840x2160 crop {rect} at {spp} spp: relMSE vs FP32 oracle {err32:.3g} "
+          f"(identical pixels {same:.5f}), vs FP64 oracle {err64:.3g}")
+    assert err32 < FP32_BAR
+    assert np.isfinite(err64)
+    assert g[crop][..., :3].max() > 0
