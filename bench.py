@@ -48,8 +48,9 @@ def parse_args():
                         "progressive call of --stress-chunk samples, default 64 steps = 4096 spp)")
     p.add_argument("--stress-chunk", type=int, default=64)
     p.add_argument("--stress-crop", type=int, default=32,
-                   help="side of the centred square the FP64 oracle renders at the full sample count "
-                        "for the stress configuration's relMSE series (0: skip)")
+                   help="side of the square (centred on the instance nearest the middle of the frame) "
+                        "the FP64 oracle renders at the full sample count for the stress "
+                        "configuration's relMSE series (0: skip)")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -384,6 +385,25 @@ def rel_mse_vs_fp64_oracle(s, img, rows, threads=None):
             "oracle_seconds": secs}
 
 
+def stress_crop_origin(s, c):
+    """Top-left corner of a c x c crop centred on the projection of the instance whose centre
+    projects nearest to the middle of the frame (in front of the camera), so the crop sees
+    geometry, not only the environment."""
+    vp = np.asarray(s.frame["camera_view_proj"], np.float64).reshape(4, 4).T
+    best, where = None, (s.width // 2, s.height // 2)
+    for inst in s.instances:
+        m = np.asarray(inst["xform"], np.float64).reshape(3, 4)
+        q = vp @ np.append(m[:, 3], 1.0)
+        if q[3] <= 0:
+            continue
+        x = (q[0] / q[3] * 0.5 + 0.5) * s.width
+        y = (0.5 - q[1] / q[3] * 0.5) * s.height
+        d = (x - s.width / 2) ** 2 + (y - s.height / 2) ** 2
+        if c / 2 <= x <= s.width - c / 2 and c / 2 <= y <= s.height - c / 2 and (best is None or d < best):
+            best, where = d, (int(x), int(y))
+    return where[0] - c // 2, where[1] - c // 2
+
+
 def run_stress(args):
     """Stress configuration (3840x2160; 16 BLAS of 10K-500K triangles, 1000 instances with a decal
     layer; Kahan-compensated progressive accumulation).  Warm-up: W calls of one chunk from sample
@@ -418,7 +438,7 @@ def run_stress(args):
     img_host = torch.empty((s.height, s.width, 4), dtype=torch.float32).pin_memory()
     img_np = img_host.numpy()
     c = args.stress_crop
-    x0, y0 = s.width // 2 - c // 2, s.height // 2 - c // 2
+    x0, y0 = stress_crop_origin(s, c)
     crops = []
     clocks = ClockSampler(local)
     torch.cuda.synchronize()
