@@ -218,6 +218,11 @@ SIGNATURES = {
     "agb_frame_set": (_I32, [_P, _P]),
     "agb_render": (_I32, [_P, ctypes.POINTER(RenderOptions), _U32, _U32, ctypes.POINTER(RenderStats)]),
     "agb_wait": (_I32, [_P]),
+    "agb_batch_create": (_I32, [_I32, _P, _U64, ctypes.POINTER(_P)]),
+    "agb_batch_destroy": (_I32, [_P]),
+    "agb_batch_render": (_I32, [_P, _P, _P, _P, _P, _U32, _P]),
+    "agb_batch_poll": (_I32, [_P]),
+    "agb_batch_set_profiling": (_I32, [_P, _I32]),
     "agb_accum_read_rect": (_I32, [_P, _I32, _U32, _U32, _U32, _U32, _P, _U64]),
     "agb_accum_read": (_I32, [_P, _I32, _P, _U64]),
     "agb_accum_device": (_I32, [_P, _I32, ctypes.POINTER(_P)]),

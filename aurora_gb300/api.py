@@ -231,6 +231,67 @@ def bsdf_batch(op, mats_ptr, idx_ptr, frames_ptr, v_ptr, l_ptr, rnd_ptr, n, out_
                                    vp(out_pdf), vp(out_lobe), stream))
 
 
+class View(Renderer):
+    """A view of an uploaded Renderer's scene (agb_view_create): its own stream, frame data and
+    render buffers; destroy views before their Renderer."""
+
+    def __init__(self, renderer, stream=None):
+        self._lib = library()
+        h = ctypes.c_void_p()
+        check(self._lib.agb_view_create(renderer.ctx, stream, ctypes.byref(h)))
+        self.ctx = h
+        self.scene = renderer.scene
+        self._keep = []
+
+
+class Batch:
+    """Batched rendering (agb_batch_*): several views or renderers, of one or several scenes and
+    resolutions, rendered by one wavefront (one launch per stage for all of them)."""
+
+    def __init__(self, max_paths=1 << 24, device=0, stream=None):
+        self._lib = library()
+        self.handle = ctypes.c_void_p()
+        check(self._lib.agb_batch_create(device, stream, int(max_paths), ctypes.byref(self.handle)))
+
+    def close(self):
+        if self.handle:
+            self._lib.agb_batch_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def render(self, items, stats=False):
+        """items: dicts with keys view (a Renderer or View with its frame set), width, height, spp,
+        and optionally start (0), seed_offset (0), accumulation (running mean | Kahan)."""
+        n = len(items)
+        views = (ctypes.c_void_p * n)(*[it["view"].ctx.value if isinstance(it["view"].ctx, ctypes.c_void_p)
+                                        else it["view"].ctx for it in items])
+        opts = (_abi.RenderOptions * n)()
+        starts = (ctypes.c_uint32 * n)()
+        counts = (ctypes.c_uint32 * n)()
+        for k, it in enumerate(items):
+            opts[k].width, opts[k].height = it["width"], it["height"]
+            opts[k].accumulation = it.get("accumulation", _abi.ACCUM_RUNNING_MEAN | _abi.ACCUM_KAHAN)
+            opts[k].seed_offset = it.get("seed_offset", 0)
+            starts[k] = it.get("start", 0)
+            counts[k] = it["spp"]
+        st = _abi.RenderStats() if stats else None
+        check(self._lib.agb_batch_render(self.handle, views, opts, starts, counts, n,
+                                         ctypes.byref(st) if st is not None else None))
+        if stats:
+            out = {f: getattr(st, f) for f, _ in _abi.RenderStats._fields_}
+            out["kernel_ms"] = dict(zip(_abi.KERNEL_FAMILIES, list(st.kernel_ms)))
+            return out
+        return None
+
+    def poll(self):
+        return self._lib.agb_batch_poll(self.handle) == _abi.AGB_OK
+
+
 class Server:
     """The serving loop (agb_server_*): register uploaded Renderers as scenes, submit requests,
     wait for their images and latencies."""

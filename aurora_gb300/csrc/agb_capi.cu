@@ -1,6 +1,7 @@
 // C ABI of the GB300 path-tracing backend (include/agb.h): context, scene upload, environment,
 // rendering, readback.  All inputs are validated on the host before any kernel sees them, so no
 // kernel indexes memory with an unchecked value.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -146,6 +147,14 @@ struct agb_context
 
     agb_frame_data frame{};
     bool frameSet = false;
+
+    // Host mirrors of the scene tables (batched rendering builds the shared namespace from them)
+    // and a counter bumped by every scene change.
+    std::vector<DevInstance> hostInstances;
+    std::vector<DevLayer> hostLayers;
+    std::vector<agb_material> hostMaterials;
+    std::vector<agb_material_textures> hostMatTex;
+    uint64_t sceneVersion = 0;
 
     // Wave buffers.
     size_t pathCapacity = 0;
@@ -498,6 +507,8 @@ AGB_API agb_status agb_geometry_create(agb_context* ctx, const float* positions,
     const float* normals, const float* texcoords, const uint32_t* indices, uint32_t vertex_count,
     uint32_t index_count, int32_t* out_geometry)
 {
+    if (ctx && !ctx->parent)
+        ctx->sceneVersion++;
     if (ctx && ctx->parent)
         return fail(AGB_ERR_INVALID_ARG, "agb_geometry_create: a view shares its parent's scene; change the parent");
     if (!ctx || !positions || !out_geometry)
@@ -756,6 +767,8 @@ AGB_API agb_status agb_tlas_read(agb_context* ctx, float* nodes_out, uint64_t no
 AGB_API agb_status agb_image_create(agb_context* ctx, const void* pixels, uint32_t width,
     uint32_t height, int32_t format, int32_t linear, int32_t* out_image)
 {
+    if (ctx && !ctx->parent)
+        ctx->sceneVersion++;
     if (ctx && ctx->parent)
         return fail(AGB_ERR_INVALID_ARG, "agb_image_create: a view shares its parent's scene; change the parent");
     if (!ctx || !pixels || !out_image || width == 0 || height == 0)
@@ -803,6 +816,8 @@ AGB_API agb_status agb_image_create(agb_context* ctx, const void* pixels, uint32
 AGB_API agb_status agb_materials_set(agb_context* ctx, const agb_material* materials,
     const agb_material_textures* textures, uint32_t count)
 {
+    if (ctx && !ctx->parent)
+        ctx->sceneVersion++;
     if (ctx && ctx->parent)
         return fail(AGB_ERR_INVALID_ARG, "agb_materials_set: a view shares its parent's scene; change the parent");
     if (!ctx || (!materials && count))
@@ -822,11 +837,18 @@ AGB_API agb_status agb_materials_set(agb_context* ctx, const agb_material* mater
     AGB_CUDA(cudaStreamSynchronize(ctx->stream), "upload materials");
     ctx->materialCount = count;
     ctx->hasMatTex     = textures != nullptr;
+    ctx->hostMaterials.assign(materials, materials + count);
+    if (textures)
+        ctx->hostMatTex.assign(textures, textures + count);
+    else
+        ctx->hostMatTex.clear();
     return AGB_OK;
 }
 
 AGB_API agb_status agb_instances_set(agb_context* ctx, const agb_instance* inst, uint32_t count)
 {
+    if (ctx && !ctx->parent)
+        ctx->sceneVersion++;
     if (ctx && ctx->parent)
         return fail(AGB_ERR_INVALID_ARG, "agb_instances_set: a view shares its parent's scene; change the parent");
     if (!ctx || (!inst && count))
@@ -974,12 +996,16 @@ AGB_API agb_status agb_instances_set(agb_context* ctx, const agb_instance* inst,
     ctx->tlasRoot      = tlasRoot;
     ctx->tlasDepth     = tlasDepth;
     ctx->tlasNodeCount = nodeCount;
+    ctx->hostInstances = std::move(di);
+    ctx->hostLayers    = std::move(dl);
     return AGB_OK;
 }
 
 AGB_API agb_status agb_environment_set(agb_context* ctx, const agb_environment_data* env,
     int32_t light_image, int32_t background_image)
 {
+    if (ctx && !ctx->parent)
+        ctx->sceneVersion++;
     if (ctx && ctx->parent)
         return fail(AGB_ERR_INVALID_ARG, "agb_environment_set: a view shares its parent's scene; change the parent");
     if (!ctx || !env)
@@ -1032,6 +1058,8 @@ AGB_API agb_status agb_environment_set(agb_context* ctx, const agb_environment_d
 
 AGB_API agb_status agb_set_environment_table(agb_context* ctx, int32_t layout)
 {
+    if (ctx && !ctx->parent)
+        ctx->sceneVersion++;
     if (ctx && ctx->parent)
         return fail(AGB_ERR_INVALID_ARG, "agb_set_environment_table: a view shares its parent's scene; change the parent");
     if (!ctx || (layout != AGB_ENV_TABLE_REFERENCE && layout != AGB_ENV_TABLE_FP64))
@@ -1042,6 +1070,8 @@ AGB_API agb_status agb_set_environment_table(agb_context* ctx, int32_t layout)
 
 AGB_API agb_status agb_ground_plane_set(agb_context* ctx, const agb_ground_plane* plane)
 {
+    if (ctx && !ctx->parent)
+        ctx->sceneVersion++;
     if (ctx && ctx->parent)
         return fail(AGB_ERR_INVALID_ARG, "agb_ground_plane_set: a view shares its parent's scene; change the parent");
     if (!ctx)
@@ -1317,6 +1347,447 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
         *stats   = r;
     }
     return AGB_OK;
+}
+
+// ------------------------------------------------------------------------- batched rendering
+// Several requests (views or contexts, of one or several scenes, any resolutions) rendered by
+// one wavefront: every stage is one launch over all of their paths (BatchTables in
+// agb_wavefront.cuh).  The scenes' tables are concatenated into a shared namespace, rebuilt when
+// the set of scenes or any of them changes.
+struct agb_batch
+{
+    agb_context* work = nullptr; // wave buffers, counters, stats, events and the stream; no scene
+    uint64_t maxPaths = 0;
+    // Shared namespace of the scenes of the last call.
+    std::vector<const agb_context*> scenes;
+    std::vector<uint64_t> versions;
+    DevBuf meshes, instances, tlas, tlasOrder, materials, matTex, images, layers;
+    std::vector<DevScene> sceneTable;
+    DevBuf sceneTableDev, reqTable, frameTable, pathReq;
+    cudaEvent_t done = nullptr;
+    ~agb_batch()
+    {
+        if (done)
+            cudaEventDestroy(done);
+        delete work;
+    }
+};
+
+namespace
+{
+
+int32_t remapTlasRef(int32_t ref, uint32_t nodeOff, uint32_t orderOff)
+{
+    if (ref >= 0)
+        return ref + int32_t(nodeOff);
+    uint32_t code  = uint32_t(~ref);
+    uint32_t first = code >> 3, cnt = code & 7u;
+    return ~int32_t(((first + orderOff) << 3) | cnt);
+}
+
+agb_status buildSharedScenes(agb_batch* b, const std::vector<agb_context*>& scenes)
+{
+    bool same = scenes.size() == b->scenes.size();
+    for (size_t k = 0; same && k < scenes.size(); k++)
+        same = scenes[k] == b->scenes[k] && scenes[k]->sceneVersion == b->versions[k];
+    if (same)
+        return AGB_OK;
+    cudaStream_t st = b->work->stream;
+    std::vector<DevMesh> M;
+    std::vector<DevInstance> I;
+    std::vector<DevLayer> L;
+    std::vector<agb_material> Mt;
+    std::vector<agb_material_textures> T;
+    std::vector<DevImage> Im;
+    std::vector<BNode> N;
+    std::vector<int32_t> O;
+    std::vector<DevScene> table;
+    bool anyTex = false;
+    for (agb_context* sc : scenes)
+        anyTex = anyTex || sc->hasMatTex;
+    for (agb_context* sc : scenes)
+    {
+        if (sc->ground.enabled)
+            return fail(AGB_ERR_INVALID_ARG, "agb_batch_render: scenes with a ground plane render alone");
+        if (sc->hostMaterials.size() != sc->materialCount || sc->hostInstances.size() != sc->instanceCount)
+            return fail(AGB_ERR_NOT_READY, "agb_batch_render: a scene has no materials or instances set");
+        const uint32_t meshOff = uint32_t(M.size()), instOff = uint32_t(I.size()), layerOff = uint32_t(L.size());
+        const uint32_t matOff = uint32_t(Mt.size()), imgOff = uint32_t(Im.size()), nodeOff = uint32_t(N.size());
+        const uint32_t orderOff = uint32_t(O.size());
+        for (auto& g : sc->geometries)
+            M.push_back(g->mesh);
+        for (auto& im : sc->images)
+            Im.push_back(im->view);
+        Mt.insert(Mt.end(), sc->hostMaterials.begin(), sc->hostMaterials.end());
+        for (uint32_t m = 0; m < sc->materialCount; m++)
+        {
+            agb_material_textures t;
+            for (int k = 0; k < AGB_TEX_SLOTS; k++)
+            {
+                int32_t v  = sc->hasMatTex ? sc->hostMatTex[m].image[k] : -1;
+                t.image[k] = v >= 0 ? v + int32_t(imgOff) : -1;
+            }
+            T.push_back(t);
+        }
+        for (DevLayer l : sc->hostLayers)
+        {
+            l.material += int32_t(matOff);
+            L.push_back(l);
+        }
+        for (DevInstance in : sc->hostInstances)
+        {
+            in.mesh += int32_t(meshOff);
+            in.material += int32_t(matOff);
+            in.layerOffset += int32_t(layerOff);
+            I.push_back(in);
+        }
+        std::vector<BNode> nodes(sc->tlasNodeCount);
+        std::vector<int32_t> order(sc->instanceCount);
+        if (!nodes.empty())
+            AGB_CUDA(cudaMemcpy(nodes.data(), sc->tlasNodes.ptr, nodes.size() * sizeof(BNode), cudaMemcpyDeviceToHost),
+                "agb_batch_render: read TLAS");
+        if (!order.empty())
+            AGB_CUDA(cudaMemcpy(order.data(), sc->tlasOrder.ptr, order.size() * sizeof(int32_t),
+                         cudaMemcpyDeviceToHost),
+                "agb_batch_render: read TLAS order");
+        for (BNode& nd : nodes)
+        {
+            nd.ref.x = remapTlasRef(nd.ref.x, nodeOff, orderOff);
+            nd.ref.y = remapTlasRef(nd.ref.y, nodeOff, orderOff);
+            N.push_back(nd);
+        }
+        for (int32_t o : order)
+            O.push_back(o + int32_t(instOff));
+        DevScene e      = sc->scene();
+        e.tlasRoot      = sc->instanceCount > 0 ? remapTlasRef(sc->tlasRoot, nodeOff, orderOff) : kDone;
+        e.instanceCount = int32_t(sc->instanceCount);
+        table.push_back(e);
+    }
+    auto put = [&](DevBuf& buf, const void* src, size_t bytes, const char* what) -> agb_status {
+        AGB_CUDA(buf.ensure(std::max<size_t>(bytes, 16)), what);
+        if (bytes)
+            AGB_CUDA(cudaMemcpyAsync(buf.ptr, src, bytes, cudaMemcpyHostToDevice, st), what);
+        return AGB_OK;
+    };
+    agb_status r;
+    if ((r = put(b->meshes, M.data(), M.size() * sizeof(DevMesh), "batch meshes")) ||
+        (r = put(b->instances, I.data(), I.size() * sizeof(DevInstance), "batch instances")) ||
+        (r = put(b->layers, L.data(), L.size() * sizeof(DevLayer), "batch layers")) ||
+        (r = put(b->materials, Mt.data(), Mt.size() * sizeof(agb_material), "batch materials")) ||
+        (r = put(b->matTex, T.data(), T.size() * sizeof(agb_material_textures), "batch textures")) ||
+        (r = put(b->images, Im.data(), Im.size() * sizeof(DevImage), "batch images")) ||
+        (r = put(b->tlas, N.data(), N.size() * sizeof(BNode), "batch TLAS")) ||
+        (r = put(b->tlasOrder, O.data(), O.size() * sizeof(int32_t), "batch TLAS order")))
+        return r;
+    for (DevScene& e : table)
+    {
+        e.meshes        = b->meshes.as<DevMesh>();
+        e.instances     = b->instances.as<DevInstance>();
+        e.tlas          = b->tlas.as<BNode>();
+        e.tlasOrder     = b->tlasOrder.as<int32_t>();
+        e.materials     = b->materials.as<agb_material>();
+        e.matTex        = anyTex ? b->matTex.as<agb_material_textures>() : nullptr;
+        e.materialCount = int32_t(Mt.size());
+        e.imageCount    = int32_t(Im.size());
+        e.images        = b->images.as<DevImage>();
+        e.layers        = b->layers.as<DevLayer>();
+    }
+    if ((r = put(b->sceneTableDev, table.data(), table.size() * sizeof(DevScene), "batch scene table")))
+        return r;
+    AGB_CUDA(cudaStreamSynchronize(st), "agb_batch_render: shared scenes");
+    b->sceneTable = table;
+    b->scenes.assign(scenes.begin(), scenes.end());
+    b->versions.clear();
+    for (agb_context* sc : scenes)
+        b->versions.push_back(sc->sceneVersion);
+    return AGB_OK;
+}
+
+} // namespace
+
+AGB_API agb_status agb_batch_create(int32_t device, void* cuda_stream, uint64_t max_paths_in_flight,
+    agb_batch** out)
+{
+    if (!out || max_paths_in_flight == 0 || max_paths_in_flight >= (1ull << 29))
+        return fail(AGB_ERR_INVALID_ARG, "agb_batch_create: bad argument");
+    *out = nullptr;
+    std::unique_ptr<agb_batch> b(new agb_batch());
+    agb_status st = agb_context_create(device, cuda_stream, &b->work);
+    if (st)
+        return st;
+    b->maxPaths = max_paths_in_flight;
+    AGB_CUDA(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming), "create event");
+    *out = b.release();
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_batch_destroy(agb_batch* b)
+{
+    if (!b)
+        return AGB_OK;
+    cudaSetDevice(b->work->device);
+    cudaStreamSynchronize(b->work->stream);
+    delete b;
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_batch_render(agb_batch* b, agb_context* const* views, const agb_render_options* options,
+    const uint32_t* sample_starts, const uint32_t* sample_counts, uint32_t count, agb_render_stats* stats)
+{
+    if (!b || !views || !options || !sample_counts || count == 0 || count > 65535)
+        return fail(AGB_ERR_INVALID_ARG, "agb_batch_render: bad argument");
+    agb_context* W = b->work;
+    agb_status st  = setDevice(W);
+    if (st)
+        return st;
+    // Requests, their scenes and options.
+    std::vector<agb_context*> scenes;
+    std::vector<int32_t> sceneOf(count);
+    int maxDepth = 0;
+    int forceOpaque = -1;
+    for (uint32_t i = 0; i < count; i++)
+    {
+        agb_context* v = views[i];
+        const agb_render_options& o = options[i];
+        if (!v || !v->frameSet)
+            return fail(AGB_ERR_NOT_READY, "agb_batch_render: a view has no frame data");
+        if (v->device != W->device)
+            return fail(AGB_ERR_INVALID_ARG, "agb_batch_render: views on another device");
+        if (o.width == 0 || o.height == 0 || uint64_t(o.width) * o.height > (1ull << 26) || sample_counts[i] == 0)
+            return fail(AGB_ERR_INVALID_ARG, "agb_batch_render: bad image size or sample count");
+        agb_context* sc = v->parent ? v->parent : v;
+        if (sc->instanceCount > 0 && sc->materialCount == 0)
+            return fail(AGB_ERR_NOT_READY, "agb_batch_render: no materials");
+        size_t k = std::find(scenes.begin(), scenes.end(), sc) - scenes.begin();
+        if (k == scenes.size())
+            scenes.push_back(sc);
+        sceneOf[i] = int32_t(k);
+        maxDepth   = std::max(maxDepth, int(v->frame.trace_depth));
+        int fo     = v->frame.is_force_opaque_shadows_enabled ? 1 : 0;
+        if (forceOpaque >= 0 && fo != forceOpaque)
+            return fail(AGB_ERR_INVALID_ARG, "agb_batch_render: views differ in opaque-shadow forcing");
+        forceOpaque = fo;
+        for (uint32_t j = 0; j < i; j++)
+            if (views[j] == v)
+                return fail(AGB_ERR_INVALID_ARG, "agb_batch_render: a view appears twice");
+    }
+    if ((st = buildSharedScenes(b, scenes)))
+        return st;
+    // Render targets, accumulation bookkeeping and AOVs of every view (on its own stream, which the
+    // batch then waits for).
+    std::vector<BatchRequest> reqs(count);
+    std::vector<uint32_t> remaining(count);
+    for (uint32_t i = 0; i < count; i++)
+    {
+        agb_context* v = views[i];
+        const agb_render_options& o = options[i];
+        uint32_t start = sample_starts ? sample_starts[i] : 0;
+        uint32_t accumMode = o.accumulation ? o.accumulation : AGB_ACCUM_RUNNING_MEAN;
+        if ((st = setDevice(v)) || (st = ensureAccum(v, o.width, o.height)))
+            return st;
+        if (start == 0)
+            v->accumulatedSamples = 0;
+        else if (v->accumulatedSamples != start || (v->lastAccumMode & accumMode) != accumMode)
+            return fail(AGB_ERR_INVALID_ARG, "agb_batch_render: sample_start must continue the view's accumulated "
+                                             "sequence in the same accumulation mode");
+        uint32_t pixels = o.width * o.height;
+        BatchRequest& q = reqs[i];
+        q               = BatchRequest{};
+        q.pixels        = pixels;
+        q.width         = o.width;
+        q.height        = o.height;
+        q.sampleBase    = start;
+        q.seedOffset    = o.seed_offset;
+        q.accumMode     = accumMode;
+        q.scene         = sceneOf[i];
+        q.traceDepth    = v->frame.trace_depth;
+        q.tlasRoot      = b->sceneTable[sceneOf[i]].tlasRoot;
+        q.aovSample     = ~0u;
+        q.accumMean     = v->accMean.as<float4>();
+        q.accumSum      = v->accSum.as<float4>();
+        q.accumComp     = v->accComp.as<float4>();
+        q.lastSample    = v->lastSample.as<float4>();
+        q.accumMoments  = v->accMoments.as<float2>();
+        if (v->frame.is_denoising_aovs_enabled)
+        {
+            AGB_CUDA(v->aovDepth.ensure(size_t(pixels) * sizeof(float)), "allocate AOVs");
+            AGB_CUDA(v->aovNormal.ensure(size_t(pixels) * sizeof(float4)), "allocate AOVs");
+            AGB_CUDA(v->aovAlbedo.ensure(size_t(pixels) * sizeof(float4)), "allocate AOVs");
+            AGB_CUDA(v->aovMotion.ensure(size_t(pixels) * sizeof(float4)), "allocate AOVs");
+            q.aovDepth  = v->aovDepth.as<float>();
+            q.aovNormal = v->aovNormal.as<float4>();
+            q.aovAlbedo = v->aovAlbedo.as<float4>();
+            q.aovMotion = v->aovMotion.as<float4>();
+            q.aovSample = start + sample_counts[i] - 1;
+        }
+        v->aovValid  = v->frame.is_denoising_aovs_enabled != 0;
+        remaining[i] = sample_counts[i];
+        AGB_CUDA(cudaEventRecord(v->ev0, v->stream), "record event");
+        AGB_CUDA(cudaStreamWaitEvent(W->stream, v->ev0, 0), "order view work before the batch");
+    }
+    if ((st = setDevice(W)))
+        return st;
+    // Waves: every unfinished request takes a share of the path budget in proportion to what it
+    // still needs (at least one sample), so small requests are not held back by large ones.
+    uint64_t launches = 0;
+    uint64_t closest = 0, shadow = 0;
+    uint32_t waves = 0;
+    W->marks.reset();
+    KernelMarks* marks = W->profiling ? &W->marks : nullptr;
+    AGB_CUDA(cudaEventRecord(W->ev0, W->stream), "record event");
+    std::vector<BatchRequest> round;
+    std::vector<agb_frame_data> frames;
+    std::vector<uint32_t> chunk(count);
+    for (;;)
+    {
+        uint64_t need = 0;
+        for (uint32_t i = 0; i < count; i++)
+            need += uint64_t(reqs[i].pixels) * remaining[i];
+        if (need == 0)
+            break;
+        double scale = need > b->maxPaths ? double(b->maxPaths) / double(need) : 1.0;
+        round.clear();
+        frames.clear();
+        uint64_t paths = 0, pixelsTotal = 0;
+        for (uint32_t i = 0; i < count; i++)
+        {
+            if (!remaining[i])
+                continue;
+            uint32_t c = std::max<uint32_t>(1, uint32_t(double(remaining[i]) * scale));
+            c = std::min(c, remaining[i]);
+            // Keep the wave within the budget (and the path index range) once it holds a request.
+            if (!round.empty() && paths + uint64_t(reqs[i].pixels) * c > std::max<uint64_t>(b->maxPaths, 1))
+                c = uint32_t(std::min<uint64_t>(c, (b->maxPaths - std::min(b->maxPaths, paths)) / reqs[i].pixels));
+            if (c == 0)
+                continue;
+            BatchRequest q = reqs[i];
+            q.samples      = c;
+            q.pathOffset   = uint32_t(paths);
+            q.pixelOffset  = uint32_t(pixelsTotal);
+            round.push_back(q);
+            frames.push_back(views[i]->frame);
+            chunk[i] = c;
+            paths += uint64_t(q.pixels) * c;
+            pixelsTotal += q.pixels;
+        }
+        if (paths >= (1ull << 29))
+            return fail(AGB_ERR_LIMIT, "agb_batch_render: wave too large");
+        if ((st = ensureWave(W, size_t(paths), maxDepth, 1)))
+            return st;
+        AGB_CUDA(b->pathReq.ensure(size_t(paths) * sizeof(uint16_t)), "allocate batch path table");
+        AGB_CUDA(b->reqTable.ensure(round.size() * sizeof(BatchRequest)), "allocate batch requests");
+        AGB_CUDA(b->frameTable.ensure(frames.size() * sizeof(agb_frame_data)), "allocate batch frames");
+        AGB_CUDA(cudaMemcpyAsync(b->reqTable.ptr, round.data(), round.size() * sizeof(BatchRequest),
+                     cudaMemcpyHostToDevice, W->stream),
+            "upload batch requests");
+        AGB_CUDA(cudaMemcpyAsync(b->frameTable.ptr, frames.data(), frames.size() * sizeof(agb_frame_data),
+                     cudaMemcpyHostToDevice, W->stream),
+            "upload batch frames");
+        size_t counterWords = size_t(maxDepth + 2) * kCounterStride;
+        AGB_CUDA(cudaMemsetAsync(W->counters.ptr, 0, counterWords * sizeof(uint32_t), W->stream), "clear counters");
+        AGB_CUDA(cudaMemsetAsync(W->stats.ptr, 0, 8 * sizeof(unsigned long long), W->stream), "clear stats");
+        BatchTables bt{};
+        bt.req          = b->reqTable.as<BatchRequest>();
+        bt.frames       = b->frameTable.as<agb_frame_data>();
+        bt.scenes       = b->sceneTableDev.as<DevScene>();
+        bt.pathReq      = b->pathReq.as<uint16_t>();
+        bt.requestCount = uint32_t(round.size());
+        bt.pixelsTotal  = uint32_t(pixelsTotal);
+        WaveParams wp{};
+        wp.paths          = uint32_t(paths);
+        wp.countTraversal = W->counting ? 1 : 0;
+        WaveBuffers wb    = W->wb;
+        wb.counters       = W->counters.as<uint32_t>();
+        DevScene shared   = b->sceneTable[0];
+        shared.ground     = DevGroundPlane{};
+        launchBatchWave(shared, frames[0], wp, wb, bt, maxDepth, forceOpaque != 0, W->stream, W->smCount, launches,
+            marks);
+        AGB_CUDA(cudaGetLastError(), "launch batch wave");
+        if (stats)
+        {
+            std::vector<uint32_t> c(counterWords);
+            AGB_CUDA(cudaMemcpyAsync(c.data(), W->counters.ptr, c.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                         W->stream),
+                "read counters");
+            AGB_CUDA(cudaStreamSynchronize(W->stream), "batch wave");
+            for (int bb = 0; bb < maxDepth; bb++)
+            {
+                closest += c[kCounterStride * bb + CNT_RAYS];
+                shadow += c[kCounterStride * bb + CNT_SHADOW];
+            }
+        }
+        for (uint32_t i = 0; i < count; i++)
+            if (remaining[i] && chunk[i])
+            {
+                reqs[i].sampleBase += chunk[i];
+                remaining[i] -= chunk[i];
+                chunk[i] = 0;
+            }
+        // The next wave's tables and counters are written by copies on the same stream, after
+        // this wave's kernels (a pageable upload stages its source before returning).
+        waves++;
+    }
+    AGB_CUDA(cudaEventRecord(W->ev1, W->stream), "record event");
+    AGB_CUDA(cudaEventRecord(b->done, W->stream), "record event");
+    for (uint32_t i = 0; i < count; i++)
+    {
+        agb_context* v = views[i];
+        uint32_t start = sample_starts ? sample_starts[i] : 0;
+        uint32_t accumMode = options[i].accumulation ? options[i].accumulation : AGB_ACCUM_RUNNING_MEAN;
+        v->accumulatedSamples = start + sample_counts[i];
+        v->lastAccumMode      = start == 0 ? accumMode : v->lastAccumMode;
+        // Work on the view's own stream (reads, denoising) follows the batch.
+        AGB_CUDA(cudaStreamWaitEvent(v->stream, b->done, 0), "order the batch before view work");
+    }
+    if (stats)
+    {
+        AGB_CUDA(cudaEventSynchronize(W->ev1), "batch render");
+        unsigned long long sv[8];
+        AGB_CUDA(cudaMemcpy(sv, W->stats.ptr, sizeof sv, cudaMemcpyDeviceToHost), "read stats");
+        if (sv[4])
+            return fail(AGB_ERR_LIMIT, "agb_batch_render: traversal stack overflow");
+        agb_render_stats r{};
+        for (uint32_t i = 0; i < count; i++)
+            r.paths += uint64_t(options[i].width) * options[i].height * sample_counts[i];
+        r.closest_rays    = closest;
+        r.shadow_rays     = shadow;
+        r.kernel_launches = launches;
+        if (marks)
+        {
+            double ms[KC_COUNT];
+            marks->sum(ms);
+            for (int k = 0; k < 6; k++)
+                r.kernel_ms[k] = ms[k];
+            for (size_t i = 0; i < marks->category.size(); i++)
+                if (marks->category[i] < 6)
+                    r.kernel_count[marks->category[i]]++;
+        }
+        float ms = 0.f;
+        AGB_CUDA(cudaEventElapsedTime(&ms, W->ev0, W->ev1), "event time");
+        r.gpu_ms = ms;
+        *stats   = r;
+    }
+    (void)waves;
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_batch_poll(agb_batch* b)
+{
+    if (!b)
+        return AGB_ERR_INVALID_ARG;
+    cudaError_t e = cudaEventQuery(b->done);
+    if (e == cudaSuccess)
+        return AGB_OK;
+    if (e == cudaErrorNotReady)
+        return AGB_ERR_NOT_READY;
+    return fail(AGB_ERR_CUDA, std::string("agb_batch_poll: ") + cudaGetErrorString(e));
+}
+
+AGB_API agb_status agb_batch_set_profiling(agb_batch* b, int32_t enabled)
+{
+    if (!b)
+        return AGB_ERR_INVALID_ARG;
+    return agb_set_profiling(b->work, enabled);
 }
 
 AGB_API agb_status agb_wait_poll(agb_context* ctx)

@@ -89,6 +89,11 @@ struct KernelMarks
 // agb_pt.cu
 void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp,
     const WaveBuffers& wb, cudaStream_t st, int smCount, uint64_t& launches, KernelMarks* marks);
+// A batched wave over several requests (BatchTables): `shared` is the scenes' shared namespace,
+// maxDepth the deepest request's trace depth.
+void launchBatchWave(const DevScene& shared, const agb_frame_data& anyFrame, const WaveParams& wp,
+    const WaveBuffers& wb, const BatchTables& bt, int maxDepth, bool forceOpaque, cudaStream_t st, int smCount,
+    uint64_t& launches, KernelMarks* marks);
 void setTraceAttributes();
 
 // agb_env_build.cu: environment sampling table on the device.  rgba: device RGBA32F texels.

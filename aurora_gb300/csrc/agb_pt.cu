@@ -67,17 +67,37 @@ __device__ void cameraRay(const agb_frame_data& f, uint32_t px, uint32_t py, uin
     }
 }
 
-__global__ void k_camera(agb_frame_data f, WaveParams wp, WaveBuffers wb)
+template <bool kBatch>
+__global__ void k_camera(agb_frame_data f, WaveParams wp, WaveBuffers wb, BatchTables bt)
 {
     uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < wp.paths; p += stride)
     {
-        uint32_t pixel = p % wp.pixels;
-        uint32_t k     = p / wp.pixels;
-        uint32_t px = pixel % wp.width, py = pixel / wp.width;
-        Rng rng     = rngInit(wp.sampleBase + k + wp.seedOffset, wp.width, px, py);
+        uint32_t r = 0, local = p;
+        uint32_t pixels = wp.pixels, width = wp.width, height = wp.height, sampleBase = wp.sampleBase;
+        uint32_t seedOffset = wp.seedOffset, aovSample = wp.aovSample;
+        float4* aovMotion = wb.aovMotion;
+        if constexpr (kBatch)
+        {
+            r                     = batchRequestOfPath(bt, p);
+            const BatchRequest& q = bt.req[r];
+            local      = p - q.pathOffset;
+            pixels     = q.pixels;
+            width      = q.width;
+            height     = q.height;
+            sampleBase = q.sampleBase;
+            seedOffset = q.seedOffset;
+            aovSample  = q.aovSample;
+            aovMotion  = q.aovMotion;
+            bt.pathReq[p] = uint16_t(r);
+        }
+        const agb_frame_data& F = kBatch ? bt.frames[r] : f;
+        uint32_t pixel = local % pixels;
+        uint32_t k     = local / pixels;
+        uint32_t px = pixel % width, py = pixel / width;
+        Rng rng     = rngInit(sampleBase + k + seedOffset, width, px, py);
         v3 o, d;
-        cameraRay(f, px, py, wp.width, wp.height, rng, o, d);
+        cameraRay(F, px, py, width, height, rng, o, d);
         wb.rayOrg[0][p]  = make_float4(o.x, o.y, o.z, 0.f);
         wb.rayDir[0][p]  = make_float4(d.x, d.y, d.z, __int_as_float(0x7f800000));
         wb.rayPath[0][p] = p;
@@ -85,8 +105,8 @@ __global__ void k_camera(agb_frame_data f, WaveParams wp, WaveBuffers wb)
         wb.contrib[p]    = make_float4(1.f, 1.f, 1.f, 0.f);
         wb.flags[p] = PF_PRIMARY | (uint32_t(CAMERA_RAY) << PF_RAYTYPE_SHIFT) |
             (uint32_t(NO_SECONDARY_RAY) << PF_MISLOBE_SHIFT);
-        if (wp.sampleBase + k == wp.aovSample)
-            wb.aovMotion[pixel] = make_float4(0.f, 0.f, 0.f, 0.f); // MainEntryPoints.slang:115-118
+        if (sampleBase + k == aovSample)
+            aovMotion[pixel] = make_float4(0.f, 0.f, 0.f, 0.f); // MainEntryPoints.slang:115-118
         float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
         wb.outDirect[p]    = z;
         wb.outDiffuse[p]   = z;
@@ -123,6 +143,20 @@ struct HitWriter
         inst[i] = hit ? h.inst : -1;
     }
 };
+// Batched waves: the TLAS root of the ray's scene, or kDone for a ray whose request has reached
+// its trace depth (k_shade handles it as the depth-limit segment without its hit).
+struct BatchQueueRayLoader : QueueRayLoader
+{
+    const uint32_t* rayPath;
+    const uint16_t* pathReq;
+    const BatchRequest* req;
+    int bounce;
+    AGB_D int32_t root(uint32_t i) const
+    {
+        const BatchRequest& q = req[pathReq[rayPath[i]]];
+        return q.traceDepth <= bounce ? kDone : q.tlasRoot;
+    }
+};
 struct ShadowLoader
 {
     const uint32_t* tag;
@@ -139,6 +173,12 @@ struct ShadowLoader
         tmin = kRayTMin;
         tmax = __int_as_float(0x7f800000);
     }
+};
+struct BatchShadowLoader : ShadowLoader
+{
+    const uint16_t* pathReq;
+    const BatchRequest* req;
+    AGB_D int32_t root(uint32_t i) const { return req[pathReq[tag[i] >> 3]].tlasRoot; }
 };
 struct OcclusionWriter
 {
@@ -190,6 +230,12 @@ struct TransparentShadowLoader
         vis[i] = make_float4(1.f, 1.f, 1.f, __int_as_float(0));
     }
 };
+struct BatchTransparentShadowLoader : TransparentShadowLoader
+{
+    const uint16_t* pathReq;
+    const BatchRequest* req;
+    AGB_D int32_t root(uint32_t i) const { return req[pathReq[rays.tag[i] >> 3]].tlasRoot; }
+};
 struct TransparentShadowWriter
 {
     static constexpr bool kRestart = true;
@@ -222,15 +268,21 @@ struct TransparentShadowWriter
     }
 };
 
-template <bool kCount>
-__global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_closest(DevScene s, WaveBuffers wb, int bounce, int cur)
+template <bool kCount, bool kBatch>
+__global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_closest(DevScene s, WaveBuffers wb,
+    int bounce, int cur, BatchTables bt)
 {
     uint32_t n      = wb.counters[bounce * kCounterStride + CNT_RAYS];
     TraceCounters c = { 0, 0 };
     bool overflow   = false;
-    persistentTrace<false, kCount>(s, n, wb.counters + bounce * kCounterStride + CNT_CLOSEST_WORK,
-        QueueRayLoader{ wb.rayOrg[cur], wb.rayDir[cur] }, HitWriter{ wb.hitTUV, wb.hitInst },
-        g_stack + threadIdx.x, kTraceBlock, c, overflow);
+    QueueRayLoader rays{ wb.rayOrg[cur], wb.rayDir[cur] };
+    if constexpr (kBatch)
+        persistentTrace<false, kCount>(s, n, wb.counters + bounce * kCounterStride + CNT_CLOSEST_WORK,
+            BatchQueueRayLoader{ rays, wb.rayPath[cur], bt.pathReq, bt.req, bounce },
+            HitWriter{ wb.hitTUV, wb.hitInst }, g_stack + threadIdx.x, kTraceBlock, c, overflow);
+    else
+        persistentTrace<false, kCount>(s, n, wb.counters + bounce * kCounterStride + CNT_CLOSEST_WORK, rays,
+            HitWriter{ wb.hitTUV, wb.hitInst }, g_stack + threadIdx.x, kTraceBlock, c, overflow);
     if (kCount)
     {
         atomicAdd(statPtr(wb, 2), c.nodes);
@@ -242,16 +294,21 @@ __global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_closes
 
 // Opaque shadow rays of the bounce's counter block: the shading's (CNT_SHADOW / CNT_SHADOW_WORK)
 // or the ground plane's (CNT_GROUND_SHADOW / CNT_GROUND_WORK).
-template <bool kCount>
+template <bool kCount, bool kBatch>
 __global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_shadow(DevScene s, WaveBuffers wb,
-    int bounce, int countSlot, int workSlot)
+    int bounce, int countSlot, int workSlot, BatchTables bt)
 {
     uint32_t n      = wb.counters[bounce * kCounterStride + countSlot];
     TraceCounters c = { 0, 0 };
     bool overflow   = false;
-    persistentTrace<true, kCount>(s, n, wb.counters + bounce * kCounterStride + workSlot,
-        ShadowLoader{ wb.shTag, wb.shOrg, wb.shDir }, OcclusionWriter{ wb.shTag, wb.occluded },
-        g_stack + threadIdx.x, kTraceBlock, c, overflow);
+    ShadowLoader rays{ wb.shTag, wb.shOrg, wb.shDir };
+    if constexpr (kBatch)
+        persistentTrace<true, kCount>(s, n, wb.counters + bounce * kCounterStride + workSlot,
+            BatchShadowLoader{ rays, bt.pathReq, bt.req }, OcclusionWriter{ wb.shTag, wb.occluded },
+            g_stack + threadIdx.x, kTraceBlock, c, overflow);
+    else
+        persistentTrace<true, kCount>(s, n, wb.counters + bounce * kCounterStride + workSlot, rays,
+            OcclusionWriter{ wb.shTag, wb.occluded }, g_stack + threadIdx.x, kTraceBlock, c, overflow);
     if (kCount)
     {
         atomicAdd(statPtr(wb, 5), c.nodes);
@@ -261,17 +318,23 @@ __global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_shadow
         atomicAdd(statPtr(wb, 4), 1ull);
 }
 
-template <bool kCount>
+template <bool kCount, bool kBatch>
 __global__ void __launch_bounds__(kTraceBlock, kTraceBlocksPerSM) k_trace_shadow_transparent(DevScene s,
-    WaveBuffers wb, int bounce)
+    WaveBuffers wb, int bounce, BatchTables bt)
 {
     uint32_t n      = wb.counters[bounce * kCounterStride + CNT_SHADOW];
     TraceCounters c = { 0, 0 };
     bool overflow   = false;
-    persistentTrace<false, kCount>(s, n, wb.counters + bounce * kCounterStride + CNT_SHADOW_WORK,
-        TransparentShadowLoader{ ShadowLoader{ wb.shTag, wb.shOrg, wb.shDir }, wb.shadePoint },
-        TransparentShadowWriter{ wb.shTag, wb.shadePoint, wb.pendSlot }, g_stack + threadIdx.x,
-        kTraceBlock, c, overflow);
+    TransparentShadowLoader rays{ ShadowLoader{ wb.shTag, wb.shOrg, wb.shDir }, wb.shadePoint };
+    if constexpr (kBatch)
+        persistentTrace<false, kCount>(s, n, wb.counters + bounce * kCounterStride + CNT_SHADOW_WORK,
+            BatchTransparentShadowLoader{ rays, bt.pathReq, bt.req },
+            TransparentShadowWriter{ wb.shTag, wb.shadePoint, wb.pendSlot }, g_stack + threadIdx.x,
+            kTraceBlock, c, overflow);
+    else
+        persistentTrace<false, kCount>(s, n, wb.counters + bounce * kCounterStride + CNT_SHADOW_WORK, rays,
+            TransparentShadowWriter{ wb.shTag, wb.shadePoint, wb.pendSlot }, g_stack + threadIdx.x,
+            kTraceBlock, c, overflow);
     if (kCount)
     {
         atomicAdd(statPtr(wb, 5), c.nodes);
@@ -373,15 +436,46 @@ AGB_D void loadShadePoint(const DevScene& s, const float4* sp, uint32_t stride, 
     geomPos             = v3{ q9.y, q9.z, q9.w };
 }
 
+// Per-path view of a wave's request: the whole wave's values for a single-request wave, the
+// path's request's for a batched one.
+struct PathRequest
+{
+    uint32_t local, pixels, width, sampleBase, aovSample;
+    int32_t traceDepth;
+    float* aovDepth;
+    float4* aovNormal;
+    float4* aovAlbedo;
+    float4* aovMotion;
+};
+template <bool kBatch>
+AGB_D PathRequest pathRequest(const WaveParams& wp, const WaveBuffers& wb, const BatchTables& bt, uint32_t p,
+    uint32_t& r, int depth)
+{
+    if constexpr (kBatch)
+    {
+        r                     = bt.pathReq[p];
+        const BatchRequest& q = bt.req[r];
+        return PathRequest{ p - q.pathOffset, q.pixels, q.width, q.sampleBase, q.aovSample, q.traceDepth,
+            q.aovDepth, q.aovNormal, q.aovAlbedo, q.aovMotion };
+    }
+    else
+    {
+        r = 0;
+        return PathRequest{ p, wp.pixels, wp.width, wp.sampleBase, wp.aovSample, depth, wb.aovDepth,
+            wb.aovNormal, wb.aovAlbedo, wb.aovMotion };
+    }
+}
+AGB_D float bounceClamp(const agb_frame_data& f)
+{
+    return f.indirect_bounce_clamp_scale > 0.f ? f.max_luminance * f.indirect_bounce_clamp_scale : 0.f;
+}
+
+template <bool kBatch>
 __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene s, agb_frame_data f,
-    WaveParams wp, WaveBuffers wb, int bounce, int cur, int depthLimit)
+    WaveParams wp, WaveBuffers wb, int bounce, int cur, int depthLimit, BatchTables bt)
 {
     uint32_t n      = wb.counters[bounce * kCounterStride + CNT_RAYS];
     uint32_t stride = gridDim.x * blockDim.x;
-    const float clampLum = f.indirect_bounce_clamp_scale > 0.f
-        ? f.max_luminance * f.indirect_bounce_clamp_scale
-        : 0.f;
-    v2 screen = v2{ float(wp.width), float(wp.height) };
     // Warp-uniform loop: every lane of a warp runs the same number of iterations so the queue
     // appends at the end of the body are executed by the whole warp.
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride)
@@ -398,6 +492,13 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
         if (valid)
         {
             p          = wb.rayPath[cur][i];
+            uint32_t r;
+            const PathRequest q = pathRequest<kBatch>(wp, wb, bt, p, r, f.trace_depth);
+            const agb_frame_data& F = kBatch ? bt.frames[r] : f;
+            const DevScene& S       = kBatch ? bt.scenes[bt.req[r].scene] : s;
+            const float clampLum    = bounceClamp(F);
+            const v2 screen         = kBatch ? v2{ float(bt.req[r].width), float(bt.req[r].height) }
+                                             : v2{ float(wp.width), float(wp.height) };
             float4 d4  = wb.rayDir[cur][i];
             v3 dir     = v3{ d4.x, d4.y, d4.z };
             uint32_t flags = wb.flags[p];
@@ -405,12 +506,13 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
             v3 contrib = v3{ c4.x, c4.y, c4.z };
             uint32_t rayType = pfRayType(flags);
             bool primary = (flags & PF_PRIMARY) != 0;
-            uint32_t pixel = p % wp.pixels;
-            v2 pixel2 = v2{ float(pixel % wp.width), float(pixel / wp.width) };
+            uint32_t pixel = q.local % q.pixels;
+            v2 pixel2 = v2{ float(pixel % q.width), float(pixel / q.width) };
             bool bg = primary || rayType == TRANSMISSION_LOBE || rayType == GROUND_PLANE_REFLECTION_RAY;
-            if (depthLimit)
+            // A batched request whose trace depth is this bounce takes the depth-limit segment here.
+            if (depthLimit || (kBatch && bounce == q.traceDepth))
             {
-                v3 direct = evaluateEnvironment(s, dir, bg, pixel2, screen) * contrib;
+                v3 direct = evaluateEnvironment(S, dir, bg, pixel2, screen) * contrib;
                 float4 li = wb.lastIndirect[p];
                 accumulateSegment(wb, p, bounce, flags, rayType, direct, v3{ li.x, li.y, li.z },
                     clampLum);
@@ -419,20 +521,20 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
             {
                 float4 h  = wb.hitTUV[i];
                 int32_t inst = wb.hitInst[i];
-                bool aov = primary && wp.sampleBase + p / wp.pixels == wp.aovSample;
+                bool aov = primary && q.sampleBase + q.local / q.pixels == q.aovSample;
                 if (inst < 0)
                 {
                     if (aov)
                     {
                         // Miss AOVs (MainEntryPoints.slang:380-406); the guide normal faces back
                         // along the ray.
-                        wb.aovDepth[pixel]  = f.sky_view_z;
-                        wb.aovNormal[pixel] = make_float4(-dir.x, -dir.y, -dir.z, 1.f);
-                        wb.aovAlbedo[pixel] = make_float4(0.f, 0.f, 0.f, 0.1f);
-                        wb.aovMotion[pixel] = skyMotion(f.camera_view_proj, f.camera_view_proj_prev,
+                        q.aovDepth[pixel]  = F.sky_view_z;
+                        q.aovNormal[pixel] = make_float4(-dir.x, -dir.y, -dir.z, 1.f);
+                        q.aovAlbedo[pixel] = make_float4(0.f, 0.f, 0.f, 0.1f);
+                        q.aovMotion[pixel] = skyMotion(F.camera_view_proj, F.camera_view_proj_prev,
                             dir, screen.x, screen.y);
                     }
-                    v3 direct = bg ? evaluateEnvironment(s, dir, true, pixel2, screen) * contrib
+                    v3 direct = bg ? evaluateEnvironment(S, dir, true, pixel2, screen) * contrib
                                    : splat(0.f);
                     accumulateSegment(wb, p, bounce, flags, rayType, direct, splat(0.f), clampLum);
                 }
@@ -443,9 +545,9 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
                         uint2 r = wb.rng[p];
                         rng     = Rng{ r.x, r.y };
                     }
-                    const DevInstance& in = s.instances[inst];
+                    const DevInstance& in = S.instances[inst];
                     v3 V       = -dir;
-                    Shading sh = computeShading(s, in, uint32_t(__float_as_int(h.w)), h.y, h.z);
+                    Shading sh = computeShading(S, in, uint32_t(__float_as_int(h.w)), h.y, h.z);
                     v2 baseUV  = sh.uv;
                     bool hitLayer = false;
                     int32_t mi    = 0;
@@ -463,7 +565,7 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
                         }
                         else
                         {
-                            const DevLayer& L = s.layers[in.layerOffset + li - 1];
+                            const DevLayer& L = S.layers[in.layerOffset + li - 1];
                             mi = L.material;
                             v2 uv = v2{ 0.f, 0.f };
                             float b3[3] = { sh.bary.x, sh.bary.y, sh.bary.z };
@@ -476,10 +578,10 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
                             sh.uv = uv;
                         }
                         matNormal = sh.N;
-                        m = loadMaterial(s, mi, sh, matNormal, genNormal);
-                        if (!primary && f.is_path_regularization_enabled)
+                        m = loadMaterial(S, mi, sh, matNormal, genNormal);
+                        if (!primary && F.is_path_regularization_enabled)
                         {
-                            float fl = lerpf(0.05f, lerpf(0.05f, 0.35f, f.path_regularization_strength),
+                            float fl = lerpf(0.05f, lerpf(0.05f, 0.35f, F.path_regularization_strength),
                                 saturatef(float(bounce) / 3.f));
                             m.specularRoughness = m.specularRoughness > fl ? m.specularRoughness : fl;
                             m.coatRoughness     = m.coatRoughness > fl ? m.coatRoughness : fl;
@@ -489,15 +591,15 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
                             // Hit AOVs for every layer evaluated (HitShaderEntryPoints.slang:149-233).
                             float4 o4 = wb.rayOrg[cur][i];
                             v3 hw     = v3{ o4.x, o4.y, o4.z } + dir * h.x;
-                            float vz  = viewDepth(f.camera_inv_view, hw);
+                            float vz  = viewDepth(F.camera_inv_view, hw);
                             v3 gn     = normalize(matNormal);
-                            wb.aovDepth[pixel]  = vz;
-                            wb.aovNormal[pixel] = make_float4(gn.x, gn.y, gn.z,
+                            q.aovDepth[pixel]  = vz;
+                            q.aovNormal[pixel] = make_float4(gn.x, gn.y, gn.z,
                                 m.specularRoughness > 0.05f ? m.specularRoughness : 0.05f);
-                            wb.aovAlbedo[pixel] = make_float4(m.baseColor.x, m.baseColor.y,
+                            q.aovAlbedo[pixel] = make_float4(m.baseColor.x, m.baseColor.y,
                                 m.baseColor.z, m.metalness());
-                            wb.aovMotion[pixel] = surfaceMotion(f.camera_view_proj,
-                                f.camera_view_proj_prev, f.camera_inv_view_prev, hw, vz, screen.x,
+                            q.aovMotion[pixel] = surfaceMotion(F.camera_view_proj,
+                                F.camera_view_proj_prev, F.camera_inv_view_prev, hw, vz, screen.x,
                                 screen.y);
                         }
                         v3 transparency = splat(1.f) - m.opacity;
@@ -530,15 +632,15 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
                         v3 so = dot(V, fr.N) < 0.f ? sh.geomPosition : sh.position;
                         float4* pslot = wb.pendSlot + size_t(p) * kMaxShadowSlots;
                         float4* pdir  = wb.shDir + size_t(p) * kMaxShadowSlots;
-                        int nl = f.distant_light_count;
-                        if (!f.is_denoising_aovs_enabled && nl > 1)
+                        int nl = F.distant_light_count;
+                        if (!F.is_denoising_aovs_enabled && nl > 1)
                         {
                             for (int l = 0; l < nl && l < 4; l++)
                             {
-                                if (f.distant_lights[l].color_and_intensity[3] <= 0.f)
+                                if (F.distant_lights[l].color_and_intensity[3] <= 0.f)
                                     continue;
                                 v3 sd;
-                                v3 r = shadeDistantLight(f.distant_lights[l], m, mc, fr, V, rng, sd);
+                                v3 r = shadeDistantLight(F.distant_lights[l], m, mc, fr, V, rng, sd);
                                 if (isBlack(r))
                                     continue;
                                 pslot[l] = make_float4(r.x, r.y, r.z, 0.f);
@@ -552,7 +654,7 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
                             float total = 0.f;
                             for (int l = 0; l < nl && l < 4; l++)
                             {
-                                const float* ci = f.distant_lights[l].color_and_intensity;
+                                const float* ci = F.distant_lights[l].color_and_intensity;
                                 w[l] = luminance(v3{ ci[0], ci[1], ci[2] }) * ci[3];
                                 total += w[l];
                             }
@@ -575,10 +677,10 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
                             }
                             else
                                 idx = int(random2D(rng).x * float(nl));
-                            if (f.distant_lights[idx].color_and_intensity[3] > 0.f)
+                            if (F.distant_lights[idx].color_and_intensity[3] > 0.f)
                             {
                                 v3 sd;
-                                v3 r = shadeDistantLight(f.distant_lights[idx], m, mc, fr, V, rng, sd);
+                                v3 r = shadeDistantLight(F.distant_lights[idx], m, mc, fr, V, rng, sd);
                                 r    = r / fmaxf_(selPdf, 1e-4f);
                                 if (!isBlack(r))
                                 {
@@ -642,8 +744,9 @@ AGB_D void storeMis(float4* mp, uint32_t stride, uint32_t j, v3 L, float pdf, v3
     w[2 * size_t(stride)] = make_float4(rnd.x, rnd.y, __uint_as_float(bitsBase), 0.f);
 }
 
+template <bool kBatch>
 __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade_scatter(DevScene s,
-    agb_frame_data f, WaveParams wp, WaveBuffers wb, int bounce, int cur)
+    agb_frame_data f, WaveParams wp, WaveBuffers wb, int bounce, int cur, BatchTables bt)
 {
     uint32_t n      = wb.counters[bounce * kCounterStride + CNT_SCATTER];
     uint32_t stride = gridDim.x * blockDim.x;
@@ -663,6 +766,7 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade_scatter(
             uint32_t slots;
             loadShadePoint(s, wb.shadePoint, wp.paths, j, m, slots, p, mc, fr, V, shPosition,
                 shGeomPosition);
+            const agb_frame_data& F = kBatch ? bt.frames[bt.pathReq[p]] : f;
             uint32_t flags = wb.flags[p];
             float4 c4      = wb.contrib[p];
             v3 contrib     = v3{ c4.x, c4.y, c4.z };
@@ -713,7 +817,7 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade_scatter(
             if (nextType == TRANSMISSION_LOBE)
                 flags ^= PF_INSIDE;
             contrib *= nextContrib;
-            if (f.is_russian_roulette_enabled && bounce + 1 >= f.russian_roulette_start_depth)
+            if (F.is_russian_roulette_enabled && bounce + 1 >= F.russian_roulette_start_depth)
             {
                 float mx   = fmaxf_(contrib.x, fmaxf_(contrib.y, contrib.z));
                 float surv = clampf(mx, 0.05f, 1.f);
@@ -740,12 +844,12 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade_scatter(
     }
 }
 
+template <bool kBatch>
 __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade_mis(DevScene s,
-    agb_frame_data f, WaveParams wp, WaveBuffers wb, int bounce)
+    agb_frame_data f, WaveParams wp, WaveBuffers wb, int bounce, BatchTables bt)
 {
     uint32_t n      = wb.counters[bounce * kCounterStride + CNT_SCATTER];
     uint32_t stride = gridDim.x * blockDim.x;
-    v2 screen = v2{ float(wp.width), float(wp.height) };
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride)
     {
         uint32_t j     = base + threadIdx.x;
@@ -768,19 +872,24 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade_mis(DevS
             int misLobe   = __float_as_int(w1.w);
             v2 rnd        = v2{ w2.x, w2.y };
             uint32_t bits = __float_as_uint(w2.z);
-            uint32_t pixel = p % wp.pixels;
-            v2 pixel2      = v2{ float(pixel % wp.width), float(pixel / wp.width) };
+            uint32_t r;
+            const PathRequest q = pathRequest<kBatch>(wp, wb, bt, p, r, f.trace_depth);
+            const DevScene& S   = kBatch ? bt.scenes[bt.req[r].scene] : s;
+            const v2 screen     = kBatch ? v2{ float(bt.req[r].width), float(bt.req[r].height) }
+                                         : v2{ float(wp.width), float(wp.height) };
+            uint32_t pixel = q.local % q.pixels;
+            v2 pixel2      = v2{ float(pixel % q.width), float(pixel / q.width) };
             float4* pslot  = wb.pendSlot + size_t(p) * kMaxShadowSlots;
             float4* pdir   = wb.shDir + size_t(p) * kMaxShadowSlots;
             // Environment MIS (ShadeFunctions.slang:135-259).
             bool mis = false;
             if (misLobe != TRANSMISSION_LOBE)
             {
-                v3 lr = evaluateEnvironment(s, L, false, pixel2, screen);
+                v3 lr = evaluateEnvironment(S, L, false, pixel2, screen);
                 if (!isBlack(lr) && !isBlack(bsdf))
                 {
-                    float lpdf = s.env.has_light_tex && s.envLight.data
-                        ? luminance(lr) / s.env.light_tex_luminance_integral
+                    float lpdf = S.env.has_light_tex && S.envLight.data
+                        ? luminance(lr) / S.env.light_tex_luminance_integral
                         : divPi(0.25f);
                     v3 res = lr * misWeight(mpdf, lpdf) * bsdf / mpdf;
                     pslot[4] = make_float4(res.x, res.y, res.z, 0.f);
@@ -788,7 +897,7 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade_mis(DevS
                     slots |= 1u << 4;
                 }
                 float lpdf;
-                lr = sampleEnvironment(s, rnd, L, lpdf);
+                lr = sampleEnvironment(S, rnd, L, lpdf);
                 int el;
                 bsdf = evaluateMaterialAndPDF(m, mc, fr, V, L, rnd, mpdf, el);
                 if (!isBlack(lr) && !isBlack(bsdf))
@@ -840,16 +949,15 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade_mis(DevS
 }
 
 // Applies shadow visibility to the pending contributions and accumulates the segment.
-__global__ void k_resolve(agb_frame_data f, WaveBuffers wb, int bounce)
+template <bool kBatch>
+__global__ void k_resolve(agb_frame_data f, WaveBuffers wb, int bounce, BatchTables bt)
 {
     uint32_t n      = wb.counters[bounce * kCounterStride + CNT_RESOLVE];
     uint32_t stride = gridDim.x * blockDim.x;
-    const float clampLum = f.indirect_bounce_clamp_scale > 0.f
-        ? f.max_luminance * f.indirect_bounce_clamp_scale
-        : 0.f;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
     {
         uint32_t p    = wb.resolveList[i];
+        const float clampLum = bounceClamp(kBatch ? bt.frames[bt.pathReq[p]] : f);
         uint32_t bits = wb.pendBits[p];
         uint32_t occ  = wb.occluded[p];
         float4 e      = wb.pendEmission[p];
@@ -1104,10 +1212,11 @@ __global__ void k_ground_shadow(DevScene s, WaveBuffers wb, int bounce)
 }
 
 // Per pixel: final radiance of each sample of the wave in sample order, then accumulation.
-__global__ void k_finalize(agb_frame_data f, WaveParams wp, WaveBuffers wb)
+// One pixel of k_finalize: the final radiance of each of the wave's samples in sample order, then
+// the accumulation (paths of the pixel at pathBase + k x pixels + pixel).
+AGB_D void finalizePixelImpl(const agb_frame_data& f, const WaveParams& wp, const WaveBuffers& wb, uint32_t pixel,
+    uint32_t pathBase)
 {
-    uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < wp.pixels; pixel += stride)
     {
         float4 mean = make_float4(0.f, 0.f, 0.f, 0.f), sum = mean, comp = mean;
         if ((wp.accumMode & AGB_ACCUM_RUNNING_MEAN) && wp.sampleBase > 0)
@@ -1123,7 +1232,7 @@ __global__ void k_finalize(agb_frame_data f, WaveParams wp, WaveBuffers wb)
             mom = wb.accumMoments[pixel];
         for (uint32_t k = 0; k < wp.samples; k++)
         {
-            uint32_t p = k * wp.pixels + pixel;
+            uint32_t p = pathBase + k * wp.pixels + pixel;
             float4 a = wb.outDirect[p], b = wb.outDiffuse[p], c = wb.outGlossy[p];
             v3 fin = (v3{ a.x, a.y, a.z } + v3{ b.x, b.y, b.z }) + v3{ c.x, c.y, c.z };
             adjustRadiance(f.max_luminance, f.is_display_errors_enabled != 0, fin);
@@ -1178,9 +1287,50 @@ __global__ void k_finalize(agb_frame_data f, WaveParams wp, WaveBuffers wb)
     }
 }
 
+template <bool kBatch>
+__global__ void k_finalize(agb_frame_data f, WaveParams wp, WaveBuffers wbIn, BatchTables bt)
+{
+    uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t total = kBatch ? bt.pixelsTotal : wp.pixels;
+    for (uint32_t gq = blockIdx.x * blockDim.x + threadIdx.x; gq < total; gq += stride)
+    {
+        // A batched wave finalizes every request's pixels: the request's accumulation targets,
+        // sample range and frame.
+        WaveParams wp2  = wp;
+        WaveBuffers wb  = wbIn;
+        uint32_t pixel  = gq;
+        uint32_t pathBase = 0;
+        uint32_t r = 0;
+        if constexpr (kBatch)
+        {
+            r                     = batchRequestOfPixel(bt, gq);
+            const BatchRequest& q = bt.req[r];
+            pixel           = gq - q.pixelOffset;
+            pathBase        = q.pathOffset;
+            wp2.pixels      = q.pixels;
+            wp2.sampleBase  = q.sampleBase;
+            wp2.samples     = q.samples;
+            wp2.accumMode   = q.accumMode;
+            wb.accumMean    = q.accumMean;
+            wb.accumSum     = q.accumSum;
+            wb.accumComp    = q.accumComp;
+            wb.lastSample   = q.lastSample;
+            wb.accumMoments = q.accumMoments;
+        }
+        const agb_frame_data& F = kBatch ? bt.frames[r] : f;
+        finalizePixelImpl(F, wp2, wb, pixel, pathBase);
+    }
+}
+
+
 // ------------------------------------------------------------------------------ launchers
-void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp,
-    const WaveBuffers& wb, cudaStream_t st, int smCount, uint64_t& launches, KernelMarks* marks)
+// One wave: `depth` bounces (the frame's trace depth; a batched wave's deepest request), the
+// ground plane's kernels when the scene has one (single-request waves only), transparent or
+// opaque shadows as `forceOpaque` says.
+template <bool kBatch>
+void launchWaveT(const DevScene& s, const agb_frame_data& f, const WaveParams& wp, const WaveBuffers& wb,
+    const BatchTables& bt, int depth, bool forceOpaque, cudaStream_t st, int smCount, uint64_t& launches,
+    KernelMarks* marks)
 {
     auto mark = [&](int category) {
         if (marks)
@@ -1190,86 +1340,109 @@ void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp
     int shadeGrid = smCount * (kShadeMinBlocks > 8 ? kShadeMinBlocks : 8);
     int traceGrid = smCount * kTraceBlocksPerSM;
     mark(KC_CAMERA);
-    k_camera<<<grid, 256, 0, st>>>(f, wp, wb);
+    k_camera<kBatch><<<grid, 256, 0, st>>>(f, wp, wb, bt);
     launches++;
     int cur = 0;
-    int depth = f.trace_depth;
     size_t stackBytes = kTraceStackBytes;
     for (int b = 0; b <= depth; b++)
     {
         if (b == depth)
         {
             mark(KC_SHADE);
-            k_shade<<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 1);
+            k_shade<kBatch><<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 1, bt);
             launches++;
             break;
         }
         mark(KC_CLOSEST);
         if (wp.countTraversal)
-            k_trace_closest<true><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, cur);
+            k_trace_closest<true, kBatch><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, cur, bt);
         else
-            k_trace_closest<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, cur);
-        if (s.ground.enabled)
+            k_trace_closest<false, kBatch><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, cur, bt);
+        if (!kBatch && s.ground.enabled)
         {
             // Ground plane for the bounce's primary rays before they are shaded.
             mark(KC_SHADE);
             k_ground<<<grid, 256, 0, st>>>(s, f, wp, wb, b, cur);
             mark(KC_SHADOW);
             if (wp.countTraversal)
-                k_trace_shadow<true><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, CNT_GROUND_SHADOW,
-                    CNT_GROUND_WORK);
+                k_trace_shadow<true, false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b,
+                    CNT_GROUND_SHADOW, CNT_GROUND_WORK, bt);
             else
-                k_trace_shadow<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, CNT_GROUND_SHADOW,
-                    CNT_GROUND_WORK);
+                k_trace_shadow<false, false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b,
+                    CNT_GROUND_SHADOW, CNT_GROUND_WORK, bt);
             mark(KC_SHADE);
             k_ground_shadow<<<grid, 256, 0, st>>>(s, wb, b);
             launches += 3;
         }
         mark(KC_SHADE);
-        k_shade<<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 0);
+        k_shade<kBatch><<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 0, bt);
         mark(KC_SHADE);
-        k_shade_scatter<<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur);
+        k_shade_scatter<kBatch><<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, bt);
         mark(KC_SHADE);
-        k_shade_mis<<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b);
+        k_shade_mis<kBatch><<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, bt);
         mark(KC_SHADOW);
-        if (!f.is_force_opaque_shadows_enabled)
+        if (!forceOpaque)
         {
             if (wp.countTraversal)
-                k_trace_shadow_transparent<true><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b);
+                k_trace_shadow_transparent<true, kBatch><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, bt);
             else
-                k_trace_shadow_transparent<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b);
+                k_trace_shadow_transparent<false, kBatch><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, bt);
         }
         else if (wp.countTraversal)
-            k_trace_shadow<true><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, CNT_SHADOW, CNT_SHADOW_WORK);
+            k_trace_shadow<true, kBatch><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, CNT_SHADOW,
+                CNT_SHADOW_WORK, bt);
         else
-            k_trace_shadow<false><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, CNT_SHADOW, CNT_SHADOW_WORK);
+            k_trace_shadow<false, kBatch><<<traceGrid, kTraceBlock, stackBytes, st>>>(s, wb, b, CNT_SHADOW,
+                CNT_SHADOW_WORK, bt);
         mark(KC_RESOLVE);
-        k_resolve<<<grid, 256, 0, st>>>(f, wb, b);
+        k_resolve<kBatch><<<grid, 256, 0, st>>>(f, wb, b, bt);
         launches += 6;
         cur ^= 1;
     }
     mark(KC_FINALIZE);
-    k_finalize<<<grid, 256, 0, st>>>(f, wp, wb);
+    k_finalize<kBatch><<<grid, 256, 0, st>>>(f, wp, wb, bt);
     launches++;
     mark(KC_END);
+}
+
+void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp,
+    const WaveBuffers& wb, cudaStream_t st, int smCount, uint64_t& launches, KernelMarks* marks)
+{
+    BatchTables none{};
+    launchWaveT<false>(s, f, wp, wb, none, f.trace_depth, f.is_force_opaque_shadows_enabled != 0, st, smCount,
+        launches, marks);
+}
+
+void launchBatchWave(const DevScene& shared, const agb_frame_data& anyFrame, const WaveParams& wp,
+    const WaveBuffers& wb, const BatchTables& bt, int maxDepth, bool forceOpaque, cudaStream_t st, int smCount,
+    uint64_t& launches, KernelMarks* marks)
+{
+    launchWaveT<true>(shared, anyFrame, wp, wb, bt, maxDepth, forceOpaque, st, smCount, launches, marks);
+}
+
+template <class K>
+void traceAttributes(K kernel, int stackBytes, int carveout)
+{
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, stackBytes);
+    cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
 }
 
 void setTraceAttributes()
 {
     int stackBytes = int(kTraceStackBytes);
     int carveout   = traceCarveoutPercent();
-    cudaFuncSetAttribute(k_trace_closest<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, stackBytes);
-    cudaFuncSetAttribute(k_trace_closest<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, stackBytes);
-    cudaFuncSetAttribute(k_trace_shadow<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, stackBytes);
-    cudaFuncSetAttribute(k_trace_shadow<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, stackBytes);
-    cudaFuncSetAttribute(k_trace_closest<true>, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
-    cudaFuncSetAttribute(k_trace_closest<false>, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
-    cudaFuncSetAttribute(k_trace_shadow<true>, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
-    cudaFuncSetAttribute(k_trace_shadow<false>, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
-    cudaFuncSetAttribute(k_trace_shadow_transparent<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, stackBytes);
-    cudaFuncSetAttribute(k_trace_shadow_transparent<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, stackBytes);
-    cudaFuncSetAttribute(k_trace_shadow_transparent<true>, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
-    cudaFuncSetAttribute(k_trace_shadow_transparent<false>, cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
+    traceAttributes(k_trace_closest<true, false>, stackBytes, carveout);
+    traceAttributes(k_trace_closest<false, false>, stackBytes, carveout);
+    traceAttributes(k_trace_closest<true, true>, stackBytes, carveout);
+    traceAttributes(k_trace_closest<false, true>, stackBytes, carveout);
+    traceAttributes(k_trace_shadow<true, false>, stackBytes, carveout);
+    traceAttributes(k_trace_shadow<false, false>, stackBytes, carveout);
+    traceAttributes(k_trace_shadow<true, true>, stackBytes, carveout);
+    traceAttributes(k_trace_shadow<false, true>, stackBytes, carveout);
+    traceAttributes(k_trace_shadow_transparent<true, false>, stackBytes, carveout);
+    traceAttributes(k_trace_shadow_transparent<false, false>, stackBytes, carveout);
+    traceAttributes(k_trace_shadow_transparent<true, true>, stackBytes, carveout);
+    traceAttributes(k_trace_shadow_transparent<false, true>, stackBytes, carveout);
 }
 
 } // namespace agb

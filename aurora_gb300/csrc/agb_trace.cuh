@@ -14,6 +14,7 @@
 #pragma once
 
 #include <type_traits>
+#include <utility>
 
 #include "agb_scene.cuh"
 
@@ -276,6 +277,25 @@ struct WriterRestarts<W, std::void_t<decltype(W::kRestart)>>
     static constexpr bool value = W::kRestart;
 };
 
+// The TLAS root a ray starts from: the scene's, or the loader's own per-ray root (batched waves,
+// where rays of several scenes share a queue).
+template <class L, class = void>
+struct LoaderHasRoot : std::false_type
+{
+};
+template <class L>
+struct LoaderHasRoot<L, decltype(void(std::declval<const L&>().root(0u)))> : std::true_type
+{
+};
+template <class Loader>
+AGB_D int32_t rayRoot(const Loader& load, const DevScene& s, uint32_t i)
+{
+    if constexpr (LoaderHasRoot<Loader>::value)
+        return load.root(i);
+    else
+        return s.instanceCount > 0 ? s.tlasRoot : kDone;
+}
+
 template <bool kAnyHit, bool kCount, class Loader, class Writer>
 AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const Loader& load,
     const Writer& write, int32_t* stack, int stride, TraceCounters& cnt, bool& overflow)
@@ -334,7 +354,7 @@ AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const 
                     load(rayIdx, o, d, tmin, tmax);
                     tmaxRay  = tmax;
                     sr       = slabSetup(o, d);
-                    ref      = s.instanceCount > 0 ? s.tlasRoot : kDone;
+                    ref      = rayRoot(load, s, rayIdx);
                     leaf     = 0;
                     leaf2    = 0;
                     sp       = 0;
@@ -506,7 +526,7 @@ AGB_D void persistentTrace(const DevScene& s, uint32_t n, uint32_t* work, const 
                 else
                 {
                     // Trace the ray again beyond the hit (the writer moved tmin past it).
-                    ref      = s.instanceCount > 0 ? s.tlasRoot : kDone;
+                    ref      = rayRoot(load, s, rayIdx);
                     sp       = 0;
                     inst     = -1;
                     nodes    = reinterpret_cast<const float4*>(s.tlas);

@@ -112,4 +112,69 @@ struct WaveParams
     uint32_t seedOffset;          // added to the sample index that seeds the random streams
 };
 
+// Batched wavefronts (agb_batch_render): one wave over the paths of several requests, of
+// different scenes and resolutions.  Request r owns paths [pathOffset, pathOffset + pixels x
+// samples) laid out like a single request's wave (local path = sample x pixels + pixel), so its
+// random streams, and therefore its image, are those of the request rendered alone.  The scenes
+// of a batch share one device namespace (meshes, instances, TLAS nodes, materials, images and
+// layers concatenated, indices offset); each scene-table entry carries that namespace plus the
+// scene's own TLAS root, environment and ground plane.
+struct BatchRequest
+{
+    uint32_t pathOffset, pixelOffset, pixels, width;
+    uint32_t height, sampleBase, samples, aovSample;
+    uint32_t seedOffset, accumMode;
+    int32_t scene;      // index into BatchTables::scenes
+    int32_t traceDepth; // the request's frame trace depth
+    int32_t tlasRoot;   // the scene's TLAS root in the shared namespace (kDone: no instances)
+    int32_t _pad[3];
+    float4* accumMean;
+    float4* accumSum;
+    float4* accumComp;
+    float4* lastSample;
+    float2* accumMoments;
+    float* aovDepth;
+    float4* aovNormal;
+    float4* aovAlbedo;
+    float4* aovMotion;
+};
+
+struct BatchTables
+{
+    const BatchRequest* req;      // null: a single-request wave
+    const agb_frame_data* frames; // one per request
+    const DevScene* scenes;
+    uint16_t* pathReq;            // request index per path
+    uint32_t requestCount;
+    uint32_t pixelsTotal;         // sum of the requests' pixels (finalize)
+};
+
+// Request owning path p (requests sorted by pathOffset; a short binary search over the table).
+AGB_D uint32_t batchRequestOfPath(const BatchTables& bt, uint32_t p)
+{
+    uint32_t lo = 0, hi = bt.requestCount;
+    while (hi - lo > 1)
+    {
+        uint32_t mid = (lo + hi) >> 1;
+        if (bt.req[mid].pathOffset <= p)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+AGB_D uint32_t batchRequestOfPixel(const BatchTables& bt, uint32_t q)
+{
+    uint32_t lo = 0, hi = bt.requestCount;
+    while (hi - lo > 1)
+    {
+        uint32_t mid = (lo + hi) >> 1;
+        if (bt.req[mid].pixelOffset <= q)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
 } // namespace agb

@@ -645,6 +645,35 @@ AGB_API agb_status agb_server_submit(agb_server* srv, const agb_serve_request* r
 AGB_API agb_status agb_server_wait(agb_server* srv, uint64_t id, int32_t timeout_ms,
     agb_serve_result* result, float* host_rgba, uint64_t capacity);
 AGB_API agb_status agb_server_memory(agb_server* srv, uint64_t* scene_bytes, uint64_t* render_bytes);
+/* Batched rendering (no counterpart in the reference): several views or contexts, of one or
+ * several scenes and of any resolutions, rendered by one wavefront, each stage one kernel launch
+ * over the paths of all of them.  Every path carries its request: its scene (the scenes' BVHs,
+ * materials and images share one device namespace built by the batch, rebuilt when a scene
+ * changes), frame data, resolution, sample range and accumulation targets.  A view's image is the
+ * one agb_render gives it alone (same random streams per pixel and sample).  The serving loop uses
+ * this to merge the requests it has admitted.
+ *   agb_batch_create: stream may be null (one is created); max_paths_in_flight bounds a wave (the
+ *     requests' samples are split over several waves beyond it, each request taking a share in
+ *     proportion to what it still needs).
+ *   agb_batch_render: views[i] renders sample_counts[i] samples from sample_starts[i] (null: 0)
+ *     with options[i] (width, height, accumulation, seed_offset; max_paths_in_flight and
+ *     env_filter_linear are ignored) and the frame data set on it.  Views must not repeat, must
+ *     agree on is_force_opaque_shadows_enabled, and their scenes must have no ground plane.
+ *     Asynchronous: the views' own streams wait for the batch, so agb_accum_read and the denoiser
+ *     calls on a view see its result; agb_batch_poll reports completion.  With stats it waits and
+ *     fills them (paths, rays, launches, device time). */
+typedef struct agb_batch agb_batch;
+AGB_API agb_status agb_batch_create(int32_t device, void* cuda_stream, uint64_t max_paths_in_flight,
+    agb_batch** out);
+AGB_API agb_status agb_batch_destroy(agb_batch* batch);
+AGB_API agb_status agb_batch_render(agb_batch* batch, agb_context* const* views,
+    const agb_render_options* options, const uint32_t* sample_starts, const uint32_t* sample_counts,
+    uint32_t count, agb_render_stats* stats);
+/* AGB_OK once the last agb_batch_render has finished on the device, AGB_ERR_NOT_READY before. */
+AGB_API agb_status agb_batch_poll(agb_batch* batch);
+/* Per-kernel-family device times in agb_batch_render's stats (like agb_set_profiling). */
+AGB_API agb_status agb_batch_set_profiling(agb_batch* batch, int32_t enabled);
+
 /* Halton (2, 3) camera jitter in pixels, centred on [-0.5, 0.5] (PTRenderer.cpp:81-95,159-174):
  * index = (phase_count ? frame_index % phase_count : frame_index) + 1. */
 AGB_API void agb_temporal_jitter(uint32_t frame_index, uint32_t phase_count, float out[2]);
