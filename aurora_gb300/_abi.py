@@ -222,6 +222,7 @@ SIGNATURES = {
     "agb_batch_destroy": (_I32, [_P]),
     "agb_batch_render": (_I32, [_P, _P, _P, _P, _P, _U32, _P]),
     "agb_batch_poll": (_I32, [_P]),
+    "agb_batch_set_scenes": (_I32, [_P, _P, _U32]),
     "agb_batch_set_profiling": (_I32, [_P, _I32]),
     "agb_accum_read_rect": (_I32, [_P, _I32, _U32, _U32, _U32, _U32, _P, _U64]),
     "agb_accum_read": (_I32, [_P, _I32, _P, _U64]),

@@ -1571,7 +1571,25 @@ AGB_API agb_status agb_batch_render(agb_batch* b, agb_context* const* views, con
             if (views[j] == v)
                 return fail(AGB_ERR_INVALID_ARG, "agb_batch_render: a view appears twice");
     }
-    if ((st = buildSharedScenes(b, scenes)))
+    // The namespace set by agb_batch_set_scenes when it holds every scene of the call (and none
+    // changed); otherwise one over this call's scenes.
+    bool covered = !b->scenes.empty();
+    for (size_t k = 0; covered && k < scenes.size(); k++)
+        covered = std::find(b->scenes.begin(), b->scenes.end(), scenes[k]) != b->scenes.end();
+    if (covered)
+    {
+        std::vector<agb_context*> keep;
+        for (const agb_context* c : b->scenes)
+            keep.push_back(const_cast<agb_context*>(c));
+        if ((st = buildSharedScenes(b, keep)))
+            return st;
+        for (uint32_t i = 0; i < count; i++)
+        {
+            agb_context* sc = views[i]->parent ? views[i]->parent : views[i];
+            sceneOf[i]      = int32_t(std::find(b->scenes.begin(), b->scenes.end(), sc) - b->scenes.begin());
+        }
+    }
+    else if ((st = buildSharedScenes(b, scenes)))
         return st;
     // Render targets, accumulation bookkeeping and AOVs of every view (on its own stream, which the
     // batch then waits for).
@@ -1769,6 +1787,25 @@ AGB_API agb_status agb_batch_render(agb_batch* b, agb_context* const* views, con
     }
     (void)waves;
     return AGB_OK;
+}
+
+AGB_API agb_status agb_batch_set_scenes(agb_batch* b, agb_context* const* scenes, uint32_t count)
+{
+    if (!b || (!scenes && count))
+        return fail(AGB_ERR_INVALID_ARG, "agb_batch_set_scenes: bad argument");
+    std::vector<agb_context*> list;
+    for (uint32_t i = 0; i < count; i++)
+    {
+        if (!scenes[i] || scenes[i]->parent)
+            return fail(AGB_ERR_INVALID_ARG, "agb_batch_set_scenes: contexts with scenes required");
+        if (std::find(list.begin(), list.end(), scenes[i]) == list.end())
+            list.push_back(scenes[i]);
+    }
+    agb_status st = setDevice(b->work);
+    if (st)
+        return st;
+    AGB_CUDA(cudaStreamSynchronize(b->work->stream), "agb_batch_set_scenes");
+    return buildSharedScenes(b, list);
 }
 
 AGB_API agb_status agb_batch_poll(agb_batch* b)

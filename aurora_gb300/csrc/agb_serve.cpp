@@ -4,11 +4,16 @@
 // total latency.
 //
 // Scenes are agb_contexts uploaded by the caller and registered with their HBM footprint; the
-// server refuses scenes beyond its HBM budget.  Each running request renders through a view of its
-// scene (agb_view_create: own stream, frame, accumulation) so requests overlap on the device;
-// views are pooled per scene and reused, and idle views are destroyed when a new request needs
-// their memory.  A request's render state (wave buffers, accumulation, AOVs) is reserved against
-// the budget before it is admitted; requests are admitted in arrival order.
+// server refuses scenes beyond its HBM budget.  Admitted requests are merged into batches: every
+// batch is one agb_batch_render, a wavefront whose every stage is a single kernel launch over the
+// paths of all of its requests, whatever their scenes and resolutions.  Two batches are in flight
+// at once, so requests that arrive while one renders form the next, which starts at once and
+// overlaps it on the device.  Each request keeps its own render state in a view of its scene
+// (agb_view_create: frame, accumulation, AOVs), pooled per scene and reused; idle views are
+// destroyed when a new request needs their memory.  A request's render state is reserved against
+// the budget before it is admitted; requests are admitted in arrival order.  A batch the batched
+// renderer refuses (a scene with a ground plane) renders request by request on the views' own
+// streams instead.
 //
 // Threads: the scheduler thread is the only one that calls the render entry points on views;
 // callers submit and wait from any thread.  Scenes must not change while the server runs.
@@ -38,8 +43,14 @@ double msSince(Clock::time_point t0, Clock::time_point t1)
     return std::chrono::duration<double, std::milli>(t1 - t0).count();
 }
 
-// Paths in flight per request wave; bounds a slot's wave buffers (agb_bytes_per_path each).
+// Paths in flight per request wave of a request rendered alone; bounds its wave buffers
+// (agb_bytes_per_path each).
 constexpr uint64_t kServeWavePaths = 1u << 21;
+// Paths in flight per batch wave (each of the two batches holds wave buffers for this many): a
+// quarter of the HBM budget over the two batches, between 4096 and 2^24 paths.
+constexpr uint64_t kBatchWavePathsMax = 1u << 24;
+constexpr uint64_t kBatchWavePathsMin = 4096;
+constexpr int kBatches                = 2;
 // Per pixel: running mean, Kahan sum and compensation, last sample (16 B each), moments (8 B),
 // AOVs (52 B), temporal history (32 B).
 constexpr uint64_t kBytesPerPixel = 4 * 16 + 8 + 52 + 32;
@@ -64,13 +75,19 @@ struct Scene
     std::vector<agb_context*> idle;
 };
 
+// A request's own render state (its batch's wave buffers are reserved with the batch).
 uint64_t estimateBytes(const agb_serve_request& r)
 {
     uint64_t pixels = uint64_t(r.width) * r.height;
-    uint64_t spw    = std::max<uint64_t>(1, kServeWavePaths / std::max<uint64_t>(1, pixels));
-    uint64_t paths  = std::min<uint64_t>(r.spp, spw) * pixels;
-    return pixels * kBytesPerPixel + paths * agb_bytes_per_path() + (1u << 20);
+    return pixels * kBytesPerPixel + (1u << 20);
 }
+
+struct Batch
+{
+    agb_batch* handle = nullptr;
+    std::vector<Request*> requests;
+    bool busy = false;
+};
 
 } // namespace
 
@@ -85,7 +102,9 @@ struct agb_server
     std::condition_variable wake, doneCv;
     std::map<int32_t, Scene> scenes;
     std::deque<Request*> queue;
-    std::vector<Request*> running;
+    std::vector<Request*> running; // rendered alone on their views' streams
+    Batch batches[kBatches];
+    uint64_t batchBytes = 0;       // wave buffers of the batches
     std::map<uint64_t, std::unique_ptr<Request>> all;
     uint64_t nextId     = 1;
     uint64_t sceneBytes = 0, reserved = 0, pooled = 0;
@@ -98,7 +117,10 @@ struct agb_server
 
     void run();
     bool admit(Request* r, std::unique_lock<std::mutex>& lk);
+    agb_status renderAlone(Request* r);
+    void launch(Batch& b);
     void finish(Request* r);
+    void release(Request* r);
     void failRequest(Request* r, agb_status st, const std::string& msg);
     void evictIdle(uint64_t need);
 };
@@ -117,7 +139,7 @@ void agb_server::evictIdle(uint64_t need)
     for (auto& kv : scenes)
     {
         Scene& sc = kv.second;
-        while (!sc.idle.empty() && sceneBytes + reserved + pooled + need > budget)
+        while (!sc.idle.empty() && sceneBytes + batchBytes + reserved + pooled + need > budget)
         {
             agb_context* v = sc.idle.back();
             sc.idle.pop_back();
@@ -129,7 +151,8 @@ void agb_server::evictIdle(uint64_t need)
     }
 }
 
-// Starts a request (lock held).  Returns false when it must wait for memory.
+// Reserves a request's memory and gives it a view with its frame set (lock held).  Returns false
+// when it must wait for memory.
 bool agb_server::admit(Request* r, std::unique_lock<std::mutex>&)
 {
     auto it = scenes.find(r->req.scene);
@@ -149,11 +172,14 @@ bool agb_server::admit(Request* r, std::unique_lock<std::mutex>&)
     }
     // A pooled view's memory is already counted; reserve only what it may still need to grow.
     uint64_t extra = need > viewBytes ? need - viewBytes : 0;
-    if (sceneBytes + reserved + pooled + extra > budget)
+    if (sceneBytes + batchBytes + reserved + pooled + extra > budget)
         evictIdle(extra);
-    if (sceneBytes + reserved + pooled + extra > budget)
+    if (sceneBytes + batchBytes + reserved + pooled + extra > budget)
     {
-        if (running.empty())
+        bool idle = running.empty();
+        for (const Batch& b : batches)
+            idle = idle && !b.busy;
+        if (idle)
         {
             failRequest(r, AGB_ERR_OOM, "request does not fit the HBM budget");
             return true;
@@ -175,37 +201,88 @@ bool agb_server::admit(Request* r, std::unique_lock<std::mutex>&)
     reserved += r->reserved;
     r->tStart = Clock::now();
     agb_frame_data f = r->req.frame;
-    bool denoise     = (r->req.flags & AGB_SERVE_DENOISE) && denoiser;
-    if (denoise)
+    if ((r->req.flags & AGB_SERVE_DENOISE) && denoiser)
         f.is_denoising_aovs_enabled = 1;
+    agb_status st = agb_frame_set(view, &f);
+    if (st)
+    {
+        std::string msg = agb_last_error();
+        release(r);
+        failRequest(r, st, msg);
+    }
+    return true;
+}
+
+agb_render_options requestOptions(const Request* r, bool denoise)
+{
     agb_render_options opt{};
     opt.width               = r->req.width;
     opt.height              = r->req.height;
     opt.accumulation        = AGB_ACCUM_RUNNING_MEAN | (denoise ? AGB_ACCUM_MOMENTS : 0u);
     opt.max_paths_in_flight = uint32_t(kServeWavePaths);
     opt.seed_offset         = r->req.seed_offset;
-    agb_status st = agb_frame_set(view, &f);
-    if (!st)
-        st = agb_render(view, &opt, 0, r->req.spp, nullptr);
-    if (st)
+    return opt;
+}
+
+// Renders a request on its view's own stream (requests of scenes the batched renderer refuses).
+agb_status agb_server::renderAlone(Request* r)
+{
+    bool denoise = (r->req.flags & AGB_SERVE_DENOISE) && denoiser;
+    agb_render_options opt = requestOptions(r, denoise);
+    return agb_render(r->view, &opt, 0, r->req.spp, nullptr);
+}
+
+// Starts a batch over its admitted requests (lock held).
+void agb_server::launch(Batch& b)
+{
+    std::vector<agb_context*> views;
+    std::vector<agb_render_options> opts;
+    std::vector<uint32_t> counts;
+    for (Request* r : b.requests)
     {
-        std::string msg = agb_last_error();
-        reserved -= r->reserved;
-        sc.idle.push_back(view);
-        uint64_t b = 0;
-        agb_context_memory(view, &b);
-        pooled += b;
-        r->view = nullptr;
-        failRequest(r, st, msg);
-        return true;
+        views.push_back(r->view);
+        opts.push_back(requestOptions(r, (r->req.flags & AGB_SERVE_DENOISE) && denoiser));
+        counts.push_back(r->req.spp);
     }
-    running.push_back(r);
-    return true;
+    agb_status st = agb_batch_render(b.handle, views.data(), opts.data(), nullptr, counts.data(),
+        uint32_t(views.size()), nullptr);
+    if (st == AGB_OK)
+    {
+        b.busy = true;
+        return;
+    }
+    // Not batchable: each request renders alone.
+    for (Request* r : b.requests)
+    {
+        st = renderAlone(r);
+        if (st)
+        {
+            std::string msg = agb_last_error();
+            release(r);
+            failRequest(r, st, msg);
+        }
+        else
+            running.push_back(r);
+    }
+    b.requests.clear();
+}
+
+// Returns a request's view to its scene's pool and its reservation to the budget.
+void agb_server::release(Request* r)
+{
+    if (!r->view)
+        return;
+    Scene& sc = scenes[r->req.scene];
+    reserved -= std::min(reserved, r->reserved);
+    uint64_t b = 0;
+    agb_context_memory(r->view, &b);
+    pooled += b;
+    sc.idle.push_back(r->view);
+    r->view = nullptr;
 }
 
 void agb_server::finish(Request* r)
 {
-    Scene& sc = scenes[r->req.scene];
     uint64_t pixels = uint64_t(r->req.width) * r->req.height;
     r->rgba.resize(pixels * 4);
     agb_status st = AGB_OK;
@@ -235,12 +312,7 @@ void agb_server::finish(Request* r)
     if (st)
         r->error = agb_last_error();
     r->tDone = Clock::now();
-    reserved -= std::min(reserved, r->reserved);
-    uint64_t b = 0;
-    agb_context_memory(r->view, &b);
-    pooled += b;
-    sc.idle.push_back(r->view);
-    r->view     = nullptr;
+    release(r);
     r->finished = true;
     doneCv.notify_all();
 }
@@ -251,9 +323,21 @@ void agb_server::run()
     std::unique_lock<std::mutex> lk(mu);
     for (;;)
     {
-        if (stop && queue.empty() && running.empty())
+        bool busy = !running.empty();
+        for (const Batch& b : batches)
+            busy = busy || b.busy;
+        if (stop && queue.empty() && !busy)
             break;
-        // Completions: a request is done when its view's work has drained.
+        // Completions: a batch is done when its wavefront has drained; a request rendered alone
+        // when its view's work has.
+        for (Batch& b : batches)
+            if (b.busy && agb_batch_poll(b.handle) != AGB_ERR_NOT_READY)
+            {
+                for (Request* r : b.requests)
+                    finish(r);
+                b.requests.clear();
+                b.busy = false;
+            }
         for (size_t i = 0; i < running.size();)
         {
             Request* r = running[i];
@@ -265,15 +349,34 @@ void agb_server::run()
             else
                 i++;
         }
-        // Admissions in arrival order while slots are free.
-        while (!queue.empty() && int(running.size()) < maxSlots)
+        // Admissions in arrival order into a free batch while slots are free; the batch starts
+        // at once with what has arrived (continuous batching).
+        int inFlight = int(running.size());
+        for (const Batch& b : batches)
+            inFlight += int(b.requests.size());
+        for (Batch& b : batches)
         {
-            Request* r = queue.front();
-            if (!admit(r, lk))
-                break;
-            queue.pop_front();
+            if (b.busy || queue.empty() || inFlight >= maxSlots)
+                continue;
+            while (!queue.empty() && inFlight < maxSlots)
+            {
+                Request* r = queue.front();
+                if (!admit(r, lk))
+                    break;
+                queue.pop_front();
+                if (r->view)
+                {
+                    b.requests.push_back(r);
+                    inFlight++;
+                }
+            }
+            if (!b.requests.empty())
+                launch(b);
         }
-        if (running.empty() && queue.empty())
+        busy = !running.empty();
+        for (const Batch& b : batches)
+            busy = busy || b.busy;
+        if (!busy && queue.empty())
         {
             wake.wait(lk);
             continue;
@@ -296,6 +399,19 @@ AGB_API agb_status agb_server_create(int32_t device, uint64_t hbm_budget_bytes, 
     s->device   = device;
     s->budget   = hbm_budget_bytes;
     s->maxSlots = max_slots;
+    // The batches' wave buffers are reserved up front.
+    uint64_t batchPaths = hbm_budget_bytes / 4 / (uint64_t(kBatches) * agb_bytes_per_path());
+    batchPaths          = std::min(kBatchWavePathsMax, std::max(kBatchWavePathsMin, batchPaths));
+    s->batchBytes       = uint64_t(kBatches) * batchPaths * agb_bytes_per_path();
+    if (s->batchBytes > hbm_budget_bytes / 2)
+        return AGB_ERR_INVALID_ARG;
+    for (Batch& b : s->batches)
+        if (agb_batch_create(device, nullptr, batchPaths, &b.handle) != AGB_OK)
+        {
+            for (Batch& c : s->batches)
+                agb_batch_destroy(c.handle);
+            return AGB_ERR_CUDA;
+        }
     agb_server* p = s.get();
     s->worker     = std::thread([p] { p->run(); });
     *out          = s.release();
@@ -313,6 +429,8 @@ AGB_API agb_status agb_server_destroy(agb_server* srv)
     srv->wake.notify_all();
     srv->worker.join();
     cudaSetDevice(srv->device);
+    for (Batch& b : srv->batches)
+        agb_batch_destroy(b.handle);
     for (auto& kv : srv->scenes)
         for (agb_context* v : kv.second.idle)
             agb_context_destroy(v);
@@ -333,10 +451,18 @@ AGB_API agb_status agb_server_add_scene(agb_server* srv, int32_t scene_id, agb_c
     std::lock_guard<std::mutex> g(srv->mu);
     if (srv->scenes.count(scene_id))
         return AGB_ERR_INVALID_ARG;
-    if (srv->sceneBytes + bytes > srv->budget)
+    if (srv->sceneBytes + srv->batchBytes + bytes > srv->budget)
         return AGB_ERR_OOM;
     srv->scenes[scene_id] = Scene{ ctx, bytes, {} };
     srv->sceneBytes += bytes;
+    // The batches' shared namespace holds every registered scene, so batches of any mix of them
+    // reuse it.
+    std::vector<agb_context*> all;
+    for (auto& kv : srv->scenes)
+        all.push_back(kv.second.ctx);
+    for (Batch& b : srv->batches)
+        if (!b.busy)
+            agb_batch_set_scenes(b.handle, all.data(), uint32_t(all.size()));
     return AGB_OK;
 }
 
@@ -414,6 +540,6 @@ AGB_API agb_status agb_server_memory(agb_server* srv, uint64_t* scene_bytes, uin
     if (scene_bytes)
         *scene_bytes = srv->sceneBytes;
     if (render_bytes)
-        *render_bytes = srv->reserved + srv->pooled;
+        *render_bytes = srv->batchBytes + srv->reserved + srv->pooled;
     return AGB_OK;
 }

@@ -181,17 +181,17 @@ def bench_time_to_rel_mse(torch, _abi, r, s, target=1e-3, ref_spp=16384, max_spp
 
 
 def bench_serving(api, _abi, n_requests, rates=(200.0, 25.0)):
-    """Serving loop on 8 resident scenes (4 of the small type, 4 instanced-icosphere scenes of the
-    large type at reduced size), Poisson arrivals, resolutions {640x360, 1280x720, 1920x1080} x
-    spp {1, 4, 16}, a Halton camera jitter per request, 150 GB HBM budget, 8 slots."""
+    """Serving loop on 8 resident scenes (seeds 0-7: the small configuration's type at even seeds,
+    the large configuration's at odd ones, both at full size), Poisson arrivals, resolutions
+    {640x360, 1280x720, 1920x1080} x spp {1, 4, 16}, a Halton camera jitter per request, 150 GB HBM
+    budget, 32 requests in flight, merged into batched wavefronts."""
     from aurora_gb300 import scenes
     rs, frames = [], []
     for k in range(8):
         if k % 2 == 0:
             sc = scenes.config_small(seed=k, width=1920, height=1080, spp=1)
         else:
-            sc = scenes.config_large(seed=k, width=1920, height=1080, spp=1, level=7, instances=16,
-                                     env_size=(512, 256))
+            sc = scenes.config_large(seed=k, width=1920, height=1080, spp=1)
         r = api.Renderer()
         r.upload(sc)
         rs.append(r)
@@ -201,7 +201,7 @@ def bench_serving(api, _abi, n_requests, rates=(200.0, 25.0)):
     try:
         for rate in rates:
             rng = np.random.default_rng(7)
-            with api.Server(hbm_budget_bytes=150 << 30, max_slots=8) as srv:
+            with api.Server(hbm_budget_bytes=150 << 30, max_slots=32) as srv:
                 for k, r in enumerate(rs):
                     _abi.check(srv.add_scene(k, r))
                 tickets, paths = [], 0

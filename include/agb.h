@@ -669,6 +669,11 @@ AGB_API agb_status agb_batch_destroy(agb_batch* batch);
 AGB_API agb_status agb_batch_render(agb_batch* batch, agb_context* const* views,
     const agb_render_options* options, const uint32_t* sample_starts, const uint32_t* sample_counts,
     uint32_t count, agb_render_stats* stats);
+/* Builds the batch's shared namespace over these scenes (contexts, not views) ahead of the renders:
+ * later calls whose scenes are all among them reuse it (rebuilt only when one of them changes).
+ * Without it, each call builds the namespace over its own scenes when they differ from the last
+ * call's.  Waits for the batch's previous work. */
+AGB_API agb_status agb_batch_set_scenes(agb_batch* batch, agb_context* const* scenes, uint32_t count);
 /* AGB_OK once the last agb_batch_render has finished on the device, AGB_ERR_NOT_READY before. */
 AGB_API agb_status agb_batch_poll(agb_batch* batch);
 /* Per-kernel-family device times in agb_batch_render's stats (like agb_set_profiling). */
