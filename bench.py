@@ -58,6 +58,8 @@ def parse_args():
     p.add_argument("--spp", type=int, default=None, help="samples per pixel override (profiling runs)")
     p.add_argument("--no-denoiser", action="store_true", help="skip the denoiser measurement")
     p.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    p.add_argument("--no-denoised-serving", action="store_true",
+                   help="skip training the denoiser and the denoised-serving measurement")
     p.add_argument("--no-time-to-error", action="store_true", help="skip the time-to-relMSE measurement")
     p.add_argument("--serve-requests", type=int, default=160)
     p.add_argument("--ground-plane", action="store_true",
@@ -237,6 +239,115 @@ def bench_serving(api, _abi, n_requests, rates=(200.0, 25.0)):
         for r in rs:
             r.close()
     return out
+
+
+def bench_denoised_serving(api, _abi, train_scenes=48, views=8, steps=6000, eval_size=(640, 360),
+                           ref_spp=4096, repeats=7):
+    """The learned denoiser trained on the tracer's own pairs, then served: relMSE (eps 1e-2)
+    against converged references of plain accumulation at 1-256 spp and of the denoised output at
+    1 and 4 spp, each frame's serving latency (one request at a time, so the latency is the
+    request's own, not queueing), and the latency ratio at equal relMSE.
+
+    Training: `train_scenes` seeded scenes alternating the two plain-method types (256x256 views
+    from random orbit cameras, `views` per scene), noisy input at 1 or 4 spp (half each), targets at
+    256 spp from independent streams; `steps` Adam steps of 4 views (lr 1.5e-4 cosine to 7.5e-6).
+    Evaluation: the 8 serving scenes (seeds 0-7, the small configuration's type at even seeds, the
+    large one's at odd seeds, full size) seen from their own cameras at eval_size, references at
+    ref_spp from independent streams."""
+    import torch
+    from aurora_gb300 import denoiser_training as dt, scenes
+    t0 = time.perf_counter()
+    parts = [dt.make_pairs(train_scenes // 2, views, size=256, spp_lo=lo, spp_hi=256, seed=lo)
+             for lo in (1, 4)]
+    feats = torch.cat([p[0] for p in parts])
+    refs = torch.cat([p[2] for p in parts])
+    pair_s = time.perf_counter() - t0
+    dn = dt.Denoiser(seed=11)
+    t0 = time.perf_counter()
+    losses = dn.train(feats, refs, steps, batch=4, lr=1.5e-4, lr_min=7.5e-6)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    del feats, refs, parts
+    w, h = eval_size
+    plain_spp = [1, 2, 4, 8, 16, 32, 64, 128, 256]
+    den_spp = [1, 4]
+    rows = []
+    rs = []
+    try:
+        for k in range(8):
+            sc = (scenes.config_small(seed=k, width=w, height=h, spp=1) if k % 2 == 0 else
+                  scenes.config_large(seed=k, width=w, height=h, spp=1))
+            r = api.Renderer()
+            r.upload(sc)
+            rs.append((r, sc))
+        with api.Server(hbm_budget_bytes=150 << 30, max_slots=4) as srv:
+            srv.set_denoiser(dn.handle)
+            for k, (r, sc) in enumerate(rs):
+                srv.add_scene(k, r)
+            for k, (r, sc) in enumerate(rs):
+                r.set_frame(sc.frame)
+                r.render(0, ref_spp, width=w, height=h, accumulation=_abi.ACCUM_KAHAN, seed_offset=1 << 26)
+                ref = r.read(_abi.ACCUM_KAHAN, w, h).copy()
+                row = {"scene": k, "type": "small" if k % 2 == 0 else "large", "plain": {}, "denoised": {}}
+                for mode, spps in (("plain", plain_spp), ("denoised", den_spp)):
+                    for spp in spps:
+                        lat, err = [], []
+                        for rep in range(repeats):
+                            st, img, info = srv.wait(srv.submit(k, sc.frame, w, h, spp, seed_offset=rep * 977,
+                                                                denoise=mode == "denoised"))
+                            _abi.check(st)
+                            lat.append(info["latency_ms"])
+                            err.append(rel_mse_np(img, ref))
+                        row[mode][spp] = {"rel_mse": float(np.mean(err)), "p50_ms": float(np.percentile(lat, 50)),
+                                          "p99_ms": float(np.percentile(lat, 99))}
+                rows.append(row)
+    finally:
+        for r, _ in rs:
+            r.close()
+        dn.close()
+
+    def mean_over(kind, mode, spp, key):
+        return float(np.mean([r[mode][spp][key] for r in rows if kind in (None, r["type"])]))
+
+    summary = {}
+    for kind in (None, "small", "large"):
+        tag = kind or "all"
+        plain = [(spp, mean_over(kind, "plain", spp, "rel_mse"), mean_over(kind, "plain", spp, "p50_ms"))
+                 for spp in plain_spp]
+        entry = {"plain": {str(spp): {"rel_mse": e, "p50_ms": t} for spp, e, t in plain}}
+        for spp in den_spp:
+            e_d = mean_over(kind, "denoised", spp, "rel_mse")
+            t_d = mean_over(kind, "denoised", spp, "p50_ms")
+            # The plain sample count of equal relMSE, interpolated on log-log between the measured
+            # counts; its latency likewise (None when plain accumulation never gets there here).
+            eq = None
+            for (s0, e0, t0_), (s1, e1, t1_) in zip(plain, plain[1:]):
+                if e0 >= e_d >= e1 and e0 > 0 and e1 > 0:
+                    a = math.log(e0 / e_d) / math.log(e0 / e1) if e0 != e1 else 0.0
+                    eq = (s0 * (s1 / s0) ** a, t0_ * (t1_ / t0_) ** a)
+                    break
+            if eq is None and e_d <= plain[0][1] and e_d < plain[-1][1]:
+                eq = None
+            entry[f"denoised_{spp}spp"] = {
+                "rel_mse": e_d, "p50_ms": t_d,
+                "plain_spp_at_equal_rel_mse": eq[0] if eq else None,
+                "plain_p50_ms_at_equal_rel_mse": eq[1] if eq else None,
+                "p50_latency_ratio": (eq[1] / t_d) if eq else None,
+                "beyond_measured_plain_range": eq is None and e_d < plain[-1][1]}
+        summary[tag] = entry
+    return {"resolution": [w, h], "reference_spp": ref_spp, "eps": 1e-2, "repeats": repeats,
+            "training": {"scenes": train_scenes, "views_per_scene": views, "crop": 256,
+                         "noisy_spp": [1, 4], "target_spp": 256, "steps": steps, "batch": 4,
+                         "pairs_seconds": pair_s, "train_seconds": train_s,
+                         "loss_first_100": float(np.mean(losses[:100])),
+                         "loss_last_100": float(np.mean(losses[-100:]))},
+            "summary": summary, "per_scene": rows}
+
+
+def rel_mse_np(x, ref, eps=1e-2):
+    x = np.asarray(x, np.float64)[..., :3]
+    r = np.asarray(ref, np.float64)[..., :3]
+    return float(np.mean((x - r) ** 2 / (r * r + eps)))
 
 
 def dist_env():
@@ -695,6 +806,8 @@ def main():
         out["denoiser"] = bench_denoiser(torch, _abi, stream, measured_peaks())
     if world == 1 and not args.no_serve:
         out["serving"] = bench_serving(api, _abi, args.serve_requests)
+    if world == 1 and not args.no_denoised_serving:
+        out["denoised_serving"] = bench_denoised_serving(api, _abi)
     if world == 1 and not args.no_cpu_baseline:
         cpu, threads, sample = cpu_render_rate(s, args.cpu_seconds)
         out["cpu_baseline"] = {"value": cpu, "unit": UNIT, "cores": threads, "kind": "port",
