@@ -241,8 +241,8 @@ def bench_serving(api, _abi, n_requests, rates=(200.0, 25.0)):
     return out
 
 
-def bench_denoised_serving(api, _abi, train_scenes=48, views=8, steps=6000, eval_size=(1920, 1080),
-                           ref_spp=1024, repeats=5):
+def bench_denoised_serving(api, _abi, train_scenes=32, views=8, steps=4000, eval_size=(1920, 1080),
+                           ref_spp=1024, repeats=3):
     """The learned denoiser trained on the tracer's own pairs, then served: relMSE (eps 1e-2)
     against converged references of plain accumulation at 1-256 spp and of the denoised output at
     1 and 4 spp, each frame's serving latency (one request at a time, so the latency is the
@@ -270,7 +270,7 @@ def bench_denoised_serving(api, _abi, train_scenes=48, views=8, steps=6000, eval
     train_s = time.perf_counter() - t0
     del feats, refs, parts
     w, h = eval_size
-    plain_spp = [1, 2, 4, 8, 16, 32, 64, 128]
+    plain_spp = [1, 2, 4, 8, 16, 32, 64]
     den_spp = [1, 4]
     rows = []
     rs = []
