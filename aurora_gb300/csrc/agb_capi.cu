@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -155,6 +156,10 @@ struct agb_context
     std::vector<agb_material> hostMaterials;
     std::vector<agb_material_textures> hostMatTex;
     uint64_t sceneVersion = 0;
+    // Union of the instances' world boxes (ray binning's grid).
+    float sceneLo[3] = { 0.f, 0.f, 0.f }, sceneHi[3] = { 0.f, 0.f, 0.f };
+    bool binRays = false;
+    DevBuf bins;
 
     // Wave buffers.
     size_t pathCapacity = 0;
@@ -286,6 +291,13 @@ agb_status ensureWave(agb_context* ctx, size_t paths, int depth, size_t waves)
     }
     size_t counterWords = size_t(depth + 2) * kCounterStride * waves;
     AGB_CUDA(ctx->counters.ensure(counterWords * sizeof(uint32_t)), "allocate counters");
+    if (!ctx->bins.ptr)
+    {
+        AGB_CUDA(ctx->bins.ensure(2 * kRayBins * sizeof(uint32_t)), "allocate ray bins");
+        AGB_CUDA(cudaMemsetAsync(ctx->bins.ptr, 0, 2 * kRayBins * sizeof(uint32_t), ctx->stream), "clear ray bins");
+    }
+    ctx->wb.binCount  = ctx->bins.as<uint32_t>();
+    ctx->wb.binOffset = ctx->bins.as<uint32_t>() + kRayBins;
     AGB_CUDA(ctx->stats.ensure(8 * sizeof(unsigned long long)), "allocate stats");
     ctx->wb.stats = ctx->stats.as<unsigned long long>();
     return AGB_OK;
@@ -406,6 +418,8 @@ AGB_API agb_status agb_context_create(int32_t device, void* cuda_stream, agb_con
     AGB_CUDA(cudaEventCreate(&ctx->ev0), "create event");
     AGB_CUDA(cudaEventCreate(&ctx->ev1), "create event");
     setTraceAttributes();
+    if (const char* e = std::getenv("AGB_BIN_RAYS"))
+        ctx->binRays = e[0] == '1';
     // Default environment: the reference's gradient defaults (EnvironmentBase.cpp:33-45),
     // identity transforms.
     agb_environment_data& e = ctx->env;
@@ -450,6 +464,7 @@ AGB_API agb_status agb_view_create(agb_context* ctx, void* cuda_stream, agb_cont
     v->smCount = ctx->smCount;
     v->deviceBytes = ctx->deviceBytes;
     v->envLayout = ctx->envLayout;
+    v->binRays   = ctx->binRays;
     AGB_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     if (cuda_stream)
         v->stream = static_cast<cudaStream_t>(cuda_stream);
@@ -941,6 +956,17 @@ AGB_API agb_status agb_instances_set(agb_context* ctx, const agb_instance* inst,
             box[3 + k] += pad;
         }
     }
+    for (int k = 0; k < 3; k++)
+    {
+        float lo = INFINITY, hi = -INFINITY;
+        for (uint32_t i = 0; i < count; i++)
+        {
+            lo = std::min(lo, boxes[6 * size_t(i) + k]);
+            hi = std::max(hi, boxes[6 * size_t(i) + 3 + k]);
+        }
+        ctx->sceneLo[k] = count ? lo : 0.f;
+        ctx->sceneHi[k] = count ? hi : 0.f;
+    }
     // TLAS depth budget: the traversal stack holds the TLAS path, an instance-exit marker and the
     // deepest BLAS path.  Near the budget the builders split at the index midpoint, so any tree
     // with ceil(log2(count)) + 2 levels to spare fits; beyond that the stack cannot hold the scene.
@@ -1298,6 +1324,13 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
         wp.countTraversal = ctx->counting ? 1 : 0;
         wp.aovSample      = aovSample;
         wp.seedOffset     = opt->seed_offset;
+        wp.binRays        = ctx->binRays ? 1 : 0;
+        for (int k = 0; k < 3; k++)
+        {
+            wp.binLo[k]    = sc->sceneLo[k];
+            float ext      = sc->sceneHi[k] - sc->sceneLo[k];
+            wp.binScale[k] = ext > 0.f ? 16.f / ext : 0.f;
+        }
         wb.counters       = ctx->counters.as<uint32_t>() + counterWords * w;
         launchWave(scene, ctx->frame, wp, wb, ctx->stream, ctx->smCount, launches, marks);
         AGB_CUDA(cudaGetLastError(), "launch wave");

@@ -1323,6 +1323,117 @@ __global__ void k_finalize(agb_frame_data f, WaveParams wp, WaveBuffers wbIn, Ba
 }
 
 
+// ----------------------------------------------------------------------------- ray binning
+// Between bounces the next rays are regrouped (a counting sort into kRayBins bins) so that the
+// lanes of a traversal warp start from nearby points in similar directions and walk overlapping
+// node sets: the origin's cell of a 16^3 grid over the scene bounds (Morton order) under the
+// direction's octant.  A ray's result does not depend on its queue position, so images are
+// unchanged.
+AGB_D uint32_t rayBin(const WaveParams& wp, float4 o, float4 d)
+{
+    const float p[3] = { o.x, o.y, o.z };
+    uint32_t c[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+    {
+        float t = (p[k] - wp.binLo[k]) * wp.binScale[k];
+        int q   = t > 0.f ? int(t) : 0;
+        c[k]    = uint32_t(q < 15 ? q : 15);
+    }
+    uint32_t m = 0;
+#pragma unroll
+    for (int b = 0; b < 4; b++)
+        m |= (((c[0] >> b) & 1u) << (3 * b)) | (((c[1] >> b) & 1u) << (3 * b + 1)) |
+            (((c[2] >> b) & 1u) << (3 * b + 2));
+    uint32_t oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
+    return (oct << 12) | m;
+}
+
+__global__ void k_bin_count(WaveParams wp, WaveBuffers wb, int bounce, int src)
+{
+    const uint32_t n    = wb.counters[bounce * kCounterStride + CNT_RAYS];
+    const uint32_t step = gridDim.x * blockDim.x;
+    const int lane      = threadIdx.x & 31;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += step)
+    {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < n;
+        const unsigned act = __ballot_sync(0xffffffffu, valid);
+        if (valid)
+        {
+            uint32_t bin   = rayBin(wp, wb.rayOrg[src][i], wb.rayDir[src][i]);
+            unsigned peers = __match_any_sync(act, bin);
+            if (lane == __ffs(peers) - 1)
+                atomicAdd(wb.binCount + bin, uint32_t(__popc(peers)));
+        }
+    }
+}
+
+// Exclusive prefix sums of the bin counts into the offsets (one block of 1024 threads, 32 bins
+// each); the counts are cleared for the next use.
+__global__ void __launch_bounds__(1024) k_bin_scan(WaveBuffers wb)
+{
+    __shared__ uint32_t part[1024];
+    constexpr uint32_t per = kRayBins / 1024;
+    const uint32_t t       = threadIdx.x;
+    uint32_t local[per];
+    uint32_t sum = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < per; k++)
+    {
+        local[k] = wb.binCount[t * per + k];
+        wb.binCount[t * per + k] = 0;
+        sum += local[k];
+    }
+    part[t] = sum;
+    __syncthreads();
+    for (uint32_t off = 1; off < 1024; off <<= 1)
+    {
+        uint32_t v = t >= off ? part[t - off] : 0u;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[t] - sum;
+#pragma unroll
+    for (uint32_t k = 0; k < per; k++)
+    {
+        wb.binOffset[t * per + k] = run;
+        run += local[k];
+    }
+}
+
+// Moves the rays of queue src into queue src ^ 1 in bin order.
+__global__ void k_bin_scatter(WaveParams wp, WaveBuffers wb, int bounce, int src)
+{
+    const uint32_t n    = wb.counters[bounce * kCounterStride + CNT_RAYS];
+    const uint32_t step = gridDim.x * blockDim.x;
+    const int lane      = threadIdx.x & 31;
+    const int dst       = src ^ 1;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += step)
+    {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < n;
+        const unsigned act = __ballot_sync(0xffffffffu, valid);
+        if (valid)
+        {
+            float4 o       = wb.rayOrg[src][i];
+            float4 d       = wb.rayDir[src][i];
+            uint32_t path  = wb.rayPath[src][i];
+            uint32_t bin   = rayBin(wp, o, d);
+            unsigned peers = __match_any_sync(act, bin);
+            int leader     = __ffs(peers) - 1;
+            uint32_t pos   = 0;
+            if (lane == leader)
+                pos = atomicAdd(wb.binOffset + bin, uint32_t(__popc(peers)));
+            pos = __shfl_sync(peers, pos, leader) + uint32_t(__popc(peers & ((1u << lane) - 1u)));
+            wb.rayOrg[dst][pos]  = o;
+            wb.rayDir[dst][pos]  = d;
+            wb.rayPath[dst][pos] = path;
+        }
+    }
+}
+
 // ------------------------------------------------------------------------------ launchers
 // One wave: `depth` bounces (the frame's trace depth; a batched wave's deepest request), the
 // ground plane's kernels when the scene has one (single-request waves only), transparent or
@@ -1397,7 +1508,18 @@ void launchWaveT(const DevScene& s, const agb_frame_data& f, const WaveParams& w
         mark(KC_RESOLVE);
         k_resolve<kBatch><<<grid, 256, 0, st>>>(f, wb, b, bt);
         launches += 6;
-        cur ^= 1;
+        if (!kBatch && wp.binRays && b + 1 < depth)
+        {
+            // The next bounce's rays, binned from queue cur ^ 1 back into queue cur (free since
+            // this bounce's shading).
+            mark(KC_RESOLVE);
+            k_bin_count<<<grid, 256, 0, st>>>(wp, wb, b + 1, cur ^ 1);
+            k_bin_scan<<<1, 1024, 0, st>>>(wb);
+            k_bin_scatter<<<grid, 256, 0, st>>>(wp, wb, b + 1, cur ^ 1);
+            launches += 3;
+        }
+        else
+            cur ^= 1;
     }
     mark(KC_FINALIZE);
     k_finalize<kBatch><<<grid, 256, 0, st>>>(f, wp, wb, bt);

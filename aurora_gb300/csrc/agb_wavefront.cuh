@@ -87,6 +87,8 @@ struct WaveBuffers
     float4* shadePoint;     // kShadePointWords float4 per shading point, word-major
     float4* misPoint;       // kMisWords float4 per shading point: the environment-MIS sample
     uint32_t* counters;     // per bounce: kCounterStride words (CNT_*)
+    uint32_t* binCount;     // kRayBins counts (zero between uses) and their running offsets
+    uint32_t* binOffset;
     // Accumulation targets (per pixel).
     float4* accumMean;
     float4* accumSum;
@@ -110,7 +112,15 @@ struct WaveParams
     int32_t countTraversal;
     uint32_t aovSample;           // sample index whose primary paths write the AOVs; ~0u = none
     uint32_t seedOffset;          // added to the sample index that seeds the random streams
+    // Ray binning between bounces (binRays != 0): the next bounce's rays are regrouped by their
+    // origin's cell in a 16^3 grid over the scene bounds and their direction octant.
+    int32_t binRays;
+    float binLo[3];
+    float binScale[3];            // cells per unit along each axis
 };
+
+constexpr int kRayBinBits = 15;   // 3 bits of octant above a 12-bit Morton cell index
+constexpr uint32_t kRayBins = 1u << kRayBinBits;
 
 // Batched wavefronts (agb_batch_render): one wave over the paths of several requests, of
 // different scenes and resolutions.  Request r owns paths [pathOffset, pathOffset + pixels x
