@@ -19,14 +19,15 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["agb_pt.cu", "agb_env_build.cu", "agb_env_noalloc.cu", "agb_temporal.cu", "agb_denoise.cu",
            "agb_unet.cu", "agb_unit.cu",
-           "agb_capi.cu", "agb_serve.cpp", "agb_aurora.cpp", "agb_obj.cpp", "agb_gltf.cpp", "agb_mtlx.cpp", "agb_image_io.cpp", "agb_bvh_build.cpp",
+           "agb_capi.cu", "agb_serve.cpp", "agb_aurora.cpp", "agb_aurora_api.cpp", "agb_obj.cpp", "agb_gltf.cpp", "agb_mtlx.cpp", "agb_image_io.cpp", "agb_bvh_build.cpp",
            "agb_bvh_gpu.cu"]
 CLI_SRC = os.path.join(HERE, "cli", "agb_render.cpp")
 CLI = os.path.join(BUILD, "agb_render")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true",
               "-prec-sqrt=true", "-Xcompiler",
-              "-fPIC,-O2,-ffp-contract=off,-fvisibility=hidden", "-I" + INCLUDE, "-I" + CSRC]
+              "-fPIC,-O2,-ffp-contract=off,-fvisibility=hidden", "-I" + INCLUDE,
+              "-I" + os.path.join(INCLUDE, "glm_shim"), "-I" + CSRC]
 
 
 def nvcc():
@@ -36,7 +37,8 @@ def nvcc():
 
 def _headers():
     out = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
-    out += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith((".h", ".hpp"))]
+    for d, _, files in os.walk(INCLUDE):
+        out += [os.path.join(d, f) for f in files if f.endswith((".h", ".hpp"))]
     return out
 
 

@@ -41,6 +41,19 @@ void check(agb_status st, const std::string& what)
         throw Error(what + ": " + agb_last_error());
 }
 
+// Sets `src`'s values in `dst`; an undefined value (std::monostate) removes the property, so its
+// default applies again.
+void merge(Properties& dst, const Properties& src)
+{
+    for (auto& kv : src)
+    {
+        if (std::holds_alternative<std::monostate>(kv.second))
+            dst.erase(kv.first);
+        else
+            dst[kv.first] = kv.second;
+    }
+}
+
 template <class T>
 const T* find(const Properties& p, const std::string& name)
 {
@@ -322,6 +335,8 @@ agb_material defaultMaterial()
 class Scene : public IScene
 {
 public:
+    explicit Scene(std::shared_ptr<LoadResourceFunction> l) : loader(std::move(l)) {}
+    std::shared_ptr<LoadResourceFunction> loader; // the renderer's; an empty function reads files
     struct Geometry
     {
         GeometryDescriptor desc;
@@ -387,14 +402,33 @@ public:
         auto store             = std::make_shared<FileImage>();
         ImageDescriptor d;
         d.linearize = linearize;
-        d.getData   = [file, store](ImageData& out) {
-            const bool hdr = file.size() >= 4 && (file.compare(file.size() - 4, 4, ".hdr") == 0 ||
-                                                     file.compare(file.size() - 4, 4, ".HDR") == 0);
+        auto isHDR  = [](const std::string& f) {
+            return f.size() >= 4 && (f.compare(f.size() - 4, 4, ".hdr") == 0 || f.compare(f.size() - 4, 4, ".HDR") == 0);
+        };
+        d.getData = [file, store, isHDR, loader = loader](ImageData& out) {
+            bool hdr = isHDR(file);
             if (store->rgba8.empty() && store->rgb32.empty())
             {
                 std::string err;
-                bool ok = hdr ? loadHDRFile(file, store->rgb32, store->w, store->h, err)
-                              : loadPNGFile(file, store->rgba8, store->w, store->h, err);
+                bool ok;
+                if (*loader)
+                {
+                    std::vector<unsigned char> bytes;
+                    std::string name = file;
+                    ok = (*loader)(file, &bytes, &name);
+                    if (!ok)
+                        err = "the resource loader failed";
+                    else
+                    {
+                        hdr = isHDR(name);
+                        std::string data(bytes.begin(), bytes.end());
+                        ok  = hdr ? decodeHDR(data, store->rgb32, store->w, store->h, err)
+                                  : decodePNG(data, store->rgba8, store->w, store->h, err);
+                    }
+                }
+                else
+                    ok = hdr ? loadHDRFile(file, store->rgb32, store->w, store->h, err)
+                             : loadPNGFile(file, store->rgba8, store->w, store->h, err);
                 if (!ok)
                 {
                     logError("image " + file + ": " + err);
@@ -402,7 +436,7 @@ public:
                 }
             }
             out.dimensions = { store->w, store->h };
-            if (hdr)
+            if (!store->rgb32.empty())
             {
                 out.pPixelBuffer = store->rgb32.data();
                 out.bytesPerRow  = size_t(store->w) * 12;
@@ -452,8 +486,7 @@ public:
                     setImageFromFilePath(im.image, im.file, im.linearize, false);
                     lin.insert(im.property);
                 }
-                for (auto& kv : fromDoc)
-                    m[kv.first] = kv.second;
+                merge(m, fromDoc);
             }
         }
         else if (type != Names::MaterialTypes::kBuiltIn)
@@ -463,16 +496,12 @@ public:
     }
     void setSamplerProperties(const Path& p, const Properties& props) override
     {
-        Properties& m = samplers[p];
-        for (auto& kv : props)
-            m[kv.first] = kv.second;
+        merge(samplers[p], props);
         dirty = true;
     }
     void setMaterialProperties(const Path& p, const Properties& props) override
     {
-        Properties& m = materials[p];
-        for (auto& kv : props)
-            m[kv.first] = kv.second;
+        merge(materials[p], props);
         dirty = true;
     }
     bool addInstance(const Path& p, const Path& geometry, const Properties& props) override
@@ -492,8 +521,7 @@ public:
         for (auto& kv : instances)
             if (kv.first == p)
             {
-                for (auto& q : props)
-                    kv.second.props[q.first] = q.second;
+                merge(kv.second.props, props);
                 dirty = true;
                 return;
             }
@@ -508,9 +536,7 @@ public:
     }
     bool setEnvironmentProperties(const Path& p, const Properties& props) override
     {
-        Properties& e = environments[p];
-        for (auto& kv : props)
-            e[kv.first] = kv.second;
+        merge(environments[p], props);
         dirty = true;
         return true;
     }
@@ -800,7 +826,8 @@ public:
         if (!im.desc.getData(data) || !data.pPixelBuffer)
             throw Error("image " + path + ": getData failed");
         const uint32_t w = uint32_t(data.dimensions[0]), h = uint32_t(data.dimensions[1]);
-        if (data.format == ImageFormat::Integer_RGBA && im.desc.linearize)
+        const bool linearize = data.overrideLinearize ? data.linearize : im.desc.linearize;
+        if (data.format == ImageFormat::Integer_RGBA && linearize)
         {
             std::vector<float> px(size_t(w) * h * 4);
             size_t row = data.bytesPerRow ? data.bytesPerRow : size_t(w) * 4;
@@ -1040,7 +1067,9 @@ public:
         if (ctx)
             agb_context_destroy(ctx);
     }
-    IScenePtr createScene() override { return std::make_shared<Scene>(); }
+    std::shared_ptr<LoadResourceFunction> loader = std::make_shared<LoadResourceFunction>();
+    IScenePtr createScene() override { return std::make_shared<Scene>(loader); }
+    void setLoadResourceFunction(LoadResourceFunction func) override { *loader = std::move(func); }
     IGroundPlanePtr createGroundPlanePointer() override { return std::make_shared<GroundPlane>(); }
     void setScene(const IScenePtr& s) override
     {
@@ -1057,8 +1086,7 @@ public:
     void setTargets(const TargetAssignments& t) override { targets = t; }
     void setOptions(const Properties& o) override
     {
-        for (auto& kv : o)
-            opts.props[kv.first] = kv.second;
+        merge(opts.props, o);
     }
     IValues& options() override { return opts; }
     void setCamera(const mat4& v, const mat4& p, float fd, float lr) override

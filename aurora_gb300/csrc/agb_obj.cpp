@@ -570,6 +570,11 @@ bool loadHDRFile(const std::string& path, std::vector<float>& rgb, int& width, i
         error = "cannot read " + path;
         return false;
     }
+    return decodeHDR(data, rgb, width, height, error);
+}
+
+bool decodeHDR(const std::string& data, std::vector<float>& rgb, int& width, int& height, std::string& error)
+{
     size_t pos = 0;
     auto nextLine = [&](std::string& l) {
         size_t e = data.find('\n', pos);

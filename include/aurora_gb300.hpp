@@ -48,8 +48,10 @@ struct Error : std::runtime_error
 // Receives recoverable errors (Aurora's AU_ERROR); null restores the stderr default.
 AGB_CPP_API void setLogCallback(std::function<void(const std::string&)> cb);
 
-// A property value (Aurora.h:125-300, reduced to the kinds this path uses).
-using PropertyValue = std::variant<bool, int, float, vec2, vec3, mat4, std::string, Strings>;
+// A property value (Aurora.h:125-300, reduced to the kinds this path uses).  std::monostate is
+// Aurora's undefined value: set through a property map it returns the property to its default
+// (ResourceStub.cpp:278-292, RendererBase.cpp:166-168).
+using PropertyValue = std::variant<bool, int, float, vec2, vec3, mat4, std::string, Strings, std::monostate>;
 using Properties    = std::map<std::string, PropertyValue>;
 
 // Property names (AuroraNames.cpp).
@@ -168,6 +170,8 @@ struct ImageData
     size_t bufferSize         = 0;
     std::array<int, 2> dimensions = { 0, 0 };
     ImageFormat format        = ImageFormat::Integer_RGBA;
+    bool overrideLinearize    = false; // use `linearize` below instead of the descriptor's
+    bool linearize            = true;
 };
 struct ImageDescriptor
 {
@@ -276,6 +280,12 @@ enum class AOV
 };
 using TargetAssignments = std::map<AOV, IRenderBufferPtr>;
 
+// Loads the bytes of a resource named by a URI (Aurora.h:54-63): the image files of
+// setImageFromFilePath and of MaterialX documents.  pFileNameOut receives a file name whose
+// extension selects the decoder (".hdr": Radiance RGBE; otherwise PNG).
+using LoadResourceFunction =
+    std::function<bool(const std::string& uri, std::vector<unsigned char>* pBufferOut, std::string* pFileNameOut)>;
+
 // The renderer (Aurora.h:1098-1222).
 class IRenderer
 {
@@ -299,6 +309,10 @@ public:
     // Built-in material types beyond the default Standard Surface: none, as in the HGI
     // backend (HGIRenderer.cpp:622-627).
     virtual const std::vector<std::string>& builtInMaterials()                       = 0;
+    // The loader for image files named by path (Aurora.h:1206-1208); without one (or after an
+    // empty function) files are read from the file system.  Scenes created before the call use it
+    // too.
+    virtual void setLoadResourceFunction(LoadResourceFunction func)                  = 0;
     virtual ~IRenderer() = default;
 };
 using IRendererPtr = std::shared_ptr<IRenderer>;

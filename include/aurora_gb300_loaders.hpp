@@ -178,6 +178,8 @@ AGB_CPP_API bool loadPNGFile(const std::string& path, std::vector<uint8_t>& rgba
 // Radiance RGBE (.hdr) image, flat or run-length encoded scanlines, to RGB floats top row first.
 AGB_CPP_API bool loadHDRFile(const std::string& path, std::vector<float>& rgb, int& width, int& height,
     std::string& error);
+AGB_CPP_API bool decodeHDR(const std::string& data, std::vector<float>& rgb, int& width, int& height,
+    std::string& error);
 // 8-bit RGBA PNG (stored deflate blocks) and little-endian PFM (RGB float, bottom row first).
 AGB_CPP_API bool savePNG(const std::string& path, const uint8_t* rgba, int width, int height, size_t stride);
 AGB_CPP_API bool savePFM(const std::string& path, const float* rgba, int width, int height, size_t stride);

@@ -70,6 +70,8 @@ void printValue(const PropertyValue& v)
     }
     else if (std::holds_alternative<mat4>(v))
         printFloats(std::get<mat4>(v).data(), 16);
+    else if (std::holds_alternative<std::monostate>(v))
+        std::printf("null");
     else
         printString(std::get<std::string>(v));
 }

@@ -14,6 +14,10 @@ tree exists; the fixtures travel, the reference does not).
                         evaluateMaterial / sampleMaterial / evaluateMaterialAndPDF on 4096 seeded
                         cases (inputs stored) with the per-case tolerances of tests/bsdf_cases.py,
                         sampleEnvironment on a seeded 64x32 environment, and random2D streams.
+  aurora_interface.txt  the binary interface of the reference's public header
+                        Libraries/Aurora/API/Aurora/Aurora.h (tests/cpp/aurora_abi_probe.cpp's
+                        vtable slots, value-type layouts and enumerator values, compiled against
+                        it) and the Names values of Libraries/Aurora/Source/AuroraNames.cpp.
 """
 import ctypes
 import json
@@ -143,4 +147,6 @@ if __name__ == "__main__":
     json.dump(frame_layout(), open(os.path.join(HERE, "frame_layout.json"), "w"), indent=1)
     np.savez_compressed(os.path.join(HERE, "alias_ref.npz"), **alias_tables())
     np.savez_compressed(os.path.join(HERE, "shaders_ref.npz"), **shader_references())
+    import aurora_interface
+    aurora_interface.write_fixture(REF)
     print("golden fixtures written")
