@@ -239,6 +239,7 @@ SIGNATURES = {
     "agb_temporal_jitter": (None, [_U32, _U32, ctypes.POINTER(ctypes.c_float)]),
     "agb_tc_gemm_bf16": (_I32, [_P, _P, _P, _I32, _I32, _I32, _P]),
     "agb_conv3x3_bf16": (_I32, [_P, _P, _P, _P, _P, _P] + [_I32] * 8 + [_P]),
+    "agb_conv3x3_pool_bf16": (_I32, [_P, _P, _P, _P, _P, _P] + [_I32] * 8 + [_P]),
     "agb_pack_conv_weights": (_I32, [_P, _I32, _I32, _I32, _P, _P]),
     "agb_conv3x3_wgrad_bf16": (_I32, [_P, _P, _P, _P] + [_I32] * 7 + [_P]),
     "agb_denoiser_create": (_I32, [_I32, _P, _U64, ctypes.POINTER(_P)]),

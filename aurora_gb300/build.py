@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libagb_cuda.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["agb_pt.cu", "agb_env_build.cu", "agb_env_noalloc.cu", "agb_temporal.cu", "agb_denoise.cu",
+SOURCES = ["agb_pt.cu", "agb_env_build.cu", "agb_env_noalloc.cu", "agb_temporal.cu", "agb_denoise.cu", "agb_conv.cu",
            "agb_unet.cu", "agb_unit.cu",
            "agb_capi.cu", "agb_serve.cpp", "agb_aurora.cpp", "agb_aurora_api.cpp", "agb_obj.cpp", "agb_gltf.cpp", "agb_mtlx.cpp", "agb_image_io.cpp", "agb_bvh_build.cpp",
            "agb_bvh_gpu.cu"]

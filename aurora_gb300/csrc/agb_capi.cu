@@ -2153,33 +2153,54 @@ AGB_API agb_status agb_tc_gemm_bf16(const uint16_t* a, const uint16_t* b, float*
     return AGB_OK;
 }
 
+static agb_status convCommon(const char* what, const uint16_t* in0, const uint16_t* in1, const uint16_t* wpack,
+    const float* bias, uint16_t* out, float* out32, uint16_t* pool, int32_t batch, int32_t height, int32_t width,
+    int32_t c0, int32_t c1, int32_t cout, int32_t up0, int32_t relu, void* cuda_stream)
+{
+    if (!in0 || !wpack || (c1 > 0 && !in1) || batch <= 0 || height <= 0 || width <= 0)
+        return fail(AGB_ERR_INVALID_ARG, std::string(what) + ": null input or empty image");
+    if (c0 < 16 || c0 % 16 || c1 < 0 || c1 % 16 || cout < 16 || cout % 16 || cout > 1024 || c0 + c1 > 1024)
+        return fail(AGB_ERR_INVALID_ARG, std::string(what) + ": channel counts must be multiples of 16 up to 1024");
+    if (width % 2)
+        return fail(AGB_ERR_INVALID_ARG, std::string(what) + ": the width must be even");
+    if ((up0 || pool) && height % 2)
+        return fail(AGB_ERR_INVALID_ARG, std::string(what) + ": an upsampled input or a pooled output needs even sizes");
+    if (int64_t(batch) * height * width >= (int64_t(1) << 31) / 128)
+        return fail(AGB_ERR_LIMIT, std::string(what) + ": too many pixels");
+    uintptr_t al = reinterpret_cast<uintptr_t>(in0) | reinterpret_cast<uintptr_t>(in1) |
+        reinterpret_cast<uintptr_t>(wpack) | reinterpret_cast<uintptr_t>(out) | reinterpret_cast<uintptr_t>(out32) |
+        reinterpret_cast<uintptr_t>(pool);
+    if (al & 15u)
+        return fail(AGB_ERR_INVALID_ARG, std::string(what) + ": pointers must be 16-byte aligned");
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    ConvLaunch c{ in0, c1 > 0 ? in1 : nullptr, wpack, bias, out, out32, batch, height, width, c0, c1, cout,
+        up0 ? 1 : 0, relu ? 1 : 0 };
+    c.pool = pool;
+    AGB_CUDA(launchConv3x3(c, st), what);
+    AGB_CUDA(cudaStreamSynchronize(st), what);
+    int flag = 0;
+    AGB_CUDA(takeTcError(&flag), what);
+    if (flag)
+        return fail(AGB_ERR_TIMEOUT, std::string(what) + ": tensor-core completion wait timed out");
+    return AGB_OK;
+}
+
 AGB_API agb_status agb_conv3x3_bf16(const uint16_t* in0, const uint16_t* in1, const uint16_t* wpack,
     const float* bias, uint16_t* out, float* out32, int32_t batch, int32_t height, int32_t width,
     int32_t c0, int32_t c1, int32_t cout, int32_t up0, int32_t relu, void* cuda_stream)
 {
-    if (!in0 || !wpack || (c1 > 0 && !in1) || batch <= 0 || height <= 0 || width <= 0)
-        return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_bf16: null input or empty image");
-    if (c0 < 16 || c0 % 16 || c1 < 0 || c1 % 16 || cout < 16 || cout % 16 || (cout > 256 && cout % 128) || cout > 1024)
-        return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_bf16: channel counts must be multiples of 16 (cout <= 256 "
-                                         "or a multiple of 128 up to 1024)");
-    if (up0 && (height % 2 || width % 2))
-        return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_bf16: upsampled input needs even sizes");
-    if (int64_t(batch) * height * width >= (int64_t(1) << 31) / 128)
-        return fail(AGB_ERR_LIMIT, "agb_conv3x3_bf16: too many pixels");
-    uintptr_t al = reinterpret_cast<uintptr_t>(in0) | reinterpret_cast<uintptr_t>(in1) |
-        reinterpret_cast<uintptr_t>(wpack) | reinterpret_cast<uintptr_t>(out) | reinterpret_cast<uintptr_t>(out32);
-    if (al & 15u)
-        return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_bf16: pointers must be 16-byte aligned");
-    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
-    ConvLaunch c{ in0, c1 > 0 ? in1 : nullptr, wpack, bias, out, out32, batch, height, width, c0, c1, cout,
-        up0 ? 1 : 0, relu ? 1 : 0 };
-    AGB_CUDA(launchConv3x3(c, st), "agb_conv3x3_bf16");
-    AGB_CUDA(cudaStreamSynchronize(st), "agb_conv3x3_bf16");
-    int flag = 0;
-    AGB_CUDA(takeTcError(&flag), "agb_conv3x3_bf16");
-    if (flag)
-        return fail(AGB_ERR_TIMEOUT, "agb_conv3x3_bf16: tensor-core completion wait timed out");
-    return AGB_OK;
+    return convCommon("agb_conv3x3_bf16", in0, in1, wpack, bias, out, out32, nullptr, batch, height, width, c0, c1,
+        cout, up0, relu, cuda_stream);
+}
+
+AGB_API agb_status agb_conv3x3_pool_bf16(const uint16_t* in0, const uint16_t* in1, const uint16_t* wpack,
+    const float* bias, uint16_t* out, uint16_t* pool, int32_t batch, int32_t height, int32_t width,
+    int32_t c0, int32_t c1, int32_t cout, int32_t up0, int32_t relu, void* cuda_stream)
+{
+    if (!pool)
+        return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_pool_bf16: null pool output");
+    return convCommon("agb_conv3x3_pool_bf16", in0, in1, wpack, bias, out, nullptr, pool, batch, height, width, c0,
+        c1, cout, up0, relu, cuda_stream);
 }
 
 AGB_API agb_status agb_conv3x3_wgrad_bf16(const uint16_t* in0, const uint16_t* in1, const uint16_t* dy,

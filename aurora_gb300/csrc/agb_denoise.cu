@@ -123,220 +123,6 @@ __global__ void __launch_bounds__(128) k_tc_gemm(const uint16_t* A, const uint16
         atomicExch(&g_tcError, 1);
 }
 
-// ------------------------------------------------------------------ 3x3 convolution
-// Implicit GEMM over row tiles.  A CTA computes 128 consecutive output pixels of one image row
-// (the MMA rows; pixels past the row end are masked) for nTile output channels (MMA columns).
-// K = 9 taps x Cin input channels.  Activations are NHWC BF16 over a batch of images; the input is
-// the concatenation of in0 (optionally read through a nearest 2x upsample from half resolution)
-// and in1 (Cin and both channel counts are multiples of 16).  Zero padding at the image border.
-//
-// For each input row dy in {-1, 0, 1} and 16-channel group g, the threads stage the 130 input
-// pixels x0-1 .. x0+128 of that row once (a "halo row": channels 0-7 of pixel r at r*16,
-// channels 8-15 at kHaloK + r*16); the three horizontal taps are three MMAs over the same staged
-// pixels, their A descriptors offset by one 16-byte pixel (leading byte offset kHaloK between the
-// K halves, stride byte offset 128 between 8-pixel groups).  Each input pixel is loaded three
-// times per channel group instead of nine.  Weights arrive pre-packed in the B-operand layout in
-// (dy, g, dx) slice order, so a stage's weights are one contiguous 1D bulk (TMA) copy.  Epilogue:
-// + bias, optional ReLU, BF16 round-to-nearest-even store (and an optional FP32 copy).
-
-struct ConvArgs
-{
-    const uint16_t* in0;   // [B][H0][W0][C0]; H0 = H / 2 when up0
-    const uint16_t* in1;   // [B][H][W][C1] or null
-    const uint16_t* wpack; // 9 * (C0 + C1) / 16 slices of Cout x 16
-    const float* bias;     // [Cout] or null
-    uint16_t* out;         // [B][H][W][Cout] or null
-    float* out32;          // [B][H][W][Cout] or null
-    int B, H, W, C0, C1, Cout, up0, relu;
-    int nTile;             // output channels per CTA (grid.y = Cout / nTile)
-    int stageRows;         // halo rows per pipeline stage
-};
-
-constexpr int kHaloRows       = 130;
-constexpr uint32_t kHaloK     = kHaloRows * 16; // one K half of a halo row
-constexpr uint32_t kHaloBytes = 2 * kHaloK;
-
-// Output channels per CTA for a layer with Cout channels: all of them up to the 256 accumulator
-// columns of one MMA tile, else tiles of 128.
-__host__ __device__ inline int convTile(int cout) { return cout <= 256 ? cout : 128; }
-// Halo rows per pipeline stage: two (six MMAs) unless the weights of a stage would crowd out a
-// second resident CTA.
-__host__ __device__ inline int convStageRows(int nTile) { return nTile >= 256 ? 1 : 2; }
-__host__ __device__ inline size_t convSmemBytes(int nTile)
-{
-    int rows = convStageRows(nTile);
-    return 2 * (size_t(rows) * kHaloBytes + size_t(rows) * 3 * nTile * 32);
-}
-
-// Halo row (dy, channels c .. c+15) of the tile starting at pixel x0 of row y of image b: pixel r
-// is x0 - 1 + r.  Thread t stages pixel t, threads 0 and 1 also pixels 128 and 129.
-__device__ __forceinline__ void stageHaloRow(const ConvArgs& a, int b, int y, int x0, int dy, int c,
-    uint8_t* halo, int tid)
-{
-    const int yy = y + dy;
-    for (int r = tid; r < kHaloRows; r += 128)
-    {
-        uint4 v0 = make_uint4(0, 0, 0, 0), v1 = v0;
-        const int xx = x0 - 1 + r;
-        if (yy >= 0 && yy < a.H && xx >= 0 && xx < a.W)
-        {
-            const uint16_t* src;
-            if (c < a.C0)
-            {
-                int h0 = a.up0 ? a.H >> 1 : a.H, w0 = a.up0 ? a.W >> 1 : a.W;
-                int y0 = a.up0 ? yy >> 1 : yy, xs = a.up0 ? xx >> 1 : xx;
-                src = a.in0 + ((size_t(b) * h0 + y0) * w0 + xs) * a.C0 + c;
-            }
-            else
-                src = a.in1 + ((size_t(b) * a.H + yy) * a.W + xx) * a.C1 + (c - a.C0);
-            v0 = __ldg(reinterpret_cast<const uint4*>(src));
-            v1 = __ldg(reinterpret_cast<const uint4*>(src) + 1);
-        }
-        *reinterpret_cast<uint4*>(halo + r * 16)          = v0;
-        *reinterpret_cast<uint4*>(halo + kHaloK + r * 16) = v1;
-    }
-}
-
-__global__ void __launch_bounds__(128) k_conv3x3(ConvArgs a)
-{
-    extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ uint64_t mmaBar[2], tmaBar[2];
-    __shared__ uint32_t tmemBase;
-    const int tid  = threadIdx.x;
-    const int warp = tid >> 5;
-    const int Cin  = a.C0 + a.C1;
-    const int G    = Cin / 16;
-    const int N    = a.nTile;
-    const int R    = a.stageRows;
-    const int cb   = int(blockIdx.y) * N;
-    const uint32_t bSlice = uint32_t(N) * 32;
-    const uint32_t aStage = uint32_t(R) * kHaloBytes;
-    const uint32_t bStage = uint32_t(R) * 3 * bSlice;
-    uint8_t* aS[2] = { smem, smem + aStage + bStage };
-    uint8_t* bS[2] = { smem + aStage, smem + 2 * aStage + bStage };
-    // This CTA's row tile.
-    const int tilesPerRow = (a.W + 127) / 128;
-    const int xt = int(blockIdx.x % unsigned(tilesPerRow));
-    const int by = int(blockIdx.x / unsigned(tilesPerRow));
-    const int y  = by % a.H;
-    const int b  = by / a.H;
-    const int x0 = xt * 128;
-    const uint32_t cols = tc::tmemCols(uint32_t(N));
-    if (warp == 0)
-        tc::tmemAlloc(&tmemBase, cols);
-    if (tid == 0)
-    {
-        for (int s = 0; s < 2; s++)
-        {
-            tc::mbarInit(&mmaBar[s], 1);
-            tc::mbarInit(&tmaBar[s], 1);
-        }
-        tc::fenceMbarInit();
-    }
-    tc::fenceBeforeSync();
-    __syncthreads();
-    tc::fenceAfterSync();
-    const uint32_t tmem  = tmemBase;
-    const uint32_t idesc = tc::idescBf16(128, uint32_t(N));
-    const int pairs      = 3 * G; // (dy, g) halo rows, dy-major
-    const int chunks     = (pairs + R - 1) / R;
-    uint32_t mmaParity[2] = { 0, 0 }, tmaParity[2] = { 0, 0 };
-    bool ok  = true;
-    int gDy  = 0, gG = 0; // halo row the next staging fills
-    for (int c = 0; c < chunks; c++)
-    {
-        const int s  = c & 1;
-        const int q0 = c * R;
-        const int nq = min(R, pairs - q0);
-        if (c >= 2)
-        {
-            ok = tc::mbarWait(&mmaBar[s], mmaParity[s]) && ok;
-            mmaParity[s] ^= 1u;
-        }
-        if (tid == 0)
-        {
-            tc::mbarExpectTx(&tmaBar[s], uint32_t(nq) * 3 * bSlice);
-            tc::bulkLoad(bS[s], a.wpack + (size_t(blockIdx.y) * (9 * G) + size_t(q0) * 3) * (bSlice / 2),
-                uint32_t(nq) * 3 * bSlice, &tmaBar[s]);
-        }
-        for (int j = 0; j < nq; j++)
-        {
-            stageHaloRow(a, b, y, x0, gDy - 1, gG * 16, aS[s] + j * kHaloBytes, tid);
-            if (++gG == G)
-            {
-                gG = 0;
-                gDy++;
-            }
-        }
-        tc::fenceProxyAsync();
-        __syncthreads();
-        if (tid == 0)
-        {
-            ok = tc::mbarWait(&tmaBar[s], tmaParity[s]) && ok;
-            tc::fenceAfterSync();
-            for (int j = 0; j < nq; j++)
-                for (int dx = 0; dx < 3; dx++)
-                {
-                    uint64_t ad = tc::smemDesc(tc::smemAddr(aS[s] + j * kHaloBytes + dx * 16), kHaloK, 128);
-                    uint64_t bd = tc::smemDesc(tc::smemAddr(bS[s] + (j * 3 + dx) * bSlice), tc::kSliceLbo,
-                        tc::kSliceSbo);
-                    tc::mma(tmem, ad, bd, idesc, (c > 0 || j > 0 || dx > 0) ? 1u : 0u);
-                }
-            tc::commit(&mmaBar[s]);
-        }
-        tmaParity[s] ^= 1u;
-        __syncwarp();
-    }
-    {
-        const int sl = (chunks - 1) & 1;
-        ok           = tc::mbarWait(&mmaBar[sl], mmaParity[sl]) && ok;
-    }
-    tc::fenceAfterSync();
-    const int x = x0 + warp * 32 + (tid & 31);
-    const size_t row = (size_t(b) * a.H + y) * a.W + x;
-    for (int c0 = 0; c0 < N; c0 += 16)
-    {
-        uint32_t r[16];
-        tc::tmemLoad16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), r);
-        tc::tmemWaitLoad();
-        if (x < a.W)
-        {
-            float v[16];
-#pragma unroll
-            for (int j = 0; j < 16; j++)
-            {
-                v[j] = __uint_as_float(r[j]) + (a.bias ? __ldg(a.bias + cb + c0 + j) : 0.f);
-                if (a.relu)
-                    v[j] = fmaxf(v[j], 0.f);
-            }
-            if (a.out)
-            {
-                uint32_t w[8];
-#pragma unroll
-                for (int j = 0; j < 8; j++)
-                    w[j] = uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(v[2 * j]))) |
-                        (uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(v[2 * j + 1]))) << 16);
-                uint4* o = reinterpret_cast<uint4*>(a.out + row * a.Cout + cb + c0);
-                o[0]     = make_uint4(w[0], w[1], w[2], w[3]);
-                o[1]     = make_uint4(w[4], w[5], w[6], w[7]);
-            }
-            if (a.out32)
-            {
-                float4* o = reinterpret_cast<float4*>(a.out32 + row * a.Cout + cb + c0);
-#pragma unroll
-                for (int j = 0; j < 4; j++)
-                    o[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
-            }
-        }
-    }
-    tc::fenceBeforeSync();
-    __syncthreads();
-    if (warp == 0)
-        tc::tmemDealloc(tmem, cols);
-    if (!ok && tid == 0)
-        atomicExch(&g_tcError, 1);
-}
-
 // ------------------------------------------------------------------ weight gradient
 // dW[tap][ci][co] += sum over pixels p of X[p + d(tap)][ci] * dY[p][co], X = concat(up(in0), in1) as
 // in the forward pass.  GEMM with rows = input channels (128 per CTA, grid.z blocks), columns =
@@ -502,45 +288,7 @@ __global__ void __launch_bounds__(128) k_conv_wgrad(WgradArgs a)
         atomicExch(&g_tcError, 1);
 }
 
-// Packs FP32 weights w[tap][ci][co] (9 x Cin x Cout) into the conv kernel's B layout (BF16).
-// flip: pack the data-gradient weights instead, w'[tap'][co][ci] = w[8 - tap'][ci][co], so that
-// k_conv3x3 over dY computes dX (the kernel's Cin is then the layer's Cout and vice versa).
-__global__ void k_pack_conv_weights(const float* w, int Cin, int Cout, int flip, uint16_t* out)
-{
-    // Packed as the kernel sees it: kCin x kCout with kCin = flip ? Cout : Cin.
-    int kCin = flip ? Cout : Cin, kCout = flip ? Cin : Cout;
-    long total = 9L * kCin * kCout;
-    for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < total; i += long(gridDim.x) * blockDim.x)
-    {
-        int n   = int(i % kCout);     // kernel output channel
-        long kk = i / kCout;          // kernel K index = tap * kCin + c
-        int tap = int(kk / kCin), c = int(kk % kCin);
-        float v = flip ? w[(size_t(8 - tap) * Cin + n) * Cout + c] : w[(size_t(tap) * Cin + c) * Cout + n];
-        // Slice order (dy, channel group, dx), the order k_conv3x3 consumes them.
-        int G = kCin / 16, kin = c % 16;
-        int slice = ((tap / 3) * G + c / 16) * 3 + tap % 3;
-        int nt = convTile(kCout), tile = n / nt, nn = n % nt;
-        size_t slices = size_t(9) * kCin / 16;
-        size_t off = (size_t(tile) * slices + slice) * nt * 16 + tc::sliceOffset(uint32_t(nn), uint32_t(kin)) / 2;
-        out[off]   = __bfloat16_as_ushort(__float2bfloat16_rn(v));
-    }
-}
-
 } // namespace
-
-cudaError_t launchConv3x3(const ConvLaunch& c, cudaStream_t st)
-{
-    int nt = convTile(c.Cout);
-    ConvArgs a{ c.in0, c.in1, c.wpack, c.bias, c.out, c.out32, c.B, c.H, c.W, c.C0, c.C1, c.Cout, c.up0, c.relu, nt,
-        convStageRows(nt) };
-    size_t smem = convSmemBytes(nt);
-    cudaError_t e = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (e != cudaSuccess)
-        return e;
-    long tiles = long(c.B) * c.H * ((c.W + 127) / 128);
-    k_conv3x3<<<dim3(unsigned(tiles), unsigned(c.Cout / nt)), 128, smem, st>>>(a);
-    return cudaGetLastError();
-}
 
 cudaError_t launchConvWgrad(const ConvLaunch& c, const uint16_t* dy, float* dw, int smCount, cudaStream_t st)
 {
@@ -561,12 +309,6 @@ cudaError_t launchConvWgrad(const ConvLaunch& c, const uint16_t* dy, float* dw, 
     return cudaGetLastError();
 }
 
-cudaError_t launchPackConvWeights(const float* w, int Cin, int Cout, int flip, uint16_t* out, cudaStream_t st)
-{
-    k_pack_conv_weights<<<256, 256, 0, st>>>(w, Cin, Cout, flip, out);
-    return cudaGetLastError();
-}
-
 cudaError_t launchTcGemm(const uint16_t* A, const uint16_t* B, float* D, int M, int N, int K, cudaStream_t st)
 {
     size_t smem = 2 * (size_t(kGemmRows) * kGemmChunk * 2 + size_t(N) * kGemmChunk * 2);
@@ -579,11 +321,16 @@ cudaError_t launchTcGemm(const uint16_t* A, const uint16_t* B, float* D, int M, 
 
 cudaError_t takeTcError(int* flag)
 {
-    int zero      = 0;
+    int zero = 0, conv = 0;
     cudaError_t e = cudaMemcpyFromSymbol(flag, g_tcError, sizeof(int));
     if (e != cudaSuccess)
         return e;
-    return cudaMemcpyToSymbol(g_tcError, &zero, sizeof(int));
+    if ((e = cudaMemcpyToSymbol(g_tcError, &zero, sizeof(int))) != cudaSuccess)
+        return e;
+    if ((e = takeConvError(&conv)) != cudaSuccess)
+        return e;
+    *flag |= conv;
+    return cudaSuccess;
 }
 
 } // namespace agb

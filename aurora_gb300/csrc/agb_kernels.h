@@ -156,7 +156,7 @@ struct TemporalSettings
 cudaError_t launchTemporalResolve(const float4* accum, const float4* history, const float4* motion,
     const float* depthView, int W, int H, const TemporalSettings& s, float4* out, cudaStream_t st);
 
-// agb_denoise.cu
+// agb_conv.cu: the 3x3 convolution (TMA-fed, warp-specialised tcgen05 implicit GEMM).
 struct ConvLaunch
 {
     const uint16_t* in0;
@@ -166,14 +166,21 @@ struct ConvLaunch
     uint16_t* out;
     float* out32;
     int B, H, W, C0, C1, Cout, up0, relu;
+    uint16_t* pool = nullptr; // [B][H/2][W/2][Cout]: 2x2 average of the BF16 outputs (H, W even)
 };
+// W even (and H even with up0 or pool); cudaErrorInvalidValue otherwise.
 cudaError_t launchConv3x3(const ConvLaunch& c, cudaStream_t st);
+cudaError_t launchPackConvWeights(const float* w, int Cin, int Cout, int flip, uint16_t* out, cudaStream_t st);
+// Reads and clears the convolution's timeout flag (1 = a bounded wait ran out).
+cudaError_t takeConvError(int* flag);
+
+// agb_denoise.cu
 // dW[tap][ci][co] += sum over pixels of X[p + d][ci] dY[p][co] (X as c.in0 / c.in1 / c.up0; c.Cout
 // the layer's output channels, at most 256).
 cudaError_t launchConvWgrad(const ConvLaunch& c, const uint16_t* dy, float* dw, int smCount, cudaStream_t st);
-cudaError_t launchPackConvWeights(const float* w, int Cin, int Cout, int flip, uint16_t* out, cudaStream_t st);
 cudaError_t launchTcGemm(const uint16_t* A, const uint16_t* B, float* D, int M, int N, int K, cudaStream_t st);
-// Reads and clears the tensor-core kernels' timeout flag (1 = a bounded wait ran out).
+// Reads and clears the tensor-core kernels' timeout flags (1 = a bounded wait ran out), the
+// convolution's included.
 cudaError_t takeTcError(int* flag);
 
 // agb_unet.cu: the U-Net denoiser (layer graph, training state, elementwise kernels).
@@ -205,7 +212,6 @@ private:
     cudaError_t ensureShape(int B, int H, int W, bool training);
     static size_t pixels(int B, int H, int W, int level);
     ConvLaunch layerLaunch(int i, const uint16_t* x) const;
-    cudaError_t pool(int src, int dst);
 
     cudaStream_t stream_ = nullptr;
     int smCount_         = 0;

@@ -98,6 +98,32 @@ __device__ __forceinline__ void bulkLoad(void* dst, const void* src, uint32_t by
                  : "memory");
 }
 
+// Tiled tensor copies global -> shared through a tensor map (TMA); completion counted on the
+// mbarrier.  Coordinates are in elements, innermost first; elements outside the tensor read as
+// zero.  The innermost coordinate times the element size must be a multiple of 16 bytes, and dst
+// 128-byte aligned.
+__device__ __forceinline__ void tensorLoad4(void* dst, const void* map, int c0, int c1, int c2, int c3,
+    uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+                 "%4, %5}], [%6];" ::"r"(smemAddr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smemAddr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tensorLoad5(void* dst, const void* map, int c0, int c1, int c2, int c3, int c4,
+    uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+                 "%4, %5, %6}], [%7];" ::"r"(smemAddr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smemAddr(bar))
+                 : "memory");
+}
+// Plain arrival (no transaction bytes).
+__device__ __forceinline__ void mbarArrive(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smemAddr(bar)) : "memory");
+}
+
 __device__ __forceinline__ void fenceProxyAsync()
 {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");

@@ -32,25 +32,6 @@ inline unsigned gridFor(long n, int block = 256)
     return unsigned(std::min<long>(std::max<long>(g, 1), 1L << 20));
 }
 
-// 2x2 average pooling, NHWC BF16; H, W of the input (even).
-__global__ void k_avgpool2(const uint16_t* x, uint16_t* y, int B, int H, int W, int C)
-{
-    long n = long(B) * (H / 2) * (W / 2) * C;
-    for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x)
-    {
-        int c    = int(i % C);
-        long t   = i / C;
-        int x2   = int(t % (W / 2));
-        t /= (W / 2);
-        int y2   = int(t % (H / 2));
-        int b    = int(t / (H / 2));
-        size_t r0 = ((size_t(b) * H + 2 * y2) * W + 2 * x2) * C + c;
-        size_t r1 = r0 + size_t(W) * C;
-        float s   = ((bf(x[r0]) + bf(x[r0 + C])) + bf(x[r1])) + bf(x[r1 + C]);
-        y[i]      = tobf(s * 0.25f);
-    }
-}
-
 // gs (H x W) += 0.25 * gp (H/2 x W/2).
 __global__ void k_avgpool2_grad(const float* gp, float* gs, int B, int H, int W, int C)
 {
@@ -445,14 +426,6 @@ ConvLaunch UnetDenoiser::layerLaunch(int i, const uint16_t* x) const
     return c;
 }
 
-cudaError_t UnetDenoiser::pool(int src, int dst)
-{
-    int lv = kActLevel[src];
-    int H = H_ >> lv, W = W_ >> lv, C = kActChannels[src];
-    k_avgpool2<<<gridFor(long(B_) * (H / 2) * (W / 2) * C), 256, 0, stream_>>>(act_[src], act_[dst], B_, H, W, C);
-    return cudaGetLastError();
-}
-
 cudaError_t UnetDenoiser::forward(const uint16_t* x, int B, int H, int W, bool training)
 {
     cudaError_t e = ensureShape(B, H, W, training);
@@ -461,13 +434,12 @@ cudaError_t UnetDenoiser::forward(const uint16_t* x, int B, int H, int W, bool t
     input_ = x;
     for (int i = 0; i < kLayers; i++)
     {
-        if (i == 2 && (e = pool(A_S0, A_P0)) != cudaSuccess)
-            return e;
-        if (i == 4 && (e = pool(A_S1, A_P1)) != cudaSuccess)
-            return e;
-        if (i == 6 && (e = pool(A_S2, A_P2)) != cudaSuccess)
-            return e;
-        if ((e = launchConv3x3(layerLaunch(i, x), stream_)) != cudaSuccess)
+        ConvLaunch c = layerLaunch(i, x);
+        // The encoder's 2x2 average pools run in the epilogue of the convolution whose output they
+        // downsample (S0 -> P0, S1 -> P1, S2 -> P2).
+        if (i == 1 || i == 3 || i == 5)
+            c.pool = act_[kLayerDefs[i].out + 1];
+        if ((e = launchConv3x3(c, stream_)) != cudaSuccess)
             return e;
     }
     return cudaSuccess;

@@ -538,10 +538,17 @@ AGB_API agb_status agb_tc_gemm_bf16(const uint16_t* a, const uint16_t* b, float*
  * out[b][y][x][:] = bias + sum over taps and input channels of in[b][y+dy][x+dx][:] * w, zero
  * padded, optional ReLU; the input is the channel concatenation of in0 (read through a nearest 2x
  * upsample from height/2 x width/2 when up0) and in1 (may be null, c1 = 0).  c0, c1 and cout are
- * multiples of 16 (c0 >= 16, cout <= 256); wpack is the output of agb_pack_conv_weights; out (BF16)
- * and out32 (FP32) may each be null.  Exported for the denoiser's parity tests. */
+ * multiples of 16 (c0 >= 16, cout <= 1024); width even (height too with up0); wpack is the output
+ * of agb_pack_conv_weights; out (BF16) and out32 (FP32) may each be null.  Exported for the
+ * denoiser's parity tests. */
 AGB_API agb_status agb_conv3x3_bf16(const uint16_t* in0, const uint16_t* in1, const uint16_t* wpack,
     const float* bias, uint16_t* out, float* out32, int32_t batch, int32_t height, int32_t width,
+    int32_t c0, int32_t c1, int32_t cout, int32_t up0, int32_t relu, void* cuda_stream);
+/* agb_conv3x3_bf16 with the encoder's 2x2 average pool fused into its epilogue: also writes
+ * pool[b][y/2][x/2][:] = bf16(0.25 * (((o(2y,2x) + o(2y,2x+1)) + o(2y+1,2x)) + o(2y+1,2x+1))) over the
+ * BF16 outputs o (height and width even).  Exported for the denoiser's parity tests. */
+AGB_API agb_status agb_conv3x3_pool_bf16(const uint16_t* in0, const uint16_t* in1, const uint16_t* wpack,
+    const float* bias, uint16_t* out, uint16_t* pool, int32_t batch, int32_t height, int32_t width,
     int32_t c0, int32_t c1, int32_t cout, int32_t up0, int32_t relu, void* cuda_stream);
 /* Weight gradient of agb_conv3x3_bf16 (same input arguments, cout <= 256): adds
  * dw[tap][cin][cout] += sum over pixels of in[p + d(tap)][cin] * dy[p][cout] into the FP32 array dw. */

@@ -73,6 +73,62 @@ def test_conv3x3_matches_oracle(agb, case):
     np.testing.assert_array_equal(g16, ref.bf16_bits(g32))
 
 
+POOL_CASES = [
+    # B, H, W, C0, C1, Cout, up0, relu: the encoder's pooled layers (32, 64, 128 channels), a
+    # decoder-shaped input, and a width spanning two 256-pixel tiles
+    (2, 16, 24, 16, 0, 32, False, True),
+    (1, 8, 12, 64, 0, 64, False, True),
+    (1, 6, 10, 128, 0, 128, False, True),
+    (2, 12, 20, 32, 32, 64, True, True),
+    (1, 4, 600, 16, 0, 32, False, False),
+]
+
+
+@pytest.mark.parametrize("case", POOL_CASES)
+def test_conv3x3_fused_pool_matches_oracle(agb, case):
+    """The 2x2 average pool in the convolution's epilogue equals a pool over the stored BF16
+    outputs, bit for bit, and the convolution itself stays within the oracle's bound."""
+    import torch
+    from aurora_gb300 import _abi
+    B, H, W, C0, C1, Cout, up0, relu = case
+    rng = np.random.default_rng(sum(case[:6]) + 11)
+    h0, w0 = (H // 2, W // 2) if up0 else (H, W)
+    x0 = ref.bf16_bits(rng.normal(0, 1, (B, h0, w0, C0)))
+    x1 = ref.bf16_bits(rng.normal(0, 1, (B, H, W, C1))) if C1 else None
+    w = ref.bf16(rng.normal(0, 0.2, (9, C0 + C1, Cout)))
+    bias = rng.normal(0, 0.1, Cout)
+    wd = torch.from_numpy(np.ascontiguousarray(w, np.float32)).cuda()
+    wp = torch.zeros(9 * (C0 + C1) * Cout, dtype=torch.int16, device="cuda")
+    _abi.check(agb.agb_pack_conv_weights(wd.data_ptr(), C0 + C1, Cout, 0, wp.data_ptr(), None))
+    d0 = to_dev(x0)
+    d1 = to_dev(x1) if x1 is not None else None
+    bd = torch.from_numpy(np.asarray(bias, np.float32)).cuda()
+    out16 = torch.zeros((B, H, W, Cout), dtype=torch.int16, device="cuda")
+    pool16 = torch.zeros((B, H // 2, W // 2, Cout), dtype=torch.int16, device="cuda")
+    _abi.check(agb.agb_conv3x3_pool_bf16(d0.data_ptr(), d1.data_ptr() if d1 is not None else None,
+                                         wp.data_ptr(), bd.data_ptr(), out16.data_ptr(),
+                                         pool16.data_ptr(), B, H, W, C0, C1, Cout,
+                                         1 if up0 else 0, 1 if relu else 0, None))
+    o16 = out16.cpu().numpy().view(np.uint16)
+    p16 = pool16.cpu().numpy().view(np.uint16)
+    xin = ref.from_bits(x0)
+    if up0:
+        xin = ref.upsample2(xin)
+    if C1:
+        xin = np.concatenate([xin, ref.from_bits(x1)], axis=3)
+    want = ref.conv3x3(xin, w, bias)
+    if relu:
+        want = np.maximum(want, 0.0)
+    scale = ref.conv3x3(np.abs(xin), np.abs(w), np.abs(bias)) + 1e-30
+    # BF16 outputs: within half a BF16 ulp (2^-8 relative) of the bound-respecting FP32 result.
+    err = np.abs(ref.from_bits(o16) - want) / (scale + np.abs(want))
+    assert err.max() < 2 ** -8 + 1e-5
+    # The pool over the stored outputs in FP32, in the order ((x00 + x01) + x10) + x11.
+    o = ref.from_bits(o16).astype(np.float32).reshape(B, H // 2, 2, W // 2, 2, Cout)
+    s = ((o[:, :, 0, :, 0] + o[:, :, 0, :, 1]) + o[:, :, 1, :, 0]) + o[:, :, 1, :, 1]
+    np.testing.assert_array_equal(p16, ref.bf16_bits(s * np.float32(0.25)))
+
+
 @pytest.mark.parametrize("case", [(2, 16, 24, 32, 16), (1, 8, 12, 256, 128), (1, 6, 10, 48, 96)])
 def test_conv3x3_data_gradient_matches_oracle(agb, case):
     B, H, W, Cin, Cout = case
