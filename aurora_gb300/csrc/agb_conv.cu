@@ -11,13 +11,15 @@
 //   - a nearest-2x-upsampled input (the decoder's in0) is staged at its own half resolution
 //     (pixels j0 - 1 .. j0 + 128 of row (y + dy) >> 1), and the same taps read it at offsets
 //     0, 1, 1 (even) and 1, 1, 2 (odd): the upsample costs nothing and is never materialised.
-// A staged row is K-major without swizzle: for one 16-channel group, channels 0-7 of entry i at
-// byte 16 i, channels 8-15 at kHalfBytes + 16 i, so one TMA box (8 channels x 130 entries) lands
-// exactly there and an MMA A descriptor at +16 bytes per entry of offset addresses any run.
+// A staged row is one TMA box (16 channels x 130 entries, 32 bytes per entry) in the K-major
+// 32-byte-swizzled layout: the 16-byte halves of entry i sit at 32 i and 32 i + 16, exchanged when
+// bit 7 of the address is set.  Both the TMA write and the MMA read apply the swizzle to the shared
+// memory address itself, so an A descriptor started 32 bytes per entry of offset later addresses
+// the run: every staged byte is a whole 32-byte sector of the source (one request per entry).
 //
 // Roles (320 threads, one CTA per SM, static round-robin over tiles):
-//   warp 0   TMA producer: per 16-channel group, (R + 2) x 2 halo rows (E, O) x 2 channel halves
-//            (or the fewer half-resolution rows of an upsampled input) by cp.async.bulk.tensor
+//   warp 0   TMA producer: per 16-channel group, (R + 2) x 2 halo rows (E, O) (or the fewer
+//            half-resolution rows of an upsampled input) by cp.async.bulk.tensor
 //            with zero fill outside the image, and the group's 9 weight slices (N x 16 each) by
 //            one 1D bulk copy, into a ring of `stages` shared-memory stages (full / empty
 //            mbarriers);
@@ -42,16 +44,13 @@
 namespace agb
 {
 
-// Set by a conv kernel whose bounded wait ran out; read and cleared with takeConvError.
-__device__ int g_convError;
-
 namespace
 {
 
 constexpr int kHaloEntries      = 130;               // 128 MMA rows + offsets 0..2
-constexpr uint32_t kBoxBytes    = kHaloEntries * 16; // one TMA box: 8 channels x 130 entries
-constexpr uint32_t kHalfBytes   = 2176;              // kBoxBytes rounded up to 128 (TMA alignment)
-constexpr uint32_t kRowBytes    = 2 * kHalfBytes;    // one staged row: both channel halves
+constexpr uint32_t kEntryBytes  = 32;                // 16 channels of one entry
+constexpr uint32_t kBoxBytes    = kHaloEntries * kEntryBytes; // one TMA box: 16 channels x 130 entries
+constexpr uint32_t kRowBytes    = 4352;              // kBoxBytes rounded up to 256 (the swizzle atom)
 constexpr int kThreads          = 320; // producer, MMA issuer, 8 epilogue warps
 constexpr uint32_t kAccStride   = 256;               // TMEM columns per accumulator buffer
 constexpr int kMaxStages        = 4;
@@ -64,6 +63,9 @@ struct ConvTmaArgs
     uint16_t* out;         // [B][H][W][Cout] or null
     float* out32;          // [B][H][W][Cout] or null
     uint16_t* pool;        // [B][H/2][W/2][Cout] or null (2x2 average of the BF16 outputs)
+    float4* rad;           // [B][H][W] RGBA radiance or null (the denoiser's output layer)
+    const uint16_t* radIn; // [B][H][W][16] features (log1p noisy radiance in channels 0-2)
+    int* error;            // set to 1 when a bounded wait runs out
     int B, H, W, Cout, up0, relu;
     int N, nTiles, R, G, G0, stages;
     int tilesX, rowBlocks, numTiles;
@@ -100,12 +102,79 @@ __device__ __forceinline__ bool leaderWait(uint64_t* bar, uint32_t parity, int l
     return __shfl_sync(0xffffffffu, got, 0) != 0;
 }
 
+// One 32-byte store (the address 32-byte aligned): a whole sector per lane.
+__device__ __forceinline__ void st256(void* p, const uint32_t (&w)[8])
+{
+    asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "r"(w[0]), "r"(w[1]), "r"(w[2]),
+        "r"(w[3]), "r"(w[4]), "r"(w[5]), "r"(w[6]), "r"(w[7])
+                 : "memory");
+}
+
 __device__ __forceinline__ float bfv(uint16_t b) { return __uint_as_float(uint32_t(b) << 16); }
 __device__ __forceinline__ uint16_t tobf(float v) { return __bfloat16_as_ushort(__float2bfloat16_rn(v)); }
 
+// Output rows per tile for N output channels: as many as one TMEM buffer of 256 columns holds
+// (2 R N), at most 4.
+__host__ __device__ constexpr int tileRows(int n) { return n >= 64 ? 2 : 4; }
+
+// The MMAs of one pipeline stage (one 16-channel input group), fully unrolled.  Halo row i (input
+// row y0 - 1 + i) feeds output rows r = i - 2 .. i (those inside the tile) through the vertical taps
+// dy = i - r; their accumulators are adjacent in TMEM and the weight slices of the three dy are
+// stacked (dy = 2, 1, 0), so one MMA per (halo row, parity, dx) covers every output row the halo
+// row feeds: N, 2N or 3N accumulator columns at once.  In the first group of a tile an
+// accumulator starts its sum (accumulate = 0) with the dx = 0 MMA of halo row r, split off as an
+// MMA of its own.
+template <int N, bool UP>
+__device__ __forceinline__ void issueStage(uint32_t aAddr, uint32_t bAddr, uint32_t dBase, bool first)
+{
+    constexpr int R = tileRows(N);
+    // K-major, 32-byte swizzle: entries of 32 bytes (16 channels), 8-entry atoms 256 bytes apart.
+    const uint64_t aDesc0 = tc::smemDescSw32(aAddr, 256);
+    const uint64_t bDesc0 = tc::smemDesc(bAddr, tc::kSliceLbo, tc::kSliceSbo);
+#pragma unroll
+    for (int i = 0; i < R + 2; i++)
+    {
+        const int rLo   = i - 2 > 0 ? i - 2 : 0;
+        const int rHi   = i < R - 1 ? i : R - 1;
+        const int count = rHi - rLo + 1;
+#pragma unroll
+        for (int par = 0; par < 2; par++)
+#pragma unroll
+            for (int dx = 0; dx < 3; dx++)
+            {
+                // Entry offset of the run: 0, 1, 1 (even outputs), 1, 1, 2 (odd outputs).
+                const uint32_t shift = par == 0 ? (dx == 0 ? 0u : 1u) : (dx == 2 ? 2u : 1u);
+                uint32_t row;
+                if (UP)
+                    row = uint32_t(((i - 1) >> 1) + 1); // half-resolution row of input row y0 - 1 + i
+                else
+                {
+                    // E for the centre tap of even outputs and the side taps of odd outputs.
+                    const int odd = par == 0 ? (dx == 1 ? 0 : 1) : (dx == 1 ? 1 : 0);
+                    row           = uint32_t(i * 2 + odd);
+                }
+                const uint64_t ad = aDesc0 + ((row * kRowBytes + shift * kEntryBytes) >> 4);
+                const uint64_t bd =
+                    bDesc0 + ((uint32_t(dx) * 3u * N * 32u + uint32_t(2 - (i - rLo)) * N * 32u) >> 4);
+                const uint32_t d = dBase + uint32_t((par * R + rLo) * N);
+                if (first && dx == 0 && i <= R - 1)
+                {
+                    if (count > 1)
+                        tc::mma(d, ad, bd, tc::idescBf16(128, uint32_t((count - 1) * N)), 1u);
+                    tc::mma(d + uint32_t((count - 1) * N), ad, bd + ((uint32_t(count - 1) * N * 32u) >> 4),
+                        tc::idescBf16(128, uint32_t(N)), 0u);
+                }
+                else
+                    tc::mma(d, ad, bd, tc::idescBf16(128, uint32_t(count * N)), 1u);
+            }
+    }
+}
+
+template <int N>
 __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_constant__ CUtensorMap tm0,
     const __grid_constant__ CUtensorMap tm1, const ConvTmaArgs a)
 {
+    constexpr int R = tileRows(N);
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint64_t full[kMaxStages], empty[kMaxStages], accFull[2], accEmpty[2], drain;
     __shared__ uint32_t tmemBase;
@@ -113,8 +182,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_consta
     const int warp = tid >> 5;
     const int lane = tid & 31;
     const int S    = a.stages;
-    const int N    = a.N;
-    const int R    = a.R;
 
     if (warp == 1)
         tc::tmemAlloc(&tmemBase, 2 * kAccStride);
@@ -169,22 +236,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_consta
                     const int c     = (in0 ? g : g - a.G0) * 16;
                     const void* map = in0 ? static_cast<const void*>(&tm0) : static_cast<const void*>(&tm1);
                     const int rows  = up ? upRowCount(q.y0, R) : (R + 2) * 2;
-                    tc::mbarExpectTx(&full[s], wBytes + uint32_t(rows) * 2u * kBoxBytes);
+                    tc::mbarExpectTx(&full[s], wBytes + uint32_t(rows) * kBoxBytes);
                     tc::bulkLoad(Bw, a.wpack + (size_t(q.nt) * a.G + g) * 9 * size_t(N) * 16, wBytes, &full[s]);
                     if (up)
                     {
                         const int h0 = upRowBase(q.y0);
                         for (int i = 0; i < rows; i++)
-                            for (int h = 0; h < 2; h++)
-                                tc::tensorLoad4(A + i * kRowBytes + h * kHalfBytes, map, c + 8 * h, q.j0 - 1, h0 + i,
-                                    q.b, &full[s]);
+                            tc::tensorLoad4(A + i * kRowBytes, map, c, q.j0 - 1, h0 + i, q.b, &full[s]);
                     }
                     else
                     {
                         for (int i = 0; i < R + 2; i++)
                             for (int p = 0; p < 2; p++)
-                                for (int h = 0; h < 2; h++)
-                                    tc::tensorLoad5(A + (i * 2 + p) * kRowBytes + h * kHalfBytes, map, c + 8 * h, p,
+                                tc::tensorLoad5(A + (i * 2 + p) * kRowBytes, map, c, p,
                                         q.j0 - 1, q.y0 - 1 + i, q.b, &full[s]);
                     }
                     issued[s]     = true;
@@ -204,12 +268,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_consta
         // ---------------------------------------------------------------- MMA issuer
         if (lane == 0)
         {
-            const uint32_t idesc = tc::idescBf16(128, uint32_t(N));
             uint32_t it = 0;
             int k       = 0;
             for (int t = blockIdx.x; t < a.numTiles && ok; t += gridDim.x, k++)
             {
-                const Tile q       = decodeTile(a, t);
                 const int buf      = k & 1;
                 const uint32_t aph = uint32_t(k >> 1) & 1u;
                 if (!tc::mbarWait(&accEmpty[buf], aph ^ 1u))
@@ -231,34 +293,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_consta
                     tc::fenceAfterSync();
                     const uint32_t aAddr = tc::smemAddr(smem + size_t(s) * a.stageBytes);
                     const uint32_t bAddr = aAddr + a.aBytes;
-                    const bool up        = g < a.G0 && a.up0;
-                    const int h0         = upRowBase(q.y0);
-                    for (int r = 0; r < R; r++)
-                        for (int par = 0; par < 2; par++)
-                        {
-                            const uint32_t d = dBase + uint32_t((r * 2 + par) * N);
-                            for (int dy = 0; dy < 3; dy++)
-                                for (int dx = 0; dx < 3; dx++)
-                                {
-                                    // Entry offset of the run: 0, 1, 1 (even outputs), 1, 1, 2 (odd).
-                                    const uint32_t shift = par == 0 ? (dx == 0 ? 0u : 1u) : (dx == 2 ? 2u : 1u);
-                                    uint32_t row;
-                                    if (up)
-                                        row = uint32_t(((q.y0 + r + dy - 1) >> 1) - h0);
-                                    else
-                                    {
-                                        // E for the centre tap of even outputs and the side taps of
-                                        // odd outputs, O otherwise.
-                                        const int odd = par == 0 ? (dx == 1 ? 0 : 1) : (dx == 1 ? 1 : 0);
-                                        row           = uint32_t((r + dy) * 2 + odd);
-                                    }
-                                    const uint64_t ad =
-                                        tc::smemDesc(aAddr + row * kRowBytes + shift * 16u, kHalfBytes, 128);
-                                    const uint64_t bd = tc::smemDesc(bAddr + uint32_t((dy * 3 + dx) * N) * 32u,
-                                        tc::kSliceLbo, tc::kSliceSbo);
-                                    tc::mma(d, ad, bd, idesc, (g | dy | dx) != 0 ? 1u : 0u);
-                                }
-                        }
+                    if (g < a.G0 && a.up0)
+                        issueStage<N, true>(aAddr, bAddr, dBase, g == 0);
+                    else
+                        issueStage<N, false>(aAddr, bAddr, dBase, g == 0);
                     tc::commit(&empty[s]);
                 }
                 if (!ok)
@@ -306,12 +344,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_consta
                 const int c0 = (item % chunks) * 16;
                 // All accumulators of the item (2 or 4) in flight before one wait.
                 uint32_t v[4][16];
-                tc::tmemLoad16(tBase + uint32_t((r * 2 + 0) * N + c0), v[0]);
-                tc::tmemLoad16(tBase + uint32_t((r * 2 + 1) * N + c0), v[1]);
+                // Accumulator (row r, parity p) at columns (p R + r) N.
+                tc::tmemLoad16(tBase + uint32_t(r * N + c0), v[0]);
+                tc::tmemLoad16(tBase + uint32_t((R + r) * N + c0), v[1]);
                 if (step == 2)
                 {
-                    tc::tmemLoad16(tBase + uint32_t((r * 2 + 2) * N + c0), v[2]);
-                    tc::tmemLoad16(tBase + uint32_t((r * 2 + 3) * N + c0), v[3]);
+                    tc::tmemLoad16(tBase + uint32_t((r + 1) * N + c0), v[2]);
+                    tc::tmemLoad16(tBase + uint32_t((R + r + 1) * N + c0), v[3]);
                 }
                 tc::tmemWaitLoad();
                 float bv[16];
@@ -344,16 +383,26 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_consta
 #pragma unroll
                         for (int i = 0; i < 8; i++)
                             w[i] = uint32_t(h[2 * i]) | (uint32_t(h[2 * i + 1]) << 16);
-                        uint4* o = reinterpret_cast<uint4*>(a.out + px * a.Cout + cb + c0);
-                        o[0]     = make_uint4(w[0], w[1], w[2], w[3]);
-                        o[1]     = make_uint4(w[4], w[5], w[6], w[7]);
+                        st256(a.out + px * a.Cout + cb + c0, w);
                     }
                     if (st && a.out32)
                     {
-                        float4* o = reinterpret_cast<float4*>(a.out32 + px * a.Cout + cb + c0);
+                        uint32_t w0[8], w1[8];
 #pragma unroll
-                        for (int i = 0; i < 4; i++)
-                            o[i] = make_float4(f[4 * i], f[4 * i + 1], f[4 * i + 2], f[4 * i + 3]);
+                        for (int i = 0; i < 8; i++)
+                        {
+                            w0[i] = __float_as_uint(f[i]);
+                            w1[i] = __float_as_uint(f[8 + i]);
+                        }
+                        st256(a.out32 + px * a.Cout + cb + c0, w0);
+                        st256(a.out32 + px * a.Cout + cb + c0 + 8, w1);
+                    }
+                    if (st && a.rad && c0 == 0)
+                    {
+                        const uint16_t* xin = a.radIn + px * 16;
+                        a.rad[px] = make_float4(fmaxf(expm1f(f[0] + bfv(__ldg(xin + 0))), 0.f),
+                            fmaxf(expm1f(f[1] + bfv(__ldg(xin + 1))), 0.f), fmaxf(expm1f(f[2] + bfv(__ldg(xin + 2))), 0.f),
+                            1.f);
                     }
                     // ((x00 + x01) + x10) + x11 over the stored BF16 values.
 #pragma unroll
@@ -367,9 +416,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_consta
                     for (int i = 0; i < 8; i++)
                         w[i] = uint32_t(tobf(psum[2 * i] * 0.25f)) | (uint32_t(tobf(psum[2 * i + 1] * 0.25f)) << 16);
                     const size_t pp = (size_t(q.b) * (a.H >> 1) + ((q.y0 + r) >> 1)) * W2 + j;
-                    uint4* o        = reinterpret_cast<uint4*>(a.pool + pp * a.Cout + cb + c0);
-                    o[0]            = make_uint4(w[0], w[1], w[2], w[3]);
-                    o[1]            = make_uint4(w[4], w[5], w[6], w[7]);
+                    st256(a.pool + pp * a.Cout + cb + c0, w);
                 }
             }
             tc::fenceBeforeSync();
@@ -384,7 +431,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_consta
     if (warp == 1)
         tc::tmemDealloc(tmem, 2 * kAccStride);
     if (!ok)
-        atomicExch(&g_convError, 1);
+        atomicExch(a.error, 1);
 }
 
 // ----------------------------------------------------------------------------- host side
@@ -412,10 +459,10 @@ cudaError_t mapPairs(CUtensorMap* m, const uint16_t* base, int B, int H, int W, 
         return cudaErrorNotSupported;
     cuuint64_t dims[5]    = { cuuint64_t(C), 2, cuuint64_t(W / 2), cuuint64_t(H), cuuint64_t(B) };
     cuuint64_t strides[4] = { cuuint64_t(C) * 2, cuuint64_t(C) * 4, cuuint64_t(W) * C * 2, cuuint64_t(H) * W * C * 2 };
-    cuuint32_t box[5]     = { 8, 1, kHaloEntries, 1, 1 };
+    cuuint32_t box[5]     = { 16, 1, kHaloEntries, 1, 1 };
     cuuint32_t es[5]      = { 1, 1, 1, 1, 1 };
     CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<uint16_t*>(base), dims, strides, box, es,
-        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
@@ -428,10 +475,10 @@ cudaError_t mapRows(CUtensorMap* m, const uint16_t* base, int B, int H0, int W0,
         return cudaErrorNotSupported;
     cuuint64_t dims[4]    = { cuuint64_t(C), cuuint64_t(W0), cuuint64_t(H0), cuuint64_t(B) };
     cuuint64_t strides[3] = { cuuint64_t(C) * 2, cuuint64_t(W0) * C * 2, cuuint64_t(H0) * W0 * C * 2 };
-    cuuint32_t box[4]     = { 8, kHaloEntries, 1, 1 };
+    cuuint32_t box[4]     = { 16, kHaloEntries, 1, 1 };
     cuuint32_t es[4]      = { 1, 1, 1, 1 };
     CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<uint16_t*>(base), dims, strides, box, es,
-        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
@@ -458,13 +505,13 @@ int smCountOf(int dev)
 // of a pair) and move fewer weight bytes per MMA than 128-channel tiles would.
 int convTileChannels(int cout) { return cout % 64 == 0 ? 64 : cout % 32 == 0 ? 32 : 16; }
 
-// Output rows per tile: as many as the 256 accumulator columns of one TMEM buffer hold (2 x N each),
-// at most 4.
-int convTileRows(int n) { return std::min(4, std::max(1, 256 / (2 * n))); }
-
 cudaError_t launchConv3x3(const ConvLaunch& c, cudaStream_t st)
 {
     if (c.W % 2 || (c.up0 && c.H % 2) || (c.pool && c.H % 2))
+        return cudaErrorInvalidValue;
+    // Outputs are written in 32-byte pieces.
+    if ((reinterpret_cast<uintptr_t>(c.out) | reinterpret_cast<uintptr_t>(c.out32) | reinterpret_cast<uintptr_t>(c.pool)) &
+        31u)
         return cudaErrorInvalidValue;
     ConvTmaArgs a{};
     a.wpack = c.wpack;
@@ -472,12 +519,12 @@ cudaError_t launchConv3x3(const ConvLaunch& c, cudaStream_t st)
     a.out   = c.out;
     a.out32 = c.out32;
     a.pool  = c.pool;
+    a.rad   = reinterpret_cast<float4*>(c.radiance);
+    a.radIn = c.radianceInput;
     a.B = c.B, a.H = c.H, a.W = c.W, a.Cout = c.Cout, a.up0 = c.up0, a.relu = c.relu;
     a.N      = convTileChannels(c.Cout);
     a.nTiles = c.Cout / a.N;
-    a.R      = convTileRows(a.N);
-    if (c.pool && a.R < 2)
-        return cudaErrorInvalidValue;
+    a.R      = tileRows(a.N);
     a.G         = (c.C0 + c.C1) / 16;
     a.G0        = c.C0 / 16;
     a.tilesX    = (c.W / 2 + 127) / 128;
@@ -487,10 +534,13 @@ cudaError_t launchConv3x3(const ConvLaunch& c, cudaStream_t st)
         return cudaErrorInvalidValue;
     a.numTiles   = int(tiles);
     a.aBytes     = uint32_t(a.R + 2) * 2 * kRowBytes;
-    a.stageBytes = (a.aBytes + 9u * uint32_t(a.N) * 32u + 127u) & ~127u;
+    a.stageBytes = (a.aBytes + 9u * uint32_t(a.N) * 32u + 1023u) & ~1023u;
     a.stages     = int(std::min<size_t>(kMaxStages, kSmemBudget / a.stageBytes));
     if (a.stages < 2)
         return cudaErrorInvalidValue;
+    cudaError_t e0 = tcErrorFlag(&a.error);
+    if (e0 != cudaSuccess)
+        return e0;
     CUtensorMap m0, m1;
     cudaError_t e = c.up0 ? mapRows(&m0, c.in0, c.B, c.H / 2, c.W / 2, c.C0) : mapPairs(&m0, c.in0, c.B, c.H, c.W, c.C0);
     if (e != cudaSuccess)
@@ -505,20 +555,21 @@ cudaError_t launchConv3x3(const ConvLaunch& c, cudaStream_t st)
     // At least half of the SM's shared memory, so that one CTA (with all 512 TMEM columns) runs
     // per SM.
     const size_t smem = std::max<size_t>(size_t(a.stages) * a.stageBytes, 120 * 1024);
-    if ((e = cudaFuncSetAttribute(k_conv3x3_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))) !=
-        cudaSuccess)
+    auto kern = a.N == 64 ? k_conv3x3_tma<64> : a.N == 32 ? k_conv3x3_tma<32> : k_conv3x3_tma<16>;
+    if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))) != cudaSuccess)
         return e;
     int dev = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess)
         return e;
     const int grid = int(std::min<long>(tiles, smCountOf(dev)));
-    k_conv3x3_tma<<<grid, kThreads, smem, st>>>(m0, m1, a);
+    kern<<<grid, kThreads, smem, st>>>(m0, m1, a);
     return cudaGetLastError();
 }
 
 // Packs FP32 weights w[tap][ci][co] (9 x Cin x Cout) into the conv kernel's B layout (BF16): per
-// channel tile and 16-channel input group, the 9 slices in (dy, dx) order, each N x 16 in the
-// K-major core-matrix layout.  flip: pack the data-gradient weights instead, w'[tap'][co][ci] =
+// channel tile and 16-channel input group, for dx = 0, 1, 2 a stack of the three vertical taps'
+// slices (dy = 2, 1, 0; N x 16 each) in the K-major core-matrix layout, so that any run of them is
+// one B operand.  flip: pack the data-gradient weights instead, w'[tap'][co][ci] =
 // w[8 - tap'][ci][co], so that the convolution over dY computes dX (its Cin is then the layer's
 // Cout and vice versa).
 __global__ void k_pack_conv_weights(const float* w, int Cin, int Cout, int flip, int nt, uint16_t* out)
@@ -532,8 +583,10 @@ __global__ void k_pack_conv_weights(const float* w, int Cin, int Cout, int flip,
         const int tap = int(kk / kCin), c = int(kk % kCin);
         const float v = flip ? w[(size_t(8 - tap) * Cin + n) * Cout + c] : w[(size_t(tap) * Cin + c) * Cout + n];
         const int G = kCin / 16, tile = n / nt, nn = n % nt;
-        const size_t slice = (size_t(tile) * G + c / 16) * 9 + tap;
-        const size_t off   = slice * nt * 16 + tc::sliceOffset(uint32_t(nn), uint32_t(c % 16)) / 2;
+        const int dy = tap / 3, dx = tap % 3;
+        const size_t stack = (size_t(tile) * G + c / 16) * 3 + dx;
+        const uint32_t row = uint32_t((2 - dy) * nt + nn);
+        const size_t off   = stack * 3 * nt * 16 + tc::sliceOffset(row, uint32_t(c % 16)) / 2;
         out[off]           = __bfloat16_as_ushort(__float2bfloat16_rn(v));
     }
 }
@@ -544,13 +597,5 @@ cudaError_t launchPackConvWeights(const float* w, int Cin, int Cout, int flip, u
     return cudaGetLastError();
 }
 
-cudaError_t takeConvError(int* flag)
-{
-    int zero      = 0;
-    cudaError_t e = cudaMemcpyFromSymbol(flag, g_convError, sizeof(int));
-    if (e != cudaSuccess)
-        return e;
-    return cudaMemcpyToSymbol(g_convError, &zero, sizeof(int));
-}
 
 } // namespace agb

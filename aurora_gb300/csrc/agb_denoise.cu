@@ -321,16 +321,13 @@ cudaError_t launchTcGemm(const uint16_t* A, const uint16_t* B, float* D, int M, 
 
 cudaError_t takeTcError(int* flag)
 {
-    int zero = 0, conv = 0;
     cudaError_t e = cudaMemcpyFromSymbol(flag, g_tcError, sizeof(int));
-    if (e != cudaSuccess)
+    if (e != cudaSuccess || *flag == 0)
         return e;
-    if ((e = cudaMemcpyToSymbol(g_tcError, &zero, sizeof(int))) != cudaSuccess)
-        return e;
-    if ((e = takeConvError(&conv)) != cudaSuccess)
-        return e;
-    *flag |= conv;
-    return cudaSuccess;
+    int zero = 0;
+    return cudaMemcpyToSymbol(g_tcError, &zero, sizeof(int));
 }
+
+cudaError_t tcErrorFlag(int** flag) { return cudaGetSymbolAddress(reinterpret_cast<void**>(flag), g_tcError); }
 
 } // namespace agb

@@ -167,21 +167,24 @@ struct ConvLaunch
     float* out32;
     int B, H, W, C0, C1, Cout, up0, relu;
     uint16_t* pool = nullptr; // [B][H/2][W/2][Cout]: 2x2 average of the BF16 outputs (H, W even)
+    // The denoiser's output layer: RGBA radiance max(expm1(out[c] + radianceInput[c]), 0) for
+    // c = 0..2 (radianceInput: the BF16 features, 16 per pixel, log1p noisy radiance in 0..2).
+    float* radiance                = nullptr;
+    const uint16_t* radianceInput  = nullptr;
 };
-// W even (and H even with up0 or pool); cudaErrorInvalidValue otherwise.
+// W even (and H even with up0 or pool), outputs 32-byte aligned; cudaErrorInvalidValue otherwise.
 cudaError_t launchConv3x3(const ConvLaunch& c, cudaStream_t st);
 cudaError_t launchPackConvWeights(const float* w, int Cin, int Cout, int flip, uint16_t* out, cudaStream_t st);
-// Reads and clears the convolution's timeout flag (1 = a bounded wait ran out).
-cudaError_t takeConvError(int* flag);
 
 // agb_denoise.cu
 // dW[tap][ci][co] += sum over pixels of X[p + d][ci] dY[p][co] (X as c.in0 / c.in1 / c.up0; c.Cout
 // the layer's output channels, at most 256).
 cudaError_t launchConvWgrad(const ConvLaunch& c, const uint16_t* dy, float* dw, int smCount, cudaStream_t st);
 cudaError_t launchTcGemm(const uint16_t* A, const uint16_t* B, float* D, int M, int N, int K, cudaStream_t st);
-// Reads and clears the tensor-core kernels' timeout flags (1 = a bounded wait ran out), the
-// convolution's included.
+// Reads and clears the tensor-core kernels' timeout flag (1 = a bounded wait ran out).
 cudaError_t takeTcError(int* flag);
+// Device address of that flag on the current device (kernels in other translation units set it).
+cudaError_t tcErrorFlag(int** flag);
 
 // agb_unet.cu: the U-Net denoiser (layer graph, training state, elementwise kernels).
 class UnetDenoiser
@@ -193,11 +196,11 @@ public:
     cudaError_t init(uint64_t seed, cudaStream_t st, int smCount);
     static size_t paramCount();
     // x: [B][H][W][16] BF16 features (H, W multiples of 8).  Keeps the activations for backward.
-    cudaError_t forward(const uint16_t* x, int B, int H, int W, bool training);
+    // rgba (inference): the denoised RGBA radiance, written by the output layer's epilogue.
+    cudaError_t forward(const uint16_t* x, int B, int H, int W, bool training, float* rgba = nullptr);
     // After forward(training): L1 loss against target RGBA (FP32) and all parameter gradients.
     cudaError_t backward(const float* target);
     cudaError_t adam(float lr);
-    cudaError_t toRadiance(float* rgba);
     cudaError_t setParams(const float* host);
     const float* params() const { return params_; }
     const float* grads() const { return grads_; }

@@ -48,6 +48,14 @@ __device__ __forceinline__ uint64_t smemDesc(uint32_t addr, uint32_t lbo, uint32
     return d;
 }
 
+// Shared-memory descriptor of a K-major operand in the 32-byte swizzle layout (rows of 32 bytes =
+// one K16 block of BF16, 8-row atoms `sbo` bytes apart; the leading byte offset is unused):
+// layout type 6 in bits 61-63.
+__device__ __forceinline__ uint64_t smemDescSw32(uint32_t addr, uint32_t sbo)
+{
+    return smemDesc(addr, 16, sbo) | (uint64_t(6) << 61);
+}
+
 // Instruction descriptor of tcgen05.mma.kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A and B
 // (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits
 // 24-28.

@@ -147,18 +147,6 @@ __global__ void k_adam(float* w, const float* g, float* m, float* v, long n, flo
     }
 }
 
-// Denoised RGBA radiance: expm1(out32 + log1p input), alpha 1.
-__global__ void k_to_radiance(const float* out32, const uint16_t* x, float4* rgba, long P)
-{
-    for (long p = blockIdx.x * long(blockDim.x) + threadIdx.x; p < P; p += long(gridDim.x) * blockDim.x)
-    {
-        float r = expm1f(out32[p * 16 + 0] + bf(x[p * 16 + 0]));
-        float g = expm1f(out32[p * 16 + 1] + bf(x[p * 16 + 1]));
-        float b = expm1f(out32[p * 16 + 2] + bf(x[p * 16 + 2]));
-        rgba[p] = make_float4(fmaxf(r, 0.f), fmaxf(g, 0.f), fmaxf(b, 0.f), 1.f);
-    }
-}
-
 __device__ __forceinline__ float2 octEncode(float3 n)
 {
     float s = fabsf(n.x) + fabsf(n.y) + fabsf(n.z);
@@ -426,7 +414,7 @@ ConvLaunch UnetDenoiser::layerLaunch(int i, const uint16_t* x) const
     return c;
 }
 
-cudaError_t UnetDenoiser::forward(const uint16_t* x, int B, int H, int W, bool training)
+cudaError_t UnetDenoiser::forward(const uint16_t* x, int B, int H, int W, bool training, float* rgba)
 {
     cudaError_t e = ensureShape(B, H, W, training);
     if (e != cudaSuccess)
@@ -439,17 +427,18 @@ cudaError_t UnetDenoiser::forward(const uint16_t* x, int B, int H, int W, bool t
         // downsample (S0 -> P0, S1 -> P1, S2 -> P2).
         if (i == 1 || i == 3 || i == 5)
             c.pool = act_[kLayerDefs[i].out + 1];
+        // Inference: the output layer's epilogue writes the radiance (expm1 of the prediction)
+        // instead of the FP32 prediction.
+        if (i == kLayers - 1 && rgba && !training)
+        {
+            c.out32         = nullptr;
+            c.radiance      = rgba;
+            c.radianceInput = x;
+        }
         if ((e = launchConv3x3(c, stream_)) != cudaSuccess)
             return e;
     }
     return cudaSuccess;
-}
-
-cudaError_t UnetDenoiser::toRadiance(float* rgba)
-{
-    long P = long(pixels(B_, H_, W_, 0));
-    k_to_radiance<<<gridFor(P), 256, 0, stream_>>>(out32_, input_, reinterpret_cast<float4*>(rgba), P);
-    return cudaGetLastError();
 }
 
 cudaError_t UnetDenoiser::backward(const float* target)

@@ -539,8 +539,8 @@ AGB_API agb_status agb_tc_gemm_bf16(const uint16_t* a, const uint16_t* b, float*
  * padded, optional ReLU; the input is the channel concatenation of in0 (read through a nearest 2x
  * upsample from height/2 x width/2 when up0) and in1 (may be null, c1 = 0).  c0, c1 and cout are
  * multiples of 16 (c0 >= 16, cout <= 1024); width even (height too with up0); wpack is the output
- * of agb_pack_conv_weights; out (BF16) and out32 (FP32) may each be null.  Exported for the
- * denoiser's parity tests. */
+ * of agb_pack_conv_weights; out (BF16) and out32 (FP32) may each be null; inputs 16-byte and
+ * outputs 32-byte aligned.  Exported for the denoiser's parity tests. */
 AGB_API agb_status agb_conv3x3_bf16(const uint16_t* in0, const uint16_t* in1, const uint16_t* wpack,
     const float* bias, uint16_t* out, float* out32, int32_t batch, int32_t height, int32_t width,
     int32_t c0, int32_t c1, int32_t cout, int32_t up0, int32_t relu, void* cuda_stream);
