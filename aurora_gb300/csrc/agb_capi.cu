@@ -2168,11 +2168,11 @@ static agb_status convCommon(const char* what, const uint16_t* in0, const uint16
     if (int64_t(batch) * height * width >= (int64_t(1) << 31) / 128)
         return fail(AGB_ERR_LIMIT, std::string(what) + ": too many pixels");
     uintptr_t al = reinterpret_cast<uintptr_t>(in0) | reinterpret_cast<uintptr_t>(in1) |
-        reinterpret_cast<uintptr_t>(wpack);
+        reinterpret_cast<uintptr_t>(wpack) | reinterpret_cast<uintptr_t>(bias);
     uintptr_t alOut = reinterpret_cast<uintptr_t>(out) | reinterpret_cast<uintptr_t>(out32) |
         reinterpret_cast<uintptr_t>(pool);
     if ((al & 15u) || (alOut & 31u))
-        return fail(AGB_ERR_INVALID_ARG, std::string(what) + ": inputs must be 16-byte and outputs 32-byte aligned");
+        return fail(AGB_ERR_INVALID_ARG, std::string(what) + ": inputs and bias must be 16-byte and outputs 32-byte aligned");
     cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
     ConvLaunch c{ in0, c1 > 0 ? in1 : nullptr, wpack, bias, out, out32, batch, height, width, c0, c1, cout,
         up0 ? 1 : 0, relu ? 1 : 0 };
@@ -2212,8 +2212,8 @@ AGB_API agb_status agb_conv3x3_wgrad_bf16(const uint16_t* in0, const uint16_t* i
         return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_wgrad_bf16: null input or empty image");
     if (c0 < 16 || c0 % 16 || c1 < 0 || c1 % 16 || cout < 16 || cout > 256 || cout % 16 || c0 + c1 > 1024)
         return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_wgrad_bf16: channel counts must be multiples of 16, cout <= 256");
-    if (up0 && (height % 2 || width % 2))
-        return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_wgrad_bf16: upsampled input needs even sizes");
+    if (width % 2 || (up0 && height % 2))
+        return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_wgrad_bf16: the width must be even (the height too with an upsampled input)");
     uintptr_t al = reinterpret_cast<uintptr_t>(in0) | reinterpret_cast<uintptr_t>(in1) | reinterpret_cast<uintptr_t>(dy);
     if (al & 15u)
         return fail(AGB_ERR_INVALID_ARG, "agb_conv3x3_wgrad_bf16: pointers must be 16-byte aligned");
@@ -2363,7 +2363,7 @@ AGB_API agb_status agb_denoiser_forward(agb_denoiser* dn, const uint16_t* featur
         return st;
     if (!features || !out_rgba || ((reinterpret_cast<uintptr_t>(features) | reinterpret_cast<uintptr_t>(out_rgba)) & 15u))
         return fail(AGB_ERR_INVALID_ARG, "agb_denoiser_forward: null or unaligned device pointer");
-    AGB_CUDA(dn->net.forward(features, batch, height, width, false, out_rgba), "agb_denoiser_forward");
+    AGB_CUDA(dn->net.infer(features, batch, height, width, out_rgba), "agb_denoiser_forward");
     AGB_CUDA(cudaStreamSynchronize(dn->stream), "agb_denoiser_forward");
     return tcStatus("agb_denoiser_forward");
 }

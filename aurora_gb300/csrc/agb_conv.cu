@@ -111,7 +111,6 @@ __device__ __forceinline__ void st256(void* p, const uint32_t (&w)[8])
 }
 
 __device__ __forceinline__ float bfv(uint16_t b) { return __uint_as_float(uint32_t(b) << 16); }
-__device__ __forceinline__ uint16_t tobf(float v) { return __bfloat16_as_ushort(__float2bfloat16_rn(v)); }
 
 // Output rows per tile for N output channels: as many as one TMEM buffer of 256 columns holds
 // (2 R N), at most 4.
@@ -354,9 +353,25 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_consta
                 }
                 tc::tmemWaitLoad();
                 float bv[16];
+                if (a.bias)
+                {
+                    const float4* bp = reinterpret_cast<const float4*>(a.bias + cb + c0);
 #pragma unroll
-                for (int i = 0; i < 16; i++)
-                    bv[i] = a.bias ? __ldg(a.bias + cb + c0 + i) : 0.f;
+                    for (int i = 0; i < 4; i++)
+                    {
+                        const float4 t4 = __ldg(bp + i);
+                        bv[4 * i]       = t4.x;
+                        bv[4 * i + 1]   = t4.y;
+                        bv[4 * i + 2]   = t4.z;
+                        bv[4 * i + 3]   = t4.w;
+                    }
+                }
+                else
+                {
+#pragma unroll
+                    for (int i = 0; i < 16; i++)
+                        bv[i] = 0.f;
+                }
                 float psum[16];
 #pragma unroll
                 for (int acc = 0; acc < 4; acc++)
@@ -366,25 +381,25 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_consta
                     const int par = acc & 1;
                     const int y   = q.y0 + r + (acc >> 1);
                     float f[16];
-                    uint16_t h[16];
 #pragma unroll
                     for (int i = 0; i < 16; i++)
                     {
                         f[i] = __uint_as_float(v[acc][i]) + bv[i];
                         if (a.relu)
                             f[i] = fmaxf(f[i], 0.f);
-                        h[i] = tobf(f[i]);
+                    }
+                    // BF16 pairs, round to nearest even (low half = the even channel).
+                    uint32_t w[8];
+#pragma unroll
+                    for (int i = 0; i < 8; i++)
+                    {
+                        const __nv_bfloat162 h2 = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
+                        w[i]                    = *reinterpret_cast<const uint32_t*>(&h2);
                     }
                     const bool st   = colOk && y < a.H;
                     const size_t px = (size_t(q.b) * a.H + y) * a.W + 2 * j + par;
                     if (st && a.out)
-                    {
-                        uint32_t w[8];
-#pragma unroll
-                        for (int i = 0; i < 8; i++)
-                            w[i] = uint32_t(h[2 * i]) | (uint32_t(h[2 * i + 1]) << 16);
                         st256(a.out + px * a.Cout + cb + c0, w);
-                    }
                     if (st && a.out32)
                     {
                         uint32_t w0[8], w1[8];
@@ -404,17 +419,27 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_consta
                             fmaxf(expm1f(f[1] + bfv(__ldg(xin + 1))), 0.f), fmaxf(expm1f(f[2] + bfv(__ldg(xin + 2))), 0.f),
                             1.f);
                     }
-                    // ((x00 + x01) + x10) + x11 over the stored BF16 values.
+                    if (step == 2)
+                    {
+                        // ((x00 + x01) + x10) + x11 over the stored BF16 values.
 #pragma unroll
-                    for (int i = 0; i < 16; i++)
-                        psum[i] = acc == 0 ? bfv(h[i]) : psum[i] + bfv(h[i]);
+                        for (int i = 0; i < 8; i++)
+                        {
+                            const float lo = __uint_as_float(w[i] << 16), hi = __uint_as_float(w[i] & 0xFFFF0000u);
+                            psum[2 * i]     = acc == 0 ? lo : psum[2 * i] + lo;
+                            psum[2 * i + 1] = acc == 0 ? hi : psum[2 * i + 1] + hi;
+                        }
+                    }
                 }
                 if (step == 2 && colOk && q.y0 + r + 1 < a.H)
                 {
                     uint32_t w[8];
 #pragma unroll
                     for (int i = 0; i < 8; i++)
-                        w[i] = uint32_t(tobf(psum[2 * i] * 0.25f)) | (uint32_t(tobf(psum[2 * i + 1] * 0.25f)) << 16);
+                    {
+                        const __nv_bfloat162 h2 = __floats2bfloat162_rn(psum[2 * i] * 0.25f, psum[2 * i + 1] * 0.25f);
+                        w[i]                    = *reinterpret_cast<const uint32_t*>(&h2);
+                    }
                     const size_t pp = (size_t(q.b) * (a.H >> 1) + ((q.y0 + r) >> 1)) * W2 + j;
                     st256(a.pool + pp * a.Cout + cb + c0, w);
                 }
@@ -430,6 +455,231 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_consta
     tc::fenceAfterSync();
     if (warp == 1)
         tc::tmemDealloc(tmem, 2 * kAccStride);
+    if (!ok)
+        atomicExch(a.error, 1);
+}
+
+// ----------------------------------------------------------------------------- weight gradient
+// dW[tap][ci][co] += sum over pixels p of X[p + d(tap)][ci] dY[p][co], X = concat(up?(in0), in1):
+// a tcgen05 GEMM with M = input channels, N = output channels and K = pixels, both operands
+// MN-major (NHWC keeps a pixel's channels contiguous).  A unit of K is 128 output pixels of one
+// row (64 pairs), split by parity as in the forward pass: dY is staged as its even and odd rows
+// (64 entries each), X as the even and odd halo rows of 66 entries, so that the horizontal taps
+// are K offsets of 0, 1 or 2 entries into the same staged rows (an upsampled source is staged at
+// half resolution, the same row in both slots).  The vertical taps: when 3 x Cin <= 128 the M
+// rows are (dy, ci) - the three halo rows' channel groups are stacked at a uniform stride, so one
+// MMA covers all nine taps' rows for its horizontal tap - otherwise a work item takes one dy and
+// 128 input channels.  Accumulators: the three horizontal taps x N columns in TMEM, summed over
+// the item's units, then added to dW with vector reductions (red.global.add.v4.f32).
+constexpr uint32_t kWgEntriesA = 66;   // 64 pairs + offsets 0..2
+constexpr uint32_t kWgEntriesB = 64;
+constexpr uint32_t kWgSlotA    = 2304; // 66 x 32 bytes rounded up to the 256-byte swizzle atom
+constexpr uint32_t kWgSlotB    = 2048; // 64 x 32 bytes
+constexpr int kWgThreads       = 192;  // producer, MMA issuer, 4 epilogue warps
+constexpr int kWgMaxStages     = 6;
+
+struct WgradTmaArgs
+{
+    float* dw;
+    int B, H, W, Cin, Cout, C0, up0;
+    int T;               // vertical taps per item: 3 (M = (dy, ci)) or 1 (M = ci)
+    int Gci;             // 16-channel groups of X per tap in an item
+    int ciTiles, coTiles, N, splits;
+    int unitsX, numUnits, unitsPerItem, numItems;
+    uint32_t stageBytes, aBytes;
+    int stages;
+    int* error;
+};
+
+template <int N>
+__global__ void __launch_bounds__(kWgThreads, 1) k_conv_wgrad_tma(const __grid_constant__ CUtensorMap tm0,
+    const __grid_constant__ CUtensorMap tm1, const __grid_constant__ CUtensorMap tmDy, const WgradTmaArgs a)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t full[kWgMaxStages], empty[kWgMaxStages], accFull;
+    __shared__ uint32_t tmemBase;
+    const int tid  = threadIdx.x;
+    const int warp = tid >> 5;
+    const int lane = tid & 31;
+    const int S    = a.stages;
+    // Item: (dy or all three, ci tile, co tile, unit range).
+    int item      = blockIdx.x;
+    const int sp  = item % a.splits;
+    item /= a.splits;
+    const int coT = item % a.coTiles;
+    item /= a.coTiles;
+    const int ciT  = item % a.ciTiles;
+    const int dyIt = item / a.ciTiles; // the item's dy when T == 1
+    const int u0   = sp * a.unitsPerItem;
+    const int u1   = min(a.numUnits, u0 + a.unitsPerItem);
+
+    if (warp == 1)
+        tc::tmemAlloc(&tmemBase, 512);
+    if (tid == 0)
+    {
+        for (int s = 0; s < S; s++)
+        {
+            tc::mbarInit(&full[s], 1);
+            tc::mbarInit(&empty[s], 1);
+        }
+        tc::mbarInit(&accFull, 1);
+        tc::fenceMbarInit();
+    }
+    tc::fenceBeforeSync();
+    __syncthreads();
+    tc::fenceAfterSync();
+    const uint32_t tmem = tmemBase;
+    bool ok             = true;
+
+    if (warp == 0)
+    {
+        if (lane == 0)
+        {
+            uint32_t lastParity[kWgMaxStages];
+            bool issued[kWgMaxStages];
+            for (int s = 0; s < S; s++)
+                issued[s] = false;
+            const uint32_t bytesA = uint32_t(a.T * a.Gci) * 2u * kWgEntriesA * 32u;
+            const uint32_t bytesB = uint32_t(N / 16) * 2u * kWgEntriesB * 32u;
+            uint32_t it = 0;
+            for (int u = u0; u < u1; u++, it++)
+            {
+                const int s       = int(it % uint32_t(S));
+                const uint32_t ph = (it / uint32_t(S)) & 1u;
+                if (!tc::mbarWait(&empty[s], ph ^ 1u))
+                {
+                    ok = false;
+                    break;
+                }
+                const int xs = u % a.unitsX;
+                const int r  = u / a.unitsX;
+                const int y  = r % a.H;
+                const int b  = r / a.H;
+                const int j0 = xs * 64;
+                uint8_t* A   = smem + size_t(s) * a.stageBytes;
+                uint8_t* Bm  = A + a.aBytes;
+                tc::mbarExpectTx(&full[s], bytesA + bytesB);
+                // X: slot (parity p, tap row t, group g) at ((p * 8) + t * Gci + g) * kWgSlotA.
+                for (int t = 0; t < a.T; t++)
+                {
+                    const int dy = a.T == 3 ? t : dyIt;
+                    const int yi = y + dy - 1;
+                    for (int g = 0; g < a.Gci; g++)
+                    {
+                        const int c = (a.T == 3 ? 0 : ciT * 128) + g * 16;
+                        for (int p = 0; p < 2; p++)
+                        {
+                            uint8_t* dst = A + (p * 8 + t * a.Gci + g) * kWgSlotA;
+                            if (c < a.C0 && a.up0)
+                                tc::tensorLoad4(dst, &tm0, c, j0 - 1, yi >> 1, b, &full[s]);
+                            else if (c < a.C0)
+                                tc::tensorLoad5(dst, &tm0, c, p, j0 - 1, yi, b, &full[s]);
+                            else
+                                tc::tensorLoad5(dst, &tm1, c - a.C0, p, j0 - 1, yi, b, &full[s]);
+                        }
+                    }
+                }
+                // dY: slot (parity p, group g) at (p * N / 16 + g) * kWgSlotB.
+                for (int g = 0; g < N / 16; g++)
+                    for (int p = 0; p < 2; p++)
+                        tc::tensorLoad5(Bm + (p * (N / 16) + g) * kWgSlotB, &tmDy, coT * N + g * 16, p, j0, y, b,
+                            &full[s]);
+                issued[s]     = true;
+                lastParity[s] = ph;
+            }
+            for (int s = 0; s < S; s++)
+                if (issued[s] && !tc::mbarWait(&full[s], lastParity[s]))
+                    ok = false;
+        }
+        __syncwarp();
+    }
+    else if (warp == 1)
+    {
+        if (lane == 0)
+        {
+            // MN-major A and B (bits 15, 16), M = 128, N.
+            const uint32_t idesc = tc::idescBf16(128, N) | (1u << 15) | (1u << 16);
+            uint32_t it          = 0;
+            bool first           = true;
+            for (int u = u0; u < u1; u++, it++)
+            {
+                const int s       = int(it % uint32_t(S));
+                const uint32_t ph = (it / uint32_t(S)) & 1u;
+                if (!tc::mbarWait(&full[s], ph))
+                {
+                    ok = false;
+                    break;
+                }
+                tc::fenceAfterSync();
+                const uint32_t aAddr  = tc::smemAddr(smem + size_t(s) * a.stageBytes);
+                const uint32_t bAddr  = aAddr + a.aBytes;
+                // MN-major, 32-byte swizzle: 16-channel atoms a slot apart (leading byte offset), 8-entry
+                // atoms 256 bytes apart (stride byte offset).
+                const uint64_t aDesc0 = tc::smemDesc(aAddr, kWgSlotA, 256) | (uint64_t(6) << 61);
+                const uint64_t bDesc0 = tc::smemDesc(bAddr, kWgSlotB, 256) | (uint64_t(6) << 61);
+#pragma unroll
+                for (int par = 0; par < 2; par++)
+#pragma unroll
+                    for (int dx = 0; dx < 3; dx++)
+                    {
+                        const uint32_t shift = par == 0 ? (dx == 0 ? 0u : 1u) : (dx == 2 ? 2u : 1u);
+                        const uint32_t odd   = par == 0 ? (dx == 1 ? 0u : 1u) : (dx == 1 ? 1u : 0u);
+                        const uint64_t ad    = aDesc0 + ((odd * 8u * kWgSlotA + shift * 32u) >> 4);
+                        const uint64_t bd    = bDesc0 + ((uint32_t(par) * (N / 16) * kWgSlotB) >> 4);
+#pragma unroll
+                        for (int ks = 0; ks < 4; ks++)
+                            tc::mma(tmem + uint32_t(dx * N), ad + ((uint32_t(ks) * 16u * 32u) >> 4),
+                                bd + ((uint32_t(ks) * 16u * 32u) >> 4), idesc,
+                                (first && par == 0 && ks == 0) ? 0u : 1u);
+                    }
+                first = false;
+                tc::commit(&empty[s]);
+            }
+            tc::commit(&accFull);
+            if (!tc::mbarWait(&accFull, 0))
+                ok = false;
+        }
+        __syncwarp();
+    }
+    else
+    {
+        // Epilogue (warps 2-5): TMEM lane m = the M row of this thread.
+        const int quad = warp & 3;
+        const int m    = quad * 32 + lane;
+        if (!leaderWait(&accFull, 0, lane))
+            ok = false;
+        else if (u1 > u0)
+        {
+            tc::fenceAfterSync();
+            const int rowsPerTap = a.Gci * 16;
+            const int t          = m / rowsPerTap;
+            const int dy         = a.T == 3 ? t : dyIt;
+            const int ci         = (a.T == 3 ? 0 : ciT * 128) + m % rowsPerTap;
+            const bool valid     = t < a.T && ci < a.Cin;
+            for (int dx = 0; dx < 3; dx++)
+                for (int c0 = 0; c0 < N; c0 += 16)
+                {
+                    uint32_t v[16];
+                    tc::tmemLoad16(tmem + (uint32_t(quad * 32) << 16) + uint32_t(dx * N + c0), v);
+                    tc::tmemWaitLoad();
+                    if (valid)
+                    {
+                        float* dst = a.dw + (size_t(dy * 3 + dx) * a.Cin + ci) * a.Cout + coT * N + c0;
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                            asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst + 4 * q),
+                                "f"(__uint_as_float(v[4 * q])), "f"(__uint_as_float(v[4 * q + 1])),
+                                "f"(__uint_as_float(v[4 * q + 2])), "f"(__uint_as_float(v[4 * q + 3]))
+                                         : "memory");
+                    }
+                }
+        }
+    }
+    tc::fenceBeforeSync();
+    __syncthreads();
+    tc::fenceAfterSync();
+    if (warp == 1)
+        tc::tmemDealloc(tmem, 512);
     if (!ok)
         atomicExch(a.error, 1);
 }
@@ -451,15 +701,16 @@ PFN_cuTensorMapEncodeTiled_v12000 encodeTiled()
     return fn;
 }
 
-// Even / odd view of a full-resolution NHWC BF16 tensor: (C, parity, W / 2, H, B), box 8 x 1 x 130.
-cudaError_t mapPairs(CUtensorMap* m, const uint16_t* base, int B, int H, int W, int C)
+// Even / odd view of a full-resolution NHWC BF16 tensor: (C, parity, W / 2, H, B), box 16 x 1 x
+// entries, 32-byte swizzle.
+cudaError_t mapPairs(CUtensorMap* m, const uint16_t* base, int B, int H, int W, int C, int entries = kHaloEntries)
 {
     auto enc = encodeTiled();
     if (!enc)
         return cudaErrorNotSupported;
     cuuint64_t dims[5]    = { cuuint64_t(C), 2, cuuint64_t(W / 2), cuuint64_t(H), cuuint64_t(B) };
     cuuint64_t strides[4] = { cuuint64_t(C) * 2, cuuint64_t(C) * 4, cuuint64_t(W) * C * 2, cuuint64_t(H) * W * C * 2 };
-    cuuint32_t box[5]     = { 16, 1, kHaloEntries, 1, 1 };
+    cuuint32_t box[5]     = { 16, 1, cuuint32_t(entries), 1, 1 };
     cuuint32_t es[5]      = { 1, 1, 1, 1, 1 };
     CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<uint16_t*>(base), dims, strides, box, es,
         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -467,15 +718,16 @@ cudaError_t mapPairs(CUtensorMap* m, const uint16_t* base, int B, int H, int W, 
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-// Plain view of a half-resolution NHWC BF16 tensor: (C, W0, H0, B), box 8 x 130.
-cudaError_t mapRows(CUtensorMap* m, const uint16_t* base, int B, int H0, int W0, int C)
+// Plain view of a half-resolution NHWC BF16 tensor: (C, W0, H0, B), box 16 x entries, 32-byte
+// swizzle.
+cudaError_t mapRows(CUtensorMap* m, const uint16_t* base, int B, int H0, int W0, int C, int entries = kHaloEntries)
 {
     auto enc = encodeTiled();
     if (!enc)
         return cudaErrorNotSupported;
     cuuint64_t dims[4]    = { cuuint64_t(C), cuuint64_t(W0), cuuint64_t(H0), cuuint64_t(B) };
     cuuint64_t strides[3] = { cuuint64_t(C) * 2, cuuint64_t(W0) * C * 2, cuuint64_t(H0) * W0 * C * 2 };
-    cuuint32_t box[4]     = { 16, kHaloEntries, 1, 1 };
+    cuuint32_t box[4]     = { 16, cuuint32_t(entries), 1, 1 };
     cuuint32_t es[4]      = { 1, 1, 1, 1 };
     CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<uint16_t*>(base), dims, strides, box, es,
         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -509,9 +761,10 @@ cudaError_t launchConv3x3(const ConvLaunch& c, cudaStream_t st)
 {
     if (c.W % 2 || (c.up0 && c.H % 2) || (c.pool && c.H % 2))
         return cudaErrorInvalidValue;
-    // Outputs are written in 32-byte pieces.
-    if ((reinterpret_cast<uintptr_t>(c.out) | reinterpret_cast<uintptr_t>(c.out32) | reinterpret_cast<uintptr_t>(c.pool)) &
-        31u)
+    // Outputs are written in 32-byte pieces, the bias read in 16-byte ones.
+    if (((reinterpret_cast<uintptr_t>(c.out) | reinterpret_cast<uintptr_t>(c.out32) | reinterpret_cast<uintptr_t>(c.pool)) &
+            31u) ||
+        (reinterpret_cast<uintptr_t>(c.bias) & 15u))
         return cudaErrorInvalidValue;
     ConvTmaArgs a{};
     a.wpack = c.wpack;
@@ -563,6 +816,57 @@ cudaError_t launchConv3x3(const ConvLaunch& c, cudaStream_t st)
         return e;
     const int grid = int(std::min<long>(tiles, smCountOf(dev)));
     kern<<<grid, kThreads, smem, st>>>(m0, m1, a);
+    return cudaGetLastError();
+}
+
+cudaError_t launchConvWgrad(const ConvLaunch& c, const uint16_t* dy, float* dw, int smCount, cudaStream_t st)
+{
+    if (c.W % 2 || (c.up0 && c.H % 2) || (reinterpret_cast<uintptr_t>(dw) & 15u))
+        return cudaErrorInvalidValue;
+    WgradTmaArgs a{};
+    a.dw = dw;
+    a.B = c.B, a.H = c.H, a.W = c.W, a.Cin = c.C0 + c.C1, a.Cout = c.Cout, a.C0 = c.C0, a.up0 = c.up0;
+    a.T       = 3 * a.Cin <= 128 ? 3 : 1;
+    a.Gci     = a.T == 3 ? a.Cin / 16 : std::min(8, a.Cin / 16);
+    a.ciTiles = a.T == 3 ? 1 : (a.Cin + 127) / 128;
+    a.N       = c.Cout <= 128 ? c.Cout : (c.Cout % 128 == 0 ? 128 : 64);
+    if (c.Cout % a.N || (a.N != 16 && a.N != 32 && a.N != 48 && a.N != 64 && a.N != 96 && a.N != 128))
+        return cudaErrorInvalidValue;
+    a.coTiles  = c.Cout / a.N;
+    a.unitsX   = (c.W / 2 + 63) / 64;
+    a.numUnits = c.B * c.H * a.unitsX;
+    const int fixedItems = (a.T == 3 ? 1 : 3) * a.ciTiles * a.coTiles;
+    const int sms        = smCount > 0 ? smCount : 148;
+    a.splits       = std::max(1, std::min(a.numUnits, (2 * sms + fixedItems - 1) / fixedItems));
+    a.unitsPerItem = (a.numUnits + a.splits - 1) / a.splits;
+    a.splits       = (a.numUnits + a.unitsPerItem - 1) / a.unitsPerItem;
+    a.numItems     = fixedItems * a.splits;
+    a.aBytes       = 2u * 8u * kWgSlotA; // all eight M atoms of both parities (unloaded ones unused)
+    a.stageBytes   = (a.aBytes + 2u * uint32_t(a.N / 16) * kWgSlotB + 1023u) & ~1023u;
+    a.stages       = int(std::min<size_t>(kWgMaxStages, kSmemBudget / a.stageBytes));
+    cudaError_t e  = tcErrorFlag(&a.error);
+    if (e != cudaSuccess)
+        return e;
+    CUtensorMap m0, m1, md;
+    e = c.up0 ? mapRows(&m0, c.in0, c.B, c.H / 2, c.W / 2, c.C0, kWgEntriesA)
+              : mapPairs(&m0, c.in0, c.B, c.H, c.W, c.C0, kWgEntriesA);
+    if (e != cudaSuccess)
+        return e;
+    if (c.C1 > 0)
+    {
+        if ((e = mapPairs(&m1, c.in1, c.B, c.H, c.W, c.C1, kWgEntriesA)) != cudaSuccess)
+            return e;
+    }
+    else
+        m1 = m0;
+    if ((e = mapPairs(&md, dy, c.B, c.H, c.W, c.Cout, kWgEntriesB)) != cudaSuccess)
+        return e;
+    const size_t smem = std::max<size_t>(size_t(a.stages) * a.stageBytes, 120 * 1024);
+    auto kern = a.N == 128 ? k_conv_wgrad_tma<128> : a.N == 96 ? k_conv_wgrad_tma<96> : a.N == 64 ? k_conv_wgrad_tma<64>
+        : a.N == 48 ? k_conv_wgrad_tma<48> : a.N == 32 ? k_conv_wgrad_tma<32> : k_conv_wgrad_tma<16>;
+    if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))) != cudaSuccess)
+        return e;
+    kern<<<a.numItems, kWgThreads, smem, st>>>(m0, m1, md, a);
     return cudaGetLastError();
 }
 

@@ -175,11 +175,12 @@ struct ConvLaunch
 // W even (and H even with up0 or pool), outputs 32-byte aligned; cudaErrorInvalidValue otherwise.
 cudaError_t launchConv3x3(const ConvLaunch& c, cudaStream_t st);
 cudaError_t launchPackConvWeights(const float* w, int Cin, int Cout, int flip, uint16_t* out, cudaStream_t st);
+// dW[tap][ci][co] += sum over pixels of X[p + d][ci] dY[p][co] (X as c.in0 / c.in1 / c.up0; c.Cout
+// the layer's output channels: up to 128, or a multiple of 64 / 128 beyond; W even).
+cudaError_t launchConvWgrad(const ConvLaunch& c, const uint16_t* dy, float* dw, int smCount, cudaStream_t st);
 
 // agb_denoise.cu
-// dW[tap][ci][co] += sum over pixels of X[p + d][ci] dY[p][co] (X as c.in0 / c.in1 / c.up0; c.Cout
-// the layer's output channels, at most 256).
-cudaError_t launchConvWgrad(const ConvLaunch& c, const uint16_t* dy, float* dw, int smCount, cudaStream_t st);
+
 cudaError_t launchTcGemm(const uint16_t* A, const uint16_t* B, float* D, int M, int N, int K, cudaStream_t st);
 // Reads and clears the tensor-core kernels' timeout flag (1 = a bounded wait ran out).
 cudaError_t takeTcError(int* flag);
@@ -198,6 +199,9 @@ public:
     // x: [B][H][W][16] BF16 features (H, W multiples of 8).  Keeps the activations for backward.
     // rgba (inference): the denoised RGBA radiance, written by the output layer's epilogue.
     cudaError_t forward(const uint16_t* x, int B, int H, int W, bool training, float* rgba = nullptr);
+    // Inference (forward with rgba) replayed from a CUDA graph of its 15 launches, captured on first
+    // use for each (x, rgba, B, H, W) and kept while the activation buffers stay (a few graphs).
+    cudaError_t infer(const uint16_t* x, int B, int H, int W, float* rgba);
     // After forward(training): L1 loss against target RGBA (FP32) and all parameter gradients.
     cudaError_t backward(const float* target);
     cudaError_t adam(float lr);
@@ -215,6 +219,7 @@ private:
     cudaError_t ensureShape(int B, int H, int W, bool training);
     static size_t pixels(int B, int H, int W, int level);
     ConvLaunch layerLaunch(int i, const uint16_t* x) const;
+    void dropGraphs();
 
     cudaStream_t stream_ = nullptr;
     int smCount_         = 0;
@@ -237,6 +242,15 @@ private:
     int B_ = 0, H_ = 0, W_ = 0;
     long step_ = 0;
     std::vector<void*> allocs_, shapeAllocs_;
+    struct Graph
+    {
+        const uint16_t* x = nullptr;
+        float* rgba       = nullptr;
+        int B = 0, H = 0, W = 0;
+        cudaGraphExec_t exec = nullptr;
+    };
+    std::vector<Graph> graphs_; // most recently used last
+    Graph pending_{};           // buffers seen once, captured when seen again
 };
 cudaError_t launchDenoiseFeatures(const float4* mean, const float2* moments, float samples, const float4* albedo,
     const float4* normal, const float* depth, float skyZ, long P, uint16_t* out, cudaStream_t st);

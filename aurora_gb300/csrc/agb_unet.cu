@@ -256,8 +256,17 @@ static int layerCout(int i) { return kLayerDefs[i].out >= 0 ? kActChannels[kLaye
 
 UnetDenoiser::~UnetDenoiser() { release(); }
 
+void UnetDenoiser::dropGraphs()
+{
+    for (Graph& g : graphs_)
+        cudaGraphExecDestroy(g.exec);
+    graphs_.clear();
+    pending_ = Graph{};
+}
+
 void UnetDenoiser::release()
 {
+    dropGraphs();
     for (void* p : allocs_)
         cudaFree(p);
     allocs_.clear();
@@ -348,6 +357,7 @@ cudaError_t UnetDenoiser::ensureShape(int B, int H, int W, bool training)
 {
     if (B == B_ && H == H_ && W == W_ && (!training || grad_[A_E0A]))
         return cudaSuccess;
+    dropGraphs(); // they name the buffers freed here
     for (void* p : shapeAllocs_)
         cudaFree(p);
     shapeAllocs_.clear();
@@ -439,6 +449,54 @@ cudaError_t UnetDenoiser::forward(const uint16_t* x, int B, int H, int W, bool t
             return e;
     }
     return cudaSuccess;
+}
+
+cudaError_t UnetDenoiser::infer(const uint16_t* x, int B, int H, int W, float* rgba)
+{
+    cudaError_t e = ensureShape(B, H, W, false);
+    if (e != cudaSuccess)
+        return e;
+    for (size_t i = 0; i < graphs_.size(); i++)
+    {
+        Graph g = graphs_[i];
+        if (g.x == x && g.rgba == rgba && g.B == B && g.H == H && g.W == W)
+        {
+            graphs_.erase(graphs_.begin() + long(i));
+            graphs_.push_back(g);
+            input_ = x;
+            return cudaGraphLaunch(g.exec, stream_);
+        }
+    }
+    // The first call with these buffers runs directly (it also loads and configures the kernels);
+    // the second captures.  Capture on this thread only: other threads keep using their streams.
+    if (!(pending_.x == x && pending_.rgba == rgba && pending_.B == B && pending_.H == H && pending_.W == W))
+    {
+        pending_ = Graph{ x, rgba, B, H, W, nullptr };
+        return forward(x, B, H, W, false, rgba);
+    }
+    if ((e = cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+        return e;
+    cudaError_t fe = forward(x, B, H, W, false, rgba);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(stream_, &graph);
+    if (fe != cudaSuccess || e != cudaSuccess)
+    {
+        if (graph)
+            cudaGraphDestroy(graph);
+        return fe != cudaSuccess ? fe : e;
+    }
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess)
+        return e;
+    if (graphs_.size() >= 8)
+    {
+        cudaGraphExecDestroy(graphs_.front().exec);
+        graphs_.erase(graphs_.begin());
+    }
+    graphs_.push_back(Graph{ x, rgba, B, H, W, exec });
+    return cudaGraphLaunch(exec, stream_);
 }
 
 cudaError_t UnetDenoiser::backward(const float* target)

@@ -550,7 +550,7 @@ AGB_API agb_status agb_conv3x3_bf16(const uint16_t* in0, const uint16_t* in1, co
 AGB_API agb_status agb_conv3x3_pool_bf16(const uint16_t* in0, const uint16_t* in1, const uint16_t* wpack,
     const float* bias, uint16_t* out, uint16_t* pool, int32_t batch, int32_t height, int32_t width,
     int32_t c0, int32_t c1, int32_t cout, int32_t up0, int32_t relu, void* cuda_stream);
-/* Weight gradient of agb_conv3x3_bf16 (same input arguments, cout <= 256): adds
+/* Weight gradient of agb_conv3x3_bf16 (same input arguments, cout <= 256, width even): adds
  * dw[tap][cin][cout] += sum over pixels of in[p + d(tap)][cin] * dy[p][cout] into the FP32 array dw. */
 AGB_API agb_status agb_conv3x3_wgrad_bf16(const uint16_t* in0, const uint16_t* in1, const uint16_t* dy,
     float* dw, int32_t batch, int32_t height, int32_t width, int32_t c0, int32_t c1, int32_t cout,
