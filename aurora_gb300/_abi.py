@@ -67,6 +67,18 @@ MATERIAL_DTYPE = np.dtype([
 assert MATERIAL_DTYPE.itemsize == 400
 
 MATERIAL_TEXTURES_DTYPE = np.dtype([_i("image", 5)])
+# agb_graph_op: a material node-graph program operation (operation codes GOP_*, inputs GIN_*,
+# outputs GOUT_*, as include/agb.h numbers them).
+GRAPH_OP_DTYPE = np.dtype([("op", "u1"), ("dst", "u1"), ("a", "u1"), ("b", "u1"), ("c", "u1"), ("d", "u1"),
+                           ("imm", "<u2")])
+GRAPH_REGS = 32
+(GOP_CONST, GOP_INPUT, GOP_ADD, GOP_SUB, GOP_MUL, GOP_DIV, GOP_MIN, GOP_MAX, GOP_POW, GOP_MOD, GOP_FLOOR,
+ GOP_CEIL, GOP_ABS, GOP_SIN, GOP_COS, GOP_SQRT, GOP_SIGN, GOP_CLAMP, GOP_MIX, GOP_DOT, GOP_NORMALIZE,
+ GOP_LENGTH, GOP_SWIZZLE, GOP_COMBINE, GOP_SELECT, GOP_IMAGE, GOP_NORMALMAP, GOP_OUTPUT) = range(28)
+(GIN_TEXCOORD, GIN_POSITION_WORLD, GIN_POSITION_OBJECT, GIN_NORMAL_WORLD, GIN_NORMAL_OBJECT,
+ GIN_TANGENT_WORLD, GIN_BITANGENT_WORLD) = range(7)
+(GOUT_BASE_COLOR, GOUT_SPECULAR_ROUGHNESS, GOUT_COAT_ROUGHNESS, GOUT_EMISSION_COLOR, GOUT_OPACITY,
+ GOUT_NORMAL) = range(6)
 
 DISTANT_LIGHT_DTYPE = np.dtype([_f("color_and_intensity", 4), _f("direction", 3), _f("cos_radius")])
 
@@ -206,6 +218,7 @@ SIGNATURES = {
     "agb_tlas_read": (_I32, [_P, _P, _U64, _P, _U64, ctypes.POINTER(_I32), ctypes.POINTER(_I32),
                              ctypes.POINTER(_U32)]),
     "agb_materials_set": (_I32, [_P, _P, _P, _U32]),
+    "agb_material_graphs_set": (_I32, [_P, _P, _P, _U32, _P, _U32, _P, _U32]),
     "agb_instances_set": (_I32, [_P, _P, _U32]),
     "agb_environment_set": (_I32, [_P, _P, _I32, _I32]),
     "agb_ground_plane_set": (_I32, [_P, _P]),

@@ -72,6 +72,16 @@ class Renderer:
         mats = np.ascontiguousarray(s.materials)
         tex = None if s.textures is None else np.ascontiguousarray(s.textures)
         check(lib.agb_materials_set(self.ctx, ptr(mats), ptr(tex), len(mats)))
+        g = getattr(s, "graphs", None)
+        if g is not None:
+            first = np.ascontiguousarray(g["first"], np.int32)
+            count = np.ascontiguousarray(g["count"], np.int32)
+            ops = np.ascontiguousarray(g["ops"], _abi.GRAPH_OP_DTYPE).copy()
+            img_op = ops["op"] == _abi.GOP_IMAGE
+            ops["imm"][img_op] = np.asarray(imgs, np.uint16)[ops["imm"][img_op]] if img_op.any() else 0
+            consts = np.ascontiguousarray(g["consts"], np.float32).reshape(-1, 4)
+            check(lib.agb_material_graphs_set(self.ctx, ptr(first), ptr(count), len(first), ptr(ops), len(ops),
+                                              ptr(consts), len(consts)))
         insts = (_abi.Instance * len(s.instances))()
         layer_arrays = []
         for k, inst in enumerate(s.instances):

@@ -606,18 +606,31 @@ public:
         std::vector<agb_material_textures> texs(1);
         std::map<Path, int32_t> matIndex;
         bool anyTexture = false;
+        // Node-graph programs of MaterialX materials, gathered into one operation / constant table.
+        std::vector<int32_t> graphFirst(1, 0), graphCount(1, 0);
+        std::vector<agb_graph_op> graphOps;
+        std::vector<float> graphConsts;
         for (auto& kv : materials)
         {
             agb_material m = defaultMaterial();
             agb_material_textures t;
             for (int k = 0; k < AGB_TEX_SLOTS; k++)
                 t.image[k] = -1;
+            int32_t gFirst = int32_t(graphOps.size()), gCount = 0;
             for (auto& p : kv.second)
             {
+                if (p.first == "materialx_graph")
+                {
+                    if (auto* prog = std::get_if<Strings>(&p.second))
+                        gCount = appendGraph(*prog, kv.first, graphOps, graphConsts);
+                    continue;
+                }
                 if (applyTextureProperty(m, t, p.first, p.second, kv.first, kv.second))
                     continue;
                 applyMaterialProperty(m, p.first, p.second, kv.first);
             }
+            graphFirst.push_back(gCount ? gFirst : 0);
+            graphCount.push_back(gCount);
             for (int k = 0; k < AGB_TEX_SLOTS; k++)
                 anyTexture = anyTexture || t.image[k] >= 0;
             matIndex[kv.first] = int32_t(mats.size());
@@ -628,6 +641,10 @@ public:
             texs[0].image[k] = -1;
         check(agb_materials_set(ctx, mats.data(), anyTexture ? texs.data() : nullptr, uint32_t(mats.size())),
             "upload materials");
+        if (!graphOps.empty())
+            check(agb_material_graphs_set(ctx, graphFirst.data(), graphCount.data(), uint32_t(mats.size()),
+                      graphOps.data(), uint32_t(graphOps.size()), graphConsts.data(), uint32_t(graphConsts.size() / 4)),
+                "upload material graphs");
         std::vector<agb_instance> insts;
         for (auto& kv : instances)
         {
@@ -813,6 +830,70 @@ public:
     // material's own (HGISampler.cpp:21-41; HGIScene.cpp:249-251, 512); an 8-bit image with
     // `linearize` set is decoded from sRGB to linear values first, as an sRGB texture format
     // decodes it.
+    // Appends a MaterialX material's node-graph program (the `materialx_graph` property: "op",
+    // "const" and "image" lines, indices local to the program) to the scene's tables, constant and
+    // image indices rebased; returns its operation count (0 when it cannot be read).
+    int32_t appendGraph(const Strings& prog, const Path& material, std::vector<agb_graph_op>& ops,
+        std::vector<float>& consts)
+    {
+        std::vector<agb_graph_op> local;
+        std::vector<float> k;
+        std::vector<int32_t> imageHandles;
+        try
+        {
+            for (const std::string& line : prog)
+            {
+                if (line.compare(0, 3, "op ") == 0)
+                {
+                    int v[7];
+                    if (std::sscanf(line.c_str() + 3, "%d %d %d %d %d %d %d", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5],
+                            &v[6]) != 7)
+                        throw Error("bad operation '" + line + "'");
+                    agb_graph_op o;
+                    o.op  = uint8_t(v[0]);
+                    o.dst = uint8_t(v[1]);
+                    o.a   = uint8_t(v[2]);
+                    o.b   = uint8_t(v[3]);
+                    o.c   = uint8_t(v[4]);
+                    o.d   = uint8_t(v[5]);
+                    o.imm = uint16_t(v[6]);
+                    local.push_back(o);
+                }
+                else if (line.compare(0, 6, "const ") == 0)
+                {
+                    float f[4];
+                    if (std::sscanf(line.c_str() + 6, "%g %g %g %g", &f[0], &f[1], &f[2], &f[3]) != 4)
+                        throw Error("bad constant '" + line + "'");
+                    k.insert(k.end(), f, f + 4);
+                }
+                else if (line.compare(0, 6, "image ") == 0)
+                {
+                    std::string path   = line.substr(6);
+                    const bool nearest = path.size() > 8 && path.compare(path.size() - 8, 8, ":nearest") == 0;
+                    if (nearest)
+                        path.resize(path.size() - 8);
+                    imageHandles.push_back(textureHandle(path, !nearest));
+                }
+            }
+        }
+        catch (const Error& e)
+        {
+            logError("material " + material + ": node graph not used: " + e.what());
+            return 0;
+        }
+        const uint16_t kBase = uint16_t(consts.size() / 4);
+        for (agb_graph_op o : local)
+        {
+            if (o.op == AGB_GOP_CONST)
+                o.imm = uint16_t(o.imm + kBase);
+            else if (o.op == AGB_GOP_IMAGE)
+                o.imm = o.imm < imageHandles.size() ? uint16_t(imageHandles[o.imm]) : uint16_t(0xFFFF);
+            ops.push_back(o);
+        }
+        consts.insert(consts.end(), k.begin(), k.end());
+        return int32_t(local.size());
+    }
+
     int32_t textureHandle(const Path& path, bool bilinear)
     {
         auto it = images.find(path);

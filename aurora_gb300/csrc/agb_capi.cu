@@ -127,6 +127,8 @@ struct agb_context
     DevBuf materials, matTex;
     uint32_t materialCount = 0;
     bool hasMatTex         = false;
+    DevBuf matGraph, graphOps, graphConsts; // material node-graph programs
+    bool hasGraphs = false;
 
     DevBuf instances, tlasNodes, tlasOrder, layers;
     std::vector<std::unique_ptr<DevBuf>> layerUVs;
@@ -208,6 +210,9 @@ struct agb_context
         s.imageCount    = int32_t(images.size());
         s.images        = imageTable.as<DevImage>();
         s.layers        = layers.as<DevLayer>();
+        s.matGraph      = hasGraphs ? matGraph.as<int2>() : nullptr;
+        s.graphOps      = hasGraphs ? graphOps.as<agb_graph_op>() : nullptr;
+        s.graphConsts   = hasGraphs ? graphConsts.as<float4>() : nullptr;
         s.env           = env;
         s.envLight      = DevImage{};
         s.envBackground = DevImage{};
@@ -857,6 +862,74 @@ AGB_API agb_status agb_materials_set(agb_context* ctx, const agb_material* mater
         ctx->hostMatTex.assign(textures, textures + count);
     else
         ctx->hostMatTex.clear();
+    ctx->hasGraphs = false; // programs belong to the material table they were set for
+    return AGB_OK;
+}
+
+AGB_API agb_status agb_material_graphs_set(agb_context* ctx, const int32_t* first, const int32_t* count,
+    uint32_t material_count, const agb_graph_op* ops, uint32_t op_count, const float* constants,
+    uint32_t constant_count)
+{
+    if (ctx && !ctx->parent)
+        ctx->sceneVersion++;
+    if (ctx && ctx->parent)
+        return fail(AGB_ERR_INVALID_ARG, "agb_material_graphs_set: a view shares its parent's scene; change the parent");
+    if (!ctx || (material_count && (!first || !count)) || (op_count && !ops) || (constant_count && !constants))
+        return fail(AGB_ERR_INVALID_ARG, "agb_material_graphs_set: null argument");
+    if (material_count != ctx->materialCount)
+        return fail(AGB_ERR_INVALID_ARG, "agb_material_graphs_set: one (first, count) pair per material of the current table");
+    if (constant_count > 65536u)
+        return fail(AGB_ERR_LIMIT, "agb_material_graphs_set: at most 65536 constants");
+    bool any = false;
+    for (uint32_t m = 0; m < material_count; m++)
+    {
+        if (count[m] == 0)
+            continue;
+        if (count[m] < 0 || count[m] > AGB_GRAPH_MAX_OPS || first[m] < 0 || int64_t(first[m]) + count[m] > int64_t(op_count))
+            return fail(AGB_ERR_INVALID_ARG, "agb_material_graphs_set: program range of material " + std::to_string(m));
+        any = true;
+    }
+    const uint32_t images = uint32_t(ctx->images.size());
+    for (uint32_t k = 0; k < op_count; k++)
+    {
+        const agb_graph_op& o = ops[k];
+        bool ok = o.op < AGB_GOP_COUNT && o.dst < AGB_GRAPH_REGS && o.a < AGB_GRAPH_REGS && o.b < AGB_GRAPH_REGS &&
+            o.c < AGB_GRAPH_REGS && o.d < AGB_GRAPH_REGS;
+        if (ok && o.op == AGB_GOP_CONST)
+            ok = o.imm < constant_count;
+        if (ok && o.op == AGB_GOP_INPUT)
+            ok = o.imm < AGB_GIN_COUNT;
+        if (ok && o.op == AGB_GOP_IMAGE)
+            ok = o.imm < images;
+        if (ok && o.op == AGB_GOP_OUTPUT)
+            ok = o.imm < AGB_GOUT_COUNT;
+        if (ok && o.op == AGB_GOP_SELECT)
+            ok = o.imm <= 2;
+        if (ok && (o.op == AGB_GOP_DOT || o.op == AGB_GOP_NORMALIZE || o.op == AGB_GOP_LENGTH))
+            ok = o.d >= 1 && o.d <= 4;
+        if (!ok)
+            return fail(AGB_ERR_INVALID_ARG, "agb_material_graphs_set: invalid operation " + std::to_string(k));
+    }
+    agb_status st = setDevice(ctx);
+    if (st)
+        return st;
+    if (!any)
+    {
+        ctx->hasGraphs = false;
+        return AGB_OK;
+    }
+    std::vector<int2> table(material_count);
+    for (uint32_t m = 0; m < material_count; m++)
+        table[m] = make_int2(first[m], count[m]);
+    std::vector<float> k4(size_t(std::max(constant_count, 1u)) * 4, 0.f);
+    if (constant_count)
+        std::memcpy(k4.data(), constants, size_t(constant_count) * 16);
+    if ((st = upload(ctx, ctx->matGraph, table.data(), table.size() * sizeof(int2), "upload material graphs")) ||
+        (st = upload(ctx, ctx->graphOps, ops, size_t(op_count) * sizeof(agb_graph_op), "upload material graphs")) ||
+        (st = upload(ctx, ctx->graphConsts, k4.data(), k4.size() * sizeof(float), "upload material graphs")))
+        return st;
+    AGB_CUDA(cudaStreamSynchronize(ctx->stream), "upload material graphs");
+    ctx->hasGraphs = true;
     return AGB_OK;
 }
 
@@ -1442,6 +1515,8 @@ agb_status buildSharedScenes(agb_batch* b, const std::vector<agb_context*>& scen
     {
         if (sc->ground.enabled)
             return fail(AGB_ERR_INVALID_ARG, "agb_batch_render: scenes with a ground plane render alone");
+        if (sc->hasGraphs)
+            return fail(AGB_ERR_INVALID_ARG, "agb_batch_render: scenes with material node graphs render alone");
         if (sc->hostMaterials.size() != sc->materialCount || sc->hostInstances.size() != sc->instanceCount)
             return fail(AGB_ERR_NOT_READY, "agb_batch_render: a scene has no materials or instances set");
         const uint32_t meshOff = uint32_t(M.size()), instOff = uint32_t(I.size()), layerOff = uint32_t(L.size());

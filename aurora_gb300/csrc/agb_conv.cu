@@ -54,7 +54,7 @@ constexpr uint32_t kRowBytes    = 4352;              // kBoxBytes rounded up to 
 constexpr int kThreads          = 320; // producer, MMA issuer, 8 epilogue warps
 constexpr uint32_t kAccStride   = 256;               // TMEM columns per accumulator buffer
 constexpr int kMaxStages        = 4;
-constexpr size_t kSmemBudget    = 220 * 1024;
+constexpr size_t kSmemBudget    = 226 * 1024; // of the 227 KB a CTA may have, static shared memory aside
 
 struct ConvTmaArgs
 {
@@ -66,6 +66,9 @@ struct ConvTmaArgs
     float4* rad;           // [B][H][W] RGBA radiance or null (the denoiser's output layer)
     const uint16_t* radIn; // [B][H][W][16] features (log1p noisy radiance in channels 0-2)
     int* error;            // set to 1 when a bounded wait runs out
+    float* g0;             // data-gradient split (see ConvLaunch)
+    float* g1;
+    int gC0, gUp;
     int B, H, W, Cout, up0, relu;
     int N, nTiles, R, G, G0, stages;
     int tilesX, rowBlocks, numTiles;
@@ -102,6 +105,15 @@ __device__ __forceinline__ bool leaderWait(uint64_t* bar, uint32_t parity, int l
     return __shfl_sync(0xffffffffu, got, 0) != 0;
 }
 
+// Waits until the grid this one programmatically depends on has completed and its memory is
+// visible (returns at once when the launch had no programmatic dependency), then lets the next
+// grid in the stream begin its own prologue.
+__device__ __forceinline__ void gridDependencyWait()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // One 32-byte store (the address 32-byte aligned): a whole sector per lane.
 __device__ __forceinline__ void st256(void* p, const uint32_t (&w)[8])
 {
@@ -113,8 +125,8 @@ __device__ __forceinline__ void st256(void* p, const uint32_t (&w)[8])
 __device__ __forceinline__ float bfv(uint16_t b) { return __uint_as_float(uint32_t(b) << 16); }
 
 // Output rows per tile for N output channels: as many as one TMEM buffer of 256 columns holds
-// (2 R N), at most 4.
-__host__ __device__ constexpr int tileRows(int n) { return n >= 64 ? 2 : 4; }
+// (2 R N), even, at most 6.
+__host__ __device__ constexpr int tileRows(int n) { return n >= 64 ? 2 : n >= 32 ? 4 : 6; }
 
 // The MMAs of one pipeline stage (one 16-channel input group), fully unrolled.  Halo row i (input
 // row y0 - 1 + i) feeds output rows r = i - 2 .. i (those inside the tile) through the vertical taps
@@ -169,7 +181,7 @@ __device__ __forceinline__ void issueStage(uint32_t aAddr, uint32_t bAddr, uint3
     }
 }
 
-template <int N>
+template <int N, bool SPLIT>
 __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_constant__ CUtensorMap tm0,
     const __grid_constant__ CUtensorMap tm1, const ConvTmaArgs a)
 {
@@ -204,6 +216,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_consta
     tc::fenceAfterSync();
     const uint32_t tmem = tmemBase;
     bool ok             = true;
+    // Programmatic dependent launch: the prologue above may overlap the previous kernel's tail;
+    // everything below reads or writes memory that kernel may still touch.
+    gridDependencyWait();
 
     if (warp == 0)
     {
@@ -318,7 +333,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_consta
         const int half     = (warp - 2) >> 2;
         const int m        = quad * 32 + lane;
         const int W2       = a.W >> 1;
-        const int step     = a.pool ? 2 : 1;
+        // The data-gradient split is its own instantiation: the forward epilogue keeps its registers.
+        constexpr bool split = SPLIT;
+        // An item is a row pair x 16 channels: its four accumulators are loaded before one wait,
+        // and a pool or an upsample gradient finds its 2x2 blocks in them (R is even).
+        constexpr int step = 2;
         const int chunks   = N / 16;
         const int items    = (R / step) * chunks;
         int k              = 0;
@@ -346,11 +365,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_consta
                 // Accumulator (row r, parity p) at columns (p R + r) N.
                 tc::tmemLoad16(tBase + uint32_t(r * N + c0), v[0]);
                 tc::tmemLoad16(tBase + uint32_t((R + r) * N + c0), v[1]);
-                if (step == 2)
-                {
-                    tc::tmemLoad16(tBase + uint32_t((r + 1) * N + c0), v[2]);
-                    tc::tmemLoad16(tBase + uint32_t((R + r + 1) * N + c0), v[3]);
-                }
+                tc::tmemLoad16(tBase + uint32_t((r + 1) * N + c0), v[2]);
+                tc::tmemLoad16(tBase + uint32_t((R + r + 1) * N + c0), v[3]);
                 tc::tmemWaitLoad();
                 float bv[16];
                 if (a.bias)
@@ -372,7 +388,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_consta
                     for (int i = 0; i < 16; i++)
                         bv[i] = 0.f;
                 }
-                float psum[16];
+                float psum[16], gsum[16];
+                const int cch   = cb + c0; // output channel of the chunk
+                const bool toG0 = split && cch < a.gC0;
 #pragma unroll
                 for (int acc = 0; acc < 4; acc++)
                 {
@@ -419,7 +437,32 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_consta
                             fmaxf(expm1f(f[1] + bfv(__ldg(xin + 1))), 0.f), fmaxf(expm1f(f[2] + bfv(__ldg(xin + 2))), 0.f),
                             1.f);
                     }
-                    if (step == 2)
+                    if (split)
+                    {
+                        if (toG0 && a.gUp)
+                        {
+                            // 2x2 block sum ((x00 + x01) + x10) + x11, added below.
+#pragma unroll
+                            for (int i = 0; i < 16; i++)
+                                gsum[i] = acc == 0 ? f[i] : gsum[i] + f[i];
+                        }
+                        else if (st)
+                        {
+                            float* g   = toG0 ? a.g0 + px * a.gC0 + cch : a.g1 + px * (a.Cout - a.gC0) + (cch - a.gC0);
+                            float4* g4 = reinterpret_cast<float4*>(g);
+#pragma unroll
+                            for (int i = 0; i < 4; i++)
+                            {
+                                float4 o = g4[i];
+                                o.x += f[4 * i];
+                                o.y += f[4 * i + 1];
+                                o.z += f[4 * i + 2];
+                                o.w += f[4 * i + 3];
+                                g4[i] = o;
+                            }
+                        }
+                    }
+                    if (a.pool)
                     {
                         // ((x00 + x01) + x10) + x11 over the stored BF16 values.
 #pragma unroll
@@ -431,7 +474,22 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv3x3_tma(const __grid_consta
                         }
                     }
                 }
-                if (step == 2 && colOk && q.y0 + r + 1 < a.H)
+                if (split && toG0 && a.gUp && colOk && q.y0 + r + 1 < a.H)
+                {
+                    const size_t pp = (size_t(q.b) * (a.H >> 1) + ((q.y0 + r) >> 1)) * W2 + j;
+                    float4* g4      = reinterpret_cast<float4*>(a.g0 + pp * a.gC0 + cch);
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+                    {
+                        float4 o = g4[i];
+                        o.x += gsum[4 * i];
+                        o.y += gsum[4 * i + 1];
+                        o.z += gsum[4 * i + 2];
+                        o.w += gsum[4 * i + 3];
+                        g4[i] = o;
+                    }
+                }
+                if (a.pool && colOk && q.y0 + r + 1 < a.H)
                 {
                     uint32_t w[8];
 #pragma unroll
@@ -530,6 +588,9 @@ __global__ void __launch_bounds__(kWgThreads, 1) k_conv_wgrad_tma(const __grid_c
     tc::fenceAfterSync();
     const uint32_t tmem = tmemBase;
     bool ok             = true;
+    // Programmatic dependent launch: the prologue above may overlap the previous kernel's tail;
+    // everything below reads or writes memory that kernel may still touch.
+    gridDependencyWait();
 
     if (warp == 0)
     {
@@ -735,6 +796,25 @@ cudaError_t mapRows(CUtensorMap* m, const uint16_t* base, int B, int H0, int W0,
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+// Launch with programmatic stream serialisation: the kernel may start while the previous kernel
+// in the stream finishes (its prologue overlaps that kernel's last wave).
+template <typename... Args, typename... Params>
+cudaError_t launchOverlapped(void (*kern)(Params...), unsigned grid, unsigned block, size_t smem, cudaStream_t st,
+    Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim            = dim3(grid);
+    cfg.blockDim           = dim3(block);
+    cfg.dynamicSmemBytes   = smem;
+    cfg.stream             = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs                                          = attr;
+    cfg.numAttrs                                       = 1;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 int smCountOf(int dev)
 {
     static int counts[64] = {};
@@ -755,7 +835,7 @@ int smCountOf(int dev)
 // Output channels per tile: 64, 32 or 16, the widest that divides cout.  Narrow tiles keep two or
 // more output rows per tile (the halo rows are shared between them, the 2x2 pool needs both rows
 // of a pair) and move fewer weight bytes per MMA than 128-channel tiles would.
-int convTileChannels(int cout) { return cout % 64 == 0 ? 64 : cout % 32 == 0 ? 32 : 16; }
+__host__ __device__ int convTileChannels(int cout) { return cout % 64 == 0 ? 64 : cout % 32 == 0 ? 32 : 16; }
 
 cudaError_t launchConv3x3(const ConvLaunch& c, cudaStream_t st)
 {
@@ -774,6 +854,13 @@ cudaError_t launchConv3x3(const ConvLaunch& c, cudaStream_t st)
     a.pool  = c.pool;
     a.rad   = reinterpret_cast<float4*>(c.radiance);
     a.radIn = c.radianceInput;
+    a.g0    = c.grad0;
+    a.g1    = c.grad1;
+    a.gC0   = c.gradC0;
+    a.gUp   = c.gradUp;
+    if ((c.grad0 || c.grad1) && (c.gradC0 % 16 || (c.gradUp && c.H % 2) ||
+                                    ((reinterpret_cast<uintptr_t>(c.grad0) | reinterpret_cast<uintptr_t>(c.grad1)) & 15u)))
+        return cudaErrorInvalidValue;
     a.B = c.B, a.H = c.H, a.W = c.W, a.Cout = c.Cout, a.up0 = c.up0, a.relu = c.relu;
     a.N      = convTileChannels(c.Cout);
     a.nTiles = c.Cout / a.N;
@@ -808,15 +895,16 @@ cudaError_t launchConv3x3(const ConvLaunch& c, cudaStream_t st)
     // At least half of the SM's shared memory, so that one CTA (with all 512 TMEM columns) runs
     // per SM.
     const size_t smem = std::max<size_t>(size_t(a.stages) * a.stageBytes, 120 * 1024);
-    auto kern = a.N == 64 ? k_conv3x3_tma<64> : a.N == 32 ? k_conv3x3_tma<32> : k_conv3x3_tma<16>;
+    const bool split = c.grad0 || c.grad1;
+    auto kern        = split ? (a.N == 64 ? k_conv3x3_tma<64, true> : a.N == 32 ? k_conv3x3_tma<32, true> : k_conv3x3_tma<16, true>)
+                             : (a.N == 64 ? k_conv3x3_tma<64, false> : a.N == 32 ? k_conv3x3_tma<32, false> : k_conv3x3_tma<16, false>);
     if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))) != cudaSuccess)
         return e;
     int dev = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess)
         return e;
     const int grid = int(std::min<long>(tiles, smCountOf(dev)));
-    kern<<<grid, kThreads, smem, st>>>(m0, m1, a);
-    return cudaGetLastError();
+    return launchOverlapped(kern, unsigned(grid), kThreads, smem, st, m0, m1, a);
 }
 
 cudaError_t launchConvWgrad(const ConvLaunch& c, const uint16_t* dy, float* dw, int smCount, cudaStream_t st)
@@ -866,8 +954,7 @@ cudaError_t launchConvWgrad(const ConvLaunch& c, const uint16_t* dy, float* dw, 
         : a.N == 48 ? k_conv_wgrad_tma<48> : a.N == 32 ? k_conv_wgrad_tma<32> : k_conv_wgrad_tma<16>;
     if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))) != cudaSuccess)
         return e;
-    kern<<<a.numItems, kWgThreads, smem, st>>>(m0, m1, md, a);
-    return cudaGetLastError();
+    return launchOverlapped(kern, unsigned(a.numItems), kWgThreads, smem, st, m0, m1, md, a);
 }
 
 // Packs FP32 weights w[tap][ci][co] (9 x Cin x Cout) into the conv kernel's B layout (BF16): per
@@ -893,6 +980,64 @@ __global__ void k_pack_conv_weights(const float* w, int Cin, int Cout, int flip,
         const size_t off   = stack * 3 * nt * 16 + tc::sliceOffset(row, uint32_t(c % 16)) / 2;
         out[off]           = __bfloat16_as_ushort(__float2bfloat16_rn(v));
     }
+}
+
+struct PackJobs
+{
+    PackJob job[kMaxPackJobs];
+    long first[kMaxPackJobs + 1]; // element offsets of the jobs
+    int count;
+};
+
+// Position of element (tap, c, n) of a kCin x kCout layer in the packed B layout (tiles of nt).
+__device__ __forceinline__ size_t packedOffset(int kCin, int nt, int tap, int c, int n)
+{
+    const int G = kCin / 16, tile = n / nt, nn = n % nt;
+    const int dy = tap / 3, dx = tap % 3;
+    const size_t stack = (size_t(tile) * G + c / 16) * 3 + dx;
+    const uint32_t row = uint32_t((2 - dy) * nt + nn);
+    return stack * 3 * nt * 16 + tc::sliceOffset(row, uint32_t(c % 16)) / 2;
+}
+
+__global__ void k_pack_conv_weights_many(const PackJobs jobs)
+{
+    const long total = jobs.first[jobs.count];
+    for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < total; i += long(gridDim.x) * blockDim.x)
+    {
+        int k = 0;
+        while (i >= jobs.first[k + 1])
+            k++;
+        const PackJob& J = jobs.job[k];
+        const long e     = i - jobs.first[k]; // (tap, ci, co) in w's order
+        const int co     = int(e % J.cout);
+        const long kk    = e / J.cout;
+        const int tap = int(kk / J.cin), ci = int(kk % J.cin);
+        const uint16_t v = __bfloat16_as_ushort(__float2bfloat16_rn(J.w[e]));
+        if (J.out)
+            J.out[packedOffset(J.cin, convTileChannels(J.cout), tap, ci, co)] = v;
+        if (J.outFlip)
+            J.outFlip[packedOffset(J.cout, convTileChannels(J.cin), 8 - tap, co, ci)] = v;
+    }
+}
+
+cudaError_t launchPackConvWeightsMany(const PackJob* jobs, int count, cudaStream_t st)
+{
+    if (count < 0 || count > kMaxPackJobs)
+        return cudaErrorInvalidValue;
+    PackJobs p{};
+    p.count    = count;
+    p.first[0] = 0;
+    for (int k = 0; k < count; k++)
+    {
+        p.job[k]       = jobs[k];
+        p.first[k + 1] = p.first[k] + 9L * jobs[k].cin * jobs[k].cout;
+    }
+    const long total = p.first[count];
+    if (total == 0)
+        return cudaSuccess;
+    const unsigned grid = unsigned(std::min<long>((total + 255) / 256, 4096));
+    k_pack_conv_weights_many<<<grid, 256, 0, st>>>(p);
+    return cudaGetLastError();
 }
 
 cudaError_t launchPackConvWeights(const float* w, int Cin, int Cout, int flip, uint16_t* out, cudaStream_t st)

@@ -171,10 +171,28 @@ struct ConvLaunch
     // c = 0..2 (radianceInput: the BF16 features, 16 per pixel, log1p noisy radiance in 0..2).
     float* radiance                = nullptr;
     const uint16_t* radianceInput  = nullptr;
+    // Data-gradient split (the FP32 result is added, not stored): output channels [0, gradC0) go
+    // to grad0 - summed over 2x2 blocks into half resolution when gradUp (the gradient of a
+    // nearest upsample) -, channels [gradC0, Cout) to grad1 at full resolution.
+    float* grad0 = nullptr;
+    float* grad1 = nullptr;
+    int gradC0   = 0;
+    int gradUp   = 0;
 };
 // W even (and H even with up0 or pool), outputs 32-byte aligned; cudaErrorInvalidValue otherwise.
 cudaError_t launchConv3x3(const ConvLaunch& c, cudaStream_t st);
 cudaError_t launchPackConvWeights(const float* w, int Cin, int Cout, int flip, uint16_t* out, cudaStream_t st);
+// Packs several layers' weights in one launch, each both ways (forward into out, data-gradient
+// into outFlip; either may be null).
+struct PackJob
+{
+    const float* w;
+    uint16_t* out;
+    uint16_t* outFlip;
+    int cin, cout;
+};
+constexpr int kMaxPackJobs = 16;
+cudaError_t launchPackConvWeightsMany(const PackJob* jobs, int count, cudaStream_t st);
 // dW[tap][ci][co] += sum over pixels of X[p + d][ci] dY[p][co] (X as c.in0 / c.in1 / c.up0; c.Cout
 // the layer's output channels: up to 128, or a multiple of 64 / 128 beyond; W even).
 cudaError_t launchConvWgrad(const ConvLaunch& c, const uint16_t* dy, float* dw, int smCount, cudaStream_t st);
@@ -236,7 +254,6 @@ private:
     float* grad_[kActs]   = {};
     float* out32_ = nullptr;
     float* gOut_  = nullptr;
-    float* dx32_  = nullptr;
     uint16_t* dpre_        = nullptr;
     const uint16_t* input_ = nullptr;
     int B_ = 0, H_ = 0, W_ = 0;

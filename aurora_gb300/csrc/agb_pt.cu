@@ -208,13 +208,15 @@ AGB_DN v3 shadowOpacity(const DevScene& s, const RayHit& h)
     const DevInstance& in = s.instances[h.inst];
     const agb_material& b = s.materials[in.material];
     bool hasOpacityImage  = s.matTex && b.has_opacity_image && s.matTex[in.material].image[AGB_TEX_OPACITY] >= 0;
-    if (b.opacity[0] == 1.f && b.opacity[1] == 1.f && b.opacity[2] == 1.f && !hasOpacityImage &&
+    // A node-graph program may drive the opacity: such a material is never taken as opaque here.
+    bool hasGraph = s.matGraph && s.matGraph[in.material].y > 0;
+    if (b.opacity[0] == 1.f && b.opacity[1] == 1.f && b.opacity[2] == 1.f && !hasOpacityImage && !hasGraph &&
         b.transmission == 0.f)
         return splat(1.f);
     Shading sh = computeShading(s, in, uint32_t(h.prim), h.u, h.v);
     v3 mn      = sh.N;
     bool gen;
-    Mat m = loadMaterial(s, in.material, sh, mn, gen);
+    Mat m = loadMaterial<true>(s, in.material, sh, mn, gen, &in);
     return m.opacity * (splat(1.f) - m.transmissionColor() * m.transmission());
 }
 
@@ -470,7 +472,8 @@ AGB_D float bounceClamp(const agb_frame_data& f)
     return f.indirect_bounce_clamp_scale > 0.f ? f.max_luminance * f.indirect_bounce_clamp_scale : 0.f;
 }
 
-template <bool kBatch>
+// kGraphs: the variant for scenes whose materials have node-graph programs (single-scene waves).
+template <bool kBatch, bool kGraphs = false>
 __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene s, agb_frame_data f,
     WaveParams wp, WaveBuffers wb, int bounce, int cur, int depthLimit, BatchTables bt)
 {
@@ -578,7 +581,7 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
                             sh.uv = uv;
                         }
                         matNormal = sh.N;
-                        m = loadMaterial(S, mi, sh, matNormal, genNormal);
+                        m = loadMaterial<kGraphs>(S, mi, sh, matNormal, genNormal, &in);
                         if (!primary && F.is_path_regularization_enabled)
                         {
                             float fl = lerpf(0.05f, lerpf(0.05f, 0.35f, F.path_regularization_strength),
@@ -1460,7 +1463,10 @@ void launchWaveT(const DevScene& s, const agb_frame_data& f, const WaveParams& w
         if (b == depth)
         {
             mark(KC_SHADE);
-            k_shade<kBatch><<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 1, bt);
+            if (!kBatch && s.matGraph)
+                k_shade<false, true><<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 1, bt);
+            else
+                k_shade<kBatch><<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 1, bt);
             launches++;
             break;
         }
@@ -1486,7 +1492,10 @@ void launchWaveT(const DevScene& s, const agb_frame_data& f, const WaveParams& w
             launches += 3;
         }
         mark(KC_SHADE);
-        k_shade<kBatch><<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 0, bt);
+        if (!kBatch && s.matGraph)
+            k_shade<false, true><<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 0, bt);
+        else
+            k_shade<kBatch><<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, 0, bt);
         mark(KC_SHADE);
         k_shade_scatter<kBatch><<<shadeGrid, kShadeBlock, 0, st>>>(s, f, wp, wb, b, cur, bt);
         mark(KC_SHADE);

@@ -93,6 +93,11 @@ struct DevScene
     int32_t imageCount;
     const DevImage* images;
     const DevLayer* layers;
+    // Material node-graph programs (agb_material_graphs_set): per material (first op, op count),
+    // null when no material has one.
+    const int2* matGraph;
+    const agb_graph_op* graphOps;
+    const float4* graphConsts;
     // Environment.
     agb_environment_data env;
     DevImage envLight;        // data null when absent
@@ -310,9 +315,160 @@ AGB_D bool materialTexture(const DevScene& s, int32_t mat, int slot, v2 uv, cons
     return true;
 }
 
-// DefaultMaterial.slang:130-239
+// A material's node-graph program (the operations of agb_material_graphs_set) over the hit:
+// writes the fields it drives into m / materialNormal.  Out of line, registers in local memory: it
+// runs only for materials that have a program.
+static __device__ __noinline__ void runMaterialGraph(const DevScene& s, int2 prog, const Shading& sh,
+    const DevInstance* inst, Mat& m, v3& materialNormal, bool& generatedNormal)
+{
+    float4 r[AGB_GRAPH_REGS];
+    for (int i = 0; i < AGB_GRAPH_REGS; i++)
+        r[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int k = 0; k < prog.y; k++)
+    {
+        const agb_graph_op o = s.graphOps[prog.x + k];
+        const float4 A = r[o.a], B = r[o.b], C = r[o.c], D = r[o.d];
+        float4 v = A;
+        switch (o.op)
+        {
+        case AGB_GOP_CONST: v = __ldg(s.graphConsts + o.imm); break;
+        case AGB_GOP_INPUT:
+        {
+            v3 q = v3{ 0.f, 0.f, 0.f };
+            switch (o.imm)
+            {
+            case AGB_GIN_TEXCOORD: q = v3{ sh.uv.x, sh.uv.y, 0.f }; break;
+            case AGB_GIN_POSITION_WORLD: q = sh.geomPosition; break;
+            case AGB_GIN_POSITION_OBJECT: q = inst ? xfPoint(inst->w2o, sh.geomPosition) : sh.geomPosition; break;
+            case AGB_GIN_NORMAL_WORLD: q = sh.N; break;
+            case AGB_GIN_NORMAL_OBJECT:
+                // Normals go back to object space with the transpose of the object-to-world matrix.
+                q = inst ? normalize(v3{ inst->o2w[0] * sh.N.x + inst->o2w[4] * sh.N.y + inst->o2w[8] * sh.N.z,
+                               inst->o2w[1] * sh.N.x + inst->o2w[5] * sh.N.y + inst->o2w[9] * sh.N.z,
+                               inst->o2w[2] * sh.N.x + inst->o2w[6] * sh.N.y + inst->o2w[10] * sh.N.z })
+                         : sh.N;
+                break;
+            case AGB_GIN_TANGENT_WORLD: q = sh.X; break;
+            case AGB_GIN_BITANGENT_WORLD: q = sh.Y; break;
+            default: break;
+            }
+            v = make_float4(q.x, q.y, q.z, 0.f);
+            break;
+        }
+        case AGB_GOP_ADD: v = make_float4(A.x + B.x, A.y + B.y, A.z + B.z, A.w + B.w); break;
+        case AGB_GOP_SUB: v = make_float4(A.x - B.x, A.y - B.y, A.z - B.z, A.w - B.w); break;
+        case AGB_GOP_MUL: v = make_float4(A.x * B.x, A.y * B.y, A.z * B.z, A.w * B.w); break;
+        case AGB_GOP_DIV: v = make_float4(A.x / B.x, A.y / B.y, A.z / B.z, A.w / B.w); break;
+        case AGB_GOP_MIN: v = make_float4(fminf(A.x, B.x), fminf(A.y, B.y), fminf(A.z, B.z), fminf(A.w, B.w)); break;
+        case AGB_GOP_MAX: v = make_float4(fmaxf(A.x, B.x), fmaxf(A.y, B.y), fmaxf(A.z, B.z), fmaxf(A.w, B.w)); break;
+        case AGB_GOP_POW:
+            v = make_float4(agb_fm::pow(A.x, B.x), agb_fm::pow(A.y, B.y), agb_fm::pow(A.z, B.z), agb_fm::pow(A.w, B.w));
+            break;
+        case AGB_GOP_MOD:
+            v = make_float4(A.x - B.x * floorf(A.x / B.x), A.y - B.y * floorf(A.y / B.y),
+                A.z - B.z * floorf(A.z / B.z), A.w - B.w * floorf(A.w / B.w));
+            break;
+        case AGB_GOP_FLOOR: v = make_float4(floorf(A.x), floorf(A.y), floorf(A.z), floorf(A.w)); break;
+        case AGB_GOP_CEIL: v = make_float4(ceilf(A.x), ceilf(A.y), ceilf(A.z), ceilf(A.w)); break;
+        case AGB_GOP_ABS: v = make_float4(fabsf(A.x), fabsf(A.y), fabsf(A.z), fabsf(A.w)); break;
+        case AGB_GOP_SIN:
+            v = make_float4(agb_fm::sin(A.x), agb_fm::sin(A.y), agb_fm::sin(A.z), agb_fm::sin(A.w));
+            break;
+        case AGB_GOP_COS:
+            v = make_float4(agb_fm::cos(A.x), agb_fm::cos(A.y), agb_fm::cos(A.z), agb_fm::cos(A.w));
+            break;
+        case AGB_GOP_SQRT: v = make_float4(sqrtf(A.x), sqrtf(A.y), sqrtf(A.z), sqrtf(A.w)); break;
+        case AGB_GOP_SIGN:
+            v = make_float4(A.x > 0.f ? 1.f : A.x < 0.f ? -1.f : 0.f, A.y > 0.f ? 1.f : A.y < 0.f ? -1.f : 0.f,
+                A.z > 0.f ? 1.f : A.z < 0.f ? -1.f : 0.f, A.w > 0.f ? 1.f : A.w < 0.f ? -1.f : 0.f);
+            break;
+        case AGB_GOP_CLAMP:
+            v = make_float4(fminf(fmaxf(A.x, B.x), C.x), fminf(fmaxf(A.y, B.y), C.y), fminf(fmaxf(A.z, B.z), C.z),
+                fminf(fmaxf(A.w, B.w), C.w));
+            break;
+        case AGB_GOP_MIX:
+            v = make_float4(B.x + C.x * (A.x - B.x), B.y + C.y * (A.y - B.y), B.z + C.z * (A.z - B.z),
+                B.w + C.w * (A.w - B.w));
+            break;
+        case AGB_GOP_DOT:
+        case AGB_GOP_NORMALIZE:
+        case AGB_GOP_LENGTH:
+        {
+            const float* a = &A.x;
+            const float* b = o.op == AGB_GOP_DOT ? &B.x : &A.x;
+            float d = 0.f;
+            for (int c = 0; c < 4 && c < o.d; c++)
+                d = c == 0 ? a[0] * b[0] : d + a[c] * b[c];
+            if (o.op == AGB_GOP_DOT)
+                v = make_float4(d, d, d, d);
+            else
+            {
+                const float len = sqrtf(d);
+                if (o.op == AGB_GOP_LENGTH)
+                    v = make_float4(len, len, len, len);
+                else
+                {
+                    float out[4] = { 0.f, 0.f, 0.f, 0.f };
+                    for (int c = 0; c < 4 && c < o.d; c++)
+                        out[c] = a[c] / len;
+                    v = make_float4(out[0], out[1], out[2], out[3]);
+                }
+            }
+            break;
+        }
+        case AGB_GOP_SWIZZLE:
+        {
+            const float a[4] = { A.x, A.y, A.z, A.w };
+            v = make_float4(a[o.imm & 3], a[(o.imm >> 2) & 3], a[(o.imm >> 4) & 3], a[(o.imm >> 6) & 3]);
+            break;
+        }
+        case AGB_GOP_COMBINE: v = make_float4(A.x, B.x, C.x, D.x); break;
+        case AGB_GOP_SELECT:
+        {
+            const bool t = o.imm == 0 ? A.x > B.x : o.imm == 1 ? A.x >= B.x : A.x == B.x;
+            v            = t ? C : D;
+            break;
+        }
+        case AGB_GOP_IMAGE:
+            v = o.imm < s.imageCount ? sampleImage(s.images[o.imm], v2{ A.x, A.y }) : make_float4(0.f, 0.f, 0.f, 0.f);
+            break;
+        case AGB_GOP_NORMALMAP:
+        {
+            v3 vv = v3{ A.x, A.y, A.z } * 2.f - splat(1.f);
+            vv.x  = vv.x * B.x;
+            vv.y  = vv.y * B.x;
+            v3 Bn = normalize(cross(sh.N, sh.X));
+            v3 n  = normalize(sh.X * vv.x + Bn * vv.y + sh.N * vv.z);
+            v     = make_float4(n.x, n.y, n.z, 0.f);
+            break;
+        }
+        case AGB_GOP_OUTPUT:
+            switch (o.imm)
+            {
+            case AGB_GOUT_BASE_COLOR: m.baseColor = v3{ A.x, A.y, A.z }; break;
+            case AGB_GOUT_SPECULAR_ROUGHNESS: m.specularRoughness = A.x; break;
+            case AGB_GOUT_COAT_ROUGHNESS: m.coatRoughness = A.x; break;
+            case AGB_GOUT_EMISSION_COLOR: m.emissionColor = v3{ A.x, A.y, A.z }; break;
+            case AGB_GOUT_OPACITY: m.opacity = v3{ A.x, A.y, A.z }; break;
+            case AGB_GOUT_NORMAL:
+                materialNormal  = v3{ A.x, A.y, A.z };
+                generatedNormal = true;
+                break;
+            default: break;
+            }
+            continue;
+        default: break;
+        }
+        r[o.dst] = v;
+    }
+}
+
+// DefaultMaterial.slang:130-239; a node-graph program, when the material has one, runs last
+// (kGraphs: the shading kernel's variant for scenes with programs; the variant without them
+// carries no trace of the check).
+template <bool kGraphs>
 AGB_D Mat loadMaterial(const DevScene& s, int32_t mi, const Shading& sh, v3& materialNormal,
-    bool& generatedNormal)
+    bool& generatedNormal, const DevInstance* inst = nullptr)
 {
     const agb_material& b = s.materials[mi];
     Mat m;
@@ -350,6 +506,12 @@ AGB_D Mat loadMaterial(const DevScene& s, int32_t mi, const Shading& sh, v3& mat
         v3 Bn  = normalize(cross(sh.N, sh.X));
         materialNormal  = normalize(sh.X * vv.x * 1.f + Bn * vv.y * 1.f + sh.N * vv.z);
         generatedNormal = true;
+    }
+    if (kGraphs && s.matGraph)
+    {
+        const int2 prog = __ldg(s.matGraph + mi);
+        if (prog.y > 0)
+            runMaterialGraph(s, prog, sh, inst, m, materialNormal, generatedNormal);
     }
     return m;
 }

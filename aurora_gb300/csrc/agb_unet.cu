@@ -32,75 +32,91 @@ inline unsigned gridFor(long n, int block = 256)
     return unsigned(std::min<long>(std::max<long>(g, 1), 1L << 20));
 }
 
-// gs (H x W) += 0.25 * gp (H/2 x W/2).
-__global__ void k_avgpool2_grad(const float* gp, float* gs, int B, int H, int W, int C)
+// gs (H x W) += 0.25 * gp (H/2 x W/2), four channels per thread.
+__global__ void k_avgpool2_grad(const float4* gp, float4* gs, int B, int H, int W, int C4)
 {
-    long n = long(B) * H * W * C;
+    const long n = long(B) * H * W * C4;
     for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x)
     {
-        int c  = int(i % C);
-        long t = i / C;
-        int x  = int(t % W);
+        const int c = int(i % C4);
+        long t      = i / C4;
+        const int x = int(t % W);
         t /= W;
-        int y  = int(t % H);
-        int b  = int(t / H);
-        gs[i] += 0.25f * gp[((size_t(b) * (H / 2) + y / 2) * (W / 2) + x / 2) * C + c];
+        const int y = int(t % H);
+        const int b = int(t / H);
+        const float4 q = gp[((size_t(b) * (H / 2) + y / 2) * (W / 2) + x / 2) * C4 + c];
+        float4 o       = gs[i];
+        o.x += 0.25f * q.x;
+        o.y += 0.25f * q.y;
+        o.z += 0.25f * q.z;
+        o.w += 0.25f * q.w;
+        gs[i] = o;
     }
 }
 
-// dPre = bf16(g * (y > 0)) (or bf16(g) without ReLU).
-__global__ void k_relu_grad(const float* g, const uint16_t* y, uint16_t* dpre, long n)
+// dPre = bf16(g * (y > 0)) (or bf16(g) without ReLU), eight values per thread.
+__global__ void k_relu_grad(const float4* g, const uint4* y, uint4* dpre, long n8)
 {
-    for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x)
-        dpre[i] = tobf((y == nullptr || bf(y[i]) > 0.f) ? g[i] : 0.f);
-}
-
-// Splits the data gradient dx (B x H x W x (C0 + C1)) of a layer input concat(up?(in0), in1):
-// g1 += channels [C0, C0 + C1); g0 += channels [0, C0) (same resolution), or, with the nearest 2x
-// upsample, the sum of each 2x2 block into the half-resolution g0.
-__global__ void k_grad_split(const float* dx, float* g0, float* g1, int B, int H, int W, int C0, int C1,
-    int up0)
-{
-    const int Cin = C0 + C1;
-    // Part 1: in1 and the non-upsampled in0 (one element each).
-    long n = long(B) * H * W * Cin;
-    for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x)
+    for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n8; i += long(gridDim.x) * blockDim.x)
     {
-        int c  = int(i % Cin);
-        long p = i / Cin;
-        if (c >= C0)
-            g1[p * C1 + (c - C0)] += dx[i];
-        else if (!up0)
-            g0[p * C0 + c] += dx[i];
-    }
-    if (!up0)
-        return;
-    // Part 2: 2x2 block sums for the upsampled in0.
-    long m = long(B) * (H / 2) * (W / 2) * C0;
-    for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < m; i += long(gridDim.x) * blockDim.x)
-    {
-        int c  = int(i % C0);
-        long t = i / C0;
-        int x2 = int(t % (W / 2));
-        t /= (W / 2);
-        int y2 = int(t % (H / 2));
-        int b  = int(t / (H / 2));
-        size_t r0 = ((size_t(b) * H + 2 * y2) * W + 2 * x2) * Cin + c;
-        size_t r1 = r0 + size_t(W) * Cin;
-        g0[i] += ((dx[r0] + dx[r0 + Cin]) + dx[r1]) + dx[r1 + Cin];
+        const float4 g0 = g[2 * i], g1 = g[2 * i + 1];
+        float v[8]      = { g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w };
+        if (y)
+        {
+            const uint4 yy      = y[i];
+            const uint32_t w[4] = { yy.x, yy.y, yy.z, yy.w };
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+            {
+                if (!(__uint_as_float(w[k] << 16) > 0.f))
+                    v[2 * k] = 0.f;
+                if (!(__uint_as_float(w[k] & 0xFFFF0000u) > 0.f))
+                    v[2 * k + 1] = 0.f;
+            }
+        }
+        uint32_t o[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            o[k] = uint32_t(tobf(v[2 * k])) | (uint32_t(tobf(v[2 * k + 1])) << 16);
+        dpre[i] = make_uint4(o[0], o[1], o[2], o[3]);
     }
 }
 
-// db[c] += sum over pixels of dPre[p][c]: each block sums a pixel range for all channels.
-__global__ void k_bias_grad(const uint16_t* dpre, float* db, long P, int C, long pixPerBlock)
+// db[c] += sum over pixels of dPre[p][c]: thread t of a block sums channels 8 (t % G8) .. + 7 over
+// pixels t / G8, t / G8 + L / G8, ... of the block's range (L = the threads in use); the block
+// then reduces per channel in shared memory and adds to db.
+__global__ void __launch_bounds__(256) k_bias_grad(const uint4* dpre, float* db, long P, int C, long pixPerBlock)
 {
-    long p0 = blockIdx.x * pixPerBlock, p1 = p0 + pixPerBlock < P ? p0 + pixPerBlock : P;
-    for (int c = threadIdx.x; c < C; c += blockDim.x)
+    __shared__ float part[256][8];
+    const int G8    = C / 8;
+    const int lanes = 256 / G8 * G8;
+    const int t     = threadIdx.x;
+    const int cg    = t % G8;
+    const long p0   = blockIdx.x * pixPerBlock;
+    const long p1   = p0 + pixPerBlock < P ? p0 + pixPerBlock : P;
+    float acc[8]    = {};
+    if (t < lanes)
+        for (long p = p0 + t / G8; p < p1; p += lanes / G8)
+        {
+            const uint4 v       = dpre[p * G8 + cg];
+            const uint32_t w[4] = { v.x, v.y, v.z, v.w };
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+            {
+                acc[2 * k] += __uint_as_float(w[k] << 16);
+                acc[2 * k + 1] += __uint_as_float(w[k] & 0xFFFF0000u);
+            }
+        }
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        part[t][k] = acc[k];
+    __syncthreads();
+    for (int c = t; c < C; c += 256)
     {
-        float s = 0.f;
-        for (long p = p0; p < p1; p++)
-            s += bf(dpre[p * C + c]);
-        atomicAdd(db + c, s);
+        float sum = 0.f;
+        for (int u = c / 8; u < lanes; u += G8)
+            sum += part[u][c % 8];
+        atomicAdd(db + c, sum);
     }
 }
 
@@ -340,17 +356,11 @@ cudaError_t UnetDenoiser::init(uint64_t seed, cudaStream_t st, int smCount)
 
 cudaError_t UnetDenoiser::repack()
 {
+    // Every layer packed both ways (forward and data-gradient layouts) in one launch.
+    PackJob jobs[kLayers];
     for (int i = 0; i < kLayers; i++)
-    {
-        cudaError_t e;
-        if ((e = launchPackConvWeights(params_ + wOff_[i], layerCin(i), layerCout(i), 0, pack_ + packOff_[i],
-                 stream_)) != cudaSuccess)
-            return e;
-        if ((e = launchPackConvWeights(params_ + wOff_[i], layerCin(i), layerCout(i), 1, packFlip_ + packOff_[i],
-                 stream_)) != cudaSuccess)
-            return e;
-    }
-    return cudaSuccess;
+        jobs[i] = PackJob{ params_ + wOff_[i], pack_ + packOff_[i], packFlip_ + packOff_[i], layerCin(i), layerCout(i) };
+    return launchPackConvWeightsMany(jobs, kLayers, stream_);
 }
 
 cudaError_t UnetDenoiser::ensureShape(int B, int H, int W, bool training)
@@ -366,11 +376,11 @@ cudaError_t UnetDenoiser::ensureShape(int B, int H, int W, bool training)
         act_[a]  = nullptr;
         grad_[a] = nullptr;
     }
-    out32_ = gOut_ = dx32_ = nullptr;
+    out32_ = gOut_ = nullptr;
     dpre_  = nullptr;
     B_ = H_ = W_ = 0;
     cudaError_t e;
-    size_t maxDpre = 0, maxDx = 0;
+    size_t maxDpre = 0;
     for (int a = 1; a < A_COUNT; a++)
     {
         size_t n = pixels(B, H, W, kActLevel[a]) * kActChannels[a];
@@ -388,11 +398,9 @@ cudaError_t UnetDenoiser::ensureShape(int B, int H, int W, bool training)
         {
             size_t pl = pixels(B, H, W, kLayerDefs[i].level);
             maxDpre   = std::max(maxDpre, pl * layerCout(i));
-            maxDx     = std::max(maxDx, pl * layerCin(i));
         }
         if ((e = alloc(reinterpret_cast<void**>(&gOut_), p0 * 16 * 4, shapeAllocs_)) != cudaSuccess ||
-            (e = alloc(reinterpret_cast<void**>(&dpre_), maxDpre * 2, shapeAllocs_)) != cudaSuccess ||
-            (e = alloc(reinterpret_cast<void**>(&dx32_), maxDx * 4, shapeAllocs_)) != cudaSuccess)
+            (e = alloc(reinterpret_cast<void**>(&dpre_), maxDpre * 2, shapeAllocs_)) != cudaSuccess)
             return e;
     }
     B_ = B;
@@ -517,35 +525,41 @@ cudaError_t UnetDenoiser::backward(const float* target)
         const int cin = layerCin(i), cout = layerCout(i);
         const long Pl = long(pixels(B_, H_, W_, L.level));
         const float* gy = L.out >= 0 ? grad_[L.out] : gOut_;
-        k_relu_grad<<<gridFor(Pl * cout), 256, 0, stream_>>>(gy, L.relu ? act_[L.out] : nullptr, dpre_, Pl * cout);
+        k_relu_grad<<<gridFor(Pl * cout / 8), 256, 0, stream_>>>(reinterpret_cast<const float4*>(gy),
+            L.relu ? reinterpret_cast<const uint4*>(act_[L.out]) : nullptr, reinterpret_cast<uint4*>(dpre_),
+            Pl * cout / 8);
         ConvLaunch c = layerLaunch(i, input_);
         if ((e = launchConvWgrad(c, dpre_, grads_ + wOff_[i], smCount_, stream_)) != cudaSuccess)
             return e;
-        long per = std::max(1L, (Pl + 4095) / 4096);
-        per      = std::max(per, 64L);
-        k_bias_grad<<<unsigned((Pl + per - 1) / per), 128, 0, stream_>>>(dpre_, grads_ + bOff_[i], Pl, cout, per);
+        const long per = std::max(256L, (Pl + 1023) / 1024);
+        k_bias_grad<<<unsigned((Pl + per - 1) / per), 256, 0, stream_>>>(reinterpret_cast<const uint4*>(dpre_),
+            grads_ + bOff_[i], Pl, cout, per);
         if (i > 0)
         {
+            // dX = the convolution of dPre with the flipped weights, added straight into the
+            // gradients of the layer's inputs (the upsampled one summed over 2x2 blocks).
             ConvLaunch d{};
-            d.in0   = dpre_;
-            d.wpack = packFlip_ + packOff_[i];
-            d.out32 = dx32_;
-            d.B     = B_;
-            d.H     = c.H;
-            d.W     = c.W;
-            d.C0    = cout;
-            d.Cout  = cin;
+            d.in0    = dpre_;
+            d.wpack  = packFlip_ + packOff_[i];
+            d.B      = B_;
+            d.H      = c.H;
+            d.W      = c.W;
+            d.C0     = cout;
+            d.Cout   = cin;
+            d.grad0  = grad_[L.in0];
+            d.grad1  = L.in1 >= 0 ? grad_[L.in1] : nullptr;
+            d.gradC0 = c.C0;
+            d.gradUp = L.up0;
             if ((e = launchConv3x3(d, stream_)) != cudaSuccess)
                 return e;
-            k_grad_split<<<gridFor(Pl * cin), 256, 0, stream_>>>(dx32_, grad_[L.in0], L.in1 >= 0 ? grad_[L.in1] : nullptr,
-                B_, c.H, c.W, c.C0, c.C1, L.up0);
         }
         int poolSrc = i == 2 ? A_S0 : i == 4 ? A_S1 : i == 6 ? A_S2 : -1;
         if (poolSrc >= 0)
         {
             int lv = kActLevel[poolSrc], Hs = H_ >> lv, Ws = W_ >> lv, C = kActChannels[poolSrc];
-            k_avgpool2_grad<<<gridFor(long(B_) * Hs * Ws * C), 256, 0, stream_>>>(grad_[poolSrc + 1], grad_[poolSrc],
-                B_, Hs, Ws, C);
+            k_avgpool2_grad<<<gridFor(long(B_) * Hs * Ws * C / 4), 256, 0, stream_>>>(
+                reinterpret_cast<const float4*>(grad_[poolSrc + 1]), reinterpret_cast<float4*>(grad_[poolSrc]), B_, Hs,
+                Ws, C / 4);
         }
     }
     return cudaGetLastError();

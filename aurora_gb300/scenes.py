@@ -350,6 +350,9 @@ class SceneDesc:
         self.instances = []     # dicts: mesh, material, xform (12), layers [(material, uv)]
         self.materials = None   # MATERIAL_DTYPE array
         self.textures = None    # MATERIAL_TEXTURES_DTYPE array or None
+        # Material node-graph programs or None: dict(first, count (int32 per material), ops
+        # (GRAPH_OP_DTYPE), consts (float32, 4 per constant)); image operands index self.images.
+        self.graphs = None
         self.images = []        # dicts: pixels, width, height, format, linear
         self.env = environment()
         self.env_light = -1     # image index

@@ -397,6 +397,63 @@ AGB_API agb_status agb_image_create(agb_context* ctx, const void* pixels, uint32
 AGB_API agb_status agb_materials_set(agb_context* ctx, const agb_material* materials,
     const agb_material_textures* textures, uint32_t count);
 
+/* Material node graphs.  The reference generates shader code from a MaterialX document's node
+ * graphs (MaterialX/BSDFCodeGenerator.cpp:55-140 binds texcoord, normal, tangent and object /
+ * world position to the generated code; MaterialGenerator.cpp:30-120 routes the graph outputs
+ * into the material's fields).  Here the host compiles a graph into a program of register
+ * operations over float4 registers (AGB_GRAPH_REGS of them) that the shading runs per hit, after
+ * the material's constants and textures are read, writing the fields the graph drives.
+ * Operations (r = registers, K = the constants, all component-wise unless stated):
+ *   CONST    r[dst] = K[imm]
+ *   INPUT    r[dst] = hit attribute imm (AGB_GIN_*; texcoord as (u, v, 0, 0), vectors with w = 0)
+ *   ADD SUB MUL DIV MIN MAX  r[dst] = r[a] op r[b];  POW r[dst] = pow(r[a], r[b]);
+ *   MOD      r[dst] = r[a] - r[b] * floor(r[a] / r[b])
+ *   FLOOR CEIL ABS SIN COS SQRT SIGN  r[dst] = f(r[a])
+ *   CLAMP    r[dst] = min(max(r[a], r[b]), r[c])
+ *   MIX      r[dst] = r[b] + r[c] * (r[a] - r[b])        (fg = a, bg = b, mix = c)
+ *   DOT      r[dst] = splat(sum over the first d components of r[a] * r[b], in order)
+ *   NORMALIZE r[dst] = the first d components of r[a] / sqrt(dot), the rest 0
+ *   LENGTH   r[dst] = splat(sqrt(dot of the first d components))
+ *   SWIZZLE  r[dst] = (r[a][imm & 3], r[a][(imm >> 2) & 3], r[a][(imm >> 4) & 3], r[a][(imm >> 6) & 3])
+ *   COMBINE  r[dst] = (r[a].x, r[b].x, r[c].x, r[d].x)
+ *   SELECT   r[dst] = (r[a].x cmp r[b].x) ? r[c] : r[d], cmp = imm (0 >, 1 >=, 2 ==)
+ *   IMAGE    r[dst] = image imm sampled at r[a].xy (its own filter, repeat addressing)
+ *   NORMALMAP r[dst] = normalize(T n.x + B n.y + N n.z), n = 2 r[a] - 1 with n.xy scaled by r[b].x,
+ *            N the shading normal, T its tangent, B = normalize(cross(N, T))
+ *   OUTPUT   material field imm (AGB_GOUT_*) = r[a] */
+enum
+{
+    AGB_GOP_CONST = 0, AGB_GOP_INPUT, AGB_GOP_ADD, AGB_GOP_SUB, AGB_GOP_MUL, AGB_GOP_DIV, AGB_GOP_MIN,
+    AGB_GOP_MAX, AGB_GOP_POW, AGB_GOP_MOD, AGB_GOP_FLOOR, AGB_GOP_CEIL, AGB_GOP_ABS, AGB_GOP_SIN,
+    AGB_GOP_COS, AGB_GOP_SQRT, AGB_GOP_SIGN, AGB_GOP_CLAMP, AGB_GOP_MIX, AGB_GOP_DOT,
+    AGB_GOP_NORMALIZE, AGB_GOP_LENGTH, AGB_GOP_SWIZZLE, AGB_GOP_COMBINE, AGB_GOP_SELECT,
+    AGB_GOP_IMAGE, AGB_GOP_NORMALMAP, AGB_GOP_OUTPUT, AGB_GOP_COUNT
+};
+enum
+{
+    AGB_GIN_TEXCOORD = 0, AGB_GIN_POSITION_WORLD, AGB_GIN_POSITION_OBJECT, AGB_GIN_NORMAL_WORLD,
+    AGB_GIN_NORMAL_OBJECT, AGB_GIN_TANGENT_WORLD, AGB_GIN_BITANGENT_WORLD, AGB_GIN_COUNT
+};
+enum
+{
+    AGB_GOUT_BASE_COLOR = 0, AGB_GOUT_SPECULAR_ROUGHNESS, AGB_GOUT_COAT_ROUGHNESS,
+    AGB_GOUT_EMISSION_COLOR, AGB_GOUT_OPACITY, AGB_GOUT_NORMAL, AGB_GOUT_COUNT
+};
+#define AGB_GRAPH_REGS 32
+#define AGB_GRAPH_MAX_OPS 4096
+typedef struct agb_graph_op
+{
+    uint8_t op, dst, a, b, c, d; /* d: also the component count of DOT / NORMALIZE / LENGTH */
+    uint16_t imm;
+} agb_graph_op;
+/* Programs for the current material table: material m runs ops[first[m] .. first[m] + count[m])
+ * (count 0: none).  Register indices below AGB_GRAPH_REGS, constant and image indices valid,
+ * at most AGB_GRAPH_MAX_OPS per program; checked here.  Replaced by the next call; cleared by
+ * agb_materials_set.  Host arrays; constants 4 floats each. */
+AGB_API agb_status agb_material_graphs_set(agb_context* ctx, const int32_t* first, const int32_t* count,
+    uint32_t material_count, const agb_graph_op* ops, uint32_t op_count, const float* constants,
+    uint32_t constant_count);
+
 /* Replaces the instance list and rebuilds the TLAS (HGIScene::rebuildInstanceList and
  * rebuildAccelerationStructure, HGI/HGIScene.cpp:192-449). Host array. */
 AGB_API agb_status agb_instances_set(agb_context* ctx, const agb_instance* instances,

@@ -79,6 +79,12 @@ struct Scene
     const Image* envLight            = nullptr;
     const Image* envBackground       = nullptr;
     const AliasEntry* envAlias       = nullptr;
+    // Material node-graph programs (agb_material_graphs_set): material m runs
+    // graphOps[graphFirst[m] .. + graphCount[m]); null when no material has one.
+    const int32_t* graphFirst        = nullptr;
+    const int32_t* graphCount        = nullptr;
+    const agb_graph_op* graphOps     = nullptr;
+    const float* graphConsts         = nullptr; // 4 per constant
 };
 
 // Ground plane: the layout of the C ABI's agb_ground_plane (the caller's IGroundPlane values,
@@ -284,9 +290,192 @@ struct PathTracer
         return true;
     }
 
-    // DefaultMaterial.slang:130-239
-    Material<T> evaluateDefaultMaterial(int32_t matIndex, const ShadingData<T>& sh,
+    // The inverse of an instance's object-to-world transform as the host computes it for the
+    // device: double precision, rounded to float.
+    static void worldToObject(const float* m, float* out)
+    {
+        double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6], g = m[8], h = m[9], i = m[10];
+        double A = e * i - f * h, Bq = -(d * i - f * g), C = d * h - e * g;
+        double det = a * A + b * Bq + c * C;
+        double inv[9] = { A / det, -(b * i - c * h) / det, (b * f - c * e) / det, Bq / det,
+            (a * i - c * g) / det, -(a * f - c * d) / det, C / det, -(a * h - b * g) / det,
+            (a * e - b * d) / det };
+        double tx = m[3], ty = m[7], tz = m[11];
+        for (int r = 0; r < 3; r++)
+        {
+            out[4 * r + 0] = float(inv[3 * r + 0]);
+            out[4 * r + 1] = float(inv[3 * r + 1]);
+            out[4 * r + 2] = float(inv[3 * r + 2]);
+            out[4 * r + 3] = float(-(inv[3 * r + 0] * tx + inv[3 * r + 1] * ty + inv[3 * r + 2] * tz));
+        }
+    }
+
+    // A material's node-graph program over the hit (the operations documented with
+    // agb_material_graphs_set), run after its constants and textures: writes the fields it drives.
+    void runMaterialGraph(int32_t matIndex, const ShadingData<T>& sh, const Instance* inst, Material<T>& m,
         v3& materialNormal, bool& isGeneratedNormal) const
+    {
+        struct R4
+        {
+            T v[4];
+        };
+        R4 r[AGB_GRAPH_REGS];
+        for (auto& q : r)
+            q = R4{ { T(0), T(0), T(0), T(0) } };
+        const int32_t first = scene->graphFirst[matIndex], count = scene->graphCount[matIndex];
+        for (int32_t k = 0; k < count; k++)
+        {
+            const agb_graph_op& o = scene->graphOps[first + k];
+            const R4 A = r[o.a], B = r[o.b], C = r[o.c], D = r[o.d];
+            R4 v = A;
+            auto each = [&](auto f) {
+                for (int c = 0; c < 4; c++)
+                    v.v[c] = f(A.v[c], B.v[c], C.v[c]);
+            };
+            switch (o.op)
+            {
+            case AGB_GOP_CONST:
+                for (int c = 0; c < 4; c++)
+                    v.v[c] = T(scene->graphConsts[4 * o.imm + c]);
+                break;
+            case AGB_GOP_INPUT:
+            {
+                v3 q(T(0));
+                switch (o.imm)
+                {
+                case AGB_GIN_TEXCOORD: q = v3(sh.texCoord.x, sh.texCoord.y, T(0)); break;
+                case AGB_GIN_POSITION_WORLD: q = sh.geomPosition; break;
+                case AGB_GIN_POSITION_OBJECT:
+                    if (inst)
+                    {
+                        float w[12];
+                        worldToObject(inst->objectToWorld, w);
+                        const v3& p = sh.geomPosition;
+                        q = v3(T(w[0]) * p.x + T(w[1]) * p.y + T(w[2]) * p.z + T(w[3]),
+                            T(w[4]) * p.x + T(w[5]) * p.y + T(w[6]) * p.z + T(w[7]),
+                            T(w[8]) * p.x + T(w[9]) * p.y + T(w[10]) * p.z + T(w[11]));
+                    }
+                    else
+                        q = sh.geomPosition;
+                    break;
+                case AGB_GIN_NORMAL_WORLD: q = sh.normal; break;
+                case AGB_GIN_NORMAL_OBJECT:
+                    if (inst)
+                    {
+                        const float* o2w = inst->objectToWorld;
+                        const v3& n      = sh.normal;
+                        q = normalize(v3(T(o2w[0]) * n.x + T(o2w[4]) * n.y + T(o2w[8]) * n.z,
+                            T(o2w[1]) * n.x + T(o2w[5]) * n.y + T(o2w[9]) * n.z,
+                            T(o2w[2]) * n.x + T(o2w[6]) * n.y + T(o2w[10]) * n.z));
+                    }
+                    else
+                        q = sh.normal;
+                    break;
+                case AGB_GIN_TANGENT_WORLD: q = sh.tangent; break;
+                case AGB_GIN_BITANGENT_WORLD: q = sh.bitangent; break;
+                default: break;
+                }
+                v = R4{ { q.x, q.y, q.z, T(0) } };
+                break;
+            }
+            case AGB_GOP_ADD: each([](T a, T b, T) { return a + b; }); break;
+            case AGB_GOP_SUB: each([](T a, T b, T) { return a - b; }); break;
+            case AGB_GOP_MUL: each([](T a, T b, T) { return a * b; }); break;
+            case AGB_GOP_DIV: each([](T a, T b, T) { return a / b; }); break;
+            case AGB_GOP_MIN: each([](T a, T b, T) { return std::fmin(a, b); }); break;
+            case AGB_GOP_MAX: each([](T a, T b, T) { return std::fmax(a, b); }); break;
+            case AGB_GOP_POW: each([](T a, T b, T) { return tpow(a, b); }); break;
+            case AGB_GOP_MOD: each([](T a, T b, T) { return a - b * std::floor(a / b); }); break;
+            case AGB_GOP_FLOOR: each([](T a, T, T) { return std::floor(a); }); break;
+            case AGB_GOP_CEIL: each([](T a, T, T) { return std::ceil(a); }); break;
+            case AGB_GOP_ABS: each([](T a, T, T) { return std::fabs(a); }); break;
+            case AGB_GOP_SIN: each([](T a, T, T) { return tsin(a); }); break;
+            case AGB_GOP_COS: each([](T a, T, T) { return tcos(a); }); break;
+            case AGB_GOP_SQRT: each([](T a, T, T) { return std::sqrt(a); }); break;
+            case AGB_GOP_SIGN: each([](T a, T, T) { return a > T(0) ? T(1) : a < T(0) ? T(-1) : T(0); }); break;
+            case AGB_GOP_CLAMP: each([](T a, T b, T c) { return std::fmin(std::fmax(a, b), c); }); break;
+            case AGB_GOP_MIX: each([](T a, T b, T c) { return b + c * (a - b); }); break;
+            case AGB_GOP_DOT:
+            case AGB_GOP_NORMALIZE:
+            case AGB_GOP_LENGTH:
+            {
+                const R4& bb = o.op == AGB_GOP_DOT ? B : A;
+                T d = T(0);
+                for (int c = 0; c < 4 && c < o.d; c++)
+                    d = c == 0 ? A.v[0] * bb.v[0] : d + A.v[c] * bb.v[c];
+                if (o.op == AGB_GOP_DOT)
+                    v = R4{ { d, d, d, d } };
+                else
+                {
+                    const T len = std::sqrt(d);
+                    if (o.op == AGB_GOP_LENGTH)
+                        v = R4{ { len, len, len, len } };
+                    else
+                    {
+                        v = R4{ { T(0), T(0), T(0), T(0) } };
+                        for (int c = 0; c < 4 && c < o.d; c++)
+                            v.v[c] = A.v[c] / len;
+                    }
+                }
+                break;
+            }
+            case AGB_GOP_SWIZZLE:
+                v = R4{ { A.v[o.imm & 3], A.v[(o.imm >> 2) & 3], A.v[(o.imm >> 4) & 3], A.v[(o.imm >> 6) & 3] } };
+                break;
+            case AGB_GOP_COMBINE: v = R4{ { A.v[0], B.v[0], C.v[0], D.v[0] } }; break;
+            case AGB_GOP_SELECT:
+            {
+                const bool t = o.imm == 0 ? A.v[0] > B.v[0] : o.imm == 1 ? A.v[0] >= B.v[0] : A.v[0] == B.v[0];
+                v            = t ? C : D;
+                break;
+            }
+            case AGB_GOP_IMAGE:
+            {
+                v3 rgb;
+                T alpha;
+                E::sample(scene->images[o.imm], v2(A.v[0], A.v[1]), rgb, alpha);
+                v = R4{ { rgb.x, rgb.y, rgb.z, alpha } };
+                break;
+            }
+            case AGB_GOP_NORMALMAP:
+            {
+                v3 vv = v3(A.v[0], A.v[1], A.v[2]) * T(2) - v3(1);
+                vv.x  = vv.x * B.v[0];
+                vv.y  = vv.y * B.v[0];
+                v3 Bn = normalize(cross(sh.normal, sh.tangent));
+                v3 n  = normalize(sh.tangent * vv.x + Bn * vv.y + sh.normal * vv.z);
+                v     = R4{ { n.x, n.y, n.z, T(0) } };
+                break;
+            }
+            case AGB_GOP_OUTPUT:
+                switch (o.imm)
+                {
+                case AGB_GOUT_BASE_COLOR: m.baseColor = v3(A.v[0], A.v[1], A.v[2]); break;
+                case AGB_GOUT_SPECULAR_ROUGHNESS: m.specularRoughness = A.v[0]; break;
+                case AGB_GOUT_COAT_ROUGHNESS: m.coatRoughness = A.v[0]; break;
+                case AGB_GOUT_EMISSION_COLOR: m.emissionColor = v3(A.v[0], A.v[1], A.v[2]); break;
+                case AGB_GOUT_OPACITY: m.opacity = v3(A.v[0], A.v[1], A.v[2]); break;
+                case AGB_GOUT_NORMAL:
+                    materialNormal    = v3(A.v[0], A.v[1], A.v[2]);
+                    isGeneratedNormal = true;
+                    break;
+                default: break;
+                }
+                continue;
+            default: break;
+            }
+            r[o.dst] = v;
+        }
+    }
+
+    bool hasGraph(int32_t matIndex) const
+    {
+        return scene->graphFirst && scene->graphCount && scene->graphCount[matIndex] > 0;
+    }
+
+    // DefaultMaterial.slang:130-239; a node-graph program, when the material has one, runs last.
+    Material<T> evaluateDefaultMaterial(int32_t matIndex, const ShadingData<T>& sh,
+        v3& materialNormal, bool& isGeneratedNormal, const Instance* inst = nullptr) const
     {
         const MaterialBlock& b = scene->materials[matIndex];
         Material<T> m;
@@ -350,6 +539,8 @@ struct PathTracer
             materialNormal    = normalize(sh.tangent * vv.x * T(1) + Bn * vv.y * T(1) + sh.normal * vv.z);
             isGeneratedNormal = true;
         }
+        if (hasGraph(matIndex))
+            runMaterialGraph(matIndex, sh, inst, m, materialNormal, isGeneratedNormal);
         m.metalColor = m.baseColor;
         return m;
     }
@@ -449,13 +640,13 @@ struct PathTracer
         bool hasOpacityImage = scene->materialTextures && b.hasOpacityTex &&
             scene->materialTextures[in.material].image[kTexOpacity] >= 0;
         bool opaque = b.opacity[0] == 1.f && b.opacity[1] == 1.f && b.opacity[2] == 1.f &&
-            !hasOpacityImage && b.transmission == 0.f;
+            !hasOpacityImage && !hasGraph(in.material) && b.transmission == 0.f;
         if (opaque)
             return v3(1);
         ShadingData<T> sh = computeShadingData(h.inst, uint32_t(h.prim), T(h.u), T(h.v));
         v3 mn = sh.normal;
         bool gen;
-        Material<T> m = evaluateDefaultMaterial(in.material, sh, mn, gen);
+        Material<T> m = evaluateDefaultMaterial(in.material, sh, mn, gen, &in);
         return m.opacity * (v3(1) - m.transmissionColor * m.transmission);
     }
 
@@ -726,7 +917,7 @@ struct PathTracer
             }
             bool isGeneratedNormal = false;
             v3 materialNormal      = sh.normal;
-            Material<T> m = evaluateDefaultMaterial(matIndex, sh, materialNormal, isGeneratedNormal);
+            Material<T> m = evaluateDefaultMaterial(matIndex, sh, materialNormal, isGeneratedNormal, &in);
             if (!p.isPrimaryRay && f.isPathRegularizationEnabled)
             {
                 T fl = lerp(T(0.05f), lerp(T(0.05f), T(0.35f), T(f.pathRegularizationStrength)),

@@ -11,6 +11,8 @@
 #include <cstddef>
 #include <cstdint>
 
+#include "../include/agb.h" // agb_graph_op and its operation / input / output codes
+
 namespace orc
 {
 

@@ -174,7 +174,9 @@ class Scene(ctypes.Structure):
                 ("materialTextures", ctypes.c_void_p), ("images", ctypes.c_void_p),
                 ("imageCount", ctypes.c_int32), ("env", ctypes.c_void_p),
                 ("envLight", ctypes.c_void_p), ("envBackground", ctypes.c_void_p),
-                ("envAlias", ctypes.c_void_p)]
+                ("envAlias", ctypes.c_void_p), ("graphFirst", ctypes.c_void_p),
+                ("graphCount", ctypes.c_void_p), ("graphOps", ctypes.c_void_p),
+                ("graphConsts", ctypes.c_void_p)]
 
 
 def image_to_rgba32f(im):
@@ -264,6 +266,15 @@ class OracleScene:
         sc.envLight = ctypes.addressof(imgs[s.env_light]) if s.env_light >= 0 else None
         sc.envBackground = ctypes.addressof(imgs[s.env_background]) if s.env_background >= 0 else None
         sc.envAlias = None if self.alias is None else self.alias.ctypes.data
+        g = getattr(s, "graphs", None)
+        if g is not None:
+            gf = np.ascontiguousarray(g["first"], np.int32)
+            gc = np.ascontiguousarray(g["count"], np.int32)
+            gops = np.ascontiguousarray(g["ops"])
+            gk = np.ascontiguousarray(g["consts"], np.float32).reshape(-1)
+            sc.graphFirst, sc.graphCount = gf.ctypes.data, gc.ctypes.data
+            sc.graphOps, sc.graphConsts = gops.ctypes.data, (gk.ctypes.data if gk.size else None)
+            self._keep += [gf, gc, gops, gk]
         self._keep += [meshes, insts, imgs, rgba]
         self.scene = sc
         self.frame = np.ascontiguousarray(s.frame).reshape(1).copy()

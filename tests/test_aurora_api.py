@@ -82,10 +82,11 @@ TEX_NAMES = {0: "base_color_image", 1: "specular_roughness_image", 2: "opacity_i
              3: "normal_image", 4: "emission_color_image"}
 
 
-def write_scene(path, s, view, proj, lights, depth, mtlx=False):
+def write_scene(path, s, view, proj, lights, depth, mtlx=False, docs=None):
     """The scene file tests/cpp/aurora_api_render.cpp reads: version 2 when the scene has material
     textures or layers (images, texture properties, per-instance layer lists; each distinct
-    layer UV set becomes one more mesh with the base mesh's geometry)."""
+    layer UV set becomes one more mesh with the base mesh's geometry).  docs (with mtlx): a
+    MaterialX document per material index to send instead of the one made from its values."""
     from aurora_gb300 import _abi, scenes
     layered = any(inst.get("layers") for inst in s.instances)
     textured = s.textures is not None and bool((np.asarray(s.textures["image"]) >= 0).any())
@@ -138,7 +139,7 @@ def write_scene(path, s, view, proj, lights, depth, mtlx=False):
                         if not os.path.exists(png):
                             open(png, "wb").write(png_bytes(np.asarray(s.images[img]["pixels"]), 6, 8, [0]))
                         tex.append((name[:-len("_image")], png))
-            doc = materialx_document(mat, props, f"m{mi}", tex).encode()
+            doc = (docs[mi] if docs and mi in docs else materialx_document(mat, props, f"m{mi}", tex)).encode()
             b += struct.pack("<II", 0xFFFFFFFF, len(doc)) + doc
             continue
         tex = []

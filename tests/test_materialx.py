@@ -156,3 +156,88 @@ def test_obj_materials_from_materialx_files():
     assert glass_on["path"].endswith("-glass:OBJFileMaterial-1")
     assert off["materials"][0]["path"].endswith("-red:OBJFileMaterial-0")
     assert on["instances"][0]["material"] == red_on["path"]
+
+
+def test_node_graphs_compile_to_programs():
+    """Inputs fed by node graphs become a per-hit program (the `materialx_graph` property): a
+    custom node expanded from its nodedef's nodegraph, texture coordinates, object position,
+    arithmetic; run by a numpy restatement of the operations, the program gives the graph's
+    values."""
+    import mtlx_graphs as mg
+    from aurora_gb300 import _abi
+    out = props(mg.CHECKER)
+    assert out["ok"] and out["warnings"] == "", out["warnings"]
+    p = out["properties"]
+    assert np.float32(p["metalness"]) == np.float32(0.3)
+    ops, consts, images = mg.decode(p["materialx_graph"])
+    assert images == [] and len(ops) > 10
+    rng = np.random.default_rng(3)
+    P = 4096
+    uv = rng.uniform(-2, 2, (P, 2)).astype(np.float32)
+    pos = rng.uniform(-3, 3, (P, 3)).astype(np.float32)
+    res = mg.evaluate(ops, consts, {_abi.GIN_TEXCOORD: uv, _abi.GIN_POSITION_OBJECT: pos})
+    checker = np.mod(np.floor(uv[:, 0] * 8) + np.floor(uv[:, 1] * 6), 2).astype(np.float32)[:, None]
+    fg, bg = np.float32([0.8, 0.2, 0.1]), np.float32([0.1, 0.3, 0.7])
+    np.testing.assert_array_equal(res[_abi.GOUT_BASE_COLOR], bg + checker * (fg - bg))
+    rough = np.clip(np.sin(pos[:, 0] * np.float32(3)), np.float32(0.15), np.float32(0.8))
+    np.testing.assert_allclose(res[_abi.GOUT_SPECULAR_ROUGHNESS][:, 0], rough, atol=1e-6)
+
+
+def test_node_graph_outputs_images_and_interfaces():
+    """A node graph with its own interface input and five outputs: base_color (an image through
+    scaled texture coordinates, tinted), emission_color (ifgreater on the luminance), normal (a
+    normal map), coat_roughness (a switch over the world normal) and opacity (swizzle, power)."""
+    import mtlx_graphs as mg
+    from aurora_gb300 import _abi
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "p.mtlx")
+        open(path, "w").write(mg.PATTERNS)
+        out = run("mtlx", path)
+    assert out["ok"] and out["warnings"] == "", out["warnings"]
+    ops, consts, images = mg.decode(out["properties"]["materialx_graph"])
+    assert images == [f"MaterialXImage/{tmp}/pattern.png:linearize:0"]
+    assert [im["property"] for im in out["images"]] == ["materialx_graph"]
+    outs = set(ops["imm"][ops["op"] == _abi.GOP_OUTPUT])
+    assert outs == {_abi.GOUT_BASE_COLOR, _abi.GOUT_EMISSION_COLOR, _abi.GOUT_NORMAL,
+                    _abi.GOUT_COAT_ROUGHNESS, _abi.GOUT_OPACITY}
+    rng = np.random.default_rng(4)
+    P = 2048
+    uv = rng.uniform(0, 1, (P, 2)).astype(np.float32)
+    n = rng.normal(size=(P, 3)).astype(np.float32)
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    t = np.cross(n, rng.normal(size=(P, 3))).astype(np.float32)
+    t /= np.linalg.norm(t, axis=1, keepdims=True)
+    img = rng.uniform(0, 1, (8, 8, 4)).astype(np.float32)
+    res = mg.evaluate(ops, consts, {_abi.GIN_TEXCOORD: uv, _abi.GIN_NORMAL_WORLD: n, _abi.GIN_TANGENT_WORLD: t},
+                      [img])
+    x = np.floor(uv[:, 0] * 3 * 8).astype(int) % 8
+    y = np.floor(uv[:, 1] * 3 * 8).astype(int) % 8
+    tex = img[y, x, :3]
+    np.testing.assert_allclose(res[_abi.GOUT_BASE_COLOR], tex * np.float32([0.9, 0.8, 0.6]), rtol=1e-6)
+    lum = tex @ np.float32([0.2722287, 0.6740818, 0.0536895])
+    glow = np.where((lum > 0.6)[:, None], np.float32([1.0, 0.5, 0.2]), 0)
+    np.testing.assert_array_equal(res[_abi.GOUT_EMISSION_COLOR][np.abs(lum - 0.6) > 1e-5],
+                                  glow[np.abs(lum - 0.6) > 1e-5])
+    which = n[:, 1] + 1
+    cr = np.where(which >= 2, 0.05, np.where(which >= 1, 0.3, 0.9)).astype(np.float32)
+    np.testing.assert_array_equal(res[_abi.GOUT_COAT_ROUGHNESS][:, 0], cr)
+    np.testing.assert_allclose(np.linalg.norm(res[_abi.GOUT_NORMAL], axis=1), 1, atol=1e-5)
+    np.testing.assert_allclose(res[_abi.GOUT_OPACITY], tex[:, [1, 1, 2]] ** np.float32(0.25), rtol=1e-5)
+
+
+def test_node_graph_refusals():
+    """A node without an implementation leaves its input at the default, with a warning; the rest
+    of the document still applies."""
+    doc = """<materialx version="1.39">
+  <noise3d name="n" type="float" />
+  <standard_surface name="S" type="surfaceshader">
+    <input name="specular_roughness" type="float" nodename="n" />
+    <input name="base_color" type="color3" nodename="missing" />
+    <input name="metalness" type="float" value="0.5" />
+  </standard_surface>
+</materialx>"""
+    out = props(doc)
+    assert out["ok"]
+    assert "materialx_graph" not in out["properties"] and out["properties"]["metalness"] == 0.5
+    assert "node <noise3d> is not supported" in out["warnings"]
+    assert "node 'missing' not found" in out["warnings"]
