@@ -330,6 +330,51 @@ agb_status ensureAccum(agb_context* ctx, uint32_t W, uint32_t H)
 
 // Collects the child boxes of the BLAS down to kCoverDepth levels (or to a leaf, or to a node that
 // is not among the `avail` nodes at hand) into out; a mesh whose root is a leaf keeps its bounds.
+// BLAS node order in memory.  The GPU builder numbers nodes level by level.  AGB_BLAS_LAYOUT=dfs
+// lays them out depth first with a node's two interior children side by side (a path's nodes
+// close together, both children of a node in one or two cache lines): the children of node n are
+// placed together, and the pairs of child 0's subtree follow before child 1's.  The tree (and so
+// every hit) is the same.  Measured on the large configuration: closest-hit 138.2 -> 137.8 ms,
+// shadow 97.8 -> 97.5 ms per frame, for a host round trip of the nodes per build, so the builder's
+// order stays the default.
+bool blasLayoutDepthFirst()
+{
+    const char* v = getenv("AGB_BLAS_LAYOUT");
+    return v && std::strcmp(v, "dfs") == 0;
+}
+
+void layoutDepthFirst(const std::vector<BNode>& in, int32_t root, std::vector<BNode>& out)
+{
+    out.clear();
+    out.reserve(in.size());
+    out.push_back(in[size_t(root)]);
+    std::vector<std::pair<int32_t, int32_t>> stack; // (node in `in`, its slot in `out`)
+    stack.push_back({ root, 0 });
+    while (!stack.empty())
+    {
+        const auto [old, slot] = stack.back();
+        stack.pop_back();
+        const int4 r     = in[size_t(old)].ref;
+        const int32_t c0 = r.x, c1 = r.y;
+        int4 nr          = r;
+        if (c0 >= 0)
+        {
+            nr.x = int32_t(out.size());
+            out.push_back(in[size_t(c0)]);
+        }
+        if (c1 >= 0)
+        {
+            nr.y = int32_t(out.size());
+            out.push_back(in[size_t(c1)]);
+        }
+        out[size_t(slot)].ref = nr;
+        if (c1 >= 0)
+            stack.push_back({ c1, nr.y });
+        if (c0 >= 0)
+            stack.push_back({ c0, nr.x });
+    }
+}
+
 void coverBoxes(const BNode* nodes, uint32_t avail, int32_t root, const float* bounds, std::vector<float>& out)
 {
     const int kCoverDepth = 5;
@@ -608,13 +653,6 @@ AGB_API agb_status agb_geometry_create(agb_context* ctx, const float* positions,
             "agb_geometry_create: GPU BVH build");
         if (depth > kBlasMaxDepth)
             return fail(AGB_ERR_LIMIT, "agb_geometry_create: BLAS deeper than the traversal stack allows");
-        if (nodeCount)
-        {
-            AGB_CUDA(g->nodes.ensure(size_t(nodeCount) * sizeof(BNode)), "allocate BVH");
-            AGB_CUDA(cudaMemcpyAsync(g->nodes.ptr, s.nodes, size_t(nodeCount) * sizeof(BNode),
-                         cudaMemcpyDeviceToDevice, ctx->stream),
-                "copy BVH");
-        }
         // The builder numbers nodes level by level, so the first ones are the top of the tree.
         std::vector<BNode> top(std::min<uint32_t>(nodeCount, 255));
         if (!top.empty())
@@ -623,6 +661,31 @@ AGB_API agb_status agb_geometry_create(agb_context* ctx, const float* positions,
                 "read BVH top");
         AGB_CUDA(cudaStreamSynchronize(ctx->stream), "upload geometry");
         coverBoxes(top.data(), uint32_t(top.size()), root, g->bounds, g->cover);
+        if (nodeCount && blasLayoutDepthFirst())
+        {
+            // Depth-first order with each node's interior children side by side (see layoutDepthFirst).
+            std::vector<BNode> level(nodeCount), dfs;
+            AGB_CUDA(cudaMemcpyAsync(level.data(), s.nodes, size_t(nodeCount) * sizeof(BNode), cudaMemcpyDeviceToHost,
+                         ctx->stream),
+                "read BVH");
+            AGB_CUDA(cudaStreamSynchronize(ctx->stream), "read BVH");
+            layoutDepthFirst(level, root, dfs);
+            root      = 0;
+            nodeCount = uint32_t(dfs.size());
+            AGB_CUDA(g->nodes.ensure(size_t(nodeCount) * sizeof(BNode)), "allocate BVH");
+            AGB_CUDA(cudaMemcpyAsync(g->nodes.ptr, dfs.data(), size_t(nodeCount) * sizeof(BNode),
+                         cudaMemcpyHostToDevice, ctx->stream),
+                "upload BVH");
+            AGB_CUDA(cudaStreamSynchronize(ctx->stream), "upload BVH");
+        }
+        else if (nodeCount)
+        {
+            AGB_CUDA(g->nodes.ensure(size_t(nodeCount) * sizeof(BNode)), "allocate BVH");
+            AGB_CUDA(cudaMemcpyAsync(g->nodes.ptr, s.nodes, size_t(nodeCount) * sizeof(BNode),
+                         cudaMemcpyDeviceToDevice, ctx->stream),
+                "copy BVH");
+            AGB_CUDA(cudaStreamSynchronize(ctx->stream), "upload geometry");
+        }
         DevMesh& m      = g->mesh;
         m.positions     = g->positions.as<float>();
         m.normals       = normals ? g->normals.as<float>() : nullptr;
@@ -2440,7 +2503,9 @@ AGB_API agb_status agb_denoiser_forward(agb_denoiser* dn, const uint16_t* featur
         return fail(AGB_ERR_INVALID_ARG, "agb_denoiser_forward: null or unaligned device pointer");
     AGB_CUDA(dn->net.infer(features, batch, height, width, out_rgba), "agb_denoiser_forward");
     AGB_CUDA(cudaStreamSynchronize(dn->stream), "agb_denoiser_forward");
-    return tcStatus("agb_denoiser_forward");
+    if (dn->net.inferTimedOut())
+        return fail(AGB_ERR_TIMEOUT, "agb_denoiser_forward: tensor-core completion wait timed out");
+    return AGB_OK;
 }
 
 AGB_API agb_status agb_denoiser_train_step(agb_denoiser* dn, const uint16_t* features,

@@ -219,7 +219,10 @@ public:
     cudaError_t forward(const uint16_t* x, int B, int H, int W, bool training, float* rgba = nullptr);
     // Inference (forward with rgba) replayed from a CUDA graph of its 15 launches, captured on first
     // use for each (x, rgba, B, H, W) and kept while the activation buffers stay (a few graphs).
+    // The tensor-core timeout flag is copied to host memory behind it on the stream: after the
+    // stream is synchronised, inferTimedOut() says whether a wait ran out (the flag is then cleared).
     cudaError_t infer(const uint16_t* x, int B, int H, int W, float* rgba);
+    bool inferTimedOut();
     // After forward(training): L1 loss against target RGBA (FP32) and all parameter gradients.
     cudaError_t backward(const float* target);
     cudaError_t adam(float lr);
@@ -238,6 +241,7 @@ private:
     static size_t pixels(int B, int H, int W, int level);
     ConvLaunch layerLaunch(int i, const uint16_t* x) const;
     void dropGraphs();
+    cudaError_t inferLaunch(const uint16_t* x, int B, int H, int W, float* rgba);
 
     cudaStream_t stream_ = nullptr;
     int smCount_         = 0;
@@ -268,6 +272,7 @@ private:
     };
     std::vector<Graph> graphs_; // most recently used last
     Graph pending_{};           // buffers seen once, captured when seen again
+    int* flagHost_ = nullptr;   // pinned copy of the tensor-core timeout flag
 };
 cudaError_t launchDenoiseFeatures(const float4* mean, const float2* moments, float samples, const float4* albedo,
     const float4* normal, const float* depth, float skyZ, long P, uint16_t* out, cudaStream_t st);

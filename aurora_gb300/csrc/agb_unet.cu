@@ -283,6 +283,9 @@ void UnetDenoiser::dropGraphs()
 void UnetDenoiser::release()
 {
     dropGraphs();
+    if (flagHost_)
+        cudaFreeHost(flagHost_);
+    flagHost_ = nullptr;
     for (void* p : allocs_)
         cudaFree(p);
     allocs_.clear();
@@ -459,11 +462,39 @@ cudaError_t UnetDenoiser::forward(const uint16_t* x, int B, int H, int W, bool t
     return cudaSuccess;
 }
 
+bool UnetDenoiser::inferTimedOut()
+{
+    if (!flagHost_ || *flagHost_ == 0)
+        return false;
+    int flag = 0;
+    takeTcError(&flag);
+    *flagHost_ = 0;
+    return true;
+}
+
 cudaError_t UnetDenoiser::infer(const uint16_t* x, int B, int H, int W, float* rgba)
 {
     cudaError_t e = ensureShape(B, H, W, false);
     if (e != cudaSuccess)
         return e;
+    if (!flagHost_)
+    {
+        if ((e = cudaMallocHost(reinterpret_cast<void**>(&flagHost_), sizeof(int))) != cudaSuccess)
+            return e;
+        *flagHost_ = 0;
+    }
+    int* flagDev = nullptr;
+    if ((e = tcErrorFlag(&flagDev)) != cudaSuccess)
+        return e;
+    e = inferLaunch(x, B, H, W, rgba);
+    if (e != cudaSuccess)
+        return e;
+    return cudaMemcpyAsync(flagHost_, flagDev, sizeof(int), cudaMemcpyDeviceToHost, stream_);
+}
+
+cudaError_t UnetDenoiser::inferLaunch(const uint16_t* x, int B, int H, int W, float* rgba)
+{
+    cudaError_t e;
     for (size_t i = 0; i < graphs_.size(); i++)
     {
         Graph g = graphs_[i];

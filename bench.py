@@ -253,7 +253,7 @@ def bench_serving(api, _abi, n_requests, rates=(200.0, 25.0)):
     return out
 
 
-def bench_denoised_serving(api, _abi, train_scenes=32, views=8, steps=4000, eval_size=(1920, 1080),
+def bench_denoised_serving(api, _abi, train_scenes=48, views=8, steps=8000, eval_size=(1920, 1080),
                            ref_spp=1024, repeats=3):
     """The learned denoiser trained on the tracer's own pairs, then served: relMSE (eps 1e-2)
     against converged references of plain accumulation at 1-256 spp and of the denoised output at
