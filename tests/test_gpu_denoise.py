@@ -44,6 +44,12 @@ CASES = [
     (1, 8, 8, 32, 16, 48, True, True),
     (1, 12, 20, 128, 0, 256, False, False),
     (3, 10, 14, 64, 64, 64, True, True),
+    # edges: one row of two pixels, an odd height (a partial row tile), the smallest upsampled
+    # input (1 x 1 at half resolution), a width over three 256-pixel tiles with two channel tiles
+    (3, 1, 2, 16, 0, 32, False, True),
+    (1, 5, 6, 32, 16, 48, False, False),
+    (2, 2, 2, 16, 16, 16, True, True),
+    (1, 3, 520, 64, 0, 128, False, True),
 ]
 
 
@@ -171,6 +177,9 @@ WGRAD_CASES = [
     (1, 8, 8, 32, 16, 48, True),
     (1, 10, 12, 256, 128, 128, True),
     (3, 9, 14, 64, 0, 256, False),
+    # edges: two-pixel rows, a width over three 128-pixel units with an upsampled input
+    (2, 3, 2, 16, 0, 16, False),
+    (1, 4, 260, 32, 32, 64, True),
 ]
 
 

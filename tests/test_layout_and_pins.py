@@ -215,3 +215,30 @@ def test_temporal_jitter_pins(oracle):
             assert oracle.temporal_jitter(frame, phases) == want
             assert api.temporal_jitter(frame, phases) == want
     assert api.temporal_jitter(0) == (0.0, float(np.float32(1 / 3) - np.float32(0.5)))
+
+
+def test_conv_entry_points_reject_bad_shapes_before_touching_the_gpu():
+    """The convolution entry points check their arguments on the host: an odd width, a pooled or
+    upsampled odd height, channel counts off the 16 grid, misaligned outputs."""
+    import ctypes
+    from aurora_gb300 import _abi
+    lib = _abi.library()
+    buf = ctypes.create_string_buffer(1 << 16)
+    base = (ctypes.addressof(buf) + 255) // 256 * 256
+    p = ctypes.c_void_p(base)
+    conv = lib.agb_conv3x3_bf16
+    pool = lib.agb_conv3x3_pool_bf16
+    wgrad = lib.agb_conv3x3_wgrad_bf16
+    cases = [
+        (conv, (p, None, p, None, p, None, 1, 4, 5, 16, 0, 32, 0, 1, None), b"width must be even"),
+        (conv, (p, None, p, None, p, None, 1, 5, 4, 16, 0, 32, 1, 1, None), b"even sizes"),
+        (conv, (p, None, p, None, p, None, 1, 4, 4, 16, 0, 24, 0, 1, None), b"multiples of 16"),
+        (conv, (p, None, p, None, ctypes.c_void_p(base + 16), None, 1, 4, 4, 16, 0, 32, 0, 1, None),
+         b"32-byte aligned"),
+        (pool, (p, None, p, None, p, p, 1, 3, 4, 16, 0, 32, 0, 1, None), b"even sizes"),
+        (pool, (p, None, p, None, p, None, 1, 4, 4, 16, 0, 32, 0, 1, None), b"null pool output"),
+        (wgrad, (p, None, p, p, 1, 4, 3, 16, 0, 32, 0, None), b"width must be even"),
+    ]
+    for fn, args, why in cases:
+        assert fn(*args) == _abi.ERR_INVALID_ARG, why
+        assert why in lib.agb_last_error(), (why, lib.agb_last_error())
