@@ -649,9 +649,18 @@ private:
 
     bool compileNode(const XmlElement& node, const Scope& S, const std::string& output, Value& out, std::string& why)
     {
-        char key[96];
-        std::snprintf(key, sizeof key, "%p/%p/", static_cast<const void*>(&node), static_cast<const void*>(S.call));
-        const std::string k = key + output;
+        // Keyed by the node and the whole chain of custom-node expansions it sits in: the same
+        // element inside a nodegraph implementation takes other inputs in another expansion.
+        std::string k;
+        char part[32];
+        std::snprintf(part, sizeof part, "%p", static_cast<const void*>(&node));
+        k += part;
+        for (const Scope* q = &S; q; q = q->parent)
+        {
+            std::snprintf(part, sizeof part, "/%p", static_cast<const void*>(q->call));
+            k += part;
+        }
+        k += "/" + output;
         auto it             = cache_.find(k);
         if (it != cache_.end())
         {

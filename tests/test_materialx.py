@@ -241,3 +241,61 @@ def test_node_graph_refusals():
     assert "materialx_graph" not in out["properties"] and out["properties"]["metalness"] == 0.5
     assert "node <noise3d> is not supported" in out["warnings"]
     assert "node 'missing' not found" in out["warnings"]
+
+
+def test_nested_custom_nodes_expand_per_instance():
+    """A custom node whose implementation uses another custom node, instanced twice with
+    different interface values: each expansion evaluates its own inner nodes (a node inside an
+    implementation graph is a different value in each expansion chain)."""
+    import mtlx_graphs as mg
+    from aurora_gb300 import _abi
+    doc = """<materialx version="1.39">
+  <nodedef name="ND_scaleu" node="scaleu">
+    <input name="k" type="float" value="1.0" />
+    <output name="out" type="float" />
+  </nodedef>
+  <nodegraph name="NG_scaleu" nodedef="ND_scaleu">
+    <texcoord name="uv" type="vector2" />
+    <extract name="u" type="float">
+      <input name="in" type="vector2" nodename="uv" />
+      <input name="index" type="integer" value="0" />
+    </extract>
+    <multiply name="m" type="float">
+      <input name="in1" type="float" nodename="u" />
+      <input name="in2" type="float" interfacename="k" />
+    </multiply>
+    <output name="out" type="float" nodename="m" />
+  </nodegraph>
+  <nodedef name="ND_twice" node="twice">
+    <input name="k" type="float" value="1.0" />
+    <output name="out" type="float" />
+  </nodedef>
+  <nodegraph name="NG_twice" nodedef="ND_twice">
+    <scaleu name="inner" type="float">
+      <input name="k" type="float" interfacename="k" />
+    </scaleu>
+    <add name="sum" type="float">
+      <input name="in1" type="float" nodename="inner" />
+      <input name="in2" type="float" nodename="inner" />
+    </add>
+    <output name="out" type="float" nodename="sum" />
+  </nodegraph>
+  <twice name="a" type="float"><input name="k" type="float" value="2.0" /></twice>
+  <twice name="b" type="float"><input name="k" type="float" value="5.0" /></twice>
+  <combine3 name="c" type="color3">
+    <input name="in1" type="float" nodename="a" />
+    <input name="in2" type="float" nodename="b" />
+    <input name="in3" type="float" value="0" />
+  </combine3>
+  <standard_surface name="S" type="surfaceshader">
+    <input name="base_color" type="color3" nodename="c" />
+  </standard_surface>
+</materialx>"""
+    out = props(doc)
+    assert out["ok"] and out["warnings"] == "", out["warnings"]
+    ops, consts, _ = mg.decode(out["properties"]["materialx_graph"])
+    uv = np.float32([[0.25, 0.5], [0.5, 0.1], [-1.0, 0.0]])
+    res = mg.evaluate(ops, consts, {_abi.GIN_TEXCOORD: uv})
+    u = uv[:, 0]
+    np.testing.assert_array_equal(res[_abi.GOUT_BASE_COLOR],
+                                  np.stack([2 * (u * 2), 2 * (u * 5), 0 * u], axis=1))
