@@ -32,39 +32,42 @@ inline unsigned gridFor(long n, int block = 256)
     return unsigned(std::min<long>(std::max<long>(g, 1), 1L << 20));
 }
 
-// gs (H x W) += 0.25 * gp (H/2 x W/2), four channels per thread.
-__global__ void k_avgpool2_grad(const float4* gp, float4* gs, int B, int H, int W, int C4)
+// The gradient of one layer's pre-activation and of its bias, from the gradient of its output:
+//   dPre[p][c] = bf16((g[p][c] + 0.25 * gp[p / 2x2][c]) * (y[p][c] > 0)),  db[c] += sum_p dPre[p][c]
+// gp (the gradient of the 2x2 average pool of y, H/2 x W/2) and y (ReLU) are optional; the bias
+// gradient sums the BF16-rounded values the weight gradient uses.  Thread i handles channels
+// 8 (i % G8) .. + 7 of pixel i / G8; the grid stride is a multiple of 256 and so of G8 (C / 8 divides
+// 256), so a thread keeps its channel group and the block reduces per channel in shared memory.
+__global__ void __launch_bounds__(256) k_preact_grad(const float4* g, const float4* gp, const uint4* y, uint4* dpre,
+    float* db, int B, int H, int W, int C)
 {
-    const long n = long(B) * H * W * C4;
-    for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x)
-    {
-        const int c = int(i % C4);
-        long t      = i / C4;
-        const int x = int(t % W);
-        t /= W;
-        const int y = int(t % H);
-        const int b = int(t / H);
-        const float4 q = gp[((size_t(b) * (H / 2) + y / 2) * (W / 2) + x / 2) * C4 + c];
-        float4 o       = gs[i];
-        o.x += 0.25f * q.x;
-        o.y += 0.25f * q.y;
-        o.z += 0.25f * q.z;
-        o.w += 0.25f * q.w;
-        gs[i] = o;
-    }
-}
-
-// dPre = bf16(g * (y > 0)) (or bf16(g) without ReLU), eight values per thread.
-__global__ void k_relu_grad(const float4* g, const uint4* y, uint4* dpre, long n8)
-{
-    for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n8; i += long(gridDim.x) * blockDim.x)
+    __shared__ float part[256][8];
+    const int G8   = C / 8;
+    const long n8  = long(B) * H * W * G8;
+    const int t    = threadIdx.x;
+    float acc[8]   = {};
+    for (long i = blockIdx.x * 256L + t; i < n8; i += long(gridDim.x) * 256)
     {
         const float4 g0 = g[2 * i], g1 = g[2 * i + 1];
         float v[8]      = { g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w };
+        if (gp)
+        {
+            const long pix = i / G8;
+            const int x    = int(pix % W);
+            const long r   = pix / W;
+            const int yy   = int(r % H);
+            const long b   = r / H;
+            const long q   = ((b * (H / 2) + yy / 2) * (W / 2) + x / 2) * G8 + (i - pix * G8);
+            const float4 p0 = gp[2 * q], p1 = gp[2 * q + 1];
+            const float pv[8] = { p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w };
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+                v[k] += 0.25f * pv[k];
+        }
         if (y)
         {
-            const uint4 yy      = y[i];
-            const uint32_t w[4] = { yy.x, yy.y, yy.z, yy.w };
+            const uint4 yv      = y[i];
+            const uint32_t w[4] = { yv.x, yv.y, yv.z, yv.w };
 #pragma unroll
             for (int k = 0; k < 4; k++)
             {
@@ -77,36 +80,13 @@ __global__ void k_relu_grad(const float4* g, const uint4* y, uint4* dpre, long n
         uint32_t o[4];
 #pragma unroll
         for (int k = 0; k < 4; k++)
+        {
             o[k] = uint32_t(tobf(v[2 * k])) | (uint32_t(tobf(v[2 * k + 1])) << 16);
+            acc[2 * k] += __uint_as_float(o[k] << 16);
+            acc[2 * k + 1] += __uint_as_float(o[k] & 0xFFFF0000u);
+        }
         dpre[i] = make_uint4(o[0], o[1], o[2], o[3]);
     }
-}
-
-// db[c] += sum over pixels of dPre[p][c]: thread t of a block sums channels 8 (t % G8) .. + 7 over
-// pixels t / G8, t / G8 + L / G8, ... of the block's range (L = the threads in use); the block
-// then reduces per channel in shared memory and adds to db.
-__global__ void __launch_bounds__(256) k_bias_grad(const uint4* dpre, float* db, long P, int C, long pixPerBlock)
-{
-    __shared__ float part[256][8];
-    const int G8    = C / 8;
-    const int lanes = 256 / G8 * G8;
-    const int t     = threadIdx.x;
-    const int cg    = t % G8;
-    const long p0   = blockIdx.x * pixPerBlock;
-    const long p1   = p0 + pixPerBlock < P ? p0 + pixPerBlock : P;
-    float acc[8]    = {};
-    if (t < lanes)
-        for (long p = p0 + t / G8; p < p1; p += lanes / G8)
-        {
-            const uint4 v       = dpre[p * G8 + cg];
-            const uint32_t w[4] = { v.x, v.y, v.z, v.w };
-#pragma unroll
-            for (int k = 0; k < 4; k++)
-            {
-                acc[2 * k] += __uint_as_float(w[k] << 16);
-                acc[2 * k + 1] += __uint_as_float(w[k] & 0xFFFF0000u);
-            }
-        }
 #pragma unroll
     for (int k = 0; k < 8; k++)
         part[t][k] = acc[k];
@@ -114,7 +94,7 @@ __global__ void __launch_bounds__(256) k_bias_grad(const uint4* dpre, float* db,
     for (int c = t; c < C; c += 256)
     {
         float sum = 0.f;
-        for (int u = c / 8; u < lanes; u += G8)
+        for (int u = c / 8; u < 256; u += G8)
             sum += part[u][c % 8];
         atomicAdd(db + c, sum);
     }
@@ -556,15 +536,17 @@ cudaError_t UnetDenoiser::backward(const float* target)
         const int cin = layerCin(i), cout = layerCout(i);
         const long Pl = long(pixels(B_, H_, W_, L.level));
         const float* gy = L.out >= 0 ? grad_[L.out] : gOut_;
-        k_relu_grad<<<gridFor(Pl * cout / 8), 256, 0, stream_>>>(reinterpret_cast<const float4*>(gy),
+        // The 2x2 pools of layers 1, 3 and 5 (S -> P): their gradient reaches S here, at half
+        // resolution, beside the gradient from the skip connection.
+        const bool pooled = i == 1 || i == 3 || i == 5;
+        const long n8     = Pl * cout / 8;
+        k_preact_grad<<<unsigned(std::min<long>((n8 + 255) / 256, 8L * smCount_)), 256, 0, stream_>>>(
+            reinterpret_cast<const float4*>(gy), pooled ? reinterpret_cast<const float4*>(grad_[L.out + 1]) : nullptr,
             L.relu ? reinterpret_cast<const uint4*>(act_[L.out]) : nullptr, reinterpret_cast<uint4*>(dpre_),
-            Pl * cout / 8);
+            grads_ + bOff_[i], B_, H_ >> L.level, W_ >> L.level, cout);
         ConvLaunch c = layerLaunch(i, input_);
         if ((e = launchConvWgrad(c, dpre_, grads_ + wOff_[i], smCount_, stream_)) != cudaSuccess)
             return e;
-        const long per = std::max(256L, (Pl + 1023) / 1024);
-        k_bias_grad<<<unsigned((Pl + per - 1) / per), 256, 0, stream_>>>(reinterpret_cast<const uint4*>(dpre_),
-            grads_ + bOff_[i], Pl, cout, per);
         if (i > 0)
         {
             // dX = the convolution of dPre with the flipped weights, added straight into the
@@ -583,14 +565,6 @@ cudaError_t UnetDenoiser::backward(const float* target)
             d.gradUp = L.up0;
             if ((e = launchConv3x3(d, stream_)) != cudaSuccess)
                 return e;
-        }
-        int poolSrc = i == 2 ? A_S0 : i == 4 ? A_S1 : i == 6 ? A_S2 : -1;
-        if (poolSrc >= 0)
-        {
-            int lv = kActLevel[poolSrc], Hs = H_ >> lv, Ws = W_ >> lv, C = kActChannels[poolSrc];
-            k_avgpool2_grad<<<gridFor(long(B_) * Hs * Ws * C / 4), 256, 0, stream_>>>(
-                reinterpret_cast<const float4*>(grad_[poolSrc + 1]), reinterpret_cast<float4*>(grad_[poolSrc]), B_, Hs,
-                Ws, C / 4);
         }
     }
     return cudaGetLastError();

@@ -109,8 +109,8 @@ def denoiser_flops_per_pixel(training=False):
 
 
 def bench_denoiser(torch, _abi, stream, peaks):
-    """Tensor-core U-Net: 1920x1080 inference and a 4 x 256^2 training step, CUDA events on the
-    denoiser's stream after warm-up."""
+    """Tensor-core U-Net: 1920x1080 inference and training steps on 4 and 16 crops of 256^2, CUDA
+    events on the denoiser's stream after warm-up."""
     import ctypes
     lib = _abi.library()
     h = ctypes.c_void_p()
@@ -118,7 +118,8 @@ def bench_denoiser(torch, _abi, stream, peaks):
     out = {}
     try:
         for tag, (B, H, W), train in (("inference_1080p", (1, 1080, 1920), False),
-                                      ("training_4x256", (4, 256, 256), True)):
+                                      ("training_4x256", (4, 256, 256), True),
+                                      ("training_16x256", (16, 256, 256), True)):
             x = torch.zeros((B, H, W, 16), dtype=torch.int16, device="cuda")
             x[..., :10] = 0x3F00  # 0.5 in BF16
             rgba = torch.zeros((B, H, W, 4), dtype=torch.float32, device="cuda")
