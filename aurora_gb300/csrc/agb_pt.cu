@@ -92,8 +92,9 @@ __global__ void k_camera(agb_frame_data f, WaveParams wp, WaveBuffers wb, BatchT
             bt.pathReq[p] = uint16_t(r);
         }
         const agb_frame_data& F = kBatch ? bt.frames[r] : f;
-        uint32_t pixel = local % pixels;
-        uint32_t k     = local / pixels;
+        uint32_t samples = kBatch ? bt.req[r].samples : wp.samples;
+        uint32_t pixel   = pathPixel(local, pixels, samples);
+        uint32_t k       = pathSample(local, pixels, samples);
         uint32_t px = pixel % width, py = pixel / width;
         Rng rng     = rngInit(sampleBase + k + seedOffset, width, px, py);
         v3 o, d;
@@ -442,7 +443,7 @@ AGB_D void loadShadePoint(const DevScene& s, const float4* sp, uint32_t stride, 
 // path's request's for a batched one.
 struct PathRequest
 {
-    uint32_t local, pixels, width, sampleBase, aovSample;
+    uint32_t local, pixels, samples, width, sampleBase, aovSample;
     int32_t traceDepth;
     float* aovDepth;
     float4* aovNormal;
@@ -457,13 +458,13 @@ AGB_D PathRequest pathRequest(const WaveParams& wp, const WaveBuffers& wb, const
     {
         r                     = bt.pathReq[p];
         const BatchRequest& q = bt.req[r];
-        return PathRequest{ p - q.pathOffset, q.pixels, q.width, q.sampleBase, q.aovSample, q.traceDepth,
+        return PathRequest{ p - q.pathOffset, q.pixels, q.samples, q.width, q.sampleBase, q.aovSample, q.traceDepth,
             q.aovDepth, q.aovNormal, q.aovAlbedo, q.aovMotion };
     }
     else
     {
         r = 0;
-        return PathRequest{ p, wp.pixels, wp.width, wp.sampleBase, wp.aovSample, depth, wb.aovDepth,
+        return PathRequest{ p, wp.pixels, wp.samples, wp.width, wp.sampleBase, wp.aovSample, depth, wb.aovDepth,
             wb.aovNormal, wb.aovAlbedo, wb.aovMotion };
     }
 }
@@ -509,7 +510,7 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
             v3 contrib = v3{ c4.x, c4.y, c4.z };
             uint32_t rayType = pfRayType(flags);
             bool primary = (flags & PF_PRIMARY) != 0;
-            uint32_t pixel = q.local % q.pixels;
+            uint32_t pixel = pathPixel(q.local, q.pixels, q.samples);
             v2 pixel2 = v2{ float(pixel % q.width), float(pixel / q.width) };
             bool bg = primary || rayType == TRANSMISSION_LOBE || rayType == GROUND_PLANE_REFLECTION_RAY;
             // A batched request whose trace depth is this bounce takes the depth-limit segment here.
@@ -524,7 +525,7 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade(DevScene
             {
                 float4 h  = wb.hitTUV[i];
                 int32_t inst = wb.hitInst[i];
-                bool aov = primary && q.sampleBase + q.local / q.pixels == q.aovSample;
+                bool aov = primary && q.sampleBase + pathSample(q.local, q.pixels, q.samples) == q.aovSample;
                 if (inst < 0)
                 {
                     if (aov)
@@ -880,7 +881,7 @@ __global__ void __launch_bounds__(kShadeBlock, kShadeMinBlocks) k_shade_mis(DevS
             const DevScene& S   = kBatch ? bt.scenes[bt.req[r].scene] : s;
             const v2 screen     = kBatch ? v2{ float(bt.req[r].width), float(bt.req[r].height) }
                                          : v2{ float(wp.width), float(wp.height) };
-            uint32_t pixel = q.local % q.pixels;
+            uint32_t pixel = pathPixel(q.local, q.pixels, q.samples);
             v2 pixel2      = v2{ float(pixel % q.width), float(pixel / q.width) };
             float4* pslot  = wb.pendSlot + size_t(p) * kMaxShadowSlots;
             float4* pdir   = wb.shDir + size_t(p) * kMaxShadowSlots;
@@ -1159,10 +1160,10 @@ __global__ void k_ground(DevScene s, agb_frame_data f, WaveParams wp, WaveBuffer
                 {
                     wb.hitInst[i] = kGroundAbsorbed;
                     wb.flags[p]   = pfSetRayType(wb.flags[p] & ~PF_PRIMARY, GROUND_PLANE_REFLECTION_RAY);
-                    if (wp.sampleBase + p / wp.pixels == wp.aovSample)
+                    if (wp.sampleBase + pathSample(p, wp.pixels, wp.samples) == wp.aovSample)
                     {
                         // writeGroundPlaneGuideAOVs (GroundPlane.slang:197-233).
-                        uint32_t pixel      = p % wp.pixels;
+                        uint32_t pixel      = pathPixel(p, wp.pixels, wp.samples);
                         float vz            = viewDepth(f.camera_inv_view, hitPos);
                         wb.aovDepth[pixel]  = vz;
                         wb.aovNormal[pixel] = make_float4(N.x, N.y, N.z, fmaxf_(g.reflectionRoughness, 0.05f));
@@ -1214,14 +1215,15 @@ __global__ void k_ground_shadow(DevScene s, WaveBuffers wb, int bounce)
     }
 }
 
-// Per pixel: final radiance of each sample of the wave in sample order, then accumulation.
-// One pixel of k_finalize: the final radiance of each of the wave's samples in sample order, then
-// the accumulation (paths of the pixel at pathBase + k x pixels + pixel).
-AGB_D void finalizePixelImpl(const agb_frame_data& f, const WaveParams& wp, const WaveBuffers& wb, uint32_t pixel,
-    uint32_t pathBase)
+// The per-pixel accumulation of k_finalize: begin() reads the pixel's accumulation state, add()
+// takes the wave's samples in sample order, end() writes the state back.
+struct PixelAccum
 {
+    float4 mean, sum, comp, res;
+    float2 mom;
+    AGB_D void begin(const WaveParams& wp, const WaveBuffers& wb, uint32_t pixel)
     {
-        float4 mean = make_float4(0.f, 0.f, 0.f, 0.f), sum = mean, comp = mean;
+        mean = sum = comp = make_float4(0.f, 0.f, 0.f, 0.f);
         if ((wp.accumMode & AGB_ACCUM_RUNNING_MEAN) && wp.sampleBase > 0)
             mean = wb.accumMean[pixel];
         if ((wp.accumMode & AGB_ACCUM_KAHAN) && wp.sampleBase > 0)
@@ -1229,53 +1231,52 @@ AGB_D void finalizePixelImpl(const agb_frame_data& f, const WaveParams& wp, cons
             sum  = wb.accumSum[pixel];
             comp = wb.accumComp[pixel];
         }
-        float4 res = mean;
-        float2 mom = make_float2(0.f, 0.f);
+        res = mean;
+        mom = make_float2(0.f, 0.f);
         if ((wp.accumMode & AGB_ACCUM_MOMENTS) && wp.sampleBase > 0)
             mom = wb.accumMoments[pixel];
-        for (uint32_t k = 0; k < wp.samples; k++)
+    }
+    // r: the sample's final radiance (rgb) and alpha; s: its sample index.
+    AGB_D void add(const WaveParams& wp, float4 r, uint32_t s)
+    {
+        res = r;
+        if (wp.accumMode & AGB_ACCUM_MOMENTS)
         {
-            uint32_t p = pathBase + k * wp.pixels + pixel;
-            float4 a = wb.outDirect[p], b = wb.outDiffuse[p], c = wb.outGlossy[p];
-            v3 fin = (v3{ a.x, a.y, a.z } + v3{ b.x, b.y, b.z }) + v3{ c.x, c.y, c.z };
-            adjustRadiance(f.max_luminance, f.is_display_errors_enabled != 0, fin);
-            res = make_float4(fin.x, fin.y, fin.z, (wb.flags[p] & PF_ALPHA) ? 1.f : 0.f);
-            uint32_t s = wp.sampleBase + k;
-            if (wp.accumMode & AGB_ACCUM_MOMENTS)
+            float l = luminance(v3{ r.x, r.y, r.z });
+            mom     = make_float2(mom.x + l, mom.y + l * l);
+        }
+        if (wp.accumMode & AGB_ACCUM_RUNNING_MEAN)
+        {
+            if (s == 0)
+                mean = res;
+            else
             {
-                float l = luminance(fin);
-                mom     = make_float2(mom.x + l, mom.y + l * l);
-            }
-            if (wp.accumMode & AGB_ACCUM_RUNNING_MEAN)
-            {
-                if (s == 0)
-                    mean = res;
-                else
-                {
-                    float t  = __fdiv_rn(1.f, float(s + 1));
-                    float om = __fsub_rn(1.f, t);
-                    mean = make_float4(__fadd_rn(__fmul_rn(mean.x, om), __fmul_rn(res.x, t)),
-                        __fadd_rn(__fmul_rn(mean.y, om), __fmul_rn(res.y, t)),
-                        __fadd_rn(__fmul_rn(mean.z, om), __fmul_rn(res.z, t)),
-                        __fadd_rn(__fmul_rn(mean.w, om), __fmul_rn(res.w, t)));
-                }
-            }
-            if (wp.accumMode & AGB_ACCUM_KAHAN)
-            {
-                // Kahan-compensated sum: y = x - c; t = sum + y; c = (t - sum) - y; sum = t.
-                float* sp = &sum.x;
-                float* cp = &comp.x;
-                const float* xp = &res.x;
-#pragma unroll
-                for (int q = 0; q < 4; q++)
-                {
-                    float y  = __fsub_rn(xp[q], cp[q]);
-                    float tt = __fadd_rn(sp[q], y);
-                    cp[q]    = __fsub_rn(__fsub_rn(tt, sp[q]), y);
-                    sp[q]    = tt;
-                }
+                float t  = __fdiv_rn(1.f, float(s + 1));
+                float om = __fsub_rn(1.f, t);
+                mean = make_float4(__fadd_rn(__fmul_rn(mean.x, om), __fmul_rn(res.x, t)),
+                    __fadd_rn(__fmul_rn(mean.y, om), __fmul_rn(res.y, t)),
+                    __fadd_rn(__fmul_rn(mean.z, om), __fmul_rn(res.z, t)),
+                    __fadd_rn(__fmul_rn(mean.w, om), __fmul_rn(res.w, t)));
             }
         }
+        if (wp.accumMode & AGB_ACCUM_KAHAN)
+        {
+            // Kahan-compensated sum: y = x - c; t = sum + y; c = (t - sum) - y; sum = t.
+            float* sp = &sum.x;
+            float* cp = &comp.x;
+            const float* xp = &res.x;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+            {
+                float y  = __fsub_rn(xp[q], cp[q]);
+                float tt = __fadd_rn(sp[q], y);
+                cp[q]    = __fsub_rn(__fsub_rn(tt, sp[q]), y);
+                sp[q]    = tt;
+            }
+        }
+    }
+    AGB_D void end(const WaveParams& wp, const WaveBuffers& wb, uint32_t pixel) const
+    {
         if (wp.accumMode & AGB_ACCUM_MOMENTS)
             wb.accumMoments[pixel] = mom;
         if (wp.accumMode & AGB_ACCUM_RUNNING_MEAN)
@@ -1288,7 +1289,65 @@ AGB_D void finalizePixelImpl(const agb_frame_data& f, const WaveParams& wp, cons
         if (wb.lastSample)
             wb.lastSample[pixel] = res;
     }
+};
+
+// The final radiance of path p (adjustRadiance of its direct + diffuse + glossy sum) and its alpha.
+AGB_D float4 finalRadiance(const agb_frame_data& f, const WaveBuffers& wb, uint32_t p)
+{
+    float4 a = wb.outDirect[p], b = wb.outDiffuse[p], c = wb.outGlossy[p];
+    v3 fin = (v3{ a.x, a.y, a.z } + v3{ b.x, b.y, b.z }) + v3{ c.x, c.y, c.z };
+    adjustRadiance(f.max_luminance, f.is_display_errors_enabled != 0, fin);
+    return make_float4(fin.x, fin.y, fin.z, (wb.flags[p] & PF_ALPHA) ? 1.f : 0.f);
 }
+
+// One pixel of k_finalize: the final radiance of each of the wave's samples in sample order, then
+// the accumulation (paths of the pixel at pathBase + pathOf(pixel, k)).
+AGB_D void finalizePixelImpl(const agb_frame_data& f, const WaveParams& wp, const WaveBuffers& wb, uint32_t pixel,
+    uint32_t pathBase)
+{
+    PixelAccum acc;
+    acc.begin(wp, wb, pixel);
+    for (uint32_t k = 0; k < wp.samples; k++)
+        acc.add(wp, finalRadiance(f, wb, pathBase + pathOf(pixel, k, wp.pixels, wp.samples)), wp.sampleBase + k);
+    acc.end(wp, wb, pixel);
+}
+
+#if AGB_SAMPLE_INNER
+// Single-scene waves with a pixel's samples side by side: the paths of a block's 256 pixels are
+// one contiguous range, read in chunks of kFinalChunk samples per pixel by consecutive threads
+// (whole 128-byte lines) into shared memory, from which each thread accumulates its pixel.
+constexpr int kFinalChunk = 8;
+__global__ void __launch_bounds__(256) k_finalize_staged(agb_frame_data f, WaveParams wp, WaveBuffers wb)
+{
+    __shared__ float4 stage[256 * (kFinalChunk + 1)];
+    const uint32_t S = wp.samples;
+    for (uint32_t pix0 = blockIdx.x * 256u; pix0 < wp.pixels; pix0 += gridDim.x * 256u)
+    {
+        const uint32_t npix  = min(256u, wp.pixels - pix0);
+        const uint32_t pixel = pix0 + threadIdx.x;
+        const bool valid     = threadIdx.x < npix;
+        PixelAccum acc;
+        if (valid)
+            acc.begin(wp, wb, pixel);
+        for (uint32_t k0 = 0; k0 < S; k0 += kFinalChunk)
+        {
+            const uint32_t kc = min(uint32_t(kFinalChunk), S - k0);
+            __syncthreads();
+            for (uint32_t e = threadIdx.x; e < npix * kc; e += 256)
+            {
+                const uint32_t j = e / kc, kk = e - j * kc;
+                stage[j * (kFinalChunk + 1) + kk] = finalRadiance(f, wb, (pix0 + j) * S + k0 + kk);
+            }
+            __syncthreads();
+            if (valid)
+                for (uint32_t kk = 0; kk < kc; kk++)
+                    acc.add(wp, stage[threadIdx.x * (kFinalChunk + 1) + kk], wp.sampleBase + k0 + kk);
+        }
+        if (valid)
+            acc.end(wp, wb, pixel);
+    }
+}
+#endif
 
 template <bool kBatch>
 __global__ void k_finalize(agb_frame_data f, WaveParams wp, WaveBuffers wbIn, BatchTables bt)
@@ -1531,7 +1590,12 @@ void launchWaveT(const DevScene& s, const agb_frame_data& f, const WaveParams& w
             cur ^= 1;
     }
     mark(KC_FINALIZE);
-    k_finalize<kBatch><<<grid, 256, 0, st>>>(f, wp, wb, bt);
+#if AGB_SAMPLE_INNER
+    if (!kBatch)
+        k_finalize_staged<<<grid, 256, 0, st>>>(f, wp, wb);
+    else
+#endif
+        k_finalize<kBatch><<<grid, 256, 0, st>>>(f, wp, wb, bt);
     launches++;
     mark(KC_END);
 }

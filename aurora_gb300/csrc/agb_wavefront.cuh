@@ -1,12 +1,32 @@
 // Wavefront path-tracer state: the per-path and per-queue arrays that live in HBM between the
-// kernels of one wave.  A wave holds `samples` consecutive sample indices for every pixel; path
-// p covers pixel p % pixels and sample sampleBase + p / pixels.
+// kernels of one wave.  A wave holds `samples` consecutive sample indices for every pixel; with
+// the samples of a pixel side by side (the default), path p covers pixel p / samples and sample
+// sampleBase + p % samples, so the 32 lanes of a warp start on one pixel's samples.
 #pragma once
 
 #include "agb_trace.cuh"
 
+#ifndef AGB_SAMPLE_INNER
+#define AGB_SAMPLE_INNER 1
+#endif
+
 namespace agb
 {
+
+// Path layout within a wave (or a batched request's range of the wave): AGB_SAMPLE_INNER = 1
+// puts a pixel's samples in consecutive paths, 0 the pixels of one sample.
+AGB_D uint32_t pathPixel(uint32_t local, uint32_t pixels, uint32_t samples)
+{
+    return AGB_SAMPLE_INNER ? local / samples : local % pixels;
+}
+AGB_D uint32_t pathSample(uint32_t local, uint32_t pixels, uint32_t samples)
+{
+    return AGB_SAMPLE_INNER ? local % samples : local / pixels;
+}
+AGB_D uint32_t pathOf(uint32_t pixel, uint32_t k, uint32_t pixels, uint32_t samples)
+{
+    return AGB_SAMPLE_INNER ? pixel * samples + k : k * pixels + pixel;
+}
 
 constexpr int kShadePointWords = 10; // float4 per shading point handed between the shading kernels
 constexpr int kMisWords        = 3;  // float4 of the environment-MIS sample per shading point
