@@ -233,7 +233,7 @@ constexpr int32_t kDone = int32_t(0x80000001);
 AGB_D bool isLeafRef(int32_t ref) { return uint32_t(ref) - uint32_t(kDone + 1) < 0x7fffffffu - 1u; }
 
 #ifndef AGB_TRACE_PARK
-#define AGB_TRACE_PARK 2
+#define AGB_TRACE_PARK 1
 #endif
 #ifndef AGB_NODE_EXIT
 #define AGB_NODE_EXIT 8
@@ -250,7 +250,7 @@ AGB_D void ldg256(const float4* p, float4& a, float4& b)
         : "l"(p));
 }
 #ifndef AGB_SHADOW_PARK
-#define AGB_SHADOW_PARK AGB_TRACE_PARK
+#define AGB_SHADOW_PARK 2
 #endif
 #ifndef AGB_SHADOW_NODE_EXIT
 #define AGB_SHADOW_NODE_EXIT AGB_NODE_EXIT
