@@ -546,6 +546,34 @@ private:
                 return c.get();
         return nullptr;
     }
+    // An image file sampled at uv (an image node's file input; its colour space decides the sRGB
+    // decode, filtertype "closest" nearest sampling): the IMAGE operation on the graph's image list.
+    Value sampleFile(const XmlElement& node, const XmlElement& file, Value uv, int n)
+    {
+        std::string path = file.attr("value");
+        if (!path.empty() && path[0] != '/' && !base_.empty())
+            path = base_ + path;
+        const std::string sp = file.has("colorspace") ? file.attr("colorspace")
+            : node.has("colorspace")                       ? node.attr("colorspace")
+                                                           : space_;
+        const bool linearize  = sp == "srgb_texture";
+        const XmlElement* ft  = childInput(node, "filtertype");
+        const bool nearest    = ft && ft->attr("value") == "closest";
+        const std::string img = "MaterialXImage/" + path + ":linearize:" + (linearize ? "1" : "0");
+        int index             = -1;
+        for (size_t q = 0; q < imagePaths_.size(); q++)
+            if (imagePaths_[q] == img + (nearest ? ":nearest" : ""))
+                index = int(q);
+        if (index < 0)
+        {
+            index = int(imagePaths_.size());
+            imagePaths_.push_back(img + (nearest ? ":nearest" : ""));
+            images_.push_back(MaterialXImage{ "materialx_graph", img, path, linearize });
+        }
+        Value out{ reg(), std::min(n, 4) };
+        emit(AGB_GOP_IMAGE, out.reg, uv.reg, 0, 0, 0, uint16_t(index));
+        return out;
+    }
     const XmlElement* nodedefFor(const std::string& category) const
     {
         for (auto& c : root_.children)
@@ -931,28 +959,59 @@ private:
                     return false;
                 uv = op2(AGB_GOP_ADD, op2(AGB_GOP_MUL, uv, tiling), offset);
             }
-            std::string path = file->attr("value");
-            if (!path.empty() && path[0] != '/' && !base_.empty())
-                path = base_ + path;
-            const std::string sp = file->has("colorspace") ? file->attr("colorspace")
-                : node.has("colorspace")                       ? node.attr("colorspace")
-                                                               : space_;
-            const bool linearize  = sp == "srgb_texture";
-            const XmlElement* ft  = childInput(node, "filtertype");
-            const bool nearest    = ft && ft->attr("value") == "closest";
-            const std::string img = "MaterialXImage/" + path + ":linearize:" + (linearize ? "1" : "0");
-            int index             = -1;
-            for (size_t q = 0; q < imagePaths_.size(); q++)
-                if (imagePaths_[q] == img + (nearest ? ":nearest" : ""))
-                    index = int(q);
-            if (index < 0)
+            out = sampleFile(node, *file, uv, n);
+            return true;
+        }
+        if (cat == "adsk:bitmap" || cat == "adsk:normal_map")
+        {
+            // Autodesk's texture nodes (their node library is not part of the reference): the file
+            // at texcoord x uv_scale + uv_offset; a bitmap's value scaled by rgbamount and, with
+            // invert, subtracted from 1; a normal map's tangent-space normal with its xy scaled by
+            // normal_scale.  The real-world mapping (realworld_scale / realworld_offset, in
+            // document distance units) and rotation_angle are not applied.
+            const XmlElement* file = childInput(node, "file");
+            if (!file || !file->has("value"))
             {
-                index = int(imagePaths_.size());
-                imagePaths_.push_back(img + (nearest ? ":nearest" : ""));
-                images_.push_back(MaterialXImage{ "materialx_graph", img, path, linearize });
+                why = "node <" + cat + "> has no file";
+                return false;
             }
-            out = Value{ reg(), std::min(n, 4) };
-            emit(AGB_GOP_IMAGE, out.reg, uv.reg, 0, 0, 0, uint16_t(index));
+            auto constantIs = [&](const char* name, std::vector<float> want) {
+                const XmlElement* c = childInput(node, name);
+                return !c || (c->has("value") && numbers(c->attr("value")) == want);
+            };
+            if (!constantIs("realworld_scale", { 1.f, 1.f }) || !constantIs("realworld_offset", { 0.f, 0.f }) ||
+                !constantIs("rotation_angle", { 0.f }))
+                warnings_ += "MaterialX <" + cat + "> '" + node.attr("name") +
+                    "': realworld_scale / realworld_offset / rotation_angle are not applied\n";
+            Value uv{ reg(), 2 }, scale, offset;
+            emit(AGB_GOP_INPUT, uv.reg, 0, 0, 0, 0, AGB_GIN_TEXCOORD);
+            if (!in("uv_scale", "vector2", "1, 1", scale) || !in("uv_offset", "vector2", "0, 0", offset))
+                return false;
+            uv = op2(AGB_GOP_ADD, op2(AGB_GOP_MUL, uv, scale), offset);
+            if (cat == "adsk:normal_map")
+            {
+                Value tex = sampleFile(node, *file, uv, 3);
+                if (!in("normal_scale", "float", "1", b))
+                    return false;
+                out = Value{ reg(), 3 };
+                emit(AGB_GOP_NORMALMAP, out.reg, tex.reg, b.reg, 0, 0, 0);
+                return true;
+            }
+            out = sampleFile(node, *file, uv, n);
+            if (childInput(node, "rgbamount"))
+            {
+                if (!in("rgbamount", "float", "1", a))
+                    return false;
+                out   = op2(AGB_GOP_MUL, out, a);
+                out.n = std::min(n, 4);
+            }
+            const XmlElement* inv = childInput(node, "invert");
+            if (inv && (inv->attr("value") == "true" || inv->attr("value") == "1"))
+            {
+                Value one = valueOf("float", "1", why);
+                out       = op2(AGB_GOP_SUB, one, out);
+                out.n     = std::min(n, 4);
+            }
             return true;
         }
         if (cat == "normalmap")
@@ -1057,6 +1116,76 @@ bool graphField(const std::string& input, int& field, int& n)
     return true;
 }
 
+// An adsk compound surface shader as the standard_surface it stands for: `out` receives copies of
+// the compound's inputs renamed to the Standard Surface inputs they drive (the reference's map of
+// compound interface inputs to material fields, MaterialX/MaterialGenerator.cpp:90-114), and
+// `constants` the values the compound fixes inside: metalness 1 for adsk:metal
+// (BSDFCodeGenerator.cpp:1525), transmission 1 for adsk:transparent (BSDFCodeGenerator.cpp:540),
+// thin_walled for adsk:glazing (BSDFCodeGenerator.cpp:1525-1526; a glazing is a thin
+// transmissive layer, so transmission 1 too: the reference counts a glazing_transmission_color as
+// non-opaque, MaterialGenerator.cpp:365-368); and for adsk:opaque, emission 1 when
+// opaque_emission is set with a positive opaque_luminance and subsurface 1 with
+// opaque_translucency (MaterialGenerator.cpp:315-333).
+bool adskCompound(const XmlElement& shader, XmlElement& out, Properties& constants)
+{
+    static const std::map<std::string, std::string> inputMap = {
+        { "layered_diffuse", "base_color" }, { "layered_roughness", "specular_roughness" },
+        { "layered_fraction", "coat" }, { "layered_anisotropy", "specular_anisotropy" },
+        { "layered_rotation", "specular_rotation" }, { "layered_normal", "normal" },
+        { "layered_bottom_f0", "specular_color" }, { "opaque_albedo", "base_color" }, { "metal_f0", "base_color" },
+        { "surface_roughness", "specular_roughness" }, { "surface_anisotropy", "specular_anisotropy" },
+        { "surface_rotation", "specular_rotation" }, { "surface_albedo", "coat_color" },
+        { "surface_normal", "normal" }, { "surface_cutout", "opacity" }, { "transparent_ior", "specular_IOR" },
+        { "transparent_color", "transmission_color" }, { "glazing_transmission_color", "transmission_color" },
+        { "glazing_transmission_roughness", "specular_roughness" }, { "glazing_f0", "specular_color" },
+        { "opaque_luminance_modifier", "emission_color" }, { "opaque_mfp_modifier", "subsurface_color" },
+    };
+    const std::string kind = shader.name;
+    if (kind != "adsk:opaque" && kind != "adsk:metal" && kind != "adsk:transparent" && kind != "adsk:glazing" &&
+        kind != "adsk:layered")
+        return false;
+    out.name  = "standard_surface";
+    out.attrs = shader.attrs;
+    auto value = [&](const char* name) -> std::string {
+        for (auto& c : shader.children)
+            if (c->name == "input" && c->attr("name") == name)
+                return c->attr("value");
+        return std::string();
+    };
+    for (auto& c : shader.children)
+    {
+        if (c->name != "input")
+            continue;
+        auto it = inputMap.find(c->attr("name"));
+        if (it == inputMap.end())
+            continue;
+        auto copy           = std::make_unique<XmlElement>();
+        copy->name          = c->name;
+        copy->attrs         = c->attrs;
+        copy->attrs["name"] = it->second;
+        out.children.push_back(std::move(copy));
+    }
+    if (kind == "adsk:metal")
+        constants["metalness"] = 1.f;
+    else if (kind == "adsk:transparent")
+        constants["transmission"] = 1.f;
+    else if (kind == "adsk:glazing")
+    {
+        constants["thin_walled"]  = true;
+        constants["transmission"] = 1.f;
+    }
+    else if (kind == "adsk:opaque")
+    {
+        const std::string e = value("opaque_emission"), t = value("opaque_translucency");
+        std::vector<float> lum = numbers(value("opaque_luminance"));
+        if ((e == "true" || e == "1") && lum.size() == 1 && lum[0] > 0.f)
+            constants["emission"] = 1.f;
+        if (t == "true" || t == "1")
+            constants["subsurface"] = 1.f;
+    }
+    return true;
+}
+
 } // namespace
 
 bool materialXToProperties(const std::string& document, Properties& properties, std::string& warnings)
@@ -1108,11 +1237,20 @@ bool materialXToProperties(const std::string& document, const std::string& baseD
         warnings += "MaterialX document: no surface shader\n";
         return false;
     }
+    // Autodesk's compound surface shaders (Prism materials) drive the Standard Surface fields
+    // their interface inputs map to; inputs outside the map are not used.
+    XmlElement compound;
+    Properties compoundConstants;
     if (shader->name != "standard_surface")
     {
-        warnings += "MaterialX document: surface shader <" + shader->name +
-            "> is not supported (only standard_surface)\n";
-        return false;
+        if (!adskCompound(*shader, compound, compoundConstants))
+        {
+            warnings += "MaterialX document: surface shader <" + shader->name +
+                "> is not supported (only standard_surface and the adsk:opaque, adsk:metal, adsk:transparent, "
+                "adsk:glazing and adsk:layered compounds)\n";
+            return false;
+        }
+        shader = &compound;
     }
     const std::string docSpace = root.has("colorspace") ? root.attr("colorspace") : "lin_rec709";
     GraphCompiler graphs(root, baseDirectory, docSpace, warnings, images);
@@ -1185,6 +1323,8 @@ bool materialXToProperties(const std::string& document, const std::string& baseD
         else
             warnings += "MaterialX input '" + n + "' of type " + type + " (value '" + v + "') is not supported\n";
     }
+    for (auto& kv : compoundConstants)
+        properties[kv.first] = kv.second;
     Strings program;
     if (!graphs.empty())
     {
