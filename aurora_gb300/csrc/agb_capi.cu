@@ -86,7 +86,7 @@ struct DevBuf
 
 struct Geometry
 {
-    DevBuf positions, normals, texcoords, indices, tris, nodes;
+    DevBuf positions, normals, texcoords, verts, indices, tris, nodes;
     DevMesh mesh{};
     uint32_t nodeCount = 0;
     // Boxes that together cover the mesh (6 floats each): the child boxes of the BLAS's top
@@ -542,7 +542,7 @@ AGB_API agb_status agb_context_memory(agb_context* ctx, uint64_t* bytes)
         ctx->aovAlbedo.bytes + ctx->aovMotion.bytes + ctx->taaHistory[0].bytes + ctx->taaHistory[1].bytes +
         uint64_t(ctx->envScratch.capacity) * 44 + ctx->stats.bytes;
     for (auto& g : ctx->geometries)
-        b += g->positions.bytes + g->normals.bytes + g->texcoords.bytes + g->indices.bytes +
+        b += g->positions.bytes + g->normals.bytes + g->texcoords.bytes + g->verts.bytes + g->indices.bytes +
             g->tris.bytes + g->nodes.bytes;
     for (auto& i : ctx->images)
         b += i->data.bytes;
@@ -686,10 +686,16 @@ AGB_API agb_status agb_geometry_create(agb_context* ctx, const float* positions,
                 "copy BVH");
             AGB_CUDA(cudaStreamSynchronize(ctx->stream), "upload geometry");
         }
+        AGB_CUDA(g->verts.ensure(size_t(vertex_count) * 2 * sizeof(float4)), "allocate vertex records");
+        AGB_CUDA(launchVertexRecords(g->positions.as<float>(), normals ? g->normals.as<float>() : nullptr,
+                     texcoords ? g->texcoords.as<float>() : nullptr, vertex_count, g->verts.as<float4>(), ctx->stream),
+            "build vertex records");
+        AGB_CUDA(cudaStreamSynchronize(ctx->stream), "build vertex records");
         DevMesh& m      = g->mesh;
         m.positions     = g->positions.as<float>();
         m.normals       = normals ? g->normals.as<float>() : nullptr;
         m.texcoords     = texcoords ? g->texcoords.as<float>() : nullptr;
+        m.verts         = g->verts.as<float4>();
         m.indices       = g->indices.as<uint32_t>();
         m.tris          = g->tris.as<float4>();
         m.nodes         = g->nodes.as<BNode>();
@@ -761,11 +767,16 @@ AGB_API agb_status agb_geometry_create(agb_context* ctx, const float* positions,
         st = upload(ctx, g->nodes, bvh.nodes.data(), bvh.nodes.size() * sizeof(BNode), "upload BVH");
     if (st)
         return st;
+    AGB_CUDA(g->verts.ensure(size_t(vertex_count) * 2 * sizeof(float4)), "allocate vertex records");
+    AGB_CUDA(launchVertexRecords(g->positions.as<float>(), normals ? g->normals.as<float>() : nullptr,
+                 texcoords ? g->texcoords.as<float>() : nullptr, vertex_count, g->verts.as<float4>(), ctx->stream),
+        "build vertex records");
     AGB_CUDA(cudaStreamSynchronize(ctx->stream), "upload geometry");
     DevMesh& m      = g->mesh;
     m.positions     = g->positions.as<float>();
     m.normals       = normals ? g->normals.as<float>() : nullptr;
     m.texcoords     = texcoords ? g->texcoords.as<float>() : nullptr;
+    m.verts         = g->verts.as<float4>();
     m.indices       = g->indices.as<uint32_t>();
     m.tris          = g->tris.as<float4>();
     m.nodes         = g->nodes.as<BNode>();

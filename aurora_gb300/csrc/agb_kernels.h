@@ -87,6 +87,9 @@ struct KernelMarks
 };
 
 // agb_pt.cu
+// DevMesh::verts from the mesh's attribute arrays (normals / texcoords may be null).
+cudaError_t launchVertexRecords(const float* positions, const float* normals, const float* texcoords,
+    uint32_t vertexCount, float4* verts, cudaStream_t stream);
 void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp,
     const WaveBuffers& wb, cudaStream_t st, int smCount, uint64_t& launches, KernelMarks* marks);
 // A batched wave over several requests (BatchTables): `shared` is the scenes' shared namespace,

@@ -1600,6 +1600,28 @@ void launchWaveT(const DevScene& s, const agb_frame_data& f, const WaveParams& w
     mark(KC_END);
 }
 
+__global__ void k_vertex_records(const float* pos, const float* nrm, const float* uv, uint32_t n, float4* out)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const float nx = nrm ? nrm[3 * size_t(i)] : 0.f, ny = nrm ? nrm[3 * size_t(i) + 1] : 0.f,
+                    nz = nrm ? nrm[3 * size_t(i) + 2] : 0.f;
+        const float u = uv ? uv[2 * size_t(i)] : 0.f, v = uv ? uv[2 * size_t(i) + 1] : 0.f;
+        out[2 * size_t(i)]     = make_float4(pos[3 * size_t(i)], pos[3 * size_t(i) + 1], pos[3 * size_t(i) + 2], nx);
+        out[2 * size_t(i) + 1] = make_float4(ny, nz, u, v);
+    }
+}
+
+cudaError_t launchVertexRecords(const float* positions, const float* normals, const float* texcoords,
+    uint32_t vertexCount, float4* verts, cudaStream_t stream)
+{
+    if (vertexCount == 0)
+        return cudaSuccess;
+    const uint32_t blocks = std::min<uint32_t>((vertexCount + 255) / 256, 65535u);
+    k_vertex_records<<<blocks, 256, 0, stream>>>(positions, normals, texcoords, vertexCount, verts);
+    return cudaGetLastError();
+}
+
 void launchWave(const DevScene& s, const agb_frame_data& f, const WaveParams& wp,
     const WaveBuffers& wb, cudaStream_t st, int smCount, uint64_t& launches, KernelMarks* marks)
 {

@@ -38,6 +38,9 @@ struct DevMesh
     const float* positions; // 3 per vertex
     const float* normals;   // 3 per vertex or null
     const float* texcoords; // 2 per vertex or null
+    // 2 per vertex, the attributes one shading fetch needs: (position, normal.x), (normal.y,
+    // normal.z, texcoord); normal and texcoord zero where the mesh has none.
+    const float4* verts;
     const uint32_t* indices; // 3 per triangle
     const float4* tris;     // 3 per triangle in BVH leaf order: v0 (w = triangle id as int), v1, v2
     const BNode* nodes;
@@ -258,17 +261,19 @@ AGB_D Shading computeShading(const DevScene& s, const DevInstance& in, uint32_t 
 #pragma unroll
     for (int i = 0; i < 3; i++)
     {
-        p[i] = ldg3(m.positions + 3 * size_t(sh.idx[i]));
+        // One 32-byte vertex record (two 16-byte loads of one sector) instead of eight scalar
+        // gathers from three arrays.
+        const float4 va = __ldg(m.verts + 2 * size_t(sh.idx[i])), vb = __ldg(m.verts + 2 * size_t(sh.idx[i]) + 1);
+        p[i] = v3{ va.x, va.y, va.z };
         gp += p[i] * b[i];
         if (m.normals)
         {
-            nn[i] = ldg3(m.normals + 3 * size_t(sh.idx[i]));
+            nn[i] = v3{ va.w, vb.x, vb.y };
             n += nn[i] * b[i];
         }
         if (m.texcoords)
         {
-            v2 t = v2{ __ldg(m.texcoords + 2 * size_t(sh.idx[i])),
-                __ldg(m.texcoords + 2 * size_t(sh.idx[i]) + 1) };
+            v2 t = v2{ vb.z, vb.w };
             uv = uv + t * b[i];
         }
     }
