@@ -74,7 +74,7 @@ GRAPH_OP_DTYPE = np.dtype([("op", "u1"), ("dst", "u1"), ("a", "u1"), ("b", "u1")
 GRAPH_REGS = 32
 (GOP_CONST, GOP_INPUT, GOP_ADD, GOP_SUB, GOP_MUL, GOP_DIV, GOP_MIN, GOP_MAX, GOP_POW, GOP_MOD, GOP_FLOOR,
  GOP_CEIL, GOP_ABS, GOP_SIN, GOP_COS, GOP_SQRT, GOP_SIGN, GOP_CLAMP, GOP_MIX, GOP_DOT, GOP_NORMALIZE,
- GOP_LENGTH, GOP_SWIZZLE, GOP_COMBINE, GOP_SELECT, GOP_IMAGE, GOP_NORMALMAP, GOP_OUTPUT) = range(28)
+ GOP_LENGTH, GOP_SWIZZLE, GOP_COMBINE, GOP_SELECT, GOP_IMAGE, GOP_NORMALMAP, GOP_OUTPUT, GOP_NOISE) = range(29)
 (GIN_TEXCOORD, GIN_POSITION_WORLD, GIN_POSITION_OBJECT, GIN_NORMAL_WORLD, GIN_NORMAL_OBJECT,
  GIN_TANGENT_WORLD, GIN_BITANGENT_WORLD) = range(7)
 (GOUT_BASE_COLOR, GOUT_SPECULAR_ROUGHNESS, GOUT_COAT_ROUGHNESS, GOUT_EMISSION_COLOR, GOUT_OPACITY,

@@ -979,6 +979,8 @@ AGB_API agb_status agb_material_graphs_set(agb_context* ctx, const int32_t* firs
             ok = o.imm < AGB_GOUT_COUNT;
         if (ok && o.op == AGB_GOP_SELECT)
             ok = o.imm <= 2;
+        if (ok && o.op == AGB_GOP_NOISE)
+            ok = o.imm <= 3;
         if (ok && (o.op == AGB_GOP_DOT || o.op == AGB_GOP_NORMALIZE || o.op == AGB_GOP_LENGTH))
             ok = o.d >= 1 && o.d <= 4;
         if (!ok)

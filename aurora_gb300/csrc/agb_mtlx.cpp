@@ -1095,6 +1095,77 @@ private:
             emit(AGB_GOP_MIX, out.reg, b.reg, a.reg, tc.reg, 0, 0);
             return true;
         }
+        if (cat == "noise2d" || cat == "noise3d" || cat == "fractal3d" || cat == "cellnoise2d" || cat == "cellnoise3d")
+        {
+            // MaterialX's noise nodes (stdlib genglsl): noise = perlin(p) x amplitude + pivot;
+            // fractal3d = amplitude x sum over octaves of diminish^i x perlin(p x lacunarity^i),
+            // accumulated in that order; cell noise = the cell's hash in [0, 1].  p: texcoord for
+            // the 2D nodes, object-space position for the 3D ones, by default.  Float outputs only
+            // (the colour / vector forms hash more channels).
+            if (type != "float")
+            {
+                why = "node <" + cat + "> of type " + type + " is not supported (float only)";
+                return false;
+            }
+            const bool flat = cat == "noise2d" || cat == "cellnoise2d";
+            Value pos;
+            if (childInput(node, flat ? "texcoord" : "position"))
+            {
+                if (!in(flat ? "texcoord" : "position", flat ? "vector2" : "vector3", flat ? "0, 0" : "0, 0, 0", pos))
+                    return false;
+            }
+            else
+            {
+                pos = Value{ reg(), flat ? 2 : 3 };
+                emit(AGB_GOP_INPUT, pos.reg, 0, 0, 0, 0, uint16_t(flat ? AGB_GIN_TEXCOORD : AGB_GIN_POSITION_OBJECT));
+            }
+            auto noise = [&](Value p, int kind) {
+                Value r{ reg(), 1 };
+                emit(AGB_GOP_NOISE, r.reg, p.reg, 0, 0, 0, uint16_t(kind));
+                return r;
+            };
+            if (cat == "cellnoise2d" || cat == "cellnoise3d")
+            {
+                out = noise(pos, flat ? 2 : 3);
+                return true;
+            }
+            if (!in("amplitude", "float", "1", a))
+                return false;
+            if (cat == "fractal3d")
+            {
+                const XmlElement* oc = childInput(node, "octaves");
+                if (oc && !oc->has("value"))
+                {
+                    why = "node <fractal3d> with a connected octaves input is not supported";
+                    return false;
+                }
+                std::vector<float> f = numbers(oc ? oc->attr("value") : "3");
+                const int octaves    = f.size() == 1 ? int(f[0]) : -1;
+                if (octaves < 0 || octaves > 16)
+                {
+                    why = "node <fractal3d> octaves must be 0 to 16";
+                    return false;
+                }
+                Value lac, dim;
+                if (!in("lacunarity", "float", "2", lac) || !in("diminish", "float", "0.5", dim))
+                    return false;
+                Value sum = constant({ 0.f }, 1), amp = constant({ 1.f }, 1);
+                for (int k = 0; k < octaves; k++)
+                {
+                    sum = op2(AGB_GOP_ADD, sum, op2(AGB_GOP_MUL, amp, noise(pos, 1)));
+                    amp = op2(AGB_GOP_MUL, amp, dim);
+                    pos = op2(AGB_GOP_MUL, pos, lac);
+                }
+                out   = op2(AGB_GOP_MUL, a, sum);
+                out.n = 1;
+                return true;
+            }
+            if (!in("pivot", "float", "0", b))
+                return false;
+            out   = op2(AGB_GOP_ADD, op2(AGB_GOP_MUL, noise(pos, flat ? 0 : 1), a), b);
+            out.n = 1;
+            return true;
+        }
         why = "node <" + cat + "> is not supported";
         return false;
     }

@@ -320,6 +320,91 @@ AGB_D bool materialTexture(const DevScene& s, int32_t mat, int slot, v2 uv, cons
     return true;
 }
 
+// MaterialX's noise functions (stdlib genglsl mx_noise.glsl, after Open Shading Language's noise):
+// Bob Jenkins' lookup3 "final" mix of the lattice point (seeded 0xdeadbeef + 4 n + 13 for n
+// coordinates) as the hash; Perlin's improved noise (gradients from the hash's low bits, fade
+// 6t^5 - 15t^4 + 10t^3, bi- / trilinear blend) scaled by 0.6616 in 2D and 0.9820 in 3D; cell noise
+// = the cell's hash / 0xffffffff.
+namespace mxNoise
+{
+AGB_D uint32_t rotl(uint32_t x, int k) { return (x << k) | (x >> (32 - k)); }
+AGB_D uint32_t final3(uint32_t a, uint32_t b, uint32_t c)
+{
+    c ^= b;
+    c -= rotl(b, 14);
+    a ^= c;
+    a -= rotl(c, 11);
+    b ^= a;
+    b -= rotl(a, 25);
+    c ^= b;
+    c -= rotl(b, 16);
+    a ^= c;
+    a -= rotl(c, 4);
+    b ^= a;
+    b -= rotl(a, 14);
+    c ^= b;
+    c -= rotl(b, 24);
+    return c;
+}
+AGB_D uint32_t hash2(int x, int y)
+{
+    const uint32_t s = 0xdeadbeefu + (2u << 2) + 13u;
+    return final3(s + uint32_t(x), s + uint32_t(y), s);
+}
+AGB_D uint32_t hash3(int x, int y, int z)
+{
+    const uint32_t s = 0xdeadbeefu + (3u << 2) + 13u;
+    return final3(s + uint32_t(x), s + uint32_t(y), s + uint32_t(z));
+}
+AGB_D float fade(float t) { return t * t * t * (t * (t * 6.f - 15.f) + 10.f); }
+AGB_D float negIf(float v, bool n) { return n ? -v : v; }
+AGB_D float grad2(uint32_t h, float x, float y)
+{
+    h &= 7u;
+    const float u = h < 4u ? x : y;
+    const float v = 2.f * (h < 4u ? y : x);
+    return negIf(u, h & 1u) + negIf(v, h & 2u);
+}
+AGB_D float grad3(uint32_t h, float x, float y, float z)
+{
+    h &= 15u;
+    const float u = h < 8u ? x : y;
+    const float v = h < 4u ? y : (h == 12u || h == 14u) ? x : z;
+    return negIf(u, h & 1u) + negIf(v, h & 2u);
+}
+AGB_D float perlin2(float px, float py)
+{
+    const int X = int(floorf(px)), Y = int(floorf(py));
+    const float fx = px - float(X), fy = py - float(Y);
+    const float u = fade(fx), v = fade(fy);
+    const float v0 = grad2(hash2(X, Y), fx, fy), v1 = grad2(hash2(X + 1, Y), fx - 1.f, fy);
+    const float v2 = grad2(hash2(X, Y + 1), fx, fy - 1.f), v3 = grad2(hash2(X + 1, Y + 1), fx - 1.f, fy - 1.f);
+    const float s1 = 1.f - u, t1 = 1.f - v;
+    return 0.6616f * (t1 * (v0 * s1 + v1 * u) + v * (v2 * s1 + v3 * u));
+}
+AGB_D float perlin3(float px, float py, float pz)
+{
+    const int X = int(floorf(px)), Y = int(floorf(py)), Z = int(floorf(pz));
+    const float fx = px - float(X), fy = py - float(Y), fz = pz - float(Z);
+    const float u = fade(fx), v = fade(fy), w = fade(fz);
+    const float v0 = grad3(hash3(X, Y, Z), fx, fy, fz), v1 = grad3(hash3(X + 1, Y, Z), fx - 1.f, fy, fz);
+    const float v2 = grad3(hash3(X, Y + 1, Z), fx, fy - 1.f, fz);
+    const float v3 = grad3(hash3(X + 1, Y + 1, Z), fx - 1.f, fy - 1.f, fz);
+    const float v4 = grad3(hash3(X, Y, Z + 1), fx, fy, fz - 1.f);
+    const float v5 = grad3(hash3(X + 1, Y, Z + 1), fx - 1.f, fy, fz - 1.f);
+    const float v6 = grad3(hash3(X, Y + 1, Z + 1), fx, fy - 1.f, fz - 1.f);
+    const float v7 = grad3(hash3(X + 1, Y + 1, Z + 1), fx - 1.f, fy - 1.f, fz - 1.f);
+    const float s1 = 1.f - u, t1 = 1.f - v, r1 = 1.f - w;
+    return 0.9820f * (r1 * (t1 * (v0 * s1 + v1 * u) + v * (v2 * s1 + v3 * u)) +
+                         w * (t1 * (v4 * s1 + v5 * u) + v * (v6 * s1 + v7 * u)));
+}
+AGB_D float cell2(float px, float py) { return float(hash2(int(floorf(px)), int(floorf(py)))) / float(0xffffffffu); }
+AGB_D float cell3(float px, float py, float pz)
+{
+    return float(hash3(int(floorf(px)), int(floorf(py)), int(floorf(pz)))) / float(0xffffffffu);
+}
+} // namespace mxNoise
+
 // A material's node-graph program (the operations of agb_material_graphs_set) over the hit:
 // writes the fields it drives into m / materialNormal.  Out of line, registers in local memory: it
 // runs only for materials that have a program.
@@ -445,6 +530,15 @@ static __device__ __noinline__ void runMaterialGraph(const DevScene& s, int2 pro
             v3 Bn = normalize(cross(sh.N, sh.X));
             v3 n  = normalize(sh.X * vv.x + Bn * vv.y + sh.N * vv.z);
             v     = make_float4(n.x, n.y, n.z, 0.f);
+            break;
+        }
+        case AGB_GOP_NOISE:
+        {
+            const float q = o.imm == 0 ? mxNoise::perlin2(A.x, A.y)
+                : o.imm == 1           ? mxNoise::perlin3(A.x, A.y, A.z)
+                : o.imm == 2           ? mxNoise::cell2(A.x, A.y)
+                                       : mxNoise::cell3(A.x, A.y, A.z);
+            v = make_float4(q, q, q, q);
             break;
         }
         case AGB_GOP_OUTPUT:

@@ -420,6 +420,10 @@ AGB_API agb_status agb_materials_set(agb_context* ctx, const agb_material* mater
  *   IMAGE    r[dst] = image imm sampled at r[a].xy (its own filter, repeat addressing)
  *   NORMALMAP r[dst] = normalize(T n.x + B n.y + N n.z), n = 2 r[a] - 1 with n.xy scaled by r[b].x,
  *            N the shading normal, T its tangent, B = normalize(cross(N, T))
+ *   NOISE    r[dst] = splat(noise imm at r[a]): 0 Perlin noise of r[a].xy, 1 of r[a].xyz, 2 cell noise
+ *            of r[a].xy, 3 of r[a].xyz (MaterialX's noise functions, stdlib mx_noise.glsl: the lookup3
+ *            final mix as the lattice hash, improved-noise gradients and fade, scaled 0.6616 / 0.9820;
+ *            cell noise = hash of the cell / 0xffffffff)
  *   OUTPUT   material field imm (AGB_GOUT_*) = r[a] */
 enum
 {
@@ -427,7 +431,7 @@ enum
     AGB_GOP_MAX, AGB_GOP_POW, AGB_GOP_MOD, AGB_GOP_FLOOR, AGB_GOP_CEIL, AGB_GOP_ABS, AGB_GOP_SIN,
     AGB_GOP_COS, AGB_GOP_SQRT, AGB_GOP_SIGN, AGB_GOP_CLAMP, AGB_GOP_MIX, AGB_GOP_DOT,
     AGB_GOP_NORMALIZE, AGB_GOP_LENGTH, AGB_GOP_SWIZZLE, AGB_GOP_COMBINE, AGB_GOP_SELECT,
-    AGB_GOP_IMAGE, AGB_GOP_NORMALMAP, AGB_GOP_OUTPUT, AGB_GOP_COUNT
+    AGB_GOP_IMAGE, AGB_GOP_NORMALMAP, AGB_GOP_OUTPUT, AGB_GOP_NOISE, AGB_GOP_COUNT
 };
 enum
 {

@@ -101,6 +101,88 @@ struct GroundPlaneData
     float reflectionRoughness = 0.1f;
 };
 
+
+// MaterialX's noise functions (its stdlib's mx_noise.glsl, after Open Shading Language): the
+// lattice hash is Bob Jenkins' lookup3 final mix of the integer cell (a = b = c = 0xdeadbeef +
+// 4 n + 13, plus the n coordinates); Perlin's improved noise takes gradients from the hash's low
+// bits (8 directions in 2D, 12 edges in 3D), blends them with the fade 6t^5 - 15t^4 + 10t^3 and
+// scales by 0.6616 (2D) / 0.9820 (3D); cell noise is the cell's hash / 0xffffffff.  T: float or
+// double for the blend; the hash is 32-bit integer arithmetic either way.
+template <class T>
+struct MxNoise
+{
+    static uint32_t rotl(uint32_t x, int k) { return (x << k) | (x >> (32 - k)); }
+    static uint32_t mix(uint32_t a, uint32_t b, uint32_t c)
+    {
+        c = (c ^ b) - rotl(b, 14);
+        a = (a ^ c) - rotl(c, 11);
+        b = (b ^ a) - rotl(a, 25);
+        c = (c ^ b) - rotl(b, 16);
+        a = (a ^ c) - rotl(c, 4);
+        b = (b ^ a) - rotl(a, 14);
+        c = (c ^ b) - rotl(b, 24);
+        return c;
+    }
+    static uint32_t hash(int x, int y)
+    {
+        const uint32_t init = 0xdeadbeefu + 8u + 13u;
+        return mix(init + uint32_t(x), init + uint32_t(y), init);
+    }
+    static uint32_t hash(int x, int y, int z)
+    {
+        const uint32_t init = 0xdeadbeefu + 12u + 13u;
+        return mix(init + uint32_t(x), init + uint32_t(y), init + uint32_t(z));
+    }
+    static T fade(T t) { return t * t * t * (t * (t * T(6) - T(15)) + T(10)); }
+    static T gradient(uint32_t h, T x, T y)
+    {
+        const bool low = (h & 7u) < 4u;
+        const T a = low ? x : y, b = T(2) * (low ? y : x);
+        return ((h & 1u) ? -a : a) + ((h & 2u) ? -b : b);
+    }
+    static T gradient(uint32_t h, T x, T y, T z)
+    {
+        h &= 15u;
+        const T a = h < 8u ? x : y;
+        const T b = h < 4u ? y : (h == 12u || h == 14u) ? x : z;
+        return ((h & 1u) ? -a : a) + ((h & 2u) ? -b : b);
+    }
+    static T perlin2(T px, T py)
+    {
+        const int X = int(std::floor(px)), Y = int(std::floor(py));
+        const T fx = px - T(X), fy = py - T(Y), u = fade(fx), v = fade(fy);
+        const T g00 = gradient(hash(X, Y), fx, fy), g10 = gradient(hash(X + 1, Y), fx - T(1), fy);
+        const T g01 = gradient(hash(X, Y + 1), fx, fy - T(1));
+        const T g11 = gradient(hash(X + 1, Y + 1), fx - T(1), fy - T(1));
+        const T iu = T(1) - u, iv = T(1) - v;
+        return T(0.6616f) * (iv * (g00 * iu + g10 * u) + v * (g01 * iu + g11 * u));
+    }
+    static T perlin3(T px, T py, T pz)
+    {
+        const int X = int(std::floor(px)), Y = int(std::floor(py)), Z = int(std::floor(pz));
+        const T fx = px - T(X), fy = py - T(Y), fz = pz - T(Z);
+        const T u = fade(fx), v = fade(fy), w = fade(fz);
+        T g[8];
+        for (int k = 0; k < 8; k++)
+        {
+            const int dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
+            g[k] = gradient(hash(X + dx, Y + dy, Z + dz), dx ? fx - T(1) : fx, dy ? fy - T(1) : fy,
+                dz ? fz - T(1) : fz);
+        }
+        const T iu = T(1) - u, iv = T(1) - v, iw = T(1) - w;
+        return T(0.9820f) * (iw * (iv * (g[0] * iu + g[1] * u) + v * (g[2] * iu + g[3] * u)) +
+                                w * (iv * (g[4] * iu + g[5] * u) + v * (g[6] * iu + g[7] * u)));
+    }
+    static T cell2(T px, T py)
+    {
+        return T(float(hash(int(std::floor(px)), int(std::floor(py))))) / T(float(0xffffffffu));
+    }
+    static T cell3(T px, T py, T pz)
+    {
+        return T(float(hash(int(std::floor(px)), int(std::floor(py)), int(std::floor(pz))))) / T(float(0xffffffffu));
+    }
+};
+
 template <class T>
 struct PathTracer
 {
@@ -445,6 +527,15 @@ struct PathTracer
                 v3 Bn = normalize(cross(sh.normal, sh.tangent));
                 v3 n  = normalize(sh.tangent * vv.x + Bn * vv.y + sh.normal * vv.z);
                 v     = R4{ { n.x, n.y, n.z, T(0) } };
+                break;
+            }
+            case AGB_GOP_NOISE:
+            {
+                const T q = o.imm == 0 ? MxNoise<T>::perlin2(A.v[0], A.v[1])
+                    : o.imm == 1       ? MxNoise<T>::perlin3(A.v[0], A.v[1], A.v[2])
+                    : o.imm == 2       ? MxNoise<T>::cell2(A.v[0], A.v[1])
+                                       : MxNoise<T>::cell3(A.v[0], A.v[1], A.v[2]);
+                v = R4{ { q, q, q, q } };
                 break;
             }
             case AGB_GOP_OUTPUT:

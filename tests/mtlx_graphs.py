@@ -187,6 +187,58 @@ PATTERNS = """<?xml version="1.0"?>
 """
 
 
+# Noise nodes: base_color mixed by a three-octave fractal of the object-space position,
+# specular_roughness from 2D Perlin noise of the scaled texcoord, emission from 3D cell noise.
+NOISE = """<?xml version="1.0"?>
+<materialx version="1.39">
+  <position name="p" type="vector3" />
+  <multiply name="p4" type="vector3">
+    <input name="in1" type="vector3" nodename="p" />
+    <input name="in2" type="float" value="4.0" />
+  </multiply>
+  <fractal3d name="marble" type="float">
+    <input name="position" type="vector3" nodename="p4" />
+    <input name="amplitude" type="float" value="0.8" />
+    <input name="octaves" type="integer" value="3" />
+    <input name="lacunarity" type="float" value="2.1" />
+    <input name="diminish" type="float" value="0.45" />
+  </fractal3d>
+  <add name="marble01" type="float">
+    <input name="in1" type="float" nodename="marble" />
+    <input name="in2" type="float" value="0.5" />
+  </add>
+  <mix name="veins" type="color3">
+    <input name="fg" type="color3" value="0.9, 0.85, 0.8" />
+    <input name="bg" type="color3" value="0.15, 0.2, 0.3" />
+    <input name="mix" type="float" nodename="marble01" />
+  </mix>
+  <texcoord name="uv" type="vector2" />
+  <multiply name="uv8" type="vector2">
+    <input name="in1" type="vector2" nodename="uv" />
+    <input name="in2" type="float" value="8.0" />
+  </multiply>
+  <noise2d name="grain" type="float">
+    <input name="texcoord" type="vector2" nodename="uv8" />
+    <input name="amplitude" type="float" value="0.3" />
+    <input name="pivot" type="float" value="0.45" />
+  </noise2d>
+  <cellnoise3d name="cells" type="float">
+    <input name="position" type="vector3" nodename="p4" />
+  </cellnoise3d>
+  <multiply name="glow" type="color3">
+    <input name="in1" type="color3" value="0.6, 0.3, 0.1" />
+    <input name="in2" type="float" nodename="cells" />
+  </multiply>
+  <standard_surface name="S" type="surfaceshader">
+    <input name="base_color" type="color3" nodename="veins" />
+    <input name="specular_roughness" type="float" nodename="grain" />
+    <input name="emission_color" type="color3" nodename="glow" />
+    <input name="emission" type="float" value="0.5" />
+  </standard_surface>
+</materialx>
+"""
+
+
 def decode(program):
     """The `materialx_graph` strings -> (ops GRAPH_OP_DTYPE, consts float32 (K, 4), image paths)."""
     ops, consts, images = [], [], []
@@ -222,6 +274,91 @@ def attach(s, programs):
         nk += len(consts)
     s.graphs = dict(first=first, count=count, ops=np.concatenate(all_ops),
                     consts=np.concatenate(all_k).reshape(-1, 4))
+
+
+# MaterialX's noise functions (its stdlib mx_noise.glsl, after OSL) in float32 numpy: lookup3's
+# final mix as the lattice hash, improved-noise gradients and fade, 0.6616 / 0.9820 scales.
+def _rotl(x, k):
+    return (x << np.uint32(k)) | (x >> np.uint32(32 - k))
+
+
+def _final(a, b, c):
+    c = (c ^ b) - _rotl(b, 14)
+    a = (a ^ c) - _rotl(c, 11)
+    b = (b ^ a) - _rotl(a, 25)
+    c = (c ^ b) - _rotl(b, 16)
+    a = (a ^ c) - _rotl(c, 4)
+    b = (b ^ a) - _rotl(a, 14)
+    c = (c ^ b) - _rotl(b, 24)
+    return c
+
+
+def noise_hash(*cells):
+    """lookup3-style hash of integer lattice coordinates (int arrays), as MaterialX seeds it."""
+    seed = np.uint32((0xdeadbeef + (len(cells) << 2) + 13) & 0xffffffff)
+    v = [seed + np.asarray(c).astype(np.int64).astype(np.uint32) for c in cells] + [seed] * (3 - len(cells))
+    with np.errstate(over="ignore"):
+        return _final(*[np.asarray(x, np.uint32) for x in v])
+
+
+def _fade(t):
+    f = np.float32
+    return t * t * t * (t * (t * f(6) - f(15)) + f(10))
+
+
+def _neg(v, n):
+    return np.where(n != 0, -v, v)
+
+
+def perlin2(x, y):
+    f = np.float32
+    X, Y = np.floor(x), np.floor(y)
+    fx, fy = (x - X).astype(f), (y - Y).astype(f)
+    X, Y = X.astype(np.int64), Y.astype(np.int64)
+
+    def g(h, a, b):
+        h = h & np.uint32(7)
+        lo = h < 4
+        u, v = np.where(lo, a, b), f(2) * np.where(lo, b, a)
+        return _neg(u, h & np.uint32(1)) + _neg(v, h & np.uint32(2))
+    u, v = _fade(fx), _fade(fy)
+    g0 = g(noise_hash(X, Y), fx, fy)
+    g1 = g(noise_hash(X + 1, Y), fx - f(1), fy)
+    g2 = g(noise_hash(X, Y + 1), fx, fy - f(1))
+    g3 = g(noise_hash(X + 1, Y + 1), fx - f(1), fy - f(1))
+    s1, t1 = f(1) - u, f(1) - v
+    return (f(0.6616) * (t1 * (g0 * s1 + g1 * u) + v * (g2 * s1 + g3 * u))).astype(f)
+
+
+def perlin3(x, y, z):
+    f = np.float32
+    X, Y, Z = np.floor(x), np.floor(y), np.floor(z)
+    fx, fy, fz = (x - X).astype(f), (y - Y).astype(f), (z - Z).astype(f)
+    X, Y, Z = X.astype(np.int64), Y.astype(np.int64), Z.astype(np.int64)
+
+    def g(h, a, b, c):
+        h = h & np.uint32(15)
+        u = np.where(h < 8, a, b)
+        v = np.where(h < 4, b, np.where((h == 12) | (h == 14), a, c))
+        return _neg(u, h & np.uint32(1)) + _neg(v, h & np.uint32(2))
+    gs = []
+    for k in range(8):
+        dx, dy, dz = k & 1, (k >> 1) & 1, k >> 2
+        gs.append(g(noise_hash(X + dx, Y + dy, Z + dz), fx - f(dx), fy - f(dy), fz - f(dz)))
+    u, v, w = _fade(fx), _fade(fy), _fade(fz)
+    s1, t1, r1 = f(1) - u, f(1) - v, f(1) - w
+    return (f(0.9820) * (r1 * (t1 * (gs[0] * s1 + gs[1] * u) + v * (gs[2] * s1 + gs[3] * u)) +
+                         w * (t1 * (gs[4] * s1 + gs[5] * u) + v * (gs[6] * s1 + gs[7] * u)))).astype(f)
+
+
+def cell2(x, y):
+    h = noise_hash(np.floor(x).astype(np.int64), np.floor(y).astype(np.int64))
+    return h.astype(np.float32) / np.float32(0xffffffff)
+
+
+def cell3(x, y, z):
+    h = noise_hash(np.floor(x).astype(np.int64), np.floor(y).astype(np.int64), np.floor(z).astype(np.int64))
+    return h.astype(np.float32) / np.float32(0xffffffff)
 
 
 def evaluate(ops, consts, inputs, images=()):
@@ -290,6 +427,10 @@ def evaluate(ops, consts, inputs, images=()):
                 n2 = t_ * vv[:, :1] + bn * vv[:, 1:2] + n_ * vv[:, 2:3]
                 v = np.zeros((P, 4), f32)
                 v[:, :3] = n2 / np.linalg.norm(n2, axis=1, keepdims=True)
+            elif op == _abi.GOP_NOISE:
+                q = (perlin2(A[:, 0], A[:, 1]) if imm == 0 else perlin3(A[:, 0], A[:, 1], A[:, 2]) if imm == 1
+                     else cell2(A[:, 0], A[:, 1]) if imm == 2 else cell3(A[:, 0], A[:, 1], A[:, 2]))
+                v = np.repeat(q[:, None], 4, 1)
             elif op == _abi.GOP_OUTPUT:
                 out[imm] = A[:, :3].copy()
                 continue

@@ -138,3 +138,33 @@ def test_cpp_interface_node_graph_document_matches_c_abi(agb, oracle):
     assert err < 1e-10
     # and the checker is there: the floor's pixels take both colours
     assert np.abs(img[..., :3]).max() > 0
+
+
+def test_noise_node_materials_match_oracle(agb, oracle):
+    """The noise program (fractal3d, noise2d, cellnoise3d) on the spheres and the floor: the
+    device's NOISE operations against the oracle's restatement of MaterialX's noise, whole renders."""
+    from aurora_gb300 import _abi, api, scenes
+    s = scenes.config_tiny(width=48, height=32, spp=4)
+    ops, k, _ = compile_doc(mg.NOISE, "n.mtlx")
+    assert (ops["op"] == _abi.GOP_NOISE).sum() == 5
+    mg.attach(s, {0: (ops, k, []), 2: (ops, k, []), 4: (ops, k, [])})
+    with api.Renderer() as r:
+        r.upload(s)
+        r.render(0, 4)
+        g = r.read(_abi.ACCUM_RUNNING_MEAN)
+    o = oracle.OracleScene(s).render(0, 4)
+    err = oracle.rel_mse(g, o["mean"])
+    print("noise scene: relMSE vs FP32 oracle", err)
+    assert err < 1e-6
+    o64 = oracle.OracleScene(s).render(0, 4, precision=64)
+    err64 = oracle.rel_mse(g, o64["mean"])
+    print("noise scene: relMSE vs FP64 oracle", err64)
+    # Cell noise and the lattice cells of the Perlin noise are discrete: a hit whose FP64 position
+    # lands in the neighbouring cell takes another value there.
+    assert err64 < 1e-2
+    plain = scenes.config_tiny(width=48, height=32, spp=4)
+    with api.Renderer() as r:
+        r.upload(plain)
+        r.render(0, 4)
+        p = r.read(_abi.ACCUM_RUNNING_MEAN)
+    assert oracle.rel_mse(g, p) > 1e-3

@@ -229,7 +229,7 @@ def test_node_graph_refusals():
     """A node without an implementation leaves its input at the default, with a warning; the rest
     of the document still applies."""
     doc = """<materialx version="1.39">
-  <noise3d name="n" type="float" />
+  <worleynoise3d name="n" type="float" />
   <standard_surface name="S" type="surfaceshader">
     <input name="specular_roughness" type="float" nodename="n" />
     <input name="base_color" type="color3" nodename="missing" />
@@ -239,7 +239,7 @@ def test_node_graph_refusals():
     out = props(doc)
     assert out["ok"]
     assert "materialx_graph" not in out["properties"] and out["properties"]["metalness"] == 0.5
-    assert "node <noise3d> is not supported" in out["warnings"]
+    assert "node <worleynoise3d> is not supported" in out["warnings"]
     assert "node 'missing' not found" in out["warnings"]
 
 
@@ -452,3 +452,48 @@ def test_reference_prism_documents_load():
         loaded += 1
         compounds += "<adsk:" in text and "standard_surface" not in text
     assert loaded >= 50 and compounds >= 30, (loaded, compounds)
+
+
+def test_noise_nodes_compile_to_programs():
+    """noise2d, fractal3d and cellnoise3d compile to NOISE operations: the program gives the node
+    formulas (noise x amplitude + pivot; amplitude x the octave sum; the cell's hash in [0, 1])
+    over the numpy restatement of MaterialX's noise functions; the noise is 0 on the integer lattice
+    and cell noise is constant inside a cell."""
+    import mtlx_graphs as mg
+    from aurora_gb300 import _abi
+    out = props(mg.NOISE)
+    assert out["ok"] and out["warnings"] == "", out["warnings"]
+    ops, consts, _ = mg.decode(out["properties"]["materialx_graph"])
+    assert (ops["op"] == _abi.GOP_NOISE).sum() == 5
+    f = np.float32
+    rng = np.random.default_rng(8)
+    P = 4096
+    uv = rng.uniform(-2, 2, (P, 2)).astype(f)
+    pos = rng.uniform(-3, 3, (P, 3)).astype(f)
+    res = mg.evaluate(ops, consts, {_abi.GIN_TEXCOORD: uv, _abi.GIN_POSITION_OBJECT: pos})
+    grain = mg.perlin2(uv[:, 0] * f(8), uv[:, 1] * f(8)) * f(0.3) + f(0.45)
+    np.testing.assert_array_equal(res[_abi.GOUT_SPECULAR_ROUGHNESS][:, 0], grain)
+    p = pos * f(4)
+    total, amp = np.zeros(P, f), f(1)
+    for _ in range(3):
+        total = total + amp * mg.perlin3(p[:, 0], p[:, 1], p[:, 2])
+        amp = amp * f(0.45)
+        p = p * f(2.1)
+    t = (f(0.8) * total + f(0.5))[:, None]
+    fg, bg = f([0.9, 0.85, 0.8]), f([0.15, 0.2, 0.3])
+    np.testing.assert_array_equal(res[_abi.GOUT_BASE_COLOR], bg + t * (fg - bg))
+    cells = mg.cell3(*(pos * f(4)).T)
+    np.testing.assert_array_equal(res[_abi.GOUT_EMISSION_COLOR], f([0.6, 0.3, 0.1]) * cells[:, None])
+    # Properties of the functions themselves.
+    lattice = rng.integers(-50, 50, (512, 3)).astype(f)
+    assert np.all(mg.perlin3(*lattice.T) == 0) and np.all(mg.perlin2(*lattice[:, :2].T) == 0)
+    q = rng.uniform(-20, 20, (20000, 3)).astype(f)
+    n3, n2 = mg.perlin3(*q.T), mg.perlin2(*q[:, :2].T)
+    assert np.abs(n3).max() < 1.1 and np.abs(n2).max() < 1.1 and n3.std() > 0.1 and n2.std() > 0.1
+    c = mg.cell3(*q.T)
+    assert c.min() >= 0 and c.max() <= 1 and abs(c.mean() - 0.5) < 0.02
+    inner = np.floor(q) + rng.uniform(0.01, 0.99, q.shape).astype(f)
+    np.testing.assert_array_equal(mg.cell3(*inner.T), c)
+    # colour-valued noise is refused with a warning
+    bad = props(mg.NOISE.replace('<noise2d name="grain" type="float">', '<noise2d name="grain" type="color3">'))
+    assert "type color3 is not supported" in bad["warnings"]
