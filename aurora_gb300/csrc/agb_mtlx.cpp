@@ -665,6 +665,39 @@ private:
         return false;
     }
 
+    // The element holding the literal value an input takes in scope S, following interface
+    // bindings (a node graph's own interface input, a custom node's input or its nodedef's
+    // default); null when the input is fed by a node.
+    const XmlElement* literalInput(const XmlElement* in, const Scope* S) const
+    {
+        for (int hops = 0; in && !in->has("value") && hops < 64; hops++)
+        {
+            if (!in->has("interfacename") || !S)
+                return nullptr;
+            const std::string name = in->attr("interfacename");
+            if (S->call)
+            {
+                if (const XmlElement* ci = childInput(*S->call, name))
+                {
+                    in = ci;
+                    S  = S->parent;
+                }
+                else
+                {
+                    const XmlElement* def = nodedefFor(S->call->name);
+                    in                    = def ? childInput(*def, name) : nullptr;
+                    S                     = nullptr;
+                }
+            }
+            else
+            {
+                in = childInput(*S->graph, name);
+                S  = S->parent ? S->parent : S;
+            }
+        }
+        return in && in->has("value") ? in : nullptr;
+    }
+
     // The named input of a node, or `def` (of `type`) when it is absent.
     bool input(const XmlElement& node, const Scope& S, const char* name, const std::string& type, const char* def,
         Value& out, std::string& why)
@@ -1134,7 +1167,7 @@ private:
             if (cat == "fractal3d")
             {
                 const XmlElement* oc = childInput(node, "octaves");
-                if (oc && !oc->has("value"))
+                if (oc && !(oc = literalInput(oc, &S)))
                 {
                     why = "node <fractal3d> with a connected octaves input is not supported";
                     return false;

@@ -452,6 +452,15 @@ def test_reference_prism_documents_load():
         loaded += 1
         compounds += "<adsk:" in text and "standard_surface" not in text
     assert loaded >= 50 and compounds >= 30, (loaded, compounds)
+    # The marble graph (a fractal3d whose octaves come from the graph's interface) compiles whole.
+    import mtlx_graphs as mg
+    from aurora_gb300 import _abi
+    marble = os.path.join(root, "MarblegraphTest.mtlx")
+    if os.path.exists(marble):
+        out = run("mtlx", marble)
+        assert out["ok"] and out["warnings"] == "", out["warnings"]
+        ops, _, _ = mg.decode(out["properties"]["materialx_graph"])
+        assert (ops["op"] == _abi.GOP_NOISE).sum() == 3
 
 
 def test_noise_nodes_compile_to_programs():
