@@ -1128,6 +1128,21 @@ private:
             emit(AGB_GOP_MIX, out.reg, b.reg, a.reg, tc.reg, 0, 0);
             return true;
         }
+        if (cat == "plus" || cat == "minus" || cat == "difference")
+        {
+            // MaterialX's compositing nodes (stdlib genglsl): mix x op(fg, bg) + (1 - mix) x bg with
+            // op = bg + fg, bg - fg, |bg - fg|.
+            Value fg, bg, mx;
+            if (!in("fg", type, zero.c_str(), fg) || !in("bg", type, zero.c_str(), bg) || !in("mix", "float", "1", mx))
+                return false;
+            Value f = cat == "plus" ? op2(AGB_GOP_ADD, bg, fg) : op2(AGB_GOP_SUB, bg, fg);
+            if (cat == "difference")
+                f = op1(AGB_GOP_ABS, f);
+            Value one = valueOf("float", "1", why);
+            out       = op2(AGB_GOP_ADD, op2(AGB_GOP_MUL, mx, f), op2(AGB_GOP_MUL, op2(AGB_GOP_SUB, one, mx), bg));
+            out.n     = n;
+            return true;
+        }
         if (cat == "noise2d" || cat == "noise3d" || cat == "fractal3d" || cat == "cellnoise2d" || cat == "cellnoise3d")
         {
             // MaterialX's noise nodes (stdlib genglsl): noise = perlin(p) x amplitude + pivot;

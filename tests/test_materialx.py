@@ -506,3 +506,45 @@ def test_noise_nodes_compile_to_programs():
     # colour-valued noise is refused with a warning
     bad = props(mg.NOISE.replace('<noise2d name="grain" type="float">', '<noise2d name="grain" type="color3">'))
     assert "type color3 is not supported" in bad["warnings"]
+
+
+def test_compositing_nodes():
+    """plus, minus and difference: mix x op(fg, bg) + (1 - mix) x bg."""
+    import mtlx_graphs as mg
+    from aurora_gb300 import _abi
+    doc = """<materialx version="1.39">
+  <texcoord name="uv" type="vector2" />
+  <convert name="c" type="color3"><input name="in" type="vector2" nodename="uv" /></convert>
+  <difference name="d" type="color3">
+    <input name="fg" type="color3" nodename="c" />
+    <input name="bg" type="color3" value="0.5, 0.25, 0.75" />
+    <input name="mix" type="float" value="0.75" />
+  </difference>
+  <plus name="p" type="color3">
+    <input name="fg" type="color3" nodename="d" />
+    <input name="bg" type="color3" value="0.1, 0.2, 0.3" />
+  </plus>
+  <extract name="u" type="float"><input name="in" type="vector2" nodename="uv" /><input name="index" type="integer" value="0" /></extract>
+  <minus name="m" type="float">
+    <input name="fg" type="float" nodename="u" />
+    <input name="bg" type="float" value="0.9" />
+    <input name="mix" type="float" value="0.5" />
+  </minus>
+  <standard_surface name="S" type="surfaceshader">
+    <input name="base_color" type="color3" nodename="p" />
+    <input name="specular_roughness" type="float" nodename="m" />
+  </standard_surface>
+</materialx>"""
+    out = props(doc)
+    assert out["ok"] and out["warnings"] == "", out["warnings"]
+    ops, consts, _ = mg.decode(out["properties"]["materialx_graph"])
+    f = np.float32
+    uv = np.random.default_rng(2).uniform(0, 1, (256, 2)).astype(f)
+    res = mg.evaluate(ops, consts, {_abi.GIN_TEXCOORD: uv})
+    c = np.concatenate([uv, np.zeros((256, 1), f)], 1)
+    bg = f([0.5, 0.25, 0.75])
+    d = f(0.75) * np.abs(bg - c) + (f(1) - f(0.75)) * bg
+    p = f(1) * (f([0.1, 0.2, 0.3]) + d) + (f(1) - f(1)) * f([0.1, 0.2, 0.3])
+    np.testing.assert_allclose(res[_abi.GOUT_BASE_COLOR], p, rtol=1e-6)
+    m = f(0.5) * (f(0.9) - uv[:, 0]) + (f(1) - f(0.5)) * f(0.9)
+    np.testing.assert_allclose(res[_abi.GOUT_SPECULAR_ROUGHNESS][:, 0], m, rtol=1e-6)
