@@ -32,6 +32,9 @@ inline unsigned gridFor(long n, int block = 256)
     return unsigned(std::min<long>(std::max<long>(g, 1), 1L << 20));
 }
 
+#ifndef AGB_PREACT_BLOCKS_PER_SM
+#define AGB_PREACT_BLOCKS_PER_SM 4
+#endif
 // The gradient of one layer's pre-activation and of its bias, from the gradient of its output:
 //   dPre[p][c] = bf16((g[p][c] + 0.25 * gp[p / 2x2][c]) * (y[p][c] > 0)),  db[c] += sum_p dPre[p][c]
 // gp (the gradient of the 2x2 average pool of y, H/2 x W/2) and y (ReLU) are optional; the bias
@@ -540,7 +543,8 @@ cudaError_t UnetDenoiser::backward(const float* target)
         // resolution, beside the gradient from the skip connection.
         const bool pooled = i == 1 || i == 3 || i == 5;
         const long n8     = Pl * cout / 8;
-        k_preact_grad<<<unsigned(std::min<long>((n8 + 255) / 256, 8L * smCount_)), 256, 0, stream_>>>(
+        k_preact_grad<<<unsigned(std::min<long>((n8 + 255) / 256, long(AGB_PREACT_BLOCKS_PER_SM) * smCount_)), 256, 0,
+            stream_>>>(
             reinterpret_cast<const float4*>(gy), pooled ? reinterpret_cast<const float4*>(grad_[L.out + 1]) : nullptr,
             L.relu ? reinterpret_cast<const uint4*>(act_[L.out]) : nullptr, reinterpret_cast<uint4*>(dpre_),
             grads_ + bOff_[i], B_, H_ >> L.level, W_ >> L.level, cout);
