@@ -1504,6 +1504,7 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
             for (int b = 0; b < depth; b++)
             {
                 r.closest_rays += c[counterWords * w + kCounterStride * b + CNT_RAYS];
+                r.shading_points += c[counterWords * w + kCounterStride * b + CNT_SCATTER];
                 r.shadow_rays += c[counterWords * w + kCounterStride * b + CNT_SHADOW];
                 r.shadow_rays += c[counterWords * w + kCounterStride * b + CNT_GROUND_SHADOW];
             }

@@ -86,6 +86,18 @@ def closest_dram_bytes_per_ray():
     return None
 
 
+def path_model(counted, value, peak):
+    paths = max(1, counted["paths"])
+    nodes_tris = (counted["node_visits"] + counted["shadow_node_visits"]) * 64 + \
+        (counted["tri_tests"] + counted["shadow_tri_tests"]) * 48
+    per_sample = (nodes_tris + counted.get("shading_points", 0) * 108) / paths + 64
+    achieved = per_sample * value / 1e9
+    return {"bytes_per_path_sample": per_sample, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "shading_points_per_path": counted.get("shading_points", 0) / paths,
+            "model": "sum over rays of node visits x 64 B + triangle tests x 48 B, + shaded hits x 108 B, "
+                     "+ 32 B running mean + 32 B Kahan per sample"}
+
+
 def simt_threads_per_instruction():
     """Active threads per executed instruction of k_trace_closest from the committed ncu summary
     (out of 32), or None."""
@@ -794,6 +806,11 @@ def main():
                       if dram_per_ray is not None else None),
         "dram_frac_note": "DRAM bytes of the committed capture per closest-hit ray x this step's rays / "
                           "the kernel's time / the measured copy bandwidth",
+        # The whole path's bytes per path sample: node and triangle records of every closest-hit
+        # and shadow ray, a 108-byte shading fetch per shaded hit (counted as the points the
+        # surface kernel hands on: a lower bound of the hits) and 32 + 32 bytes of FP32 + Kahan
+        # accumulation per sample, times path-samples/s, against the copy bandwidth.
+        "path_model": path_model(counted, value / world, peak),
         "simt_threads_per_instruction": simt_threads_per_instruction(),
         "dominant_family_by_time": dominant,
         "kernel_ms_per_step": {k: v / steps for k, v in kernel_ms.items()},

@@ -317,6 +317,7 @@ typedef struct agb_render_stats
      * shading, shadow traversal, resolve, finalize. */
     double kernel_ms[6];
     uint64_t kernel_count[6];     /* launches per kernel family */
+    uint64_t shading_points;      /* hits shaded through the BSDF (the surface kernel's points) */
 } agb_render_stats;
 
 /* ------------------------------------------------------------------------------------------ */
