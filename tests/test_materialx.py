@@ -437,7 +437,7 @@ def test_reference_prism_documents_load():
     these are its files, not copies)."""
     import glob
     import pytest
-    root = "/root/reference/Tests/Assets/Materials"
+    root = os.path.join(os.environ.get("AURORA_REFERENCE_ROOT", "/root/reference"), "Tests", "Assets", "Materials")
     files = sorted(glob.glob(os.path.join(root, "**", "*.mtlx"), recursive=True))
     if not files:
         pytest.skip("reference test assets not present")
