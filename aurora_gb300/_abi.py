@@ -156,7 +156,8 @@ class RenderStats(ctypes.Structure):
                 ("tri_tests", ctypes.c_uint64), ("shadow_node_visits", ctypes.c_uint64),
                 ("shadow_tri_tests", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
                 ("gpu_ms", ctypes.c_double), ("kernel_ms", ctypes.c_double * 6),
-                ("kernel_count", ctypes.c_uint64 * 6), ("shading_points", ctypes.c_uint64)]
+                ("kernel_count", ctypes.c_uint64 * 6), ("shading_points", ctypes.c_uint64),
+                ("closest_rays_per_bounce", ctypes.c_uint64 * 16), ("shadow_rays_per_bounce", ctypes.c_uint64 * 16)]
 
 KERNEL_FAMILIES = ("camera", "trace_closest", "shade", "trace_shadow", "resolve", "finalize")
 

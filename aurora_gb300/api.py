@@ -130,6 +130,8 @@ class Renderer:
             out = {f: getattr(st, f) for f, _ in _abi.RenderStats._fields_}
             out["kernel_ms"] = dict(zip(_abi.KERNEL_FAMILIES, list(st.kernel_ms)))
             out["kernel_count"] = dict(zip(_abi.KERNEL_FAMILIES, list(st.kernel_count)))
+            out["closest_rays_per_bounce"] = list(st.closest_rays_per_bounce)
+            out["shadow_rays_per_bounce"] = list(st.shadow_rays_per_bounce)
             return out
         return None
 
@@ -295,6 +297,9 @@ class Batch:
         if stats:
             out = {f: getattr(st, f) for f, _ in _abi.RenderStats._fields_}
             out["kernel_ms"] = dict(zip(_abi.KERNEL_FAMILIES, list(st.kernel_ms)))
+            out["kernel_count"] = dict(zip(_abi.KERNEL_FAMILIES, list(st.kernel_count)))
+            out["closest_rays_per_bounce"] = list(st.closest_rays_per_bounce)
+            out["shadow_rays_per_bounce"] = list(st.shadow_rays_per_bounce)
             return out
         return None
 

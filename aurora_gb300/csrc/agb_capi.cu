@@ -1503,10 +1503,17 @@ AGB_API agb_status agb_render(agb_context* ctx, const agb_render_options* opt,
         {
             for (int b = 0; b < depth; b++)
             {
-                r.closest_rays += c[counterWords * w + kCounterStride * b + CNT_RAYS];
+                const uint64_t cr = c[counterWords * w + kCounterStride * b + CNT_RAYS];
+                const uint64_t sr = uint64_t(c[counterWords * w + kCounterStride * b + CNT_SHADOW]) +
+                    c[counterWords * w + kCounterStride * b + CNT_GROUND_SHADOW];
+                r.closest_rays += cr;
                 r.shading_points += c[counterWords * w + kCounterStride * b + CNT_SCATTER];
-                r.shadow_rays += c[counterWords * w + kCounterStride * b + CNT_SHADOW];
-                r.shadow_rays += c[counterWords * w + kCounterStride * b + CNT_GROUND_SHADOW];
+                r.shadow_rays += sr;
+                if (b < 16)
+                {
+                    r.closest_rays_per_bounce[b] += cr;
+                    r.shadow_rays_per_bounce[b] += sr;
+                }
             }
         }
         r.node_visits        = s[2];

@@ -860,7 +860,9 @@ def main():
                 "d2h_bytes_per_step": int(s.width * s.height * 16),
                 "ms_per_step": 1000.0 * e2e_time / args.steps},
         "gpu_launches": int(launches),
-        "rays_per_step": {"closest": counted["closest_rays"], "shadow": counted["shadow_rays"]},
+        "rays_per_step": {"closest": counted["closest_rays"], "shadow": counted["shadow_rays"],
+                          "closest_per_bounce": [int(v) for v in counted["closest_rays_per_bounce"]],
+                          "shadow_per_bounce": [int(v) for v in counted["shadow_rays_per_bounce"]]},
         "per_ray": {
             "closest_node_visits": counted["node_visits"] / max(1, counted["closest_rays"]),
             "closest_tri_tests": counted["tri_tests"] / max(1, counted["closest_rays"]),

@@ -318,6 +318,8 @@ typedef struct agb_render_stats
     double kernel_ms[6];
     uint64_t kernel_count[6];     /* launches per kernel family */
     uint64_t shading_points;      /* hits shaded through the BSDF (the surface kernel's points) */
+    uint64_t closest_rays_per_bounce[16]; /* closest-hit rays of bounces 0-15 (summed over waves) */
+    uint64_t shadow_rays_per_bounce[16];  /* shadow rays of bounces 0-15 */
 } agb_render_stats;
 
 /* ------------------------------------------------------------------------------------------ */
