@@ -192,6 +192,30 @@ ORC_API void orc_random_stream(uint32_t sampleIndex, uint32_t screenWidth, uint3
     }
 }
 
+// MaterialX's noise functions (the graph interpreter's NOISE operation): kind 0 Perlin 2D of
+// (x, y), 1 Perlin 3D, 2 cell 2D, 3 cell 3D; xyz: 3 floats per point; out: n values.
+ORC_API void orc_mx_noise(int precision, int kind, const float* xyz, int64_t n, double* out)
+{
+    for (int64_t i = 0; i < n; i++)
+    {
+        const float* p = xyz + 3 * i;
+        if (precision == 64)
+        {
+            using N = MxNoise<double>;
+            out[i] = kind == 0 ? N::perlin2(p[0], p[1]) : kind == 1 ? N::perlin3(p[0], p[1], p[2])
+                : kind == 2    ? N::cell2(p[0], p[1])
+                               : N::cell3(p[0], p[1], p[2]);
+        }
+        else
+        {
+            using N = MxNoise<float>;
+            out[i] = kind == 0 ? N::perlin2(p[0], p[1]) : kind == 1 ? N::perlin3(p[0], p[1], p[2])
+                : kind == 2    ? N::cell2(p[0], p[1])
+                               : N::cell3(p[0], p[1], p[2]);
+        }
+    }
+}
+
 // op: 0 evaluateMaterial, 1 sampleMaterial, 2 evaluateMaterialAndPDF.  frames: 12 floats each.
 ORC_API void orc_bsdf_batch(int op, int precision, const MaterialBlock* mats,
     const int32_t* matIndex, const float* frames, const float* V, const float* L, const float* rnd,

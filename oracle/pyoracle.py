@@ -20,6 +20,15 @@ import build_oracle  # noqa: E402
 _lib = None
 
 
+def mx_noise(kind, xyz, precision=32):
+    """The oracle's MaterialX noise (kind 0 Perlin 2D, 1 Perlin 3D, 2 cell 2D, 3 cell 3D) at (n, 3)
+    float32 points; float64 results (FP32 values exactly when precision is 32)."""
+    xyz = np.ascontiguousarray(xyz, np.float32)
+    out = np.zeros(len(xyz), np.float64)
+    lib().orc_mx_noise(precision, kind, xyz.ctypes.data, len(xyz), out.ctypes.data)
+    return out
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -29,6 +38,7 @@ def lib():
         L.orc_layout.restype = ctypes.c_int
         L.orc_layout.argtypes = [ctypes.c_int]
         L.orc_random_stream.argtypes = [ctypes.c_uint32] * 4 + [ctypes.c_int, P]
+        L.orc_mx_noise.argtypes = [ctypes.c_int, ctypes.c_int, P, ctypes.c_int64, P]
         L.orc_bsdf_batch.argtypes = [ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, ctypes.c_int64,
                                      P, P, P, P]
         L.orc_alias_build.argtypes = [ctypes.c_int, P, ctypes.c_uint32, ctypes.c_uint32, P,

@@ -548,3 +548,24 @@ def test_compositing_nodes():
     np.testing.assert_allclose(res[_abi.GOUT_BASE_COLOR], p, rtol=1e-6)
     m = f(0.5) * (f(0.9) - uv[:, 0]) + (f(1) - f(0.5)) * f(0.9)
     np.testing.assert_allclose(res[_abi.GOUT_SPECULAR_ROUGHNESS][:, 0], m, rtol=1e-6)
+
+
+def test_oracle_noise_matches_numpy_restatement():
+    """The oracle's MaterialX noise (C++, FP32) equals the numpy restatement bit for bit; its FP64
+    form stays within 1e-5 of it: two independent writings of the same published functions (the
+    device matches the FP32 oracle in the GPU render tests)."""
+    import sys
+    import mtlx_graphs as mg
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+    import pyoracle
+    f = np.float32
+    rng = np.random.default_rng(12)
+    q = np.concatenate([rng.uniform(-40, 40, (20000, 3)), rng.integers(-9, 9, (500, 3)) + 0.5,
+                        rng.integers(-9, 9, (500, 3))]).astype(f)
+    want = [mg.perlin2(q[:, 0], q[:, 1]), mg.perlin3(q[:, 0], q[:, 1], q[:, 2]),
+            mg.cell2(q[:, 0], q[:, 1]), mg.cell3(q[:, 0], q[:, 1], q[:, 2])]
+    for kind in range(4):
+        got = pyoracle.mx_noise(kind, q, precision=32).astype(f)
+        np.testing.assert_array_equal(got, want[kind], err_msg=f"kind {kind}")
+        got64 = pyoracle.mx_noise(kind, q, precision=64)
+        assert np.abs(got64 - want[kind]).max() < 1e-5, kind
