@@ -1128,6 +1128,47 @@ private:
             emit(AGB_GOP_MIX, out.reg, b.reg, a.reg, tc.reg, 0, 0);
             return true;
         }
+        if (cat == "smoothstep")
+        {
+            // t = clamp((in - low) / (high - low), 0, 1); t^2 (3 - 2t), component-wise.
+            Value lo, hi;
+            if (!in("in", type, zero.c_str(), a) || !in("low", type, zero.c_str(), lo) ||
+                !in("high", type, one.c_str(), hi))
+                return false;
+            Value t = op2(AGB_GOP_DIV, op2(AGB_GOP_SUB, a, lo), op2(AGB_GOP_SUB, hi, lo));
+            Value z = valueOf("float", "0", why), u = valueOf("float", "1", why);
+            Value c{ reg(), t.n };
+            emit(AGB_GOP_CLAMP, c.reg, t.reg, z.reg, u.reg, 0, 0);
+            Value three = valueOf("float", "3", why), two = valueOf("float", "2", why);
+            out   = op2(AGB_GOP_MUL, op2(AGB_GOP_MUL, c, c), op2(AGB_GOP_SUB, three, op2(AGB_GOP_MUL, two, c)));
+            out.n = n;
+            return true;
+        }
+        if (cat == "crossproduct")
+        {
+            // in1.yzx in2.zxy - in1.zxy in2.yzx
+            if (!in("in1", "vector3", "0, 0, 0", a) || !in("in2", "vector3", "0, 0, 0", b))
+                return false;
+            const uint16_t yzx = 1 | (2 << 2), zxy = 2 | (1 << 4);
+            out   = op2(AGB_GOP_SUB, op2(AGB_GOP_MUL, op1(AGB_GOP_SWIZZLE, a, 3, yzx), op1(AGB_GOP_SWIZZLE, b, 3, zxy)),
+                  op2(AGB_GOP_MUL, op1(AGB_GOP_SWIZZLE, a, 3, zxy), op1(AGB_GOP_SWIZZLE, b, 3, yzx)));
+            out.n = 3;
+            return true;
+        }
+        if (cat == "rotate2d")
+        {
+            // MaterialX's rotate2d: (c x + s y, -s x + c y), angle `amount` in degrees.
+            if (!in("in", "vector2", "0, 0", a) || !in("amount", "float", "0", b))
+                return false;
+            Value r  = op2(AGB_GOP_MUL, b, constant({ float(3.14159265358979323846 / 180.0) }, 1));
+            Value sn = op1(AGB_GOP_SIN, r), cs = op1(AGB_GOP_COS, r);
+            Value x = op1(AGB_GOP_SWIZZLE, a, 1, 0x00), y = op1(AGB_GOP_SWIZZLE, a, 1, 0x55);
+            Value rx = op2(AGB_GOP_ADD, op2(AGB_GOP_MUL, cs, x), op2(AGB_GOP_MUL, sn, y));
+            Value ry = op2(AGB_GOP_SUB, op2(AGB_GOP_MUL, cs, y), op2(AGB_GOP_MUL, sn, x));
+            out = Value{ reg(), 2 };
+            emit(AGB_GOP_COMBINE, out.reg, rx.reg, ry.reg, rx.reg, rx.reg, 0);
+            return true;
+        }
         if (cat == "plus" || cat == "minus" || cat == "difference")
         {
             // MaterialX's compositing nodes (stdlib genglsl): mix x op(fg, bg) + (1 - mix) x bg with

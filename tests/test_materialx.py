@@ -569,3 +569,45 @@ def test_oracle_noise_matches_numpy_restatement():
         np.testing.assert_array_equal(got, want[kind], err_msg=f"kind {kind}")
         got64 = pyoracle.mx_noise(kind, q, precision=64)
         assert np.abs(got64 - want[kind]).max() < 1e-5, kind
+
+
+def test_smoothstep_crossproduct_rotate2d():
+    """smoothstep (t^2 (3 - 2t) of the clamped ramp), crossproduct and rotate2d (degrees) compile
+    to the operations that give MaterialX's formulas."""
+    import mtlx_graphs as mg
+    from aurora_gb300 import _abi
+    doc = """<materialx version="1.39">
+  <texcoord name="uv" type="vector2" />
+  <rotate2d name="r" type="vector2">
+    <input name="in" type="vector2" nodename="uv" />
+    <input name="amount" type="float" value="30" />
+  </rotate2d>
+  <extract name="u" type="float"><input name="in" type="vector2" nodename="r" /><input name="index" type="integer" value="0" /></extract>
+  <smoothstep name="s" type="float">
+    <input name="in" type="float" nodename="u" />
+    <input name="low" type="float" value="0.2" />
+    <input name="high" type="float" value="0.7" />
+  </smoothstep>
+  <position name="p" type="vector3" />
+  <crossproduct name="c" type="vector3">
+    <input name="in1" type="vector3" nodename="p" />
+    <input name="in2" type="vector3" value="0.3, -0.5, 0.8" />
+  </crossproduct>
+  <standard_surface name="S" type="surfaceshader">
+    <input name="specular_roughness" type="float" nodename="s" />
+    <input name="base_color" type="color3" nodename="c" />
+  </standard_surface>
+</materialx>"""
+    out = props(doc)
+    assert out["ok"] and out["warnings"] == "", out["warnings"]
+    ops, consts, _ = mg.decode(out["properties"]["materialx_graph"])
+    f = np.float32
+    rng = np.random.default_rng(5)
+    uv = rng.uniform(-1, 1, (512, 2)).astype(f)
+    pos = rng.uniform(-2, 2, (512, 3)).astype(f)
+    res = mg.evaluate(ops, consts, {_abi.GIN_TEXCOORD: uv, _abi.GIN_POSITION_OBJECT: pos})
+    a = np.radians(30.0)
+    u = np.cos(a) * uv[:, 0] + np.sin(a) * uv[:, 1]
+    t = np.clip((u - 0.2) / 0.5, 0, 1)
+    np.testing.assert_allclose(res[_abi.GOUT_SPECULAR_ROUGHNESS][:, 0], t * t * (3 - 2 * t), atol=2e-6)
+    np.testing.assert_allclose(res[_abi.GOUT_BASE_COLOR], np.cross(pos, f([0.3, -0.5, 0.8])), atol=1e-6)
