@@ -242,3 +242,28 @@ def test_conv_entry_points_reject_bad_shapes_before_touching_the_gpu():
     for fn, args, why in cases:
         assert fn(*args) == _abi.ERR_INVALID_ARG, why
         assert why in lib.agb_last_error(), (why, lib.agb_last_error())
+
+
+def test_render_stats_layout_matches_ctypes(tmp_path):
+    """agb_render_stats as the C compiler lays it out (include/agb.h) equals the ctypes mirror the
+    Python host reads it through: size and the offsets of the fields appended last."""
+    import shutil
+    import subprocess
+    from aurora_gb300 import _abi
+    gcc = shutil.which("gcc")
+    if not gcc:
+        pytest.skip("no C compiler")
+    include = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    src = tmp_path / "stats.c"
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "agb.h"\n'
+                   'int main(void) { printf("%zu %zu %zu %zu\\n", sizeof(agb_render_stats), '
+                   'offsetof(agb_render_stats, shading_points), '
+                   'offsetof(agb_render_stats, closest_rays_per_bounce), '
+                   'offsetof(agb_render_stats, shadow_rays_per_bounce)); return 0; }\n')
+    exe = tmp_path / "stats"
+    subprocess.check_call([gcc, "-I" + include, str(src), "-o", str(exe)])
+    size, sp, cb, sb = map(int, subprocess.check_output([str(exe)]).split())
+    S = _abi.RenderStats
+    assert size == ctypes.sizeof(S)
+    assert (sp, cb, sb) == (S.shading_points.offset, S.closest_rays_per_bounce.offset,
+                            S.shadow_rays_per_bounce.offset)
